@@ -1,0 +1,971 @@
+// axg_api.cu -- the C-ABI of include/axisem_gb300.h.
+//
+// axg_create validates the descriptor, plans the patch colouring of the
+// solid and fluid domains (axg_plan.cpp), packs the per-element data in
+// launch order (one contiguous block of metric terms per element), builds the
+// solid-fluid coupling tables and copies everything to HBM.  axg_run advances
+// the Newmark loop of SOLVER/time_evol_wave.F90:353-500 with the kernels of
+// axg_kernels.cuh, captured in CUDA graphs of `steps_per_graph` steps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "axg_kernels.cuh"
+#include "axg_plan.h"
+#include "axisem_gb300.h"
+
+using namespace axg;
+
+namespace {
+
+std::string g_create_error = "no error";
+
+std::string fmt(const char *f, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, f);
+  vsnprintf(buf, sizeof buf, f, ap);
+  va_end(ap);
+  return buf;
+}
+
+// metric array order of an element block (SOLID_TERMS_USED)
+std::vector<int> solid_slots(int pole) {
+  std::vector<int> s = {AXG_M_1,  AXG_M_2,  AXG_M_3,  AXG_M_4,  AXG_M_W1, AXG_M11S, AXG_M21S, AXG_M41S,
+                        AXG_M12S, AXG_M22S, AXG_M32S, AXG_M42S, AXG_M11Z, AXG_M21Z, AXG_M41Z};
+  if (pole == AXG_DIPOLE)
+    s.insert(s.end(), {AXG_M_5, AXG_M_6, AXG_M_7, AXG_M_8, AXG_M_W2, AXG_M_W3, AXG_M13S, AXG_M33S, AXG_M43S});
+  if (pole == AXG_QUADPOLE)
+    s.insert(s.end(), {AXG_M_5, AXG_M_6, AXG_M_7, AXG_M_8, AXG_M_W2, AXG_M_W3, AXG_M_W4, AXG_M_W5,
+                       AXG_M1PHI, AXG_M2PHI, AXG_M4PHI});
+  return s;
+}
+std::vector<int> axial_slots(int pole) {
+  if (pole == AXG_MONOPOLE) return {AXG_M0_W1, AXG_M0_W2, AXG_M0_W3};
+  if (pole == AXG_DIPOLE)
+    return {AXG_M0_W1, AXG_M0_W2, AXG_M0_W3, AXG_M0_W4, AXG_M0_W6, AXG_M0_W7, AXG_M0_W8, AXG_M0_W9, AXG_M0_W10};
+  return {AXG_M0_W1, AXG_M0_W2, AXG_M0_W3, AXG_M0_W4, AXG_M0_W5, AXG_M0_W6};
+}
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t n = 0;
+};
+
+struct DomainDev {
+  PatchMeta *meta = nullptr;
+  uint32_t *pts = nullptr;
+  uint16_t *elpts = nullptr;
+  int32_t *elinfo = nullptr;
+  float *metric = nullptr;
+  float *m0 = nullptr;
+  float *fsmask = nullptr;
+  float *srcfl = nullptr;
+};
+
+struct CouplingHost {
+  std::vector<int32_t> pt_gidx, start, src_gidx;
+  std::vector<float> b1, b2, mask;
+};
+
+}  // namespace
+
+struct axg_handle {
+  // descriptor scalars
+  int pole = 0, fluid_src = 0;
+  int64_t nel_s = 0, nel_f = 0, nglob_s = 0, nglob_f = 0;
+  int32_t niter = 0, seis_it = 1, num_rec = 0, nseismo = 0;
+  bool absorbing = false;
+  double dt = 0, magnitude = 0;
+  std::vector<int32_t> igloc_s, igloc_f, rec_gidx;
+  std::vector<uint8_t> pre_s, pre_f;
+  DomainPlan ps, pf;
+  int patch_elems = 64, steps_per_graph = 16;
+  // device
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  SpecDev spec{};
+  std::vector<void *> allocs;
+  int64_t dev_bytes = 0;
+  DomainDev ds, df;
+  float *su[3] = {}, *sv[3] = {}, *sa[3] = {}, *sf[3] = {};
+  float *fu = nullptr, *fv = nullptr, *fa = nullptr, *ff = nullptr;
+  float *inv_mass_s = nullptr, *inv_mass_f = nullptr, *gamma_s = nullptr, *gamma_f = nullptr;
+  float *stf = nullptr, *rec = nullptr;
+  int32_t *iter = nullptr, *blowup = nullptr, *rec_gidx_d = nullptr;
+  int32_t *src_gidx_d = nullptr;
+  float *src_val_d = nullptr;
+  int32_t n_src = 0;
+  Coupling to_fluid{}, to_solid{};
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err = "no error";
+  int64_t kernels_per_step = 0, kernels_per_force = 0;
+};
+
+namespace {
+
+int fail(axg_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(axg_handle *h, cudaError_t e, const char *what) {
+  const int code = (e == cudaErrorMemoryAllocation) ? AXG_ERR_OOM : AXG_ERR_CUDA;
+  return fail(h, code, fmt("%s: %s", what, cudaGetErrorString(e)));
+}
+
+#define CK(call)                                                   \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call);         \
+  } while (0)
+
+template <typename T>
+int dalloc(axg_handle *h, T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return AXG_OK;
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
+  h->allocs.push_back(q);
+  h->dev_bytes += (int64_t)(count * sizeof(T));
+  *p = (T *)q;
+  return AXG_OK;
+}
+
+template <typename T>
+int upload(axg_handle *h, T **p, const std::vector<T> &v) {
+  int rc = dalloc(h, p, v.size());
+  if (rc) return rc;
+  if (!v.empty()) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return AXG_OK;
+}
+
+// ---------------------------------------------------------------- validation
+
+int validate(const axg_mesh_desc *d) {
+  auto bad = [](const std::string &m) { return fail(nullptr, AXG_ERR_BAD_DESC, m); };
+  if (!d) return bad("descriptor is NULL");
+  if (d->abi_version != AXG_ABI_VERSION) return bad(fmt("abi_version %d, expected %d", d->abi_version, AXG_ABI_VERSION));
+  if (d->npol != AXG_NPOL) return bad(fmt("npol = %d; only npol = 4 is supported", d->npol));
+  if (d->src_type < 0 || d->src_type > 2) return bad("src_type must be monopole/dipole/quadpole (0..2)");
+  if (d->nel_solid <= 0 || d->nglob_solid <= 0) return bad("nel_solid and nglob_solid must be positive");
+  if (d->nel_fluid < 0 || d->nglob_fluid < 0) return bad("negative fluid sizes");
+  if (d->nel_fluid > 0 && d->nglob_fluid <= 0) return bad("nglob_fluid must be positive with fluid elements");
+  if (!d->igloc_solid) return bad("igloc_solid is NULL");
+  if (d->nel_fluid > 0 && !d->igloc_fluid) return bad("igloc_fluid is NULL");
+  if (!d->G0 || !d->G1 || !d->G1T || !d->G2 || !d->G2T) return bad("spectral matrices G0..G2T are required");
+  for (int s : solid_slots(d->src_type))
+    if (!d->m_solid[s]) return bad(fmt("solid metric array %d required by this pole type is NULL", s));
+  if (d->naxel_solid < 0 || d->naxel_solid > d->nel_solid) return bad("naxel_solid out of range");
+  if (d->naxel_solid > 0) {
+    if (!d->ax_el_solid) return bad("ax_el_solid is NULL");
+    for (int s : axial_slots(d->src_type))
+      if (!d->m0_solid[s]) return bad(fmt("axial vector M0_w%d is NULL", s + 1));
+    for (int k = 0; k < d->naxel_solid; ++k)
+      if (d->ax_el_solid[k] < 1 || d->ax_el_solid[k] > d->nel_solid) return bad("ax_el_solid entry out of range");
+  }
+  if (!d->inv_mass_rho) return bad("inv_mass_rho is NULL");
+  if (d->nel_fluid > 0) {
+    for (int t = 0; t < (d->src_type == AXG_MONOPOLE ? 3 : 4); ++t)
+      if (!d->m_fluid[t]) return bad(fmt("fluid metric array %d is NULL", t));
+    if (!d->inv_mass_fluid) return bad("inv_mass_fluid is NULL");
+    if (d->naxel_fluid < 0 || d->naxel_fluid > d->nel_fluid) return bad("naxel_fluid out of range");
+    if (d->naxel_fluid > 0) {
+      if (!d->ax_el_fluid) return bad("ax_el_fluid is NULL");
+      for (int k = 0; k < d->naxel_fluid; ++k)
+        if (d->ax_el_fluid[k] < 1 || d->ax_el_fluid[k] > d->nel_fluid) return bad("ax_el_fluid entry out of range");
+      if (d->src_type != AXG_MONOPOLE && !d->m0_w_fl) return bad("M0_w_fl is NULL");
+    }
+  }
+  if (d->nel_bdry < 0) return bad("nel_bdry < 0");
+  if (d->nel_bdry > 0) {
+    if (d->nel_fluid <= 0) return bad("solid-fluid boundary without fluid elements");
+    if (!d->bdry_matr || !d->bdry_solid_el || !d->bdry_fluid_el || !d->bdry_jpol_solid || !d->bdry_jpol_fluid)
+      return bad("boundary arrays are NULL");
+    for (int b = 0; b < d->nel_bdry; ++b) {
+      if (d->bdry_solid_el[b] < 1 || d->bdry_solid_el[b] > d->nel_solid) return bad("bdry_solid_el out of range");
+      if (d->bdry_fluid_el[b] < 1 || d->bdry_fluid_el[b] > d->nel_fluid) return bad("bdry_fluid_el out of range");
+      if (d->bdry_jpol_solid[b] < 0 || d->bdry_jpol_solid[b] > 4) return bad("bdry_jpol_solid out of range");
+      if (d->bdry_jpol_fluid[b] < 0 || d->bdry_jpol_fluid[b] > 4) return bad("bdry_jpol_fluid out of range");
+    }
+  }
+  if (d->nelsrc < 0 || d->nelsrc > 8) return bad("nelsrc must be within 0..8");
+  if (d->nelsrc > 0) {
+    if (!d->ielsrc) return bad("ielsrc is NULL");
+    const int nmax = d->fluid_src ? d->nel_fluid : d->nel_solid;
+    for (int k = 0; k < d->nelsrc; ++k)
+      if (d->ielsrc[k] < 1 || d->ielsrc[k] > nmax) return bad("ielsrc entry out of range");
+    if (d->fluid_src ? !d->source_term_fl : !d->source_term_el) return bad("source term array is NULL");
+  }
+  if (d->niter < 0) return bad("niter < 0");
+  if (d->niter > 0 && !d->stf) return bad("stf is NULL");
+  if (d->num_rec < 0) return bad("num_rec < 0");
+  if (d->num_rec > 0) {
+    if (!d->recfile_el) return bad("recfile_el is NULL");
+    if (d->seis_it < 1) return bad("seis_it must be >= 1");
+    for (int r = 0; r < d->num_rec; ++r) {
+      const int e = d->recfile_el[r], ip = d->recfile_el[r + d->num_rec], jp = d->recfile_el[r + 2 * d->num_rec];
+      if (e < 1 || e > d->nel_solid || ip < 0 || ip > 4 || jp < 0 || jp > 4) return bad("recfile_el entry out of range");
+    }
+  }
+  if (d->have_absorbing_bc && (!d->solid_absorbing_gamma || (d->nel_fluid > 0 && !d->fluid_absorbing_gamma)))
+    return bad("absorbing gamma arrays are NULL");
+  if (!(d->deltat > 0) && d->niter > 0) return bad("deltat must be positive");
+  if (d->anel_true) return fail(nullptr, AXG_ERR_UNSUPPORTED, "attenuation (anel_true) is not implemented in this build");
+  return AXG_OK;
+}
+
+// per global point value of an element-local array (first copy wins)
+std::vector<float> per_point(const float *elem, const std::vector<int32_t> &igloc, int64_t nglob) {
+  std::vector<float> out(nglob, 0.f);
+  std::vector<uint8_t> set(nglob, 0);
+  for (size_t p = 0; p < igloc.size(); ++p) {
+    const int64_t g = igloc[p] - 1;
+    if (!set[g]) {
+      out[g] = elem[p];
+      set[g] = 1;
+    }
+  }
+  return out;
+}
+
+int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid) {
+  const DomainPlan &pl = fluid ? h->pf : h->ps;
+  DomainDev &dd = fluid ? h->df : h->ds;
+  const int64_t nel = pl.nel;
+  if (nel == 0) return AXG_OK;
+  const int pole = d->src_type;
+  const int nonmono = pole != AXG_MONOPOLE;
+  // axial flags and slots
+  std::vector<uint8_t> axial(nel, 0);
+  const int nax = fluid ? d->naxel_fluid : d->naxel_solid;
+  const int32_t *axl = fluid ? d->ax_el_fluid : d->ax_el_solid;
+  for (int k = 0; k < nax; ++k) axial[axl[k] - 1] = 1;
+  std::vector<int> slots;
+  int nt;
+  if (fluid) {
+    nt = nonmono ? 4 : 3;
+  } else {
+    slots = solid_slots(pole);
+    nt = (int)slots.size();
+  }
+  const int bs = block_stride(nt);
+  std::vector<float> metric((size_t)nel * bs, 0.f);
+  std::vector<int32_t> elinfo(nel, 0);
+  const std::vector<int> aslots = fluid ? std::vector<int>{0} : axial_slots(pole);
+  const int na = (int)aslots.size();
+  std::vector<float> m0;
+  std::vector<float> fsmask;
+  const bool use_fs = fluid && d->fluid_free_surface_mask != nullptr;
+  if (use_fs) fsmask.resize((size_t)nel * 25);
+  // source slot of each element
+  std::vector<int8_t> srcslot(nel, -1);
+  if (d->nelsrc > 0 && (bool)d->fluid_src == fluid)
+    for (int k = 0; k < d->nelsrc; ++k) srcslot[d->ielsrc[k] - 1] = (int8_t)k;
+  int32_t axcount = 0;
+  for (int64_t s = 0; s < nel; ++s) {
+    const int64_t e = pl.elem_order[s];
+    float *blk = metric.data() + (size_t)s * bs;
+    for (int t = 0; t < nt; ++t) {
+      const float *src = fluid ? d->m_fluid[t] : d->m_solid[slots[t]];
+      std::memcpy(blk + 25 * t, src + 25 * e, 25 * sizeof(float));
+    }
+    int32_t info = 0;
+    if (axial[e]) {
+      info = axcount + 1;
+      for (int q = 0; q < na; ++q)
+        for (int jj = 0; jj < 5; ++jj)
+          m0.push_back(fluid ? (nonmono ? d->m0_w_fl[5 * e + jj] : 0.f) : d->m0_solid[aslots[q]][5 * e + jj]);
+      ++axcount;
+    }
+    if (srcslot[e] >= 0) info |= (srcslot[e] + 1) << 24;
+    elinfo[s] = info;
+    if (use_fs) std::memcpy(fsmask.data() + 25 * s, d->fluid_free_surface_mask + 25 * e, 25 * sizeof(float));
+  }
+  std::vector<uint32_t> pts = pl.pt_words;
+  if (!fluid && h->n_src > 0) {
+    // mark the points that carry a solid source term
+    std::vector<uint8_t> issrc(h->nglob_s, 0);
+    // the host copy of the source table is rebuilt here from the descriptor
+    for (int k = 0; k < d->nelsrc; ++k) {
+      const int64_t e = d->ielsrc[k] - 1;
+      for (int q = 0; q < 25; ++q) {
+        bool nz = false;
+        for (int c = 0; c < 3; ++c) nz |= d->source_term_el[q + 25 * k + 200 * c] != 0.f;
+        if (nz) issrc[h->igloc_s[25 * e + q] - 1] = 1;
+      }
+    }
+    for (auto &w : pts)
+      if (issrc[w & kPtIndexMask]) w |= kPtSource;
+  }
+  int rc;
+  if ((rc = upload(h, &dd.meta, pl.meta))) return rc;
+  if ((rc = upload(h, &dd.pts, pts))) return rc;
+  if ((rc = upload(h, &dd.elpts, pl.elem_pts))) return rc;
+  if ((rc = upload(h, &dd.elinfo, elinfo))) return rc;
+  if ((rc = upload(h, &dd.metric, metric))) return rc;
+  if ((rc = upload(h, &dd.m0, m0))) return rc;
+  if (use_fs && (rc = upload(h, &dd.fsmask, fsmask))) return rc;
+  if (fluid && d->fluid_src && d->nelsrc > 0) {
+    std::vector<float> s((size_t)8 * 25, 0.f);
+    for (int k = 0; k < d->nelsrc; ++k)
+      for (int q = 0; q < 25; ++q) s[25 * k + q] = d->source_term_fl[q + 25 * k];
+    if ((rc = upload(h, &dd.srcfl, s))) return rc;
+  }
+  return AXG_OK;
+}
+
+int upload_coupling(axg_handle *h, const CouplingHost &c, Coupling &out) {
+  out.n = (int32_t)c.pt_gidx.size();
+  int rc;
+  int32_t *pg, *st, *sg;
+  float *b1, *b2, *mk;
+  if ((rc = upload(h, &pg, c.pt_gidx))) return rc;
+  if ((rc = upload(h, &st, c.start))) return rc;
+  if ((rc = upload(h, &sg, c.src_gidx))) return rc;
+  if ((rc = upload(h, &b1, c.b1))) return rc;
+  if ((rc = upload(h, &b2, c.b2))) return rc;
+  if ((rc = upload(h, &mk, c.mask))) return rc;
+  out.pt_gidx = pg;
+  out.start = st;
+  out.src_gidx = sg;
+  out.b1 = b1;
+  out.b2 = b2;
+  out.mask = mk;
+  return AXG_OK;
+}
+
+// group (receiver point, contribution) pairs by receiving point, keeping the
+// boundary-list order inside each group
+CouplingHost make_coupling(std::vector<std::tuple<int32_t, int32_t, float, float, float>> &v) {
+  std::stable_sort(v.begin(), v.end(),
+                   [](const auto &a, const auto &b) { return std::get<0>(a) < std::get<0>(b); });
+  CouplingHost c;
+  for (size_t k = 0; k < v.size(); ++k) {
+    if (k == 0 || std::get<0>(v[k]) != std::get<0>(v[k - 1])) {
+      c.pt_gidx.push_back(std::get<0>(v[k]));
+      c.start.push_back((int32_t)k);
+    }
+    c.src_gidx.push_back(std::get<1>(v[k]));
+    c.b1.push_back(std::get<2>(v[k]));
+    c.b2.push_back(std::get<3>(v[k]));
+    c.mask.push_back(std::get<4>(v[k]));
+  }
+  c.start.push_back((int32_t)v.size());
+  return c;
+}
+
+StateArgs solid_state(axg_handle *h) {
+  StateArgs s{};
+  for (int c = 0; c < 3; ++c) {
+    s.u[c] = h->su[c];
+    s.v[c] = h->sv[c];
+    s.a[c] = h->sa[c];
+    s.f[c] = h->sf[c];
+  }
+  s.inv_mass = h->inv_mass_s;
+  s.gamma = h->gamma_s;
+  s.stf = h->stf;
+  s.iter = h->iter;
+  s.blowup = h->blowup;
+  s.thresh = (float)(10.0 * std::fabs(h->magnitude));
+  s.dt = (float)h->dt;
+  s.hdt = (float)(0.5 * h->dt);
+  s.hdt2 = (float)(0.5 * h->dt * h->dt);
+  s.src.gidx = h->src_gidx_d;
+  s.src.val = h->src_val_d;
+  s.src.n = h->n_src;
+  return s;
+}
+
+StateArgs fluid_state(axg_handle *h) {
+  StateArgs s = solid_state(h);
+  for (int c = 0; c < 3; ++c) s.u[c] = s.v[c] = s.a[c] = s.f[c] = nullptr;
+  s.u[0] = h->fu;
+  s.v[0] = h->fv;
+  s.a[0] = h->fa;
+  s.f[0] = h->ff;
+  s.inv_mass = h->inv_mass_f;
+  s.gamma = h->gamma_f;
+  s.src.n = 0;
+  return s;
+}
+
+DomainArgs domain_args(const DomainDev &dd) {
+  DomainArgs a{};
+  a.meta = dd.meta;
+  a.pts = dd.pts;
+  a.elpts = dd.elpts;
+  a.elinfo = dd.elinfo;
+  a.metric = dd.metric;
+  a.m0 = dd.m0;
+  a.fsmask = dd.fsmask;
+  a.srcfl = dd.srcfl;
+  return a;
+}
+
+template <int POLE, int MODE>
+void launch_solid_colours(axg_handle *h, cudaStream_t s) {
+  DomainArgs a = domain_args(h->ds);
+  StateArgs st = solid_state(h);
+  for (int c = 0; c < h->ps.n_colours; ++c) {
+    a.patch_begin = h->ps.colour_start[c];
+    const int n = h->ps.colour_start[c + 1] - h->ps.colour_start[c];
+    solid_patch_kernel<POLE, MODE><<<n, kThreads, 0, s>>>(a, st, h->spec);
+  }
+}
+
+template <int MODE>
+void launch_solid(axg_handle *h, cudaStream_t s) {
+  if (h->pole == AXG_MONOPOLE) launch_solid_colours<POLE_MONO, MODE>(h, s);
+  else if (h->pole == AXG_DIPOLE) launch_solid_colours<POLE_DI, MODE>(h, s);
+  else launch_solid_colours<POLE_QUAD, MODE>(h, s);
+}
+
+__global__ void zero_points_kernel(const int32_t *gidx, int32_t n, float *f0, float *f1, float *f2) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int g = gidx[q];
+  f0[g] = 0.f;
+  if (f1) f1[g] = 0.f;
+  f2[g] = 0.f;
+}
+
+void enqueue_force(axg_handle *h, cudaStream_t s) {
+  if (h->to_solid.n > 0)
+    zero_points_kernel<<<(h->to_solid.n + 255) / 256, 256, 0, s>>>(h->to_solid.pt_gidx, h->to_solid.n, h->sf[0],
+                                                                   h->sf[1], h->sf[2]);
+  launch_solid<MODE_FORCE>(h, s);
+}
+
+void enqueue_step(axg_handle *h, cudaStream_t s) {
+  StateArgs ss = solid_state(h), fs = fluid_state(h);
+  if (h->nel_f > 0) {
+    if (h->to_fluid.n > 0) {
+      const int nb = (h->to_fluid.n + 255) / 256;
+      if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(h->to_fluid, ss, h->ff);
+      else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(h->to_fluid, ss, h->ff);
+    }
+    DomainArgs a = domain_args(h->df);
+    for (int c = 0; c < h->pf.n_colours; ++c) {
+      a.patch_begin = h->pf.colour_start[c];
+      const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
+      if (h->pole == AXG_MONOPOLE) fluid_patch_kernel<0><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+      else fluid_patch_kernel<1><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+    }
+    if (h->to_solid.n > 0) {
+      const int nb = (h->to_solid.n + 255) / 256;
+      if (h->pole == AXG_MONOPOLE) couple_to_solid_kernel<POLE_MONO><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
+      else if (h->pole == AXG_DIPOLE) couple_to_solid_kernel<POLE_DI><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
+      else couple_to_solid_kernel<POLE_QUAD><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
+    }
+  }
+  launch_solid<MODE_NEWMARK>(h, s);
+  receivers_kernel<<<1, 256, 0, s>>>(ss, h->rec_gidx_d, h->num_rec, h->seis_it, h->pole, h->rec, h->nseismo,
+                                     h->iter);
+}
+
+int build_graph(axg_handle *h, int nsteps) {
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < nsteps; ++k) enqueue_step(h, h->stream);
+  CK(cudaStreamEndCapture(h->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+  h->graph_steps = nsteps;
+  return AXG_OK;
+}
+
+void release(axg_handle *h) {
+  if (!h) return;
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  for (void *p : h->allocs) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  h->allocs.clear();
+}
+
+int state_ptrs(axg_handle *h, int field, float **p, int *nc, int64_t *nglob, bool *fluid) {
+  *fluid = false;
+  *nglob = h->nglob_s;
+  *nc = 3;
+  switch (field) {
+    case AXG_FIELD_DISP: for (int c = 0; c < 3; ++c) p[c] = h->su[c]; return AXG_OK;
+    case AXG_FIELD_VELO: for (int c = 0; c < 3; ++c) p[c] = h->sv[c]; return AXG_OK;
+    case AXG_FIELD_ACC0: for (int c = 0; c < 3; ++c) p[c] = h->sa[c]; return AXG_OK;
+    default: break;
+  }
+  *fluid = true;
+  *nglob = h->nglob_f;
+  *nc = 1;
+  switch (field) {
+    case AXG_FIELD_CHI: p[0] = h->fu; return AXG_OK;
+    case AXG_FIELD_DCHI: p[0] = h->fv; return AXG_OK;
+    case AXG_FIELD_DDCHI0: p[0] = h->fa; return AXG_OK;
+    default: break;
+  }
+  return fail(h, AXG_ERR_BAD_ARG, fmt("field %d not available", field));
+}
+
+
+// points written first by a coupling pre-pass (receiving side of bdry_copy2*)
+void prepass_flags(const axg_mesh_desc *d, std::vector<uint8_t> &pre_s, std::vector<uint8_t> &pre_f) {
+  pre_s.assign(d->nglob_solid, 0);
+  pre_f.assign(d->nel_fluid > 0 ? d->nglob_fluid : 0, 0);
+  for (int b = 0; b < d->nel_bdry; ++b) {
+    const int64_t es = d->bdry_solid_el[b] - 1, ef = d->bdry_fluid_el[b] - 1;
+    for (int i = 0; i < 5; ++i) {
+      pre_s[d->igloc_solid[25 * es + i + 5 * d->bdry_jpol_solid[b]] - 1] = 1;
+      pre_f[d->igloc_fluid[25 * ef + i + 5 * d->bdry_jpol_fluid[b]] - 1] = 1;
+    }
+  }
+}
+
+int check_igloc(const int32_t *ig, int64_t n, int64_t nglob, const char *what) {
+  for (int64_t p = 0; p < n; ++p)
+    if (ig[p] < 1 || ig[p] > nglob) return fail(nullptr, AXG_ERR_BAD_DESC, fmt("%s entry outside 1..nglob", what));
+  return AXG_OK;
+}
+
+}  // namespace
+
+extern "C" int axg_reset(axg_handle *h);
+extern "C" int axg_device_count(void);
+
+namespace {
+int create_impl(axg_handle *h, const axg_mesh_desc *d) {
+  int rc = AXG_OK;
+  h->pole = d->src_type;
+  h->fluid_src = d->fluid_src;
+  h->nel_s = d->nel_solid;
+  h->nel_f = d->nel_fluid;
+  h->nglob_s = d->nglob_solid;
+  h->nglob_f = d->nglob_fluid;
+  h->niter = d->niter;
+  h->seis_it = d->seis_it > 0 ? d->seis_it : 1;
+  h->num_rec = d->num_rec;
+  h->nseismo = d->niter / h->seis_it + 1;
+  h->absorbing = d->have_absorbing_bc != 0;
+  h->dt = d->deltat;
+  h->magnitude = d->magnitude;
+  h->igloc_s.assign(d->igloc_solid, d->igloc_solid + 25 * h->nel_s);
+  if (h->nel_f > 0) h->igloc_f.assign(d->igloc_fluid, d->igloc_fluid + 25 * h->nel_f);
+  for (int64_t p = 0; p < 25 * h->nel_s; ++p)
+    if (h->igloc_s[p] < 1 || h->igloc_s[p] > h->nglob_s)
+      return fail(h, AXG_ERR_BAD_DESC, "igloc_solid entry outside 1..nglob_solid");
+  for (int64_t p = 0; p < 25 * h->nel_f; ++p)
+    if (h->igloc_f[p] < 1 || h->igloc_f[p] > h->nglob_f)
+      return fail(h, AXG_ERR_BAD_DESC, "igloc_fluid entry outside 1..nglob_fluid");
+
+  // solid-fluid coupling tables (the receiving points are written first by a pre-pass)
+  std::vector<std::tuple<int32_t, int32_t, float, float, float>> tf, ts;
+  std::vector<uint8_t> axs(h->nel_s, 0), axf(h->nel_f > 0 ? h->nel_f : 1, 0);
+  for (int k = 0; k < d->naxel_solid; ++k) axs[d->ax_el_solid[k] - 1] = 1;
+  for (int k = 0; k < d->naxel_fluid; ++k) axf[d->ax_el_fluid[k] - 1] = 1;
+  const int nb = d->nel_bdry;
+  for (int b = 0; b < nb; ++b) {
+    const int64_t es = d->bdry_solid_el[b] - 1, ef = d->bdry_fluid_el[b] - 1;
+    const int js = d->bdry_jpol_solid[b], jf = d->bdry_jpol_fluid[b];
+    for (int i = 0; i < 5; ++i) {
+      const int32_t gs = h->igloc_s[25 * es + i + 5 * js] - 1;
+      const int32_t gf = h->igloc_f[25 * ef + i + 5 * jf] - 1;
+      const float b1 = d->bdry_matr[i + 5 * b], b2 = d->bdry_matr[i + 5 * (b + nb)];
+      float mf = (d->src_type != AXG_MONOPOLE && axf[ef] && i == 0) ? 0.f : 1.f;
+      if (d->fluid_free_surface_mask) mf *= d->fluid_free_surface_mask[25 * ef + i + 5 * jf];
+      tf.emplace_back(gf, gs, b1, b2, mf);
+      ts.emplace_back(gs, gf, b1, b2, (axs[es] && i == 0) ? 0.f : 1.f);
+    }
+  }
+  CouplingHost cf = make_coupling(tf), cs = make_coupling(ts);
+  h->pre_s.assign(h->nglob_s, 0);
+  for (int32_t g : cs.pt_gidx) h->pre_s[g] = 1;
+  if (h->nel_f > 0) {
+    h->pre_f.assign(h->nglob_f, 0);
+    for (int32_t g : cf.pt_gidx) h->pre_f[g] = 1;
+  }
+  std::string perr = build_plan(h->igloc_s.data(), h->nel_s, h->nglob_s, h->patch_elems, h->pre_s, h->ps);
+  if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "solid plan: " + perr);
+  if (h->nel_f > 0) {
+    perr = build_plan(h->igloc_f.data(), h->nel_f, h->nglob_f, h->patch_elems, h->pre_f, h->pf);
+    if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "fluid plan: " + perr);
+  }
+#ifdef AXG_VALIDATE_PLAN
+  perr = validate_plan(h->igloc_s.data(), h->nel_s, h->nglob_s, h->pre_s, h->ps);
+  if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "solid plan invalid: " + perr);
+#endif
+
+  // receivers and the solid source table
+  for (int r = 0; r < h->num_rec; ++r) {
+    const int64_t e = d->recfile_el[r] - 1;
+    const int ip = d->recfile_el[r + h->num_rec], jp = d->recfile_el[r + 2 * h->num_rec];
+    h->rec_gidx.push_back(h->igloc_s[25 * e + ip + 5 * jp] - 1);
+  }
+  std::vector<int32_t> src_g;
+  std::vector<float> src_v;
+  if (!d->fluid_src) {
+    std::map<int32_t, int> seen;
+    for (int k = 0; k < d->nelsrc; ++k) {
+      const int64_t e = d->ielsrc[k] - 1;
+      for (int q = 0; q < 25; ++q) {
+        float v[3];
+        bool nz = false;
+        for (int c = 0; c < 3; ++c) {
+          v[c] = d->source_term_el[q + 25 * k + 200 * c];
+          nz |= v[c] != 0.f;
+        }
+        const int32_t g = h->igloc_s[25 * e + q] - 1;
+        if (!nz || seen.count(g)) continue;
+        seen[g] = 1;
+        src_g.push_back(g);
+        src_v.insert(src_v.end(), v, v + 3);
+      }
+    }
+  }
+  h->n_src = (int32_t)src_g.size();
+
+  // ---- device
+  CK(cudaGetDevice(&h->device));
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&h->ev0));
+  CK(cudaEventCreate(&h->ev1));
+  for (int k = 0; k < 25; ++k) {
+    h->spec.g1[k] = d->G1[k];
+    h->spec.g2[k] = d->G2[k];
+  }
+  for (int k = 0; k < 5; ++k) h->spec.g0[k] = d->G0[k];
+  if ((rc = build_domain(h, d, false))) return rc;
+  if ((rc = build_domain(h, d, true))) return rc;
+  const bool mono = h->pole == AXG_MONOPOLE;
+  for (int c = 0; c < 3; ++c) {
+    if (mono && c == 1) continue;
+    if ((rc = dalloc(h, &h->su[c], h->nglob_s)) || (rc = dalloc(h, &h->sv[c], h->nglob_s)) ||
+        (rc = dalloc(h, &h->sa[c], h->nglob_s)) || (rc = dalloc(h, &h->sf[c], h->nglob_s)))
+      return rc;
+  }
+  if ((rc = upload(h, &h->inv_mass_s, per_point(d->inv_mass_rho, h->igloc_s, h->nglob_s)))) return rc;
+  if (h->absorbing && (rc = upload(h, &h->gamma_s, per_point(d->solid_absorbing_gamma, h->igloc_s, h->nglob_s))))
+    return rc;
+  if (h->nel_f > 0) {
+    if ((rc = dalloc(h, &h->fu, h->nglob_f)) || (rc = dalloc(h, &h->fv, h->nglob_f)) ||
+        (rc = dalloc(h, &h->fa, h->nglob_f)) || (rc = dalloc(h, &h->ff, h->nglob_f)))
+      return rc;
+    if ((rc = upload(h, &h->inv_mass_f, per_point(d->inv_mass_fluid, h->igloc_f, h->nglob_f)))) return rc;
+    if (h->absorbing &&
+        (rc = upload(h, &h->gamma_f, per_point(d->fluid_absorbing_gamma, h->igloc_f, h->nglob_f))))
+      return rc;
+  }
+  std::vector<float> stf(d->stf ? d->stf : (const float *)nullptr, d->stf ? d->stf + d->niter : nullptr);
+  if (stf.empty()) stf.assign(1, 0.f);
+  if ((rc = upload(h, &h->stf, stf))) return rc;
+  if ((rc = dalloc(h, &h->rec, (size_t)h->nseismo * 3 * std::max(h->num_rec, 1)))) return rc;
+  if ((rc = upload(h, &h->rec_gidx_d, h->rec_gidx))) return rc;
+  if ((rc = upload(h, &h->src_gidx_d, src_g))) return rc;
+  if ((rc = upload(h, &h->src_val_d, src_v))) return rc;
+  if ((rc = dalloc(h, &h->iter, 2))) return rc;
+  h->blowup = h->iter + 1;
+  if ((rc = upload_coupling(h, cf, h->to_fluid))) return rc;
+  if ((rc = upload_coupling(h, cs, h->to_solid))) return rc;
+  h->kernels_per_force = h->ps.n_colours + (h->to_solid.n > 0 ? 1 : 0);
+  h->kernels_per_step = h->ps.n_colours + 1 +
+                        (h->nel_f > 0 ? h->pf.n_colours + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);
+  return axg_reset(h);
+}
+}  // namespace
+
+// ============================================================== C-ABI
+
+extern "C" {
+
+const char *axg_version(void) { return "axisem_gb300 1 (sm_103a, patch-coloured assembly)"; }
+
+int axg_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int axg_create(const axg_mesh_desc *d, axg_handle **out) {
+  if (!out) return fail(nullptr, AXG_ERR_BAD_ARG, "out is NULL");
+  *out = nullptr;
+  int rc = validate(d);
+  if (rc) return rc;
+  if (axg_device_count() < 1) return fail(nullptr, AXG_ERR_NO_DEVICE, "no CUDA device is visible");
+  axg_handle *h = new axg_handle();
+  rc = create_impl(h, d);
+  if (rc) {
+    g_create_error = h->err;
+    release(h);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return AXG_OK;
+}
+
+int axg_reset(axg_handle *h) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  for (int c = 0; c < 3; ++c) {
+    if (h->su[c]) CK(cudaMemsetAsync(h->su[c], 0, h->nglob_s * sizeof(float), h->stream));
+    if (h->sv[c]) CK(cudaMemsetAsync(h->sv[c], 0, h->nglob_s * sizeof(float), h->stream));
+    if (h->sa[c]) CK(cudaMemsetAsync(h->sa[c], 0, h->nglob_s * sizeof(float), h->stream));
+    if (h->sf[c]) CK(cudaMemsetAsync(h->sf[c], 0, h->nglob_s * sizeof(float), h->stream));
+  }
+  if (h->nel_f > 0) {
+    CK(cudaMemsetAsync(h->fu, 0, h->nglob_f * sizeof(float), h->stream));
+    CK(cudaMemsetAsync(h->fv, 0, h->nglob_f * sizeof(float), h->stream));
+    CK(cudaMemsetAsync(h->fa, 0, h->nglob_f * sizeof(float), h->stream));
+    CK(cudaMemsetAsync(h->ff, 0, h->nglob_f * sizeof(float), h->stream));
+  }
+  // the iter-0 seismogram sample (dump_stuff(0,...)) is the zero wavefield
+  CK(cudaMemsetAsync(h->rec, 0, (size_t)h->nseismo * 3 * std::max(h->num_rec, 1) * sizeof(float), h->stream));
+  CK(cudaMemsetAsync(h->iter, 0, 2 * sizeof(int32_t), h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return AXG_OK;
+}
+
+int axg_run(axg_handle *h, int32_t first_iter, int32_t n_iter) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  if (n_iter < 0 || first_iter < 1 || (int64_t)first_iter + n_iter - 1 > h->niter)
+    return fail(h, AXG_ERR_BAD_ARG, fmt("iterations %d..%d outside 1..niter=%d", first_iter, first_iter + n_iter - 1,
+                                        h->niter));
+  if (n_iter == 0) return AXG_OK;
+  CK(cudaMemcpyAsync(h->iter, &first_iter, sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  int32_t done = 0;
+  while (done < n_iter) {
+    const int k = std::min<int32_t>(h->steps_per_graph, n_iter - done);
+    if (k == h->steps_per_graph) {
+      if (!h->graph || h->graph_steps != k) {
+        int rc = build_graph(h, k);
+        if (rc) return rc;
+      }
+      CK(cudaGraphLaunch(h->graph, h->stream));
+    } else {
+      for (int s = 0; s < k; ++s) enqueue_step(h, h->stream);
+      CK(cudaGetLastError());
+    }
+    done += k;
+    int32_t bl = 0;
+    CK(cudaMemcpyAsync(&bl, h->blowup, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (bl != 0)
+      return fail(h, AXG_ERR_BLOWUP,
+                  fmt("displacements blew up: |disp(1,1,:,:)| > 10 |magnitude| at time step %d", bl + 1));
+  }
+  return AXG_OK;
+}
+
+int axg_get_receivers(axg_handle *h, float *out, int32_t cap, int32_t *nseismo_out) {
+  if (!h || !out) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  if (cap < h->nseismo) return fail(h, AXG_ERR_BAD_ARG, fmt("nseismo_cap %d < nseismo %d", cap, h->nseismo));
+  std::vector<float> buf((size_t)h->nseismo * 3 * std::max(h->num_rec, 1));
+  CK(cudaMemcpyAsync(buf.data(), h->rec, buf.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  int32_t it = 0;
+  CK(cudaMemcpyAsync(&it, h->iter, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int r = 0; r < h->num_rec; ++r)
+    for (int c = 0; c < 3; ++c)
+      for (int s = 0; s < h->nseismo; ++s)
+        out[s + (int64_t)cap * (c + 3 * (int64_t)r)] = buf[s + (int64_t)h->nseismo * (c + 3 * (int64_t)r)];
+  // samples written: iter 0 plus every seis_it steps completed
+  const int32_t last = it > 0 ? it - 1 : 0;
+  if (nseismo_out) *nseismo_out = std::min(h->nseismo, last / h->seis_it + 1);
+  return AXG_OK;
+}
+
+int axg_get_state(axg_handle *h, int32_t field, float *out) {
+  if (!h || !out) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  if (field == AXG_FIELD_MEMVAR) return fail(h, AXG_ERR_UNSUPPORTED, "attenuation is not implemented in this build");
+  float *p[3] = {};
+  int nc;
+  int64_t ng;
+  bool fluid;
+  int rc = state_ptrs(h, field, p, &nc, &ng, &fluid);
+  if (rc) return rc;
+  const std::vector<int32_t> &ig = fluid ? h->igloc_f : h->igloc_s;
+  const int64_t cs = (int64_t)ig.size();
+  std::vector<float> g(ng);
+  for (int c = 0; c < nc; ++c) {
+    if (!p[c]) {
+      std::fill(out + cs * c, out + cs * (c + 1), 0.f);
+      continue;
+    }
+    CK(cudaMemcpyAsync(g.data(), p[c], ng * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int64_t q = 0; q < cs; ++q) out[q + cs * c] = g[ig[q] - 1];
+  }
+  return AXG_OK;
+}
+
+int axg_set_state(axg_handle *h, int32_t field, const float *in) {
+  if (!h || !in) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  if (field == AXG_FIELD_MEMVAR) return fail(h, AXG_ERR_UNSUPPORTED, "attenuation is not implemented in this build");
+  float *p[3] = {};
+  int nc;
+  int64_t ng;
+  bool fluid;
+  int rc = state_ptrs(h, field, p, &nc, &ng, &fluid);
+  if (rc) return rc;
+  const std::vector<int32_t> &ig = fluid ? h->igloc_f : h->igloc_s;
+  const int64_t cs = (int64_t)ig.size();
+  for (int c = 0; c < nc; ++c) {
+    if (!p[c]) continue;
+    std::vector<float> g = per_point(in + cs * c, ig, ng);
+    CK(cudaMemcpy(p[c], g.data(), ng * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  return AXG_OK;
+}
+
+int axg_upload_gvec_disp(axg_handle *h, const float *u) {
+  if (!h || !u) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  for (int c = 0; c < 3; ++c)
+    if (h->su[c])
+      CK(cudaMemcpyAsync(h->su[c], u + h->nglob_s * c, h->nglob_s * sizeof(float), cudaMemcpyHostToDevice,
+                         h->stream));
+  return AXG_OK;
+}
+
+int axg_download_gvec_force(axg_handle *h, float *f) {
+  if (!h || !f) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  for (int c = 0; c < 3; ++c) {
+    if (h->sf[c])
+      CK(cudaMemcpyAsync(f + h->nglob_s * c, h->sf[c], h->nglob_s * sizeof(float), cudaMemcpyDeviceToHost,
+                         h->stream));
+    else
+      std::memset(f + h->nglob_s * c, 0, h->nglob_s * sizeof(float));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return AXG_OK;
+}
+
+int axg_stiffness_assembled_device(axg_handle *h, void *stream) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+  enqueue_force(h, s);
+  CK(cudaGetLastError());
+  return AXG_OK;
+}
+
+int axg_stiffness_assembled(axg_handle *h, const float *u, float *f) {
+  if (!h || !u || !f) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  int rc = axg_upload_gvec_disp(h, u);
+  if (rc) return rc;
+  enqueue_force(h, h->stream);
+  CK(cudaGetLastError());
+  return axg_download_gvec_force(h, f);
+}
+
+int axg_set_tuning(axg_handle *h, int32_t patch_elems, int32_t steps_per_graph) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  if (steps_per_graph < 0 || steps_per_graph > 4096) return fail(h, AXG_ERR_BAD_ARG, "steps_per_graph out of range");
+  if (patch_elems != 0 && patch_elems != h->patch_elems)
+    return fail(h, AXG_ERR_UNSUPPORTED, "patch_elems is fixed at axg_create in this build");
+  if (steps_per_graph > 0 && steps_per_graph != h->steps_per_graph) {
+    h->steps_per_graph = steps_per_graph;
+    if (h->graph) {
+      cudaGraphExecDestroy(h->graph);
+      h->graph = nullptr;
+    }
+  }
+  return AXG_OK;
+}
+
+int axg_get_info(axg_handle *h, axg_info *info) {
+  if (!h || !info) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  std::memset(info, 0, sizeof *info);
+  info->n_patches_solid = h->ps.n_patches;
+  info->n_patches_fluid = h->pf.n_patches;
+  info->n_colours_solid = h->ps.n_colours;
+  info->n_colours_fluid = h->pf.n_colours;
+  info->max_subrounds_solid = h->ps.max_rounds;
+  info->max_subrounds_fluid = h->pf.max_rounds;
+  info->device_bytes = h->dev_bytes;
+  info->kernels_per_step = h->kernels_per_step;
+  info->kernels_per_force = h->kernels_per_force;
+  info->patch_points_solid = h->ps.total_pts;
+  return AXG_OK;
+}
+
+int axg_get_solid_colouring(axg_handle *h, int32_t *patch_of_elem, int32_t *colour_of_patch, int64_t cap) {
+  if (!h || !patch_of_elem || !colour_of_patch) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  if (cap < h->ps.n_patches) return fail(h, AXG_ERR_BAD_ARG, "n_patch_cap too small");
+  std::memcpy(patch_of_elem, h->ps.patch_of_elem.data(), h->nel_s * sizeof(int32_t));
+  std::memcpy(colour_of_patch, h->ps.colour_of_patch.data(), h->ps.n_patches * sizeof(int32_t));
+  return AXG_OK;
+}
+
+int axg_plan_check(const axg_mesh_desc *d, int32_t patch_elems, axg_info *info) {
+  if (!info) return fail(nullptr, AXG_ERR_BAD_ARG, "info is NULL");
+  int rc = validate(d);
+  if (rc) return rc;
+  if ((rc = check_igloc(d->igloc_solid, 25 * (int64_t)d->nel_solid, d->nglob_solid, "igloc_solid"))) return rc;
+  if (d->nel_fluid > 0 &&
+      (rc = check_igloc(d->igloc_fluid, 25 * (int64_t)d->nel_fluid, d->nglob_fluid, "igloc_fluid")))
+    return rc;
+  std::vector<uint8_t> pre_s, pre_f;
+  prepass_flags(d, pre_s, pre_f);
+  std::memset(info, 0, sizeof *info);
+  DomainPlan ps, pf;
+  std::string e = build_plan(d->igloc_solid, d->nel_solid, d->nglob_solid, patch_elems, pre_s, ps);
+  if (e.empty()) e = validate_plan(d->igloc_solid, d->nel_solid, d->nglob_solid, pre_s, ps);
+  if (!e.empty()) return fail(nullptr, AXG_ERR_BAD_DESC, "solid plan: " + e);
+  if (d->nel_fluid > 0) {
+    e = build_plan(d->igloc_fluid, d->nel_fluid, d->nglob_fluid, patch_elems, pre_f, pf);
+    if (e.empty()) e = validate_plan(d->igloc_fluid, d->nel_fluid, d->nglob_fluid, pre_f, pf);
+    if (!e.empty()) return fail(nullptr, AXG_ERR_BAD_DESC, "fluid plan: " + e);
+  }
+  info->n_patches_solid = ps.n_patches;
+  info->n_patches_fluid = pf.n_patches;
+  info->n_colours_solid = ps.n_colours;
+  info->n_colours_fluid = pf.n_colours;
+  info->max_subrounds_solid = ps.max_rounds;
+  info->max_subrounds_fluid = pf.max_rounds;
+  info->patch_points_solid = ps.total_pts;
+  info->kernels_per_force = ps.n_colours;
+  return AXG_OK;
+}
+
+int axg_time_stiffness(axg_handle *h, int32_t n, float *ms_avg) {
+  if (!h || !ms_avg || n < 1) return fail(h, AXG_ERR_BAD_ARG, "bad argument");
+  CK(cudaEventRecord(h->ev0, h->stream));
+  for (int k = 0; k < n; ++k) enqueue_force(h, h->stream);
+  CK(cudaEventRecord(h->ev1, h->stream));
+  CK(cudaEventSynchronize(h->ev1));
+  CK(cudaGetLastError());
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  *ms_avg = ms / n;
+  return AXG_OK;
+}
+
+void axg_destroy(axg_handle *h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  release(h);
+  delete h;
+}
+
+const char *axg_last_error(axg_handle *h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+}  // extern "C"

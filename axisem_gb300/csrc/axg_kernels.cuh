@@ -1,0 +1,630 @@
+// axg_kernels.cuh -- sm_103a kernels of the AxiSEM time loop.
+//
+// One CTA per patch of elements (axg_plan.h); one warp per element, one lane
+// per GLL point (i, j) = (lane % 5, lane / 5), lanes 25..31 idle.  The 5x5
+// tensor-product contractions of the reference (mxm_4 / vxm_4 of
+// SOLVER/unrolled_loops.f90) are done with warp shuffles: lane (i, j) reads
+// the five values of its column (k, j) or row (i, k) from the other lanes.
+// Per-lane copies of the needed rows/columns of G1, G2 stay in registers.
+//
+// A patch kernel has three phases:
+//   1. gather: the patch's global points are read once into shared memory
+//      (time loop: the Newmark predictor is applied on the fly, so that the
+//      arrays in HBM always hold the reference's state disp/velo/acc0);
+//   2. elements, sub-round by sub-round: each warp computes its element's
+//      stiffness and adds it into the shared point accumulators (elements
+//      of one sub-round share no point, so there is no race);
+//   3. write-back: partial sums are added to the global force (the first
+//      writer stores); the last writer of a point applies the Newmark
+//      corrector (SOLVER/time_evol_wave.F90:466-494) in registers and stores
+//      disp/velo/acc0 -- the assembled force of that point never touches HBM.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "axg_plan.h"
+
+namespace axg {
+
+constexpr int kWarps = 8;
+constexpr int kThreads = 32 * kWarps;
+constexpr unsigned kFull = 0xffffffffu;
+
+enum { POLE_MONO = 0, POLE_DI = 1, POLE_QUAD = 2 };
+enum { MODE_FORCE = 0, MODE_NEWMARK = 1 };
+
+// slot of each metric array inside an element's block (same order as the
+// host packing, SOLID_TERMS_USED of the Python mirror)
+enum : int {
+  S_M1 = 0, S_M2, S_M3, S_M4, S_MW1, S_M11S, S_M21S, S_M41S, S_M12S, S_M22S, S_M32S, S_M42S,
+  S_M11Z, S_M21Z, S_M41Z,
+  S_M5 = 15, S_M6, S_M7, S_M8, S_MW2, S_MW3,
+  // dipole
+  S_M13S = 21, S_M33S, S_M43S,
+  // quadrupole
+  S_MW4 = 21, S_MW5, S_M1PHI, S_M2PHI, S_M4PHI
+};
+__host__ __device__ constexpr int n_terms(int pole) { return pole == POLE_MONO ? 15 : (pole == POLE_DI ? 24 : 26); }
+__host__ __device__ constexpr int n_axial(int pole) { return pole == POLE_MONO ? 3 : (pole == POLE_DI ? 9 : 6); }
+__host__ __device__ constexpr int block_stride(int nt) { return ((nt * 25 + 3) / 4) * 4; }
+
+struct SpecDev {
+  float g1[25], g2[25], g0[5];
+};
+
+struct SrcTable {           // solid source points (<= 200)
+  const int32_t *gidx;      // global point
+  const float *val;         // (n, 3)
+  int32_t n;
+};
+
+struct DomainArgs {
+  const PatchMeta *meta;
+  const uint32_t *pts;
+  const uint16_t *elpts;
+  const int32_t *elinfo;    // bits 0..23: axial slot + 1; bits 24..27: source slot + 1
+  const float *metric;      // per element block_stride(nt) floats (launch order)
+  const float *m0;          // per axial slot n_axial*5 floats
+  const float *fsmask;      // fluid free-surface mask per element (launch order) or null
+  const float *srcfl;       // fluid element source terms (8, 25) or null
+  int32_t patch_begin;
+};
+
+struct StateArgs {
+  float *u[3];              // disp (solid, gvec layout) / chi (fluid: u[0])
+  float *v[3];              // velo / dchi
+  float *a[3];              // acc0 / ddchi0
+  float *f[3];              // force partial sums
+  const float *inv_mass;    // per global point
+  const float *gamma;       // absorbing gamma per global point or null
+  const float *stf;         // (niter)
+  const int32_t *iter;      // device iteration counter (1-based iter of this step)
+  int32_t *blowup;          // first iteration that blew up (0 = none)
+  float thresh;             // 10 |magnitude|
+  float dt, hdt, hdt2;
+  SrcTable src;
+};
+
+// ------------------------------------------------------------ small helpers
+
+__device__ __forceinline__ float predict(float d, float v, float a, float dt, float hdt2) {
+  // disp + deltat*velo + half_dt_sq*acc0 (SOLVER/time_evol_wave.F90:357-364)
+  return fmaf(hdt2, a, fmaf(dt, v, d));
+}
+
+// X(i,j) = sum_k c[k] * v(k,j)   (v(k,j) held by lane k + 5 j)
+__device__ __forceinline__ float dxi(float v, const float (&c)[5], int j5) {
+  float s = c[0] * __shfl_sync(kFull, v, j5);
+  s = fmaf(c[1], __shfl_sync(kFull, v, j5 + 1), s);
+  s = fmaf(c[2], __shfl_sync(kFull, v, j5 + 2), s);
+  s = fmaf(c[3], __shfl_sync(kFull, v, j5 + 3), s);
+  s = fmaf(c[4], __shfl_sync(kFull, v, j5 + 4), s);
+  return s;
+}
+// X(i,j) = sum_k v(i,k) * c[k]   (v(i,k) held by lane i + 5 k)
+__device__ __forceinline__ float deta(float v, const float (&c)[5], int i) {
+  float s = __shfl_sync(kFull, v, i) * c[0];
+  s = fmaf(__shfl_sync(kFull, v, i + 5), c[1], s);
+  s = fmaf(__shfl_sync(kFull, v, i + 10), c[2], s);
+  s = fmaf(__shfl_sync(kFull, v, i + 15), c[3], s);
+  s = fmaf(__shfl_sync(kFull, v, i + 20), c[4], s);
+  return s;
+}
+
+// per-lane rows/columns of the derivative matrices (column-major G(a,b) = g[a+5b])
+struct LaneCoef {
+  float xi2[5], xi1[5];    // G2(k,i), G1(k,i): first stage d/dxi  (mxm_4(G2T,u))
+  float eta[5];            // G2(k,j): first stage d/deta          (mxm_4(u,G2))
+  float sxi2[5], sxi1[5];  // G2(i,k), G1(i,k): second stage       (mxm_4(G2,S))
+  float seta[5];           // G2(j,k): second stage                (mxm_4(S,G2T))
+  float g0i;               // G0(i)
+  float g0[5];             // G0(k)
+};
+
+__device__ __forceinline__ void load_coef(const SpecDev &sp, int i, int j, LaneCoef &c) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    c.xi2[k] = sp.g2[k + 5 * i];
+    c.xi1[k] = sp.g1[k + 5 * i];
+    c.eta[k] = sp.g2[k + 5 * j];
+    c.sxi2[k] = sp.g2[i + 5 * k];
+    c.sxi1[k] = sp.g1[i + 5 * k];
+    c.seta[k] = sp.g2[j + 5 * k];
+    c.g0[k] = sp.g0[k];
+  }
+  c.g0i = sp.g0[i];
+}
+
+template <bool AX>
+__device__ __forceinline__ const float (&cxi(const LaneCoef &c))[5] { return AX ? c.xi1 : c.xi2; }
+template <bool AX>
+__device__ __forceinline__ const float (&csxi(const LaneCoef &c))[5] { return AX ? c.sxi1 : c.sxi2; }
+
+__device__ __forceinline__ float ldm(const float *blk, int slot, int lane) {
+  return __ldcs(blk + slot * 25 + lane);
+}
+
+// ------------------------------------------------------------ element stiffness
+
+// glob_stiffness_mono_4 (SOLVER/stiffness_mono.f90:60-157) for lane (i, j)
+template <bool AX>
+__device__ __forceinline__ void stiff_mono(const LaneCoef &c, const float *blk, const float *m0, int lane,
+                                           int i, int j, float us, float uz, float &fs, float &fz) {
+  const int j5 = 5 * j;
+  float X1 = dxi(us, cxi<AX>(c), j5);
+  float X2 = dxi(uz, cxi<AX>(c), j5);
+  float X3 = deta(us, c.eta, i);
+  float X4 = deta(uz, c.eta, i);
+  const float m1 = ldm(blk, S_M1, lane), m2 = ldm(blk, S_M2, lane), m3 = ldm(blk, S_M3, lane),
+              m4 = ldm(blk, S_M4, lane), mw1 = ldm(blk, S_MW1, lane);
+  const float m11s = ldm(blk, S_M11S, lane), m21s = ldm(blk, S_M21S, lane), m41s = ldm(blk, S_M41S, lane),
+              m12s = ldm(blk, S_M12S, lane), m22s = ldm(blk, S_M22S, lane), m32s = ldm(blk, S_M32S, lane),
+              m42s = ldm(blk, S_M42S, lane), m11z = ldm(blk, S_M11Z, lane), m21z = ldm(blk, S_M21Z, lane),
+              m41z = ldm(blk, S_M41Z, lane);
+  float ls = m4 * X4 + m2 * X3 + m1 * X1 + m3 * X2 + us * mw1;
+  const float S1s = m11s * X3 + m21s * X1 + m12s * X4 + m22s * X2 + m1 * us;
+  const float S2s = m11s * X1 + m41s * X3 + m32s * X2 + m42s * X4 + m2 * us;
+  const float S1z = m11z * X4 + m21z * X2 + m32s * X3 + m22s * X1 + m3 * us;
+  const float S2z = m11z * X2 + m41z * X4 + m12s * X1 + m42s * X3 + m4 * us;
+  X2 = deta(S2s, c.seta, i);
+  X4 = deta(S2z, c.seta, i);
+  X1 = dxi(S1s, csxi<AX>(c), j5);
+  X3 = dxi(S1z, csxi<AX>(c), j5);
+  ls = ls + X1 + X2;
+  float lz = X3 + X4;
+  if (AX) {
+    const float w1 = m0[0 * 5 + j], w2 = m0[1 * 5 + j], w3 = m0[2 * 5 + j];
+    float V1 = dxi(us, c.g0, j5);   // vxm_4(G0, us)
+    float V2 = deta(uz, c.eta, 0);  // vxm_4(uz(0,:), G2)
+    float V4 = w1 * V1 + w3 * V2;
+    const float V3 = dxi(uz, c.g0, j5);
+    V4 = V4 + w2 * V3;
+    float Xa = c.g0i * (w2 * V1);
+    const float V2b = w3 * V1;
+    const float V1b = deta(V2b, c.seta, 0);  // vxm_4(V2, G2T)
+    if (i == 0) Xa = Xa + V1b;
+    ls = ls + c.g0i * V4;
+    lz = Xa + lz;
+  }
+  fs = ls;
+  fz = lz;
+}
+
+// glob_stiffness_di_4 (SOLVER/stiffness_di.f90:60-256)
+template <bool AX>
+__device__ __forceinline__ void stiff_di(const LaneCoef &c, const float *blk, const float *m0, int lane, int i,
+                                         int j, float u1, float u2, float u3, float &f1, float &f2, float &f3) {
+  const int j5 = 5 * j;
+  float X4 = deta(u1, c.eta, i), X5 = deta(u2, c.eta, i), X6 = deta(u3, c.eta, i);
+  float X1 = dxi(u1, cxi<AX>(c), j5), X2 = dxi(u2, cxi<AX>(c), j5), X3 = dxi(u3, cxi<AX>(c), j5);
+  const float X7 = X1 + X2, X8 = X4 + X5;
+  const float m1 = ldm(blk, S_M1, lane), m2 = ldm(blk, S_M2, lane), m3 = ldm(blk, S_M3, lane),
+              m4 = ldm(blk, S_M4, lane), m5 = ldm(blk, S_M5, lane), m6 = ldm(blk, S_M6, lane),
+              m7 = ldm(blk, S_M7, lane), m8 = ldm(blk, S_M8, lane);
+  const float mw1 = ldm(blk, S_MW1, lane), mw2 = ldm(blk, S_MW2, lane), mw3 = ldm(blk, S_MW3, lane);
+  const float m11s = ldm(blk, S_M11S, lane), m21s = ldm(blk, S_M21S, lane), m41s = ldm(blk, S_M41S, lane),
+              m12s = ldm(blk, S_M12S, lane), m22s = ldm(blk, S_M22S, lane), m42s = ldm(blk, S_M42S, lane),
+              m13s = ldm(blk, S_M13S, lane), m23s = ldm(blk, S_M32S, lane), m33s = ldm(blk, S_M33S, lane),
+              m43s = ldm(blk, S_M43S, lane), m11z = ldm(blk, S_M11Z, lane), m21z = ldm(blk, S_M21Z, lane),
+              m41z = ldm(blk, S_M41Z, lane);
+  const float ls2 = m8 * X6 + m7 * X3 + m1 * X1 + m5 * X2 + m2 * X4 + m6 * X5 + mw1 * u2 + mw2 * u3;
+  const float ls3 = m4 * X4 - m4 * X5 + m3 * X1 - m3 * X2 + mw2 * u2 + mw3 * u3;
+  float c1 = m13s * X6, c2 = m23s * X3, c3 = m3 * u3;
+  float s1p = c1 + c2 + c3 + m11s * X4 + m21s * X1 + m12s * X5 + m22s * X2 + m1 * u2;
+  float s1m = c1 + c2 - c3 + m11s * X5 + m21s * X2 + m12s * X4 + m22s * X1 + m5 * u2;
+  c1 = m33s * X3;
+  c2 = m43s * X6;
+  c3 = m4 * u3;
+  const float s2p = c1 + c2 + c3 + m11s * X1 + m41s * X4 + m12s * X2 + m42s * X5 + m2 * u2;
+  const float s2m = c1 + c2 - c3 + m11s * X2 + m41s * X5 + m12s * X1 + m42s * X4 + m6 * u2;
+  float S1z = m33s * X8 + m23s * X7 + m11z * X6 + m21z * X3 + m7 * u2;
+  const float S2z = m13s * X7 + m43s * X8 + m11z * X3 + m41z * X6 + m8 * u2;
+  X1 = dxi(s1p, csxi<AX>(c), j5);
+  X3 = dxi(s1m, csxi<AX>(c), j5);
+  X5 = dxi(S1z, csxi<AX>(c), j5);
+  X2 = deta(s2p, c.seta, i);
+  X4 = deta(s2m, c.seta, i);
+  X6 = deta(S2z, c.seta, i);
+  float l1 = X1 + X2;
+  float l2 = X3 + X4 + ls2;
+  float l3 = X5 + X6 + ls3;
+  if (AX) {
+    // M0_w slots: 0:w1 1:w2 2:w3 3:w4 4:w6 5:w7 6:w8 7:w9 8:w10
+    const float w1 = m0[0 * 5 + j], w2 = m0[1 * 5 + j], w3 = m0[2 * 5 + j], w4 = m0[3 * 5 + j],
+                w6 = m0[4 * 5 + j], w7 = m0[5 * 5 + j], w8 = m0[6 * 5 + j], w9 = m0[7 * 5 + j],
+                w10 = m0[8 * 5 + j];
+    const float V1 = dxi(u1, c.g0, j5), V2 = dxi(u2, c.g0, j5), V3 = dxi(u3, c.g0, j5);
+    const float V4 = deta(u1, c.eta, 0), V5 = deta(u2, c.eta, 0);
+    (void)V5;
+    const float a_p = w1 * V2 + w3 * V3;
+    const float a_m = w1 * V1 + (w2 + w6) * V4 + w9 * V2 + w10 * V3;
+    const float a_z = w3 * V1 + (w4 + w8) * V4 + w7 * V3 + w10 * V2;
+    float S1p = c.g0i * a_p;
+    const float S1m = c.g0i * a_m;
+    S1z = c.g0i * a_z;
+    const float V4b = (w2 + w6) * V2 + (w4 + w8) * V3;
+    const float V1b = deta(V4b, c.seta, 0);
+    if (i == 0) S1p = S1p + V1b;
+    l1 = l1 + S1p;
+    l2 = l2 + S1m;
+    l3 = l3 + S1z;
+  }
+  f1 = l1;
+  f2 = l2;
+  f3 = l3;
+}
+
+// glob_stiffness_quad_4 (SOLVER/stiffness_quad.f90:238-414)
+template <bool AX>
+__device__ __forceinline__ void stiff_quad(const LaneCoef &c, const float *blk, const float *m0, int lane,
+                                           int i, int j, float us, float up, float uz, float &f1, float &f2,
+                                           float &f3) {
+  const int j5 = 5 * j;
+  float X1 = dxi(us, cxi<AX>(c), j5), X2 = dxi(up, cxi<AX>(c), j5), X3 = dxi(uz, cxi<AX>(c), j5);
+  float X4 = deta(us, c.eta, i), X5 = deta(up, c.eta, i), X6 = deta(uz, c.eta, i);
+  const float m1 = ldm(blk, S_M1, lane), m2 = ldm(blk, S_M2, lane), m3 = ldm(blk, S_M3, lane),
+              m4 = ldm(blk, S_M4, lane), m5 = ldm(blk, S_M5, lane), m6 = ldm(blk, S_M6, lane),
+              m7 = ldm(blk, S_M7, lane), m8 = ldm(blk, S_M8, lane);
+  const float mw1 = ldm(blk, S_MW1, lane), mw2 = ldm(blk, S_MW2, lane), mw3 = ldm(blk, S_MW3, lane),
+              mw4 = ldm(blk, S_MW4, lane), mw5 = ldm(blk, S_MW5, lane);
+  const float m11s = ldm(blk, S_M11S, lane), m21s = ldm(blk, S_M21S, lane), m41s = ldm(blk, S_M41S, lane),
+              m12s = ldm(blk, S_M12S, lane), m22s = ldm(blk, S_M22S, lane), m32s = ldm(blk, S_M32S, lane),
+              m42s = ldm(blk, S_M42S, lane), m11z = ldm(blk, S_M11Z, lane), m21z = ldm(blk, S_M21Z, lane),
+              m41z = ldm(blk, S_M41Z, lane), m1p = ldm(blk, S_M1PHI, lane), m2p = ldm(blk, S_M2PHI, lane),
+              m4p = ldm(blk, S_M4PHI, lane);
+  const float c1 = m2 * X4, c2 = m1 * X1, c3 = m6 * X5, c4 = m5 * X2, c5 = m4 * X6, c6 = m3 * X3;
+  float ls = c1 + c2 + 2.f * (c3 + c4) + c5 + c6 + mw1 * us + mw2 * up + 2.f * mw3 * uz;
+  float lp = -2.f * (c1 + c2 + c5 + c6) - (c3 + c4) + mw2 * us + mw4 * up - mw3 * uz;
+  float lz = 2.f * (m8 * X5 + m7 * X2) + mw3 * (2.f * us - up) + mw5 * uz;
+  const float usm = us - 2.f * up, ups = 2.f * us - up;
+  const float S1s = m11s * X4 + m21s * X1 + m12s * X6 + m22s * X3 + m1 * usm;
+  const float S2s = m11s * X1 + m41s * X4 + m32s * X3 + m42s * X6 + m2 * usm;
+  const float S1z = m11z * X6 + m21z * X3 + m32s * X4 + m22s * X1 + m3 * usm;
+  const float S2z = m11z * X3 + m41z * X6 + m12s * X1 + m42s * X4 + m4 * usm;
+  const float S1p = m1p * X5 + m2p * X2 + m5 * ups + 2.f * m7 * uz;
+  const float S2p = m1p * X2 + m4p * X5 + m6 * ups + 2.f * m8 * uz;
+  X2 = deta(S2s, c.seta, i);
+  X4 = deta(S2p, c.seta, i);
+  X6 = deta(S2z, c.seta, i);
+  X1 = dxi(S1s, csxi<AX>(c), j5);
+  X3 = dxi(S1p, csxi<AX>(c), j5);
+  X5 = dxi(S1z, csxi<AX>(c), j5);
+  ls = ls + X1 + X2;
+  lp = lp + X3 + X4;
+  lz = lz + X5 + X6;
+  if (AX) {
+    const float w1 = m0[0 * 5 + j], w2 = m0[1 * 5 + j], w3 = m0[2 * 5 + j], w4 = m0[3 * 5 + j],
+                w5 = m0[4 * 5 + j], w6 = m0[5 * 5 + j];
+    const float V1 = dxi(us, c.g0, j5), V2 = dxi(up, c.g0, j5), V3 = dxi(uz, c.g0, j5);
+    ls = ls + c.g0i * (w1 * V1 + w2 * V2 + w3 * V3);
+    lp = lp + c.g0i * (w2 * V1 + w4 * V2 + w5 * V3);
+    lz = lz + c.g0i * (w3 * V1 + w5 * V2 + w6 * V3);
+  }
+  f1 = ls;
+  f2 = lp;
+  f3 = lz;
+}
+
+// glob_fluid_stiffness_4 (SOLVER/stiffness_fluid.f90:139-216)
+template <bool AX, bool NONMONO>
+__device__ __forceinline__ float stiff_fluid(const LaneCoef &c, const float *blk, const float *m0, int lane,
+                                             int i, int j, float chi) {
+  const int j5 = 5 * j;
+  float X1 = dxi(chi, cxi<AX>(c), j5);
+  float X2 = deta(chi, c.eta, i);
+  const float m1 = __ldcs(blk + 0 * 25 + lane), m2 = __ldcs(blk + 1 * 25 + lane),
+              m4 = __ldcs(blk + 2 * 25 + lane);
+  const float S1 = m1 * X2 + m2 * X1;
+  const float S2 = m1 * X1 + m4 * X2;
+  X1 = dxi(S1, csxi<AX>(c), j5);
+  X2 = deta(S2, c.seta, i);
+  float loc = X1 + X2;
+  if (NONMONO) {
+    loc = loc + __ldcs(blk + 3 * 25 + lane) * chi;
+    if (AX) {
+      const float V1 = dxi(chi, c.g0, j5);
+      loc = loc + c.g0i * (m0[j] * V1);
+    }
+  }
+  return loc;
+}
+
+// ------------------------------------------------------------ solid patch kernel
+
+template <int POLE, int MODE>
+__global__ void __launch_bounds__(kThreads) solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp) {
+  constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
+  constexpr int NT = n_terms(POLE), NA = n_axial(POLE);
+  constexpr int BS = block_stride(NT);
+  __shared__ float s_u[NC][kMaxPatchPoints];
+  __shared__ float s_f[NC][kMaxPatchPoints];
+  __shared__ uint32_t s_w[kMaxPatchPoints];
+  // component c of the shared arrays -> global component (mono: s, z)
+  auto gc = [](int c) { return (POLE == POLE_MONO && c == 1) ? 2 : c; };
+
+  if (MODE == MODE_NEWMARK && *st.blowup) return;
+  const PatchMeta m = d.meta[d.patch_begin + blockIdx.x];
+
+  // 1. gather (+ predictor)
+  for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
+    const uint32_t w = d.pts[m.pt_start + t];
+    const uint32_t g = w & kPtIndexMask;
+    s_w[t] = w;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      float u = st.u[gc(c)][g];
+      if (MODE == MODE_NEWMARK) u = predict(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2);
+      s_u[c][t] = u;
+      s_f[c][t] = 0.f;
+    }
+  }
+  __syncthreads();
+
+  // 2. elements
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool active = lane < 25;
+  const int i = lane % 5, j = active ? lane / 5 : 0;
+  LaneCoef coef;
+  load_coef(sp, i, j, coef);
+  int r0 = 0;
+  for (int r = 0; r < m.n_rounds; ++r) {
+    const int r1 = m.round_end[r];
+    for (int s = r0 + warp; s < r1; s += kWarps) {
+      const int64_t el = (int64_t)m.elem_start + s;
+      const int32_t info = __ldg(d.elinfo + el);
+      const int axslot = (info & 0xFFFFFF) - 1;
+      const float *blk = d.metric + el * BS;
+      const int idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
+      float u[3] = {0.f, 0.f, 0.f};
+      if (active) {
+        u[0] = s_u[0][idx];
+        if (POLE == POLE_MONO) {
+          u[2] = s_u[1][idx];
+        } else {
+          u[1] = s_u[1][idx];
+          u[2] = s_u[2][idx];
+        }
+      }
+      if (MODE == MODE_NEWMARK && lane == 6) {
+        // runtime_info guard on disp(1,1,:,:) (SOLVER/time_evol_wave.F90:1042)
+        const float mx = fmaxf(fabsf(u[0]), fmaxf(fabsf(u[1]), fabsf(u[2])));
+        if (!(mx <= st.thresh)) atomicCAS(st.blowup, 0, *st.iter);
+      }
+      const bool ax = axslot >= 0;
+      if (ax && i == 0) {  // apply_axis_mask_{one,two,three}comp on disp
+        if (POLE == POLE_MONO) u[0] = 0.f;
+        if (POLE == POLE_DI) { u[1] = 0.f; u[2] = 0.f; }
+        if (POLE == POLE_QUAD) { u[0] = 0.f; u[1] = 0.f; u[2] = 0.f; }
+      }
+      float f0, f1 = 0.f, f2;
+      const float *m0 = ax ? d.m0 + (int64_t)axslot * (NA * 5) : nullptr;
+      if (POLE == POLE_MONO) {
+        if (ax) stiff_mono<true>(coef, blk, m0, lane, i, j, u[0], u[2], f0, f2);
+        else stiff_mono<false>(coef, blk, m0, lane, i, j, u[0], u[2], f0, f2);
+      } else if (POLE == POLE_DI) {
+        if (ax) stiff_di<true>(coef, blk, m0, lane, i, j, u[0], u[1], u[2], f0, f1, f2);
+        else stiff_di<false>(coef, blk, m0, lane, i, j, u[0], u[1], u[2], f0, f1, f2);
+      } else {
+        if (ax) stiff_quad<true>(coef, blk, m0, lane, i, j, u[0], u[1], u[2], f0, f1, f2);
+        else stiff_quad<false>(coef, blk, m0, lane, i, j, u[0], u[1], u[2], f0, f1, f2);
+      }
+      if (ax && i == 0) {  // axis mask of acc1
+        if (POLE == POLE_MONO) f0 = 0.f;
+        if (POLE == POLE_DI) { f1 = 0.f; f2 = 0.f; }
+        if (POLE == POLE_QUAD) { f0 = 0.f; f1 = 0.f; f2 = 0.f; }
+      }
+      if (active) {
+        s_f[0][idx] += f0;
+        if (POLE == POLE_MONO) {
+          s_f[1][idx] += f2;
+        } else {
+          s_f[1][idx] += f1;
+          s_f[2][idx] += f2;
+        }
+      }
+    }
+    r0 = r1;
+    __syncthreads();
+  }
+
+  // 3. write-back
+  float stf1 = 0.f;
+  if (MODE == MODE_NEWMARK) stf1 = st.stf[*st.iter - 1];
+  for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
+    const uint32_t w = s_w[t];
+    const uint32_t g = w & kPtIndexMask;
+    float v[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      v[c] = s_f[c][t];
+      if (!(w & kPtFirst)) v[c] = st.f[gc(c)][g] + v[c];
+    }
+    if (MODE == MODE_FORCE || !(w & kPtLast)) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) st.f[gc(c)][g] = v[c];
+      continue;
+    }
+    // last writer: source, corrector, store the new state
+    if ((w & kPtSource) && stf1 != 0.f) {
+      for (int q = 0; q < st.src.n; ++q)
+        if ((uint32_t)st.src.gidx[q] == g) {
+#pragma unroll
+          for (int c = 0; c < NC; ++c) v[c] = v[c] - st.src.val[3 * q + gc(c)] * stf1;
+        }
+    }
+    const float im = st.inv_mass[g];
+    const float gam = st.gamma ? st.gamma[g] : 0.f;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const int cg = gc(c);
+      float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im) * v[c] : -im * v[c];
+      const float vel = st.v[cg][g];
+      const float dsp = s_u[c][t];
+      if (st.gamma) a = a - 2.f * gam * vel - gam * gam * dsp;
+      st.v[cg][g] = fmaf(st.hdt, st.a[cg][g] + a, vel);
+      st.a[cg][g] = a;
+      st.u[cg][g] = dsp;
+    }
+  }
+}
+
+// ------------------------------------------------------------ fluid patch kernel
+
+template <int NONMONO>
+__global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp) {
+  __shared__ float s_u[kMaxPatchPoints];
+  __shared__ float s_f[kMaxPatchPoints];
+  __shared__ uint32_t s_w[kMaxPatchPoints];
+  constexpr int BS = block_stride(NONMONO ? 4 : 3);
+  if (*st.blowup) return;
+  const PatchMeta m = d.meta[d.patch_begin + blockIdx.x];
+  for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
+    const uint32_t w = d.pts[m.pt_start + t];
+    const uint32_t g = w & kPtIndexMask;
+    s_w[t] = w;
+    s_u[t] = predict(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2);
+    s_f[t] = 0.f;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool active = lane < 25;
+  const int i = lane % 5, j = active ? lane / 5 : 0;
+  LaneCoef coef;
+  load_coef(sp, i, j, coef);
+  const float stf1 = st.stf[*st.iter - 1];
+  int r0 = 0;
+  for (int r = 0; r < m.n_rounds; ++r) {
+    const int r1 = m.round_end[r];
+    for (int s = r0 + warp; s < r1; s += kWarps) {
+      const int64_t el = (int64_t)m.elem_start + s;
+      const int32_t info = __ldg(d.elinfo + el);
+      const int axslot = (info & 0xFFFFFF) - 1;
+      const int srcslot = ((info >> 24) & 0xF) - 1;
+      const bool ax = axslot >= 0;
+      const float *blk = d.metric + el * BS;
+      const int idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
+      float chi = active ? s_u[idx] : 0.f;
+      if (NONMONO && ax && i == 0) chi = 0.f;  // apply_axis_mask_scal(chi)
+      const float *m0 = ax ? d.m0 + (int64_t)axslot * 5 : nullptr;
+      float f = ax ? stiff_fluid<true, NONMONO>(coef, blk, m0, lane, i, j, chi)
+                   : stiff_fluid<false, NONMONO>(coef, blk, m0, lane, i, j, chi);
+      if (srcslot >= 0 && stf1 != 0.f && active) f = f - d.srcfl[srcslot * 25 + lane] * stf1;
+      if (NONMONO && ax && i == 0) f = 0.f;
+      if (d.fsmask && active) f = f * d.fsmask[el * 25 + lane];
+      if (active) s_f[idx] += f;
+    }
+    r0 = r1;
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
+    const uint32_t w = s_w[t];
+    const uint32_t g = w & kPtIndexMask;
+    float v = s_f[t];
+    if (!(w & kPtFirst)) v = st.f[0][g] + v;
+    if (!(w & kPtLast)) {
+      st.f[0][g] = v;
+      continue;
+    }
+    float a = -st.inv_mass[g] * v;
+    const float dchi = st.v[0][g];
+    const float chi = s_u[t];
+    if (st.gamma) {
+      const float gam = st.gamma[g];
+      a = a - 2.f * gam * dchi - gam * gam * chi;
+    }
+    st.v[0][g] = fmaf(st.hdt, st.a[0][g] + a, dchi);
+    st.a[0][g] = a;
+    st.u[0][g] = chi;
+  }
+}
+
+// ------------------------------------------------------------ coupling pre-passes
+
+struct Coupling {
+  // per boundary point (of the receiving domain): CSR of contributions
+  const int32_t *pt_gidx;   // receiving global point
+  const int32_t *start;     // n+1
+  const int32_t *src_gidx;  // sending global point per contribution
+  const float *b1, *b2;     // bdry_matr(ipol, b, 1/2) per contribution
+  const float *mask;        // per contribution: 0 where the receiving copy is masked, else 1 (or fs mask)
+  int32_t n;
+};
+
+// bdry_copy2fluid (SOLVER/time_evol_wave.F90:1532-1571): fluid force starts
+// with -(b1 * u_s [+ u_phi] + b2 * u_z) of the predicted solid displacement
+template <int DIPOLE>
+__global__ void couple_to_fluid_kernel(Coupling cp, StateArgs solid, float *ffl) {
+  if (*solid.blowup) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= cp.n) return;
+  float acc = 0.f;
+  for (int k = cp.start[q]; k < cp.start[q + 1]; ++k) {
+    const int gs = cp.src_gidx[k];
+    const float us = predict(solid.u[0][gs], solid.v[0][gs], solid.a[0][gs], solid.dt, solid.hdt2);
+    const float uz = predict(solid.u[2][gs], solid.v[2][gs], solid.a[2][gs], solid.dt, solid.hdt2);
+    float x = us;
+    if (DIPOLE) x = us + predict(solid.u[1][gs], solid.v[1][gs], solid.a[1][gs], solid.dt, solid.hdt2);
+    acc = acc + cp.mask[k] * (-cp.b1[k] * x - cp.b2[k] * uz);
+  }
+  ffl[cp.pt_gidx[q]] = acc;
+}
+
+// bdry_copy2solid (SOLVER/time_evol_wave.F90:1577-1611): solid force starts
+// with b1 * ddchi (s [and phi] components) and b2 * ddchi (z) of the new
+// fluid acceleration; `mask` holds per contribution the axis mask bits.
+template <int POLE>
+__global__ void couple_to_solid_kernel(Coupling cp, StateArgs fluid, StateArgs solid) {
+  if (*solid.blowup) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= cp.n) return;
+  float fs = 0.f, fp = 0.f, fz = 0.f;
+  for (int k = cp.start[q]; k < cp.start[q + 1]; ++k) {
+    const float a = fluid.a[0][cp.src_gidx[k]];
+    const bool masked = cp.mask[k] == 0.f;  // solid copy sits at ipol=0 of an axial element
+    float ts = cp.b1[k] * a, tp = POLE == POLE_DI ? cp.b1[k] * a : 0.f, tz = cp.b2[k] * a;
+    if (masked) {
+      if (POLE == POLE_MONO) ts = 0.f;
+      if (POLE == POLE_DI) { tp = 0.f; tz = 0.f; }
+      if (POLE == POLE_QUAD) { ts = 0.f; tp = 0.f; tz = 0.f; }
+    }
+    fs = fs + ts;
+    fp = fp + tp;
+    fz = fz + tz;
+  }
+  const int g = cp.pt_gidx[q];
+  solid.f[0][g] = fs;
+  if (POLE != POLE_MONO) solid.f[1][g] = fp;
+  solid.f[2][g] = fz;
+}
+
+// ------------------------------------------------------------ receivers, step counter
+
+// nc_compute_recfile_seis_bare (SOLVER/seismograms.f90:783-820) every seis_it
+// steps into rec(nseismo, 3, num_rec); advances the step counter afterwards.
+__global__ void receivers_kernel(StateArgs solid, const int32_t *rec_gidx, int32_t num_rec, int32_t seis_it,
+                                 int32_t pole, float *rec, int32_t nseismo, int32_t *iter_ctr) {
+  const int32_t iter = *iter_ctr;
+  __syncthreads();
+  if (!*solid.blowup && seis_it > 0 && iter % seis_it == 0) {
+    const int32_t is = iter / seis_it;
+    if (is < nseismo) {
+      for (int r = threadIdx.x; r < num_rec; r += blockDim.x) {
+        const int g = rec_gidx[r];
+        const float us = solid.u[0][g], uz = solid.u[2][g];
+        const float up = pole == POLE_MONO ? 0.f : solid.u[1][g];
+        float v1 = us, v2 = up, v3 = uz;
+        if (pole == POLE_MONO) v2 = 0.f;
+        if (pole == POLE_DI) { v1 = us + up; v2 = us - up; }
+        const int64_t n = nseismo;
+        rec[is + n * (0 + 3 * (int64_t)r)] = v1;
+        rec[is + n * (1 + 3 * (int64_t)r)] = v2;
+        rec[is + n * (2 + 3 * (int64_t)r)] = v3;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *iter_ctr = iter + 1;
+}
+
+}  // namespace axg

@@ -1,0 +1,292 @@
+// axg_plan.cpp -- patch construction, patch colouring and sub-round split.
+// See axg_plan.h for what the kernels require of the plan.
+#include "axg_plan.h"
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+namespace axg {
+
+namespace {
+
+// point -> elements (CSR), elements listed in increasing order
+struct PointElems {
+  std::vector<int64_t> start;
+  std::vector<int32_t> elems;
+};
+
+PointElems point_elements(const int32_t *igloc, int64_t nel, int64_t nglob) {
+  PointElems pe;
+  pe.start.assign(nglob + 1, 0);
+  for (int64_t p = 0; p < 25 * nel; ++p) pe.start[igloc[p]]++;  // igloc is 1-based
+  for (int64_t g = 0; g < nglob; ++g) pe.start[g + 1] += pe.start[g];
+  pe.elems.resize(25 * nel);
+  std::vector<int64_t> fill(pe.start.begin(), pe.start.end() - 1);
+  for (int64_t e = 0; e < nel; ++e)
+    for (int k = 0; k < 25; ++k) {
+      const int64_t g = igloc[25 * e + k] - 1;
+      // an element lists a point once even if it appears twice (degenerate)
+      const int64_t s = pe.start[g];
+      bool dup = false;
+      for (int64_t q = s; q < fill[g]; ++q)
+        if (pe.elems[q] == e) dup = true;
+      if (!dup) pe.elems[fill[g]++] = (int32_t)e;
+    }
+  // compact duplicates (never happens on valid meshes)
+  for (int64_t g = 0; g < nglob; ++g)
+    for (int64_t q = fill[g]; q < pe.start[g + 1]; ++q) pe.elems[q] = -1;
+  return pe;
+}
+
+}  // namespace
+
+std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems,
+                       const std::vector<uint8_t> &prepass, DomainPlan &plan) {
+  plan = DomainPlan();
+  plan.nel = nel;
+  plan.nglob = nglob;
+  if (patch_elems < 1 || patch_elems > kMaxPatchElems) return "patch_elems out of range";
+  plan.patch_elems = patch_elems;
+  if (nel == 0) {
+    plan.colour_start.assign(1, 0);
+    return "";
+  }
+  if (nglob <= 0 || nglob > (int64_t)kPtIndexMask) return "nglob out of range";
+  for (int64_t p = 0; p < 25 * nel; ++p)
+    if (igloc[p] < 1 || igloc[p] > nglob) return "igloc entry outside 1..nglob";
+
+  const PointElems pe = point_elements(igloc, nel, nglob);
+
+  // ---- 1. patches: greedy compact growth ---------------------------------
+  plan.patch_of_elem.assign(nel, -1);
+  std::vector<int32_t> score(nel, 0);
+  std::vector<int32_t> cand;
+  std::vector<std::vector<int32_t>> patches;
+  int64_t next_seed = 0;
+  while (true) {
+    while (next_seed < nel && plan.patch_of_elem[next_seed] >= 0) ++next_seed;
+    if (next_seed >= nel) break;
+    const int32_t pid = (int32_t)patches.size();
+    std::vector<int32_t> members;
+    cand.clear();
+    int32_t add = (int32_t)next_seed;
+    while (true) {
+      plan.patch_of_elem[add] = pid;
+      members.push_back(add);
+      score[add] = 0;
+      if ((int)members.size() >= patch_elems) break;
+      for (int k = 0; k < 25; ++k) {
+        const int64_t g = igloc[25 * (int64_t)add + k] - 1;
+        for (int64_t q = pe.start[g]; q < pe.start[g + 1]; ++q) {
+          const int32_t e2 = pe.elems[q];
+          if (e2 < 0 || plan.patch_of_elem[e2] >= 0) continue;
+          if (score[e2] == 0) cand.push_back(e2);
+          score[e2]++;
+        }
+      }
+      int32_t best = -1;
+      for (int32_t c : cand) {
+        if (plan.patch_of_elem[c] >= 0) continue;
+        if (best < 0 || score[c] > score[best] || (score[c] == score[best] && c < best)) best = c;
+      }
+      if (best < 0) break;
+      add = best;
+    }
+    for (int32_t c : cand) score[c] = 0;
+    patches.push_back(std::move(members));
+  }
+  plan.n_patches = (int32_t)patches.size();
+
+  // ---- 2. colour the patches (greedy, creation order) --------------------
+  plan.colour_of_patch.assign(plan.n_patches, -1);
+  std::vector<int32_t> mark(64, -1);
+  int32_t ncol = 0;
+  for (int32_t p = 0; p < plan.n_patches; ++p) {
+    for (int32_t e : patches[p])
+      for (int k = 0; k < 25; ++k) {
+        const int64_t g = igloc[25 * (int64_t)e + k] - 1;
+        for (int64_t q = pe.start[g]; q < pe.start[g + 1]; ++q) {
+          const int32_t e2 = pe.elems[q];
+          if (e2 < 0) continue;
+          const int32_t p2 = plan.patch_of_elem[e2];
+          if (p2 == p) continue;
+          const int32_t c2 = plan.colour_of_patch[p2];
+          if (c2 >= 0) {
+            if (c2 >= (int32_t)mark.size()) mark.resize(c2 + 1, -1);
+            mark[c2] = p;
+          }
+        }
+      }
+    int32_t c = 0;
+    while (c < (int32_t)mark.size() && mark[c] == p) ++c;
+    if (c >= (int32_t)mark.size()) mark.resize(c + 1, -1);
+    plan.colour_of_patch[p] = c;
+    ncol = std::max(ncol, c + 1);
+  }
+  plan.n_colours = ncol;
+
+  // launch order of patches: by colour, then creation order
+  std::vector<int32_t> order(plan.n_patches);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+    return plan.colour_of_patch[a] < plan.colour_of_patch[b];
+  });
+  plan.colour_start.assign(ncol + 1, 0);
+  for (int32_t p = 0; p < plan.n_patches; ++p) plan.colour_start[plan.colour_of_patch[p] + 1]++;
+  for (int32_t c = 0; c < ncol; ++c) plan.colour_start[c + 1] += plan.colour_start[c];
+
+  // ---- 3. first / last writer per point ----------------------------------
+  // colour range of the patches touching each point
+  std::vector<int32_t> cmin(nglob, INT32_MAX), cmax(nglob, -1);
+  for (int64_t e = 0; e < nel; ++e) {
+    const int32_t c = plan.colour_of_patch[plan.patch_of_elem[e]];
+    for (int k = 0; k < 25; ++k) {
+      const int64_t g = igloc[25 * e + k] - 1;
+      cmin[g] = std::min(cmin[g], c);
+      cmax[g] = std::max(cmax[g], c);
+    }
+  }
+
+  // ---- 4. sub-rounds, points, element -> point indices --------------------
+  plan.meta.resize(plan.n_patches);
+  plan.elem_order.resize(nel);
+  plan.elem_pts.resize(25 * nel);
+  plan.pt_words.clear();
+  plan.pt_words.reserve((size_t)(nglob * 1.2) + 16);
+  int64_t eslot = 0;
+  std::vector<int32_t> round_of(kMaxPatchElems);
+  std::vector<uint32_t> pts;
+  std::vector<uint32_t> ptmask(nglob, 0);
+  for (int32_t lp = 0; lp < plan.n_patches; ++lp) {
+    const int32_t p = order[lp];
+    std::vector<int32_t> mem = patches[p];
+    std::sort(mem.begin(), mem.end());
+    const int n = (int)mem.size();
+    // greedy sub-rounds: element a gets the smallest round not used by an
+    // earlier element of the patch that shares a point with it
+    int nrounds = 0;
+    for (int a = 0; a < n; ++a) {
+      uint32_t used = 0;
+      for (int k = 0; k < 25; ++k) used |= ptmask[igloc[25 * (int64_t)mem[a] + k] - 1];
+      int r = 0;
+      while (used & (1u << r)) ++r;
+      if (r >= kMaxSubrounds) return "patch needs more sub-rounds than supported";
+      round_of[a] = r;
+      nrounds = std::max(nrounds, r + 1);
+      for (int k = 0; k < 25; ++k) ptmask[igloc[25 * (int64_t)mem[a] + k] - 1] |= 1u << r;
+    }
+    for (int a = 0; a < n; ++a)
+      for (int k = 0; k < 25; ++k) ptmask[igloc[25 * (int64_t)mem[a] + k] - 1] = 0;
+    std::vector<int> idx(n);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return round_of[x] < round_of[y]; });
+    PatchMeta &m = plan.meta[lp];
+    std::memset(&m, 0, sizeof m);
+    m.elem_start = (int32_t)eslot;
+    m.pt_start = (int32_t)plan.pt_words.size();
+    m.n_elems = (uint16_t)n;
+    m.n_rounds = (uint8_t)nrounds;
+    for (int r = 0; r < nrounds; ++r) {
+      int cnt = 0;
+      for (int a = 0; a < n; ++a) cnt += round_of[a] <= r;
+      m.round_end[r] = (uint8_t)cnt;
+    }
+    plan.max_rounds = std::max(plan.max_rounds, nrounds);
+    // unique points, sorted by global index
+    pts.clear();
+    for (int a = 0; a < n; ++a)
+      for (int k = 0; k < 25; ++k) pts.push_back((uint32_t)(igloc[25 * (int64_t)mem[a] + k] - 1));
+    std::sort(pts.begin(), pts.end());
+    pts.erase(std::unique(pts.begin(), pts.end()), pts.end());
+    if (pts.size() > (size_t)kMaxPatchPoints) return "patch has too many points";
+    m.n_pts = (uint16_t)pts.size();
+    plan.max_pts = std::max<int32_t>(plan.max_pts, (int32_t)pts.size());
+    const int32_t col = plan.colour_of_patch[p];
+    for (uint32_t g : pts) {
+      uint32_t w = g;
+      const bool pre = !prepass.empty() && prepass[g];
+      if (cmin[g] == col && !pre) w |= kPtFirst;
+      if (cmax[g] == col) w |= kPtLast;
+      plan.pt_words.push_back(w);
+    }
+    for (int t = 0; t < n; ++t) {
+      const int a = idx[t];
+      const int32_t e = mem[a];
+      plan.elem_order[eslot] = e;
+      for (int k = 0; k < 25; ++k) {
+        const uint32_t g = (uint32_t)(igloc[25 * (int64_t)e + k] - 1);
+        const auto it = std::lower_bound(pts.begin(), pts.end(), g);
+        plan.elem_pts[25 * eslot + k] = (uint16_t)(it - pts.begin());
+      }
+      ++eslot;
+    }
+  }
+  plan.total_pts = (int64_t)plan.pt_words.size();
+  return "";
+}
+
+std::string validate_plan(const int32_t *igloc, int64_t nel, int64_t nglob,
+                          const std::vector<uint8_t> &prepass, const DomainPlan &plan) {
+  if ((int64_t)plan.patch_of_elem.size() != nel) return "patch_of_elem size";
+  if (nel == 0) return "";
+  std::vector<int32_t> seen(nel, 0);
+  for (int64_t s = 0; s < nel; ++s) {
+    const int32_t e = plan.elem_order[s];
+    if (e < 0 || e >= nel) return "elem_order out of range";
+    if (seen[e]++) return "element appears twice in launch order";
+  }
+  // same-colour patches must not share a point; same-round elements neither
+  std::vector<int32_t> owner_patch(nglob, -1), owner_colour(nglob, -1);
+  std::vector<int32_t> nfirst(nglob, 0), nlast(nglob, 0), ntouch(nglob, 0);
+  for (int32_t c = 0; c < plan.n_colours; ++c) {
+    std::vector<int32_t> touched;
+    for (int32_t lp = plan.colour_start[c]; lp < plan.colour_start[c + 1]; ++lp) {
+      const PatchMeta &m = plan.meta[lp];
+      for (int t = 0; t < m.n_pts; ++t) {
+        const uint32_t w = plan.pt_words[m.pt_start + t];
+        const int64_t g = w & kPtIndexMask;
+        if (g >= nglob) return "point word index out of range";
+        if (owner_colour[g] == c && owner_patch[g] != lp) return "two patches of one colour share a point";
+        owner_colour[g] = c;
+        owner_patch[g] = lp;
+        ntouch[g]++;
+        if (w & kPtFirst) nfirst[g]++;
+        if (w & kPtLast) nlast[g]++;
+      }
+      int r0 = 0;
+      for (int r = 0; r < m.n_rounds; ++r) {
+        const int r1 = m.round_end[r];
+        std::vector<int64_t> gs;
+        for (int s = r0; s < r1; ++s) {
+          const int32_t e = plan.elem_order[m.elem_start + s];
+          std::vector<int64_t> ge;
+          for (int k = 0; k < 25; ++k) ge.push_back(igloc[25 * (int64_t)e + k] - 1);
+          std::sort(ge.begin(), ge.end());
+          ge.erase(std::unique(ge.begin(), ge.end()), ge.end());
+          gs.insert(gs.end(), ge.begin(), ge.end());
+          for (int k = 0; k < 25; ++k) {
+            const uint16_t li = plan.elem_pts[25 * (int64_t)(m.elem_start + s) + k];
+            if (li >= m.n_pts) return "element point index outside patch";
+            if ((int64_t)(plan.pt_words[m.pt_start + li] & kPtIndexMask) != igloc[25 * (int64_t)e + k] - 1)
+              return "element point index maps to the wrong global point";
+          }
+        }
+        std::sort(gs.begin(), gs.end());
+        if (std::adjacent_find(gs.begin(), gs.end()) != gs.end())
+          return "two elements of one sub-round share a point";
+        r0 = r1;
+      }
+      if (r0 != m.n_elems) return "sub-round counts do not cover the patch";
+    }
+  }
+  for (int64_t g = 0; g < nglob; ++g) {
+    if (ntouch[g] == 0) continue;
+    const bool pre = !prepass.empty() && prepass[g];
+    if (nlast[g] != 1) return "point without exactly one last writer";
+    if (nfirst[g] != (pre ? 0 : 1)) return "point first-writer count wrong";
+  }
+  return "";
+}
+
+}  // namespace axg

@@ -1,0 +1,77 @@
+// axg_plan.h -- host-side planning of the patch-coloured assembly.
+//
+// The reference assembles element contributions with a sequential
+// gather/scatter over igloc (SOLVER/commun.F90:99-158).  On the GPU every
+// CTA owns a *patch* of elements: it gathers the patch's global points into
+// shared memory once, accumulates its elements' contributions there in a
+// fixed order (elements are split into sub-rounds that share no point), and
+// writes the patch sums back.  Patches that share a point get different
+// colours and run in different launches, so the global write-back is
+// race-free without atomics, and the order in which a point's partial sums
+// are added (pre-pass, then colour 0, 1, ...) is fixed: results are
+// bit-reproducible run to run.
+//
+// The planner is plain C++ with no CUDA dependency so that it can be checked
+// on a machine without a GPU.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace axg {
+
+constexpr int kMaxPatchElems = 64;      // elements per patch (upper bound)
+constexpr int kMaxSubrounds = 12;       // conflict-free element groups per patch
+constexpr int kMaxPatchPoints = 25 * kMaxPatchElems;
+
+// bits of a patch point word: global index in the low 28 bits
+constexpr uint32_t kPtIndexMask = 0x0FFFFFFFu;
+constexpr uint32_t kPtFirst = 1u << 28;   // first writer: store, do not read partial sum
+constexpr uint32_t kPtLast = 1u << 29;    // last writer: the sum is final
+constexpr uint32_t kPtSource = 1u << 30;  // point carries a solid source term
+
+struct PatchMeta {            // 32 bytes, device layout
+  int32_t elem_start;         // first element (launch order)
+  int32_t pt_start;           // first point word
+  uint16_t n_elems;
+  uint16_t n_pts;
+  uint8_t n_rounds;
+  uint8_t round_end[19];      // cumulative element counts per sub-round (<= kMaxSubrounds used)
+};
+static_assert(sizeof(PatchMeta) == 32, "PatchMeta must be 32 bytes");
+
+struct DomainPlan {
+  int64_t nel = 0, nglob = 0;
+  int patch_elems = 0;
+  int32_t n_patches = 0;
+  int32_t n_colours = 0;
+  int32_t max_rounds = 0;
+  int32_t max_pts = 0;
+  std::vector<int32_t> patch_of_elem;    // nel (reference element order)
+  std::vector<int32_t> colour_of_patch;  // n_patches (creation order)
+  std::vector<int32_t> colour_start;     // n_colours+1 offsets into launch order of patches
+  std::vector<PatchMeta> meta;           // n_patches, launch order
+  std::vector<int32_t> elem_order;       // nel: reference element (0-based) at each launch slot
+  std::vector<uint32_t> pt_words;        // concatenated patch point words
+  std::vector<uint16_t> elem_pts;        // 25*nel, launch order: patch-local point index
+  int64_t total_pts = 0;
+};
+
+// Builds patches (compact greedy growth over the element adjacency graph),
+// colours them, splits each patch into sub-rounds and fills the point words.
+//   igloc     : 25*nel 1-based global indices (walk ipol fastest)
+//   prepass   : per global point, 1 if a pre-pass kernel writes it first
+//               (solid-fluid coupling), may be empty
+// Returns an empty string on success, else the reason.
+std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems,
+                       const std::vector<uint8_t> &prepass, DomainPlan &plan);
+
+// Checks the invariants the kernels rely on (used by the tests and by
+// axg_create in debug builds): every element in exactly one patch, no two
+// patches of one colour share a point, no two elements of one sub-round share
+// a point, first/last flags consistent.  Returns "" when valid.
+std::string validate_plan(const int32_t *igloc, int64_t nel, int64_t nglob,
+                          const std::vector<uint8_t> &prepass, const DomainPlan &plan);
+
+}  // namespace axg

@@ -1,0 +1,135 @@
+"""Host-side mirror of the reference's time-loop interface over the C-ABI.
+
+``Solver`` stands where ``time_loop`` (SOLVER/time_evol_wave.F90:231) is
+called from ``SOLVER/main.f90:92``: it is created from the module arrays the
+Fortran setup produced (here: a ``Mesh``), runs the Newmark loop on the GPU
+and returns the seismograms in the reference's ``(nseismo, 3, num_rec)``
+layout.  Errors are raised as ``AxgError`` carrying the library's status code
+and message (the reference stops through ``pcheck``, SOLVER/commun.F90:578).
+There is no CPU fallback: without the CUDA library or a GPU this raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from .mesh import Mesh
+
+
+class AxgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"axg error {code}: {msg}")
+        self.code = code
+
+
+def _check(lib, h, rc):
+    if rc != _abi.AXG_OK:
+        msg = lib.axg_last_error(h).decode()
+        raise AxgError(rc, msg)
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Solver:
+    """One solve on one GPU (one axg_handle)."""
+
+    def __init__(self, mesh: Mesh, lib=None):
+        self.lib = lib or _abi.load_library()
+        self.mesh = mesh
+        self._desc = mesh.desc()
+        h = C.c_void_p()
+        rc = self.lib.axg_create(C.byref(self._desc), C.byref(h))
+        _check(self.lib, None, rc)
+        self.h = h
+        self.nseismo = (mesh.niter // max(mesh.seis_it, 1)) + 1
+
+    # -- lifecycle --------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.axg_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- time loop ----------------------------------------------------------
+    def reset(self):
+        _check(self.lib, self.h, self.lib.axg_reset(self.h))
+
+    def run(self, first_iter: int = 1, n_iter: int | None = None):
+        if n_iter is None:
+            n_iter = self.mesh.niter - first_iter + 1
+        _check(self.lib, self.h, self.lib.axg_run(self.h, first_iter, n_iter))
+
+    def receivers(self) -> np.ndarray:
+        out = np.zeros((self.nseismo, 3, max(self.mesh.num_rec, 1)), dtype=np.float32, order="F")
+        n = C.c_int32()
+        _check(self.lib, self.h, self.lib.axg_get_receivers(self.h, _fp(out), self.nseismo, C.byref(n)))
+        return out[:, :, : self.mesh.num_rec]
+
+    def get_state(self, field: int) -> np.ndarray:
+        m = self.mesh
+        if field in (_abi.FIELD_DISP, _abi.FIELD_VELO, _abi.FIELD_ACC0):
+            out = np.zeros((5, 5, m.nel_solid, 3), dtype=np.float32, order="F")
+        else:
+            out = np.zeros((5, 5, m.nel_fluid), dtype=np.float32, order="F")
+        _check(self.lib, self.h, self.lib.axg_get_state(self.h, field, _fp(out)))
+        return out
+
+    def set_state(self, field: int, arr: np.ndarray):
+        a = np.asfortranarray(arr, dtype=np.float32)
+        _check(self.lib, self.h, self.lib.axg_set_state(self.h, field, _fp(a)))
+
+    # -- stiffness + assembly (micro-benchmark operation) ------------------
+    def stiffness_assembled(self, u_gvec: np.ndarray) -> np.ndarray:
+        u = np.asfortranarray(u_gvec, dtype=np.float32)
+        f = np.zeros_like(u, order="F")
+        _check(self.lib, self.h, self.lib.axg_stiffness_assembled(self.h, _fp(u), _fp(f)))
+        return f
+
+    def upload_disp(self, u_gvec: np.ndarray):
+        u = np.asfortranarray(u_gvec, dtype=np.float32)
+        _check(self.lib, self.h, self.lib.axg_upload_gvec_disp(self.h, _fp(u)))
+
+    def download_force(self) -> np.ndarray:
+        f = np.zeros((self.mesh.nglob_solid, 3), dtype=np.float32, order="F")
+        _check(self.lib, self.h, self.lib.axg_download_gvec_force(self.h, _fp(f)))
+        return f
+
+    def stiffness_device(self, stream: int | None = None):
+        _check(self.lib, self.h, self.lib.axg_stiffness_assembled_device(self.h, stream))
+
+    def time_stiffness(self, n: int) -> float:
+        ms = C.c_float()
+        _check(self.lib, self.h, self.lib.axg_time_stiffness(self.h, n, C.byref(ms)))
+        return ms.value
+
+    def set_tuning(self, patch_elems: int = 0, steps_per_graph: int = 0):
+        _check(self.lib, self.h, self.lib.axg_set_tuning(self.h, patch_elems, steps_per_graph))
+
+    def info(self) -> dict:
+        inf = _abi.Info()
+        _check(self.lib, self.h, self.lib.axg_get_info(self.h, C.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in _abi.Info._fields_}
+
+    def solid_colouring(self):
+        inf = self.info()
+        pe = np.zeros(self.mesh.nel_solid, dtype=np.int32)
+        cp = np.zeros(inf["n_patches_solid"], dtype=np.int32)
+        _check(self.lib, self.h, self.lib.axg_get_solid_colouring(
+            self.h, pe.ctypes.data_as(C.POINTER(C.c_int32)), cp.ctypes.data_as(C.POINTER(C.c_int32)),
+            len(cp)))
+        return pe, cp

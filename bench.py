@@ -1,0 +1,321 @@
+"""Benchmark of the stiffness + assembly step on one GB300.
+
+Workload (the synthetic stiffness/assembly micro-benchmark): a structured
+1024 x 1024 grid of npol = 4 solid elements (2^20 elements, 16 785 409 global
+points), 1 % axial elements, seeded bilinear geometry and materials,
+3-component FP32 displacement ~ N(0, 1e-6).  One step = one evaluation of the
+assembled quadrupole stiffness force
+    f = pdistsum_solid(axis_mask(glob_stiffness_quad_4(axis_mask(u))))
+over all elements (SOLVER/stiffness_quad.f90:238, SOLVER/commun.F90:69).
+The metric is GLL-point-steps/s: 25 * 2^20 element-local GLL points per step.
+
+  value : device-resident inputs, CUDA events on the library's stream;
+  e2e   : through the C-ABI call with host (pinned) buffers, the host->device
+          copy of u and the device->host copy of f inside every step.
+The inputs (2.8 GB of metric terms) are far larger than the 129 MB L2, so no
+L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun each rank runs an independent replica on its own GPU (the
+stiffness/assembly step has no exchange step on one mesh); rank 0 prints the
+JSON line with the whole-job throughput.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+POLES = {"mono": 0, "di": 1, "quad": 2}
+N_TERMS = {0: 15, 1: 24, 2: 26}
+N_AXIAL = {0: 3, 1: 9, 2: 6}
+N_COMP = {0: 2, 1: 3, 2: 3}
+METRIC = "GLL-point-steps/s (stiffness+assembly, 1 GB300)"
+
+
+def algorithmic_bytes(nel: int, nglob: int, nax: int, pole: int) -> int:
+    """Bytes one stiffness+assembly must move at least: every metric array and
+    the numbering read once (E (100 n_m + 100)), u read and f written once per
+    global point (G 8 n_c), axial vectors (A 20 n_a)."""
+    return nel * (100 * N_TERMS[pole] + 100) + nglob * 8 * N_COMP[pole] + nax * 20 * N_AXIAL[pole]
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.idx = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self) -> dict:
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("AXG_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample_mesh(pole: int, n: int):
+    from axisem_gb300.mesh import random_gvec, structured_mesh
+    m = structured_mesh(n, n, pole, terms="pole")
+    return m, random_gvec(m)
+
+
+def time_oracle(pole: int, seconds: float, threads: int, n: int = 96):
+    """Throughput of the FP32 oracle (the CPU restatement of the reference's
+    stiffness + pdistsum) on `threads` independent n x n element sub-meshes
+    run concurrently (ctypes releases the GIL), for about `seconds`."""
+    from oracle import oracle as orc
+    orc.build()
+    meshes = [cpu_sample_mesh(pole, n) for _ in range(threads)]
+    counts = [0] * threads
+    stop = time.perf_counter() + seconds
+
+    def work(k):
+        m, u = meshes[k]
+        while time.perf_counter() < stop or counts[k] == 0:
+            orc.stiffness_assembled(m, u, np.float32)
+            counts[k] += 1
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    dt = time.perf_counter() - t0
+    pts = sum(c * meshes[0][0].nel_solid * 25 for c in counts)
+    return pts / dt, f"{threads} x {n}x{n} elements, {sum(counts)} steps in {dt:.1f} s"
+
+
+def run_reference(args):
+    ws, rank, _ = dist_init()
+    if rank != 0:
+        return
+    pole = POLES[args.pole]
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        time_oracle(pole, 0.5, threads)
+    for _ in range(args.steps):
+        v, sample = time_oracle(pole, args.ref_seconds, threads)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GLL-point-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"stiffness+assembly, {args.pole}pole, structured grid (oracle sample)",
+                       "pole": args.pole},
+            "cpu_baseline": {"value": value, "unit": "GLL-point-steps/s", "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "GLL-point-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    ws, rank, local = dist_init()
+    import torch
+    torch.cuda.set_device(local)
+    import axisem_gb300.build as b
+    b.build()
+    from axisem_gb300.mesh import random_gvec, structured_mesh
+    from axisem_gb300.solver import Solver
+
+    pole = POLES[args.pole]
+    n = args.size
+    t0 = time.perf_counter()
+    mesh = structured_mesh(n, n, pole, terms="pole", seed=20261203 + rank)
+    u = random_gvec(mesh, seed=20261204 + rank)
+    t_mesh = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    s = Solver(mesh)
+    t_create = time.perf_counter() - t0
+    info = s.info()
+    s.upload_disp(u)
+    for _ in range(max(args.warmup, 3)):
+        s.stiffness_device()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing (CUDA events on the library's stream)
+    with ClockSampler(local) as clk:
+        barrier(ws)
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        ms = s.time_stiffness(args.steps)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+        barrier(ws)
+    clocks = clk.summary()
+    ms = max_over_ranks(ms, ws)
+    pts_step = mesh.nel_solid * 25
+    value = ws * pts_step / (ms * 1e-3)
+
+    # ---- end-to-end through the C-ABI with pinned host buffers
+    ng = mesh.nglob_solid
+    hu = torch.empty((3, ng), dtype=torch.float32, pin_memory=True).numpy()
+    hu[:] = u.T
+    hf = torch.empty((3, ng), dtype=torch.float32, pin_memory=True).numpy()
+    ufort = hu.T  # (ng, 3) column-major view of the pinned buffer
+    import ctypes as C
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    for _ in range(2):
+        s.lib.axg_stiffness_assembled(s.h, fp(hu), fp(hf))
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc = s.lib.axg_stiffness_assembled(s.h, fp(hu), fp(hf))
+        assert rc == 0, s.lib.axg_last_error(s.h)
+    torch.cuda.synchronize()
+    e_s = max_over_ranks((time.perf_counter() - e0) / args.steps, ws)
+    e2e = ws * pts_step / e_s
+    assert np.isfinite(hf).all() and ufort.shape == (ng, 3)
+
+    # ---- roofline of the stiffness+assembly kernels (all colour launches of one step)
+    nbytes = algorithmic_bytes(mesh.nel_solid, ng, len(mesh.ax_el_solid), pole)
+    peak, peak_kind = measured_peaks()
+    achieved = nbytes / (ms * 1e-3) / 1e9
+    prof = ROOT / "profiles" / f"stiffness_assembly_{args.pole}_{n}x{n}.traffic.json"
+    traffic = None
+    if prof.exists():
+        traffic = json.loads(prof.read_text()).get("dram_bytes_per_step")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, sample = time_oracle(pole, args.cpu_seconds, 1)
+        cpu = {"value": v, "unit": "GLL-point-steps/s", "cores": 1, "kind": "port", "sample": sample}
+
+    s.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "GLL-point-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"stiffness+assembly, {args.pole}pole, {n}x{n} structured quads "
+                               f"({mesh.nel_solid} elements, {ng} global points, 1% axial)",
+                   "pole": args.pole, "elements": mesh.nel_solid, "global_points": ng,
+                   "parallelism": f"replicas x{ws}",
+                   "l2": "inputs (metric terms) 20x larger than L2; no flush needed"},
+        "e2e": {"value": e2e, "unit": "GLL-point-steps/s", "h2d_bytes_per_step": int(ng * 12),
+                "d2h_bytes_per_step": int(ng * 12)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_step": nbytes,
+                     "kernel": "solid_patch_kernel<quad,force> (all colour launches of one step)"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": int(args.steps * info["kernels_per_force"]),
+        "plan": {"patches": info["n_patches_solid"], "colours": info["n_colours_solid"],
+                 "patch_points_over_global": info["patch_points_solid"] / ng,
+                 "device_gb": info["device_bytes"] / 1e9},
+        "setup_s": {"mesh": round(t_mesh, 2), "create": round(t_create, 2)},
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--pole", default="quad", choices=list(POLES))
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,260 @@
+/*
+ * axisem_gb300.h -- C-ABI of the GB300 (sm_103a) AxiSEM solver time loop.
+ *
+ * The library replaces the body of the reference's `time_loop`
+ * (SOLVER/time_evol_wave.F90:231-245, Newmark path `sf_time_loop_newmark`
+ * SOLVER/time_evol_wave.F90:264-502) and, for the stiffness/assembly
+ * micro-benchmark, the pair `glob_stiffness_{mono,di,quad}_4` +
+ * `pdistsum_solid` (SOLVER/stiffness_*.f90, SOLVER/commun.F90:69-171).
+ *
+ * Everything the Fortran host computes before the loop (mesh database,
+ * precomputed metric terms, source, receivers, attenuation constants) is
+ * handed over through `axg_mesh_desc` as plain pointers to the module
+ * arrays, in the reference's own Fortran column-major layouts and
+ * `realkind = 4` (float) precision.  The library copies what it needs to
+ * HBM in `axg_create`; the caller keeps ownership of every host array.
+ *
+ * All entry points return an `int` status (AXG_OK == 0); none of them
+ * calls exit()/abort().  A handle is single-caller: calls on one handle
+ * must not overlap.  Every function is `extern "C"`, takes plain pointers
+ * and sizes, and can be bound from Fortran with `bind(c)` interfaces
+ * (the binding is shown in INTEGRATION.md).
+ */
+#ifndef AXISEM_GB300_H
+#define AXISEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AXG_ABI_VERSION 1
+#define AXG_NPOL 4   /* only npol = 4 (5x5 GLL points) is supported, as the *_4 kernels */
+
+/* ---- status codes ---------------------------------------------------- */
+enum axg_status {
+  AXG_OK = 0,
+  AXG_ERR_BAD_DESC = 1,      /* inconsistent sizes, null required array, bad index */
+  AXG_ERR_OOM = 2,           /* device allocation failed */
+  AXG_ERR_CUDA = 3,          /* any other CUDA runtime error */
+  AXG_ERR_BLOWUP = 4,        /* |disp(1,1,:,:)| > 10 |magnitude| (runtime_info) */
+  AXG_ERR_TIMEOUT = 5,       /* a bounded device wait ran out */
+  AXG_ERR_NO_DEVICE = 6,     /* no CUDA device / extension cannot run here */
+  AXG_ERR_BAD_ARG = 7,       /* bad argument to a call other than axg_create */
+  AXG_ERR_UNSUPPORTED = 8    /* valid input the library does not implement */
+};
+
+/* src_type(1) of the reference (SOLVER/data_source.f90; mapping in
+ * SOLVER/source.f90:63-80). */
+enum axg_pole { AXG_MONOPOLE = 0, AXG_DIPOLE = 1, AXG_QUADPOLE = 2 };
+
+/* Solid metric arrays of module data_matr (SOLVER/data_matr.f90:45-76),
+ * each real(0:4,0:4,nel_solid).  Which ones a pole type reads:
+ *   monopole  : M_1..M_4, M_w1, M11s M21s M41s M12s M22s M32s M42s M11z M21z M41z (15)
+ *   dipole    : + M_5..M_8, M_w2, M_w3, M13s, M33s, M43s                         (24)
+ *   quadrupole: + M_5..M_8, M_w2..M_w5, M1phi, M2phi, M4phi                      (26)
+ * Arrays a pole does not read may be NULL. */
+enum axg_solid_term {
+  AXG_M_1 = 0, AXG_M_2, AXG_M_3, AXG_M_4, AXG_M_5, AXG_M_6, AXG_M_7, AXG_M_8,
+  AXG_M_W1, AXG_M_W2, AXG_M_W3, AXG_M_W4, AXG_M_W5,
+  AXG_M11S, AXG_M21S, AXG_M41S, AXG_M12S, AXG_M22S, AXG_M32S, AXG_M42S,
+  AXG_M11Z, AXG_M21Z, AXG_M41Z,
+  AXG_M13S, AXG_M33S, AXG_M43S,
+  AXG_M1PHI, AXG_M2PHI, AXG_M4PHI,
+  AXG_N_SOLID_TERMS
+};
+
+/* Axial vectors M0_w1..M0_w10, each real(0:4,nel_solid) (SOLVER/data_matr.f90:78-83).
+ * monopole reads w1..w3, dipole w1..w4,w6..w10, quadrupole w1..w6. */
+enum axg_axial_term {
+  AXG_M0_W1 = 0, AXG_M0_W2, AXG_M0_W3, AXG_M0_W4, AXG_M0_W5,
+  AXG_M0_W6, AXG_M0_W7, AXG_M0_W8, AXG_M0_W9, AXG_M0_W10,
+  AXG_N_AXIAL_TERMS
+};
+
+/* Fluid metric arrays (SOLVER/data_matr.f90:86-89), real(0:4,0:4,nel_fluid);
+ * M_w_fl only for dipole/quadrupole. */
+enum axg_fluid_term { AXG_M1CHI = 0, AXG_M2CHI, AXG_M4CHI, AXG_M_W_FL, AXG_N_FLUID_TERMS };
+
+/* Everything the time loop reads.  Field names are the reference's; all
+ * element/point indices are the reference's 1-based values. */
+typedef struct axg_mesh_desc {
+  int32_t abi_version;       /* = AXG_ABI_VERSION */
+  int32_t npol;              /* = 4 */
+  int32_t src_type;          /* enum axg_pole: src_type(1) */
+  int32_t fluid_src;         /* source sits in the fluid (add_source_fl) */
+
+  int32_t nel_solid, nel_fluid;
+  int32_t nglob_solid, nglob_fluid;
+  int32_t naxel_solid, naxel_fluid;
+  int32_t nel_bdry;
+  int32_t nelsrc;            /* <= 8 */
+
+  int32_t niter;             /* length of stf */
+  int32_t seis_it;           /* receiver sampling every seis_it steps */
+  int32_t num_rec;
+  int32_t have_absorbing_bc;
+
+  double deltat;             /* data_time: deltat (FP64) */
+  double magnitude;          /* blow-up threshold = 10*|magnitude| */
+
+  /* numbering (SOLVER/data_mesh.f90:57-58): igloc(25*nel), walk ipol fastest */
+  const int32_t *igloc_solid, *igloc_fluid;
+  const int32_t *ax_el_solid, *ax_el_fluid;      /* (naxel_*) element numbers */
+
+  /* spectral matrices (SOLVER/data_spec.f90) */
+  const float *G0;                               /* (0:4) */
+  const float *G1, *G1T, *G2, *G2T;              /* (0:4,0:4) */
+
+  const float *m_solid[AXG_N_SOLID_TERMS];
+  const float *m0_solid[AXG_N_AXIAL_TERMS];
+  const float *m_fluid[AXG_N_FLUID_TERMS];
+  const float *m0_w_fl;                          /* (0:4,nel_fluid), non-monopole */
+
+  const float *inv_mass_rho;                     /* (0:4,0:4,nel_solid) */
+  const float *inv_mass_fluid;                   /* (0:4,0:4,nel_fluid) */
+  const float *fluid_free_surface_mask;          /* (0:4,0:4,nel_fluid) or NULL (= 1) */
+  const float *solid_absorbing_gamma;            /* (0:4,0:4,nel_solid), if have_absorbing_bc */
+  const float *fluid_absorbing_gamma;            /* (0:4,0:4,nel_fluid), if have_absorbing_bc */
+
+  /* solid-fluid boundary (SOLVER/data_mesh.f90:106-110, data_matr bdry_matr) */
+  const float *bdry_matr;                        /* (0:4,nel_bdry,2) */
+  const int32_t *bdry_solid_el, *bdry_fluid_el;  /* (nel_bdry) */
+  const int32_t *bdry_jpol_solid, *bdry_jpol_fluid;
+
+  /* source (SOLVER/data_source.f90): ielsrc(8), source_term_el(0:4,0:4,8,3)
+   * or source_term_fl(0:4,0:4,8), stf(niter) */
+  const int32_t *ielsrc;
+  const float *source_term_el;
+  const float *source_term_fl;
+  const float *stf;
+
+  /* receivers: recfile_el(num_rec,3) = (element, ipol, jpol), column-major */
+  const int32_t *recfile_el;
+
+  /* coarse-grained (cg4) attenuation (SOLVER/attenuation.f90:81-202) */
+  int32_t anel_true;
+  int32_t n_sls;                                 /* n_sls_attenuation */
+  int32_t do_corr_lowq;
+  int32_t att_coarse_grained;                    /* must be 1 when anel_true */
+  const double *y_j_attenuation;                 /* (n_sls) */
+  const double *exp_w_j_deltat;                  /* (n_sls) */
+  const double *ts_fac_t, *ts_fac_tm1;           /* (n_sls) */
+  const float *Q_mu, *Q_kappa;                   /* (nel_solid) */
+  const float *delta_mu_cg4, *delta_kappa_cg4;   /* (1:4,nel_solid) */
+  const float *Y_cg4, *V_s_eta_cg4, *V_s_xi_cg4, *V_z_eta_cg4, *V_z_xi_cg4;  /* (1:4,nel_solid) */
+  const float *DsDeta_over_J_sol_cg4, *DzDeta_over_J_sol_cg4;
+  const float *DsDxi_over_J_sol_cg4, *DzDxi_over_J_sol_cg4;                  /* (1:4,nel_solid) */
+  const float *inv_s_solid;                      /* (0:4,0:4,nel_solid) */
+} axg_mesh_desc;
+
+typedef struct axg_handle axg_handle;
+
+/* State arrays for axg_get_state / axg_set_state, returned in the reference's
+ * element-local layouts disp(0:4,0:4,nel_solid,3), chi(0:4,0:4,nel_fluid),
+ * memory_var_cg4(1:4,6,n_sls,nel_solid). */
+enum axg_field {
+  AXG_FIELD_DISP = 0, AXG_FIELD_VELO, AXG_FIELD_ACC0,
+  AXG_FIELD_CHI, AXG_FIELD_DCHI, AXG_FIELD_DDCHI0,
+  AXG_FIELD_MEMVAR
+};
+
+/* Library build/version string; never NULL. */
+const char *axg_version(void);
+
+/* Number of CUDA devices visible (0 when none); never fails. */
+int axg_device_count(void);
+
+/* Copies the mesh, metric terms, source and receiver tables to HBM and builds
+ * the element patches, the patch colouring and the point renumbering.
+ * Replaces the data hand-over before SOLVER/time_evol_wave.F90:264 (the
+ * Fortran module arrays of data_matr / data_mesh / data_source).
+ * `*out` is set to a handle (or NULL on failure, with the reason in
+ * axg_last_error(NULL)). */
+int axg_create(const axg_mesh_desc *desc, axg_handle **out);
+
+/* Zeroes the wavefields, memory variables and seismogram buffer and records
+ * the iter-0 seismogram sample (SOLVER/time_evol_wave.F90:310-344). */
+int axg_reset(axg_handle *h);
+
+/* Advances n_iter Newmark steps, iterations first_iter .. first_iter+n_iter-1
+ * (1-based, as `iter` in SOLVER/time_evol_wave.F90:353), using stf(iter).
+ * Steps are launched in CUDA graphs of `steps_per_graph` (axg_set_tuning).
+ * Returns AXG_ERR_BLOWUP when the blow-up guard of runtime_info
+ * (SOLVER/time_evol_wave.F90:1042) fired; the flag is polled once per graph. */
+int axg_run(axg_handle *h, int32_t first_iter, int32_t n_iter);
+
+/* Seismograms so far, in the NetCDF layout recdumpvar(nseismo,3,num_rec)
+ * (SOLVER/nc_routines.F90:531-538), column-major; `nseismo_cap` is the first
+ * extent of `out`; components as nc_compute_recfile_seis_bare
+ * (SOLVER/seismograms.f90:783-820).  *nseismo_out = samples written. */
+int axg_get_receivers(axg_handle *h, float *out, int32_t nseismo_cap, int32_t *nseismo_out);
+
+/* Copies a state field to the host in the reference's element-local layout. */
+int axg_get_state(axg_handle *h, int32_t field, float *out);
+
+/* Sets a state field from the reference's element-local layout (the value of
+ * each global point is taken from its first element-local copy). */
+int axg_set_state(axg_handle *h, int32_t field, const float *in);
+
+/* Stiffness + assembly, the config-2 micro-benchmark operation:
+ * u is gvec-layout displacement (nglob_solid,3) column-major in the
+ * reference's global numbering (igloc), f receives the assembled
+ *   f = pdistsum_solid( axis_mask( glob_stiffness_<pole>(u) ) )
+ * in the same layout (SOLVER/stiffness_*_4, SOLVER/apply_masks.f90,
+ * SOLVER/commun.F90:69-171).  Host pointers; copies are included. */
+int axg_stiffness_assembled(axg_handle *h, const float *u_gvec, float *f_gvec);
+
+/* The same operation on device-resident buffers of the handle: reads the
+ * handle's displacement field and writes the handle's force buffer; used to
+ * time the kernels alone.  `stream` may be NULL (the handle's stream). */
+int axg_stiffness_assembled_device(axg_handle *h, void *stream);
+
+/* Uploads a gvec-layout displacement (nglob_solid,3) into the handle's
+ * displacement field / downloads the handle's force buffer as gvec layout. */
+int axg_upload_gvec_disp(axg_handle *h, const float *u_gvec);
+int axg_download_gvec_force(axg_handle *h, float *f_gvec);
+
+/* Tuning knobs: elements per patch (<= 64), steps per CUDA graph. 0 = keep. */
+int axg_set_tuning(axg_handle *h, int32_t patch_elems, int32_t steps_per_graph);
+
+/* Introspection for tests and the benchmark. */
+typedef struct axg_info {
+  int64_t n_patches_solid, n_patches_fluid;
+  int32_t n_colours_solid, n_colours_fluid;
+  int32_t max_subrounds_solid, max_subrounds_fluid;
+  int64_t device_bytes;               /* bytes the handle holds in HBM */
+  int64_t kernels_per_step;           /* kernel launches in one Newmark step */
+  int64_t kernels_per_force;          /* kernel launches in one stiffness+assembly */
+  int64_t patch_points_solid;         /* sum over patches of their point counts */
+} axg_info;
+int axg_get_info(axg_handle *h, axg_info *info);
+
+/* Per-element patch colour of the solid elements (1-based reference order);
+ * for validation of the atomic-free colouring. */
+int axg_get_solid_colouring(axg_handle *h, int32_t *patch_of_elem, int32_t *colour_of_patch,
+                            int64_t n_patch_cap);
+
+/* Plans the patch colouring of the solid (and fluid) domain on the host only
+ * -- no GPU is touched -- and checks every invariant the kernels rely on:
+ * each element in one patch, no two patches of one colour sharing a global
+ * point, no two elements of one sub-round sharing a point, exactly one first
+ * and one last writer per point.  `info` receives the plan sizes
+ * (device_bytes = 0).  Returns AXG_ERR_BAD_DESC with the violated invariant. */
+int axg_plan_check(const axg_mesh_desc *desc, int32_t patch_elems, axg_info *info);
+
+/* Event-timed repeat of axg_stiffness_assembled_device: n launches, returns the
+ * average device time in ms of one stiffness+assembly (all colour launches). */
+int axg_time_stiffness(axg_handle *h, int32_t n, float *ms_avg);
+
+void axg_destroy(axg_handle *h);
+
+/* Message of the last error on `h` (or of the last failed axg_create when h is
+ * NULL); never NULL. */
+const char *axg_last_error(axg_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AXISEM_GB300_H */

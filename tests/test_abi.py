@@ -1,0 +1,133 @@
+"""The C-ABI library on a machine without a GPU: it loads, exports every entry
+point include/axisem_gb300.h declares, validates descriptors the way the
+reference's setup stops on bad input, and its host-side planner (patches,
+colours, sub-rounds) satisfies the invariants the atomic-free assembly needs."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from axisem_gb300 import _abi
+from axisem_gb300.mesh import coupled_mesh, structured_mesh
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "axisem_gb300.h"
+
+
+def declared_functions():
+    txt = HEADER.read_text()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(axg_[a-z_]+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _abi.SIGNATURES, f"{n} missing from the Python mirror"
+
+
+def test_header_struct_matches_mirror():
+    # every field of axg_mesh_desc appears in the ctypes mirror, in order
+    txt = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    body = txt[txt.index("typedef struct axg_mesh_desc {"):txt.index("} axg_mesh_desc;")]
+    fields = []
+    for decl in body.split(";")[:-1]:
+        decl = decl.split("{")[-1]
+        for part in decl.split(","):
+            nm = re.findall(r"\**\s*([A-Za-z_][A-Za-z0-9_]*)\s*(\[[^\]]*\])?\s*$", part.strip())
+            if nm:
+                fields.append(nm[0][0])
+    mirror = [f for f, _ in _abi.MeshDesc._fields_]
+    assert fields == mirror
+
+
+def test_version_and_device_count(lib):
+    assert b"sm_103a" in lib.axg_version()
+    assert lib.axg_device_count() >= 0
+
+
+def _create(lib, desc):
+    h = C.c_void_p()
+    rc = lib.axg_create(C.byref(desc), C.byref(h))
+    return rc, lib.axg_last_error(None).decode(), h
+
+
+@pytest.mark.parametrize("mutate,code,needle", [
+    (lambda d: setattr(d, "npol", 3), _abi.AXG_ERR_BAD_DESC, "npol"),
+    (lambda d: setattr(d, "abi_version", 99), _abi.AXG_ERR_BAD_DESC, "abi_version"),
+    (lambda d: setattr(d, "src_type", 5), _abi.AXG_ERR_BAD_DESC, "src_type"),
+    (lambda d: setattr(d, "nelsrc", 9), _abi.AXG_ERR_BAD_DESC, "nelsrc"),
+    (lambda d: setattr(d, "seis_it", 0), _abi.AXG_ERR_BAD_DESC, "seis_it"),
+    (lambda d: setattr(d, "anel_true", 1), _abi.AXG_ERR_UNSUPPORTED, "attenuation"),
+])
+def test_descriptor_validation(lib, mutate, code, needle):
+    m = coupled_mesh(6, 3, 2, 1, niter=10)
+    d = m.desc()
+    mutate(d)
+    rc, msg, h = _create(lib, d)
+    assert rc == code and needle in msg
+    assert not h.value
+
+
+def test_null_metric_array_rejected(lib):
+    m = structured_mesh(4, 4, 2)
+    d = m.desc()
+    d.m_solid[_abi.SOLID_TERMS.index("M1phi")] = C.cast(None, C.POINTER(C.c_float))
+    rc, msg, _ = _create(lib, d)
+    assert rc == _abi.AXG_ERR_BAD_DESC and "NULL" in msg
+
+
+def test_out_of_range_indices_rejected(lib):
+    m = coupled_mesh(6, 3, 2, 0, niter=10)
+    m.recfile_el = m.recfile_el.copy(order="F")
+    m.recfile_el[0, 1] = 7
+    rc, msg, _ = _create(lib, m.desc())
+    assert rc == _abi.AXG_ERR_BAD_DESC and "recfile_el" in msg
+    m = structured_mesh(4, 4, 0)
+    m.igloc_solid = m.igloc_solid.copy()
+    m.igloc_solid[3] = m.nglob_solid + 1
+    inf = _abi.Info()
+    rc = lib.axg_plan_check(C.byref(m.desc()), 64, C.byref(inf))
+    assert rc == _abi.AXG_ERR_BAD_DESC
+
+
+def test_create_without_gpu_reports_no_device(lib):
+    if lib.axg_device_count() > 0:
+        pytest.skip("a GPU is present")
+    rc, msg, h = _create(lib, structured_mesh(4, 4, 0).desc())
+    assert rc == _abi.AXG_ERR_NO_DEVICE and not h.value
+
+
+@pytest.mark.parametrize("ni,nj,pe", [(64, 48, 64), (33, 17, 64), (20, 20, 16), (7, 3, 5), (1, 1, 64)])
+def test_plan_invariants(lib, ni, nj, pe):
+    m = structured_mesh(ni, nj, 2, axial="random1pct")
+    inf = _abi.Info()
+    rc = lib.axg_plan_check(C.byref(m.desc()), pe, C.byref(inf))
+    assert rc == 0, lib.axg_last_error(None)
+    assert inf.n_colours_solid >= 1 and inf.max_subrounds_solid <= 12
+    assert inf.patch_points_solid >= m.nglob_solid
+
+
+def test_plan_on_permuted_numbering(lib):
+    """Unstructured numbering: a random permutation of global ids and of the
+    element order must still give a valid plan."""
+    rng = np.random.default_rng(0)
+    m = structured_mesh(24, 18, 1)
+    perm = rng.permutation(m.nglob_solid) + 1
+    ig = perm[m.igloc_solid - 1].astype(np.int32)
+    eperm = rng.permutation(m.nel_solid)
+    m.igloc_solid = ig.reshape(m.nel_solid, 25)[eperm].reshape(-1).copy()
+    inf = _abi.Info()
+    rc = lib.axg_plan_check(C.byref(m.desc()), 64, C.byref(inf))
+    assert rc == 0, lib.axg_last_error(None)
+
+
+def test_plan_coupled(lib):
+    m = coupled_mesh(40, 12, 9, 2)
+    inf = _abi.Info()
+    rc = lib.axg_plan_check(C.byref(m.desc()), 64, C.byref(inf))
+    assert rc == 0, lib.axg_last_error(None)
+    assert inf.n_patches_fluid > 0
