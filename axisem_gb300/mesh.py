@@ -329,7 +329,8 @@ def gauss_stf(niter: int, deltat: float, period: float) -> np.ndarray:
 def coupled_mesh(ni: int, nj_solid: int, nj_fluid: int, src_type: int = _abi.MONOPOLE, *,
                  niter: int = 60, seed: int = 7, axial_column: bool = True, fluid_src: bool = False,
                  num_rec: int = 6, seis_it: int = 2, deltat: float = 2e-6,
-                 free_surface: bool = False, absorbing: bool = False) -> Mesh:
+                 free_surface: bool = False, absorbing: bool = False,
+                 bdry_scale: float = 1.0) -> Mesh:
     """A solid layer on top of a fluid layer, both ni elements wide, with
     the solid-fluid boundary along the fluid's top edge (jpol = 4) and the
     solid's bottom edge (jpol = 0); the I = 0 column lies on the axis.  A
@@ -346,10 +347,11 @@ def coupled_mesh(ni: int, nj_solid: int, nj_fluid: int, src_type: int = _abi.MON
         m.nel_fluid, m.nglob_fluid, m.igloc_fluid = nelf, ngf, igf
         m.ax_el_fluid = (np.arange(nj_fluid) * ni + 1).astype(I32) if axial_column else np.zeros(0, I32)
         wt2 = np.outer(m.spec.wt, m.spec.wt)
-        sc = 1e-10 * wt2[:, :, None]
+        # K / M ~ (v / h)^2 ~ 1e8 as in the solid (metric ~1e11, inverse mass ~1e-3)
+        sc = 1e-2 * wt2[:, :, None]
         for name in FLUID_TERMS:
             m.m_fluid[name] = _f(sc * rng.uniform(-1.0, 1.0, size=(5, 5, nelf)))
-        m.m0_w_fl = _f(1e-10 * rng.uniform(-1.0, 1.0, size=(5, nelf)))
+        m.m0_w_fl = _f(1e-2 * rng.uniform(-1.0, 1.0, size=(5, nelf)))
         m.inv_mass_fluid = _f(1e10 * rng.uniform(0.5, 2.0, size=(5, 5, nelf)))
         # assembled inverse mass: make copies of one point agree
         g = m.inv_mass_fluid.reshape(-1, order="F")
@@ -365,7 +367,7 @@ def coupled_mesh(ni: int, nj_solid: int, nj_fluid: int, src_type: int = _abi.MON
         m.bdry_solid_el = (np.arange(ni) + 1).astype(I32)
         m.bdry_jpol_fluid = np.full(ni, 4, dtype=I32)
         m.bdry_jpol_solid = np.zeros(ni, dtype=I32)
-        m.bdry_matr = _f(1e-2 * rng.uniform(-1.0, 1.0, size=(5, ni, 2)))
+        m.bdry_matr = _f(bdry_scale * rng.uniform(-1.0, 1.0, size=(5, ni, 2)))
     # solid inverse mass: consistent copies
     per = np.zeros(m.nglob_solid, dtype=F32)
     per[m.igloc_solid - 1] = m.inv_mass_rho.reshape(-1, order="F")
@@ -382,7 +384,7 @@ def coupled_mesh(ni: int, nj_solid: int, nj_fluid: int, src_type: int = _abi.MON
     ic = ni // 2
     m.ielsrc = np.zeros(8, dtype=I32)
     if fluid_src and nj_fluid > 1:
-        jc = 1
+        jc = nj_fluid - 1
         els = [(jc - 1) * ni + ic - 1, (jc - 1) * ni + ic, jc * ni + ic - 1, jc * ni + ic]
         pts = [(4, 4), (0, 4), (4, 0), (0, 0)]
         st = np.zeros((5, 5, 8), dtype=F32, order="F")
