@@ -147,6 +147,7 @@ SIGNATURES = {
     "axg_get_solid_colouring": (C.c_int, [C.c_void_p, _ip, _ip, C.c_int64]),
     "axg_plan_check": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.POINTER(Info)]),
     "axg_time_stiffness": (C.c_int, [C.c_void_p, C.c_int32, _fp]),
+    "axg_device_check_report": (C.c_int, [_ip]),
     "axg_destroy": (None, [C.c_void_p]),
     "axg_last_error": (C.c_char_p, [C.c_void_p]),
 }
@@ -159,6 +160,8 @@ def load_library(path: str | os.PathLike | None = None):
     global _lib
     if _lib is not None and path is None:
         return _lib
+    if path is None and os.environ.get("AXG_LIBRARY"):
+        path = os.environ["AXG_LIBRARY"]  # e.g. a build with device bounds checks
     p = Path(path) if path is not None else LIB_PATH
     if not p.exists():
         raise RuntimeError(

@@ -70,6 +70,7 @@ struct DomainDev {
   float *m0 = nullptr;
   float *fsmask = nullptr;
   float *srcfl = nullptr;
+  int64_t n_m0 = 0;
 };
 
 struct CouplingHost {
@@ -137,7 +138,9 @@ int dalloc(axg_handle *h, T **p, size_t count) {
   *p = nullptr;
   if (count == 0) return AXG_OK;
   void *q = nullptr;
-  cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+  // 256 bytes of tail padding: no kernel reads past an extent, the pad only
+  // keeps a future vectorised tail load inside the allocation
+  cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 256);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
   h->allocs.push_back(q);
   h->dev_bytes += (int64_t)(count * sizeof(T));
@@ -318,6 +321,7 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid) {
   if ((rc = upload(h, &dd.elinfo, elinfo))) return rc;
   if ((rc = upload(h, &dd.metric, metric))) return rc;
   if ((rc = upload(h, &dd.m0, m0))) return rc;
+  dd.n_m0 = (int64_t)m0.size();
   if (use_fs && (rc = upload(h, &dd.fsmask, fsmask))) return rc;
   if (fluid && d->fluid_src && d->nelsrc > 0) {
     std::vector<float> s((size_t)8 * 25, 0.f);
@@ -345,6 +349,7 @@ int upload_coupling(axg_handle *h, const CouplingHost &c, Coupling &out) {
   out.b1 = b1;
   out.b2 = b2;
   out.mask = mk;
+  out.n_contrib = (int64_t)c.src_gidx.size();
   return AXG_OK;
 }
 
@@ -388,6 +393,8 @@ StateArgs solid_state(axg_handle *h) {
   s.src.gidx = h->src_gidx_d;
   s.src.val = h->src_val_d;
   s.src.n = h->n_src;
+  s.nglob = h->nglob_s;
+  s.niter = std::max(h->niter, 1);
   return s;
 }
 
@@ -401,11 +408,16 @@ StateArgs fluid_state(axg_handle *h) {
   s.inv_mass = h->inv_mass_f;
   s.gamma = h->gamma_f;
   s.src.n = 0;
+  s.nglob = h->nglob_f;
   return s;
 }
 
-DomainArgs domain_args(const DomainDev &dd) {
+DomainArgs domain_args(const DomainDev &dd, const DomainPlan &pl) {
   DomainArgs a{};
+  a.n_patches = pl.n_patches;
+  a.n_pts = pl.total_pts;
+  a.n_elem = pl.nel;
+  a.n_m0 = dd.n_m0;
   a.meta = dd.meta;
   a.pts = dd.pts;
   a.elpts = dd.elpts;
@@ -419,7 +431,7 @@ DomainArgs domain_args(const DomainDev &dd) {
 
 template <int POLE, int MODE>
 void launch_solid_colours(axg_handle *h, cudaStream_t s) {
-  DomainArgs a = domain_args(h->ds);
+  DomainArgs a = domain_args(h->ds, h->ps);
   StateArgs st = solid_state(h);
   for (int c = 0; c < h->ps.n_colours; ++c) {
     a.patch_begin = h->ps.colour_start[c];
@@ -459,7 +471,7 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
       if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(h->to_fluid, ss, h->ff);
       else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(h->to_fluid, ss, h->ff);
     }
-    DomainArgs a = domain_args(h->df);
+    DomainArgs a = domain_args(h->df, h->pf);
     for (int c = 0; c < h->pf.n_colours; ++c) {
       a.patch_begin = h->pf.colour_start[c];
       const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
@@ -684,6 +696,10 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
   h->blowup = h->iter + 1;
   if ((rc = upload_coupling(h, cf, h->to_fluid))) return rc;
   if ((rc = upload_coupling(h, cs, h->to_solid))) return rc;
+  h->to_fluid.nglob_recv = h->nglob_f;
+  h->to_fluid.nglob_send = h->nglob_s;
+  h->to_solid.nglob_recv = h->nglob_s;
+  h->to_solid.nglob_send = h->nglob_f;
   h->kernels_per_force = h->ps.n_colours + (h->to_solid.n > 0 ? 1 : 0);
   h->kernels_per_step = h->ps.n_colours + 1 +
                         (h->nel_f > 0 ? h->pf.n_colours + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);
@@ -964,6 +980,18 @@ void axg_destroy(axg_handle *h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   release(h);
   delete h;
+}
+
+int axg_device_check_report(int32_t *out8) {
+  if (!out8) return fail(nullptr, AXG_ERR_BAD_ARG, "out8 is NULL");
+#ifdef AXG_DEVICE_CHECKS
+  cudaError_t e = cudaMemcpyFromSymbol(out8, g_axg_check, 8 * sizeof(int32_t));
+  if (e != cudaSuccess) return fail(nullptr, AXG_ERR_CUDA, cudaGetErrorString(e));
+  return AXG_OK;
+#else
+  std::memset(out8, 0, 8 * sizeof(int32_t));
+  return fail(nullptr, AXG_ERR_UNSUPPORTED, "device checks are not compiled into this build");
+#endif
 }
 
 const char *axg_last_error(axg_handle *h) { return h ? h->err.c_str() : g_create_error.c_str(); }

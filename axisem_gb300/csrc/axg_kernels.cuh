@@ -27,6 +27,32 @@
 
 namespace axg {
 
+// Debug variant (-DAXG_DEVICE_CHECKS): every global and shared index is
+// checked against its bound; the first violation is recorded in
+// g_axg_check = {flag, kernel id, source line, 0, index lo, index hi, bound lo,
+// bound hi} and the access is skipped.  Nothing traps.  Normal builds compile
+// the checks away.
+#ifdef AXG_DEVICE_CHECKS
+__device__ int32_t g_axg_check[8];
+__device__ __noinline__ bool axg_record(int kern, int line, long long idx, long long bound) {
+  if (atomicCAS(&g_axg_check[0], 0, 1) == 0) {
+    g_axg_check[1] = kern;
+    g_axg_check[2] = line;
+    g_axg_check[4] = (int32_t)(idx & 0xffffffff);
+    g_axg_check[5] = (int32_t)(idx >> 32);
+    g_axg_check[6] = (int32_t)(bound & 0xffffffff);
+    g_axg_check[7] = (int32_t)(bound >> 32);
+  }
+  return false;
+}
+#define AXG_BOUND(idx, bound, kern)                                                          \
+  ((((long long)(idx)) >= 0 && ((long long)(idx)) < ((long long)(bound)))                    \
+       ? true                                                                               \
+       : axg_record((kern), __LINE__, (long long)(idx), (long long)(bound)))
+#else
+#define AXG_BOUND(idx, bound, kern) true
+#endif
+
 constexpr int kWarps = 8;
 constexpr int kThreads = 32 * kWarps;
 constexpr unsigned kFull = 0xffffffffu;
@@ -69,6 +95,7 @@ struct DomainArgs {
   const float *fsmask;      // fluid free-surface mask per element (launch order) or null
   const float *srcfl;       // fluid element source terms (8, 25) or null
   int32_t patch_begin;
+  int64_t n_patches, n_pts, n_elem, n_m0;   // buffer extents (checked builds)
 };
 
 struct StateArgs {
@@ -84,6 +111,8 @@ struct StateArgs {
   float thresh;             // 10 |magnitude|
   float dt, hdt, hdt2;
   SrcTable src;
+  int64_t nglob;            // extent of the state arrays (checked builds)
+  int32_t niter;            // extent of stf
 };
 
 // ------------------------------------------------------------ small helpers
@@ -141,6 +170,7 @@ __device__ __forceinline__ const float (&cxi(const LaneCoef &c))[5] { return AX 
 template <bool AX>
 __device__ __forceinline__ const float (&csxi(const LaneCoef &c))[5] { return AX ? c.sxi1 : c.sxi2; }
 
+// element-local value of metric array `slot` at point `lane` (< 25)
 __device__ __forceinline__ float ldm(const float *blk, int slot, int lane) {
   return __ldcs(blk + slot * 25 + lane);
 }
@@ -343,14 +373,20 @@ __global__ void __launch_bounds__(kThreads) solid_patch_kernel(DomainArgs d, Sta
   // component c of the shared arrays -> global component (mono: s, z)
   auto gc = [](int c) { return (POLE == POLE_MONO && c == 1) ? 2 : c; };
 
-  if (MODE == MODE_NEWMARK && *st.blowup) return;
+  __shared__ int s_stop;
+  if (threadIdx.x == 0) s_stop = (MODE == MODE_NEWMARK) ? *st.blowup : 0;
+  __syncthreads();
+  if (s_stop) return;  // uniform across the CTA
+  if (!AXG_BOUND(d.patch_begin + blockIdx.x, d.n_patches, 1)) return;
   const PatchMeta m = d.meta[d.patch_begin + blockIdx.x];
 
   // 1. gather (+ predictor)
   for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
+    if (!AXG_BOUND(t, kMaxPatchPoints, 1) || !AXG_BOUND(m.pt_start + t, d.n_pts, 1)) continue;
     const uint32_t w = d.pts[m.pt_start + t];
     const uint32_t g = w & kPtIndexMask;
     s_w[t] = w;
+    if (!AXG_BOUND(g, st.nglob, 1)) continue;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       float u = st.u[gc(c)][g];
@@ -365,17 +401,24 @@ __global__ void __launch_bounds__(kThreads) solid_patch_kernel(DomainArgs d, Sta
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool active = lane < 25;
   const int i = lane % 5, j = active ? lane / 5 : 0;
+  // idle lanes 25..31 take part in the shuffles; their loads of an element's
+  // data go to point 24 so that no lane reads past the element's block (the
+  // block of the last element ends where the allocation ends)
+  const int ml = active ? lane : 24;
   LaneCoef coef;
   load_coef(sp, i, j, coef);
   int r0 = 0;
   for (int r = 0; r < m.n_rounds; ++r) {
     const int r1 = m.round_end[r];
     for (int s = r0 + warp; s < r1; s += kWarps) {
-      const int64_t el = (int64_t)m.elem_start + s;
+      int64_t el = (int64_t)m.elem_start + s;
+      if (!AXG_BOUND(el, d.n_elem, 2)) el = 0;
       const int32_t info = __ldg(d.elinfo + el);
-      const int axslot = (info & 0xFFFFFF) - 1;
+      int axslot = (info & 0xFFFFFF) - 1;
+      if (axslot >= 0 && !AXG_BOUND((int64_t)(axslot + 1) * NA * 5 - 1, d.n_m0, 2)) axslot = -1;
       const float *blk = d.metric + el * BS;
-      const int idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
+      int idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
+      if (!AXG_BOUND(idx, m.n_pts, 2)) idx = 0;
       float u[3] = {0.f, 0.f, 0.f};
       if (active) {
         u[0] = s_u[0][idx];
@@ -400,14 +443,14 @@ __global__ void __launch_bounds__(kThreads) solid_patch_kernel(DomainArgs d, Sta
       float f0, f1 = 0.f, f2;
       const float *m0 = ax ? d.m0 + (int64_t)axslot * (NA * 5) : nullptr;
       if (POLE == POLE_MONO) {
-        if (ax) stiff_mono<true>(coef, blk, m0, lane, i, j, u[0], u[2], f0, f2);
-        else stiff_mono<false>(coef, blk, m0, lane, i, j, u[0], u[2], f0, f2);
+        if (ax) stiff_mono<true>(coef, blk, m0, ml, i, j, u[0], u[2], f0, f2);
+        else stiff_mono<false>(coef, blk, m0, ml, i, j, u[0], u[2], f0, f2);
       } else if (POLE == POLE_DI) {
-        if (ax) stiff_di<true>(coef, blk, m0, lane, i, j, u[0], u[1], u[2], f0, f1, f2);
-        else stiff_di<false>(coef, blk, m0, lane, i, j, u[0], u[1], u[2], f0, f1, f2);
+        if (ax) stiff_di<true>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
+        else stiff_di<false>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
       } else {
-        if (ax) stiff_quad<true>(coef, blk, m0, lane, i, j, u[0], u[1], u[2], f0, f1, f2);
-        else stiff_quad<false>(coef, blk, m0, lane, i, j, u[0], u[1], u[2], f0, f1, f2);
+        if (ax) stiff_quad<true>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
+        else stiff_quad<false>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
       }
       if (ax && i == 0) {  // axis mask of acc1
         if (POLE == POLE_MONO) f0 = 0.f;
@@ -430,10 +473,12 @@ __global__ void __launch_bounds__(kThreads) solid_patch_kernel(DomainArgs d, Sta
 
   // 3. write-back
   float stf1 = 0.f;
-  if (MODE == MODE_NEWMARK) stf1 = st.stf[*st.iter - 1];
+  if (MODE == MODE_NEWMARK && AXG_BOUND(*st.iter - 1, st.niter, 3)) stf1 = st.stf[*st.iter - 1];
   for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
+    if (!AXG_BOUND(t, kMaxPatchPoints, 3)) continue;
     const uint32_t w = s_w[t];
     const uint32_t g = w & kPtIndexMask;
+    if (!AXG_BOUND(g, st.nglob, 3)) continue;
     float v[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
@@ -477,12 +522,18 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
   __shared__ float s_f[kMaxPatchPoints];
   __shared__ uint32_t s_w[kMaxPatchPoints];
   constexpr int BS = block_stride(NONMONO ? 4 : 3);
-  if (*st.blowup) return;
+  __shared__ int s_stop;
+  if (threadIdx.x == 0) s_stop = *st.blowup;
+  __syncthreads();
+  if (s_stop) return;  // uniform across the CTA
+  if (!AXG_BOUND(d.patch_begin + blockIdx.x, d.n_patches, 11)) return;
   const PatchMeta m = d.meta[d.patch_begin + blockIdx.x];
   for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
+    if (!AXG_BOUND(t, kMaxPatchPoints, 11) || !AXG_BOUND(m.pt_start + t, d.n_pts, 11)) continue;
     const uint32_t w = d.pts[m.pt_start + t];
     const uint32_t g = w & kPtIndexMask;
     s_w[t] = w;
+    if (!AXG_BOUND(g, st.nglob, 11)) continue;
     s_u[t] = predict(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2);
     s_f[t] = 0.f;
   }
@@ -490,25 +541,32 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool active = lane < 25;
   const int i = lane % 5, j = active ? lane / 5 : 0;
+  // idle lanes 25..31 take part in the shuffles; their loads of an element's
+  // data go to point 24 so that no lane reads past the element's block (the
+  // block of the last element ends where the allocation ends)
+  const int ml = active ? lane : 24;
   LaneCoef coef;
   load_coef(sp, i, j, coef);
-  const float stf1 = st.stf[*st.iter - 1];
+  const float stf1 = AXG_BOUND(*st.iter - 1, st.niter, 12) ? st.stf[*st.iter - 1] : 0.f;
   int r0 = 0;
   for (int r = 0; r < m.n_rounds; ++r) {
     const int r1 = m.round_end[r];
     for (int s = r0 + warp; s < r1; s += kWarps) {
-      const int64_t el = (int64_t)m.elem_start + s;
+      int64_t el = (int64_t)m.elem_start + s;
+      if (!AXG_BOUND(el, d.n_elem, 12)) el = 0;
       const int32_t info = __ldg(d.elinfo + el);
-      const int axslot = (info & 0xFFFFFF) - 1;
+      int axslot = (info & 0xFFFFFF) - 1;
+      if (axslot >= 0 && !AXG_BOUND((int64_t)(axslot + 1) * 5 - 1, d.n_m0, 12)) axslot = -1;
       const int srcslot = ((info >> 24) & 0xF) - 1;
       const bool ax = axslot >= 0;
       const float *blk = d.metric + el * BS;
-      const int idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
+      int idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
+      if (!AXG_BOUND(idx, m.n_pts, 12)) idx = 0;
       float chi = active ? s_u[idx] : 0.f;
       if (NONMONO && ax && i == 0) chi = 0.f;  // apply_axis_mask_scal(chi)
       const float *m0 = ax ? d.m0 + (int64_t)axslot * 5 : nullptr;
-      float f = ax ? stiff_fluid<true, NONMONO>(coef, blk, m0, lane, i, j, chi)
-                   : stiff_fluid<false, NONMONO>(coef, blk, m0, lane, i, j, chi);
+      float f = ax ? stiff_fluid<true, NONMONO>(coef, blk, m0, ml, i, j, chi)
+                   : stiff_fluid<false, NONMONO>(coef, blk, m0, ml, i, j, chi);
       if (srcslot >= 0 && stf1 != 0.f && active) f = f - d.srcfl[srcslot * 25 + lane] * stf1;
       if (NONMONO && ax && i == 0) f = 0.f;
       if (d.fsmask && active) f = f * d.fsmask[el * 25 + lane];
@@ -520,6 +578,7 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
   for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
     const uint32_t w = s_w[t];
     const uint32_t g = w & kPtIndexMask;
+    if (!AXG_BOUND(g, st.nglob, 13)) continue;
     float v = s_f[t];
     if (!(w & kPtFirst)) v = st.f[0][g] + v;
     if (!(w & kPtLast)) {
@@ -549,6 +608,7 @@ struct Coupling {
   const float *b1, *b2;     // bdry_matr(ipol, b, 1/2) per contribution
   const float *mask;        // per contribution: 0 where the receiving copy is masked, else 1 (or fs mask)
   int32_t n;
+  int64_t n_contrib, nglob_recv, nglob_send;  // extents (checked builds)
 };
 
 // bdry_copy2fluid (SOLVER/time_evol_wave.F90:1532-1571): fluid force starts
@@ -560,14 +620,16 @@ __global__ void couple_to_fluid_kernel(Coupling cp, StateArgs solid, float *ffl)
   if (q >= cp.n) return;
   float acc = 0.f;
   for (int k = cp.start[q]; k < cp.start[q + 1]; ++k) {
+    if (!AXG_BOUND(k, cp.n_contrib, 21)) break;
     const int gs = cp.src_gidx[k];
+    if (!AXG_BOUND(gs, cp.nglob_send, 21)) continue;
     const float us = predict(solid.u[0][gs], solid.v[0][gs], solid.a[0][gs], solid.dt, solid.hdt2);
     const float uz = predict(solid.u[2][gs], solid.v[2][gs], solid.a[2][gs], solid.dt, solid.hdt2);
     float x = us;
     if (DIPOLE) x = us + predict(solid.u[1][gs], solid.v[1][gs], solid.a[1][gs], solid.dt, solid.hdt2);
     acc = acc + cp.mask[k] * (-cp.b1[k] * x - cp.b2[k] * uz);
   }
-  ffl[cp.pt_gidx[q]] = acc;
+  if (AXG_BOUND(cp.pt_gidx[q], cp.nglob_recv, 22)) ffl[cp.pt_gidx[q]] = acc;
 }
 
 // bdry_copy2solid (SOLVER/time_evol_wave.F90:1577-1611): solid force starts
@@ -580,6 +642,7 @@ __global__ void couple_to_solid_kernel(Coupling cp, StateArgs fluid, StateArgs s
   if (q >= cp.n) return;
   float fs = 0.f, fp = 0.f, fz = 0.f;
   for (int k = cp.start[q]; k < cp.start[q + 1]; ++k) {
+    if (!AXG_BOUND(k, cp.n_contrib, 23) || !AXG_BOUND(cp.src_gidx[k], cp.nglob_send, 23)) break;
     const float a = fluid.a[0][cp.src_gidx[k]];
     const bool masked = cp.mask[k] == 0.f;  // solid copy sits at ipol=0 of an axial element
     float ts = cp.b1[k] * a, tp = POLE == POLE_DI ? cp.b1[k] * a : 0.f, tz = cp.b2[k] * a;
@@ -593,6 +656,7 @@ __global__ void couple_to_solid_kernel(Coupling cp, StateArgs fluid, StateArgs s
     fz = fz + tz;
   }
   const int g = cp.pt_gidx[q];
+  if (!AXG_BOUND(g, cp.nglob_recv, 24)) return;
   solid.f[0][g] = fs;
   if (POLE != POLE_MONO) solid.f[1][g] = fp;
   solid.f[2][g] = fz;
@@ -611,6 +675,7 @@ __global__ void receivers_kernel(StateArgs solid, const int32_t *rec_gidx, int32
     if (is < nseismo) {
       for (int r = threadIdx.x; r < num_rec; r += blockDim.x) {
         const int g = rec_gidx[r];
+        if (!AXG_BOUND(g, solid.nglob, 31)) continue;
         const float us = solid.u[0][g], uz = solid.u[2][g];
         const float up = pole == POLE_MONO ? 0.f : solid.u[1][g];
         float v1 = us, v2 = up, v3 = uz;

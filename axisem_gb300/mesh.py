@@ -330,7 +330,7 @@ def coupled_mesh(ni: int, nj_solid: int, nj_fluid: int, src_type: int = _abi.MON
                  niter: int = 60, seed: int = 7, axial_column: bool = True, fluid_src: bool = False,
                  num_rec: int = 6, seis_it: int = 2, deltat: float = 2e-6,
                  free_surface: bool = False, absorbing: bool = False,
-                 bdry_scale: float = 1.0) -> Mesh:
+                 bdry_scale: float = 1.0, terms: str = "all") -> Mesh:
     """A solid layer on top of a fluid layer, both ni elements wide, with
     the solid-fluid boundary along the fluid's top edge (jpol = 4) and the
     solid's bottom edge (jpol = 0); the I = 0 column lies on the axis.  A
@@ -340,7 +340,7 @@ def coupled_mesh(ni: int, nj_solid: int, nj_fluid: int, src_type: int = _abi.MON
     (SOLVER/source.f90:1133); receivers sit on the top surface."""
     rng = np.random.default_rng(seed)
     m = structured_mesh(ni, nj_solid, src_type, seed=seed, axial="column" if axial_column else "none",
-                        terms="all")
+                        terms=terms)
     if nj_fluid > 0:
         igf, ngf = structured_igloc(ni, nj_fluid)
         nelf = ni * nj_fluid

@@ -248,6 +248,12 @@ int axg_plan_check(const axg_mesh_desc *desc, int32_t patch_elems, axg_info *inf
  * average device time in ms of one stiffness+assembly (all colour launches). */
 int axg_time_stiffness(axg_handle *h, int32_t n, float *ms_avg);
 
+/* Debug builds compiled with -DAXG_DEVICE_CHECKS check every device index
+ * against its bound and record the first violation instead of accessing
+ * memory.  Fills out8 = {flag, kernel id, source line, 0, index lo, index hi,
+ * bound lo, bound hi}; returns AXG_ERR_UNSUPPORTED in normal builds. */
+int axg_device_check_report(int32_t *out8);
+
 void axg_destroy(axg_handle *h);
 
 /* Message of the last error on `h` (or of the last failed axg_create when h is
