@@ -110,6 +110,8 @@ struct axg_handle {
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int num_sms = 1, solid_ctas = 1;
+  int32_t *errw = nullptr;
   std::string err = "no error";
   int64_t kernels_per_step = 0, kernels_per_force = 0;
 };
@@ -386,6 +388,7 @@ StateArgs solid_state(axg_handle *h) {
   s.stf = h->stf;
   s.iter = h->iter;
   s.blowup = h->blowup;
+  s.err = h->errw;
   s.thresh = (float)(10.0 * std::fabs(h->magnitude));
   s.dt = (float)h->dt;
   s.hdt = (float)(0.5 * h->dt);
@@ -430,13 +433,32 @@ DomainArgs domain_args(const DomainDev &dd, const DomainPlan &pl) {
 }
 
 template <int POLE, int MODE>
+constexpr int solid_smem_bytes() {
+  constexpr int NC = POLE == POLE_MONO ? 2 : 3;
+  return SolidSmem<NC, block_stride(n_terms(POLE))>::bytes;
+}
+
+template <int POLE, int MODE>
+int prepare_solid_kernel(axg_handle *h) {
+  auto fn = solid_patch_kernel<POLE, MODE>;
+  CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, solid_smem_bytes<POLE, MODE>()));
+  CK(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, solid_smem_bytes<POLE, MODE>()));
+  if (per_sm < 1) return fail(h, AXG_ERR_CUDA, "solid kernel does not fit on an SM");
+  h->solid_ctas = per_sm * h->num_sms;
+  return AXG_OK;
+}
+
+template <int POLE, int MODE>
 void launch_solid_colours(axg_handle *h, cudaStream_t s) {
   DomainArgs a = domain_args(h->ds, h->ps);
   StateArgs st = solid_state(h);
   for (int c = 0; c < h->ps.n_colours; ++c) {
     a.patch_begin = h->ps.colour_start[c];
     const int n = h->ps.colour_start[c + 1] - h->ps.colour_start[c];
-    solid_patch_kernel<POLE, MODE><<<n, kThreads, 0, s>>>(a, st, h->spec);
+    const int grid = std::min(n, h->solid_ctas);
+    solid_patch_kernel<POLE, MODE><<<grid, kThreads, solid_smem_bytes<POLE, MODE>(), s>>>(a, st, h->spec, n);
   }
 }
 
@@ -692,8 +714,20 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
   if ((rc = upload(h, &h->rec_gidx_d, h->rec_gidx))) return rc;
   if ((rc = upload(h, &h->src_gidx_d, src_g))) return rc;
   if ((rc = upload(h, &h->src_val_d, src_v))) return rc;
-  if ((rc = dalloc(h, &h->iter, 2))) return rc;
+  if ((rc = dalloc(h, &h->iter, 4))) return rc;
   h->blowup = h->iter + 1;
+  h->errw = h->iter + 2;
+  CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
+  if (h->pole == AXG_MONOPOLE) {
+    if ((rc = prepare_solid_kernel<POLE_MONO, MODE_FORCE>(h)) || (rc = prepare_solid_kernel<POLE_MONO, MODE_NEWMARK>(h)))
+      return rc;
+  } else if (h->pole == AXG_DIPOLE) {
+    if ((rc = prepare_solid_kernel<POLE_DI, MODE_FORCE>(h)) || (rc = prepare_solid_kernel<POLE_DI, MODE_NEWMARK>(h)))
+      return rc;
+  } else {
+    if ((rc = prepare_solid_kernel<POLE_QUAD, MODE_FORCE>(h)) || (rc = prepare_solid_kernel<POLE_QUAD, MODE_NEWMARK>(h)))
+      return rc;
+  }
   if ((rc = upload_coupling(h, cf, h->to_fluid))) return rc;
   if ((rc = upload_coupling(h, cs, h->to_solid))) return rc;
   h->to_fluid.nglob_recv = h->nglob_f;
@@ -756,7 +790,7 @@ int axg_reset(axg_handle *h) {
   }
   // the iter-0 seismogram sample (dump_stuff(0,...)) is the zero wavefield
   CK(cudaMemsetAsync(h->rec, 0, (size_t)h->nseismo * 3 * std::max(h->num_rec, 1) * sizeof(float), h->stream));
-  CK(cudaMemsetAsync(h->iter, 0, 2 * sizeof(int32_t), h->stream));
+  CK(cudaMemsetAsync(h->iter, 0, 4 * sizeof(int32_t), h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return AXG_OK;
 }
@@ -782,9 +816,12 @@ int axg_run(axg_handle *h, int32_t first_iter, int32_t n_iter) {
       CK(cudaGetLastError());
     }
     done += k;
-    int32_t bl = 0;
-    CK(cudaMemcpyAsync(&bl, h->blowup, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    int32_t flags[2] = {0, 0};
+    CK(cudaMemcpyAsync(flags, h->blowup, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    const int32_t bl = flags[0];
+    if (flags[1] != 0)
+      return fail(h, AXG_ERR_TIMEOUT, "a bounded device wait on a bulk copy gave up");
     if (bl != 0)
       return fail(h, AXG_ERR_BLOWUP,
                   fmt("displacements blew up: |disp(1,1,:,:)| > 10 |magnitude| at time step %d", bl + 1));

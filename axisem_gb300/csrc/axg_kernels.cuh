@@ -24,6 +24,7 @@
 #include <stdint.h>
 
 #include "axg_plan.h"
+#include "axg_tma.cuh"
 
 namespace axg {
 
@@ -108,6 +109,7 @@ struct StateArgs {
   const float *stf;         // (niter)
   const int32_t *iter;      // device iteration counter (1-based iter of this step)
   int32_t *blowup;          // first iteration that blew up (0 = none)
+  int32_t *err;             // device error word (AXG_ERR_TIMEOUT when a bounded wait gave up)
   float thresh;             // 10 |magnitude|
   float dt, hdt, hdt2;
   SrcTable src;
@@ -170,10 +172,9 @@ __device__ __forceinline__ const float (&cxi(const LaneCoef &c))[5] { return AX 
 template <bool AX>
 __device__ __forceinline__ const float (&csxi(const LaneCoef &c))[5] { return AX ? c.sxi1 : c.sxi2; }
 
-// element-local value of metric array `slot` at point `lane` (< 25)
-__device__ __forceinline__ float ldm(const float *blk, int slot, int lane) {
-  return __ldcs(blk + slot * 25 + lane);
-}
+// element-local value of metric array `slot` at point `lane` (< 25); `blk` is
+// the element's block staged in shared memory
+__device__ __forceinline__ float ldm(const float *blk, int slot, int lane) { return blk[slot * 25 + lane]; }
 
 // ------------------------------------------------------------ element stiffness
 
@@ -362,155 +363,243 @@ __device__ __forceinline__ float stiff_fluid(const LaneCoef &c, const float *blk
 
 // ------------------------------------------------------------ solid patch kernel
 
+constexpr int kStages = 3;  // element blocks in flight per warp (TMA ring depth)
+
+// shared-memory layout of the solid kernel (bytes)
+template <int NC, int BS>
+struct SolidSmem {
+  static constexpr int u_off = 0;
+  static constexpr int f_off = u_off + NC * kMaxPatchPoints * 4;
+  static constexpr int w_off = f_off + NC * kMaxPatchPoints * 4;
+  static constexpr int ring_off = ((w_off + kMaxPatchPoints * 4 + 127) / 128) * 128;
+  static constexpr int bar_off = ring_off + kWarps * kStages * BS * 4;
+  static constexpr int bytes = bar_off + kWarps * kStages * 8;
+};
+
+// the elements warp `w` processes in a patch, in order: sub-round by
+// sub-round, elements w, w + kWarps, ... of each round
+struct WarpIter {
+  int r, s;
+  __device__ __forceinline__ void norm(const PatchMeta &m, int w) {
+    while (r < m.n_rounds && s >= m.round_end[r]) {
+      ++r;
+      s = m.round_end[r - 1] + w;
+    }
+  }
+  __device__ __forceinline__ bool valid(const PatchMeta &m) const { return r < m.n_rounds; }
+};
+
 template <int POLE, int MODE>
-__global__ void __launch_bounds__(kThreads) solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp) {
+__global__ void __launch_bounds__(kThreads, 2)
+    solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches) {
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
   constexpr int NT = n_terms(POLE), NA = n_axial(POLE);
   constexpr int BS = block_stride(NT);
-  __shared__ float s_u[NC][kMaxPatchPoints];
-  __shared__ float s_f[NC][kMaxPatchPoints];
-  __shared__ uint32_t s_w[kMaxPatchPoints];
+  constexpr uint32_t BSB = BS * 4;
+  using L = SolidSmem<NC, BS>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float(*s_u)[kMaxPatchPoints] = reinterpret_cast<float(*)[kMaxPatchPoints]>(smem + L::u_off);
+  float(*s_f)[kMaxPatchPoints] = reinterpret_cast<float(*)[kMaxPatchPoints]>(smem + L::f_off);
+  uint32_t *s_w = reinterpret_cast<uint32_t *>(smem + L::w_off);
+  float *ring = reinterpret_cast<float *>(smem + L::ring_off);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bar_off);
+  __shared__ int s_stop;
   // component c of the shared arrays -> global component (mono: s, z)
   auto gc = [](int c) { return (POLE == POLE_MONO && c == 1) ? 2 : c; };
 
-  __shared__ int s_stop;
-  if (threadIdx.x == 0) s_stop = (MODE == MODE_NEWMARK) ? *st.blowup : 0;
-  __syncthreads();
-  if (s_stop) return;  // uniform across the CTA
-  if (!AXG_BOUND(d.patch_begin + blockIdx.x, d.n_patches, 1)) return;
-  const PatchMeta m = d.meta[d.patch_begin + blockIdx.x];
-
-  // 1. gather (+ predictor)
-  for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
-    if (!AXG_BOUND(t, kMaxPatchPoints, 1) || !AXG_BOUND(m.pt_start + t, d.n_pts, 1)) continue;
-    const uint32_t w = d.pts[m.pt_start + t];
-    const uint32_t g = w & kPtIndexMask;
-    s_w[t] = w;
-    if (!AXG_BOUND(g, st.nglob, 1)) continue;
-#pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      float u = st.u[gc(c)][g];
-      if (MODE == MODE_NEWMARK) u = predict(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2);
-      s_u[c][t] = u;
-      s_f[c][t] = 0.f;
-    }
-  }
-  __syncthreads();
-
-  // 2. elements
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x < kWarps * kStages) mbar_init(&bars[threadIdx.x], 1);
+  if (threadIdx.x == 0) s_stop = (MODE == MODE_NEWMARK) ? *st.blowup : 0;
+  fence_mbar_init();
+  __syncthreads();
+  if (s_stop) return;  // uniform across the CTA; no copy has been issued
+
   const bool active = lane < 25;
   const int i = lane % 5, j = active ? lane / 5 : 0;
-  // idle lanes 25..31 take part in the shuffles; their loads of an element's
-  // data go to point 24 so that no lane reads past the element's block (the
-  // block of the last element ends where the allocation ends)
+  // idle lanes 25..31 take part in the shuffles; their reads of an element's
+  // data go to point 24 so that no lane reads past the element's block
   const int ml = active ? lane : 24;
   LaneCoef coef;
   load_coef(sp, i, j, coef);
-  int r0 = 0;
-  for (int r = 0; r < m.n_rounds; ++r) {
-    const int r1 = m.round_end[r];
-    for (int s = r0 + warp; s < r1; s += kWarps) {
-      int64_t el = (int64_t)m.elem_start + s;
-      if (!AXG_BOUND(el, d.n_elem, 2)) el = 0;
-      const int32_t info = __ldg(d.elinfo + el);
-      int axslot = (info & 0xFFFFFF) - 1;
-      if (axslot >= 0 && !AXG_BOUND((int64_t)(axslot + 1) * NA * 5 - 1, d.n_m0, 2)) axslot = -1;
-      const float *blk = d.metric + el * BS;
-      int idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
-      if (!AXG_BOUND(idx, m.n_pts, 2)) idx = 0;
-      float u[3] = {0.f, 0.f, 0.f};
-      if (active) {
-        u[0] = s_u[0][idx];
-        if (POLE == POLE_MONO) {
-          u[2] = s_u[1][idx];
-        } else {
-          u[1] = s_u[1][idx];
-          u[2] = s_u[2][idx];
-        }
-      }
-      if (MODE == MODE_NEWMARK && lane == 6) {
-        // runtime_info guard on disp(1,1,:,:) (SOLVER/time_evol_wave.F90:1042)
-        const float mx = fmaxf(fabsf(u[0]), fmaxf(fabsf(u[1]), fabsf(u[2])));
-        if (!(mx <= st.thresh)) atomicCAS(st.blowup, 0, *st.iter);
-      }
-      const bool ax = axslot >= 0;
-      if (ax && i == 0) {  // apply_axis_mask_{one,two,three}comp on disp
-        if (POLE == POLE_MONO) u[0] = 0.f;
-        if (POLE == POLE_DI) { u[1] = 0.f; u[2] = 0.f; }
-        if (POLE == POLE_QUAD) { u[0] = 0.f; u[1] = 0.f; u[2] = 0.f; }
-      }
-      float f0, f1 = 0.f, f2;
-      const float *m0 = ax ? d.m0 + (int64_t)axslot * (NA * 5) : nullptr;
-      if (POLE == POLE_MONO) {
-        if (ax) stiff_mono<true>(coef, blk, m0, ml, i, j, u[0], u[2], f0, f2);
-        else stiff_mono<false>(coef, blk, m0, ml, i, j, u[0], u[2], f0, f2);
-      } else if (POLE == POLE_DI) {
-        if (ax) stiff_di<true>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
-        else stiff_di<false>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
-      } else {
-        if (ax) stiff_quad<true>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
-        else stiff_quad<false>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
-      }
-      if (ax && i == 0) {  // axis mask of acc1
-        if (POLE == POLE_MONO) f0 = 0.f;
-        if (POLE == POLE_DI) { f1 = 0.f; f2 = 0.f; }
-        if (POLE == POLE_QUAD) { f0 = 0.f; f1 = 0.f; f2 = 0.f; }
-      }
-      if (active) {
-        s_f[0][idx] += f0;
-        if (POLE == POLE_MONO) {
-          s_f[1][idx] += f2;
-        } else {
-          s_f[1][idx] += f1;
-          s_f[2][idx] += f2;
-        }
-      }
-    }
-    r0 = r1;
-    __syncthreads();
-  }
-
-  // 3. write-back
+  const uint64_t pol = policy_evict_first();
+  float *my_ring = ring + warp * kStages * BS;
+  uint64_t *my_bars = bars + warp * kStages;
+  uint32_t kcount = 0;  // elements this warp has consumed (slot = kcount % kStages)
   float stf1 = 0.f;
   if (MODE == MODE_NEWMARK && AXG_BOUND(*st.iter - 1, st.niter, 3)) stf1 = st.stf[*st.iter - 1];
-  for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
-    if (!AXG_BOUND(t, kMaxPatchPoints, 3)) continue;
-    const uint32_t w = s_w[t];
-    const uint32_t g = w & kPtIndexMask;
-    if (!AXG_BOUND(g, st.nglob, 3)) continue;
-    float v[NC];
-#pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      v[c] = s_f[c][t];
-      if (!(w & kPtFirst)) v[c] = st.f[gc(c)][g] + v[c];
-    }
-    if (MODE == MODE_FORCE || !(w & kPtLast)) {
-#pragma unroll
-      for (int c = 0; c < NC; ++c) st.f[gc(c)][g] = v[c];
-      continue;
-    }
-    // last writer: source, corrector, store the new state
-    if ((w & kPtSource) && stf1 != 0.f) {
-      for (int q = 0; q < st.src.n; ++q)
-        if ((uint32_t)st.src.gidx[q] == g) {
-#pragma unroll
-          for (int c = 0; c < NC; ++c) v[c] = v[c] - st.src.val[3 * q + gc(c)] * stf1;
+
+  for (int pp = blockIdx.x; pp < n_colour_patches; pp += gridDim.x) {
+    if (!AXG_BOUND(d.patch_begin + pp, d.n_patches, 1)) break;
+    const PatchMeta m = d.meta[d.patch_begin + pp];
+
+    // 0. start the bulk copies of this warp's first kStages element blocks
+    WarpIter pf{0, warp};
+    pf.norm(m, warp);
+    for (int q = 0; q < kStages && pf.valid(m); ++q) {
+      if (lane == 0) {
+        const int64_t el = (int64_t)m.elem_start + pf.s;
+        if (AXG_BOUND(el, d.n_elem, 2)) {
+          const uint32_t slot = (kcount + q) % kStages;
+          bulk_g2s(my_ring + slot * BS, d.metric + el * BS, BSB, &my_bars[slot], pol);
         }
+      }
+      pf.s += kWarps;
+      pf.norm(m, warp);
     }
-    const float im = st.inv_mass[g];
-    const float gam = st.gamma ? st.gamma[g] : 0.f;
+
+    // 1. gather (+ predictor), four points per thread in flight
+    for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += 4 * kThreads) {
+      uint32_t w[4];
+      float uu[4][NC];
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      const int cg = gc(c);
-      float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im) * v[c] : -im * v[c];
-      const float vel = st.v[cg][g];
-      const float dsp = s_u[c][t];
-      if (st.gamma) a = a - 2.f * gam * vel - gam * gam * dsp;
-      st.v[cg][g] = fmaf(st.hdt, st.a[cg][g] + a, vel);
-      st.a[cg][g] = a;
-      st.u[cg][g] = dsp;
+      for (int q = 0; q < 4; ++q) {
+        const int t = t0 + q * kThreads;
+        w[q] = (t < m.n_pts && AXG_BOUND(m.pt_start + t, d.n_pts, 1)) ? d.pts[m.pt_start + t] : 0xFFFFFFFFu;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t g = w[q] & kPtIndexMask;
+        const bool ok = w[q] != 0xFFFFFFFFu && AXG_BOUND(g, st.nglob, 1);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          float u = ok ? st.u[gc(c)][g] : 0.f;
+          if (MODE == MODE_NEWMARK && ok) u = predict(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2);
+          uu[q][c] = u;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int t = t0 + q * kThreads;
+        if (t < m.n_pts) {
+          s_w[t] = w[q];
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            s_u[c][t] = uu[q][c];
+            s_f[c][t] = 0.f;
+          }
+        }
+      }
     }
+    __syncthreads();
+
+    // 2. elements, sub-round by sub-round
+    int r0 = 0;
+    for (int r = 0; r < m.n_rounds; ++r) {
+      const int r1 = m.round_end[r];
+      for (int s = r0 + warp; s < r1; s += kWarps) {
+        int64_t el = (int64_t)m.elem_start + s;
+        if (!AXG_BOUND(el, d.n_elem, 2)) el = 0;
+        const uint32_t slot = kcount % kStages;
+        mbar_wait_bounded(&my_bars[slot], (kcount / kStages) & 1u, st.err);
+        const float *blk = my_ring + slot * BS;
+        const int32_t info = __ldg(d.elinfo + el);
+        int axslot = (info & 0xFFFFFF) - 1;
+        if (axslot >= 0 && !AXG_BOUND((int64_t)(axslot + 1) * NA * 5 - 1, d.n_m0, 2)) axslot = -1;
+        int idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
+        if (!AXG_BOUND(idx, m.n_pts, 2)) idx = 0;
+        float u[3] = {0.f, 0.f, 0.f};
+        if (active) {
+          u[0] = s_u[0][idx];
+          if (POLE == POLE_MONO) {
+            u[2] = s_u[1][idx];
+          } else {
+            u[1] = s_u[1][idx];
+            u[2] = s_u[2][idx];
+          }
+        }
+        if (MODE == MODE_NEWMARK && lane == 6) {
+          // runtime_info guard on disp(1,1,:,:) (SOLVER/time_evol_wave.F90:1042)
+          const float mx = fmaxf(fabsf(u[0]), fmaxf(fabsf(u[1]), fabsf(u[2])));
+          if (!(mx <= st.thresh)) atomicCAS(st.blowup, 0, *st.iter);
+        }
+        const bool ax = axslot >= 0;
+        if (ax && i == 0) {  // apply_axis_mask_{one,two,three}comp on disp
+          if (POLE == POLE_MONO) u[0] = 0.f;
+          if (POLE == POLE_DI) { u[1] = 0.f; u[2] = 0.f; }
+          if (POLE == POLE_QUAD) { u[0] = 0.f; u[1] = 0.f; u[2] = 0.f; }
+        }
+        float f0, f1 = 0.f, f2;
+        const float *m0 = ax ? d.m0 + (int64_t)axslot * (NA * 5) : nullptr;
+        if (POLE == POLE_MONO) {
+          if (ax) stiff_mono<true>(coef, blk, m0, ml, i, j, u[0], u[2], f0, f2);
+          else stiff_mono<false>(coef, blk, m0, ml, i, j, u[0], u[2], f0, f2);
+        } else if (POLE == POLE_DI) {
+          if (ax) stiff_di<true>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
+          else stiff_di<false>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
+        } else {
+          if (ax) stiff_quad<true>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
+          else stiff_quad<false>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
+        }
+        if (ax && i == 0) {  // axis mask of acc1
+          if (POLE == POLE_MONO) f0 = 0.f;
+          if (POLE == POLE_DI) { f1 = 0.f; f2 = 0.f; }
+          if (POLE == POLE_QUAD) { f0 = 0.f; f1 = 0.f; f2 = 0.f; }
+        }
+        if (active) {
+          s_f[0][idx] += f0;
+          if (POLE == POLE_MONO) {
+            s_f[1][idx] += f2;
+          } else {
+            s_f[1][idx] += f1;
+            s_f[2][idx] += f2;
+          }
+        }
+        // the slot is free again: start the copy of the element kStages ahead
+        __syncwarp();
+        if (pf.valid(m)) {
+          if (lane == 0) {
+            const int64_t pel = (int64_t)m.elem_start + pf.s;
+            fence_proxy_async();  // the warp's reads of the slot precede the async-proxy write
+            if (AXG_BOUND(pel, d.n_elem, 2)) bulk_g2s(my_ring + slot * BS, d.metric + pel * BS, BSB, &my_bars[slot], pol);
+          }
+          pf.s += kWarps;
+          pf.norm(m, warp);
+        }
+        ++kcount;
+      }
+      r0 = r1;
+      __syncthreads();
+    }
+
+    // 3. write-back
+    for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
+      const uint32_t w = s_w[t];
+      const uint32_t g = w & kPtIndexMask;
+      if (!AXG_BOUND(g, st.nglob, 3)) continue;
+      float v[NC];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        v[c] = s_f[c][t];
+        if (!(w & kPtFirst)) v[c] = st.f[gc(c)][g] + v[c];
+      }
+      if (MODE == MODE_FORCE || !(w & kPtLast)) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) st.f[gc(c)][g] = v[c];
+        continue;
+      }
+      // last writer: source, corrector, store the new state
+      if ((w & kPtSource) && stf1 != 0.f) {
+        for (int q = 0; q < st.src.n; ++q)
+          if ((uint32_t)st.src.gidx[q] == g) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) v[c] = v[c] - st.src.val[3 * q + gc(c)] * stf1;
+          }
+      }
+      const float im = st.inv_mass[g];
+      const float gam = st.gamma ? st.gamma[g] : 0.f;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const int cg = gc(c);
+        float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im) * v[c] : -im * v[c];
+        const float vel = st.v[cg][g];
+        const float dsp = s_u[c][t];
+        if (st.gamma) a = a - 2.f * gam * vel - gam * gam * dsp;
+        st.v[cg][g] = fmaf(st.hdt, st.a[cg][g] + a, vel);
+        st.a[cg][g] = a;
+        st.u[cg][g] = dsp;
+      }
+    }
+    __syncthreads();
   }
 }
 
