@@ -267,7 +267,8 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid) {
     slots = solid_slots(pole);
     nt = (int)slots.size();
   }
-  const int bs = block_stride(nt);
+  // solid blocks carry the element's point indices and info word inline
+  const int bs = fluid ? block_stride(nt) : solid_block_stride(nt);
   std::vector<float> metric((size_t)nel * bs, 0.f);
   std::vector<int32_t> elinfo(nel, 0);
   const std::vector<int> aslots = fluid ? std::vector<int>{0} : axial_slots(pole);
@@ -298,6 +299,10 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid) {
     }
     if (srcslot[e] >= 0) info |= (srcslot[e] + 1) << 24;
     elinfo[s] = info;
+    if (!fluid) {
+      std::memcpy(blk + solid_idx_off(nt), &pl.elem_pts[25 * s], 25 * sizeof(uint16_t));
+      std::memcpy(blk + solid_info_off(nt), &info, sizeof(int32_t));
+    }
     if (use_fs) std::memcpy(fsmask.data() + 25 * s, d->fluid_free_surface_mask + 25 * e, 25 * sizeof(float));
   }
   std::vector<uint32_t> pts = pl.pt_words;
@@ -435,7 +440,7 @@ DomainArgs domain_args(const DomainDev &dd, const DomainPlan &pl) {
 template <int POLE, int MODE>
 constexpr int solid_smem_bytes() {
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;
-  return SolidSmem<NC, block_stride(n_terms(POLE))>::bytes;
+  return SolidSmem<NC, solid_block_stride(n_terms(POLE))>::bytes;
 }
 
 template <int POLE, int MODE>

@@ -75,6 +75,11 @@ enum : int {
 __host__ __device__ constexpr int n_terms(int pole) { return pole == POLE_MONO ? 15 : (pole == POLE_DI ? 24 : 26); }
 __host__ __device__ constexpr int n_axial(int pole) { return pole == POLE_MONO ? 3 : (pole == POLE_DI ? 9 : 6); }
 __host__ __device__ constexpr int block_stride(int nt) { return ((nt * 25 + 3) / 4) * 4; }
+// solid element block: nt*25 metric floats, then 25 uint16 patch-local point
+// indices (50 bytes), 2 bytes pad, the int32 element info word; 16-byte multiple
+__host__ __device__ constexpr int solid_idx_off(int nt) { return nt * 25; }      // in floats
+__host__ __device__ constexpr int solid_info_off(int nt) { return nt * 25 + 13; }  // in floats
+__host__ __device__ constexpr int solid_block_stride(int nt) { return ((nt * 25 + 14 + 3) / 4) * 4; }
 
 struct SpecDev {
   float g1[25], g2[25], g0[5];
@@ -394,7 +399,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches) {
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
   constexpr int NT = n_terms(POLE), NA = n_axial(POLE);
-  constexpr int BS = block_stride(NT);
+  constexpr int BS = solid_block_stride(NT);
   constexpr uint32_t BSB = BS * 4;
   using L = SolidSmem<NC, BS>;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -492,10 +497,10 @@ __global__ void __launch_bounds__(kThreads, 2)
         const uint32_t slot = kcount % kStages;
         mbar_wait_bounded(&my_bars[slot], (kcount / kStages) & 1u, st.err);
         const float *blk = my_ring + slot * BS;
-        const int32_t info = __ldg(d.elinfo + el);
+        const int32_t info = *reinterpret_cast<const int32_t *>(blk + solid_info_off(NT));
         int axslot = (info & 0xFFFFFF) - 1;
         if (axslot >= 0 && !AXG_BOUND((int64_t)(axslot + 1) * NA * 5 - 1, d.n_m0, 2)) axslot = -1;
-        int idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
+        int idx = active ? reinterpret_cast<const uint16_t *>(blk + solid_idx_off(NT))[lane] : 0;
         if (!AXG_BOUND(idx, m.n_pts, 2)) idx = 0;
         float u[3] = {0.f, 0.f, 0.f};
         if (active) {
