@@ -140,6 +140,7 @@ SIGNATURES = {
     "axg_set_state": (C.c_int, [C.c_void_p, C.c_int32, _fp]),
     "axg_stiffness_assembled": (C.c_int, [C.c_void_p, _fp, _fp]),
     "axg_stiffness_assembled_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "axg_stiffness_assembled_noalloc": (C.c_int, [C.POINTER(MeshDesc), _fp, _fp]),
     "axg_upload_gvec_disp": (C.c_int, [C.c_void_p, _fp]),
     "axg_download_gvec_force": (C.c_int, [C.c_void_p, _fp]),
     "axg_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -745,6 +746,196 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
   return axg_reset(h);
 }
 }  // namespace
+
+// ============================================================== no-allocation variant
+//
+// Stiffness + assembly for callers that cannot allocate device memory: code
+// running where cudaMalloc is unavailable or forbidden (inside another
+// runtime's memory pool, a driver callback, a process whose device memory is
+// fully reserved up front).  It runs the same planner and the same
+// solid_patch_kernel<pole, FORCE> as axg_stiffness_assembled, but every
+// device-side buffer -- plan, packed element blocks, u, f and control words --
+// lives in one file-scope static device array of kNoAllocScratchBytes.  Each
+// GPU that loads this library holds that array until the process exits.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+struct NoAllocDevice {
+  bool ready = false;
+  unsigned char *base = nullptr;  // device address of g_noalloc_scratch on this device
+  int grid_cap[3] = {0, 0, 0};    // resident CTAs of the FORCE kernel per pole
+};
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+
+template <int POLE>
+int noalloc_prepare_kernel(int nsm, int *cap) {
+  auto fn = solid_patch_kernel<POLE, MODE_FORCE>;
+  const int bytes = solid_smem_bytes<POLE, MODE_FORCE>();
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  int per_sm = 0;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, bytes);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "no-allocation set-up");
+  *cap = std::max(per_sm, 1) * nsm;
+  return AXG_OK;
+}
+
+// once per device, with that device current: the symbol's device address and
+// the kernel attributes (call before any stream capture)
+int noalloc_setup(NoAllocDevice **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDevice");
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(nullptr, AXG_ERR_UNSUPPORTED, "device ordinal too large");
+  NoAllocDevice &nd = g_noalloc_dev[dev];
+  if (!nd.ready) {
+    void *ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    int nsm = 0;
+    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaDeviceGetAttribute");
+    int rc;
+    if ((rc = noalloc_prepare_kernel<POLE_MONO>(nsm, &nd.grid_cap[0])) ||
+        (rc = noalloc_prepare_kernel<POLE_DI>(nsm, &nd.grid_cap[1])) ||
+        (rc = noalloc_prepare_kernel<POLE_QUAD>(nsm, &nd.grid_cap[2])))
+      return rc;
+    nd.base = static_cast<unsigned char *>(ptr);
+    nd.ready = true;
+  }
+  *out = &nd;
+  return AXG_OK;
+}
+
+template <int POLE>
+void noalloc_launch(const DomainArgs &a0, const StateArgs &st, const SpecDev &sp, const DomainPlan &pl, int cap) {
+  DomainArgs a = a0;
+  for (int c = 0; c < pl.n_colours; ++c) {
+    a.patch_begin = pl.colour_start[c];
+    const int n = pl.colour_start[c + 1] - pl.colour_start[c];
+    solid_patch_kernel<POLE, MODE_FORCE><<<std::min(n, cap), kThreads, solid_smem_bytes<POLE, MODE_FORCE>(), 0>>>(
+        a, st, sp, n);
+  }
+}
+
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+}  // namespace
+
+extern "C" int axg_stiffness_assembled_noalloc(const axg_mesh_desc *d, const float *u_gvec, float *f_gvec) {
+  if (!u_gvec || !f_gvec) return fail(nullptr, AXG_ERR_BAD_ARG, "u_gvec and f_gvec must not be NULL");
+  int rc = validate(d);
+  if (rc) return rc;
+  if ((rc = check_igloc(d->igloc_solid, 25 * (int64_t)d->nel_solid, d->nglob_solid, "igloc_solid"))) return rc;
+  if (axg_device_count() < 1) return fail(nullptr, AXG_ERR_NO_DEVICE, "no CUDA device is visible");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  NoAllocDevice *nd = nullptr;
+  if ((rc = noalloc_setup(&nd))) return rc;
+
+  // plan and pack on the host (the same planner as axg_create)
+  const int pole = d->src_type;
+  const int64_t nel = d->nel_solid, nglob = d->nglob_solid;
+  DomainPlan pl;
+  std::string perr = build_plan(d->igloc_solid, nel, nglob, kMaxPatchElems, std::vector<uint8_t>(), pl);
+  if (!perr.empty()) return fail(nullptr, AXG_ERR_BAD_DESC, "solid plan: " + perr);
+  const std::vector<int> slots = solid_slots(pole), aslots = axial_slots(pole);
+  const int nt = (int)slots.size(), na = (int)aslots.size();
+  const int bs = solid_block_stride(nt);
+  std::vector<uint8_t> axial(nel, 0);
+  for (int k = 0; k < d->naxel_solid; ++k) axial[d->ax_el_solid[k] - 1] = 1;
+  int64_t nax = 0;
+  for (int64_t e = 0; e < nel; ++e) nax += axial[e];
+
+  // scratch layout; everything 256-byte aligned
+  const size_t o_meta = 0;
+  const size_t o_pts = align256(o_meta + pl.meta.size() * sizeof(PatchMeta));
+  const size_t o_metric = align256(o_pts + pl.pt_words.size() * sizeof(uint32_t));
+  const size_t o_m0 = align256(o_metric + (size_t)nel * bs * sizeof(float));
+  const size_t o_u = align256(o_m0 + (size_t)nax * na * 5 * sizeof(float));
+  const size_t o_f = align256(o_u + (size_t)nglob * 3 * sizeof(float));
+  const size_t o_ctl = align256(o_f + (size_t)nglob * 3 * sizeof(float));
+  const size_t total = align256(o_ctl + 4 * sizeof(int32_t)) + 256;  // + tail pad
+  if (total > kNoAllocScratchBytes)
+    return fail(nullptr, AXG_ERR_BAD_ARG,
+                fmt("mesh needs %zu bytes of device scratch; the no-allocation entry point holds at most %zu "
+                    "bytes (%d elements of %d metric arrays need about %zu)",
+                    total, kNoAllocScratchBytes, (int)nel, nt, (size_t)nel * bs * 4));
+
+  std::vector<float> metric((size_t)nel * bs, 0.f), m0;
+  m0.reserve((size_t)nax * na * 5);
+  int32_t axcount = 0;
+  for (int64_t s = 0; s < nel; ++s) {
+    const int64_t e = pl.elem_order[s];
+    float *blk = metric.data() + (size_t)s * bs;
+    for (int t = 0; t < nt; ++t) std::memcpy(blk + 25 * t, d->m_solid[slots[t]] + 25 * e, 25 * sizeof(float));
+    int32_t info = 0;
+    if (axial[e]) {
+      info = ++axcount;
+      for (int q = 0; q < na; ++q)
+        for (int jj = 0; jj < 5; ++jj) m0.push_back(d->m0_solid[aslots[q]][5 * e + jj]);
+    }
+    std::memcpy(blk + solid_idx_off(nt), &pl.elem_pts[25 * s], 25 * sizeof(uint16_t));
+    std::memcpy(blk + solid_info_off(nt), &info, sizeof(int32_t));
+  }
+
+  unsigned char *base = nd->base;
+  auto put = [&](size_t off, const void *src, size_t bytes) -> int {
+    if (bytes == 0) return AXG_OK;
+    cudaError_t e = cudaMemcpy(base + off, src, bytes, cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? AXG_OK : cuda_fail(nullptr, e, "cudaMemcpy to the no-allocation scratch");
+  };
+  const int32_t zeros[4] = {0, 0, 0, 0};  // the control words must start at zero on every call
+  if ((rc = put(o_meta, pl.meta.data(), pl.meta.size() * sizeof(PatchMeta))) ||
+      (rc = put(o_pts, pl.pt_words.data(), pl.pt_words.size() * sizeof(uint32_t))) ||
+      (rc = put(o_metric, metric.data(), metric.size() * sizeof(float))) ||
+      (rc = put(o_m0, m0.data(), m0.size() * sizeof(float))) ||
+      (rc = put(o_u, u_gvec, (size_t)nglob * 3 * sizeof(float))) || (rc = put(o_ctl, zeros, sizeof zeros)))
+    return rc;
+
+  DomainArgs a{};
+  a.meta = reinterpret_cast<const PatchMeta *>(base + o_meta);
+  a.pts = reinterpret_cast<const uint32_t *>(base + o_pts);
+  a.metric = reinterpret_cast<const float *>(base + o_metric);
+  a.m0 = reinterpret_cast<const float *>(base + o_m0);
+  a.n_patches = pl.n_patches;
+  a.n_pts = pl.total_pts;
+  a.n_elem = nel;
+  a.n_m0 = (int64_t)m0.size();
+  StateArgs st{};
+  float *u = reinterpret_cast<float *>(base + o_u), *f = reinterpret_cast<float *>(base + o_f);
+  for (int c = 0; c < 3; ++c) {
+    st.u[c] = u + nglob * c;
+    st.f[c] = f + nglob * c;
+  }
+  int32_t *ctl = reinterpret_cast<int32_t *>(base + o_ctl);
+  st.iter = ctl;
+  st.blowup = ctl + 1;
+  st.err = ctl + 2;
+  st.nglob = nglob;
+  st.niter = 1;
+  SpecDev sp{};
+  for (int k = 0; k < 25; ++k) {
+    sp.g1[k] = d->G1[k];
+    sp.g2[k] = d->G2[k];
+  }
+  for (int k = 0; k < 5; ++k) sp.g0[k] = d->G0[k];
+  if (pole == AXG_MONOPOLE) noalloc_launch<POLE_MONO>(a, st, sp, pl, nd->grid_cap[0]);
+  else if (pole == AXG_DIPOLE) noalloc_launch<POLE_DI>(a, st, sp, pl, nd->grid_cap[1]);
+  else noalloc_launch<POLE_QUAD>(a, st, sp, pl, nd->grid_cap[2]);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "no-allocation kernel launch");
+  int32_t ctl_h[4];
+  e = cudaMemcpy(f_gvec, f, (size_t)nglob * 3 * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(ctl_h, ctl, sizeof ctl_h, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMemcpy from the no-allocation scratch");
+  if (ctl_h[2] != 0) return fail(nullptr, AXG_ERR_TIMEOUT, "a bounded device wait on a bulk copy gave up");
+  if (pole == AXG_MONOPOLE) std::memset(f_gvec + nglob, 0, (size_t)nglob * sizeof(float));  // unused phi
+  return AXG_OK;
+}
 
 // ============================================================== C-ABI
 

@@ -211,6 +211,22 @@ int axg_stiffness_assembled(axg_handle *h, const float *u_gvec, float *f_gvec);
  * time the kernels alone.  `stream` may be NULL (the handle's stream). */
 int axg_stiffness_assembled_device(axg_handle *h, void *stream);
 
+/* Stiffness + assembly (the same operation and result as
+ * axg_stiffness_assembled, from the same descriptor and host buffers) for
+ * callers that cannot allocate device memory, e.g. code running where
+ * cudaMalloc is unavailable or forbidden.  This entry point has no
+ * counterpart in the reference.  It makes no cudaMalloc/cudaFree call and
+ * uses no allocating library routine: all device data (plan, element blocks,
+ * u, f) lives in one 32 MiB static device array that every GPU loading the
+ * library holds until exit, which limits the mesh to roughly 11 000
+ * quadrupole elements (larger meshes return AXG_ERR_BAD_ARG naming the size
+ * needed).  The first call on a device looks up the array's device address
+ * and sets kernel attributes; make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race (host threads
+ * are serialised).  Uses the legacy default stream; host memory is used for
+ * planning. */
+int axg_stiffness_assembled_noalloc(const axg_mesh_desc *desc, const float *u_gvec, float *f_gvec);
+
 /* Uploads a gvec-layout displacement (nglob_solid,3) into the handle's
  * displacement field / downloads the handle's force buffer as gvec layout. */
 int axg_upload_gvec_disp(axg_handle *h, const float *u_gvec);
