@@ -58,7 +58,8 @@ AXIAL_TERMS_USED = {
     QUADPOLE: ["M0_w1", "M0_w2", "M0_w3", "M0_w4", "M0_w5", "M0_w6"],
 }
 
-FIELD_DISP, FIELD_VELO, FIELD_ACC0, FIELD_CHI, FIELD_DCHI, FIELD_DDCHI0, FIELD_MEMVAR = range(7)
+(FIELD_DISP, FIELD_VELO, FIELD_ACC0, FIELD_CHI, FIELD_DCHI, FIELD_DDCHI0, FIELD_MEMVAR, FIELD_ATT_SRC_TR,
+ FIELD_ATT_SRC_DEV) = range(9)
 
 _fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int32)

@@ -115,6 +115,12 @@ struct axg_handle {
   int32_t *errw = nullptr;
   std::string err = "no error";
   int64_t kernels_per_step = 0, kernels_per_force = 0;
+  int solid_ctas_step = 1;
+  // coarse-grained attenuation
+  bool anel = false;
+  int nsls = 0;
+  AnelArgs an{};
+  std::vector<int32_t> slot_of_elem_s;  // solid element -> launch slot
 };
 
 namespace {
@@ -230,7 +236,20 @@ int validate(const axg_mesh_desc *d) {
   if (d->have_absorbing_bc && (!d->solid_absorbing_gamma || (d->nel_fluid > 0 && !d->fluid_absorbing_gamma)))
     return bad("absorbing gamma arrays are NULL");
   if (!(d->deltat > 0) && d->niter > 0) return bad("deltat must be positive");
-  if (d->anel_true) return fail(nullptr, AXG_ERR_UNSUPPORTED, "attenuation (anel_true) is not implemented in this build");
+  if (d->anel_true) {
+    if (d->att_coarse_grained != 1)
+      return fail(nullptr, AXG_ERR_UNSUPPORTED,
+                  "only the coarse-grained (cg4) attenuation is implemented: att_coarse_grained must be 1");
+    if (d->n_sls < 1 || d->n_sls > kMaxSls)
+      return fail(nullptr, AXG_ERR_UNSUPPORTED, fmt("n_sls = %d; 1..%d are supported", d->n_sls, kMaxSls));
+    if (!d->y_j_attenuation || !d->exp_w_j_deltat || !d->ts_fac_t || !d->ts_fac_tm1 || !d->Q_mu || !d->Q_kappa ||
+        !d->delta_mu_cg4 || !d->delta_kappa_cg4 || !d->Y_cg4 || !d->V_s_eta_cg4 || !d->V_s_xi_cg4 ||
+        !d->V_z_eta_cg4 || !d->V_z_xi_cg4 || !d->DsDeta_over_J_sol_cg4 || !d->DzDeta_over_J_sol_cg4 ||
+        !d->DsDxi_over_J_sol_cg4 || !d->DzDxi_over_J_sol_cg4 || !d->inv_s_solid)
+      return bad("attenuation arrays are NULL");
+    for (int64_t e = 0; e < d->nel_solid; ++e)
+      if (!(d->Q_mu[e] > 0.f) || !(d->Q_kappa[e] > 0.f)) return bad("Q_mu and Q_kappa must be positive");
+  }
   return AXG_OK;
 }
 
@@ -438,41 +457,59 @@ DomainArgs domain_args(const DomainDev &dd, const DomainPlan &pl) {
   return a;
 }
 
-template <int POLE, int MODE>
+template <int POLE, int MODE, bool ANEL>
 constexpr int solid_smem_bytes() {
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;
-  return SolidSmem<NC, solid_block_stride(n_terms(POLE))>::bytes;
+  return SolidSmem<NC, solid_block_stride(n_terms(POLE)), solid_stages(ANEL), ANEL ? kAnelSlot : 0>::bytes;
 }
 
-template <int POLE, int MODE>
-int prepare_solid_kernel(axg_handle *h) {
-  auto fn = solid_patch_kernel<POLE, MODE>;
-  CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, solid_smem_bytes<POLE, MODE>()));
+// sets the kernel's shared-memory attributes; *ctas = resident CTAs on the GPU
+template <int POLE, int MODE, bool ANEL>
+int prepare_solid_kernel(axg_handle *h, int *ctas) {
+  auto fn = solid_patch_kernel<POLE, MODE, ANEL>;
+  constexpr int bytes = solid_smem_bytes<POLE, MODE, ANEL>();
+  CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   CK(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, solid_smem_bytes<POLE, MODE>()));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, bytes));
   if (per_sm < 1) return fail(h, AXG_ERR_CUDA, "solid kernel does not fit on an SM");
-  h->solid_ctas = per_sm * h->num_sms;
+  *ctas = per_sm * h->num_sms;
   return AXG_OK;
 }
 
-template <int POLE, int MODE>
+template <int POLE>
+int prepare_solid_kernels(axg_handle *h) {
+  int rc = prepare_solid_kernel<POLE, MODE_FORCE, false>(h, &h->solid_ctas);
+  if (rc) return rc;
+  if (h->anel) return prepare_solid_kernel<POLE, MODE_NEWMARK, true>(h, &h->solid_ctas_step);
+  return prepare_solid_kernel<POLE, MODE_NEWMARK, false>(h, &h->solid_ctas_step);
+}
+
+template <int POLE, int MODE, bool ANEL>
 void launch_solid_colours(axg_handle *h, cudaStream_t s) {
   DomainArgs a = domain_args(h->ds, h->ps);
   StateArgs st = solid_state(h);
+  const int ctas = MODE == MODE_FORCE ? h->solid_ctas : h->solid_ctas_step;
   for (int c = 0; c < h->ps.n_colours; ++c) {
     a.patch_begin = h->ps.colour_start[c];
     const int n = h->ps.colour_start[c + 1] - h->ps.colour_start[c];
-    const int grid = std::min(n, h->solid_ctas);
-    solid_patch_kernel<POLE, MODE><<<grid, kThreads, solid_smem_bytes<POLE, MODE>(), s>>>(a, st, h->spec, n);
+    const int grid = std::min(n, ctas);
+    solid_patch_kernel<POLE, MODE, ANEL>
+        <<<grid, kThreads, solid_smem_bytes<POLE, MODE, ANEL>(), s>>>(a, st, h->spec, n, h->an);
   }
+}
+
+template <int POLE, int MODE>
+void launch_solid_pole(axg_handle *h, cudaStream_t s) {
+  if (MODE == MODE_NEWMARK && h->anel) launch_solid_colours<POLE, MODE_NEWMARK, true>(h, s);
+  else launch_solid_colours<POLE, MODE, false>(h, s);
 }
 
 template <int MODE>
 void launch_solid(axg_handle *h, cudaStream_t s) {
-  if (h->pole == AXG_MONOPOLE) launch_solid_colours<POLE_MONO, MODE>(h, s);
-  else if (h->pole == AXG_DIPOLE) launch_solid_colours<POLE_DI, MODE>(h, s);
-  else launch_solid_colours<POLE_QUAD, MODE>(h, s);
+  if (h->pole == AXG_MONOPOLE) launch_solid_pole<POLE_MONO, MODE>(h, s);
+  else if (h->pole == AXG_DIPOLE) launch_solid_pole<POLE_DI, MODE>(h, s);
+  else launch_solid_pole<POLE_QUAD, MODE>(h, s);
 }
 
 __global__ void zero_points_kernel(const int32_t *gidx, int32_t n, float *f0, float *f1, float *f2) {
@@ -586,6 +623,80 @@ int check_igloc(const int32_t *ig, int64_t n, int64_t nglob, const char *what) {
   return AXG_OK;
 }
 
+// fast_correct (SOLVER/attenuation.f90:1139-1155): first-order correction of
+// the linearised SLS weights, yp_j = y_j * dy_j
+void sls_fast_correct(const double *y, double *yp, int n) {
+  double dy = 1.0 + 0.5 * y[0];
+  yp[0] = y[0] * dy;
+  for (int k = 1; k < n; ++k) {
+    dy = dy + (dy - 0.5) * y[k - 1] + 0.5 * y[k];
+    yp[k] = y[k] * dy;
+  }
+}
+
+// Attenuation tables of the time loop (SOLVER/attenuation.f90:81-202):
+//  * per distinct Q value a row ts_fac_t(j) a_j(Q), ts_fac_tm1(j) a_j(Q), with
+//    a_j = yp_j / sum(yp_j), yp_j = y_j / Q (fast_correct'ed when
+//    do_corr_lowq), computed in double as the reference does (:113-131) and
+//    rounded to float once;
+//  * per element (launch order) the cg4 constants and the two row indices;
+//  * the per-element state, zeroed by axg_reset.
+int build_anel(axg_handle *h, const axg_mesh_desc *d) {
+  const int nsls = d->n_sls;
+  const int64_t nel = h->nel_s;
+  const DomainPlan &pl = h->ps;
+  std::map<float, int32_t> qrow;
+  std::vector<float> qtab;
+  auto row = [&](float Q) {
+    auto it = qrow.find(Q);
+    if (it != qrow.end()) return it->second;
+    double y[kMaxSls], yp[kMaxSls], sum = 0.0;
+    for (int j = 0; j < nsls; ++j) y[j] = d->y_j_attenuation[j] / (double)Q;
+    if (d->do_corr_lowq) sls_fast_correct(y, yp, nsls);
+    else for (int j = 0; j < nsls; ++j) yp[j] = y[j];
+    for (int j = 0; j < nsls; ++j) sum += yp[j];
+    const int32_t r = (int32_t)qrow.size();
+    qtab.resize((size_t)(r + 1) * 2 * kMaxSls, 0.f);
+    for (int j = 0; j < nsls; ++j) {
+      const double a = yp[j] / sum;
+      qtab[(size_t)r * 2 * kMaxSls + j] = (float)(d->ts_fac_t[j] * a);
+      qtab[(size_t)r * 2 * kMaxSls + kMaxSls + j] = (float)(d->ts_fac_tm1[j] * a);
+    }
+    qrow[Q] = r;
+    return r;
+  };
+  std::vector<float> consts((size_t)nel * kAnelConst, 0.f);
+  const float *fields[11] = {d->delta_mu_cg4, d->delta_kappa_cg4, d->Y_cg4,  d->V_s_eta_cg4,
+                             d->V_s_xi_cg4,   d->V_z_eta_cg4,    d->V_z_xi_cg4, d->DsDeta_over_J_sol_cg4,
+                             d->DzDeta_over_J_sol_cg4, d->DsDxi_over_J_sol_cg4, d->DzDxi_over_J_sol_cg4};
+  const int cg_pt[4] = {1 + 5 * 1, 1 + 5 * 3, 3 + 5 * 1, 3 + 5 * 3};
+  for (int64_t s = 0; s < nel; ++s) {
+    const int64_t e = pl.elem_order[s];
+    float *c = consts.data() + (size_t)s * kAnelConst;
+    for (int f = 0; f < 11; ++f)
+      for (int k = 0; k < 4; ++k) c[4 * f + k] = fields[f][4 * e + k];
+    for (int k = 0; k < 4; ++k) c[A_INVS + k] = d->inv_s_solid[25 * e + cg_pt[k]];
+    const int32_t qm = row(d->Q_mu[e]), qk = row(d->Q_kappa[e]);
+    std::memcpy(c + A_QMU, &qm, 4);
+    std::memcpy(c + A_QKA, &qk, 4);
+  }
+  h->nsls = nsls;
+  h->an.nsls = nsls;
+  h->an.state_stride = anel_state_stride(nsls);
+  h->an.n_q = (int32_t)qrow.size();
+  for (int j = 0; j < kMaxSls; ++j) h->an.ex[j] = j < nsls ? (float)d->exp_w_j_deltat[j] : 0.f;
+  h->slot_of_elem_s.assign(nel, 0);
+  for (int64_t s = 0; s < nel; ++s) h->slot_of_elem_s[pl.elem_order[s]] = (int32_t)s;
+  int rc;
+  float *cp = nullptr, *qp = nullptr;
+  if ((rc = upload(h, &cp, consts))) return rc;
+  if ((rc = upload(h, &qp, qtab))) return rc;
+  h->an.consts = cp;
+  h->an.qtab = qp;
+  if ((rc = dalloc(h, &h->an.state, (size_t)nel * h->an.state_stride))) return rc;
+  return AXG_OK;
+}
+
 }  // namespace
 
 extern "C" int axg_reset(axg_handle *h);
@@ -607,6 +718,7 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
   h->absorbing = d->have_absorbing_bc != 0;
   h->dt = d->deltat;
   h->magnitude = d->magnitude;
+  h->anel = d->anel_true != 0;
   h->igloc_s.assign(d->igloc_solid, d->igloc_solid + 25 * h->nel_s);
   if (h->nel_f > 0) h->igloc_f.assign(d->igloc_fluid, d->igloc_fluid + 25 * h->nel_f);
   for (int64_t p = 0; p < 25 * h->nel_s; ++p)
@@ -724,16 +836,11 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
   h->blowup = h->iter + 1;
   h->errw = h->iter + 2;
   CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
-  if (h->pole == AXG_MONOPOLE) {
-    if ((rc = prepare_solid_kernel<POLE_MONO, MODE_FORCE>(h)) || (rc = prepare_solid_kernel<POLE_MONO, MODE_NEWMARK>(h)))
-      return rc;
-  } else if (h->pole == AXG_DIPOLE) {
-    if ((rc = prepare_solid_kernel<POLE_DI, MODE_FORCE>(h)) || (rc = prepare_solid_kernel<POLE_DI, MODE_NEWMARK>(h)))
-      return rc;
-  } else {
-    if ((rc = prepare_solid_kernel<POLE_QUAD, MODE_FORCE>(h)) || (rc = prepare_solid_kernel<POLE_QUAD, MODE_NEWMARK>(h)))
-      return rc;
-  }
+  if (h->anel && (rc = build_anel(h, d))) return rc;
+  if (h->pole == AXG_MONOPOLE) rc = prepare_solid_kernels<POLE_MONO>(h);
+  else if (h->pole == AXG_DIPOLE) rc = prepare_solid_kernels<POLE_DI>(h);
+  else rc = prepare_solid_kernels<POLE_QUAD>(h);
+  if (rc) return rc;
   if ((rc = upload_coupling(h, cf, h->to_fluid))) return rc;
   if ((rc = upload_coupling(h, cs, h->to_solid))) return rc;
   h->to_fluid.nglob_recv = h->nglob_f;
@@ -773,8 +880,8 @@ NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
 
 template <int POLE>
 int noalloc_prepare_kernel(int nsm, int *cap) {
-  auto fn = solid_patch_kernel<POLE, MODE_FORCE>;
-  const int bytes = solid_smem_bytes<POLE, MODE_FORCE>();
+  auto fn = solid_patch_kernel<POLE, MODE_FORCE, false>;
+  const int bytes = solid_smem_bytes<POLE, MODE_FORCE, false>();
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   int per_sm = 0;
@@ -817,8 +924,8 @@ void noalloc_launch(const DomainArgs &a0, const StateArgs &st, const SpecDev &sp
   for (int c = 0; c < pl.n_colours; ++c) {
     a.patch_begin = pl.colour_start[c];
     const int n = pl.colour_start[c + 1] - pl.colour_start[c];
-    solid_patch_kernel<POLE, MODE_FORCE><<<std::min(n, cap), kThreads, solid_smem_bytes<POLE, MODE_FORCE>(), 0>>>(
-        a, st, sp, n);
+    solid_patch_kernel<POLE, MODE_FORCE, false>
+        <<<std::min(n, cap), kThreads, solid_smem_bytes<POLE, MODE_FORCE, false>(), 0>>>(a, st, sp, n, AnelArgs{});
   }
 }
 
@@ -937,6 +1044,32 @@ extern "C" int axg_stiffness_assembled_noalloc(const axg_mesh_desc *d, const flo
   return AXG_OK;
 }
 
+namespace {
+// Reads (out) or writes (in) one attenuation state field in the reference's
+// layouts: memory_var_cg4(1:4,6,n_sls,nel_solid), src_tr_tm1_glob_cg4(1:4,
+// nel_solid), src_dev_tm1_glob_cg4(1:4,6,nel_solid).
+int anel_state_io(axg_handle *h, int field, float *out, const float *in) {
+  if (field != AXG_FIELD_MEMVAR && field != AXG_FIELD_ATT_SRC_TR && field != AXG_FIELD_ATT_SRC_DEV)
+    return fail(h, AXG_ERR_BAD_ARG, fmt("field %d not available", field));
+  if (!h->anel) return fail(h, AXG_ERR_BAD_ARG, "the handle was created without attenuation (anel_true = 0)");
+  const int64_t nel = h->nel_s, stride = h->an.state_stride;
+  const int nsls = h->nsls;
+  int off = 0, len = 24 * nsls;  // floats per element of this field, and where they start in the state
+  if (field == AXG_FIELD_ATT_SRC_TR) off = 24 * nsls, len = 4;
+  if (field == AXG_FIELD_ATT_SRC_DEV) off = 24 * nsls + 4, len = 24;
+  std::vector<float> st((size_t)nel * stride);
+  CK(cudaMemcpyAsync(st.data(), h->an.state, st.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int64_t e = 0; e < nel; ++e) {
+    float *blk = st.data() + (size_t)h->slot_of_elem_s[e] * stride + off;
+    if (out) std::memcpy(out + (size_t)e * len, blk, len * sizeof(float));
+    else std::memcpy(blk, in + (size_t)e * len, len * sizeof(float));
+  }
+  if (in) CK(cudaMemcpy(h->an.state, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return AXG_OK;
+}
+}  // namespace
+
 // ============================================================== C-ABI
 
 extern "C" {
@@ -987,6 +1120,8 @@ int axg_reset(axg_handle *h) {
   // the iter-0 seismogram sample (dump_stuff(0,...)) is the zero wavefield
   CK(cudaMemsetAsync(h->rec, 0, (size_t)h->nseismo * 3 * std::max(h->num_rec, 1) * sizeof(float), h->stream));
   CK(cudaMemsetAsync(h->iter, 0, 4 * sizeof(int32_t), h->stream));
+  if (h->anel)
+    CK(cudaMemsetAsync(h->an.state, 0, (size_t)h->nel_s * h->an.state_stride * sizeof(float), h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return AXG_OK;
 }
@@ -1045,7 +1180,7 @@ int axg_get_receivers(axg_handle *h, float *out, int32_t cap, int32_t *nseismo_o
 
 int axg_get_state(axg_handle *h, int32_t field, float *out) {
   if (!h || !out) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
-  if (field == AXG_FIELD_MEMVAR) return fail(h, AXG_ERR_UNSUPPORTED, "attenuation is not implemented in this build");
+  if (field >= AXG_FIELD_MEMVAR) return anel_state_io(h, field, out, nullptr);
   float *p[3] = {};
   int nc;
   int64_t ng;
@@ -1069,7 +1204,7 @@ int axg_get_state(axg_handle *h, int32_t field, float *out) {
 
 int axg_set_state(axg_handle *h, int32_t field, const float *in) {
   if (!h || !in) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
-  if (field == AXG_FIELD_MEMVAR) return fail(h, AXG_ERR_UNSUPPORTED, "attenuation is not implemented in this build");
+  if (field >= AXG_FIELD_MEMVAR) return anel_state_io(h, field, nullptr, in);
   float *p[3] = {};
   int nc;
   int64_t ng;

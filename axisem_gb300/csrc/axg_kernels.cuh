@@ -184,14 +184,20 @@ __device__ __forceinline__ float ldm(const float *blk, int slot, int lane) { ret
 // ------------------------------------------------------------ element stiffness
 
 // glob_stiffness_mono_4 (SOLVER/stiffness_mono.f90:60-157) for lane (i, j)
+// gx[c], ge[c] receive the first-stage derivatives d/dxi (mxm_4(G2T or G1T, u))
+// and d/deta (mxm_4(u, G2)) of component c at the lane's point, the inputs of
+// the cg4 strain (SOLVER/pointwise_derivatives.f90:216-250)
 template <bool AX>
 __device__ __forceinline__ void stiff_mono(const LaneCoef &c, const float *blk, const float *m0, int lane,
-                                           int i, int j, float us, float uz, float &fs, float &fz) {
+                                           int i, int j, float us, float uz, float &fs, float &fz,
+                                           float (&gx)[3], float (&ge)[3]) {
   const int j5 = 5 * j;
   float X1 = dxi(us, cxi<AX>(c), j5);
   float X2 = dxi(uz, cxi<AX>(c), j5);
   float X3 = deta(us, c.eta, i);
   float X4 = deta(uz, c.eta, i);
+  gx[0] = X1; gx[1] = 0.f; gx[2] = X2;
+  ge[0] = X3; ge[1] = 0.f; ge[2] = X4;
   const float m1 = ldm(blk, S_M1, lane), m2 = ldm(blk, S_M2, lane), m3 = ldm(blk, S_M3, lane),
               m4 = ldm(blk, S_M4, lane), mw1 = ldm(blk, S_MW1, lane);
   const float m11s = ldm(blk, S_M11S, lane), m21s = ldm(blk, S_M21S, lane), m41s = ldm(blk, S_M41S, lane),
@@ -230,10 +236,13 @@ __device__ __forceinline__ void stiff_mono(const LaneCoef &c, const float *blk, 
 // glob_stiffness_di_4 (SOLVER/stiffness_di.f90:60-256)
 template <bool AX>
 __device__ __forceinline__ void stiff_di(const LaneCoef &c, const float *blk, const float *m0, int lane, int i,
-                                         int j, float u1, float u2, float u3, float &f1, float &f2, float &f3) {
+                                         int j, float u1, float u2, float u3, float &f1, float &f2, float &f3,
+                                         float (&gx)[3], float (&ge)[3]) {
   const int j5 = 5 * j;
   float X4 = deta(u1, c.eta, i), X5 = deta(u2, c.eta, i), X6 = deta(u3, c.eta, i);
   float X1 = dxi(u1, cxi<AX>(c), j5), X2 = dxi(u2, cxi<AX>(c), j5), X3 = dxi(u3, cxi<AX>(c), j5);
+  gx[0] = X1; gx[1] = X2; gx[2] = X3;
+  ge[0] = X4; ge[1] = X5; ge[2] = X6;
   const float X7 = X1 + X2, X8 = X4 + X5;
   const float m1 = ldm(blk, S_M1, lane), m2 = ldm(blk, S_M2, lane), m3 = ldm(blk, S_M3, lane),
               m4 = ldm(blk, S_M4, lane), m5 = ldm(blk, S_M5, lane), m6 = ldm(blk, S_M6, lane),
@@ -295,10 +304,12 @@ __device__ __forceinline__ void stiff_di(const LaneCoef &c, const float *blk, co
 template <bool AX>
 __device__ __forceinline__ void stiff_quad(const LaneCoef &c, const float *blk, const float *m0, int lane,
                                            int i, int j, float us, float up, float uz, float &f1, float &f2,
-                                           float &f3) {
+                                           float &f3, float (&gx)[3], float (&ge)[3]) {
   const int j5 = 5 * j;
   float X1 = dxi(us, cxi<AX>(c), j5), X2 = dxi(up, cxi<AX>(c), j5), X3 = dxi(uz, cxi<AX>(c), j5);
   float X4 = deta(us, c.eta, i), X5 = deta(up, c.eta, i), X6 = deta(uz, c.eta, i);
+  gx[0] = X1; gx[1] = X2; gx[2] = X3;
+  ge[0] = X4; ge[1] = X5; ge[2] = X6;
   const float m1 = ldm(blk, S_M1, lane), m2 = ldm(blk, S_M2, lane), m3 = ldm(blk, S_M3, lane),
               m4 = ldm(blk, S_M4, lane), m5 = ldm(blk, S_M5, lane), m6 = ldm(blk, S_M6, lane),
               m7 = ldm(blk, S_M7, lane), m8 = ldm(blk, S_M8, lane);
@@ -366,20 +377,206 @@ __device__ __forceinline__ float stiff_fluid(const LaneCoef &c, const float *blk
   return loc;
 }
 
+// ------------------------------------------------------------ attenuation (cg4)
+//
+// Coarse-grained SLS attenuation: memory variables live at the four GLL
+// points (1,1), (1,3), (3,1), (3,3) of every solid element, the lanes 6, 16,
+// 8, 18 of the element's warp ("cg lanes", cg index k = 0..3 in that order,
+// the order of the reference's (1:4) arrays).
+//
+// Per element (launch order) the host packs two arrays:
+//   constants, kAnelConst floats: [field][k] for the fields below, then the
+//     two Q-table rows (int32 bits) of Q_mu and Q_kappa;
+//   state, anel_state_stride(n_sls) floats: memory_var_cg4(1:4,6,n_sls) in
+//     the reference's order, src_tr_tm1(1:4), src_dev_tm1(1:4,6).
+// Both travel with the element's metric block into the warp's ring; the
+// updated state is written back from shared memory.
+constexpr int kMaxSls = 8;
+enum : int {
+  A_DMU = 0, A_DKA = 4, A_Y = 8, A_VSE = 12, A_VSX = 16, A_VZE = 20, A_VZX = 24,
+  A_DSDETA = 28, A_DZDETA = 32, A_DSDXI = 36, A_DZDXI = 40, A_INVS = 44, A_QMU = 48, A_QKA = 49
+};
+constexpr int kAnelConst = 52;  // floats, a 16-byte multiple
+__host__ __device__ constexpr int anel_state_stride(int nsls) { return ((24 * nsls + 28 + 3) / 4) * 4; }
+constexpr int kAnelSlot = kAnelConst + anel_state_stride(kMaxSls);  // floats per ring slot
+
+struct AnelArgs {
+  const float *consts;      // per element kAnelConst floats (launch order)
+  float *state;             // per element state_stride floats (launch order)
+  const float *qtab;        // per distinct Q: ts_fac_t(j) a_j(Q) at [0, kMaxSls), ts_fac_tm1(j) a_j(Q) after
+  float ex[kMaxSls];        // exp_w_j_deltat
+  int32_t nsls, state_stride, n_q;
+};
+
+// Anelastic stiffness (glob_anel_stiffness_{mono,di,quad}_cg4,
+// SOLVER/stiffness_mono.f90:511, SOLVER/stiffness_di.f90:727,
+// SOLVER/stiffness_quad.f90:672) for lane (i, j): subtracts the divergence of
+// the summed memory-variable stress from f.  The sparse products
+// mxm_cg4_sparse_b(G, S1) and mxm_cg4_sparse_a(S2, G2T) of
+// SOLVER/unrolled_loops.f90 become two shuffles each: X1(i,j) for j in {1,3}
+// takes S1 at (1,j), (3,j); X2(i,j) for i in {1,3} takes S2 at (i,1), (i,3).
+template <int POLE, bool AX>
+__device__ __forceinline__ void anel_stiffness(const LaneCoef &c, const float *cs, const float *R, int nsls,
+                                               bool cg, int k, int i, int j, bool active, float &f0, float &f1,
+                                               float &f2) {
+  float S1a = 0.f, S2a = 0.f, S1b = 0.f, S2b = 0.f, S1z = 0.f, S2z = 0.f;
+  float ya = 0.f, yb = 0.f, yz = 0.f;
+  if (cg) {
+    float r[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int q = 0; q < nsls; ++q)
+#pragma unroll
+      for (int v = 0; v < 6; ++v) r[v] = r[v] + R[(q * 6 + v) * 4 + k];
+    const float vse = cs[A_VSE + k], vsx = cs[A_VSX + k], vze = cs[A_VZE + k], vzx = cs[A_VZX + k];
+    const float yl = cs[A_Y + k];
+    if (POLE == POLE_DI) {
+      S1a = vze * (r[0] - r[5]) + vse * (r[4] - r[3]);
+      S2a = vzx * (r[0] - r[5]) + vsx * (r[4] - r[3]);
+      S1b = vze * (r[0] + r[5]) + vse * (r[4] + r[3]);
+      S2b = vzx * (r[0] + r[5]) + vsx * (r[4] + r[3]);
+    } else {
+      S1a = vze * r[0] + vse * r[4];
+      S2a = vzx * r[0] + vsx * r[4];
+      if (POLE == POLE_QUAD) {
+        S1b = vze * r[5] + vse * r[3];
+        S2b = vzx * r[5] + vsx * r[3];
+      }
+    }
+    S1z = vze * r[4] + vse * r[2];
+    S2z = vzx * r[4] + vsx * r[2];
+    if (POLE == POLE_MONO) {
+      ya = yl * r[1];
+    } else if (POLE == POLE_DI) {
+      yb = 2.f * yl * (r[1] - r[5]);
+      yz = -(yl * r[3]);
+    } else {
+      ya = yl * (r[1] - 2.f * r[5]);
+      yb = yl * (r[5] - 2.f * r[1]);
+      yz = -(2.f * yl * r[3]);
+    }
+  }
+  const bool jc = active && (j == 1 || j == 3), ic = active && (i == 1 || i == 3);
+  const int sj1 = 1 + 5 * j, sj3 = 3 + 5 * j, si1 = i + 5, si3 = i + 15;
+  const float gi1 = csxi<AX>(c)[1], gi3 = csxi<AX>(c)[3];  // G(i,1), G(i,3); G = G1 on axial elements
+  const float g1j = c.seta[1], g3j = c.seta[3];            // G2T(1,j), G2T(3,j)
+  auto x1 = [&](float S) {
+    const float p = __shfl_sync(kFull, S, sj1), q = __shfl_sync(kFull, S, sj3);
+    return jc ? gi1 * p + gi3 * q : 0.f;
+  };
+  auto x2 = [&](float S) {
+    const float p = __shfl_sync(kFull, S, si1), q = __shfl_sync(kFull, S, si3);
+    return ic ? p * g1j + q * g3j : 0.f;
+  };
+  const float la = x1(S1a) + x2(S2a) + ya;
+  const float lz = x1(S1z) + x2(S2z) + yz;
+  f0 = f0 - la;
+  f2 = f2 - lz;
+  if (POLE == POLE_DI) {
+    const float lb = x1(S1b) + x2(S2b) + yb;
+    f1 = f1 - lb;
+  } else if (POLE == POLE_QUAD) {
+    const float lb = (-x1(S1b) - x2(S2b)) + yb;
+    f1 = f1 - lb;
+  }
+}
+
+// Memory-variable time step of one cg lane (time_step_memvars_cg4,
+// SOLVER/attenuation.f90:81-202) with the strain of
+// compute_strain_att_el_cg4 (:471-535): gx, ge are the lane's first-stage
+// derivatives d/dxi, d/deta of the three displacement components, u its
+// (predicted, axis-masked) displacement.  The gradient at a cg point is
+// axisym_gradient_solid_el_cg4 (SOLVER/pointwise_derivatives.f90:216-250),
+// f/s is f_over_s_solid_el_cg4 (:55-75) with the stored 1/s.  Updates the
+// state R (shared memory) in place.
+template <int POLE>
+__device__ __forceinline__ void anel_memvar_step(const float *cs, float *R, const AnelArgs &an, int k,
+                                                 const float (&u)[3], const float (&gx)[3], const float (&ge)[3]) {
+  const float dsdeta = cs[A_DSDETA + k], dzdeta = cs[A_DZDETA + k];
+  const float dsdxi = cs[A_DSDXI + k], dzdxi = cs[A_DZDXI + k], invs = cs[A_INVS + k];
+  auto grad_s = [&](float m1, float m2) { return dzdeta * m1 + dzdxi * m2; };
+  auto grad_z = [&](float m1, float m2) { return dsdeta * m1 + dsdxi * m2; };
+  float g[6];
+  float b1x = gx[0], b1e = ge[0];
+  if (POLE == POLE_DI) {
+    b1x = gx[0] + gx[1];
+    b1e = ge[0] + ge[1];
+  }
+  const float b1s = grad_s(b1x, b1e), b1z = grad_z(b1x, b1e);
+  const float b2s = grad_s(gx[2], ge[2]), b2z = grad_z(gx[2], ge[2]);
+  g[0] = b1s;
+  g[2] = b2z;
+  g[4] = b1z + b2s;
+  if (POLE == POLE_MONO) {
+    g[1] = invs * u[0];
+    g[3] = 0.f;
+    g[5] = 0.f;
+  } else if (POLE == POLE_DI) {
+    g[1] = 2.f * (invs * u[1]);
+    const float cx = gx[0] - gx[1], ce = ge[0] - ge[1];
+    g[3] = -(invs * u[2]) - grad_z(cx, ce);
+    g[5] = -g[1] - grad_s(cx, ce);
+  } else {
+    g[1] = invs * (u[0] - 2.f * u[1]);
+    g[3] = -2.f * (invs * u[2]) - grad_z(gx[1], ge[1]);
+    g[5] = invs * (u[1] - 2.f * u[0]) - grad_s(gx[1], ge[1]);
+  }
+  const float tr = g[0] + g[1] + g[2];
+  const float dm = cs[A_DMU + k], dka = cs[A_DKA + k];
+  const float src_tr = dka * tr;
+  float sd[6];
+#pragma unroll
+  for (int v = 0; v < 3; ++v) sd[v] = (dm * 2.f) * (g[v] - tr * (1.f / 3.f));
+  sd[4] = dm * g[4];
+  sd[3] = POLE == POLE_MONO ? 0.f : dm * g[3];
+  sd[5] = POLE == POLE_MONO ? 0.f : dm * g[5];
+  const int nsls = an.nsls;
+  float *trm1 = R + 24 * nsls, *dm1 = trm1 + 4;
+  const float tr_old = trm1[k];
+  float dev_old[6];
+#pragma unroll
+  for (int v = 0; v < 6; ++v) dev_old[v] = dm1[v * 4 + k];
+  int qmu = __float_as_int(cs[A_QMU]), qka = __float_as_int(cs[A_QKA]);
+  if (!AXG_BOUND(qmu, an.n_q, 4)) qmu = 0;
+  if (!AXG_BOUND(qka, an.n_q, 4)) qka = 0;
+  const float *tmu = an.qtab + qmu * 2 * kMaxSls, *tka = an.qtab + qka * 2 * kMaxSls;
+  for (int q = 0; q < nsls; ++q) {
+    const float ctm = __ldg(tmu + q), ctm1m = __ldg(tmu + kMaxSls + q);
+    const float ctk = __ldg(tka + q), ctm1k = __ldg(tka + kMaxSls + q);
+    const float e = an.ex[q];
+    const float trb = ctk * src_tr + ctm1k * tr_old;
+    float *Rq = R + q * 24 + k;
+#pragma unroll
+    for (int v = 0; v < 6; ++v) {
+      if (POLE == POLE_MONO && (v == 3 || v == 5)) continue;
+      const float db = ctm * sd[v] + ctm1m * dev_old[v];
+      float nv = e * Rq[v * 4] + db;
+      if (v < 3) nv = nv + trb;
+      Rq[v * 4] = nv;
+    }
+  }
+  trm1[k] = src_tr;
+#pragma unroll
+  for (int v = 0; v < 6; ++v) dm1[v * 4 + k] = sd[v];
+}
+
 // ------------------------------------------------------------ solid patch kernel
 
 constexpr int kStages = 3;  // element blocks in flight per warp (TMA ring depth)
 
-// shared-memory layout of the solid kernel (bytes)
-template <int NC, int BS>
+// shared-memory layout of the solid kernel (bytes); STG ring stages per warp,
+// AS floats of attenuation data per stage (0 without attenuation)
+template <int NC, int BS, int STG, int AS>
 struct SolidSmem {
   static constexpr int u_off = 0;
   static constexpr int f_off = u_off + NC * kMaxPatchPoints * 4;
   static constexpr int w_off = f_off + NC * kMaxPatchPoints * 4;
   static constexpr int ring_off = ((w_off + kMaxPatchPoints * 4 + 127) / 128) * 128;
-  static constexpr int bar_off = ring_off + kWarps * kStages * BS * 4;
-  static constexpr int bytes = bar_off + kWarps * kStages * 8;
+  static constexpr int aring_off = ring_off + kWarps * STG * BS * 4;
+  static constexpr int bar_off = aring_off + kWarps * STG * AS * 4;
+  static constexpr int bytes = bar_off + kWarps * STG * 8;
 };
+// ring depth: three element blocks in flight, two with attenuation (keeps two
+// CTAs per SM)
+__host__ __device__ constexpr int solid_stages(bool anel) { return anel ? 2 : kStages; }
 
 // the elements warp `w` processes in a patch, in order: sub-round by
 // sub-round, elements w, w + kWarps, ... of each round
@@ -394,26 +591,33 @@ struct WarpIter {
   __device__ __forceinline__ bool valid(const PatchMeta &m) const { return r < m.n_rounds; }
 };
 
-template <int POLE, int MODE>
+// ANEL (time loop only): attenuation of the solid, the anelastic stiffness
+// before the axis mask of acc1 and the memory-variable step after it, as in
+// SOLVER/time_evol_wave.F90 (anel_true, cg4).
+template <int POLE, int MODE, bool ANEL>
 __global__ void __launch_bounds__(kThreads, 2)
-    solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches) {
+    solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches, AnelArgs an) {
+  static_assert(!ANEL || MODE == MODE_NEWMARK, "attenuation runs in the time loop only");
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
   constexpr int NT = n_terms(POLE), NA = n_axial(POLE);
   constexpr int BS = solid_block_stride(NT);
   constexpr uint32_t BSB = BS * 4;
-  using L = SolidSmem<NC, BS>;
+  constexpr int STG = solid_stages(ANEL);
+  constexpr int AS = ANEL ? kAnelSlot : 0;
+  using L = SolidSmem<NC, BS, STG, AS>;
   extern __shared__ __align__(128) unsigned char smem[];
   float(*s_u)[kMaxPatchPoints] = reinterpret_cast<float(*)[kMaxPatchPoints]>(smem + L::u_off);
   float(*s_f)[kMaxPatchPoints] = reinterpret_cast<float(*)[kMaxPatchPoints]>(smem + L::f_off);
   uint32_t *s_w = reinterpret_cast<uint32_t *>(smem + L::w_off);
   float *ring = reinterpret_cast<float *>(smem + L::ring_off);
+  float *aring = reinterpret_cast<float *>(smem + L::aring_off);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bar_off);
   __shared__ int s_stop;
   // component c of the shared arrays -> global component (mono: s, z)
   auto gc = [](int c) { return (POLE == POLE_MONO && c == 1) ? 2 : c; };
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x < kWarps * kStages) mbar_init(&bars[threadIdx.x], 1);
+  if (threadIdx.x < kWarps * STG) mbar_init(&bars[threadIdx.x], 1);
   if (threadIdx.x == 0) s_stop = (MODE == MODE_NEWMARK) ? *st.blowup : 0;
   fence_mbar_init();
   __syncthreads();
@@ -427,9 +631,26 @@ __global__ void __launch_bounds__(kThreads, 2)
   LaneCoef coef;
   load_coef(sp, i, j, coef);
   const uint64_t pol = policy_evict_first();
-  float *my_ring = ring + warp * kStages * BS;
-  uint64_t *my_bars = bars + warp * kStages;
-  uint32_t kcount = 0;  // elements this warp has consumed (slot = kcount % kStages)
+  float *my_ring = ring + warp * STG * BS;
+  float *my_aring = aring + warp * STG * AS;
+  uint64_t *my_bars = bars + warp * STG;
+  uint32_t kcount = 0;  // elements this warp has consumed (slot = kcount % STG)
+  // cg lane index k of the attenuation points (1,1), (1,3), (3,1), (3,3)
+  const bool cg = active && (i == 1 || i == 3) && (j == 1 || j == 3);
+  const int kcg = 2 * (i >> 1) + (j >> 1);
+  const uint32_t state_bytes = ANEL ? (uint32_t)an.state_stride * 4u : 0u;
+  // one thread: start the copies of element `el` into ring slot `slot`
+  auto issue = [&](uint32_t slot, int64_t el) {
+    if (ANEL) {
+      mbar_expect_tx(&my_bars[slot], BSB + kAnelConst * 4 + state_bytes);
+      bulk_g2s_tx(my_ring + slot * BS, d.metric + el * BS, BSB, &my_bars[slot], pol);
+      bulk_g2s_tx(my_aring + slot * AS, an.consts + el * kAnelConst, kAnelConst * 4, &my_bars[slot], pol);
+      bulk_g2s_tx(my_aring + slot * AS + kAnelConst, an.state + el * an.state_stride, state_bytes, &my_bars[slot],
+                  pol);
+    } else {
+      bulk_g2s(my_ring + slot * BS, d.metric + el * BS, BSB, &my_bars[slot], pol);
+    }
+  };
   float stf1 = 0.f;
   if (MODE == MODE_NEWMARK && AXG_BOUND(*st.iter - 1, st.niter, 3)) stf1 = st.stf[*st.iter - 1];
 
@@ -437,16 +658,13 @@ __global__ void __launch_bounds__(kThreads, 2)
     if (!AXG_BOUND(d.patch_begin + pp, d.n_patches, 1)) break;
     const PatchMeta m = d.meta[d.patch_begin + pp];
 
-    // 0. start the bulk copies of this warp's first kStages element blocks
+    // 0. start the bulk copies of this warp's first STG element blocks
     WarpIter pf{0, warp};
     pf.norm(m, warp);
-    for (int q = 0; q < kStages && pf.valid(m); ++q) {
+    for (int q = 0; q < STG && pf.valid(m); ++q) {
       if (lane == 0) {
         const int64_t el = (int64_t)m.elem_start + pf.s;
-        if (AXG_BOUND(el, d.n_elem, 2)) {
-          const uint32_t slot = (kcount + q) % kStages;
-          bulk_g2s(my_ring + slot * BS, d.metric + el * BS, BSB, &my_bars[slot], pol);
-        }
+        if (AXG_BOUND(el, d.n_elem, 2)) issue((kcount + q) % STG, el);
       }
       pf.s += kWarps;
       pf.norm(m, warp);
@@ -494,8 +712,8 @@ __global__ void __launch_bounds__(kThreads, 2)
       for (int s = r0 + warp; s < r1; s += kWarps) {
         int64_t el = (int64_t)m.elem_start + s;
         if (!AXG_BOUND(el, d.n_elem, 2)) el = 0;
-        const uint32_t slot = kcount % kStages;
-        mbar_wait_bounded(&my_bars[slot], (kcount / kStages) & 1u, st.err);
+        const uint32_t slot = kcount % STG;
+        mbar_wait_bounded(&my_bars[slot], (kcount / STG) & 1u, st.err);
         const float *blk = my_ring + slot * BS;
         const int32_t info = *reinterpret_cast<const int32_t *>(blk + solid_info_off(NT));
         int axslot = (info & 0xFFFFFF) - 1;
@@ -524,16 +742,22 @@ __global__ void __launch_bounds__(kThreads, 2)
           if (POLE == POLE_QUAD) { u[0] = 0.f; u[1] = 0.f; u[2] = 0.f; }
         }
         float f0, f1 = 0.f, f2;
+        float gx[3], ge[3];
         const float *m0 = ax ? d.m0 + (int64_t)axslot * (NA * 5) : nullptr;
         if (POLE == POLE_MONO) {
-          if (ax) stiff_mono<true>(coef, blk, m0, ml, i, j, u[0], u[2], f0, f2);
-          else stiff_mono<false>(coef, blk, m0, ml, i, j, u[0], u[2], f0, f2);
+          if (ax) stiff_mono<true>(coef, blk, m0, ml, i, j, u[0], u[2], f0, f2, gx, ge);
+          else stiff_mono<false>(coef, blk, m0, ml, i, j, u[0], u[2], f0, f2, gx, ge);
         } else if (POLE == POLE_DI) {
-          if (ax) stiff_di<true>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
-          else stiff_di<false>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
+          if (ax) stiff_di<true>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2, gx, ge);
+          else stiff_di<false>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2, gx, ge);
         } else {
-          if (ax) stiff_quad<true>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
-          else stiff_quad<false>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2);
+          if (ax) stiff_quad<true>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2, gx, ge);
+          else stiff_quad<false>(coef, blk, m0, ml, i, j, u[0], u[1], u[2], f0, f1, f2, gx, ge);
+        }
+        float *ablk = my_aring + slot * AS;  // attenuation constants, then state
+        if (ANEL) {
+          if (ax) anel_stiffness<POLE, true>(coef, ablk, ablk + kAnelConst, an.nsls, cg, kcg, i, j, active, f0, f1, f2);
+          else anel_stiffness<POLE, false>(coef, ablk, ablk + kAnelConst, an.nsls, cg, kcg, i, j, active, f0, f1, f2);
         }
         if (ax && i == 0) {  // axis mask of acc1
           if (POLE == POLE_MONO) f0 = 0.f;
@@ -549,13 +773,23 @@ __global__ void __launch_bounds__(kThreads, 2)
             s_f[2][idx] += f2;
           }
         }
-        // the slot is free again: start the copy of the element kStages ahead
+        if (ANEL) {
+          // memory variables of this step from the predicted, masked
+          // displacement (time_step_memvars after pdistsum_solid in
+          // SOLVER/time_evol_wave.F90), then the element's state back to HBM
+          if (cg) anel_memvar_step<POLE>(ablk, ablk + kAnelConst, an, kcg, u, gx, ge);
+          __syncwarp();
+          const float4 *src4 = reinterpret_cast<const float4 *>(ablk + kAnelConst);
+          float4 *dst4 = reinterpret_cast<float4 *>(an.state + el * an.state_stride);
+          for (int q = lane; q < an.state_stride / 4; q += 32) dst4[q] = src4[q];
+        }
+        // the slot is free again: start the copy of the element STG ahead
         __syncwarp();
         if (pf.valid(m)) {
           if (lane == 0) {
             const int64_t pel = (int64_t)m.elem_start + pf.s;
             fence_proxy_async();  // the warp's reads of the slot precede the async-proxy write
-            if (AXG_BOUND(pel, d.n_elem, 2)) bulk_g2s(my_ring + slot * BS, d.metric + pel * BS, BSB, &my_bars[slot], pol);
+            if (AXG_BOUND(pel, d.n_elem, 2)) issue(slot, pel);
           }
           pf.s += kWarps;
           pf.norm(m, warp);

@@ -43,6 +43,22 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
       : "memory");
 }
 
+// arm the barrier once for several copies that complete on it
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+// bulk copy completing on a barrier that mbar_expect_tx already armed
+__device__ __forceinline__ void bulk_g2s_tx(void *dst, const void *src, uint32_t bytes, uint64_t *bar,
+                                            uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(policy)
+      : "memory");
+}
+
 // L2 policy for data read once per step (the metric terms)
 __device__ __forceinline__ uint64_t policy_evict_first() {
   uint64_t p;

@@ -414,3 +414,46 @@ def coupled_mesh(ni: int, nj_solid: int, nj_fluid: int, src_type: int = _abi.MON
         [top * ni + recs + 1, np.full(num_rec, 2), np.full(num_rec, 4)], axis=1).astype(I32))
     m.magnitude = 1e20
     return m
+
+
+def add_attenuation(m: Mesh, n_sls: int = 5, seed: int = 77, do_corr_lowq: bool = True) -> Mesh:
+    """Seeded coarse-grained (cg4) attenuation data for a mesh.
+
+    SLS relaxation frequencies are log-spaced over the mesh's band and the
+    coefficients y_j positive; the time-stepping factors follow the exact
+    integration of the reference (SOLVER/attenuation.f90:882-887):
+        exp_w_j_deltat = exp(-w_j dt)
+        ts_fac_tm1     = (1 - exp_w_j_deltat) / (w_j dt) - exp_w_j_deltat
+        ts_fac_t       = (exp_w_j_deltat - 1) / (w_j dt) + 1
+    Q_mu / Q_kappa take a few PREM-like values per element (the reference's
+    Q is constant inside an element).  The per-element cg4 factors (the
+    modulus defects delta_mu/kappa, the weights Y and V of the anelastic
+    stiffness, the mapping derivatives of the strain and 1/s) are seeded
+    values with physical signs and scales."""
+    rng = np.random.default_rng(seed)
+    nel = m.nel_solid
+    dt = m.deltat
+    w = np.logspace(-1.3, 0.0, n_sls) / dt   # w_j dt from 0.05 to 1
+    y = rng.uniform(0.1, 1.0, n_sls)
+    ex = np.exp(-w * dt)
+    ts_tm1 = (1 - ex) / (w * dt) - ex
+    ts_t = (ex - 1) / (w * dt) + 1
+    qmu_vals = np.array([80.0, 143.0, 312.0, 600.0], dtype=F32)
+    qka_vals = np.array([1327.7, 57823.0], dtype=F32)
+    cg = lambda lo, hi: _f(rng.uniform(lo, hi, size=(4, nel)))  # noqa: E731
+    sgn = lambda lo, hi: _f(rng.uniform(lo, hi, size=(4, nel)) * rng.choice([-1.0, 1.0], size=(4, nel)))  # noqa: E731
+    inv_s = _f(rng.uniform(0.5, 2.0, size=(5, 5, nel)))
+    m.anel = {
+        "y_j": y, "exp_w_j_deltat": ex, "ts_fac_t": ts_t, "ts_fac_tm1": ts_tm1,
+        "do_corr_lowq": int(do_corr_lowq),
+        "Q_mu": qmu_vals[rng.integers(0, len(qmu_vals), nel)],
+        "Q_kappa": qka_vals[rng.integers(0, len(qka_vals), nel)],
+        "delta_mu_cg4": cg(1e9, 1e10), "delta_kappa_cg4": cg(1e9, 1e10),
+        "Y_cg4": cg(0.5, 5.0),
+        "V_s_eta_cg4": sgn(0.5, 5.0), "V_s_xi_cg4": sgn(0.5, 5.0),
+        "V_z_eta_cg4": sgn(0.5, 5.0), "V_z_xi_cg4": sgn(0.5, 5.0),
+        "DsDeta_over_J_sol_cg4": sgn(0.5, 2.0), "DzDeta_over_J_sol_cg4": sgn(0.5, 2.0),
+        "DsDxi_over_J_sol_cg4": sgn(0.5, 2.0), "DzDxi_over_J_sol_cg4": sgn(0.5, 2.0),
+        "inv_s_solid": inv_s,
+    }
+    return m

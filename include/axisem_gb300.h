@@ -135,7 +135,7 @@ typedef struct axg_mesh_desc {
 
   /* coarse-grained (cg4) attenuation (SOLVER/attenuation.f90:81-202) */
   int32_t anel_true;
-  int32_t n_sls;                                 /* n_sls_attenuation */
+  int32_t n_sls;                                 /* n_sls_attenuation, 1..8 */
   int32_t do_corr_lowq;
   int32_t att_coarse_grained;                    /* must be 1 when anel_true */
   const double *y_j_attenuation;                 /* (n_sls) */
@@ -153,11 +153,15 @@ typedef struct axg_handle axg_handle;
 
 /* State arrays for axg_get_state / axg_set_state, returned in the reference's
  * element-local layouts disp(0:4,0:4,nel_solid,3), chi(0:4,0:4,nel_fluid),
- * memory_var_cg4(1:4,6,n_sls,nel_solid). */
+ * memory_var_cg4(1:4,6,n_sls,nel_solid), and the attenuation source terms of
+ * the previous step src_tr_tm1_glob_cg4(1:4,nel_solid),
+ * src_dev_tm1_glob_cg4(1:4,6,nel_solid) (SOLVER/attenuation.f90:153-154,
+ * 196-197).  The three attenuation fields need a handle created with
+ * anel_true. */
 enum axg_field {
   AXG_FIELD_DISP = 0, AXG_FIELD_VELO, AXG_FIELD_ACC0,
   AXG_FIELD_CHI, AXG_FIELD_DCHI, AXG_FIELD_DDCHI0,
-  AXG_FIELD_MEMVAR
+  AXG_FIELD_MEMVAR, AXG_FIELD_ATT_SRC_TR, AXG_FIELD_ATT_SRC_DEV
 };
 
 /* Library build/version string; never NULL. */

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from axisem_gb300 import _abi
-from axisem_gb300.mesh import coupled_mesh, structured_mesh
+from axisem_gb300.mesh import add_attenuation, coupled_mesh, structured_mesh
 
 HEADER = Path(__file__).resolve().parents[1] / "include" / "axisem_gb300.h"
 
@@ -61,7 +61,12 @@ def _create(lib, desc):
     (lambda d: setattr(d, "src_type", 5), _abi.AXG_ERR_BAD_DESC, "src_type"),
     (lambda d: setattr(d, "nelsrc", 9), _abi.AXG_ERR_BAD_DESC, "nelsrc"),
     (lambda d: setattr(d, "seis_it", 0), _abi.AXG_ERR_BAD_DESC, "seis_it"),
-    (lambda d: setattr(d, "anel_true", 1), _abi.AXG_ERR_UNSUPPORTED, "attenuation"),
+    (lambda d: (setattr(d, "anel_true", 1), setattr(d, "att_coarse_grained", 0)), _abi.AXG_ERR_UNSUPPORTED,
+     "coarse-grained"),
+    (lambda d: (setattr(d, "anel_true", 1), setattr(d, "att_coarse_grained", 1)), _abi.AXG_ERR_UNSUPPORTED,
+     "n_sls"),
+    (lambda d: (setattr(d, "anel_true", 1), setattr(d, "att_coarse_grained", 1), setattr(d, "n_sls", 5)),
+     _abi.AXG_ERR_BAD_DESC, "attenuation arrays"),
 ])
 def test_descriptor_validation(lib, mutate, code, needle):
     m = coupled_mesh(6, 3, 2, 1, niter=10)
@@ -70,6 +75,18 @@ def test_descriptor_validation(lib, mutate, code, needle):
     rc, msg, h = _create(lib, d)
     assert rc == code and needle in msg
     assert not h.value
+
+
+def test_attenuation_descriptor_validation(lib):
+    m = add_attenuation(coupled_mesh(6, 3, 2, 2, niter=10))
+    d = m.desc()
+    d.n_sls = 9
+    rc, msg, h = _create(lib, d)
+    assert rc == _abi.AXG_ERR_UNSUPPORTED and "n_sls" in msg and not h.value
+    m.anel["Q_mu"] = m.anel["Q_mu"].copy()
+    m.anel["Q_mu"][3] = 0.0
+    rc, msg, h = _create(lib, m.desc())
+    assert rc == _abi.AXG_ERR_BAD_DESC and "Q_mu" in msg and not h.value
 
 
 def test_null_metric_array_rejected(lib):
