@@ -266,10 +266,11 @@ def run_gpu(args):
     if prof.exists():
         traffic = json.loads(prof.read_text()).get("dram_bytes_per_step")
 
-    timeloop = None
+    timeloop = timeloop_anel = None
     if args.timeloop_steps > 0:
         s.close()
         timeloop = run_timeloop(args, pole, ws, rank)
+        timeloop_anel = run_timeloop(args, pole, ws, rank, anel=True)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -296,6 +297,7 @@ def run_gpu(args):
                      "kernel": "solid_patch_kernel<quad,force> (all colour launches of one step)"},
         "cpu_baseline": cpu,
         "timeloop": timeloop,
+        "timeloop_anel": timeloop_anel,
         "clocks": clocks,
         "gpu_launches": int(args.steps * info["kernels_per_force"]),
         "plan": {"patches": info["n_patches_solid"], "colours": info["n_colours_solid"],
@@ -322,17 +324,30 @@ def timeloop_bytes(m, pole: int) -> int:
     return b
 
 
-def run_timeloop(args, pole, ws, rank):
+def anel_bytes(m, pole: int) -> int:
+    """Algorithmic bytes the cg4 attenuation adds to a Newmark step: per solid
+    element the memory variables (4 cg points x n_e components x n_sls, n_e = 4
+    monopole, 6 otherwise) and the previous step's sources (4 x (1 + n_e))
+    read and written, and the 48 constant floats plus 2 Q indices read."""
+    ne = 4 if pole == 0 else 6
+    nsls = len(m.anel["y_j"])
+    return m.nel_solid * (4 * ne * nsls * 8 + 4 * (1 + ne) * 8 + 48 * 4 + 8)
+
+
+def run_timeloop(args, pole, ws, rank, anel=False):
     """Newmark steps (SOLVER/time_evol_wave.F90:353-500) on a coupled mesh of
-    1024 x 768 solid over 1024 x 256 fluid elements, through axg_run."""
+    1024 x 768 solid over 1024 x 256 fluid elements, through axg_run; with
+    `anel`, cg4 attenuation with 5 standard linear solids in the solid."""
     import torch
-    from axisem_gb300.mesh import coupled_mesh
+    from axisem_gb300.mesh import add_attenuation, coupled_mesh
     from axisem_gb300.solver import Solver
     n = args.size
     nsteps = args.timeloop_steps
     warm = 16
     m = coupled_mesh(n, 3 * n // 4, n // 4, pole, niter=warm + nsteps, seed=5 + rank, num_rec=200,
                      seis_it=4, deltat=2e-6, terms="pole")
+    if anel:
+        m = add_attenuation(m, n_sls=5, seed=77 + rank)
     s = Solver(m)
     s.set_tuning(steps_per_graph=16)
     s.run(1, warm)
@@ -346,11 +361,11 @@ def run_timeloop(args, pole, ws, rank):
     rec = s.receivers()
     s.close()
     pts = 25 * (m.nel_solid + m.nel_fluid)
-    nb = timeloop_bytes(m, pole)
+    nb = timeloop_bytes(m, pole) + (anel_bytes(m, pole) if anel else 0)
     peak, _ = measured_peaks()
     return {"value": ws * pts / dt, "unit": "GLL-point-steps/s", "ms_per_step": dt * 1e3,
             "mesh": f"{n}x{3 * n // 4} solid + {n}x{n // 4} fluid elements, {args.pole}pole, "
-                    f"source + 200 receivers",
+                    f"source + 200 receivers" + (", cg4 attenuation with 5 SLS" if anel else ""),
             "algorithmic_bytes_per_step": nb, "achieved_gbs": nb / dt / 1e9,
             "frac_of_hbm": nb / dt / 1e9 / peak, "kernels_per_step": info["kernels_per_step"],
             "finite": bool(np.isfinite(rec).all())}
