@@ -118,6 +118,8 @@ class Info(C.Structure):
         ("kernels_per_step", C.c_int64),
         ("kernels_per_force", C.c_int64),
         ("patch_points_solid", C.c_int64),
+        ("patch_elems_solid", C.c_int32), ("growth_solid", C.c_int32),
+        ("patch_elems_fluid", C.c_int32), ("growth_fluid", C.c_int32),
     ]
 
 
@@ -134,6 +136,7 @@ SIGNATURES = {
     "axg_version": (C.c_char_p, []),
     "axg_device_count": (C.c_int, []),
     "axg_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(C.c_void_p)]),
+    "axg_create_tuned": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "axg_reset": (C.c_int, [C.c_void_p]),
     "axg_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "axg_get_receivers": (C.c_int, [C.c_void_p, _fp, C.c_int32, _ip]),
@@ -147,7 +150,7 @@ SIGNATURES = {
     "axg_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "axg_get_info": (C.c_int, [C.c_void_p, C.POINTER(Info)]),
     "axg_get_solid_colouring": (C.c_int, [C.c_void_p, _ip, _ip, C.c_int64]),
-    "axg_plan_check": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.POINTER(Info)]),
+    "axg_plan_check": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(Info)]),
     "axg_time_stiffness": (C.c_int, [C.c_void_p, C.c_int32, _fp]),
     "axg_device_check_report": (C.c_int, [_ip]),
     "axg_destroy": (None, [C.c_void_p]),

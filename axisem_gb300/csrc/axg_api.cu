@@ -91,7 +91,8 @@ struct axg_handle {
   std::vector<int32_t> igloc_s, igloc_f, rec_gidx;
   std::vector<uint8_t> pre_s, pre_f;
   DomainPlan ps, pf;
-  int patch_elems = 64, steps_per_graph = 16;
+  int patch_elems = 0, growth = -1;  // requested patch shape (0 / -1: tuned)
+  int steps_per_graph = 16;
   // device
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -339,7 +340,7 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid) {
       }
     }
     for (auto &w : pts)
-      if (issrc[w & kPtIndexMask]) w |= kPtSource;
+      if (w != kPtPad && issrc[w & kPtIndexMask]) w |= kPtSource;
   }
   int rc;
   if ((rc = upload(h, &dd.meta, pl.meta))) return rc;
@@ -617,6 +618,15 @@ void prepass_flags(const axg_mesh_desc *d, std::vector<uint8_t> &pre_s, std::vec
   }
 }
 
+// tuned (or requested) patch shape, then the plan
+std::string plan_domain(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
+                        const std::vector<uint8_t> &prepass, DomainPlan &plan) {
+  int pe = patch_elems, gr = growth;
+  std::string e = tune_plan(igloc, nel, nglob, patch_elems, growth, &pe, &gr);
+  if (!e.empty()) return e;
+  return build_plan(igloc, nel, nglob, pe, gr, prepass, plan);
+}
+
 int check_igloc(const int32_t *ig, int64_t n, int64_t nglob, const char *what) {
   for (int64_t p = 0; p < n; ++p)
     if (ig[p] < 1 || ig[p] > nglob) return fail(nullptr, AXG_ERR_BAD_DESC, fmt("%s entry outside 1..nglob", what));
@@ -754,10 +764,10 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
     h->pre_f.assign(h->nglob_f, 0);
     for (int32_t g : cf.pt_gidx) h->pre_f[g] = 1;
   }
-  std::string perr = build_plan(h->igloc_s.data(), h->nel_s, h->nglob_s, h->patch_elems, h->pre_s, h->ps);
+  std::string perr = plan_domain(h->igloc_s.data(), h->nel_s, h->nglob_s, h->patch_elems, h->growth, h->pre_s, h->ps);
   if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "solid plan: " + perr);
   if (h->nel_f > 0) {
-    perr = build_plan(h->igloc_f.data(), h->nel_f, h->nglob_f, h->patch_elems, h->pre_f, h->pf);
+    perr = plan_domain(h->igloc_f.data(), h->nel_f, h->nglob_f, h->patch_elems, h->growth, h->pre_f, h->pf);
     if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "fluid plan: " + perr);
   }
 #ifdef AXG_VALIDATE_PLAN
@@ -947,7 +957,7 @@ extern "C" int axg_stiffness_assembled_noalloc(const axg_mesh_desc *d, const flo
   const int pole = d->src_type;
   const int64_t nel = d->nel_solid, nglob = d->nglob_solid;
   DomainPlan pl;
-  std::string perr = build_plan(d->igloc_solid, nel, nglob, kMaxPatchElems, std::vector<uint8_t>(), pl);
+  std::string perr = plan_domain(d->igloc_solid, nel, nglob, 0, -1, std::vector<uint8_t>(), pl);
   if (!perr.empty()) return fail(nullptr, AXG_ERR_BAD_DESC, "solid plan: " + perr);
   const std::vector<int> slots = solid_slots(pole), aslots = axial_slots(pole);
   const int nt = (int)slots.size(), na = (int)aslots.size();
@@ -1085,13 +1095,20 @@ int axg_device_count(void) {
   return n;
 }
 
-int axg_create(const axg_mesh_desc *d, axg_handle **out) {
+int axg_create(const axg_mesh_desc *d, axg_handle **out) { return axg_create_tuned(d, 0, -1, out); }
+
+int axg_create_tuned(const axg_mesh_desc *d, int32_t patch_elems, int32_t growth, axg_handle **out) {
   if (!out) return fail(nullptr, AXG_ERR_BAD_ARG, "out is NULL");
   *out = nullptr;
+  if (patch_elems < 0 || patch_elems > kMaxPatchElems)
+    return fail(nullptr, AXG_ERR_BAD_ARG, fmt("patch_elems %d outside 0..%d", patch_elems, kMaxPatchElems));
+  if (growth < -1 || growth > kGrowLayered) return fail(nullptr, AXG_ERR_BAD_ARG, "growth must be -1, 0 or 1");
   int rc = validate(d);
   if (rc) return rc;
   if (axg_device_count() < 1) return fail(nullptr, AXG_ERR_NO_DEVICE, "no CUDA device is visible");
   axg_handle *h = new axg_handle();
+  h->patch_elems = patch_elems;
+  h->growth = growth;
   rc = create_impl(h, d);
   if (rc) {
     g_create_error = h->err;
@@ -1263,8 +1280,8 @@ int axg_stiffness_assembled(axg_handle *h, const float *u, float *f) {
 int axg_set_tuning(axg_handle *h, int32_t patch_elems, int32_t steps_per_graph) {
   if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
   if (steps_per_graph < 0 || steps_per_graph > 4096) return fail(h, AXG_ERR_BAD_ARG, "steps_per_graph out of range");
-  if (patch_elems != 0 && patch_elems != h->patch_elems)
-    return fail(h, AXG_ERR_UNSUPPORTED, "patch_elems is fixed at axg_create in this build");
+  if (patch_elems != 0 && patch_elems != h->ps.patch_elems)
+    return fail(h, AXG_ERR_UNSUPPORTED, "the patch shape is fixed at creation (axg_create_tuned)");
   if (steps_per_graph > 0 && steps_per_graph != h->steps_per_graph) {
     h->steps_per_graph = steps_per_graph;
     if (h->graph) {
@@ -1287,7 +1304,12 @@ int axg_get_info(axg_handle *h, axg_info *info) {
   info->device_bytes = h->dev_bytes;
   info->kernels_per_step = h->kernels_per_step;
   info->kernels_per_force = h->kernels_per_force;
-  info->patch_points_solid = h->ps.total_pts;
+  info->patch_points_solid = 0;
+  for (const PatchMeta &m : h->ps.meta) info->patch_points_solid += m.n_pts;
+  info->patch_elems_solid = h->ps.patch_elems;
+  info->growth_solid = h->ps.growth;
+  info->patch_elems_fluid = h->pf.patch_elems;
+  info->growth_fluid = h->pf.growth;
   return AXG_OK;
 }
 
@@ -1299,7 +1321,7 @@ int axg_get_solid_colouring(axg_handle *h, int32_t *patch_of_elem, int32_t *colo
   return AXG_OK;
 }
 
-int axg_plan_check(const axg_mesh_desc *d, int32_t patch_elems, axg_info *info) {
+int axg_plan_check(const axg_mesh_desc *d, int32_t patch_elems, int32_t growth, axg_info *info) {
   if (!info) return fail(nullptr, AXG_ERR_BAD_ARG, "info is NULL");
   int rc = validate(d);
   if (rc) return rc;
@@ -1311,11 +1333,13 @@ int axg_plan_check(const axg_mesh_desc *d, int32_t patch_elems, axg_info *info) 
   prepass_flags(d, pre_s, pre_f);
   std::memset(info, 0, sizeof *info);
   DomainPlan ps, pf;
-  std::string e = build_plan(d->igloc_solid, d->nel_solid, d->nglob_solid, patch_elems, pre_s, ps);
+  if (patch_elems < 0 || patch_elems > kMaxPatchElems) return fail(nullptr, AXG_ERR_BAD_ARG, "patch_elems out of range");
+  if (growth < -1 || growth > kGrowLayered) return fail(nullptr, AXG_ERR_BAD_ARG, "growth must be -1, 0 or 1");
+  std::string e = plan_domain(d->igloc_solid, d->nel_solid, d->nglob_solid, patch_elems, growth, pre_s, ps);
   if (e.empty()) e = validate_plan(d->igloc_solid, d->nel_solid, d->nglob_solid, pre_s, ps);
   if (!e.empty()) return fail(nullptr, AXG_ERR_BAD_DESC, "solid plan: " + e);
   if (d->nel_fluid > 0) {
-    e = build_plan(d->igloc_fluid, d->nel_fluid, d->nglob_fluid, patch_elems, pre_f, pf);
+    e = plan_domain(d->igloc_fluid, d->nel_fluid, d->nglob_fluid, patch_elems, growth, pre_f, pf);
     if (e.empty()) e = validate_plan(d->igloc_fluid, d->nel_fluid, d->nglob_fluid, pre_f, pf);
     if (!e.empty()) return fail(nullptr, AXG_ERR_BAD_DESC, "fluid plan: " + e);
   }
@@ -1325,8 +1349,13 @@ int axg_plan_check(const axg_mesh_desc *d, int32_t patch_elems, axg_info *info) 
   info->n_colours_fluid = pf.n_colours;
   info->max_subrounds_solid = ps.max_rounds;
   info->max_subrounds_fluid = pf.max_rounds;
-  info->patch_points_solid = ps.total_pts;
+  info->patch_points_solid = 0;
+  for (const PatchMeta &m : ps.meta) info->patch_points_solid += m.n_pts;
   info->kernels_per_force = ps.n_colours;
+  info->patch_elems_solid = ps.patch_elems;
+  info->growth_solid = ps.growth;
+  info->patch_elems_fluid = pf.patch_elems;
+  info->growth_fluid = pf.growth;
   return AXG_OK;
 }
 

@@ -14,8 +14,9 @@
 //   2. elements, sub-round by sub-round: each warp computes its element's
 //      stiffness and adds it into the shared point accumulators (elements
 //      of one sub-round share no point, so there is no race);
-//   3. write-back: partial sums are added to the global force (the first
-//      writer stores); the last writer of a point applies the Newmark
+//   3. write-back: the accumulators (which started from the partial sums of
+//      earlier writers) are stored to the global force; the last writer of a
+//      point applies the Newmark
 //      corrector (SOLVER/time_evol_wave.F90:466-494) in registers and stores
 //      disp/velo/acc0 -- the assembled force of that point never touches HBM.
 #pragma once
@@ -560,7 +561,7 @@ __device__ __forceinline__ void anel_memvar_step(const float *cs, float *R, cons
 
 // ------------------------------------------------------------ solid patch kernel
 
-constexpr int kStages = 3;  // element blocks in flight per warp (TMA ring depth)
+constexpr int kStages = 2;  // element blocks in flight per warp (TMA ring depth)
 
 // shared-memory layout of the solid kernel (bytes); STG ring stages per warp,
 // AS floats of attenuation data per stage (0 without attenuation)
@@ -574,9 +575,12 @@ struct SolidSmem {
   static constexpr int bar_off = aring_off + kWarps * STG * AS * 4;
   static constexpr int bytes = bar_off + kWarps * STG * 8;
 };
-// ring depth: three element blocks in flight, two with attenuation (keeps two
-// CTAs per SM)
-__host__ __device__ constexpr int solid_stages(bool anel) { return anel ? 2 : kStages; }
+// ring depth (the same with attenuation, whose blocks ride in a second ring)
+__host__ __device__ constexpr int solid_stages(bool) { return kStages; }
+// resident CTAs per SM the kernel is compiled for: the Newmark kernel keeps
+// three (its register-staged gather is latency-bound; 80 registers), the
+// others two (no spills at 128 registers)
+__host__ __device__ constexpr int solid_min_ctas(int mode, bool anel) { return mode == MODE_NEWMARK && !anel ? 3 : 2; }
 
 // the elements warp `w` processes in a patch, in order: sub-round by
 // sub-round, elements w, w + kWarps, ... of each round
@@ -595,7 +599,7 @@ struct WarpIter {
 // before the axis mask of acc1 and the memory-variable step after it, as in
 // SOLVER/time_evol_wave.F90 (anel_true, cg4).
 template <int POLE, int MODE, bool ANEL>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
     solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches, AnelArgs an) {
   static_assert(!ANEL || MODE == MODE_NEWMARK, "attenuation runs in the time loop only");
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
@@ -613,11 +617,17 @@ __global__ void __launch_bounds__(kThreads, 2)
   float *aring = reinterpret_cast<float *>(smem + L::aring_off);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bar_off);
   __shared__ int s_stop;
+  // sub-round r of a patch is complete when all threads have arrived on
+  // s_round[r] after their accumulations of round r
+  __shared__ __align__(8) uint64_t s_round[kMaxSubrounds];
+  __shared__ __align__(8) uint64_t s_wbar;  // the patch's point words have landed in s_w
   // component c of the shared arrays -> global component (mono: s, z)
   auto gc = [](int c) { return (POLE == POLE_MONO && c == 1) ? 2 : c; };
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x < kWarps * STG) mbar_init(&bars[threadIdx.x], 1);
+  if (threadIdx.x < kMaxSubrounds) mbar_init(&s_round[threadIdx.x], kThreads);
+  if (threadIdx.x == 0) mbar_init(&s_wbar, 1);
   if (threadIdx.x == 0) s_stop = (MODE == MODE_NEWMARK) ? *st.blowup : 0;
   fence_mbar_init();
   __syncthreads();
@@ -635,6 +645,8 @@ __global__ void __launch_bounds__(kThreads, 2)
   float *my_aring = aring + warp * STG * AS;
   uint64_t *my_bars = bars + warp * STG;
   uint32_t kcount = 0;  // elements this warp has consumed (slot = kcount % STG)
+  uint32_t round_par = 0;  // bit r: parity of the next completion of s_round[r]
+  uint32_t pcount = 0;     // patches this CTA has started (parity of s_wbar)
   // cg lane index k of the attenuation points (1,1), (1,3), (3,1), (3,3)
   const bool cg = active && (i == 1 || i == 3) && (j == 1 || j == 3);
   const int kcg = 2 * (i >> 1) + (j >> 1);
@@ -658,47 +670,90 @@ __global__ void __launch_bounds__(kThreads, 2)
     if (!AXG_BOUND(d.patch_begin + pp, d.n_patches, 1)) break;
     const PatchMeta m = d.meta[d.patch_begin + pp];
 
-    // 0. start the bulk copies of this warp's first STG element blocks
-    WarpIter pf{0, warp};
-    pf.norm(m, warp);
-    for (int q = 0; q < STG && pf.valid(m); ++q) {
-      if (lane == 0) {
-        const int64_t el = (int64_t)m.elem_start + pf.s;
-        if (AXG_BOUND(el, d.n_elem, 2)) issue((kcount + q) % STG, el);
+    // 0. bulk copy of the patch's point words into s_w (each patch's words
+    //    start 16-byte aligned, padded to a multiple of four)
+    if (threadIdx.x == 0) {
+      const uint32_t nw = ((uint32_t)m.n_pts + 3u) & ~3u;
+      if (nw > 0 && AXG_BOUND((int64_t)m.pt_start + nw - 1, d.n_pts, 1)) {
+        fence_proxy_async();  // the previous patch's reads of s_w precede the async-proxy write
+        bulk_g2s(s_w, d.pts + m.pt_start, nw * 4u, &s_wbar, pol);
+      } else {
+        mbar_arrive(&s_wbar);
       }
-      pf.s += kWarps;
-      pf.norm(m, warp);
     }
-
-    // 1. gather (+ predictor), four points per thread in flight
-    for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += 4 * kThreads) {
-      uint32_t w[4];
-      float uu[4][NC];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int t = t0 + q * kThreads;
-        w[q] = (t < m.n_pts && AXG_BOUND(m.pt_start + t, d.n_pts, 1)) ? d.pts[m.pt_start + t] : 0xFFFFFFFFu;
+    // this warp's first STG element blocks (stiffness mode: after the gather's
+    // loads are issued, so that those are not queued behind the blocks)
+    WarpIter pf{0, warp};
+    auto prefetch_first = [&]() {
+      pf = WarpIter{0, warp};
+      pf.norm(m, warp);
+      for (int q = 0; q < STG && pf.valid(m); ++q) {
+        if (lane == 0) {
+          const int64_t el = (int64_t)m.elem_start + pf.s;
+          if (AXG_BOUND(el, d.n_elem, 2)) issue((kcount + q) % STG, el);
+        }
+        pf.s += kWarps;
+        pf.norm(m, warp);
       }
+    };
+    // 1. gather.  A point that an earlier writer (coupling pre-pass, earlier
+    //    colour) already holds a partial sum for starts its accumulator from
+    //    that sum, so that the write-back is a plain store.
+    if (MODE != MODE_FORCE) prefetch_first();
+    mbar_wait_bounded(&s_wbar, pcount & 1u, st.err);
+    ++pcount;
+    if (MODE == MODE_FORCE) {
+      // asynchronous 4-byte copies straight into shared memory: all of a
+      // thread's loads are in flight at once
+      for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
+        const uint32_t w = s_w[t];
+        const uint32_t g = w & kPtIndexMask;
+        if (!AXG_BOUND(g, st.nglob, 1)) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const uint32_t g = w[q] & kPtIndexMask;
-        const bool ok = w[q] != 0xFFFFFFFFu && AXG_BOUND(g, st.nglob, 1);
+          for (int c = 0; c < NC; ++c) s_u[c][t] = s_f[c][t] = 0.f;
+          continue;
+        }
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
-          float u = ok ? st.u[gc(c)][g] : 0.f;
-          if (MODE == MODE_NEWMARK && ok) u = predict(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2);
-          uu[q][c] = u;
+          cp_async4(&s_u[c][t], st.u[gc(c)] + g);
+          if (w & kPtFirst) s_f[c][t] = 0.f;
+          else cp_async4(&s_f[c][t], st.f[gc(c)] + g);
         }
       }
+      prefetch_first();
+      cp_async_wait_all();
+    } else {
+      // Newmark predictor on the fly, four points per thread in flight
+      for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += 4 * kThreads) {
+        uint32_t w[4];
+        float uu[4][NC], ff[4][NC];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int t = t0 + q * kThreads;
-        if (t < m.n_pts) {
-          s_w[t] = w[q];
+        for (int q = 0; q < 4; ++q) {
+          const int t = t0 + q * kThreads;
+          w[q] = t < m.n_pts ? s_w[t] : kPtPad;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint32_t g = w[q] & kPtIndexMask;
+          const bool ok = w[q] != kPtPad && AXG_BOUND(g, st.nglob, 1);
+          const bool part = ok && !(w[q] & kPtFirst);
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
-            s_u[c][t] = uu[q][c];
-            s_f[c][t] = 0.f;
+            float u = ok ? st.u[gc(c)][g] : 0.f;
+            if (ok) u = predict(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2);
+            uu[q][c] = u;
+            ff[q][c] = part ? st.f[gc(c)][g] : 0.f;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int t = t0 + q * kThreads;
+          if (t < m.n_pts) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+              s_u[c][t] = uu[q][c];
+              s_f[c][t] = ff[q][c];
+            }
           }
         }
       }
@@ -709,6 +764,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     int r0 = 0;
     for (int r = 0; r < m.n_rounds; ++r) {
       const int r1 = m.round_end[r];
+      bool ready = r == 0;  // round r-1 complete (waited for)
       for (int s = r0 + warp; s < r1; s += kWarps) {
         int64_t el = (int64_t)m.elem_start + s;
         if (!AXG_BOUND(el, d.n_elem, 2)) el = 0;
@@ -764,6 +820,12 @@ __global__ void __launch_bounds__(kThreads, 2)
           if (POLE == POLE_DI) { f1 = 0.f; f2 = 0.f; }
           if (POLE == POLE_QUAD) { f0 = 0.f; f1 = 0.f; f2 = 0.f; }
         }
+        // the previous sub-round's accumulations must be complete; the wait
+        // comes after this element's stiffness, which hides it
+        if (!ready) {
+          mbar_wait_bounded(&s_round[r - 1], (round_par >> (r - 1)) & 1u, st.err);
+          ready = true;
+        }
         if (active) {
           s_f[0][idx] += f0;
           if (POLE == POLE_MONO) {
@@ -796,9 +858,11 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
         ++kcount;
       }
+      mbar_arrive(&s_round[r]);  // this thread's accumulations of round r are done
       r0 = r1;
-      __syncthreads();
     }
+    round_par ^= (1u << m.n_rounds) - 1u;  // each used s_round completed once in this patch
+    __syncthreads();
 
     // 3. write-back
     for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
@@ -807,10 +871,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       if (!AXG_BOUND(g, st.nglob, 3)) continue;
       float v[NC];
 #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        v[c] = s_f[c][t];
-        if (!(w & kPtFirst)) v[c] = st.f[gc(c)][g] + v[c];
-      }
+      for (int c = 0; c < NC; ++c) v[c] = s_f[c][t];
       if (MODE == MODE_FORCE || !(w & kPtLast)) {
 #pragma unroll
         for (int c = 0; c < NC; ++c) st.f[gc(c)][g] = v[c];

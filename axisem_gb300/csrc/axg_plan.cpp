@@ -41,13 +41,15 @@ PointElems point_elements(const int32_t *igloc, int64_t nel, int64_t nglob) {
 
 }  // namespace
 
-std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems,
+std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
                        const std::vector<uint8_t> &prepass, DomainPlan &plan) {
   plan = DomainPlan();
   plan.nel = nel;
   plan.nglob = nglob;
   if (patch_elems < 1 || patch_elems > kMaxPatchElems) return "patch_elems out of range";
+  if (growth != kGrowCompact && growth != kGrowLayered) return "unknown patch growth";
   plan.patch_elems = patch_elems;
+  plan.growth = growth;
   if (nel == 0) {
     plan.colour_start.assign(1, 0);
     return "";
@@ -58,23 +60,96 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
 
   const PointElems pe = point_elements(igloc, nel, nglob);
 
-  // ---- 1. patches: greedy compact growth ---------------------------------
+  // ---- 1. patches -----------------------------------------------------------
+  // Seeds are taken in element order (the lowest unassigned element).
+  //  compact: the next member is the candidate sharing the most points with
+  //           the patch (ties: lowest element);
+  //  layered: breadth-first layers of point-sharing neighbours, inside a layer
+  //           the candidates sharing the most points first.  From the corner of
+  //           a structured block a patch of k^2 elements is a k x k square.
   plan.patch_of_elem.assign(nel, -1);
   std::vector<int32_t> score(nel, 0);
   std::vector<int32_t> cand;
   std::vector<std::vector<int32_t>> patches;
   int64_t next_seed = 0;
-  while (true) {
+  const bool layered = growth == kGrowLayered;
+  std::vector<uint32_t> ptstamp(nglob, 0), elstamp(nel, 0);
+  uint32_t stamp = 0;
+  while (layered) {
+    while (next_seed < nel && plan.patch_of_elem[next_seed] >= 0) ++next_seed;
+    if (next_seed >= nel) break;
+    const int32_t pid = (int32_t)patches.size();
+    ++stamp;
+    std::vector<int32_t> members{(int32_t)next_seed}, layer{(int32_t)next_seed}, next;
+    plan.patch_of_elem[next_seed] = pid;
+    elstamp[next_seed] = stamp;
+    int npts = 0;  // distinct points of the patch
+    for (int k = 0; k < 25; ++k) {
+      const int64_t g = igloc[25 * next_seed + k] - 1;
+      npts += ptstamp[g] != stamp;
+      ptstamp[g] = stamp;
+    }
+    while ((int)members.size() < patch_elems) {
+      next.clear();
+      for (int32_t e : layer)
+        for (int k = 0; k < 25; ++k) {
+          const int64_t g = igloc[25 * (int64_t)e + k] - 1;
+          for (int64_t q = pe.start[g]; q < pe.start[g + 1]; ++q) {
+            const int32_t e2 = pe.elems[q];
+            if (e2 < 0 || plan.patch_of_elem[e2] >= 0 || elstamp[e2] == stamp) continue;
+            elstamp[e2] = stamp;
+            next.push_back(e2);
+          }
+        }
+      if (next.empty()) break;
+      for (int32_t c : next) {
+        score[c] = 0;
+        for (int k = 0; k < 25; ++k) score[c] += ptstamp[igloc[25 * (int64_t)c + k] - 1] == stamp;
+      }
+      std::stable_sort(next.begin(), next.end(), [&](int32_t a, int32_t b) {
+        return score[a] != score[b] ? score[a] > score[b] : a < b;
+      });
+      layer.clear();
+      for (int32_t c : next) {
+        if ((int)members.size() >= patch_elems) break;
+        const int add = 25 - score[c];  // points not yet in the patch
+        if (npts + add > kMaxPatchPoints) continue;
+        npts += add;
+        plan.patch_of_elem[c] = pid;
+        members.push_back(c);
+        layer.push_back(c);
+        for (int k = 0; k < 25; ++k) ptstamp[igloc[25 * (int64_t)c + k] - 1] = stamp;
+        // later candidates of this layer may now share more points
+        for (int32_t c2 : next)
+          if (plan.patch_of_elem[c2] < 0) {
+            int sc = 0;
+            for (int k = 0; k < 25; ++k) sc += ptstamp[igloc[25 * (int64_t)c2 + k] - 1] == stamp;
+            score[c2] = sc;
+          }
+      }
+      if (layer.empty()) break;
+      for (int32_t c : next) score[c] = 0;
+    }
+    patches.push_back(std::move(members));
+  }
+  while (!layered) {
     while (next_seed < nel && plan.patch_of_elem[next_seed] >= 0) ++next_seed;
     if (next_seed >= nel) break;
     const int32_t pid = (int32_t)patches.size();
     std::vector<int32_t> members;
     cand.clear();
+    ++stamp;  // ptstamp: points in the patch; elstamp: candidates over the point cap
+    int npts = 0;
     int32_t add = (int32_t)next_seed;
     while (true) {
       plan.patch_of_elem[add] = pid;
       members.push_back(add);
       score[add] = 0;
+      for (int k = 0; k < 25; ++k) {
+        const int64_t g = igloc[25 * (int64_t)add + k] - 1;
+        npts += ptstamp[g] != stamp;
+        ptstamp[g] = stamp;
+      }
       if ((int)members.size() >= patch_elems) break;
       for (int k = 0; k < 25; ++k) {
         const int64_t g = igloc[25 * (int64_t)add + k] - 1;
@@ -86,15 +161,85 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
         }
       }
       int32_t best = -1;
-      for (int32_t c : cand) {
-        if (plan.patch_of_elem[c] >= 0) continue;
-        if (best < 0 || score[c] > score[best] || (score[c] == score[best] && c < best)) best = c;
+      while (true) {
+        best = -1;
+        for (int32_t c : cand) {
+          if (plan.patch_of_elem[c] >= 0 || elstamp[c] == stamp) continue;
+          if (best < 0 || score[c] > score[best] || (score[c] == score[best] && c < best)) best = c;
+        }
+        if (best < 0) break;
+        int extra = 0;
+        for (int k = 0; k < 25; ++k) extra += ptstamp[igloc[25 * (int64_t)best + k] - 1] != stamp;
+        if (npts + extra <= kMaxPatchPoints) break;
+        elstamp[best] = stamp;  // would overflow the patch's points
       }
       if (best < 0) break;
       add = best;
     }
     for (int32_t c : cand) score[c] = 0;
     patches.push_back(std::move(members));
+  }
+  // ---- 1b. fragments: growth can leave small holes between full patches;
+  // each patch of fewer than patch_elems / 4 elements is merged into the
+  // adjacent patch with the fewest elements that can take it (the merged
+  // patch stays within kMaxPatchElems elements and kMaxPatchPoints points).
+  // A fragment costs a whole gather / write-back cycle for a few elements.
+  {
+    const int small = std::max(1, patch_elems / 4);
+    std::vector<int32_t> npts(patches.size(), -1);
+    std::vector<uint32_t> seen(nglob, 0);
+    uint32_t mstamp = 0;
+    auto count_points = [&](const std::vector<int32_t> &a, const std::vector<int32_t> *b) {
+      ++mstamp;
+      int32_t n = 0;
+      for (const std::vector<int32_t> *v : {&a, b}) {
+        if (!v) continue;
+        for (int32_t e : *v)
+          for (int k = 0; k < 25; ++k) {
+            const int64_t g = igloc[25 * (int64_t)e + k] - 1;
+            if (seen[g] != mstamp) {
+              seen[g] = mstamp;
+              ++n;
+            }
+          }
+      }
+      return n;
+    };
+    for (size_t p = 0; p < patches.size(); ++p) {
+      if (patches[p].empty() || (int)patches[p].size() >= small) continue;
+      // neighbouring patches, best = fewest elements that fit
+      int32_t best = -1;
+      for (int32_t e : patches[p])
+        for (int k = 0; k < 25; ++k) {
+          const int64_t g = igloc[25 * (int64_t)e + k] - 1;
+          for (int64_t q = pe.start[g]; q < pe.start[g + 1]; ++q) {
+            const int32_t e2 = pe.elems[q];
+            if (e2 < 0) continue;
+            const int32_t p2 = plan.patch_of_elem[e2];
+            if (p2 == (int32_t)p) continue;
+            if (patches[p2].size() + patches[p].size() > (size_t)kMaxPatchElems) continue;
+            if (best >= 0 && (patches[p2].size() > patches[best].size() ||
+                              (patches[p2].size() == patches[best].size() && p2 >= best)))
+              continue;
+            if (count_points(patches[p2], &patches[p]) > kMaxPatchPoints) continue;
+            best = p2;
+          }
+        }
+      if (best < 0) continue;
+      for (int32_t e : patches[p]) {
+        plan.patch_of_elem[e] = best;
+        patches[best].push_back(e);
+      }
+      patches[p].clear();
+    }
+    // renumber the surviving patches in creation order
+    std::vector<std::vector<int32_t>> kept;
+    for (auto &v : patches)
+      if (!v.empty()) {
+        for (int32_t e : v) plan.patch_of_elem[e] = (int32_t)kept.size();
+        kept.push_back(std::move(v));
+      }
+    patches.swap(kept);
   }
   plan.n_patches = (int32_t)patches.size();
 
@@ -163,15 +308,24 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
     std::vector<int32_t> mem = patches[p];
     std::sort(mem.begin(), mem.end());
     const int n = (int)mem.size();
-    // greedy sub-rounds: element a gets the smallest round not used by an
-    // earlier element of the patch that shares a point with it
+    // greedy sub-rounds: element a goes to a round not used by an earlier
+    // element of the patch that shares a point with it; among those, the
+    // first round whose element count is not a multiple of the CTA's 8 warps
+    // (the element then costs no extra warp iteration), else the first one
     int nrounds = 0;
+    int rcount[kMaxSubrounds] = {};
     for (int a = 0; a < n; ++a) {
       uint32_t used = 0;
       for (int k = 0; k < 25; ++k) used |= ptmask[igloc[25 * (int64_t)mem[a] + k] - 1];
       int r = 0;
       while (used & (1u << r)) ++r;
+      for (int q = r; q < nrounds; ++q)
+        if (!(used & (1u << q)) && rcount[q] % 8 != 0) {
+          r = q;
+          break;
+        }
       if (r >= kMaxSubrounds) return "patch needs more sub-rounds than supported";
+      ++rcount[r];
       round_of[a] = r;
       nrounds = std::max(nrounds, r + 1);
       for (int k = 0; k < 25; ++k) ptmask[igloc[25 * (int64_t)mem[a] + k] - 1] |= 1u << r;
@@ -210,6 +364,8 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
       if (cmax[g] == col) w |= kPtLast;
       plan.pt_words.push_back(w);
     }
+    // the next patch's words start on a 16-byte boundary (bulk copies)
+    while (plan.pt_words.size() % 4 != 0) plan.pt_words.push_back(kPtPad);
     for (int t = 0; t < n; ++t) {
       const int a = idx[t];
       const int32_t e = mem[a];
@@ -286,6 +442,61 @@ std::string validate_plan(const int32_t *igloc, int64_t nel, int64_t nglob,
     if (nlast[g] != 1) return "point without exactly one last writer";
     if (nfirst[g] != (pre ? 0 : 1)) return "point first-writer count wrong";
   }
+  return "";
+}
+
+int64_t plan_cost(const DomainPlan &plan) {
+  // warp iterations of the patch kernels: per patch a fixed overhead (gather,
+  // write-back and the CTA barriers, about four element iterations measured
+  // on GB300), each sub-round ceil(elements / 8 warps), and a point term for
+  // the gather and write-back traffic (256 points per iteration)
+  int64_t c = 0;
+  for (const PatchMeta &m : plan.meta) {
+    c += 4 * 256 + m.n_pts;
+    int r0 = 0;
+    for (int r = 0; r < m.n_rounds; ++r) {
+      c += 256 * ((m.round_end[r] - r0 + 7) / 8);
+      r0 = m.round_end[r];
+    }
+  }
+  return c;
+}
+
+std::string tune_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
+                      int *best_pe, int *best_growth) {
+  *best_pe = patch_elems > 0 ? patch_elems : kMaxPatchElems;
+  *best_growth = growth >= 0 ? growth : kGrowLayered;
+  if (patch_elems > 0 && growth >= 0) return "";
+  // candidates are compared on a prefix of the mesh (element order), its
+  // points renumbered compactly
+  const int64_t n = std::min<int64_t>(nel, kTunePrefix);
+  if (n == 0) return "";
+  std::vector<int32_t> ig(igloc, igloc + 25 * n);
+  std::vector<int32_t> ids(ig);
+  std::sort(ids.begin(), ids.end());
+  ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+  for (int32_t &v : ig) v = (int32_t)(std::lower_bound(ids.begin(), ids.end(), v) - ids.begin()) + 1;
+  (void)nglob;
+  std::vector<int> sizes;
+  if (patch_elems > 0) sizes.push_back(patch_elems);
+  else sizes = {32, 40, 48, 56, 64};
+  std::vector<int> growths;
+  if (growth >= 0) growths.push_back(growth);
+  else growths = {kGrowLayered, kGrowCompact};
+  double best = -1;
+  for (int pe : sizes)
+    for (int gr : growths) {
+      DomainPlan pl;
+      std::string e = build_plan(ig.data(), n, (int64_t)ids.size(), pe, gr, std::vector<uint8_t>(), pl);
+      if (!e.empty()) continue;
+      const double c = (double)plan_cost(pl);
+      if (best < 0 || c < best) {
+        best = c;
+        *best_pe = pe;
+        *best_growth = gr;
+      }
+    }
+  if (best < 0) return "no patch size yields a valid plan";
   return "";
 }
 

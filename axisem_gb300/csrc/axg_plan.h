@@ -23,13 +23,19 @@ namespace axg {
 
 constexpr int kMaxPatchElems = 64;      // elements per patch (upper bound)
 constexpr int kMaxSubrounds = 12;       // conflict-free element groups per patch
-constexpr int kMaxPatchPoints = 25 * kMaxPatchElems;
+// points per patch: sized so that three Newmark CTAs fit on an SM (an 8 x 8
+// patch of a structured grid has 33^2 = 1089 points); growth stops at it
+constexpr int kMaxPatchPoints = 1104;
+constexpr int64_t kTunePrefix = 65536;  // elements the patch-size tuner plans
+
+enum PatchGrowth { kGrowCompact = 0, kGrowLayered = 1 };
 
 // bits of a patch point word: global index in the low 28 bits
 constexpr uint32_t kPtIndexMask = 0x0FFFFFFFu;
 constexpr uint32_t kPtFirst = 1u << 28;   // first writer: store, do not read partial sum
 constexpr uint32_t kPtLast = 1u << 29;    // last writer: the sum is final
 constexpr uint32_t kPtSource = 1u << 30;  // point carries a solid source term
+constexpr uint32_t kPtPad = 0xFFFFFFFFu;  // padding after a patch's words (each patch starts 16-byte aligned)
 
 struct PatchMeta {            // 32 bytes, device layout
   int32_t elem_start;         // first element (launch order)
@@ -44,6 +50,7 @@ static_assert(sizeof(PatchMeta) == 32, "PatchMeta must be 32 bytes");
 struct DomainPlan {
   int64_t nel = 0, nglob = 0;
   int patch_elems = 0;
+  int growth = kGrowCompact;
   int32_t n_patches = 0;
   int32_t n_colours = 0;
   int32_t max_rounds = 0;
@@ -53,19 +60,29 @@ struct DomainPlan {
   std::vector<int32_t> colour_start;     // n_colours+1 offsets into launch order of patches
   std::vector<PatchMeta> meta;           // n_patches, launch order
   std::vector<int32_t> elem_order;       // nel: reference element (0-based) at each launch slot
-  std::vector<uint32_t> pt_words;        // concatenated patch point words
+  std::vector<uint32_t> pt_words;        // patch point words, each patch padded to a multiple of 4
   std::vector<uint16_t> elem_pts;        // 25*nel, launch order: patch-local point index
   int64_t total_pts = 0;
 };
 
-// Builds patches (compact greedy growth over the element adjacency graph),
-// colours them, splits each patch into sub-rounds and fills the point words.
+// Builds patches of up to patch_elems elements (growth: kGrowCompact or
+// kGrowLayered over the point-sharing element graph), merges fragments,
+// colours the patches, splits each patch into sub-rounds and fills the point
+// words.
 //   igloc     : 25*nel 1-based global indices (walk ipol fastest)
 //   prepass   : per global point, 1 if a pre-pass kernel writes it first
 //               (solid-fluid coupling), may be empty
 // Returns an empty string on success, else the reason.
-std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems,
+std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
                        const std::vector<uint8_t> &prepass, DomainPlan &plan);
+
+// Model cost of a plan in 1/256 warp iterations of the patch kernels.
+int64_t plan_cost(const DomainPlan &plan);
+
+// Patch-size tuner: picks (patch_elems, growth) of least plan_cost on the
+// first kTunePrefix elements.  patch_elems > 0 or growth >= 0 fix that choice.
+std::string tune_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
+                      int *best_pe, int *best_growth);
 
 // Checks the invariants the kernels rely on (used by the tests and by
 // axg_create in debug builds): every element in exactly one patch, no two

@@ -59,6 +59,20 @@ __device__ __forceinline__ void bulk_g2s_tx(void *dst, const void *src, uint32_t
       : "memory");
 }
 
+// plain arrival (release semantics at CTA scope) of the calling thread
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// 4-byte asynchronous global -> shared copy (no register staging), and the
+// wait for all of the thread's outstanding ones
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // L2 policy for data read once per step (the metric terms)
 __device__ __forceinline__ uint64_t policy_evict_first() {
   uint64_t p;

@@ -37,12 +37,14 @@ def _fp(a):
 class Solver:
     """One solve on one GPU (one axg_handle)."""
 
-    def __init__(self, mesh: Mesh, lib=None):
+    def __init__(self, mesh: Mesh, lib=None, patch_elems: int = 0, growth: int = -1):
+        """patch_elems / growth: the patch shape (axg_create_tuned); 0 / -1
+        let the planner's tuner choose, as axg_create does."""
         self.lib = lib or _abi.load_library()
         self.mesh = mesh
         self._desc = mesh.desc()
         h = C.c_void_p()
-        rc = self.lib.axg_create(C.byref(self._desc), C.byref(h))
+        rc = self.lib.axg_create_tuned(C.byref(self._desc), patch_elems, growth, C.byref(h))
         _check(self.lib, None, rc)
         self.h = h
         self.nseismo = (mesh.niter // max(mesh.seis_it, 1)) + 1

@@ -236,8 +236,20 @@ int axg_stiffness_assembled_noalloc(const axg_mesh_desc *desc, const float *u_gv
 int axg_upload_gvec_disp(axg_handle *h, const float *u_gvec);
 int axg_download_gvec_force(axg_handle *h, float *f_gvec);
 
-/* Tuning knobs: elements per patch (<= 64), steps per CUDA graph. 0 = keep. */
+/* Tuning knobs after creation: steps per CUDA graph (0 = keep).  The patch
+ * shape is fixed at creation (axg_create_tuned); patch_elems must be 0 or the
+ * handle's value. */
 int axg_set_tuning(axg_handle *h, int32_t patch_elems, int32_t steps_per_graph);
+
+/* axg_create with the patch shape chosen by the caller: patch_elems 1..64
+ * elements per patch and growth 0 (compact: most shared points first) or 1
+ * (layered: breadth-first layers, square patches on structured blocks).
+ * 0 / -1 leave the choice to the planner's tuner, which axg_create always
+ * uses: it compares patch sizes {32,40,48,56,64} x both growths on the first
+ * 65 536 elements of each domain by a model of the kernels' warp iterations
+ * (patch overhead, conflict-free sub-rounds of 8 warps, patch points).
+ * This entry point has no counterpart in the reference. */
+int axg_create_tuned(const axg_mesh_desc *desc, int32_t patch_elems, int32_t growth, axg_handle **out);
 
 /* Introspection for tests and the benchmark. */
 typedef struct axg_info {
@@ -248,6 +260,8 @@ typedef struct axg_info {
   int64_t kernels_per_step;           /* kernel launches in one Newmark step */
   int64_t kernels_per_force;          /* kernel launches in one stiffness+assembly */
   int64_t patch_points_solid;         /* sum over patches of their point counts */
+  int32_t patch_elems_solid, growth_solid;  /* patch shape the planner used */
+  int32_t patch_elems_fluid, growth_fluid;
 } axg_info;
 int axg_get_info(axg_handle *h, axg_info *info);
 
@@ -256,13 +270,14 @@ int axg_get_info(axg_handle *h, axg_info *info);
 int axg_get_solid_colouring(axg_handle *h, int32_t *patch_of_elem, int32_t *colour_of_patch,
                             int64_t n_patch_cap);
 
-/* Plans the patch colouring of the solid (and fluid) domain on the host only
+/* Plans (patch_elems 0 / growth -1 = tuned, as axg_create) the patch
+ * colouring of the solid (and fluid) domain on the host only
  * -- no GPU is touched -- and checks every invariant the kernels rely on:
  * each element in one patch, no two patches of one colour sharing a global
  * point, no two elements of one sub-round sharing a point, exactly one first
  * and one last writer per point.  `info` receives the plan sizes
  * (device_bytes = 0).  Returns AXG_ERR_BAD_DESC with the violated invariant. */
-int axg_plan_check(const axg_mesh_desc *desc, int32_t patch_elems, axg_info *info);
+int axg_plan_check(const axg_mesh_desc *desc, int32_t patch_elems, int32_t growth, axg_info *info);
 
 /* Event-timed repeat of axg_stiffness_assembled_device: n launches, returns the
  * average device time in ms of one stiffness+assembly (all colour launches). */

@@ -107,7 +107,7 @@ def test_out_of_range_indices_rejected(lib):
     m.igloc_solid = m.igloc_solid.copy()
     m.igloc_solid[3] = m.nglob_solid + 1
     inf = _abi.Info()
-    rc = lib.axg_plan_check(C.byref(m.desc()), 64, C.byref(inf))
+    rc = lib.axg_plan_check(C.byref(m.desc()), 64, -1, C.byref(inf))
     assert rc == _abi.AXG_ERR_BAD_DESC
 
 
@@ -118,14 +118,32 @@ def test_create_without_gpu_reports_no_device(lib):
     assert rc == _abi.AXG_ERR_NO_DEVICE and not h.value
 
 
-@pytest.mark.parametrize("ni,nj,pe", [(64, 48, 64), (33, 17, 64), (20, 20, 16), (7, 3, 5), (1, 1, 64)])
-def test_plan_invariants(lib, ni, nj, pe):
+@pytest.mark.parametrize("growth", [0, 1, -1])
+@pytest.mark.parametrize("ni,nj,pe", [(64, 48, 64), (33, 17, 64), (20, 20, 16), (7, 3, 5), (1, 1, 64),
+                                      (50, 30, 48), (41, 23, 0)])
+def test_plan_invariants(lib, ni, nj, pe, growth):
     m = structured_mesh(ni, nj, 2, axial="random1pct")
     inf = _abi.Info()
-    rc = lib.axg_plan_check(C.byref(m.desc()), pe, C.byref(inf))
+    rc = lib.axg_plan_check(C.byref(m.desc()), pe, growth, C.byref(inf))
     assert rc == 0, lib.axg_last_error(None)
     assert inf.n_colours_solid >= 1 and inf.max_subrounds_solid <= 12
     assert inf.patch_points_solid >= m.nglob_solid
+
+
+def test_tuner_picks_square_patches_on_structured_grid(lib):
+    """On a structured grid the tuner's cost model prefers layered growth with
+    64-element (8 x 8) patches: four conflict-free sub-rounds of 16 elements,
+    four colours, no fragments."""
+    m = structured_mesh(64, 64, 2, axial="none")
+    inf = _abi.Info()
+    assert lib.axg_plan_check(C.byref(m.desc()), 0, -1, C.byref(inf)) == 0
+    assert (inf.patch_elems_solid, inf.growth_solid) == (64, 1)
+    assert (inf.n_patches_solid, inf.n_colours_solid, inf.max_subrounds_solid) == (64, 4, 4)
+    # an explicit shape is kept
+    assert lib.axg_plan_check(C.byref(m.desc()), 48, 0, C.byref(inf)) == 0
+    assert (inf.patch_elems_solid, inf.growth_solid) == (48, 0)
+    assert lib.axg_plan_check(C.byref(m.desc()), 65, -1, C.byref(inf)) == _abi.AXG_ERR_BAD_ARG
+    assert lib.axg_plan_check(C.byref(m.desc()), 64, 2, C.byref(inf)) == _abi.AXG_ERR_BAD_ARG
 
 
 def test_plan_on_permuted_numbering(lib):
@@ -138,13 +156,13 @@ def test_plan_on_permuted_numbering(lib):
     eperm = rng.permutation(m.nel_solid)
     m.igloc_solid = ig.reshape(m.nel_solid, 25)[eperm].reshape(-1).copy()
     inf = _abi.Info()
-    rc = lib.axg_plan_check(C.byref(m.desc()), 64, C.byref(inf))
+    rc = lib.axg_plan_check(C.byref(m.desc()), 64, -1, C.byref(inf))
     assert rc == 0, lib.axg_last_error(None)
 
 
 def test_plan_coupled(lib):
     m = coupled_mesh(40, 12, 9, 2)
     inf = _abi.Info()
-    rc = lib.axg_plan_check(C.byref(m.desc()), 64, C.byref(inf))
+    rc = lib.axg_plan_check(C.byref(m.desc()), 64, -1, C.byref(inf))
     assert rc == 0, lib.axg_last_error(None)
     assert inf.n_patches_fluid > 0
