@@ -461,7 +461,8 @@ DomainArgs domain_args(const DomainDev &dd, const DomainPlan &pl) {
 template <int POLE, int MODE, bool ANEL>
 constexpr int solid_smem_bytes() {
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;
-  return SolidSmem<NC, solid_block_stride(n_terms(POLE)), solid_stages(ANEL), ANEL ? kAnelSlot : 0>::bytes;
+  return SolidSmem<NC, solid_block_stride(n_terms(POLE)), solid_stages(ANEL), ANEL ? kAnelSlot : 0,
+                   solid_buffers(MODE)>::bytes;
 }
 
 // sets the kernel's shared-memory attributes; *ctas = resident CTAs on the GPU

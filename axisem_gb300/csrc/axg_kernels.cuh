@@ -563,20 +563,25 @@ __device__ __forceinline__ void anel_memvar_step(const float *cs, float *R, cons
 
 constexpr int kStages = 2;  // element blocks in flight per warp (TMA ring depth)
 
-// shared-memory layout of the solid kernel (bytes); STG ring stages per warp,
-// AS floats of attenuation data per stage (0 without attenuation)
-template <int NC, int BS, int STG, int AS>
+// shared-memory layout of the solid kernel (bytes); NB buffers of the patch
+// state (u, f, point words), STG ring stages per warp, AS floats of
+// attenuation data per stage (0 without attenuation)
+template <int NC, int BS, int STG, int AS, int NB>
 struct SolidSmem {
+  static constexpr int u_bytes = NC * kMaxPatchPoints * 4, w_bytes = kMaxPatchPoints * 4;
   static constexpr int u_off = 0;
-  static constexpr int f_off = u_off + NC * kMaxPatchPoints * 4;
-  static constexpr int w_off = f_off + NC * kMaxPatchPoints * 4;
-  static constexpr int ring_off = ((w_off + kMaxPatchPoints * 4 + 127) / 128) * 128;
+  static constexpr int f_off = u_off + NB * u_bytes;
+  static constexpr int w_off = f_off + NB * u_bytes;
+  static constexpr int ring_off = ((w_off + NB * w_bytes + 127) / 128) * 128;
   static constexpr int aring_off = ring_off + kWarps * STG * BS * 4;
   static constexpr int bar_off = aring_off + kWarps * STG * AS * 4;
   static constexpr int bytes = bar_off + kWarps * STG * 8;
 };
 // ring depth (the same with attenuation, whose blocks ride in a second ring)
 __host__ __device__ constexpr int solid_stages(bool) { return kStages; }
+// patch-state buffers: the stiffness kernel gathers the next patch while it
+// computes the current one (two CTAs per SM fit), the Newmark kernel does not
+__host__ __device__ constexpr int solid_buffers(int mode) { return mode == MODE_FORCE ? 2 : 1; }
 // resident CTAs per SM the kernel is compiled for: the Newmark kernel keeps
 // three (its register-staged gather is latency-bound; 80 registers), the
 // others two (no spills at 128 registers)
@@ -608,11 +613,12 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
   constexpr uint32_t BSB = BS * 4;
   constexpr int STG = solid_stages(ANEL);
   constexpr int AS = ANEL ? kAnelSlot : 0;
-  using L = SolidSmem<NC, BS, STG, AS>;
+  constexpr int NB = solid_buffers(MODE);
+  using L = SolidSmem<NC, BS, STG, AS, NB>;
   extern __shared__ __align__(128) unsigned char smem[];
-  float(*s_u)[kMaxPatchPoints] = reinterpret_cast<float(*)[kMaxPatchPoints]>(smem + L::u_off);
-  float(*s_f)[kMaxPatchPoints] = reinterpret_cast<float(*)[kMaxPatchPoints]>(smem + L::f_off);
-  uint32_t *s_w = reinterpret_cast<uint32_t *>(smem + L::w_off);
+  auto su_of = [&](int b) { return reinterpret_cast<float(*)[kMaxPatchPoints]>(smem + L::u_off + b * L::u_bytes); };
+  auto sf_of = [&](int b) { return reinterpret_cast<float(*)[kMaxPatchPoints]>(smem + L::f_off + b * L::u_bytes); };
+  auto sw_of = [&](int b) { return reinterpret_cast<uint32_t *>(smem + L::w_off + b * L::w_bytes); };
   float *ring = reinterpret_cast<float *>(smem + L::ring_off);
   float *aring = reinterpret_cast<float *>(smem + L::aring_off);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bar_off);
@@ -620,14 +626,14 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
   // sub-round r of a patch is complete when all threads have arrived on
   // s_round[r] after their accumulations of round r
   __shared__ __align__(8) uint64_t s_round[kMaxSubrounds];
-  __shared__ __align__(8) uint64_t s_wbar;  // the patch's point words have landed in s_w
+  __shared__ __align__(8) uint64_t s_wbar[2];  // a patch's point words have landed in buffer b
   // component c of the shared arrays -> global component (mono: s, z)
   auto gc = [](int c) { return (POLE == POLE_MONO && c == 1) ? 2 : c; };
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x < kWarps * STG) mbar_init(&bars[threadIdx.x], 1);
   if (threadIdx.x < kMaxSubrounds) mbar_init(&s_round[threadIdx.x], kThreads);
-  if (threadIdx.x == 0) mbar_init(&s_wbar, 1);
+  if (threadIdx.x < 2) mbar_init(&s_wbar[threadIdx.x], 1);
   if (threadIdx.x == 0) s_stop = (MODE == MODE_NEWMARK) ? *st.blowup : 0;
   fence_mbar_init();
   __syncthreads();
@@ -646,7 +652,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
   uint64_t *my_bars = bars + warp * STG;
   uint32_t kcount = 0;  // elements this warp has consumed (slot = kcount % STG)
   uint32_t round_par = 0;  // bit r: parity of the next completion of s_round[r]
-  uint32_t pcount = 0;     // patches this CTA has started (parity of s_wbar)
+  uint32_t pcount = 0;     // patches this CTA has started: buffer pcount % NB, s_wbar parity (pcount / NB) & 1
   // cg lane index k of the attenuation points (1,1), (1,3), (3,1), (3,3)
   const bool cg = active && (i == 1 || i == 3) && (j == 1 || j == 3);
   const int kcg = 2 * (i >> 1) + (j >> 1);
@@ -666,23 +672,71 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
   float stf1 = 0.f;
   if (MODE == MODE_NEWMARK && AXG_BOUND(*st.iter - 1, st.niter, 3)) stf1 = st.stf[*st.iter - 1];
 
+  // one thread: bulk copy of a patch's point words into buffer b (each
+  // patch's words start 16-byte aligned, padded to a multiple of four)
+  auto issue_words = [&](int b, int32_t pt_start, int n_pts) {
+    const uint32_t nw = ((uint32_t)n_pts + 3u) & ~3u;
+    if (nw > 0 && AXG_BOUND((int64_t)pt_start + nw - 1, d.n_pts, 1)) {
+      fence_proxy_async();  // earlier generic reads of the buffer precede the async-proxy write
+      bulk_g2s(sw_of(b), d.pts + pt_start, nw * 4u, &s_wbar[b], pol);
+    } else {
+      mbar_arrive(&s_wbar[b]);
+    }
+  };
+  // every thread (stiffness mode): asynchronous 4-byte copies of its points'
+  // u, and of the partial sums of points an earlier writer (earlier colour,
+  // coupling pre-pass) holds, straight into buffer b.  A point's accumulator
+  // starts from that partial sum, so that the write-back is a plain store.
+  auto issue_gather = [&](int b, int n_pts) {
+    float(*gu)[kMaxPatchPoints] = su_of(b);
+    float(*gf)[kMaxPatchPoints] = sf_of(b);
+    const uint32_t *gw = sw_of(b);
+    for (int t = threadIdx.x; t < n_pts; t += kThreads) {
+      const uint32_t w = gw[t];
+      const uint32_t g = w & kPtIndexMask;
+      if (!AXG_BOUND(g, st.nglob, 1)) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) gu[c][t] = gf[c][t] = 0.f;
+        continue;
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        cp_async4(&gu[c][t], st.u[gc(c)] + g);
+        if (w & kPtFirst) gf[c][t] = 0.f;
+        else cp_async4(&gf[c][t], st.f[gc(c)] + g);
+      }
+    }
+    cp_async_commit();
+  };
+  // stiffness mode: the CTA's first patch is gathered here, each later one
+  // while the CTA computes the patch before it
+  if (MODE == MODE_FORCE && blockIdx.x < n_colour_patches && AXG_BOUND(d.patch_begin + blockIdx.x, d.n_patches, 1)) {
+    const PatchMeta m0 = d.meta[d.patch_begin + blockIdx.x];
+    if (threadIdx.x == 0) issue_words(0, m0.pt_start, m0.n_pts);
+    mbar_wait_bounded(&s_wbar[0], 0u, st.err);
+    issue_gather(0, m0.n_pts);
+  }
+
   for (int pp = blockIdx.x; pp < n_colour_patches; pp += gridDim.x) {
     if (!AXG_BOUND(d.patch_begin + pp, d.n_patches, 1)) break;
     const PatchMeta m = d.meta[d.patch_begin + pp];
-
-    // 0. bulk copy of the patch's point words into s_w (each patch's words
-    //    start 16-byte aligned, padded to a multiple of four)
-    if (threadIdx.x == 0) {
-      const uint32_t nw = ((uint32_t)m.n_pts + 3u) & ~3u;
-      if (nw > 0 && AXG_BOUND((int64_t)m.pt_start + nw - 1, d.n_pts, 1)) {
-        fence_proxy_async();  // the previous patch's reads of s_w precede the async-proxy write
-        bulk_g2s(s_w, d.pts + m.pt_start, nw * 4u, &s_wbar, pol);
-      } else {
-        mbar_arrive(&s_wbar);
+    const int buf = pcount % NB;
+    float(*s_u)[kMaxPatchPoints] = su_of(buf);
+    float(*s_f)[kMaxPatchPoints] = sf_of(buf);
+    const uint32_t *s_w = sw_of(buf);
+    // stiffness mode: the next patch's point words go to the other buffer now
+    int next_npts = 0;
+    if (MODE == MODE_FORCE) {
+      const int ppn = pp + gridDim.x;
+      if (ppn < n_colour_patches && AXG_BOUND(d.patch_begin + ppn, d.n_patches, 1)) {
+        const PatchMeta mn = d.meta[d.patch_begin + ppn];
+        next_npts = mn.n_pts;
+        if (threadIdx.x == 0) issue_words(buf ^ 1, mn.pt_start, mn.n_pts);
       }
+    } else if (threadIdx.x == 0) {
+      issue_words(0, m.pt_start, m.n_pts);
     }
-    // this warp's first STG element blocks (stiffness mode: after the gather's
-    // loads are issued, so that those are not queued behind the blocks)
+    // this warp's first STG element blocks
     WarpIter pf{0, warp};
     auto prefetch_first = [&]() {
       pf = WarpIter{0, warp};
@@ -699,30 +753,11 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
     // 1. gather.  A point that an earlier writer (coupling pre-pass, earlier
     //    colour) already holds a partial sum for starts its accumulator from
     //    that sum, so that the write-back is a plain store.
-    if (MODE != MODE_FORCE) prefetch_first();
-    mbar_wait_bounded(&s_wbar, pcount & 1u, st.err);
-    ++pcount;
+    prefetch_first();
     if (MODE == MODE_FORCE) {
-      // asynchronous 4-byte copies straight into shared memory: all of a
-      // thread's loads are in flight at once
-      for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
-        const uint32_t w = s_w[t];
-        const uint32_t g = w & kPtIndexMask;
-        if (!AXG_BOUND(g, st.nglob, 1)) {
-#pragma unroll
-          for (int c = 0; c < NC; ++c) s_u[c][t] = s_f[c][t] = 0.f;
-          continue;
-        }
-#pragma unroll
-        for (int c = 0; c < NC; ++c) {
-          cp_async4(&s_u[c][t], st.u[gc(c)] + g);
-          if (w & kPtFirst) s_f[c][t] = 0.f;
-          else cp_async4(&s_f[c][t], st.f[gc(c)] + g);
-        }
-      }
-      prefetch_first();
-      cp_async_wait_all();
+      cp_async_wait_all();  // this thread's copies of the patch (issued during the previous one)
     } else {
+      mbar_wait_bounded(&s_wbar[0], pcount & 1u, st.err);
       // Newmark predictor on the fly, four points per thread in flight
       for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += 4 * kThreads) {
         uint32_t w[4];
@@ -860,6 +895,11 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
       }
       mbar_arrive(&s_round[r]);  // this thread's accumulations of round r are done
       r0 = r1;
+      if (MODE == MODE_FORCE && r == 0 && next_npts > 0) {
+        // the next patch's words have landed in the other buffer: start its gather
+        mbar_wait_bounded(&s_wbar[buf ^ 1], ((pcount + 1) / NB) & 1u, st.err);
+        issue_gather(buf ^ 1, next_npts);
+      }
     }
     round_par ^= (1u << m.n_rounds) - 1u;  // each used s_round completed once in this patch
     __syncthreads();
@@ -900,6 +940,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
       }
     }
     __syncthreads();
+    ++pcount;
   }
 }
 
