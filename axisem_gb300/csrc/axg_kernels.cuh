@@ -587,17 +587,36 @@ __host__ __device__ constexpr int solid_buffers(int mode) { return mode == MODE_
 // others two (no spills at 128 registers)
 __host__ __device__ constexpr int solid_min_ctas(int mode, bool anel) { return mode == MODE_NEWMARK && !anel ? 3 : 2; }
 
+// the sub-round ends of a patch held in registers (8 bits per round), so
+// that no per-patch array is indexed at run time: a PatchMeta indexed that
+// way lives in local memory, and each lookup is a local load
+struct PatchRounds {
+  uint64_t lo;  // round_end[0..7]
+  uint32_t hi;  // round_end[8..11]
+  int n;
+  __device__ __forceinline__ explicit PatchRounds(const PatchMeta &m) : lo(0), hi(0), n(m.n_rounds) {
+    static_assert(kMaxSubrounds <= 12, "PatchRounds holds 12 rounds");
+#pragma unroll
+    for (int r = 0; r < 8; ++r) lo |= (uint64_t)m.round_end[r] << (8 * r);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) hi |= (uint32_t)m.round_end[8 + r] << (8 * r);
+  }
+  __device__ __forceinline__ int end(int r) const {
+    return r < 8 ? (int)((lo >> (8 * r)) & 0xFFu) : (int)((hi >> (8 * (r - 8))) & 0xFFu);
+  }
+};
+
 // the elements warp `w` processes in a patch, in order: sub-round by
 // sub-round, elements w, w + kWarps, ... of each round
 struct WarpIter {
   int r, s;
-  __device__ __forceinline__ void norm(const PatchMeta &m, int w) {
-    while (r < m.n_rounds && s >= m.round_end[r]) {
+  __device__ __forceinline__ void norm(const PatchRounds &m, int w) {
+    while (r < m.n && s >= m.end(r)) {
       ++r;
-      s = m.round_end[r - 1] + w;
+      s = m.end(r - 1) + w;
     }
   }
-  __device__ __forceinline__ bool valid(const PatchMeta &m) const { return r < m.n_rounds; }
+  __device__ __forceinline__ bool valid(const PatchRounds &m) const { return r < m.n; }
 };
 
 // ANEL (time loop only): attenuation of the solid, the anelastic stiffness
@@ -720,6 +739,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
   for (int pp = blockIdx.x; pp < n_colour_patches; pp += gridDim.x) {
     if (!AXG_BOUND(d.patch_begin + pp, d.n_patches, 1)) break;
     const PatchMeta m = d.meta[d.patch_begin + pp];
+    const PatchRounds pr(m);
     const int buf = pcount % NB;
     float(*s_u)[kMaxPatchPoints] = su_of(buf);
     float(*s_f)[kMaxPatchPoints] = sf_of(buf);
@@ -740,14 +760,14 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
     WarpIter pf{0, warp};
     auto prefetch_first = [&]() {
       pf = WarpIter{0, warp};
-      pf.norm(m, warp);
-      for (int q = 0; q < STG && pf.valid(m); ++q) {
+      pf.norm(pr, warp);
+      for (int q = 0; q < STG && pf.valid(pr); ++q) {
         if (lane == 0) {
           const int64_t el = (int64_t)m.elem_start + pf.s;
           if (AXG_BOUND(el, d.n_elem, 2)) issue((kcount + q) % STG, el);
         }
         pf.s += kWarps;
-        pf.norm(m, warp);
+        pf.norm(pr, warp);
       }
     };
     // 1. gather.  A point that an earlier writer (coupling pre-pass, earlier
@@ -797,8 +817,8 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
 
     // 2. elements, sub-round by sub-round
     int r0 = 0;
-    for (int r = 0; r < m.n_rounds; ++r) {
-      const int r1 = m.round_end[r];
+    for (int r = 0; r < pr.n; ++r) {
+      const int r1 = pr.end(r);
       bool ready = r == 0;  // round r-1 complete (waited for)
       for (int s = r0 + warp; s < r1; s += kWarps) {
         int64_t el = (int64_t)m.elem_start + s;
@@ -882,14 +902,14 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
         }
         // the slot is free again: start the copy of the element STG ahead
         __syncwarp();
-        if (pf.valid(m)) {
+        if (pf.valid(pr)) {
           if (lane == 0) {
             const int64_t pel = (int64_t)m.elem_start + pf.s;
             fence_proxy_async();  // the warp's reads of the slot precede the async-proxy write
             if (AXG_BOUND(pel, d.n_elem, 2)) issue(slot, pel);
           }
           pf.s += kWarps;
-          pf.norm(m, warp);
+          pf.norm(pr, warp);
         }
         ++kcount;
       }
@@ -901,7 +921,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
         issue_gather(buf ^ 1, next_npts);
       }
     }
-    round_par ^= (1u << m.n_rounds) - 1u;  // each used s_round completed once in this patch
+    round_par ^= (1u << pr.n) - 1u;  // each used s_round completed once in this patch
     __syncthreads();
 
     // 3. write-back
@@ -978,9 +998,10 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
   LaneCoef coef;
   load_coef(sp, i, j, coef);
   const float stf1 = AXG_BOUND(*st.iter - 1, st.niter, 12) ? st.stf[*st.iter - 1] : 0.f;
+  const PatchRounds pr(m);
   int r0 = 0;
-  for (int r = 0; r < m.n_rounds; ++r) {
-    const int r1 = m.round_end[r];
+  for (int r = 0; r < pr.n; ++r) {
+    const int r1 = pr.end(r);
     for (int s = r0 + warp; s < r1; s += kWarps) {
       int64_t el = (int64_t)m.elem_start + s;
       if (!AXG_BOUND(el, d.n_elem, 12)) el = 0;
