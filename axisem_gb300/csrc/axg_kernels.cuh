@@ -418,15 +418,19 @@ struct AnelArgs {
 // takes S1 at (1,j), (3,j); X2(i,j) for i in {1,3} takes S2 at (i,1), (i,3).
 template <int POLE, bool AX>
 __device__ __forceinline__ void anel_stiffness(const LaneCoef &c, const float *cs, const float *R, int nsls,
-                                               bool cg, int k, int i, int j, bool active, float &f0, float &f1,
-                                               float &f2) {
+                                               bool cg, int k, int i, int j, bool active, int lane, float &f0,
+                                               float &f1, float &f2) {
   float S1a = 0.f, S2a = 0.f, S1b = 0.f, S2b = 0.f, S1z = 0.f, S2z = 0.f;
   float ya = 0.f, yb = 0.f, yz = 0.f;
-  if (cg) {
-    float r[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int q = 0; q < nsls; ++q)
+  // lanes 0..23 sum entry (component lane / 4, cg point lane % 4) over the
+  // SLS; cg lane k then collects its six components
+  float rs = 0.f;
+  if (lane < 24)
+    for (int q = 0; q < nsls; ++q) rs = rs + R[q * 24 + lane];
+  float r[6];
 #pragma unroll
-      for (int v = 0; v < 6; ++v) r[v] = r[v] + R[(q * 6 + v) * 4 + k];
+  for (int v = 0; v < 6; ++v) r[v] = __shfl_sync(kFull, rs, (v * 4 + k) & 31);
+  if (cg) {
     const float vse = cs[A_VSE + k], vsx = cs[A_VSX + k], vze = cs[A_VZE + k], vzx = cs[A_VZX + k];
     const float yl = cs[A_Y + k];
     if (POLE == POLE_DI) {
@@ -480,83 +484,78 @@ __device__ __forceinline__ void anel_stiffness(const LaneCoef &c, const float *c
   }
 }
 
-// Memory-variable time step of one cg lane (time_step_memvars_cg4,
+// Memory-variable time step of an element (time_step_memvars_cg4,
 // SOLVER/attenuation.f90:81-202) with the strain of
-// compute_strain_att_el_cg4 (:471-535): gx, ge are the lane's first-stage
-// derivatives d/dxi, d/deta of the three displacement components, u its
-// (predicted, axis-masked) displacement.  The gradient at a cg point is
+// compute_strain_att_el_cg4 (:471-535).  The four cg lanes form the strain
+// at their point: gx, ge are the lane's first-stage derivatives d/dxi,
+// d/deta of the three displacement components, u its (predicted,
+// axis-masked) displacement; the gradient at a cg point is
 // axisym_gradient_solid_el_cg4 (SOLVER/pointwise_derivatives.f90:216-250),
-// f/s is f_over_s_solid_el_cg4 (:55-75) with the stored 1/s.  Updates the
-// state R (shared memory) in place.
+// f/s is f_over_s_solid_el_cg4 (:55-75) with the stored 1/s.  They leave the
+// step's sources in `scr` (src_dev(v,k) at 4v+k, src_tr(k) at 24+k); then
+// every lane of the warp updates memory variables R(k,v,j) (entry
+// 24j + 4v + k) in place, and the sources become the previous step's.
 template <int POLE>
-__device__ __forceinline__ void anel_memvar_step(const float *cs, float *R, const AnelArgs &an, int k,
-                                                 const float (&u)[3], const float (&gx)[3], const float (&ge)[3]) {
-  const float dsdeta = cs[A_DSDETA + k], dzdeta = cs[A_DZDETA + k];
-  const float dsdxi = cs[A_DSDXI + k], dzdxi = cs[A_DZDXI + k], invs = cs[A_INVS + k];
-  auto grad_s = [&](float m1, float m2) { return dzdeta * m1 + dzdxi * m2; };
-  auto grad_z = [&](float m1, float m2) { return dsdeta * m1 + dsdxi * m2; };
-  float g[6];
-  float b1x = gx[0], b1e = ge[0];
-  if (POLE == POLE_DI) {
-    b1x = gx[0] + gx[1];
-    b1e = ge[0] + ge[1];
-  }
-  const float b1s = grad_s(b1x, b1e), b1z = grad_z(b1x, b1e);
-  const float b2s = grad_s(gx[2], ge[2]), b2z = grad_z(gx[2], ge[2]);
-  g[0] = b1s;
-  g[2] = b2z;
-  g[4] = b1z + b2s;
-  if (POLE == POLE_MONO) {
-    g[1] = invs * u[0];
-    g[3] = 0.f;
-    g[5] = 0.f;
-  } else if (POLE == POLE_DI) {
-    g[1] = 2.f * (invs * u[1]);
-    const float cx = gx[0] - gx[1], ce = ge[0] - ge[1];
-    g[3] = -(invs * u[2]) - grad_z(cx, ce);
-    g[5] = -g[1] - grad_s(cx, ce);
-  } else {
-    g[1] = invs * (u[0] - 2.f * u[1]);
-    g[3] = -2.f * (invs * u[2]) - grad_z(gx[1], ge[1]);
-    g[5] = invs * (u[1] - 2.f * u[0]) - grad_s(gx[1], ge[1]);
-  }
-  const float tr = g[0] + g[1] + g[2];
-  const float dm = cs[A_DMU + k], dka = cs[A_DKA + k];
-  const float src_tr = dka * tr;
-  float sd[6];
-#pragma unroll
-  for (int v = 0; v < 3; ++v) sd[v] = (dm * 2.f) * (g[v] - tr * (1.f / 3.f));
-  sd[4] = dm * g[4];
-  sd[3] = POLE == POLE_MONO ? 0.f : dm * g[3];
-  sd[5] = POLE == POLE_MONO ? 0.f : dm * g[5];
+__device__ __forceinline__ void anel_memvar_step(const float *cs, float *R, float *scr, const AnelArgs &an, bool cg,
+                                                 int k, int lane, const float (&u)[3], const float (&gx)[3],
+                                                 const float (&ge)[3]) {
   const int nsls = an.nsls;
   float *trm1 = R + 24 * nsls, *dm1 = trm1 + 4;
-  const float tr_old = trm1[k];
-  float dev_old[6];
+  if (cg) {
+    const float dsdeta = cs[A_DSDETA + k], dzdeta = cs[A_DZDETA + k];
+    const float dsdxi = cs[A_DSDXI + k], dzdxi = cs[A_DZDXI + k], invs = cs[A_INVS + k];
+    auto grad_s = [&](float m1, float m2) { return dzdeta * m1 + dzdxi * m2; };
+    auto grad_z = [&](float m1, float m2) { return dsdeta * m1 + dsdxi * m2; };
+    float g[6];
+    float b1x = gx[0], b1e = ge[0];
+    if (POLE == POLE_DI) {
+      b1x = gx[0] + gx[1];
+      b1e = ge[0] + ge[1];
+    }
+    const float b1s = grad_s(b1x, b1e), b1z = grad_z(b1x, b1e);
+    const float b2s = grad_s(gx[2], ge[2]), b2z = grad_z(gx[2], ge[2]);
+    g[0] = b1s;
+    g[2] = b2z;
+    g[4] = b1z + b2s;
+    if (POLE == POLE_MONO) {
+      g[1] = invs * u[0];
+      g[3] = 0.f;
+      g[5] = 0.f;
+    } else if (POLE == POLE_DI) {
+      g[1] = 2.f * (invs * u[1]);
+      const float cx = gx[0] - gx[1], ce = ge[0] - ge[1];
+      g[3] = -(invs * u[2]) - grad_z(cx, ce);
+      g[5] = -g[1] - grad_s(cx, ce);
+    } else {
+      g[1] = invs * (u[0] - 2.f * u[1]);
+      g[3] = -2.f * (invs * u[2]) - grad_z(gx[1], ge[1]);
+      g[5] = invs * (u[1] - 2.f * u[0]) - grad_s(gx[1], ge[1]);
+    }
+    const float tr = g[0] + g[1] + g[2];
+    const float dm = cs[A_DMU + k];
 #pragma unroll
-  for (int v = 0; v < 6; ++v) dev_old[v] = dm1[v * 4 + k];
+    for (int v = 0; v < 3; ++v) scr[4 * v + k] = (dm * 2.f) * (g[v] - tr * (1.f / 3.f));
+    scr[12 + k] = POLE == POLE_MONO ? 0.f : dm * g[3];
+    scr[16 + k] = dm * g[4];
+    scr[20 + k] = POLE == POLE_MONO ? 0.f : dm * g[5];
+    scr[24 + k] = cs[A_DKA + k] * tr;
+  }
+  __syncwarp();
   int qmu = __float_as_int(cs[A_QMU]), qka = __float_as_int(cs[A_QKA]);
   if (!AXG_BOUND(qmu, an.n_q, 4)) qmu = 0;
   if (!AXG_BOUND(qka, an.n_q, 4)) qka = 0;
   const float *tmu = an.qtab + qmu * 2 * kMaxSls, *tka = an.qtab + qka * 2 * kMaxSls;
-  for (int q = 0; q < nsls; ++q) {
-    const float ctm = __ldg(tmu + q), ctm1m = __ldg(tmu + kMaxSls + q);
-    const float ctk = __ldg(tka + q), ctm1k = __ldg(tka + kMaxSls + q);
-    const float e = an.ex[q];
-    const float trb = ctk * src_tr + ctm1k * tr_old;
-    float *Rq = R + q * 24 + k;
-#pragma unroll
-    for (int v = 0; v < 6; ++v) {
-      if (POLE == POLE_MONO && (v == 3 || v == 5)) continue;
-      const float db = ctm * sd[v] + ctm1m * dev_old[v];
-      float nv = e * Rq[v * 4] + db;
-      if (v < 3) nv = nv + trb;
-      Rq[v * 4] = nv;
-    }
+  for (int e = lane; e < 24 * nsls; e += 32) {
+    const int q = e / 24, vk = e - 24 * q, v = vk >> 2, kk = vk & 3;
+    if (POLE == POLE_MONO && (v == 3 || v == 5)) continue;  // never written for the monopole
+    const float db = __ldg(tmu + q) * scr[vk] + __ldg(tmu + kMaxSls + q) * dm1[vk];
+    float nv = an.ex[q] * R[e] + db;
+    if (v < 3) nv = nv + (__ldg(tka + q) * scr[24 + kk] + __ldg(tka + kMaxSls + q) * trm1[kk]);
+    R[e] = nv;
   }
-  trm1[k] = src_tr;
-#pragma unroll
-  for (int v = 0; v < 6; ++v) dm1[v * 4 + k] = sd[v];
+  __syncwarp();
+  if (lane < 4) trm1[lane] = scr[24 + lane];
+  else if (lane < 28) dm1[lane - 4] = scr[lane - 4];
 }
 
 // ------------------------------------------------------------ solid patch kernel
@@ -574,7 +573,8 @@ struct SolidSmem {
   static constexpr int w_off = f_off + NB * u_bytes;
   static constexpr int ring_off = ((w_off + NB * w_bytes + 127) / 128) * 128;
   static constexpr int aring_off = ring_off + kWarps * STG * BS * 4;
-  static constexpr int bar_off = aring_off + kWarps * STG * AS * 4;
+  static constexpr int scr_off = aring_off + kWarps * STG * AS * 4;     // attenuation: 32 floats per warp
+  static constexpr int bar_off = scr_off + (AS > 0 ? kWarps * 32 * 4 : 0);
   static constexpr int bytes = bar_off + kWarps * STG * 8;
 };
 // ring depth (the same with attenuation, whose blocks ride in a second ring)
@@ -624,7 +624,8 @@ struct WarpIter {
 // SOLVER/time_evol_wave.F90 (anel_true, cg4).
 template <int POLE, int MODE, bool ANEL>
 __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
-    solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches, AnelArgs an) {
+    solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches,
+                       const __grid_constant__ AnelArgs an) {  // an.ex[] is indexed at run time
   static_assert(!ANEL || MODE == MODE_NEWMARK, "attenuation runs in the time loop only");
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
   constexpr int NT = n_terms(POLE), NA = n_axial(POLE);
@@ -640,6 +641,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
   auto sw_of = [&](int b) { return reinterpret_cast<uint32_t *>(smem + L::w_off + b * L::w_bytes); };
   float *ring = reinterpret_cast<float *>(smem + L::ring_off);
   float *aring = reinterpret_cast<float *>(smem + L::aring_off);
+  float *scr = reinterpret_cast<float *>(smem + L::scr_off);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bar_off);
   __shared__ int s_stop;
   // sub-round r of a patch is complete when all threads have arrived on
@@ -867,8 +869,8 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
         }
         float *ablk = my_aring + slot * AS;  // attenuation constants, then state
         if (ANEL) {
-          if (ax) anel_stiffness<POLE, true>(coef, ablk, ablk + kAnelConst, an.nsls, cg, kcg, i, j, active, f0, f1, f2);
-          else anel_stiffness<POLE, false>(coef, ablk, ablk + kAnelConst, an.nsls, cg, kcg, i, j, active, f0, f1, f2);
+          if (ax) anel_stiffness<POLE, true>(coef, ablk, ablk + kAnelConst, an.nsls, cg, kcg, i, j, active, lane, f0, f1, f2);
+          else anel_stiffness<POLE, false>(coef, ablk, ablk + kAnelConst, an.nsls, cg, kcg, i, j, active, lane, f0, f1, f2);
         }
         if (ax && i == 0) {  // axis mask of acc1
           if (POLE == POLE_MONO) f0 = 0.f;
@@ -894,7 +896,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
           // memory variables of this step from the predicted, masked
           // displacement (time_step_memvars after pdistsum_solid in
           // SOLVER/time_evol_wave.F90), then the element's state back to HBM
-          if (cg) anel_memvar_step<POLE>(ablk, ablk + kAnelConst, an, kcg, u, gx, ge);
+          anel_memvar_step<POLE>(ablk, ablk + kAnelConst, scr + warp * 32, an, cg, kcg, lane, u, gx, ge);
           __syncwarp();
           const float4 *src4 = reinterpret_cast<const float4 *>(ablk + kAnelConst);
           float4 *dst4 = reinterpret_cast<float4 *>(an.state + el * an.state_stride);
