@@ -355,21 +355,21 @@ __device__ __forceinline__ void stiff_quad(const LaneCoef &c, const float *blk, 
 }
 
 // glob_fluid_stiffness_4 (SOLVER/stiffness_fluid.f90:139-216)
+// mt: the lane's M1chi, M2chi, M4chi (and M_w_fl) values
 template <bool AX, bool NONMONO>
-__device__ __forceinline__ float stiff_fluid(const LaneCoef &c, const float *blk, const float *m0, int lane,
-                                             int i, int j, float chi) {
+__device__ __forceinline__ float stiff_fluid(const LaneCoef &c, const float (&mt)[4], const float *m0, int i,
+                                             int j, float chi) {
   const int j5 = 5 * j;
   float X1 = dxi(chi, cxi<AX>(c), j5);
   float X2 = deta(chi, c.eta, i);
-  const float m1 = __ldcs(blk + 0 * 25 + lane), m2 = __ldcs(blk + 1 * 25 + lane),
-              m4 = __ldcs(blk + 2 * 25 + lane);
+  const float m1 = mt[0], m2 = mt[1], m4 = mt[2];
   const float S1 = m1 * X2 + m2 * X1;
   const float S2 = m1 * X1 + m4 * X2;
   X1 = dxi(S1, csxi<AX>(c), j5);
   X2 = deta(S2, c.seta, i);
   float loc = X1 + X2;
   if (NONMONO) {
-    loc = loc + __ldcs(blk + 3 * 25 + lane) * chi;
+    loc = loc + mt[3] * chi;
     if (AX) {
       const float V1 = dxi(chi, c.g0, j5);
       loc = loc + c.g0i * (m0[j] * V1);
@@ -780,17 +780,19 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
       cp_async_wait_all();  // this thread's copies of the patch (issued during the previous one)
     } else {
       mbar_wait_bounded(&s_wbar[0], pcount & 1u, st.err);
-      // Newmark predictor on the fly, four points per thread in flight
-      for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += 4 * kThreads) {
-        uint32_t w[4];
-        float uu[4][NC], ff[4][NC];
+      // Newmark predictor on the fly; kGB points per thread in flight cover
+      // a whole patch (kGB * kThreads >= kMaxPatchPoints): one memory latency
+      constexpr int kGB = (kMaxPatchPoints + kThreads - 1) / kThreads;
+      for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += kGB * kThreads) {
+        uint32_t w[kGB];
+        float uu[kGB][NC], ff[kGB][NC];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < kGB; ++q) {
           const int t = t0 + q * kThreads;
           w[q] = t < m.n_pts ? s_w[t] : kPtPad;
         }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < kGB; ++q) {
           const uint32_t g = w[q] & kPtIndexMask;
           const bool ok = w[q] != kPtPad && AXG_BOUND(g, st.nglob, 1);
           const bool part = ok && !(w[q] & kPtFirst);
@@ -803,7 +805,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
           }
         }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < kGB; ++q) {
           const int t = t0 + q * kThreads;
           if (t < m.n_pts) {
 #pragma unroll
@@ -927,38 +929,69 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
     __syncthreads();
 
     // 3. write-back
-    for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
-      const uint32_t w = s_w[t];
-      const uint32_t g = w & kPtIndexMask;
-      if (!AXG_BOUND(g, st.nglob, 3)) continue;
-      float v[NC];
+    if (MODE == MODE_FORCE) {
+      for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
+        const uint32_t g = s_w[t] & kPtIndexMask;
+        if (!AXG_BOUND(g, st.nglob, 3)) continue;
 #pragma unroll
-      for (int c = 0; c < NC; ++c) v[c] = s_f[c][t];
-      if (MODE == MODE_FORCE || !(w & kPtLast)) {
-#pragma unroll
-        for (int c = 0; c < NC; ++c) st.f[gc(c)][g] = v[c];
-        continue;
+        for (int c = 0; c < NC; ++c) st.f[gc(c)][g] = s_f[c][t];
       }
-      // last writer: source, corrector, store the new state
-      if ((w & kPtSource) && stf1 != 0.f) {
-        for (int q = 0; q < st.src.n; ++q)
-          if ((uint32_t)st.src.gidx[q] == g) {
+    } else {
+      // kWB points per thread at a time: all of their loads (velocity,
+      // acceleration, inverse mass, gamma) are issued before any store, so
+      // that one memory latency covers them (stores to the same arrays would
+      // otherwise keep the compiler from hoisting the next point's loads)
+      constexpr int kWB = 3;
+      for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += kWB * kThreads) {
+        uint32_t w[kWB];
+        float vel[kWB][NC], acc[kWB][NC], im[kWB], gam[kWB];
 #pragma unroll
-            for (int c = 0; c < NC; ++c) v[c] = v[c] - st.src.val[3 * q + gc(c)] * stf1;
+        for (int q = 0; q < kWB; ++q) {
+          const int t = t0 + q * kThreads;
+          w[q] = t < m.n_pts ? s_w[t] : kPtPad;
+          const uint32_t g = w[q] & kPtIndexMask;
+          const bool last = w[q] != kPtPad && (w[q] & kPtLast) && AXG_BOUND(g, st.nglob, 3);
+          im[q] = last ? st.inv_mass[g] : 0.f;
+          gam[q] = last && st.gamma ? st.gamma[g] : 0.f;
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            vel[q][c] = last ? st.v[gc(c)][g] : 0.f;
+            acc[q][c] = last ? st.a[gc(c)][g] : 0.f;
           }
-      }
-      const float im = st.inv_mass[g];
-      const float gam = st.gamma ? st.gamma[g] : 0.f;
+        }
 #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        const int cg = gc(c);
-        float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im) * v[c] : -im * v[c];
-        const float vel = st.v[cg][g];
-        const float dsp = s_u[c][t];
-        if (st.gamma) a = a - 2.f * gam * vel - gam * gam * dsp;
-        st.v[cg][g] = fmaf(st.hdt, st.a[cg][g] + a, vel);
-        st.a[cg][g] = a;
-        st.u[cg][g] = dsp;
+        for (int q = 0; q < kWB; ++q) {
+          const int t = t0 + q * kThreads;
+          if (w[q] == kPtPad) continue;
+          const uint32_t g = w[q] & kPtIndexMask;
+          if (!AXG_BOUND(g, st.nglob, 3)) continue;
+          float v[NC];
+#pragma unroll
+          for (int c = 0; c < NC; ++c) v[c] = s_f[c][t];
+          if (!(w[q] & kPtLast)) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) st.f[gc(c)][g] = v[c];
+            continue;
+          }
+          // last writer: source, corrector, store the new state
+          if ((w[q] & kPtSource) && stf1 != 0.f) {
+            for (int k = 0; k < st.src.n; ++k)
+              if ((uint32_t)st.src.gidx[k] == g) {
+#pragma unroll
+                for (int c = 0; c < NC; ++c) v[c] = v[c] - st.src.val[3 * k + gc(c)] * stf1;
+              }
+          }
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            const int cg = gc(c);
+            float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im[q]) * v[c] : -im[q] * v[c];
+            const float dsp = s_u[c][t];
+            if (st.gamma) a = a - 2.f * gam[q] * vel[q][c] - gam[q] * gam[q] * dsp;
+            st.v[cg][g] = fmaf(st.hdt, acc[q][c] + a, vel[q][c]);
+            st.a[cg][g] = a;
+            st.u[cg][g] = dsp;
+          }
+        }
       }
     }
     __syncthreads();
@@ -968,26 +1001,50 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
 
 // ------------------------------------------------------------ fluid patch kernel
 
+// One CTA per patch.  The gather reads each point's chi, dchi, ddchi0 (and the
+// partial sum of an earlier writer) in one batch of loads per thread; each
+// warp loads the metric terms of its next element while it computes the
+// current one; the write-back loads the last writers' inverse mass, dchi and
+// ddchi0 in one batch before it stores.
 template <int NONMONO>
 __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp) {
   __shared__ float s_u[kMaxPatchPoints];
   __shared__ float s_f[kMaxPatchPoints];
   __shared__ uint32_t s_w[kMaxPatchPoints];
   constexpr int BS = block_stride(NONMONO ? 4 : 3);
+  constexpr int kGB = (kMaxPatchPoints + kThreads - 1) / kThreads;  // points per thread: one batch per patch
   __shared__ int s_stop;
   if (threadIdx.x == 0) s_stop = *st.blowup;
   __syncthreads();
   if (s_stop) return;  // uniform across the CTA
   if (!AXG_BOUND(d.patch_begin + blockIdx.x, d.n_patches, 11)) return;
   const PatchMeta m = d.meta[d.patch_begin + blockIdx.x];
-  for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
-    if (!AXG_BOUND(t, kMaxPatchPoints, 11) || !AXG_BOUND(m.pt_start + t, d.n_pts, 11)) continue;
-    const uint32_t w = d.pts[m.pt_start + t];
-    const uint32_t g = w & kPtIndexMask;
-    s_w[t] = w;
-    if (!AXG_BOUND(g, st.nglob, 11)) continue;
-    s_u[t] = predict(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2);
-    s_f[t] = 0.f;
+  {
+    uint32_t w[kGB];
+    float uu[kGB], ff[kGB];
+#pragma unroll
+    for (int q = 0; q < kGB; ++q) {
+      const int t = threadIdx.x + q * kThreads;
+      w[q] = (t < m.n_pts && AXG_BOUND(m.pt_start + t, d.n_pts, 11)) ? d.pts[m.pt_start + t] : kPtPad;
+    }
+#pragma unroll
+    for (int q = 0; q < kGB; ++q) {
+      const uint32_t g = w[q] & kPtIndexMask;
+      const bool ok = w[q] != kPtPad && AXG_BOUND(g, st.nglob, 11);
+      uu[q] = ok ? predict(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2) : 0.f;
+      // a point an earlier writer (coupling pre-pass, earlier colour) holds a
+      // partial sum for starts from that sum: the write-back only stores
+      ff[q] = ok && !(w[q] & kPtFirst) ? st.f[0][g] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < kGB; ++q) {
+      const int t = threadIdx.x + q * kThreads;
+      if (t < m.n_pts) {
+        s_w[t] = w[q];
+        s_u[t] = uu[q];
+        s_f[t] = ff[q];
+      }
+    }
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1001,53 +1058,92 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
   load_coef(sp, i, j, coef);
   const float stf1 = AXG_BOUND(*st.iter - 1, st.niter, 12) ? st.stf[*st.iter - 1] : 0.f;
   const PatchRounds pr(m);
+  // an element's data as this lane needs it
+  struct FluidElem {
+    float mt[4];
+    int32_t info;
+    int idx;
+  };
+  auto load_elem = [&](int s_) {
+    FluidElem e;
+    int64_t el = (int64_t)m.elem_start + s_;
+    if (!AXG_BOUND(el, d.n_elem, 12)) el = 0;
+    const float *blk = d.metric + el * BS;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) e.mt[t] = (t < (NONMONO ? 4 : 3)) ? __ldcs(blk + t * 25 + ml) : 0.f;
+    e.info = __ldg(d.elinfo + el);
+    e.idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
+    return e;
+  };
+  WarpIter it{0, warp};
+  it.norm(pr, warp);
+  FluidElem cur{};
+  if (it.valid(pr)) cur = load_elem(it.s);
   int r0 = 0;
   for (int r = 0; r < pr.n; ++r) {
     const int r1 = pr.end(r);
     for (int s = r0 + warp; s < r1; s += kWarps) {
+      // start the loads of this warp's next element (in this or a later round)
+      WarpIter nxt = it;
+      nxt.s += kWarps;
+      nxt.norm(pr, warp);
+      FluidElem nx{};
+      if (nxt.valid(pr)) nx = load_elem(nxt.s);
       int64_t el = (int64_t)m.elem_start + s;
       if (!AXG_BOUND(el, d.n_elem, 12)) el = 0;
-      const int32_t info = __ldg(d.elinfo + el);
-      int axslot = (info & 0xFFFFFF) - 1;
+      int axslot = (cur.info & 0xFFFFFF) - 1;
       if (axslot >= 0 && !AXG_BOUND((int64_t)(axslot + 1) * 5 - 1, d.n_m0, 12)) axslot = -1;
-      const int srcslot = ((info >> 24) & 0xF) - 1;
+      const int srcslot = ((cur.info >> 24) & 0xF) - 1;
       const bool ax = axslot >= 0;
-      const float *blk = d.metric + el * BS;
-      int idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
+      int idx = cur.idx;
       if (!AXG_BOUND(idx, m.n_pts, 12)) idx = 0;
       float chi = active ? s_u[idx] : 0.f;
       if (NONMONO && ax && i == 0) chi = 0.f;  // apply_axis_mask_scal(chi)
       const float *m0 = ax ? d.m0 + (int64_t)axslot * 5 : nullptr;
-      float f = ax ? stiff_fluid<true, NONMONO>(coef, blk, m0, ml, i, j, chi)
-                   : stiff_fluid<false, NONMONO>(coef, blk, m0, ml, i, j, chi);
+      float f = ax ? stiff_fluid<true, NONMONO>(coef, cur.mt, m0, i, j, chi)
+                   : stiff_fluid<false, NONMONO>(coef, cur.mt, m0, i, j, chi);
       if (srcslot >= 0 && stf1 != 0.f && active) f = f - d.srcfl[srcslot * 25 + lane] * stf1;
       if (NONMONO && ax && i == 0) f = 0.f;
       if (d.fsmask && active) f = f * d.fsmask[el * 25 + lane];
       if (active) s_f[idx] += f;
+      cur = nx;
+      it = nxt;
     }
     r0 = r1;
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < m.n_pts; t += kThreads) {
-    const uint32_t w = s_w[t];
-    const uint32_t g = w & kPtIndexMask;
-    if (!AXG_BOUND(g, st.nglob, 13)) continue;
-    float v = s_f[t];
-    if (!(w & kPtFirst)) v = st.f[0][g] + v;
-    if (!(w & kPtLast)) {
-      st.f[0][g] = v;
-      continue;
+  {
+    uint32_t w[kGB];
+    float vel[kGB], acc[kGB], im[kGB], gam[kGB];
+#pragma unroll
+    for (int q = 0; q < kGB; ++q) {
+      const int t = threadIdx.x + q * kThreads;
+      w[q] = t < m.n_pts ? s_w[t] : kPtPad;
+      const uint32_t g = w[q] & kPtIndexMask;
+      const bool last = w[q] != kPtPad && (w[q] & kPtLast) && AXG_BOUND(g, st.nglob, 13);
+      im[q] = last ? st.inv_mass[g] : 0.f;
+      gam[q] = last && st.gamma ? st.gamma[g] : 0.f;
+      vel[q] = last ? st.v[0][g] : 0.f;
+      acc[q] = last ? st.a[0][g] : 0.f;
     }
-    float a = -st.inv_mass[g] * v;
-    const float dchi = st.v[0][g];
-    const float chi = s_u[t];
-    if (st.gamma) {
-      const float gam = st.gamma[g];
-      a = a - 2.f * gam * dchi - gam * gam * chi;
+#pragma unroll
+    for (int q = 0; q < kGB; ++q) {
+      const int t = threadIdx.x + q * kThreads;
+      if (w[q] == kPtPad) continue;
+      const uint32_t g = w[q] & kPtIndexMask;
+      if (!AXG_BOUND(g, st.nglob, 13)) continue;
+      const float v = s_f[t];
+      if (!(w[q] & kPtLast)) {
+        st.f[0][g] = v;
+        continue;
+      }
+      float a = -im[q] * v;
+      const float chi = s_u[t];
+      if (st.gamma) a = a - 2.f * gam[q] * vel[q] - gam[q] * gam[q] * chi;
+      st.v[0][g] = fmaf(st.hdt, acc[q] + a, vel[q]);
+      st.a[0][g] = a;
+      st.u[0][g] = chi;
     }
-    st.v[0][g] = fmaf(st.hdt, st.a[0][g] + a, dchi);
-    st.a[0][g] = a;
-    st.u[0][g] = chi;
   }
 }
 
