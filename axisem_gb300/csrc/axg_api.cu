@@ -462,7 +462,7 @@ template <int POLE, int MODE, bool ANEL>
 constexpr int solid_smem_bytes() {
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;
   return SolidSmem<NC, solid_block_stride(n_terms(POLE)), solid_stages(ANEL), ANEL ? kAnelSlot : 0,
-                   solid_buffers(MODE)>::bytes;
+                   solid_buffers(MODE), solid_row(MODE, ANEL)>::bytes;
 }
 
 // sets the kernel's shared-memory attributes; *ctas = resident CTAs on the GPU

@@ -565,9 +565,9 @@ constexpr int kStages = 2;  // element blocks in flight per warp (TMA ring depth
 // shared-memory layout of the solid kernel (bytes); NB buffers of the patch
 // state (u, f, point words), STG ring stages per warp, AS floats of
 // attenuation data per stage (0 without attenuation)
-template <int NC, int BS, int STG, int AS, int NB>
+template <int NC, int BS, int STG, int AS, int NB, int ROW>
 struct SolidSmem {
-  static constexpr int u_bytes = NC * kMaxPatchPoints * 4, w_bytes = kMaxPatchPoints * 4;
+  static constexpr int u_bytes = NC * ROW * 4, w_bytes = kMaxPatchPoints * 4;
   static constexpr int u_off = 0;
   static constexpr int f_off = u_off + NB * u_bytes;
   static constexpr int w_off = f_off + NB * u_bytes;
@@ -582,6 +582,17 @@ __host__ __device__ constexpr int solid_stages(bool) { return kStages; }
 // patch-state buffers: the stiffness kernel gathers the next patch while it
 // computes the current one (two CTAs per SM fit), the Newmark kernel does not
 __host__ __device__ constexpr int solid_buffers(int mode) { return mode == MODE_FORCE ? 2 : 1; }
+// Bank swizzle of the shared point arrays: patch point t lives at
+// t + pad * (t / 32).  An element's 25 points sit in five runs of five
+// consecutive patch points, one run per element row; on structured blocks
+// the runs lie a patch width (33 for 8 x 8 patches) apart, so unpadded they
+// share only 9 of the 32 banks (5-way conflicts), padded by 4 words per 32
+// they fall on 25 distinct banks.  The two-CTA kernels have the shared
+// memory to spare; the three-CTA elastic Newmark kernel does not.
+__host__ __device__ constexpr int solid_pad(int mode, bool anel) { return mode == MODE_FORCE || anel ? 4 : 0; }
+__host__ __device__ constexpr int solid_row(int mode, bool anel) {
+  return kMaxPatchPoints + solid_pad(mode, anel) * ((kMaxPatchPoints + 31) / 32);
+}
 // resident CTAs per SM the kernel is compiled for: the Newmark kernel keeps
 // three (its register-staged gather is latency-bound; 80 registers), the
 // others two (no spills at 128 registers)
@@ -634,10 +645,12 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
   constexpr int STG = solid_stages(ANEL);
   constexpr int AS = ANEL ? kAnelSlot : 0;
   constexpr int NB = solid_buffers(MODE);
-  using L = SolidSmem<NC, BS, STG, AS, NB>;
+  constexpr int ROW = solid_row(MODE, ANEL), PAD = solid_pad(MODE, ANEL);
+  using L = SolidSmem<NC, BS, STG, AS, NB, ROW>;
   extern __shared__ __align__(128) unsigned char smem[];
-  auto su_of = [&](int b) { return reinterpret_cast<float(*)[kMaxPatchPoints]>(smem + L::u_off + b * L::u_bytes); };
-  auto sf_of = [&](int b) { return reinterpret_cast<float(*)[kMaxPatchPoints]>(smem + L::f_off + b * L::u_bytes); };
+  auto su_of = [&](int b) { return reinterpret_cast<float(*)[ROW]>(smem + L::u_off + b * L::u_bytes); };
+  auto sf_of = [&](int b) { return reinterpret_cast<float(*)[ROW]>(smem + L::f_off + b * L::u_bytes); };
+  auto spos = [](int t) { return t + PAD * (t >> 5); };  // swizzled position of patch point t
   auto sw_of = [&](int b) { return reinterpret_cast<uint32_t *>(smem + L::w_off + b * L::w_bytes); };
   float *ring = reinterpret_cast<float *>(smem + L::ring_off);
   float *aring = reinterpret_cast<float *>(smem + L::aring_off);
@@ -709,22 +722,23 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
   // coupling pre-pass) holds, straight into buffer b.  A point's accumulator
   // starts from that partial sum, so that the write-back is a plain store.
   auto issue_gather = [&](int b, int n_pts) {
-    float(*gu)[kMaxPatchPoints] = su_of(b);
-    float(*gf)[kMaxPatchPoints] = sf_of(b);
+    float(*gu)[ROW] = su_of(b);
+    float(*gf)[ROW] = sf_of(b);
     const uint32_t *gw = sw_of(b);
     for (int t = threadIdx.x; t < n_pts; t += kThreads) {
       const uint32_t w = gw[t];
       const uint32_t g = w & kPtIndexMask;
+      const int pt = spos(t);
       if (!AXG_BOUND(g, st.nglob, 1)) {
 #pragma unroll
-        for (int c = 0; c < NC; ++c) gu[c][t] = gf[c][t] = 0.f;
+        for (int c = 0; c < NC; ++c) gu[c][pt] = gf[c][pt] = 0.f;
         continue;
       }
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        cp_async4(&gu[c][t], st.u[gc(c)] + g);
-        if (w & kPtFirst) gf[c][t] = 0.f;
-        else cp_async4(&gf[c][t], st.f[gc(c)] + g);
+        cp_async4(&gu[c][pt], st.u[gc(c)] + g);
+        if (w & kPtFirst) gf[c][pt] = 0.f;
+        else cp_async4(&gf[c][pt], st.f[gc(c)] + g);
       }
     }
     cp_async_commit();
@@ -743,8 +757,8 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
     const PatchMeta m = d.meta[d.patch_begin + pp];
     const PatchRounds pr(m);
     const int buf = pcount % NB;
-    float(*s_u)[kMaxPatchPoints] = su_of(buf);
-    float(*s_f)[kMaxPatchPoints] = sf_of(buf);
+    float(*s_u)[ROW] = su_of(buf);
+    float(*s_f)[ROW] = sf_of(buf);
     const uint32_t *s_w = sw_of(buf);
     // stiffness mode: the next patch's point words go to the other buffer now
     int next_npts = 0;
@@ -810,8 +824,8 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
           if (t < m.n_pts) {
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
-              s_u[c][t] = uu[q][c];
-              s_f[c][t] = ff[q][c];
+              s_u[c][spos(t)] = uu[q][c];
+              s_f[c][spos(t)] = ff[q][c];
             }
           }
         }
@@ -835,6 +849,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
         if (axslot >= 0 && !AXG_BOUND((int64_t)(axslot + 1) * NA * 5 - 1, d.n_m0, 2)) axslot = -1;
         int idx = active ? reinterpret_cast<const uint16_t *>(blk + solid_idx_off(NT))[lane] : 0;
         if (!AXG_BOUND(idx, m.n_pts, 2)) idx = 0;
+        idx = spos(idx);
         float u[3] = {0.f, 0.f, 0.f};
         if (active) {
           u[0] = s_u[0][idx];
@@ -934,7 +949,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
         const uint32_t g = s_w[t] & kPtIndexMask;
         if (!AXG_BOUND(g, st.nglob, 3)) continue;
 #pragma unroll
-        for (int c = 0; c < NC; ++c) st.f[gc(c)][g] = s_f[c][t];
+        for (int c = 0; c < NC; ++c) st.f[gc(c)][g] = s_f[c][spos(t)];
       }
     } else {
       // kWB points per thread at a time: all of their loads (velocity,
@@ -967,7 +982,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
           if (!AXG_BOUND(g, st.nglob, 3)) continue;
           float v[NC];
 #pragma unroll
-          for (int c = 0; c < NC; ++c) v[c] = s_f[c][t];
+          for (int c = 0; c < NC; ++c) v[c] = s_f[c][spos(t)];
           if (!(w[q] & kPtLast)) {
 #pragma unroll
             for (int c = 0; c < NC; ++c) st.f[gc(c)][g] = v[c];
@@ -985,7 +1000,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
           for (int c = 0; c < NC; ++c) {
             const int cg = gc(c);
             float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im[q]) * v[c] : -im[q] * v[c];
-            const float dsp = s_u[c][t];
+            const float dsp = s_u[c][spos(t)];
             if (st.gamma) a = a - 2.f * gam[q] * vel[q][c] - gam[q] * gam[q] * dsp;
             st.v[cg][g] = fmaf(st.hdt, acc[q][c] + a, vel[q][c]);
             st.a[cg][g] = a;
