@@ -120,6 +120,7 @@ class Info(C.Structure):
         ("patch_points_solid", C.c_int64),
         ("patch_elems_solid", C.c_int32), ("growth_solid", C.c_int32),
         ("patch_elems_fluid", C.c_int32), ("growth_fluid", C.c_int32),
+        ("ctas_per_sm_force", C.c_int32), ("ctas_per_sm_step", C.c_int32),
     ]
 
 

@@ -1311,6 +1311,8 @@ int axg_get_info(axg_handle *h, axg_info *info) {
   info->growth_solid = h->ps.growth;
   info->patch_elems_fluid = h->pf.patch_elems;
   info->growth_fluid = h->pf.growth;
+  info->ctas_per_sm_force = h->solid_ctas / std::max(h->num_sms, 1);
+  info->ctas_per_sm_step = h->solid_ctas_step / std::max(h->num_sms, 1);
   return AXG_OK;
 }
 

@@ -587,9 +587,9 @@ __host__ __device__ constexpr int solid_buffers(int mode) { return mode == MODE_
 // consecutive patch points, one run per element row; on structured blocks
 // the runs lie a patch width (33 for 8 x 8 patches) apart, so unpadded they
 // share only 9 of the 32 banks (5-way conflicts), padded by 4 words per 32
-// they fall on 25 distinct banks.  The two-CTA kernels have the shared
-// memory to spare; the three-CTA elastic Newmark kernel does not.
-__host__ __device__ constexpr int solid_pad(int mode, bool anel) { return mode == MODE_FORCE || anel ? 4 : 0; }
+// they fall on 25 distinct banks.  The three-CTA elastic Newmark kernel can
+// only afford 2 words per 32 (banks i + 3j: at most 2-way conflicts).
+__host__ __device__ constexpr int solid_pad(int mode, bool anel) { return mode == MODE_FORCE || anel ? 4 : 2; }
 __host__ __device__ constexpr int solid_row(int mode, bool anel) {
   return kMaxPatchPoints + solid_pad(mode, anel) * ((kMaxPatchPoints + 31) / 32);
 }

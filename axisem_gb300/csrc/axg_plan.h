@@ -24,8 +24,9 @@ namespace axg {
 constexpr int kMaxPatchElems = 64;      // elements per patch (upper bound)
 constexpr int kMaxSubrounds = 12;       // conflict-free element groups per patch
 // points per patch: sized so that three Newmark CTAs fit on an SM (an 8 x 8
-// patch of a structured grid has 33^2 = 1089 points); growth stops at it
-constexpr int kMaxPatchPoints = 1104;
+// patch of a structured grid has 33^2 = 1089 points); growth stops at it.
+// A multiple of 4 (the point words of a patch are copied in 16-byte units).
+constexpr int kMaxPatchPoints = 1092;
 constexpr int64_t kTunePrefix = 65536;  // elements the patch-size tuner plans
 
 enum PatchGrowth { kGrowCompact = 0, kGrowLayered = 1 };

@@ -301,6 +301,8 @@ def run_gpu(args):
         "clocks": clocks,
         "gpu_launches": int(args.steps * info["kernels_per_force"]),
         "plan": {"patches": info["n_patches_solid"], "colours": info["n_colours_solid"],
+                 "patch_elems": info["patch_elems_solid"], "growth": ["compact", "layered"][info["growth_solid"]],
+                 "ctas_per_sm": info["ctas_per_sm_force"],
                  "patch_points_over_global": info["patch_points_solid"] / ng,
                  "device_gb": info["device_bytes"] / 1e9},
         "setup_s": {"mesh": round(t_mesh, 2), "create": round(t_create, 2)},
@@ -368,6 +370,7 @@ def run_timeloop(args, pole, ws, rank, anel=False):
                     f"source + 200 receivers" + (", cg4 attenuation with 5 SLS" if anel else ""),
             "algorithmic_bytes_per_step": nb, "achieved_gbs": nb / dt / 1e9,
             "frac_of_hbm": nb / dt / 1e9 / peak, "kernels_per_step": info["kernels_per_step"],
+            "solid_ctas_per_sm": info["ctas_per_sm_step"],
             "finite": bool(np.isfinite(rec).all())}
 
 

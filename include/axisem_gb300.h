@@ -262,6 +262,7 @@ typedef struct axg_info {
   int64_t patch_points_solid;         /* sum over patches of their point counts */
   int32_t patch_elems_solid, growth_solid;  /* patch shape the planner used */
   int32_t patch_elems_fluid, growth_fluid;
+  int32_t ctas_per_sm_force, ctas_per_sm_step;  /* resident solid-kernel CTAs per SM */
 } axg_info;
 int axg_get_info(axg_handle *h, axg_info *info);
 
