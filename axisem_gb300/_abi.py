@@ -59,7 +59,7 @@ AXIAL_TERMS_USED = {
 }
 
 (FIELD_DISP, FIELD_VELO, FIELD_ACC0, FIELD_CHI, FIELD_DCHI, FIELD_DDCHI0, FIELD_MEMVAR, FIELD_ATT_SRC_TR,
- FIELD_ATT_SRC_DEV) = range(9)
+ FIELD_ATT_SRC_DEV, FIELD_DISP_COMP, FIELD_VELO_COMP, FIELD_CHI_COMP, FIELD_DCHI_COMP) = range(13)
 
 _fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int32)
@@ -138,6 +138,7 @@ SIGNATURES = {
     "axg_device_count": (C.c_int, []),
     "axg_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(C.c_void_p)]),
     "axg_create_tuned": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "axg_set_compensated": (C.c_int, [C.c_void_p, C.c_int32]),
     "axg_reset": (C.c_int, [C.c_void_p]),
     "axg_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "axg_get_receivers": (C.c_int, [C.c_void_p, _fp, C.c_int32, _ip]),

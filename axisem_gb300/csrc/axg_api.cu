@@ -117,6 +117,9 @@ struct axg_handle {
   std::string err = "no error";
   int64_t kernels_per_step = 0, kernels_per_force = 0;
   int solid_ctas_step = 1;
+  // compensated (Kahan) time integration
+  bool kahan = false;
+  float *cu_s[3] = {}, *cv_s[3] = {}, *cu_f = nullptr, *cv_f = nullptr;
   // coarse-grained attenuation
   bool anel = false;
   int nsls = 0;
@@ -327,6 +330,16 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid) {
     if (use_fs) std::memcpy(fsmask.data() + 25 * s, d->fluid_free_surface_mask + 25 * e, 25 * sizeof(float));
   }
   std::vector<uint32_t> pts = pl.pt_words;
+  {
+    // points on the axis: the last writer stores their masked components as
+    // zero, as the reference's axis masks leave its state
+    std::vector<uint8_t> onaxis(fluid ? h->nglob_f : h->nglob_s, 0);
+    const std::vector<int32_t> &ig = fluid ? h->igloc_f : h->igloc_s;
+    for (int k = 0; k < nax; ++k)
+      for (int jj = 0; jj < 5; ++jj) onaxis[ig[25 * (int64_t)(axl[k] - 1) + 5 * jj] - 1] = 1;
+    for (auto &w : pts)
+      if (w != kPtPad && onaxis[w & kPtIndexMask]) w |= kPtAxis;
+  }
   if (!fluid && h->n_src > 0) {
     // mark the points that carry a solid source term
     std::vector<uint8_t> issrc(h->nglob_s, 0);
@@ -409,6 +422,10 @@ StateArgs solid_state(axg_handle *h) {
     s.a[c] = h->sa[c];
     s.f[c] = h->sf[c];
   }
+  for (int c = 0; c < 3; ++c) {
+    s.cu[c] = h->kahan ? h->cu_s[c] : nullptr;
+    s.cv[c] = h->kahan ? h->cv_s[c] : nullptr;
+  }
   s.inv_mass = h->inv_mass_s;
   s.gamma = h->gamma_s;
   s.stf = h->stf;
@@ -429,7 +446,9 @@ StateArgs solid_state(axg_handle *h) {
 
 StateArgs fluid_state(axg_handle *h) {
   StateArgs s = solid_state(h);
-  for (int c = 0; c < 3; ++c) s.u[c] = s.v[c] = s.a[c] = s.f[c] = nullptr;
+  for (int c = 0; c < 3; ++c) s.u[c] = s.v[c] = s.a[c] = s.f[c] = s.cu[c] = s.cv[c] = nullptr;
+  s.cu[0] = h->kahan ? h->cu_f : nullptr;
+  s.cv[0] = h->kahan ? h->cv_f : nullptr;
   s.u[0] = h->fu;
   s.v[0] = h->fv;
   s.a[0] = h->fa;
@@ -458,18 +477,18 @@ DomainArgs domain_args(const DomainDev &dd, const DomainPlan &pl) {
   return a;
 }
 
-template <int POLE, int MODE, bool ANEL>
+template <int POLE, int MODE, bool ANEL, bool KAHAN = false>
 constexpr int solid_smem_bytes() {
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;
   return SolidSmem<NC, solid_block_stride(n_terms(POLE)), solid_stages(ANEL), ANEL ? kAnelSlot : 0,
-                   solid_buffers(MODE), solid_row(MODE, ANEL)>::bytes;
+                   solid_buffers(MODE), solid_row(MODE, ANEL, KAHAN), KAHAN>::bytes;
 }
 
 // sets the kernel's shared-memory attributes; *ctas = resident CTAs on the GPU
-template <int POLE, int MODE, bool ANEL>
+template <int POLE, int MODE, bool ANEL, bool KAHAN>
 int prepare_solid_kernel(axg_handle *h, int *ctas) {
-  auto fn = solid_patch_kernel<POLE, MODE, ANEL>;
-  constexpr int bytes = solid_smem_bytes<POLE, MODE, ANEL>();
+  auto fn = solid_patch_kernel<POLE, MODE, ANEL, KAHAN>;
+  constexpr int bytes = solid_smem_bytes<POLE, MODE, ANEL, KAHAN>();
   CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   CK(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
@@ -479,15 +498,27 @@ int prepare_solid_kernel(axg_handle *h, int *ctas) {
   return AXG_OK;
 }
 
+// the stiffness kernel and the Newmark kernel the handle's modes select
 template <int POLE>
 int prepare_solid_kernels(axg_handle *h) {
-  int rc = prepare_solid_kernel<POLE, MODE_FORCE, false>(h, &h->solid_ctas);
+  int rc = prepare_solid_kernel<POLE, MODE_FORCE, false, false>(h, &h->solid_ctas);
   if (rc) return rc;
-  if (h->anel) return prepare_solid_kernel<POLE, MODE_NEWMARK, true>(h, &h->solid_ctas_step);
-  return prepare_solid_kernel<POLE, MODE_NEWMARK, false>(h, &h->solid_ctas_step);
+  int *c = &h->solid_ctas_step;
+  if (h->anel) {
+    return h->kahan ? prepare_solid_kernel<POLE, MODE_NEWMARK, true, true>(h, c)
+                    : prepare_solid_kernel<POLE, MODE_NEWMARK, true, false>(h, c);
+  }
+  return h->kahan ? prepare_solid_kernel<POLE, MODE_NEWMARK, false, true>(h, c)
+                  : prepare_solid_kernel<POLE, MODE_NEWMARK, false, false>(h, c);
 }
 
-template <int POLE, int MODE, bool ANEL>
+int prepare_kernels(axg_handle *h) {
+  if (h->pole == AXG_MONOPOLE) return prepare_solid_kernels<POLE_MONO>(h);
+  if (h->pole == AXG_DIPOLE) return prepare_solid_kernels<POLE_DI>(h);
+  return prepare_solid_kernels<POLE_QUAD>(h);
+}
+
+template <int POLE, int MODE, bool ANEL, bool KAHAN>
 void launch_solid_colours(axg_handle *h, cudaStream_t s) {
   DomainArgs a = domain_args(h->ds, h->ps);
   StateArgs st = solid_state(h);
@@ -496,15 +527,22 @@ void launch_solid_colours(axg_handle *h, cudaStream_t s) {
     a.patch_begin = h->ps.colour_start[c];
     const int n = h->ps.colour_start[c + 1] - h->ps.colour_start[c];
     const int grid = std::min(n, ctas);
-    solid_patch_kernel<POLE, MODE, ANEL>
-        <<<grid, kThreads, solid_smem_bytes<POLE, MODE, ANEL>(), s>>>(a, st, h->spec, n, h->an);
+    solid_patch_kernel<POLE, MODE, ANEL, KAHAN>
+        <<<grid, kThreads, solid_smem_bytes<POLE, MODE, ANEL, KAHAN>(), s>>>(a, st, h->spec, n, h->an);
   }
 }
 
 template <int POLE, int MODE>
 void launch_solid_pole(axg_handle *h, cudaStream_t s) {
-  if (MODE == MODE_NEWMARK && h->anel) launch_solid_colours<POLE, MODE_NEWMARK, true>(h, s);
-  else launch_solid_colours<POLE, MODE, false>(h, s);
+  if (MODE == MODE_FORCE) {
+    launch_solid_colours<POLE, MODE_FORCE, false, false>(h, s);
+  } else if (h->anel) {
+    if (h->kahan) launch_solid_colours<POLE, MODE_NEWMARK, true, true>(h, s);
+    else launch_solid_colours<POLE, MODE_NEWMARK, true, false>(h, s);
+  } else {
+    if (h->kahan) launch_solid_colours<POLE, MODE_NEWMARK, false, true>(h, s);
+    else launch_solid_colours<POLE, MODE_NEWMARK, false, false>(h, s);
+  }
 }
 
 template <int MODE>
@@ -542,8 +580,13 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
     for (int c = 0; c < h->pf.n_colours; ++c) {
       a.patch_begin = h->pf.colour_start[c];
       const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
-      if (h->pole == AXG_MONOPOLE) fluid_patch_kernel<0><<<n, kThreads, 0, s>>>(a, fs, h->spec);
-      else fluid_patch_kernel<1><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+      if (h->pole == AXG_MONOPOLE) {
+        if (h->kahan) fluid_patch_kernel<0, true><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+        else fluid_patch_kernel<0, false><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+      } else {
+        if (h->kahan) fluid_patch_kernel<1, true><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+        else fluid_patch_kernel<1, false><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+      }
     }
     if (h->to_solid.n > 0) {
       const int nb = (h->to_solid.n + 255) / 256;
@@ -591,6 +634,11 @@ int state_ptrs(axg_handle *h, int field, float **p, int *nc, int64_t *nglob, boo
     case AXG_FIELD_DISP: for (int c = 0; c < 3; ++c) p[c] = h->su[c]; return AXG_OK;
     case AXG_FIELD_VELO: for (int c = 0; c < 3; ++c) p[c] = h->sv[c]; return AXG_OK;
     case AXG_FIELD_ACC0: for (int c = 0; c < 3; ++c) p[c] = h->sa[c]; return AXG_OK;
+    case AXG_FIELD_DISP_COMP:
+    case AXG_FIELD_VELO_COMP:
+      if (!h->cu_s[0]) return fail(h, AXG_ERR_BAD_ARG, "the compensated mode was never enabled on this handle");
+      for (int c = 0; c < 3; ++c) p[c] = field == AXG_FIELD_DISP_COMP ? h->cu_s[c] : h->cv_s[c];
+      return AXG_OK;
     default: break;
   }
   *fluid = true;
@@ -600,6 +648,11 @@ int state_ptrs(axg_handle *h, int field, float **p, int *nc, int64_t *nglob, boo
     case AXG_FIELD_CHI: p[0] = h->fu; return AXG_OK;
     case AXG_FIELD_DCHI: p[0] = h->fv; return AXG_OK;
     case AXG_FIELD_DDCHI0: p[0] = h->fa; return AXG_OK;
+    case AXG_FIELD_CHI_COMP:
+    case AXG_FIELD_DCHI_COMP:
+      if (!h->cu_s[0]) return fail(h, AXG_ERR_BAD_ARG, "the compensated mode was never enabled on this handle");
+      p[0] = field == AXG_FIELD_CHI_COMP ? h->cu_f : h->cv_f;
+      return AXG_OK;
     default: break;
   }
   return fail(h, AXG_ERR_BAD_ARG, fmt("field %d not available", field));
@@ -848,10 +901,7 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
   h->errw = h->iter + 2;
   CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
   if (h->anel && (rc = build_anel(h, d))) return rc;
-  if (h->pole == AXG_MONOPOLE) rc = prepare_solid_kernels<POLE_MONO>(h);
-  else if (h->pole == AXG_DIPOLE) rc = prepare_solid_kernels<POLE_DI>(h);
-  else rc = prepare_solid_kernels<POLE_QUAD>(h);
-  if (rc) return rc;
+  if ((rc = prepare_kernels(h))) return rc;
   if ((rc = upload_coupling(h, cf, h->to_fluid))) return rc;
   if ((rc = upload_coupling(h, cs, h->to_solid))) return rc;
   h->to_fluid.nglob_recv = h->nglob_f;
@@ -891,8 +941,8 @@ NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
 
 template <int POLE>
 int noalloc_prepare_kernel(int nsm, int *cap) {
-  auto fn = solid_patch_kernel<POLE, MODE_FORCE, false>;
-  const int bytes = solid_smem_bytes<POLE, MODE_FORCE, false>();
+  auto fn = solid_patch_kernel<POLE, MODE_FORCE, false, false>;
+  const int bytes = solid_smem_bytes<POLE, MODE_FORCE, false, false>();
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   int per_sm = 0;
@@ -935,8 +985,9 @@ void noalloc_launch(const DomainArgs &a0, const StateArgs &st, const SpecDev &sp
   for (int c = 0; c < pl.n_colours; ++c) {
     a.patch_begin = pl.colour_start[c];
     const int n = pl.colour_start[c + 1] - pl.colour_start[c];
-    solid_patch_kernel<POLE, MODE_FORCE, false>
-        <<<std::min(n, cap), kThreads, solid_smem_bytes<POLE, MODE_FORCE, false>(), 0>>>(a, st, sp, n, AnelArgs{});
+    solid_patch_kernel<POLE, MODE_FORCE, false, false>
+        <<<std::min(n, cap), kThreads, solid_smem_bytes<POLE, MODE_FORCE, false, false>(), 0>>>(a, st, sp, n,
+                                                                                           AnelArgs{});
   }
 }
 
@@ -1140,6 +1191,8 @@ int axg_reset(axg_handle *h) {
   CK(cudaMemsetAsync(h->iter, 0, 4 * sizeof(int32_t), h->stream));
   if (h->anel)
     CK(cudaMemsetAsync(h->an.state, 0, (size_t)h->nel_s * h->an.state_stride * sizeof(float), h->stream));
+  for (float *p : {h->cu_s[0], h->cu_s[1], h->cu_s[2], h->cv_s[0], h->cv_s[1], h->cv_s[2], h->cu_f, h->cv_f})
+    if (p) CK(cudaMemsetAsync(p, 0, (p == h->cu_f || p == h->cv_f ? h->nglob_f : h->nglob_s) * sizeof(float), h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return AXG_OK;
 }
@@ -1198,7 +1251,7 @@ int axg_get_receivers(axg_handle *h, float *out, int32_t cap, int32_t *nseismo_o
 
 int axg_get_state(axg_handle *h, int32_t field, float *out) {
   if (!h || !out) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
-  if (field >= AXG_FIELD_MEMVAR) return anel_state_io(h, field, out, nullptr);
+  if (field >= AXG_FIELD_MEMVAR && field <= AXG_FIELD_ATT_SRC_DEV) return anel_state_io(h, field, out, nullptr);
   float *p[3] = {};
   int nc;
   int64_t ng;
@@ -1222,7 +1275,7 @@ int axg_get_state(axg_handle *h, int32_t field, float *out) {
 
 int axg_set_state(axg_handle *h, int32_t field, const float *in) {
   if (!h || !in) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
-  if (field >= AXG_FIELD_MEMVAR) return anel_state_io(h, field, nullptr, in);
+  if (field >= AXG_FIELD_MEMVAR && field <= AXG_FIELD_ATT_SRC_DEV) return anel_state_io(h, field, nullptr, in);
   float *p[3] = {};
   int nc;
   int64_t ng;
@@ -1291,6 +1344,32 @@ int axg_set_tuning(axg_handle *h, int32_t patch_elems, int32_t steps_per_graph) 
     }
   }
   return AXG_OK;
+}
+
+int axg_set_compensated(axg_handle *h, int32_t on) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  if (on && !h->cu_s[0]) {
+    // first use: zeroed compensation for every stored component
+    int rc;
+    const bool mono = h->pole == AXG_MONOPOLE;
+    for (int c = 0; c < 3; ++c) {
+      if (mono && c == 1) continue;
+      if ((rc = dalloc(h, &h->cu_s[c], h->nglob_s)) || (rc = dalloc(h, &h->cv_s[c], h->nglob_s))) return rc;
+      CK(cudaMemset(h->cu_s[c], 0, h->nglob_s * sizeof(float)));
+      CK(cudaMemset(h->cv_s[c], 0, h->nglob_s * sizeof(float)));
+    }
+    if (h->nel_f > 0) {
+      if ((rc = dalloc(h, &h->cu_f, h->nglob_f)) || (rc = dalloc(h, &h->cv_f, h->nglob_f))) return rc;
+      CK(cudaMemset(h->cu_f, 0, h->nglob_f * sizeof(float)));
+      CK(cudaMemset(h->cv_f, 0, h->nglob_f * sizeof(float)));
+    }
+  }
+  h->kahan = on != 0;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return prepare_kernels(h);
 }
 
 int axg_get_info(axg_handle *h, axg_info *info) {

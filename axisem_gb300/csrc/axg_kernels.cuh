@@ -110,6 +110,7 @@ struct StateArgs {
   float *v[3];              // velo / dchi
   float *a[3];              // acc0 / ddchi0
   float *f[3];              // force partial sums
+  float *cu[3], *cv[3];     // compensated mode: running compensation of disp / velo (chi / dchi), else null
   const float *inv_mass;    // per global point
   const float *gamma;       // absorbing gamma per global point or null
   const float *stf;         // (niter)
@@ -128,6 +129,29 @@ struct StateArgs {
 __device__ __forceinline__ float predict(float d, float v, float a, float dt, float hdt2) {
   // disp + deltat*velo + half_dt_sq*acc0 (SOLVER/time_evol_wave.F90:357-364)
   return fmaf(hdt2, a, fmaf(dt, v, d));
+}
+
+// Compensated mode (no counterpart in the reference): x + inc by Kahan's
+// compensated summation.  c carries the low-order part the previous additions
+// lost; it is taken off the increment before the addition and replaced by
+// what this addition loses, so that rounding does not accumulate over many
+// steps.  (No fast-math: the compiler keeps (t - x) - y as written.)
+__device__ __forceinline__ float kahan_add(float x, float inc, float &c) {
+  const float y = inc - c;
+  const float t = x + y;
+  c = (t - x) - y;
+  return t;
+}
+// components apply_axis_mask_{onecomp,twocomp,threecomp} zero on the axis
+// (SOLVER/apply_masks.f90): s (monopole), phi and z (dipole), all (quadrupole)
+template <int POLE>
+__device__ __forceinline__ bool axis_masked(int comp) {
+  return POLE == POLE_QUAD || (POLE == POLE_MONO ? comp == 0 : comp != 0);
+}
+
+// the predictor of the compensated mode: increment dt v + dt^2/2 a
+__device__ __forceinline__ float predict_comp(float d, float v, float a, float dt, float hdt2, float &c) {
+  return kahan_add(d, fmaf(hdt2, a, dt * v), c);
 }
 
 // X(i,j) = sum_k c[k] * v(k,j)   (v(k,j) held by lane k + 5 j)
@@ -565,12 +589,13 @@ constexpr int kStages = 2;  // element blocks in flight per warp (TMA ring depth
 // shared-memory layout of the solid kernel (bytes); NB buffers of the patch
 // state (u, f, point words), STG ring stages per warp, AS floats of
 // attenuation data per stage (0 without attenuation)
-template <int NC, int BS, int STG, int AS, int NB, int ROW>
+template <int NC, int BS, int STG, int AS, int NB, int ROW, bool KAHAN>
 struct SolidSmem {
   static constexpr int u_bytes = NC * ROW * 4, w_bytes = kMaxPatchPoints * 4;
   static constexpr int u_off = 0;
   static constexpr int f_off = u_off + NB * u_bytes;
-  static constexpr int w_off = f_off + NB * u_bytes;
+  static constexpr int c_off = f_off + NB * u_bytes;  // compensated mode: predictor compensation
+  static constexpr int w_off = c_off + (KAHAN ? u_bytes : 0);
   static constexpr int ring_off = ((w_off + NB * w_bytes + 127) / 128) * 128;
   static constexpr int aring_off = ring_off + kWarps * STG * BS * 4;
   static constexpr int scr_off = aring_off + kWarps * STG * AS * 4;     // attenuation: 32 floats per warp
@@ -582,6 +607,12 @@ __host__ __device__ constexpr int solid_stages(bool) { return kStages; }
 // patch-state buffers: the stiffness kernel gathers the next patch while it
 // computes the current one (two CTAs per SM fit), the Newmark kernel does not
 __host__ __device__ constexpr int solid_buffers(int mode) { return mode == MODE_FORCE ? 2 : 1; }
+// resident CTAs per SM the kernel is compiled for: the Newmark kernel keeps
+// three (its register-staged gather is latency-bound; 80 registers), the
+// others two (no spills at 128 registers)
+__host__ __device__ constexpr int solid_min_ctas(int mode, bool anel, bool kahan = false) {
+  return mode == MODE_NEWMARK && !anel && !kahan ? 3 : 2;
+}
 // Bank swizzle of the shared point arrays: patch point t lives at
 // t + pad * (t / 32).  An element's 25 points sit in five runs of five
 // consecutive patch points, one run per element row; on structured blocks
@@ -589,14 +620,12 @@ __host__ __device__ constexpr int solid_buffers(int mode) { return mode == MODE_
 // share only 9 of the 32 banks (5-way conflicts), padded by 4 words per 32
 // they fall on 25 distinct banks.  The three-CTA elastic Newmark kernel can
 // only afford 2 words per 32 (banks i + 3j: at most 2-way conflicts).
-__host__ __device__ constexpr int solid_pad(int mode, bool anel) { return mode == MODE_FORCE || anel ? 4 : 2; }
-__host__ __device__ constexpr int solid_row(int mode, bool anel) {
-  return kMaxPatchPoints + solid_pad(mode, anel) * ((kMaxPatchPoints + 31) / 32);
+__host__ __device__ constexpr int solid_pad(int mode, bool anel, bool kahan = false) {
+  return solid_min_ctas(mode, anel, kahan) == 2 ? 4 : 2;
 }
-// resident CTAs per SM the kernel is compiled for: the Newmark kernel keeps
-// three (its register-staged gather is latency-bound; 80 registers), the
-// others two (no spills at 128 registers)
-__host__ __device__ constexpr int solid_min_ctas(int mode, bool anel) { return mode == MODE_NEWMARK && !anel ? 3 : 2; }
+__host__ __device__ constexpr int solid_row(int mode, bool anel, bool kahan = false) {
+  return kMaxPatchPoints + solid_pad(mode, anel, kahan) * ((kMaxPatchPoints + 31) / 32);
+}
 
 // the sub-round ends of a patch held in registers (8 bits per round), so
 // that no per-patch array is indexed at run time: a PatchMeta indexed that
@@ -633,11 +662,15 @@ struct WarpIter {
 // ANEL (time loop only): attenuation of the solid, the anelastic stiffness
 // before the axis mask of acc1 and the memory-variable step after it, as in
 // SOLVER/time_evol_wave.F90 (anel_true, cg4).
-template <int POLE, int MODE, bool ANEL>
-__global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
+// KAHAN (time loop only): compensated summation of the predictor and the
+// velocity corrector (kahan_add); the predictor's new compensation travels
+// from the gather to the last writer in shared memory.
+template <int POLE, int MODE, bool ANEL, bool KAHAN>
+__global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
     solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches,
                        const __grid_constant__ AnelArgs an) {  // an.ex[] is indexed at run time
   static_assert(!ANEL || MODE == MODE_NEWMARK, "attenuation runs in the time loop only");
+  static_assert(!KAHAN || MODE == MODE_NEWMARK, "the compensated mode is a time-loop mode");
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
   constexpr int NT = n_terms(POLE), NA = n_axial(POLE);
   constexpr int BS = solid_block_stride(NT);
@@ -645,11 +678,12 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
   constexpr int STG = solid_stages(ANEL);
   constexpr int AS = ANEL ? kAnelSlot : 0;
   constexpr int NB = solid_buffers(MODE);
-  constexpr int ROW = solid_row(MODE, ANEL), PAD = solid_pad(MODE, ANEL);
-  using L = SolidSmem<NC, BS, STG, AS, NB, ROW>;
+  constexpr int ROW = solid_row(MODE, ANEL, KAHAN), PAD = solid_pad(MODE, ANEL, KAHAN);
+  using L = SolidSmem<NC, BS, STG, AS, NB, ROW, KAHAN>;
   extern __shared__ __align__(128) unsigned char smem[];
   auto su_of = [&](int b) { return reinterpret_cast<float(*)[ROW]>(smem + L::u_off + b * L::u_bytes); };
   auto sf_of = [&](int b) { return reinterpret_cast<float(*)[ROW]>(smem + L::f_off + b * L::u_bytes); };
+  float(*s_cu)[ROW] = reinterpret_cast<float(*)[ROW]>(smem + L::c_off);  // compensated mode only
   auto spos = [](int t) { return t + PAD * (t >> 5); };  // swizzled position of patch point t
   auto sw_of = [&](int b) { return reinterpret_cast<uint32_t *>(smem + L::w_off + b * L::w_bytes); };
   float *ring = reinterpret_cast<float *>(smem + L::ring_off);
@@ -799,7 +833,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
       constexpr int kGB = (kMaxPatchPoints + kThreads - 1) / kThreads;
       for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += kGB * kThreads) {
         uint32_t w[kGB];
-        float uu[kGB][NC], ff[kGB][NC];
+        float uu[kGB][NC], ff[kGB][NC], cc[KAHAN ? kGB : 1][NC];
 #pragma unroll
         for (int q = 0; q < kGB; ++q) {
           const int t = t0 + q * kThreads;
@@ -813,7 +847,13 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
             float u = ok ? st.u[gc(c)][g] : 0.f;
-            if (ok) u = predict(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2);
+            if (KAHAN) {
+              float k = ok ? st.cu[gc(c)][g] : 0.f;
+              if (ok) u = predict_comp(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2, k);
+              cc[KAHAN ? q : 0][c] = k;
+            } else if (ok) {
+              u = predict(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2);
+            }
             uu[q][c] = u;
             ff[q][c] = part ? st.f[gc(c)][g] : 0.f;
           }
@@ -826,6 +866,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
             for (int c = 0; c < NC; ++c) {
               s_u[c][spos(t)] = uu[q][c];
               s_f[c][spos(t)] = ff[q][c];
+              if (KAHAN) s_cu[c][spos(t)] = cc[KAHAN ? q : 0][c];
             }
           }
         }
@@ -959,7 +1000,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
       constexpr int kWB = 3;
       for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += kWB * kThreads) {
         uint32_t w[kWB];
-        float vel[kWB][NC], acc[kWB][NC], im[kWB], gam[kWB];
+        float vel[kWB][NC], acc[kWB][NC], im[kWB], gam[kWB], kv[KAHAN ? kWB : 1][NC];
 #pragma unroll
         for (int q = 0; q < kWB; ++q) {
           const int t = t0 + q * kThreads;
@@ -972,6 +1013,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
           for (int c = 0; c < NC; ++c) {
             vel[q][c] = last ? st.v[gc(c)][g] : 0.f;
             acc[q][c] = last ? st.a[gc(c)][g] : 0.f;
+            if (KAHAN) kv[KAHAN ? q : 0][c] = last ? st.cv[gc(c)][g] : 0.f;
           }
         }
 #pragma unroll
@@ -1002,9 +1044,19 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
             float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im[q]) * v[c] : -im[q] * v[c];
             const float dsp = s_u[c][spos(t)];
             if (st.gamma) a = a - 2.f * gam[q] * vel[q][c] - gam[q] * gam[q] * dsp;
-            st.v[cg][g] = fmaf(st.hdt, acc[q][c] + a, vel[q][c]);
+            if (KAHAN) {
+              float k = kv[KAHAN ? q : 0][c];
+              st.v[cg][g] = kahan_add(vel[q][c], st.hdt * (acc[q][c] + a), k);
+              st.cv[cg][g] = k;
+              st.cu[cg][g] = s_cu[c][spos(t)];
+            } else {
+              st.v[cg][g] = fmaf(st.hdt, acc[q][c] + a, vel[q][c]);
+            }
             st.a[cg][g] = a;
-            st.u[cg][g] = dsp;
+            // the axis masks of the reference zero these components of its state
+            const bool zero = (w[q] & kPtAxis) && axis_masked<POLE>(cg);
+            st.u[cg][g] = zero ? 0.f : dsp;
+            if (KAHAN && zero) st.cu[cg][g] = 0.f;
           }
         }
       }
@@ -1021,10 +1073,11 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL))
 // warp loads the metric terms of its next element while it computes the
 // current one; the write-back loads the last writers' inverse mass, dchi and
 // ddchi0 in one batch before it stores.
-template <int NONMONO>
+template <int NONMONO, bool KAHAN>
 __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp) {
   __shared__ float s_u[kMaxPatchPoints];
   __shared__ float s_f[kMaxPatchPoints];
+  __shared__ float s_cu[KAHAN ? kMaxPatchPoints : 1];  // compensated mode: predictor compensation
   __shared__ uint32_t s_w[kMaxPatchPoints];
   constexpr int BS = block_stride(NONMONO ? 4 : 3);
   constexpr int kGB = (kMaxPatchPoints + kThreads - 1) / kThreads;  // points per thread: one batch per patch
@@ -1036,7 +1089,7 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
   const PatchMeta m = d.meta[d.patch_begin + blockIdx.x];
   {
     uint32_t w[kGB];
-    float uu[kGB], ff[kGB];
+    float uu[kGB], ff[kGB], cc[KAHAN ? kGB : 1];
 #pragma unroll
     for (int q = 0; q < kGB; ++q) {
       const int t = threadIdx.x + q * kThreads;
@@ -1046,7 +1099,13 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
     for (int q = 0; q < kGB; ++q) {
       const uint32_t g = w[q] & kPtIndexMask;
       const bool ok = w[q] != kPtPad && AXG_BOUND(g, st.nglob, 11);
-      uu[q] = ok ? predict(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2) : 0.f;
+      if (KAHAN) {
+        float k = ok ? st.cu[0][g] : 0.f;
+        uu[q] = ok ? predict_comp(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2, k) : 0.f;
+        cc[KAHAN ? q : 0] = k;
+      } else {
+        uu[q] = ok ? predict(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2) : 0.f;
+      }
       // a point an earlier writer (coupling pre-pass, earlier colour) holds a
       // partial sum for starts from that sum: the write-back only stores
       ff[q] = ok && !(w[q] & kPtFirst) ? st.f[0][g] : 0.f;
@@ -1058,6 +1117,7 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
         s_w[t] = w[q];
         s_u[t] = uu[q];
         s_f[t] = ff[q];
+        if (KAHAN) s_cu[t] = cc[KAHAN ? q : 0];
       }
     }
   }
@@ -1129,7 +1189,7 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
   }
   {
     uint32_t w[kGB];
-    float vel[kGB], acc[kGB], im[kGB], gam[kGB];
+    float vel[kGB], acc[kGB], im[kGB], gam[kGB], kv[KAHAN ? kGB : 1];
 #pragma unroll
     for (int q = 0; q < kGB; ++q) {
       const int t = threadIdx.x + q * kThreads;
@@ -1140,6 +1200,7 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
       gam[q] = last && st.gamma ? st.gamma[g] : 0.f;
       vel[q] = last ? st.v[0][g] : 0.f;
       acc[q] = last ? st.a[0][g] : 0.f;
+      if (KAHAN) kv[KAHAN ? q : 0] = last ? st.cv[0][g] : 0.f;
     }
 #pragma unroll
     for (int q = 0; q < kGB; ++q) {
@@ -1155,9 +1216,19 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
       float a = -im[q] * v;
       const float chi = s_u[t];
       if (st.gamma) a = a - 2.f * gam[q] * vel[q] - gam[q] * gam[q] * chi;
-      st.v[0][g] = fmaf(st.hdt, acc[q] + a, vel[q]);
+      if (KAHAN) {
+        float k = kv[KAHAN ? q : 0];
+        st.v[0][g] = kahan_add(vel[q], st.hdt * (acc[q] + a), k);
+        st.cv[0][g] = k;
+        st.cu[0][g] = s_cu[t];
+      } else {
+        st.v[0][g] = fmaf(st.hdt, acc[q] + a, vel[q]);
+      }
       st.a[0][g] = a;
-      st.u[0][g] = chi;
+      // apply_axis_mask_scal zeroes chi on the axis (non-monopole)
+      const bool zero = NONMONO && (w[q] & kPtAxis);
+      st.u[0][g] = zero ? 0.f : chi;
+      if (KAHAN && zero) st.cu[0][g] = 0.f;
     }
   }
 }
@@ -1187,10 +1258,18 @@ __global__ void couple_to_fluid_kernel(Coupling cp, StateArgs solid, float *ffl)
     if (!AXG_BOUND(k, cp.n_contrib, 21)) break;
     const int gs = cp.src_gidx[k];
     if (!AXG_BOUND(gs, cp.nglob_send, 21)) continue;
-    const float us = predict(solid.u[0][gs], solid.v[0][gs], solid.a[0][gs], solid.dt, solid.hdt2);
-    const float uz = predict(solid.u[2][gs], solid.v[2][gs], solid.a[2][gs], solid.dt, solid.hdt2);
+    // the same predicted displacement as the solid kernel's gather
+    auto pred = [&](int c) {
+      if (solid.cu[0]) {
+        float k = solid.cu[c][gs];
+        return predict_comp(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid.dt, solid.hdt2, k);
+      }
+      return predict(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid.dt, solid.hdt2);
+    };
+    const float us = pred(0);
+    const float uz = pred(2);
     float x = us;
-    if (DIPOLE) x = us + predict(solid.u[1][gs], solid.v[1][gs], solid.a[1][gs], solid.dt, solid.hdt2);
+    if (DIPOLE) x = us + pred(1);
     acc = acc + cp.mask[k] * (-cp.b1[k] * x - cp.b2[k] * uz);
   }
   if (AXG_BOUND(cp.pt_gidx[q], cp.nglob_recv, 22)) ffl[cp.pt_gidx[q]] = acc;

@@ -36,6 +36,7 @@ constexpr uint32_t kPtIndexMask = 0x0FFFFFFFu;
 constexpr uint32_t kPtFirst = 1u << 28;   // first writer: store, do not read partial sum
 constexpr uint32_t kPtLast = 1u << 29;    // last writer: the sum is final
 constexpr uint32_t kPtSource = 1u << 30;  // point carries a solid source term
+constexpr uint32_t kPtAxis = 1u << 31;    // point on the axis (ipol = 0 of an axial element); set by the host
 constexpr uint32_t kPtPad = 0xFFFFFFFFu;  // padding after a patch's words (each patch starts 16-byte aligned)
 
 struct PatchMeta {            // 32 bytes, device layout

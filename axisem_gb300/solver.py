@@ -85,7 +85,8 @@ class Solver:
     def get_state(self, field: int) -> np.ndarray:
         m = self.mesh
         nsls = max(int(m.anel.get("y_j").size), 1) if m.anel else 1
-        if field in (_abi.FIELD_DISP, _abi.FIELD_VELO, _abi.FIELD_ACC0):
+        if field in (_abi.FIELD_DISP, _abi.FIELD_VELO, _abi.FIELD_ACC0, _abi.FIELD_DISP_COMP,
+                     _abi.FIELD_VELO_COMP):
             out = np.zeros((5, 5, m.nel_solid, 3), dtype=np.float32, order="F")
         elif field == _abi.FIELD_MEMVAR:      # memory_var_cg4(1:4,6,n_sls,nel_solid)
             out = np.zeros((4, 6, nsls, m.nel_solid), dtype=np.float32, order="F")
@@ -125,6 +126,10 @@ class Solver:
         ms = C.c_float()
         _check(self.lib, self.h, self.lib.axg_time_stiffness(self.h, n, C.byref(ms)))
         return ms.value
+
+    def set_compensated(self, on: bool = True):
+        """Kahan-compensated predictor / corrector (axg_set_compensated)."""
+        _check(self.lib, self.h, self.lib.axg_set_compensated(self.h, int(bool(on))))
 
     def set_tuning(self, patch_elems: int = 0, steps_per_graph: int = 0):
         _check(self.lib, self.h, self.lib.axg_set_tuning(self.h, patch_elems, steps_per_graph))

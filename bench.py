@@ -266,11 +266,12 @@ def run_gpu(args):
     if prof.exists():
         traffic = json.loads(prof.read_text()).get("dram_bytes_per_step")
 
-    timeloop = timeloop_anel = None
+    timeloop = timeloop_anel = timeloop_comp = None
     if args.timeloop_steps > 0:
         s.close()
         timeloop = run_timeloop(args, pole, ws, rank)
         timeloop_anel = run_timeloop(args, pole, ws, rank, anel=True)
+        timeloop_comp = run_timeloop(args, pole, ws, rank, compensated=True)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -298,6 +299,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "timeloop": timeloop,
         "timeloop_anel": timeloop_anel,
+        "timeloop_compensated": timeloop_comp,
         "clocks": clocks,
         "gpu_launches": int(args.steps * info["kernels_per_force"]),
         "plan": {"patches": info["n_patches_solid"], "colours": info["n_colours_solid"],
@@ -336,10 +338,11 @@ def anel_bytes(m, pole: int) -> int:
     return m.nel_solid * (4 * ne * nsls * 8 + 4 * (1 + ne) * 8 + 48 * 4 + 8)
 
 
-def run_timeloop(args, pole, ws, rank, anel=False):
+def run_timeloop(args, pole, ws, rank, anel=False, compensated=False):
     """Newmark steps (SOLVER/time_evol_wave.F90:353-500) on a coupled mesh of
     1024 x 768 solid over 1024 x 256 fluid elements, through axg_run; with
-    `anel`, cg4 attenuation with 5 standard linear solids in the solid."""
+    `anel`, cg4 attenuation with 5 standard linear solids in the solid; with
+    `compensated`, the Kahan-compensated predictor/corrector."""
     import torch
     from axisem_gb300.mesh import add_attenuation, coupled_mesh
     from axisem_gb300.solver import Solver
@@ -352,6 +355,8 @@ def run_timeloop(args, pole, ws, rank, anel=False):
         m = add_attenuation(m, n_sls=5, seed=77 + rank)
     s = Solver(m)
     s.set_tuning(steps_per_graph=16)
+    if compensated:
+        s.set_compensated(True)
     s.run(1, warm)
     torch.cuda.synchronize()
     barrier(ws)
@@ -364,10 +369,13 @@ def run_timeloop(args, pole, ws, rank, anel=False):
     s.close()
     pts = 25 * (m.nel_solid + m.nel_fluid)
     nb = timeloop_bytes(m, pole) + (anel_bytes(m, pole) if anel else 0)
+    if compensated:  # the compensation of disp/velo (chi/dchi) read and written once per point
+        nb += m.nglob_solid * 16 * N_COMP[pole] + m.nglob_fluid * 16
     peak, _ = measured_peaks()
     return {"value": ws * pts / dt, "unit": "GLL-point-steps/s", "ms_per_step": dt * 1e3,
             "mesh": f"{n}x{3 * n // 4} solid + {n}x{n // 4} fluid elements, {args.pole}pole, "
-                    f"source + 200 receivers" + (", cg4 attenuation with 5 SLS" if anel else ""),
+                    f"source + 200 receivers" + (", cg4 attenuation with 5 SLS" if anel else "")
+                    + (", compensated (Kahan) time integration" if compensated else ""),
             "algorithmic_bytes_per_step": nb, "achieved_gbs": nb / dt / 1e9,
             "frac_of_hbm": nb / dt / 1e9 / peak, "kernels_per_step": info["kernels_per_step"],
             "solid_ctas_per_sm": info["ctas_per_sm_step"],

@@ -161,7 +161,10 @@ typedef struct axg_handle axg_handle;
 enum axg_field {
   AXG_FIELD_DISP = 0, AXG_FIELD_VELO, AXG_FIELD_ACC0,
   AXG_FIELD_CHI, AXG_FIELD_DCHI, AXG_FIELD_DDCHI0,
-  AXG_FIELD_MEMVAR, AXG_FIELD_ATT_SRC_TR, AXG_FIELD_ATT_SRC_DEV
+  AXG_FIELD_MEMVAR, AXG_FIELD_ATT_SRC_TR, AXG_FIELD_ATT_SRC_DEV,
+  /* compensated mode (axg_set_compensated): the running compensation terms
+   * of disp, velo (solid layout) and chi, dchi (fluid layout) */
+  AXG_FIELD_DISP_COMP, AXG_FIELD_VELO_COMP, AXG_FIELD_CHI_COMP, AXG_FIELD_DCHI_COMP
 };
 
 /* Library build/version string; never NULL. */
@@ -240,6 +243,15 @@ int axg_download_gvec_force(axg_handle *h, float *f_gvec);
  * shape is fixed at creation (axg_create_tuned); patch_elems must be 0 or the
  * handle's value. */
 int axg_set_tuning(axg_handle *h, int32_t patch_elems, int32_t steps_per_graph);
+
+/* Compensated time integration on (1) or off (0): the predictor
+ * disp += dt velo + dt^2/2 acc0 and the corrector velo += dt/2 (acc0 + acc1)
+ * (and chi, dchi in the fluid) use Kahan's compensated summation in FP32, with
+ * a running compensation per point kept in HBM, so that rounding does not
+ * accumulate over 1e4-1e5 steps.  Stiffness, coupling and attenuation are
+ * unchanged.  The first call allocates the compensation (zero; axg_reset
+ * zeroes it too).  No counterpart in the reference. */
+int axg_set_compensated(axg_handle *h, int32_t on);
 
 /* axg_create with the patch shape chosen by the caller: patch_elems 1..64
  * elements per patch and growth 0 (compact: most shared points first) or 1
