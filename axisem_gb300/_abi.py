@@ -121,6 +121,7 @@ class Info(C.Structure):
         ("patch_elems_solid", C.c_int32), ("growth_solid", C.c_int32),
         ("patch_elems_fluid", C.c_int32), ("growth_fluid", C.c_int32),
         ("ctas_per_sm_force", C.c_int32), ("ctas_per_sm_step", C.c_int32),
+        ("mesh_bytes", C.c_int64),
     ]
 
 
@@ -139,6 +140,10 @@ SIGNATURES = {
     "axg_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(C.c_void_p)]),
     "axg_create_tuned": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "axg_set_compensated": (C.c_int, [C.c_void_p, C.c_int32]),
+    "axg_create_sharing": (C.c_int, [C.c_void_p, C.POINTER(MeshDesc), C.POINTER(C.c_void_p)]),
+    "axg_run_async": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "axg_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "axg_wait": (C.c_int, [C.c_void_p]),
     "axg_reset": (C.c_int, [C.c_void_p]),
     "axg_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "axg_get_receivers": (C.c_int, [C.c_void_p, _fp, C.c_int32, _ip]),

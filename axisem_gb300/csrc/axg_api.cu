@@ -74,6 +74,17 @@ struct DomainDev {
   int64_t n_m0 = 0;
 };
 
+// Device buffers of a mesh (element blocks, plans, masses, coupling tables,
+// attenuation constants): owned jointly by every handle that solves on the
+// mesh (axg_create_sharing), freed with the last of them.
+struct MeshPool {
+  std::vector<void *> allocs;
+  int64_t bytes = 0;
+  ~MeshPool() {
+    for (void *p : allocs) cudaFree(p);
+  }
+};
+
 struct CouplingHost {
   std::vector<int32_t> pt_gidx, start, src_gidx;
   std::vector<float> b1, b2, mask;
@@ -112,6 +123,8 @@ struct axg_handle {
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_done = nullptr;  // end of the work axg_run_async queued
+  bool pending = false;
   int num_sms = 1, solid_ctas = 1;
   int32_t *errw = nullptr;
   std::string err = "no error";
@@ -125,6 +138,9 @@ struct axg_handle {
   int nsls = 0;
   AnelArgs an{};
   std::vector<int32_t> slot_of_elem_s;  // solid element -> launch slot
+  // mesh-level buffers, shared with the handles created from this one
+  std::shared_ptr<MeshPool> mesh;
+  bool in_mesh = false;  // allocations go to the mesh pool while set
 };
 
 namespace {
@@ -152,10 +168,20 @@ int dalloc(axg_handle *h, T **p, size_t count) {
   if (count == 0) return AXG_OK;
   void *q = nullptr;
   // 256 bytes of tail padding: no kernel reads past an extent, the pad only
-  // keeps a future vectorised tail load inside the allocation
-  cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 256);
+  // keeps a future vectorised tail load inside the allocation.  A solve's own
+  // buffers are stream-ordered (cudaMallocAsync / cudaFreeAsync on its
+  // stream): creating or destroying a solve then does not synchronise the
+  // device, so other solves keep running.
+  const bool mesh_level = h->in_mesh && h->mesh;
+  cudaError_t e = mesh_level ? cudaMalloc(&q, count * sizeof(T) + 256)
+                             : cudaMallocAsync(&q, count * sizeof(T) + 256, h->stream);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
-  h->allocs.push_back(q);
+  if (mesh_level) {
+    h->mesh->allocs.push_back(q);
+    h->mesh->bytes += (int64_t)(count * sizeof(T));
+  } else {
+    h->allocs.push_back(q);
+  }
   h->dev_bytes += (int64_t)(count * sizeof(T));
   *p = (T *)q;
   return AXG_OK;
@@ -165,7 +191,9 @@ template <typename T>
 int upload(axg_handle *h, T **p, const std::vector<T> &v) {
   int rc = dalloc(h, p, v.size());
   if (rc) return rc;
-  if (!v.empty()) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  if (v.empty()) return AXG_OK;
+  if (h->in_mesh && h->mesh) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  else CK(cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));  // pageable: staged
   return AXG_OK;
 }
 
@@ -271,7 +299,10 @@ std::vector<float> per_point(const float *elem, const std::vector<int32_t> &iglo
   return out;
 }
 
-int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid) {
+// mesh_part: the element blocks, patch metadata and axial vectors (mesh
+// pool); always: the point words (source and axis flags), element info words
+// and fluid source terms of this solve
+int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid, bool mesh_part) {
   const DomainPlan &pl = fluid ? h->pf : h->ps;
   DomainDev &dd = fluid ? h->df : h->ds;
   const int64_t nel = pl.nel;
@@ -293,14 +324,14 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid) {
   }
   // solid blocks carry the element's point indices and info word inline
   const int bs = fluid ? block_stride(nt) : solid_block_stride(nt);
-  std::vector<float> metric((size_t)nel * bs, 0.f);
+  std::vector<float> metric(mesh_part ? (size_t)nel * bs : 0, 0.f);
   std::vector<int32_t> elinfo(nel, 0);
   const std::vector<int> aslots = fluid ? std::vector<int>{0} : axial_slots(pole);
   const int na = (int)aslots.size();
   std::vector<float> m0;
   std::vector<float> fsmask;
   const bool use_fs = fluid && d->fluid_free_surface_mask != nullptr;
-  if (use_fs) fsmask.resize((size_t)nel * 25);
+  if (use_fs && mesh_part) fsmask.resize((size_t)nel * 25);
   // source slot of each element
   std::vector<int8_t> srcslot(nel, -1);
   if (d->nelsrc > 0 && (bool)d->fluid_src == fluid)
@@ -308,22 +339,25 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid) {
   int32_t axcount = 0;
   for (int64_t s = 0; s < nel; ++s) {
     const int64_t e = pl.elem_order[s];
+    int32_t info = 0;
+    if (axial[e]) {
+      info = axcount + 1;
+      if (mesh_part)
+        for (int q = 0; q < na; ++q)
+          for (int jj = 0; jj < 5; ++jj)
+            m0.push_back(fluid ? (nonmono ? d->m0_w_fl[5 * e + jj] : 0.f) : d->m0_solid[aslots[q]][5 * e + jj]);
+      ++axcount;
+    }
+    if (srcslot[e] >= 0) info |= (srcslot[e] + 1) << 24;
+    elinfo[s] = info;
+    if (!mesh_part) continue;
     float *blk = metric.data() + (size_t)s * bs;
     for (int t = 0; t < nt; ++t) {
       const float *src = fluid ? d->m_fluid[t] : d->m_solid[slots[t]];
       std::memcpy(blk + 25 * t, src + 25 * e, 25 * sizeof(float));
     }
-    int32_t info = 0;
-    if (axial[e]) {
-      info = axcount + 1;
-      for (int q = 0; q < na; ++q)
-        for (int jj = 0; jj < 5; ++jj)
-          m0.push_back(fluid ? (nonmono ? d->m0_w_fl[5 * e + jj] : 0.f) : d->m0_solid[aslots[q]][5 * e + jj]);
-      ++axcount;
-    }
-    if (srcslot[e] >= 0) info |= (srcslot[e] + 1) << 24;
-    elinfo[s] = info;
     if (!fluid) {
+      // the solid kernel reads only the axial slot of this info word
       std::memcpy(blk + solid_idx_off(nt), &pl.elem_pts[25 * s], 25 * sizeof(uint16_t));
       std::memcpy(blk + solid_info_off(nt), &info, sizeof(int32_t));
     }
@@ -356,14 +390,19 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid) {
       if (w != kPtPad && issrc[w & kPtIndexMask]) w |= kPtSource;
   }
   int rc;
-  if ((rc = upload(h, &dd.meta, pl.meta))) return rc;
+  if (mesh_part) {
+    h->in_mesh = true;
+    if ((rc = upload(h, &dd.meta, pl.meta)) || (rc = upload(h, &dd.elpts, pl.elem_pts)) ||
+        (rc = upload(h, &dd.metric, metric)) || (rc = upload(h, &dd.m0, m0)) ||
+        (use_fs && (rc = upload(h, &dd.fsmask, fsmask)))) {
+      h->in_mesh = false;
+      return rc;
+    }
+    h->in_mesh = false;
+    dd.n_m0 = (int64_t)m0.size();
+  }
   if ((rc = upload(h, &dd.pts, pts))) return rc;
-  if ((rc = upload(h, &dd.elpts, pl.elem_pts))) return rc;
   if ((rc = upload(h, &dd.elinfo, elinfo))) return rc;
-  if ((rc = upload(h, &dd.metric, metric))) return rc;
-  if ((rc = upload(h, &dd.m0, m0))) return rc;
-  dd.n_m0 = (int64_t)m0.size();
-  if (use_fs && (rc = upload(h, &dd.fsmask, fsmask))) return rc;
   if (fluid && d->fluid_src && d->nelsrc > 0) {
     std::vector<float> s((size_t)8 * 25, 0.f);
     for (int k = 0; k < d->nelsrc; ++k)
@@ -621,7 +660,8 @@ void release(axg_handle *h) {
   if (h->graph) cudaGraphExecDestroy(h->graph);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
-  for (void *p : h->allocs) cudaFree(p);
+  if (h->ev_done) cudaEventDestroy(h->ev_done);
+  for (void *p : h->allocs) cudaFreeAsync(p, h->stream);
   if (h->stream) cudaStreamDestroy(h->stream);
   h->allocs.clear();
 }
@@ -705,7 +745,7 @@ void sls_fast_correct(const double *y, double *yp, int n) {
 //    rounded to float once;
 //  * per element (launch order) the cg4 constants and the two row indices;
 //  * the per-element state, zeroed by axg_reset.
-int build_anel(axg_handle *h, const axg_mesh_desc *d) {
+int build_anel(axg_handle *h, const axg_mesh_desc *d, bool mesh_part) {
   const int nsls = d->n_sls;
   const int64_t nel = h->nel_s;
   const DomainPlan &pl = h->ps;
@@ -753,9 +793,14 @@ int build_anel(axg_handle *h, const axg_mesh_desc *d) {
   for (int64_t s = 0; s < nel; ++s) h->slot_of_elem_s[pl.elem_order[s]] = (int32_t)s;
   int rc;
   float *cp = nullptr, *qp = nullptr;
-  if ((rc = upload(h, &cp, consts))) return rc;
-  if ((rc = upload(h, &qp, qtab))) return rc;
-  h->an.consts = cp;
+  if (mesh_part) {  // the per-element constants belong to the mesh
+    h->in_mesh = true;
+    rc = upload(h, &cp, consts);
+    h->in_mesh = false;
+    if (rc) return rc;
+    h->an.consts = cp;
+  }
+  if ((rc = upload(h, &qp, qtab))) return rc;  // depends on dt: this solve's
   h->an.qtab = qp;
   if ((rc = dalloc(h, &h->an.state, (size_t)nel * h->an.state_stride))) return rc;
   return AXG_OK;
@@ -767,7 +812,9 @@ extern "C" int axg_reset(axg_handle *h);
 extern "C" int axg_device_count(void);
 
 namespace {
-int create_impl(axg_handle *h, const axg_mesh_desc *d) {
+// share: an existing handle on the same mesh (axg_create_sharing) whose
+// plans and mesh-level device buffers are used instead of building new ones
+int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share = nullptr) {
   int rc = AXG_OK;
   h->pole = d->src_type;
   h->fluid_src = d->fluid_src;
@@ -783,51 +830,72 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
   h->dt = d->deltat;
   h->magnitude = d->magnitude;
   h->anel = d->anel_true != 0;
-  h->igloc_s.assign(d->igloc_solid, d->igloc_solid + 25 * h->nel_s);
-  if (h->nel_f > 0) h->igloc_f.assign(d->igloc_fluid, d->igloc_fluid + 25 * h->nel_f);
-  for (int64_t p = 0; p < 25 * h->nel_s; ++p)
-    if (h->igloc_s[p] < 1 || h->igloc_s[p] > h->nglob_s)
-      return fail(h, AXG_ERR_BAD_DESC, "igloc_solid entry outside 1..nglob_solid");
-  for (int64_t p = 0; p < 25 * h->nel_f; ++p)
-    if (h->igloc_f[p] < 1 || h->igloc_f[p] > h->nglob_f)
-      return fail(h, AXG_ERR_BAD_DESC, "igloc_fluid entry outside 1..nglob_fluid");
-
-  // solid-fluid coupling tables (the receiving points are written first by a pre-pass)
-  std::vector<std::tuple<int32_t, int32_t, float, float, float>> tf, ts;
-  std::vector<uint8_t> axs(h->nel_s, 0), axf(h->nel_f > 0 ? h->nel_f : 1, 0);
-  for (int k = 0; k < d->naxel_solid; ++k) axs[d->ax_el_solid[k] - 1] = 1;
-  for (int k = 0; k < d->naxel_fluid; ++k) axf[d->ax_el_fluid[k] - 1] = 1;
-  const int nb = d->nel_bdry;
-  for (int b = 0; b < nb; ++b) {
-    const int64_t es = d->bdry_solid_el[b] - 1, ef = d->bdry_fluid_el[b] - 1;
-    const int js = d->bdry_jpol_solid[b], jf = d->bdry_jpol_fluid[b];
-    for (int i = 0; i < 5; ++i) {
-      const int32_t gs = h->igloc_s[25 * es + i + 5 * js] - 1;
-      const int32_t gf = h->igloc_f[25 * ef + i + 5 * jf] - 1;
-      const float b1 = d->bdry_matr[i + 5 * b], b2 = d->bdry_matr[i + 5 * (b + nb)];
-      float mf = (d->src_type != AXG_MONOPOLE && axf[ef] && i == 0) ? 0.f : 1.f;
-      if (d->fluid_free_surface_mask) mf *= d->fluid_free_surface_mask[25 * ef + i + 5 * jf];
-      tf.emplace_back(gf, gs, b1, b2, mf);
-      ts.emplace_back(gs, gf, b1, b2, (axs[es] && i == 0) ? 0.f : 1.f);
+  CouplingHost cf, cs;
+  if (share) {
+    // the same mesh: sizes, pole, numbering, axial elements, boundary and
+    // attenuation layout must match (the metric terms are taken as equal)
+    if (share->pole != h->pole || share->nel_s != h->nel_s || share->nel_f != h->nel_f ||
+        share->nglob_s != h->nglob_s || share->nglob_f != h->nglob_f || share->absorbing != h->absorbing ||
+        share->anel != h->anel || (h->anel && share->nsls != d->n_sls))
+      return fail(h, AXG_ERR_BAD_DESC, "axg_create_sharing: the descriptor is not of the handle's mesh");
+    if (std::memcmp(share->igloc_s.data(), d->igloc_solid, 25 * h->nel_s * sizeof(int32_t)) != 0 ||
+        (h->nel_f > 0 && std::memcmp(share->igloc_f.data(), d->igloc_fluid, 25 * h->nel_f * sizeof(int32_t)) != 0))
+      return fail(h, AXG_ERR_BAD_DESC, "axg_create_sharing: the global numbering differs from the handle's mesh");
+    h->igloc_s = share->igloc_s;
+    h->igloc_f = share->igloc_f;
+    h->pre_s = share->pre_s;
+    h->pre_f = share->pre_f;
+    h->ps = share->ps;
+    h->pf = share->pf;
+    h->patch_elems = share->patch_elems;
+    h->growth = share->growth;
+  } else {
+    h->igloc_s.assign(d->igloc_solid, d->igloc_solid + 25 * h->nel_s);
+    if (h->nel_f > 0) h->igloc_f.assign(d->igloc_fluid, d->igloc_fluid + 25 * h->nel_f);
+    for (int64_t p = 0; p < 25 * h->nel_s; ++p)
+      if (h->igloc_s[p] < 1 || h->igloc_s[p] > h->nglob_s)
+        return fail(h, AXG_ERR_BAD_DESC, "igloc_solid entry outside 1..nglob_solid");
+    for (int64_t p = 0; p < 25 * h->nel_f; ++p)
+      if (h->igloc_f[p] < 1 || h->igloc_f[p] > h->nglob_f)
+        return fail(h, AXG_ERR_BAD_DESC, "igloc_fluid entry outside 1..nglob_fluid");
+    // solid-fluid coupling tables (the receiving points are written first by a pre-pass)
+    std::vector<std::tuple<int32_t, int32_t, float, float, float>> tf, ts;
+    std::vector<uint8_t> axs(h->nel_s, 0), axf(h->nel_f > 0 ? h->nel_f : 1, 0);
+    for (int k = 0; k < d->naxel_solid; ++k) axs[d->ax_el_solid[k] - 1] = 1;
+    for (int k = 0; k < d->naxel_fluid; ++k) axf[d->ax_el_fluid[k] - 1] = 1;
+    const int nb = d->nel_bdry;
+    for (int b = 0; b < nb; ++b) {
+      const int64_t es = d->bdry_solid_el[b] - 1, ef = d->bdry_fluid_el[b] - 1;
+      const int js = d->bdry_jpol_solid[b], jf = d->bdry_jpol_fluid[b];
+      for (int i = 0; i < 5; ++i) {
+        const int32_t gs = h->igloc_s[25 * es + i + 5 * js] - 1;
+        const int32_t gf = h->igloc_f[25 * ef + i + 5 * jf] - 1;
+        const float b1 = d->bdry_matr[i + 5 * b], b2 = d->bdry_matr[i + 5 * (b + nb)];
+        float mf = (d->src_type != AXG_MONOPOLE && axf[ef] && i == 0) ? 0.f : 1.f;
+        if (d->fluid_free_surface_mask) mf *= d->fluid_free_surface_mask[25 * ef + i + 5 * jf];
+        tf.emplace_back(gf, gs, b1, b2, mf);
+        ts.emplace_back(gs, gf, b1, b2, (axs[es] && i == 0) ? 0.f : 1.f);
+      }
     }
-  }
-  CouplingHost cf = make_coupling(tf), cs = make_coupling(ts);
-  h->pre_s.assign(h->nglob_s, 0);
-  for (int32_t g : cs.pt_gidx) h->pre_s[g] = 1;
-  if (h->nel_f > 0) {
-    h->pre_f.assign(h->nglob_f, 0);
-    for (int32_t g : cf.pt_gidx) h->pre_f[g] = 1;
-  }
-  std::string perr = plan_domain(h->igloc_s.data(), h->nel_s, h->nglob_s, h->patch_elems, h->growth, h->pre_s, h->ps);
-  if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "solid plan: " + perr);
-  if (h->nel_f > 0) {
-    perr = plan_domain(h->igloc_f.data(), h->nel_f, h->nglob_f, h->patch_elems, h->growth, h->pre_f, h->pf);
-    if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "fluid plan: " + perr);
-  }
+    cf = make_coupling(tf);
+    cs = make_coupling(ts);
+    h->pre_s.assign(h->nglob_s, 0);
+    for (int32_t g : cs.pt_gidx) h->pre_s[g] = 1;
+    if (h->nel_f > 0) {
+      h->pre_f.assign(h->nglob_f, 0);
+      for (int32_t g : cf.pt_gidx) h->pre_f[g] = 1;
+    }
+    std::string perr = plan_domain(h->igloc_s.data(), h->nel_s, h->nglob_s, h->patch_elems, h->growth, h->pre_s, h->ps);
+    if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "solid plan: " + perr);
+    if (h->nel_f > 0) {
+      perr = plan_domain(h->igloc_f.data(), h->nel_f, h->nglob_f, h->patch_elems, h->growth, h->pre_f, h->pf);
+      if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "fluid plan: " + perr);
+    }
 #ifdef AXG_VALIDATE_PLAN
-  perr = validate_plan(h->igloc_s.data(), h->nel_s, h->nglob_s, h->pre_s, h->ps);
-  if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "solid plan invalid: " + perr);
+    perr = validate_plan(h->igloc_s.data(), h->nel_s, h->nglob_s, h->pre_s, h->ps);
+    if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "solid plan invalid: " + perr);
 #endif
+  }
 
   // receivers and the solid source table
   for (int r = 0; r < h->num_rec; ++r) {
@@ -860,16 +928,49 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
 
   // ---- device
   CK(cudaGetDevice(&h->device));
+  if (share && share->device != h->device)
+    return fail(h, AXG_ERR_BAD_ARG, "axg_create_sharing: the handle's mesh is on another device");
   CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&h->ev0));
   CK(cudaEventCreate(&h->ev1));
+  CK(cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming));
   for (int k = 0; k < 25; ++k) {
     h->spec.g1[k] = d->G1[k];
     h->spec.g2[k] = d->G2[k];
   }
   for (int k = 0; k < 5; ++k) h->spec.g0[k] = d->G0[k];
-  if ((rc = build_domain(h, d, false))) return rc;
-  if ((rc = build_domain(h, d, true))) return rc;
+  CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
+  if (share) {
+    h->mesh = share->mesh;
+    h->ds = share->ds;
+    h->df = share->df;
+    h->inv_mass_s = share->inv_mass_s;
+    h->inv_mass_f = share->inv_mass_f;
+    h->gamma_s = share->gamma_s;
+    h->gamma_f = share->gamma_f;
+    h->to_fluid = share->to_fluid;
+    h->to_solid = share->to_solid;
+    h->an.consts = share->an.consts;
+    h->dev_bytes = h->mesh->bytes;
+  } else {
+    h->mesh = std::make_shared<MeshPool>();
+    h->in_mesh = true;
+    rc = upload(h, &h->inv_mass_s, per_point(d->inv_mass_rho, h->igloc_s, h->nglob_s));
+    if (!rc && h->absorbing) rc = upload(h, &h->gamma_s, per_point(d->solid_absorbing_gamma, h->igloc_s, h->nglob_s));
+    if (!rc && h->nel_f > 0) rc = upload(h, &h->inv_mass_f, per_point(d->inv_mass_fluid, h->igloc_f, h->nglob_f));
+    if (!rc && h->nel_f > 0 && h->absorbing)
+      rc = upload(h, &h->gamma_f, per_point(d->fluid_absorbing_gamma, h->igloc_f, h->nglob_f));
+    if (!rc) rc = upload_coupling(h, cf, h->to_fluid);
+    if (!rc) rc = upload_coupling(h, cs, h->to_solid);
+    h->in_mesh = false;
+    if (rc) return rc;
+    h->to_fluid.nglob_recv = h->nglob_f;
+    h->to_fluid.nglob_send = h->nglob_s;
+    h->to_solid.nglob_recv = h->nglob_s;
+    h->to_solid.nglob_send = h->nglob_f;
+  }
+  if ((rc = build_domain(h, d, false, !share))) return rc;
+  if ((rc = build_domain(h, d, true, !share))) return rc;
   const bool mono = h->pole == AXG_MONOPOLE;
   for (int c = 0; c < 3; ++c) {
     if (mono && c == 1) continue;
@@ -877,16 +978,9 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
         (rc = dalloc(h, &h->sa[c], h->nglob_s)) || (rc = dalloc(h, &h->sf[c], h->nglob_s)))
       return rc;
   }
-  if ((rc = upload(h, &h->inv_mass_s, per_point(d->inv_mass_rho, h->igloc_s, h->nglob_s)))) return rc;
-  if (h->absorbing && (rc = upload(h, &h->gamma_s, per_point(d->solid_absorbing_gamma, h->igloc_s, h->nglob_s))))
-    return rc;
   if (h->nel_f > 0) {
     if ((rc = dalloc(h, &h->fu, h->nglob_f)) || (rc = dalloc(h, &h->fv, h->nglob_f)) ||
         (rc = dalloc(h, &h->fa, h->nglob_f)) || (rc = dalloc(h, &h->ff, h->nglob_f)))
-      return rc;
-    if ((rc = upload(h, &h->inv_mass_f, per_point(d->inv_mass_fluid, h->igloc_f, h->nglob_f)))) return rc;
-    if (h->absorbing &&
-        (rc = upload(h, &h->gamma_f, per_point(d->fluid_absorbing_gamma, h->igloc_f, h->nglob_f))))
       return rc;
   }
   std::vector<float> stf(d->stf ? d->stf : (const float *)nullptr, d->stf ? d->stf + d->niter : nullptr);
@@ -899,15 +993,8 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d) {
   if ((rc = dalloc(h, &h->iter, 4))) return rc;
   h->blowup = h->iter + 1;
   h->errw = h->iter + 2;
-  CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
-  if (h->anel && (rc = build_anel(h, d))) return rc;
+  if (h->anel && (rc = build_anel(h, d, !share))) return rc;
   if ((rc = prepare_kernels(h))) return rc;
-  if ((rc = upload_coupling(h, cf, h->to_fluid))) return rc;
-  if ((rc = upload_coupling(h, cs, h->to_solid))) return rc;
-  h->to_fluid.nglob_recv = h->nglob_f;
-  h->to_fluid.nglob_send = h->nglob_s;
-  h->to_solid.nglob_recv = h->nglob_s;
-  h->to_solid.nglob_send = h->nglob_f;
   h->kernels_per_force = h->ps.n_colours + (h->to_solid.n > 0 ? 1 : 0);
   h->kernels_per_step = h->ps.n_colours + 1 +
                         (h->nel_f > 0 ? h->pf.n_colours + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);
@@ -1127,7 +1214,10 @@ int anel_state_io(axg_handle *h, int field, float *out, const float *in) {
     if (out) std::memcpy(out + (size_t)e * len, blk, len * sizeof(float));
     else std::memcpy(blk, in + (size_t)e * len, len * sizeof(float));
   }
-  if (in) CK(cudaMemcpy(h->an.state, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice));
+  if (in) {
+    CK(cudaMemcpyAsync(h->an.state, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
   return AXG_OK;
 }
 }  // namespace
@@ -1148,6 +1238,24 @@ int axg_device_count(void) {
 }
 
 int axg_create(const axg_mesh_desc *d, axg_handle **out) { return axg_create_tuned(d, 0, -1, out); }
+
+int axg_create_sharing(axg_handle *mesh_of, const axg_mesh_desc *d, axg_handle **out) {
+  if (!out) return fail(nullptr, AXG_ERR_BAD_ARG, "out is NULL");
+  *out = nullptr;
+  if (!mesh_of) return fail(nullptr, AXG_ERR_BAD_ARG, "mesh_of is NULL");
+  int rc = validate(d);
+  if (rc) return rc;
+  axg_handle *h = new axg_handle();
+  rc = create_impl(h, d, mesh_of);
+  if (rc) {
+    g_create_error = h->err;
+    release(h);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return AXG_OK;
+}
 
 int axg_create_tuned(const axg_mesh_desc *d, int32_t patch_elems, int32_t growth, axg_handle **out) {
   if (!out) return fail(nullptr, AXG_ERR_BAD_ARG, "out is NULL");
@@ -1231,6 +1339,73 @@ int axg_run(axg_handle *h, int32_t first_iter, int32_t n_iter) {
   return AXG_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// reads the device flags after the handle's queued work completed
+int check_flags(axg_handle *h) {
+  int32_t flags[2] = {0, 0};
+  CK(cudaMemcpyAsync(flags, h->blowup, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (flags[1] != 0) return fail(h, AXG_ERR_TIMEOUT, "a bounded device wait on a bulk copy gave up");
+  if (flags[0] != 0)
+    return fail(h, AXG_ERR_BLOWUP,
+                fmt("displacements blew up: |disp(1,1,:,:)| > 10 |magnitude| at time step %d", flags[0] + 1));
+  return AXG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int axg_run_async(axg_handle *h, int32_t first_iter, int32_t n_iter) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  if (n_iter < 0 || first_iter < 1 || (int64_t)first_iter + n_iter - 1 > h->niter)
+    return fail(h, AXG_ERR_BAD_ARG, fmt("iterations %d..%d outside 1..niter=%d", first_iter, first_iter + n_iter - 1,
+                                        h->niter));
+  if (n_iter == 0) return AXG_OK;
+  // the kernels of a step after a blow-up return at once, so all steps can
+  // be queued without a check in between
+  CK(cudaMemcpyAsync(h->iter, &first_iter, sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  for (int32_t done = 0; done < n_iter;) {
+    const int k = std::min<int32_t>(h->steps_per_graph, n_iter - done);
+    if (k == h->steps_per_graph) {
+      if (!h->graph || h->graph_steps != k) {
+        int rc = build_graph(h, k);
+        if (rc) return rc;
+      }
+      CK(cudaGraphLaunch(h->graph, h->stream));
+    } else {
+      for (int q = 0; q < k; ++q) enqueue_step(h, h->stream);
+      CK(cudaGetLastError());
+    }
+    done += k;
+  }
+  CK(cudaEventRecord(h->ev_done, h->stream));
+  h->pending = true;
+  return AXG_OK;
+}
+
+int axg_poll(axg_handle *h, int32_t *done) {
+  if (!h || !done) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  *done = 1;
+  if (!h->pending) return AXG_OK;
+  const cudaError_t e = cudaEventQuery(h->ev_done);
+  if (e == cudaErrorNotReady) {
+    *done = 0;
+    return AXG_OK;
+  }
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventQuery");
+  h->pending = false;
+  return check_flags(h);
+}
+
+int axg_wait(axg_handle *h) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  CK(cudaStreamSynchronize(h->stream));
+  h->pending = false;
+  return check_flags(h);
+}
+
 int axg_get_receivers(axg_handle *h, float *out, int32_t cap, int32_t *nseismo_out) {
   if (!h || !out) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
   if (cap < h->nseismo) return fail(h, AXG_ERR_BAD_ARG, fmt("nseismo_cap %d < nseismo %d", cap, h->nseismo));
@@ -1287,7 +1462,8 @@ int axg_set_state(axg_handle *h, int32_t field, const float *in) {
   for (int c = 0; c < nc; ++c) {
     if (!p[c]) continue;
     std::vector<float> g = per_point(in + cs * c, ig, ng);
-    CK(cudaMemcpy(p[c], g.data(), ng * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(p[c], g.data(), ng * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
   }
   return AXG_OK;
 }
@@ -1355,14 +1531,15 @@ int axg_set_compensated(axg_handle *h, int32_t on) {
     for (int c = 0; c < 3; ++c) {
       if (mono && c == 1) continue;
       if ((rc = dalloc(h, &h->cu_s[c], h->nglob_s)) || (rc = dalloc(h, &h->cv_s[c], h->nglob_s))) return rc;
-      CK(cudaMemset(h->cu_s[c], 0, h->nglob_s * sizeof(float)));
-      CK(cudaMemset(h->cv_s[c], 0, h->nglob_s * sizeof(float)));
+      CK(cudaMemsetAsync(h->cu_s[c], 0, h->nglob_s * sizeof(float), h->stream));
+      CK(cudaMemsetAsync(h->cv_s[c], 0, h->nglob_s * sizeof(float), h->stream));
     }
     if (h->nel_f > 0) {
       if ((rc = dalloc(h, &h->cu_f, h->nglob_f)) || (rc = dalloc(h, &h->cv_f, h->nglob_f))) return rc;
-      CK(cudaMemset(h->cu_f, 0, h->nglob_f * sizeof(float)));
-      CK(cudaMemset(h->cv_f, 0, h->nglob_f * sizeof(float)));
+      CK(cudaMemsetAsync(h->cu_f, 0, h->nglob_f * sizeof(float), h->stream));
+      CK(cudaMemsetAsync(h->cv_f, 0, h->nglob_f * sizeof(float), h->stream));
     }
+    CK(cudaStreamSynchronize(h->stream));
   }
   h->kahan = on != 0;
   if (h->graph) {
@@ -1390,6 +1567,7 @@ int axg_get_info(axg_handle *h, axg_info *info) {
   info->growth_solid = h->ps.growth;
   info->patch_elems_fluid = h->pf.patch_elems;
   info->growth_fluid = h->pf.growth;
+  info->mesh_bytes = h->mesh ? h->mesh->bytes : 0;
   info->ctas_per_sm_force = h->solid_ctas / std::max(h->num_sms, 1);
   info->ctas_per_sm_step = h->solid_ctas_step / std::max(h->num_sms, 1);
   return AXG_OK;

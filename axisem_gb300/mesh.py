@@ -326,18 +326,61 @@ def gauss_stf(niter: int, deltat: float, period: float) -> np.ndarray:
     return np.exp(-((decay / period) * (t - shift)) ** 2).astype(F32)
 
 
+def set_source_receivers(m: Mesh, ni: int, nj_solid: int, nj_fluid: int, val, *, src_row: int = 1,
+                         num_rec: int = 6, niter: int = 60, deltat: float = 2e-6, seis_it: int = 2) -> Mesh:
+    """The solve-specific part of a coupled mesh: a point source on the
+    lattice corner (ni // 2, src_row) of the solid (moment vector `val`; None
+    puts a pressure source in the fluid, near the solid-fluid boundary),
+    stored in the four elements holding the point; `num_rec` receivers on the
+    top surface; the Gaussian stf of `niter` steps of `deltat`."""
+    ic = ni // 2
+    m.ielsrc = np.zeros(8, dtype=I32)
+    if val is None:
+        jc = nj_fluid - 1
+        els = [(jc - 1) * ni + ic - 1, (jc - 1) * ni + ic, jc * ni + ic - 1, jc * ni + ic]
+        pts = [(4, 4), (0, 4), (4, 0), (0, 0)]
+        st = np.zeros((5, 5, 8), dtype=F32, order="F")
+        for k, (e, (ip, jp)) in enumerate(zip(els, pts)):
+            m.ielsrc[k] = e + 1
+            st[ip, jp, k] = 1e-3
+        m.source_term_fl = st
+        m.fluid_src = 1
+        m.nelsrc = 4
+    else:
+        jc = min(max(int(src_row), 1), nj_solid - 1)
+        els = [(jc - 1) * ni + ic - 1, (jc - 1) * ni + ic, jc * ni + ic - 1, jc * ni + ic]
+        pts = [(4, 4), (0, 4), (4, 0), (0, 0)]
+        st = np.zeros((5, 5, 8, 3), dtype=F32, order="F")
+        for k, (e, (ip, jp)) in enumerate(zip(els, pts)):
+            m.ielsrc[k] = e + 1
+            st[ip, jp, k, :] = val
+        m.source_term_el = st
+        m.nelsrc = 4
+    m.deltat = deltat
+    m.stf = gauss_stf(niter, deltat, 20 * deltat)   # niter and num_rec follow from stf and recfile_el
+    m.seis_it = seis_it
+    top = nj_solid - 1
+    recs = np.linspace(0, ni - 1, num_rec).astype(int)
+    m.recfile_el = np.asfortranarray(np.stack(
+        [top * ni + recs + 1, np.full(num_rec, 2), np.full(num_rec, 4)], axis=1).astype(I32))
+    return m
+
+
 def coupled_mesh(ni: int, nj_solid: int, nj_fluid: int, src_type: int = _abi.MONOPOLE, *,
                  niter: int = 60, seed: int = 7, axial_column: bool = True, fluid_src: bool = False,
                  num_rec: int = 6, seis_it: int = 2, deltat: float = 2e-6,
                  free_surface: bool = False, absorbing: bool = False,
-                 bdry_scale: float = 1.0, terms: str = "all") -> Mesh:
+                 bdry_scale: float = 1.0, terms: str = "all", src_row: int = 1) -> Mesh:
     """A solid layer on top of a fluid layer, both ni elements wide, with
     the solid-fluid boundary along the fluid's top edge (jpol = 4) and the
     solid's bottom edge (jpol = 0); the I = 0 column lies on the axis.  A
     point source sits on an interior lattice point shared by four solid (or
     fluid) elements -- the source term is stored in the element-local copies of
     every element holding that point, as the reference does after assembly
-    (SOLVER/source.f90:1133); receivers sit on the top surface."""
+    (SOLVER/source.f90:1133); receivers sit on the top surface.  src_row
+    (1 .. nj_solid-1) is the lattice row of a solid source: deeper rows lie
+    nearer the fluid.  Source, receivers, niter and deltat change no other
+    array, so meshes differing only in them are the same mesh."""
     rng = np.random.default_rng(seed)
     m = structured_mesh(ni, nj_solid, src_type, seed=seed, axial="column" if axial_column else "none",
                         terms=terms)
@@ -380,38 +423,10 @@ def coupled_mesh(ni: int, nj_solid: int, nj_fluid: int, src_type: int = _abi.MON
             gf = np.zeros(m.nglob_fluid, dtype=F32)
             gf[m.igloc_fluid - 1] = 10.0 * rng.uniform(0, 1, size=m.igloc_fluid.shape)
             m.fluid_absorbing_gamma = _f(gf[m.igloc_fluid - 1].reshape(m.nel_fluid, 5, 5).transpose(2, 1, 0))
-    # source at lattice corner (I, J) = (ni//2, 1) of the solid (or fluid) grid
-    ic = ni // 2
-    m.ielsrc = np.zeros(8, dtype=I32)
-    if fluid_src and nj_fluid > 1:
-        jc = nj_fluid - 1
-        els = [(jc - 1) * ni + ic - 1, (jc - 1) * ni + ic, jc * ni + ic - 1, jc * ni + ic]
-        pts = [(4, 4), (0, 4), (4, 0), (0, 0)]
-        st = np.zeros((5, 5, 8), dtype=F32, order="F")
-        for k, (e, (ip, jp)) in enumerate(zip(els, pts)):
-            m.ielsrc[k] = e + 1
-            st[ip, jp, k] = 1e-3
-        m.source_term_fl = st
-        m.fluid_src = 1
-        m.nelsrc = 4
-    else:
-        jc = 1
-        els = [(jc - 1) * ni + ic - 1, (jc - 1) * ni + ic, jc * ni + ic - 1, jc * ni + ic]
-        pts = [(4, 4), (0, 4), (4, 0), (0, 0)]
-        val = rng.uniform(-1.0, 1.0, size=3).astype(F32) * 1e3
-        st = np.zeros((5, 5, 8, 3), dtype=F32, order="F")
-        for k, (e, (ip, jp)) in enumerate(zip(els, pts)):
-            m.ielsrc[k] = e + 1
-            st[ip, jp, k, :] = val
-        m.source_term_el = st
-        m.nelsrc = 4
-    m.deltat = deltat
-    m.stf = gauss_stf(niter, deltat, 20 * deltat)
-    m.seis_it = seis_it
-    top = nj_solid - 1
-    recs = np.linspace(0, ni - 1, num_rec).astype(int)
-    m.recfile_el = np.asfortranarray(np.stack(
-        [top * ni + recs + 1, np.full(num_rec, 2), np.full(num_rec, 4)], axis=1).astype(I32))
+    # source at lattice corner (I, J) = (ni//2, src_row) of the solid (or fluid) grid
+    val = None if (fluid_src and nj_fluid > 1) else rng.uniform(-1.0, 1.0, size=3).astype(F32) * 1e3
+    set_source_receivers(m, ni, nj_solid, nj_fluid, val, src_row=src_row, num_rec=num_rec, niter=niter,
+                         deltat=deltat, seis_it=seis_it)
     m.magnitude = 1e20
     return m
 

@@ -1,0 +1,237 @@
+"""Continuous-batching serving of time-loop solves on one GB300.
+
+No counterpart in the reference, which runs one solve per MPI job.  A request
+is one solve: a dominant period (which, with the source type, selects the
+mesh), a source type (monopole / dipole / quadrupole), a source depth, a
+receiver count and a seismogram duration.  The server
+
+  * keeps one resident mesh per (period, source type) in HBM: a small holder
+    solve creates it (axg_create) the first time it is needed, every request
+    on it shares it (axg_create_sharing) and owns only its wavefields,
+    source, receivers and stream;
+  * admits waiting requests in arrival order while their device bytes fit
+    the budget (a mesh not yet resident counts with its own bytes);
+  * advances every admitted solve in chunks of steps queued on its own
+    stream (axg_run_async), so that the solves' kernels overlap on the GPU,
+    and polls them (axg_poll); a finished solve returns its seismograms and
+    frees its memory, which admits the next request.
+
+The meshes are seeded synthetic coupled meshes (a solid layer over a fluid
+layer, `coupled_mesh`) whose size grows as the period shrinks; they stand in
+for the mesher's PREM meshes, which this build has no mesher for.
+"""
+from __future__ import annotations
+
+import collections
+import copy
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from .mesh import Mesh, coupled_mesh, set_source_receivers
+from .solver import Solver
+
+# period (s) -> coupled mesh (ni, nj_solid, nj_fluid): ~4x the elements per halving
+MESH_OF_PERIOD = {50: (32, 24, 8), 25: (64, 48, 16), 10: (128, 96, 32)}
+STEPS_PER_PERIOD = 4     # steps per period of seismogram (scaled down from the mesher's dt)
+DELTAT = 2e-8            # s; keeps the synthetic operators stable over the run lengths used
+POLES = (_abi.MONOPOLE, _abi.DIPOLE, _abi.QUADPOLE)
+
+
+@dataclass
+class Request:
+    rid: int
+    t_arrive: float      # s after the start of the stream
+    period: int          # 50, 25 or 10 s
+    pole: int            # 0 mono, 1 di, 2 quad
+    depth_km: float      # source depth, 0..700 km
+    n_rec: int           # receivers on the surface
+    duration_s: float    # seismogram length
+
+    @property
+    def key(self):
+        return (self.period, self.pole)
+
+    @property
+    def niter(self) -> int:
+        return max(8, int(round(self.duration_s / self.period * STEPS_PER_PERIOD)))
+
+
+def request_stream(n: int, rate_per_s: float, seed: int = 2026) -> list[Request]:
+    """Seeded Poisson arrivals; period uniform in {50, 25, 10} s, source type
+    uniform, depth uniform in [0, 700] km, receivers uniform in [20, 500],
+    duration uniform in [1800, 3600] s."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate_per_s, size=n))
+    return [Request(k, float(t[k]), int(rng.choice([50, 25, 10])), int(rng.integers(0, 3)),
+                    float(rng.uniform(0, 700)), int(rng.integers(20, 501)), float(rng.uniform(1800, 3600)))
+            for k in range(n)]
+
+
+_TEMPLATES: dict = {}   # (period, pole) -> (host mesh, source moment): the mesh database a server keeps loaded
+
+
+def request_mesh(req: Request, niter: int | None = None) -> Mesh:
+    """The solve's mesh descriptor: the period's mesh (kept on the host after
+    its first use) with this request's source row (depth), receivers and run
+    length."""
+    ni, njs, njf = MESH_OF_PERIOD[req.period]
+    if req.key not in _TEMPLATES:
+        t = coupled_mesh(ni, njs, njf, req.pole, niter=1, seed=11, num_rec=1, seis_it=4, deltat=DELTAT,
+                         terms="pole")
+        _TEMPLATES[req.key] = (t, t.source_term_el[4, 4, 0, :].copy())   # the moment at the source corner
+    tmpl, val = _TEMPLATES[req.key]
+    m = copy.copy(tmpl)   # shares the mesh arrays; the solve's fields are replaced below
+    row = 1 + int(round(req.depth_km / 700.0 * (njs - 2)))
+    nrec = min(req.n_rec, ni)   # receivers on distinct surface elements
+    return set_source_receivers(m, ni, njs, njf, val, src_row=njs - 1 - row, num_rec=nrec,
+                                niter=req.niter if niter is None else niter, deltat=DELTAT, seis_it=4)
+
+
+@dataclass
+class Job:
+    req: Request
+    solver: Solver
+    bytes: int
+    next_iter: int = 1
+    t_admit: float = 0.0
+
+
+@dataclass
+class Result:
+    rid: int
+    latency_s: float
+    seismograms: np.ndarray
+
+
+@dataclass
+class ServeStats:
+    wall_s: float
+    results: dict = field(default_factory=dict)
+    peak_bytes: int = 0
+    max_concurrent: int = 0
+
+    def summary(self) -> dict:
+        lat = np.array([r.latency_s for r in self.results.values()])
+        return {"solves": len(lat), "wall_s": self.wall_s,
+                "solves_per_hour": len(lat) / self.wall_s * 3600.0,
+                "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                "peak_device_gb": self.peak_bytes / 1e9, "max_concurrent": self.max_concurrent}
+
+
+def _solve_bytes(s: Solver) -> tuple[int, int]:
+    inf = s.info()
+    return inf["device_bytes"] - inf["mesh_bytes"], inf["mesh_bytes"]
+
+
+class Server:
+    """The serving loop; `budget_bytes` bounds the HBM the solves and
+    resident meshes may hold."""
+
+    def __init__(self, budget_bytes: float = 64e9, chunk: int = 0, lib=None):
+        """chunk: steps queued per call for a solve (0: all of them at once;
+        smaller chunks let a long solve yield the host loop between chunks)."""
+        self.lib = lib or _abi.load_library()
+        self.budget = budget_bytes
+        self.chunk = chunk
+        self.meshes: dict = {}      # key -> holder Solver (keeps the mesh resident)
+        self.mesh_bytes: dict = {}
+        self.used = 0
+
+    def close(self):
+        for s in self.meshes.values():
+            s.close()
+        self.meshes.clear()
+
+    def _holder(self, req: Request) -> Solver:
+        if req.key not in self.meshes:
+            s = Solver(request_mesh(req, niter=1), lib=self.lib)
+            own, mesh = _solve_bytes(s)
+            self.meshes[req.key] = s
+            self.mesh_bytes[req.key] = own + mesh
+            self.used += own + mesh
+        return self.meshes[req.key]
+
+    def _estimate(self, req: Request) -> int:
+        ni, njs, njf = MESH_OF_PERIOD[req.period]
+        nglob = (4 * ni + 1) * (4 * njs + 1) + (4 * ni + 1) * (4 * njf + 1)
+        need = nglob * 4 * 4 * 3 + 4 * req.niter * 3 * req.n_rec + (1 << 20)   # wavefields, seismograms
+        if req.key not in self.meshes:
+            need += 4 * need   # a mesh is a few times its wavefields
+        return need
+
+    def preload(self, keys):
+        """Make the meshes of `keys` ((period, pole) pairs) resident."""
+        for period, pole in keys:
+            self._holder(Request(-1, 0.0, period, pole, 0.0, 1, 1800.0))
+
+    def _launch(self, job: Job):
+        left = job.req.niter - job.next_iter + 1
+        n = left if self.chunk <= 0 else min(self.chunk, left)
+        job.solver.run_async(job.next_iter, n)
+        job.next_iter += n
+
+    def run(self, requests: list[Request], sequential: bool = False, resident: bool = False) -> ServeStats:
+        """Serves `requests` (arrival times relative to the call).  sequential:
+        one solve at a time, each on its own freshly built mesh -- the plain
+        path run request after request, the baseline -- or, with `resident`,
+        on the server's resident meshes (the gain of overlapping alone)."""
+        pending = collections.deque(sorted(requests, key=lambda r: r.t_arrive))
+        waiting: collections.deque = collections.deque()
+        active: list[Job] = []
+        stats = ServeStats(wall_s=0.0)
+        t0 = time.perf_counter()
+        while pending or waiting or active:
+            now = time.perf_counter() - t0
+            while pending and pending[0].t_arrive <= now:
+                waiting.append(pending.popleft())
+            # admission
+            while waiting and (not sequential or not active):
+                req = waiting[0]
+                if active and self.used + self._estimate(req) > self.budget:
+                    break
+                waiting.popleft()
+                fresh = sequential and not resident
+                if fresh:
+                    s = Solver(request_mesh(req), lib=self.lib)
+                else:
+                    s = Solver(request_mesh(req), lib=self.lib, share_with=self._holder(req))
+                own, mesh = _solve_bytes(s)
+                nbytes = own + (mesh if fresh else 0)
+                self.used += nbytes
+                job = Job(req, s, nbytes, t_admit=time.perf_counter() - t0)
+                self._launch(job)
+                active.append(job)
+            stats.peak_bytes = max(stats.peak_bytes, self.used)
+            stats.max_concurrent = max(stats.max_concurrent, len(active))
+            # progress
+            progressed = False
+            for job in list(active):
+                if not job.solver.poll():
+                    continue
+                progressed = True
+                if job.next_iter <= job.req.niter:
+                    self._launch(job)
+                    continue
+                rec = job.solver.receivers().copy()
+                done = time.perf_counter() - t0
+                stats.results[job.req.rid] = Result(job.req.rid, done - job.req.t_arrive, rec)
+                job.solver.close()
+                self.used -= job.bytes
+                active.remove(job)
+            if not progressed:
+                if not active and pending and not waiting:
+                    time.sleep(max(0.0, min(0.01, pending[0].t_arrive - (time.perf_counter() - t0))))
+                else:
+                    time.sleep(20e-6)
+        stats.wall_s = time.perf_counter() - t0
+        return stats
+
+
+def solve_alone(req: Request, lib=None) -> np.ndarray:
+    """The request's seismograms from a solve on its own, built from scratch."""
+    with Solver(request_mesh(req), lib=lib) as s:
+        s.run()
+        return s.receivers().copy()

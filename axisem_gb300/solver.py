@@ -37,14 +37,21 @@ def _fp(a):
 class Solver:
     """One solve on one GPU (one axg_handle)."""
 
-    def __init__(self, mesh: Mesh, lib=None, patch_elems: int = 0, growth: int = -1):
+    def __init__(self, mesh: Mesh, lib=None, patch_elems: int = 0, growth: int = -1,
+                 share_with: "Solver | None" = None):
         """patch_elems / growth: the patch shape (axg_create_tuned); 0 / -1
-        let the planner's tuner choose, as axg_create does."""
+        let the planner's tuner choose, as axg_create does.  share_with: an
+        open Solver on the same mesh whose device mesh data this solve shares
+        (axg_create_sharing); only the source, receivers and run length of
+        `mesh` are then this solve's."""
         self.lib = lib or _abi.load_library()
         self.mesh = mesh
         self._desc = mesh.desc()
         h = C.c_void_p()
-        rc = self.lib.axg_create_tuned(C.byref(self._desc), patch_elems, growth, C.byref(h))
+        if share_with is not None:
+            rc = self.lib.axg_create_sharing(share_with.h, C.byref(self._desc), C.byref(h))
+        else:
+            rc = self.lib.axg_create_tuned(C.byref(self._desc), patch_elems, growth, C.byref(h))
         _check(self.lib, None, rc)
         self.h = h
         self.nseismo = (mesh.niter // max(mesh.seis_it, 1)) + 1
@@ -75,6 +82,21 @@ class Solver:
         if n_iter is None:
             n_iter = self.mesh.niter - first_iter + 1
         _check(self.lib, self.h, self.lib.axg_run(self.h, first_iter, n_iter))
+
+    def run_async(self, first_iter: int = 1, n_iter: int | None = None):
+        """Queue steps on the solve's stream and return (axg_run_async)."""
+        if n_iter is None:
+            n_iter = self.mesh.niter - first_iter + 1
+        _check(self.lib, self.h, self.lib.axg_run_async(self.h, first_iter, n_iter))
+
+    def poll(self) -> bool:
+        """True once the queued steps have finished (axg_poll)."""
+        done = C.c_int32(0)
+        _check(self.lib, self.h, self.lib.axg_poll(self.h, C.byref(done)))
+        return bool(done.value)
+
+    def wait(self):
+        _check(self.lib, self.h, self.lib.axg_wait(self.h))
 
     def receivers(self) -> np.ndarray:
         out = np.zeros((self.nseismo, 3, max(self.mesh.num_rec, 1)), dtype=np.float32, order="F")

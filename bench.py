@@ -273,6 +273,8 @@ def run_gpu(args):
         timeloop_anel = run_timeloop(args, pole, ws, rank, anel=True)
         timeloop_comp = run_timeloop(args, pole, ws, rank, compensated=True)
 
+    serving = run_serving(args) if args.serve_requests > 0 else None
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, sample = time_oracle(pole, args.cpu_seconds, 1)
@@ -300,6 +302,7 @@ def run_gpu(args):
         "timeloop": timeloop,
         "timeloop_anel": timeloop_anel,
         "timeloop_compensated": timeloop_comp,
+        "serving": serving,
         "clocks": clocks,
         "gpu_launches": int(args.steps * info["kernels_per_force"]),
         "plan": {"patches": info["n_patches_solid"], "colours": info["n_colours_solid"],
@@ -382,6 +385,37 @@ def run_timeloop(args, pole, ws, rank, anel=False, compensated=False):
             "finite": bool(np.isfinite(rec).all())}
 
 
+def run_serving(args):
+    """Continuous-batching serving (axisem_gb300.serve; the meshes of the
+    stream resident before it starts) against the same request list run one
+    solve at a time, each on its own freshly built mesh (the plain path,
+    sequentially).  Seeded Poisson arrivals at args.serve_rate per second;
+    each request's seismograms must be identical in both runs."""
+    from axisem_gb300.serve import Server, request_stream
+    reqs = request_stream(args.serve_requests, args.serve_rate, seed=2026)
+    srv = Server(budget_bytes=64e9)
+    try:
+        srv.preload({r.key for r in reqs})   # the server's meshes are resident before the stream starts
+        served = srv.run(reqs)
+    finally:
+        srv.close()
+    seq_srv = Server(budget_bytes=64e9)
+    try:
+        seq = seq_srv.run(reqs, sequential=True)
+        seq_srv.preload({r.key for r in reqs})
+        seq_res = seq_srv.run(reqs, sequential=True, resident=True)
+    finally:
+        seq_srv.close()
+    same = all(np.array_equal(served.results[r.rid].seismograms, seq.results[r.rid].seismograms) for r in reqs)
+    a, b = served.summary(), seq.summary()
+    return {"requests": len(reqs), "arrival_rate_per_s": args.serve_rate,
+            "mix": "period {50,25,10} s -> 1k/4k/16k-element coupled meshes, pole {mono,di,quad}, "
+                   "depth 0-700 km, 20-500 receivers, 1800-3600 s",
+            "served": a, "sequential_plain": b, "sequential_resident_meshes": seq_res.summary(),
+            "solves_per_hour_ratio": a["solves_per_hour"] / b["solves_per_hour"],
+            "results_identical_to_sequential": bool(same)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -394,6 +428,8 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--timeloop-steps", type=int, default=64)
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-rate", type=float, default=1000.0)   # saturating: measures capacity
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -244,6 +244,25 @@ int axg_download_gvec_force(axg_handle *h, float *f_gvec);
  * handle's value. */
 int axg_set_tuning(axg_handle *h, int32_t patch_elems, int32_t steps_per_graph);
 
+/* A further solve on the mesh of an existing handle (serving: meshes stay
+ * resident, solves come and go).  `desc` must describe the same mesh -- sizes,
+ * pole type, global numbering, axial elements, attenuation layout are
+ * checked; metric terms, masses and boundary terms are taken from `mesh_of`
+ * -- while its source, stf, receivers, niter, seis_it, deltat and magnitude
+ * are this solve's.  Element blocks, plans, masses, coupling tables and
+ * attenuation constants stay shared (freed with the last handle of the
+ * mesh); the new handle has its own wavefields, stream and CUDA graph.
+ * No counterpart in the reference. */
+int axg_create_sharing(axg_handle *mesh_of, const axg_mesh_desc *desc, axg_handle **out);
+
+/* axg_run without waiting: the steps are queued on the handle's stream (so
+ * the solves of several handles run concurrently); axg_poll sets *done
+ * once they finished, axg_wait blocks until then.  Both then report a
+ * blow-up or a bounded-wait timeout as axg_run does. */
+int axg_run_async(axg_handle *h, int32_t first_iter, int32_t n_iter);
+int axg_poll(axg_handle *h, int32_t *done);
+int axg_wait(axg_handle *h);
+
 /* Compensated time integration on (1) or off (0): the predictor
  * disp += dt velo + dt^2/2 acc0 and the corrector velo += dt/2 (acc0 + acc1)
  * (and chi, dchi in the fluid) use Kahan's compensated summation in FP32, with
@@ -275,6 +294,7 @@ typedef struct axg_info {
   int32_t patch_elems_solid, growth_solid;  /* patch shape the planner used */
   int32_t patch_elems_fluid, growth_fluid;
   int32_t ctas_per_sm_force, ctas_per_sm_step;  /* resident solid-kernel CTAs per SM */
+  int64_t mesh_bytes;                 /* part of device_bytes shared by the handles of one mesh */
 } axg_info;
 int axg_get_info(axg_handle *h, axg_info *info);
 
