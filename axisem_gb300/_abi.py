@@ -58,6 +58,8 @@ AXIAL_TERMS_USED = {
     QUADPOLE: ["M0_w1", "M0_w2", "M0_w3", "M0_w4", "M0_w5", "M0_w6"],
 }
 
+(SCHEME_NEWMARK2, SCHEME_SYMPLEC4, SCHEME_ML_SO4M5, SCHEME_ML_SO6M7, SCHEME_KL_O8M17,
+ SCHEME_SS_35O10) = range(6)
 (FIELD_DISP, FIELD_VELO, FIELD_ACC0, FIELD_CHI, FIELD_DCHI, FIELD_DDCHI0, FIELD_MEMVAR, FIELD_ATT_SRC_TR,
  FIELD_ATT_SRC_DEV, FIELD_DISP_COMP, FIELD_VELO_COMP, FIELD_CHI_COMP, FIELD_DCHI_COMP) = range(13)
 
@@ -141,6 +143,10 @@ SIGNATURES = {
     "axg_create_tuned": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "axg_set_compensated": (C.c_int, [C.c_void_p, C.c_int32]),
     "axg_create_sharing": (C.c_int, [C.c_void_p, C.POINTER(MeshDesc), C.POINTER(C.c_void_p)]),
+    "axg_symplectic_coefficients": (C.c_int, [C.c_int32, C.c_double, C.POINTER(C.c_double),
+                                              C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                              C.POINTER(C.c_int32)]),
+    "axg_set_time_scheme": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
     "axg_run_async": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "axg_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "axg_wait": (C.c_int, [C.c_void_p]),

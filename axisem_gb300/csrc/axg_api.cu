@@ -130,6 +130,10 @@ struct axg_handle {
   std::string err = "no error";
   int64_t kernels_per_step = 0, kernels_per_force = 0;
   int solid_ctas_step = 1;
+  // time scheme: 0 Newmark (newmark2), else a symplectic scheme of nstages stages
+  int scheme = 0, nstages = 0;
+  std::vector<float> sym_cd, sym_cv;   // coefd(1:nstages+1) deltat, coefv(1:nstages) deltat
+  float *stf_stages = nullptr;         // (niter, nstages): the stf at the stages' times
   // compensated (Kahan) time integration
   bool kahan = false;
   float *cu_s[3] = {}, *cv_s[3] = {}, *cu_f = nullptr, *cv_f = nullptr;
@@ -543,6 +547,7 @@ int prepare_solid_kernels(axg_handle *h) {
   int rc = prepare_solid_kernel<POLE, MODE_FORCE, false, false>(h, &h->solid_ctas);
   if (rc) return rc;
   int *c = &h->solid_ctas_step;
+  if (h->scheme != AXG_SCHEME_NEWMARK2) return prepare_solid_kernel<POLE, MODE_SYMPLECTIC, false, false>(h, c);
   if (h->anel) {
     return h->kahan ? prepare_solid_kernel<POLE, MODE_NEWMARK, true, true>(h, c)
                     : prepare_solid_kernel<POLE, MODE_NEWMARK, true, false>(h, c);
@@ -607,7 +612,13 @@ void enqueue_force(axg_handle *h, cudaStream_t s) {
   launch_solid<MODE_FORCE>(h, s);
 }
 
+void enqueue_step_symplectic(axg_handle *h, cudaStream_t s);
+
 void enqueue_step(axg_handle *h, cudaStream_t s) {
+  if (h->scheme != AXG_SCHEME_NEWMARK2) {
+    enqueue_step_symplectic(h, s);
+    return;
+  }
   StateArgs ss = solid_state(h), fs = fluid_state(h);
   if (h->nel_f > 0) {
     if (h->to_fluid.n > 0) {
@@ -635,6 +646,61 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
     }
   }
   launch_solid<MODE_NEWMARK>(h, s);
+  receivers_kernel<<<1, 256, 0, s>>>(ss, h->rec_gidx_d, h->num_rec, h->seis_it, h->pole, h->rec, h->nseismo,
+                                     h->iter);
+}
+
+// One step of symplectic_time_loop (SOLVER/time_evol_wave.F90:587-727):
+// per stage the drift (on the gathers), fluid stiffness and the coupling
+// into it, solid stiffness, the coupling into the solid, the kicks (by the
+// last writers); then the final drift and the seismograms.
+template <int POLE>
+void launch_solid_symplectic(axg_handle *h, cudaStream_t s, const StateArgs &st) {
+  DomainArgs a = domain_args(h->ds, h->ps);
+  for (int c = 0; c < h->ps.n_colours; ++c) {
+    a.patch_begin = h->ps.colour_start[c];
+    const int n = h->ps.colour_start[c + 1] - h->ps.colour_start[c];
+    solid_patch_kernel<POLE, MODE_SYMPLECTIC, false, false>
+        <<<std::min(n, h->solid_ctas_step), kThreads, solid_smem_bytes<POLE, MODE_SYMPLECTIC, false, false>(), s>>>(
+            a, st, h->spec, n, h->an);
+  }
+}
+
+void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
+  for (int i = 0; i < h->nstages; ++i) {
+    StateArgs ss = solid_state(h), fs = fluid_state(h);
+    ss.dt = fs.dt = h->sym_cd[i];
+    ss.hdt2 = fs.hdt2 = 0.f;  // the coupling's predictor is then the drift u + coefd(i) v
+    ss.kick = fs.kick = h->sym_cv[i];
+    ss.stf = h->stf_stages + (int64_t)i * std::max(h->niter, 1);
+    if (h->nel_f > 0) {
+      if (h->to_fluid.n > 0) {
+        const int nb = (h->to_fluid.n + 255) / 256;
+        if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(h->to_fluid, ss, h->ff);
+        else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(h->to_fluid, ss, h->ff);
+      }
+      DomainArgs a = domain_args(h->df, h->pf);
+      a.fsmask = nullptr;  // symplectic_time_loop applies no free-surface mask
+      for (int c = 0; c < h->pf.n_colours; ++c) {
+        a.patch_begin = h->pf.colour_start[c];
+        const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
+        if (h->pole == AXG_MONOPOLE) fluid_patch_kernel<0, false, true><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+        else fluid_patch_kernel<1, false, true><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+      }
+      if (h->to_solid.n > 0) {
+        const int nb = (h->to_solid.n + 255) / 256;
+        if (h->pole == AXG_MONOPOLE) couple_to_solid_kernel<POLE_MONO><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
+        else if (h->pole == AXG_DIPOLE) couple_to_solid_kernel<POLE_DI><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
+        else couple_to_solid_kernel<POLE_QUAD><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
+      }
+    }
+    if (h->pole == AXG_MONOPOLE) launch_solid_symplectic<POLE_MONO>(h, s, ss);
+    else if (h->pole == AXG_DIPOLE) launch_solid_symplectic<POLE_DI>(h, s, ss);
+    else launch_solid_symplectic<POLE_QUAD>(h, s, ss);
+  }
+  StateArgs ss = solid_state(h), fs = fluid_state(h);
+  const int64_t n = std::max(h->nglob_s, h->nel_f > 0 ? h->nglob_f : 0);
+  drift_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ss, fs, h->sym_cd[h->nstages]);
   receivers_kernel<<<1, 256, 0, s>>>(ss, h->rec_gidx_d, h->num_rec, h->seis_it, h->pole, h->rec, h->nseismo,
                                      h->iter);
 }
@@ -710,6 +776,73 @@ void prepass_flags(const axg_mesh_desc *d, std::vector<uint8_t> &pre_s, std::vec
       pre_f[d->igloc_fluid[25 * ef + i + 5 * d->bdry_jpol_fluid[b]] - 1] = 1;
     }
   }
+}
+
+// Coefficients of the symplectic schemes (symplectic_coefficients,
+// SOLVER/time_evol_wave.F90:749-967): coefd(1:n+1) drifts and coefv(1:n)
+// kicks, in units of deltat.  The reference writes most of these constants
+// without a kind suffix, so they are single-precision values widened to
+// double (sp below); and its SS_scheme (:972-992) computes the middle drift
+// as 1 / 2 - sum(...) in Fortran integer division (1 / 2 = 0) -- both are
+// restated as it computes them.  Returns nstages, 0 for an unknown scheme.
+double sp(double x) { return (double)(float)x; }
+void ss_scheme(const std::vector<double> &g, std::vector<double> &a, std::vector<double> &b) {
+  const int n = (int)g.size(), ns = 2 * n + 1;
+  a.assign(ns + 1, 0.0);
+  b.assign(ns, 0.0);
+  a[0] = g[0] / 2.0;
+  for (int i = 1; i < n; ++i) a[i] = (g[i - 1] + g[i]) / 2.0;
+  double sa = 0.0;
+  for (int i = 0; i < n; ++i) sa += a[i];
+  a[n] = 0.0 - sa;  // 1 / 2 - sum(a(1:n)) with integer 1 / 2
+  for (int i = n + 1; i <= 2 * n + 1; ++i) a[i] = a[2 * n + 1 - i];
+  double sg = 0.0;
+  for (int i = 0; i < n; ++i) b[i] = g[i], sg += g[i];
+  b[n] = 1.0 - 2.0 * sg;
+  for (int i = n + 1; i < 2 * n + 1; ++i) b[i] = b[2 * n - i];
+}
+int symplectic_coefficients(int scheme, std::vector<double> &cd, std::vector<double> &cv) {
+  cd.clear();
+  cv.clear();
+  if (scheme == AXG_SCHEME_SYMPLEC4) {  // PEFRL (Omelyan, Mryglod and Folk, 2002)
+    const double zeta = sp(+0.1786178958448091), iota = sp(-0.2123418310626054),
+                 kappa = sp(-0.06626458266981849);
+    cd = {zeta, kappa, 1.0 - 2.0 * (zeta + kappa), kappa, zeta};
+    cv = {0.5 - iota, iota, iota, 0.5 - iota};
+  } else if (scheme == AXG_SCHEME_ML_SO4M5) {  // McLachlan (1995), order 4, m = 5
+    const double rho = (14.0 - std::sqrt(19.0)) / 108.0, theta = (20.0 - 7.0 * std::sqrt(19.0)) / 108.0;
+    const double nu = 2.0 / 5.0, lambda = -1.0 / 10.0;
+    cd = {rho, theta, 0.5 - rho - theta, 0.5 - rho - theta, theta, rho};
+    cv = {nu, lambda, 1.0 - 2.0 * (nu + lambda), lambda, nu};
+  } else if (scheme == AXG_SCHEME_ML_SO6M7) {  // McLachlan (1995), order 6, m = 7
+    const double d[4] = {sp(-1.01308797891717472981), sp(1.18742957373254270702), sp(-0.01833585209646059034),
+                         sp(0.34399425728109261313)};
+    const double v[4] = {sp(0.00016600692650009894), sp(-0.37962421426377360608), sp(0.68913741185181063674),
+                         sp(0.38064159097092574080)};
+    cd = {d[0], d[1], d[2], d[3], d[3], d[2], d[1], d[0]};
+    cv = {v[0], v[1], v[2], v[3], v[2], v[1], v[0]};
+  } else if (scheme == AXG_SCHEME_KL_O8M17) {  // Kahan and Li (1997), order 8
+    const double g[8] = {0.13020248308889008088, 0.56116298177510838456, -0.38947496264484728641,
+                         0.15884190655515560090, -0.39590389413323757734, 0.18453964097831570709,
+                         0.25837438768632204729, 0.29501172360931029887};
+    std::vector<double> gv;
+    for (double x : g) gv.push_back(sp(x));
+    ss_scheme(gv, cd, cv);
+  } else if (scheme == AXG_SCHEME_SS_35O10) {  // Sofroniou and Spaletta (2004), order 10
+    const double g[17] = {0.078795722521686419263907679337684, 0.31309610341510852776481247192647,
+                          0.027918383235078066109520273275299, -0.22959284159390709415121339679655,
+                          0.13096206107716486317465685927961, -0.26973340565451071434460973222411,
+                          0.074973343155891435666137105641410, 0.11199342399981020488957508073640,
+                          0.36613344954622675119314812353150, -0.39910563013603589787862981058340,
+                          0.10308739852747107731580277001372, 0.41143087395589023782070411897608,
+                          -0.0048663605831352617621956593099771, -0.39203335370863990644808193642610,
+                          0.051942502962449647037182904015976, 0.050665090759924496335874344156866,
+                          0.049674370639729879054568800279461};
+    std::vector<double> gv;
+    for (double x : g) gv.push_back(sp(x));
+    ss_scheme(gv, cd, cv);
+  }
+  return (int)cv.size();
 }
 
 // tuned (or requested) patch shape, then the plan
@@ -1547,6 +1680,63 @@ int axg_set_compensated(axg_handle *h, int32_t on) {
     h->graph = nullptr;
   }
   return prepare_kernels(h);
+}
+
+int axg_symplectic_coefficients(int32_t scheme, double deltat, double *coefd, double *coefv, double *coeff,
+                                int32_t *nstages) {
+  if (!coefd || !coefv || !coeff || !nstages) return fail(nullptr, AXG_ERR_BAD_ARG, "NULL argument");
+  std::vector<double> cd, cv;
+  const int n = symplectic_coefficients(scheme, cd, cv);
+  if (n == 0) return fail(nullptr, AXG_ERR_BAD_ARG, fmt("scheme %d is not a symplectic scheme", scheme));
+  double acc = 0.0;
+  for (int i = 0; i <= n; ++i) coefd[i] = cd[i] * deltat;  // coefd = coefd * deltat
+  for (int i = 0; i < n; ++i) {
+    coefv[i] = cv[i] * deltat;
+    acc += coefd[i];
+    coeff[i] = acc;  // coeff(i) = sum(coefd(1:i))
+  }
+  *nstages = n;
+  return AXG_OK;
+}
+
+int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  if (scheme == AXG_SCHEME_NEWMARK2) {
+    h->scheme = 0;
+    h->nstages = 0;
+  } else {
+    std::vector<double> cd, cv;
+    const int n = symplectic_coefficients(scheme, cd, cv);
+    if (n == 0) return fail(h, AXG_ERR_BAD_ARG, fmt("unknown time scheme %d", scheme));
+    if (h->anel || h->kahan || h->fluid_src || h->df.fsmask)
+      return fail(h, AXG_ERR_UNSUPPORTED,
+                  "symplectic schemes: attenuation, the compensated mode, a fluid source and a fluid free surface "
+                  "are not supported");
+    if (!stf_stages) return fail(h, AXG_ERR_BAD_ARG, "stf_stages is NULL");
+    h->sym_cd.resize(n + 1);
+    h->sym_cv.resize(n);
+    for (int i = 0; i <= n; ++i) h->sym_cd[i] = (float)(cd[i] * h->dt);
+    for (int i = 0; i < n; ++i) h->sym_cv[i] = (float)(cv[i] * h->dt);
+    std::vector<float> stf(stf_stages, stf_stages + (size_t)std::max(h->niter, 1) * n);
+    int rc;
+    if ((rc = upload(h, &h->stf_stages, stf))) return rc;
+    h->scheme = scheme;
+    h->nstages = n;
+  }
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  int rc = prepare_kernels(h);
+  if (rc) return rc;
+  if (h->scheme) {
+    h->kernels_per_step = (int64_t)h->nstages * (h->ps.n_colours + (h->nel_f > 0 ? h->pf.n_colours +
+                          (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0)) + 2;
+  } else {
+    h->kernels_per_step = h->ps.n_colours + 1 +
+                          (h->nel_f > 0 ? h->pf.n_colours + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);
+  }
+  return axg_reset(h);
 }
 
 int axg_get_info(axg_handle *h, axg_info *info) {

@@ -60,7 +60,11 @@ constexpr int kThreads = 32 * kWarps;
 constexpr unsigned kFull = 0xffffffffu;
 
 enum { POLE_MONO = 0, POLE_DI = 1, POLE_QUAD = 2 };
-enum { MODE_FORCE = 0, MODE_NEWMARK = 1 };
+// FORCE: stiffness + assembly; NEWMARK: a Newmark step
+// (SOLVER/time_evol_wave.F90:264-502); SYMPLECTIC: one stage of a symplectic
+// step (SOLVER/time_evol_wave.F90:516-742): drift u + c_d v on the gather,
+// kick v + c_v a by the last writer
+enum { MODE_FORCE = 0, MODE_NEWMARK = 1, MODE_SYMPLECTIC = 2 };
 
 // slot of each metric array inside an element's block (same order as the
 // host packing, SOLID_TERMS_USED of the Python mirror)
@@ -118,7 +122,8 @@ struct StateArgs {
   int32_t *blowup;          // first iteration that blew up (0 = none)
   int32_t *err;             // device error word (AXG_ERR_TIMEOUT when a bounded wait gave up)
   float thresh;             // 10 |magnitude|
-  float dt, hdt, hdt2;
+  float dt, hdt, hdt2;      // Newmark: deltat, deltat/2, deltat^2/2; symplectic stage: dt = coefd(i) deltat
+  float kick;               // symplectic stage: coefv(i) deltat
   SrcTable src;
   int64_t nglob;            // extent of the state arrays (checked builds)
   int32_t niter;            // extent of stf
@@ -611,7 +616,7 @@ __host__ __device__ constexpr int solid_buffers(int mode) { return mode == MODE_
 // three (its register-staged gather is latency-bound; 80 registers), the
 // others two (no spills at 128 registers)
 __host__ __device__ constexpr int solid_min_ctas(int mode, bool anel, bool kahan = false) {
-  return mode == MODE_NEWMARK && !anel && !kahan ? 3 : 2;
+  return mode != MODE_FORCE && !anel && !kahan ? 3 : 2;
 }
 // Bank swizzle of the shared point arrays: patch point t lives at
 // t + pad * (t / 32).  An element's 25 points sit in five runs of five
@@ -669,8 +674,9 @@ template <int POLE, int MODE, bool ANEL, bool KAHAN>
 __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
     solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches,
                        const __grid_constant__ AnelArgs an) {  // an.ex[] is indexed at run time
-  static_assert(!ANEL || MODE == MODE_NEWMARK, "attenuation runs in the time loop only");
-  static_assert(!KAHAN || MODE == MODE_NEWMARK, "the compensated mode is a time-loop mode");
+  static_assert(!ANEL || MODE == MODE_NEWMARK, "attenuation runs in the Newmark time loop only");
+  static_assert(!KAHAN || MODE == MODE_NEWMARK, "the compensated mode is a Newmark time-loop mode");
+  constexpr bool TL = MODE != MODE_FORCE;  // a time-loop mode
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
   constexpr int NT = n_terms(POLE), NA = n_axial(POLE);
   constexpr int BS = solid_block_stride(NT);
@@ -702,7 +708,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
   if (threadIdx.x < kWarps * STG) mbar_init(&bars[threadIdx.x], 1);
   if (threadIdx.x < kMaxSubrounds) mbar_init(&s_round[threadIdx.x], kThreads);
   if (threadIdx.x < 2) mbar_init(&s_wbar[threadIdx.x], 1);
-  if (threadIdx.x == 0) s_stop = (MODE == MODE_NEWMARK) ? *st.blowup : 0;
+  if (threadIdx.x == 0) s_stop = TL ? *st.blowup : 0;
   fence_mbar_init();
   __syncthreads();
   if (s_stop) return;  // uniform across the CTA; no copy has been issued
@@ -738,7 +744,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
     }
   };
   float stf1 = 0.f;
-  if (MODE == MODE_NEWMARK && AXG_BOUND(*st.iter - 1, st.niter, 3)) stf1 = st.stf[*st.iter - 1];
+  if (TL && AXG_BOUND(*st.iter - 1, st.niter, 3)) stf1 = st.stf[*st.iter - 1];
 
   // one thread: bulk copy of a patch's point words into buffer b (each
   // patch's words start 16-byte aligned, padded to a multiple of four)
@@ -851,6 +857,8 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
               float k = ok ? st.cu[gc(c)][g] : 0.f;
               if (ok) u = predict_comp(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2, k);
               cc[KAHAN ? q : 0][c] = k;
+            } else if (ok && MODE == MODE_SYMPLECTIC) {
+              u = fmaf(st.dt, st.v[gc(c)][g], u);  // drift: disp + velo * coefd(i)
             } else if (ok) {
               u = predict(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2);
             }
@@ -901,7 +909,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
             u[2] = s_u[2][idx];
           }
         }
-        if (MODE == MODE_NEWMARK && lane == 6) {
+        if (TL && lane == 6) {
           // runtime_info guard on disp(1,1,:,:) (SOLVER/time_evol_wave.F90:1042)
           const float mx = fmaxf(fabsf(u[0]), fmaxf(fabsf(u[1]), fabsf(u[2])));
           if (!(mx <= st.thresh)) atomicCAS(st.blowup, 0, *st.iter);
@@ -1012,7 +1020,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
             vel[q][c] = last ? st.v[gc(c)][g] : 0.f;
-            acc[q][c] = last ? st.a[gc(c)][g] : 0.f;
+            acc[q][c] = last && MODE == MODE_NEWMARK ? st.a[gc(c)][g] : 0.f;
             if (KAHAN) kv[KAHAN ? q : 0][c] = last ? st.cv[gc(c)][g] : 0.f;
           }
         }
@@ -1041,8 +1049,20 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
             const int cg = gc(c);
-            float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im[q]) * v[c] : -im[q] * v[c];
             const float dsp = s_u[c][spos(t)];
+            if (MODE == MODE_SYMPLECTIC) {
+              // kick (SOLVER/time_evol_wave.F90:688-717): acc = -inv_mass acc
+              // [- absorbing terms], velo += acc * coefv(i); the dipole's z
+              // component takes twice the whole acceleration
+              float a = -im[q] * v[c];
+              if (st.gamma) a = a - 2.f * gam[q] * vel[q][c] - gam[q] * gam[q] * dsp;
+              st.v[cg][g] = fmaf((POLE == POLE_DI && cg == 2) ? 2.f * st.kick : st.kick, a, vel[q][c]);
+              st.a[cg][g] = a;
+              const bool zero = (w[q] & kPtAxis) && axis_masked<POLE>(cg);
+              st.u[cg][g] = zero ? 0.f : dsp;
+              continue;
+            }
+            float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im[q]) * v[c] : -im[q] * v[c];
             if (st.gamma) a = a - 2.f * gam[q] * vel[q][c] - gam[q] * gam[q] * dsp;
             if (KAHAN) {
               float k = kv[KAHAN ? q : 0][c];
@@ -1073,7 +1093,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
 // warp loads the metric terms of its next element while it computes the
 // current one; the write-back loads the last writers' inverse mass, dchi and
 // ddchi0 in one batch before it stores.
-template <int NONMONO, bool KAHAN>
+template <int NONMONO, bool KAHAN, bool SYMP = false>
 __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp) {
   __shared__ float s_u[kMaxPatchPoints];
   __shared__ float s_f[kMaxPatchPoints];
@@ -1103,6 +1123,8 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
         float k = ok ? st.cu[0][g] : 0.f;
         uu[q] = ok ? predict_comp(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2, k) : 0.f;
         cc[KAHAN ? q : 0] = k;
+      } else if (SYMP) {
+        uu[q] = ok ? fmaf(st.dt, st.v[0][g], st.u[0][g]) : 0.f;  // drift: chi + dchi * coefd(i)
       } else {
         uu[q] = ok ? predict(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2) : 0.f;
       }
@@ -1199,7 +1221,7 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
       im[q] = last ? st.inv_mass[g] : 0.f;
       gam[q] = last && st.gamma ? st.gamma[g] : 0.f;
       vel[q] = last ? st.v[0][g] : 0.f;
-      acc[q] = last ? st.a[0][g] : 0.f;
+      acc[q] = last && !SYMP ? st.a[0][g] : 0.f;
       if (KAHAN) kv[KAHAN ? q : 0] = last ? st.cv[0][g] : 0.f;
     }
 #pragma unroll
@@ -1216,7 +1238,9 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
       float a = -im[q] * v;
       const float chi = s_u[t];
       if (st.gamma) a = a - 2.f * gam[q] * vel[q] - gam[q] * gam[q] * chi;
-      if (KAHAN) {
+      if (SYMP) {
+        st.v[0][g] = fmaf(st.kick, a, vel[q]);  // dchi + coefv(i) * ddchi
+      } else if (KAHAN) {
         float k = kv[KAHAN ? q : 0];
         st.v[0][g] = kahan_add(vel[q], st.hdt * (acc[q] + a), k);
         st.cv[0][g] = k;
@@ -1231,6 +1255,18 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
       if (KAHAN && zero) st.cu[0][g] = 0.f;
     }
   }
+}
+
+// The final drift of a symplectic step (SOLVER/time_evol_wave.F90:722-727):
+// chi += dchi * coefd(nstages+1), disp += velo * coefd(nstages+1), on every
+// global point.
+__global__ void drift_kernel(StateArgs solid, StateArgs fluid, float cd) {
+  if (*solid.blowup) return;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < solid.nglob)
+    for (int c = 0; c < 3; ++c)
+      if (solid.u[c]) solid.u[c][q] = fmaf(cd, solid.v[c][q], solid.u[c][q]);
+  if (fluid.u[0] && q < fluid.nglob) fluid.u[0][q] = fmaf(cd, fluid.v[0][q], fluid.u[0][q]);
 }
 
 // ------------------------------------------------------------ coupling pre-passes

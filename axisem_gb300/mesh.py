@@ -315,6 +315,14 @@ def gvec_to_elemental(mesh: Mesh, g: np.ndarray, fluid: bool = False) -> np.ndar
     return out
 
 
+def gauss_at(t: np.ndarray, period: float) -> np.ndarray:
+    """The Gaussian source time function of gauss_stf at times t (FP64 in,
+    realkind out), for the stage times of a symplectic step
+    (compute_stf_t, SOLVER/source.f90:208-233)."""
+    decay, shift = 3.5, 1.5 * period
+    return np.exp(-((decay / period) * (np.asarray(t, np.float64) - shift)) ** 2).astype(F32)
+
+
 def gauss_stf(niter: int, deltat: float, period: float) -> np.ndarray:
     """Gaussian source time function sampled at t = iter * deltat (the
     reference's `gauss` STF shape, SOLVER/source.f90:587-600: exp(-(decay/period

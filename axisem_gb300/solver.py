@@ -34,6 +34,17 @@ def _fp(a):
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
+def symplectic_coefficients(scheme: int, deltat: float, lib=None):
+    """(coefd, coefv, coeff) of a symplectic scheme times deltat
+    (axg_symplectic_coefficients)."""
+    lib = lib or _abi.load_library()
+    a, b, c = (C.c_double * 40)(), (C.c_double * 40)(), (C.c_double * 40)()
+    n = C.c_int32()
+    _check(lib, None, lib.axg_symplectic_coefficients(scheme, deltat, a, b, c, C.byref(n)))
+    n = n.value
+    return np.array(a[: n + 1]), np.array(b[:n]), np.array(c[:n])
+
+
 class Solver:
     """One solve on one GPU (one axg_handle)."""
 
@@ -148,6 +159,19 @@ class Solver:
         ms = C.c_float()
         _check(self.lib, self.h, self.lib.axg_time_stiffness(self.h, n, C.byref(ms)))
         return ms.value
+
+    def set_time_scheme(self, scheme: int, stf_stages: np.ndarray | None = None):
+        """axg_set_time_scheme.  For a symplectic scheme without stf_stages,
+        the mesh's Gaussian stf (period 20 deltat, as the test meshes use) is
+        evaluated at the stage times t_(iter-1) + coeff(i)."""
+        if scheme != _abi.SCHEME_NEWMARK2 and stf_stages is None:
+            from .mesh import gauss_at
+            _, _, coeff = symplectic_coefficients(scheme, self.mesh.deltat, self.lib)
+            t = (np.arange(self.mesh.niter)[:, None] * self.mesh.deltat + coeff[None, :])
+            stf_stages = gauss_at(t, 20 * self.mesh.deltat)
+        ptr = None if stf_stages is None else _fp(np.asfortranarray(stf_stages, dtype=np.float32))
+        self._stf_stages = stf_stages
+        _check(self.lib, self.h, self.lib.axg_set_time_scheme(self.h, scheme, ptr))
 
     def set_compensated(self, on: bool = True):
         """Kahan-compensated predictor / corrector (axg_set_compensated)."""

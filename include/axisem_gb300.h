@@ -263,6 +263,34 @@ int axg_run_async(axg_handle *h, int32_t first_iter, int32_t n_iter);
 int axg_poll(axg_handle *h, int32_t *done);
 int axg_wait(axg_handle *h);
 
+/* Time schemes of the reference (time_scheme in inparam_advanced,
+ * SOLVER/time_evol_wave.F90:231-245, 516-967). */
+enum axg_scheme {
+  AXG_SCHEME_NEWMARK2 = 0,  /* the default */
+  AXG_SCHEME_SYMPLEC4,      /* 4th order PEFRL, 4 stages */
+  AXG_SCHEME_ML_SO4M5,      /* 4th order McLachlan, 5 stages */
+  AXG_SCHEME_ML_SO6M7,      /* 6th order McLachlan, 7 stages */
+  AXG_SCHEME_KL_O8M17,      /* 8th order Kahan-Li, 17 stages */
+  AXG_SCHEME_SS_35O10       /* 10th order Sofroniou-Spaletta, 35 stages */
+};
+
+/* The drift / kick coefficients of a symplectic scheme times deltat, as
+ * symplectic_coefficients computes them: coefd[0..nstages], coefv[0..nstages-1]
+ * and the stage times coeff[i] = sum(coefd[0..i]) (host only; arrays of at
+ * least 36 entries).  A caller evaluates its source time function at
+ * t_(iter-1) + coeff[i] for axg_set_time_scheme. */
+int axg_symplectic_coefficients(int32_t scheme, double deltat, double *coefd, double *coefv, double *coeff,
+                                int32_t *nstages);
+
+/* Selects the time scheme of the handle's time loop.  For a symplectic
+ * scheme, stf_stages(niter, nstages) (column-major) holds the source time
+ * function at the stage times of every step (compute_stf_t at
+ * t - deltat + coeff(i)); the Newmark scheme ignores it.  The symplectic
+ * schemes follow symplectic_time_loop; attenuation, the compensated mode, a
+ * fluid source and a fluid free surface are not supported with them here
+ * (AXG_ERR_UNSUPPORTED).  Resets the state. */
+int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages);
+
 /* Compensated time integration on (1) or off (0): the predictor
  * disp += dt velo + dt^2/2 acc0 and the corrector velo += dt/2 (acc0 + acc1)
  * (and chi, dchi in the fluid) use Kahan's compensated summation in FP32, with

@@ -24,6 +24,7 @@
  *   runtime_info blow-up check                              SOLVER/time_evol_wave.F90:1042-1054
  *   nc_compute_recfile_seis_bare                            SOLVER/seismograms.f90:783-820
  *   sf_time_loop_newmark                                    SOLVER/time_evol_wave.F90:264-502
+ *   symplectic_time_loop (elastic)                          SOLVER/time_evol_wave.F90:516-742
  *
  * Compiled twice: REAL=float (the reference's realkind=sp build) and
  * REAL=double (realkind=dp, the FP64 oracle).  Mixed-precision expressions
@@ -996,6 +997,123 @@ int ORC(time_loop)(const axg_mesh_desc *d, REAL *disp, REAL *velo, REAL *acc0, R
   }
   free(acc1);
   free(ddchi1);
+  return status;
+}
+
+/* symplectic_time_loop (SOLVER/time_evol_wave.F90:516-742) without
+ * attenuation: iterations first_iter..first_iter+n_iter-1 of an nstages
+ * scheme whose drifts coefd(1:nstages+1) and kicks coefv(1:nstages) are
+ * given times deltat; stf_stages(niter, nstages) holds the source time
+ * function at the stage times.  disp, velo (0:4,0:4,nel_solid,3), chi, dchi
+ * (0:4,0:4,nel_fluid) carry the state; seismograms as in time_loop. */
+int ORC(time_loop_symplectic)(const axg_mesh_desc *d, int32_t nstages, const double *coefd, const double *coefv,
+                              const float *stf_stages, REAL *disp, REAL *velo, REAL *chi, REAL *dchi,
+                              int32_t first_iter, int32_t n_iter, float *rec, int32_t nseismo_cap,
+                              int32_t *iseismo, int32_t *blowup_iter) {
+  const int64_t nes = d->nel_solid, cs = 25 * nes, nef = d->nel_fluid, cf = 25 * nef;
+  const int mono = d->src_type == AXG_MONOPOLE, di = d->src_type == AXG_DIPOLE;
+  REAL *acc = (REAL *)calloc((size_t)(3 * cs > 0 ? 3 * cs : 1), sizeof(REAL));
+  REAL *ddchi = (REAL *)calloc((size_t)(cf > 0 ? cf : 1), sizeof(REAL));
+  const double thresh = 10.0 * fabs(d->magnitude);
+  int status = 0;
+  for (int32_t iter = first_iter; iter < first_iter + n_iter; ++iter) {
+    REAL mx = 0;
+    for (int64_t e = 0; e < nes; ++e)
+      for (int c = 0; c < 3; ++c) {
+        REAL v = (REAL)fabs((double)disp[25 * e + 1 + 5 * 1 + cs * c]);
+        if (v > mx) mx = v;
+      }
+    if ((double)mx > thresh) {
+      if (blowup_iter) *blowup_iter = iter;
+      status = AXG_ERR_BLOWUP;
+      break;
+    }
+    for (int i = 0; i < nstages; ++i) {
+      for (int64_t p = 0; p < cf; ++p) chi[p] = (REAL)((double)chi[p] + (double)dchi[p] * coefd[i]);
+      for (int c = 0; c < 3; ++c) {
+        if (c == 1 && mono) continue;
+        for (int64_t p = 0; p < cs; ++p)
+          disp[p + cs * c] = (REAL)((double)disp[p + cs * c] + (double)velo[p + cs * c] * coefd[i]);
+      }
+      if (nef > 0) {
+        if (!mono) mask_fluid(d, chi);
+        ORC(stiffness_fluid)(d, chi, ddchi);
+        bdry_copy2fluid(d, ddchi, disp);
+        if (!mono) mask_fluid(d, ddchi);
+        ORC(pdistsum_fluid)(d, ddchi);
+      }
+      mask_solid(d, disp);
+      ORC(stiffness_solid)(d, disp, acc);
+      if (nef > 0) {
+        for (int64_t p = 0; p < cf; ++p) ddchi[p] = -ddchi[p] * (REAL)d->inv_mass_fluid[p];
+        if (d->have_absorbing_bc)
+          for (int64_t p = 0; p < cf; ++p) {
+            const REAL g = (REAL)d->fluid_absorbing_gamma[p];
+            ddchi[p] = ddchi[p] - 2 * g * dchi[p] - g * g * chi[p];
+          }
+        bdry_copy2solid(d, acc, ddchi);
+      }
+      mask_solid(d, acc);
+      ORC(pdistsum_solid)(d, acc, 3);
+      for (int64_t p = 0; p < cf; ++p) dchi[p] = (REAL)((double)dchi[p] + coefv[i] * (double)ddchi[p]);
+      const REAL stf1 = (REAL)stf_stages[(int64_t)(iter - 1) + (int64_t)d->niter * i];
+      if (stf1 != 0)
+        for (int k = 0; k < d->nelsrc; ++k) {
+          const int64_t e = d->ielsrc[k] - 1;
+          for (int c = 0; c < 3; ++c)
+            for (int q = 0; q < 25; ++q)
+              acc[25 * e + q + cs * c] = acc[25 * e + q + cs * c] - (REAL)d->source_term_el[q + 25 * k + 200 * c] * stf1;
+        }
+      const int order[3] = {0, 1, 2};
+      for (int oc = 0; oc < 3; ++oc) {
+        const int c = order[oc];
+        if (c == 1 && mono) continue;
+        for (int64_t p = 0; p < cs; ++p) {
+          const int64_t q = p + cs * c;
+          REAL a = -(REAL)d->inv_mass_rho[p] * acc[q];
+          if (d->have_absorbing_bc) {
+            const REAL g = (REAL)d->solid_absorbing_gamma[p];
+            a = a - 2 * g * velo[q] - g * g * disp[q];
+          }
+          acc[q] = a;
+          if (c == 2 && di)
+            velo[q] = (REAL)((double)velo[q] + 2.0 * (double)acc[q] * coefv[i]);
+          else
+            velo[q] = (REAL)((double)velo[q] + (double)acc[q] * coefv[i]);
+        }
+      }
+    }
+    for (int64_t p = 0; p < cf; ++p) chi[p] = (REAL)((double)chi[p] + (double)dchi[p] * coefd[nstages]);
+    for (int c = 0; c < 3; ++c) {
+      if (c == 1 && mono) continue;
+      for (int64_t p = 0; p < cs; ++p)
+        disp[p + cs * c] = (REAL)((double)disp[p + cs * c] + (double)velo[p + cs * c] * coefd[nstages]);
+    }
+    if (d->num_rec > 0 && rec && d->seis_it > 0 && iter % d->seis_it == 0) {
+      if (*iseismo < nseismo_cap) {
+        const int64_t n = nseismo_cap, is = *iseismo;
+        for (int r = 0; r < d->num_rec; ++r) {
+          const int64_t e = d->recfile_el[r] - 1;
+          const int ip = d->recfile_el[r + d->num_rec], jp = d->recfile_el[r + 2 * d->num_rec];
+          const int64_t p = 25 * e + ip + 5 * jp;
+          REAL v1, v2, v3;
+          if (mono) {
+            v1 = disp[p]; v2 = 0; v3 = disp[p + 2 * cs];
+          } else if (di) {
+            v1 = disp[p] + disp[p + cs]; v2 = disp[p] - disp[p + cs]; v3 = disp[p + 2 * cs];
+          } else {
+            v1 = disp[p]; v2 = disp[p + cs]; v3 = disp[p + 2 * cs];
+          }
+          rec[is + n * (0 + 3 * (int64_t)r)] = (float)v1;
+          rec[is + n * (1 + 3 * (int64_t)r)] = (float)v2;
+          rec[is + n * (2 + 3 * (int64_t)r)] = (float)v3;
+        }
+      }
+      *iseismo += 1;
+    }
+  }
+  free(acc);
+  free(ddchi);
   return status;
 }
 

@@ -107,5 +107,93 @@ class TimeLoop:
                   C.c_int32(n_iter), _p(self.rec, C.c_float), C.c_int32(self.nseismo),
                   C.byref(self.iseismo), C.byref(self.blowup_iter))
 
+    def run_symplectic(self, first_iter: int, n_iter: int, scheme: int, stf_stages: np.ndarray) -> int:
+        """symplectic_time_loop (elastic) for iterations first_iter..; the
+        scheme's coefficients are this module's restatement
+        (symplectic_coefficients), stf_stages (niter, nstages) the source time
+        function at the stage times."""
+        ct = self.ct
+        cd, cv, _ = symplectic_coefficients(scheme, self.mesh.deltat)
+        stf = np.asfortranarray(stf_stages, dtype=np.float32)
+        fn = getattr(lib(), f"orc_{self.tag}_time_loop_symplectic")
+        fn.restype = C.c_int
+        return fn(C.byref(self.d), C.c_int32(len(cv)), _p(cd, C.c_double), _p(cv, C.c_double),
+                  _p(stf, C.c_float), _p(self.disp, ct), _p(self.velo, ct), _p(self.chi, ct), _p(self.dchi, ct),
+                  C.c_int32(first_iter), C.c_int32(n_iter), _p(self.rec, C.c_float), C.c_int32(self.nseismo),
+                  C.byref(self.iseismo), C.byref(self.blowup_iter))
+
     def receivers(self) -> np.ndarray:
         return self.rec[:, :, : self.mesh.num_rec]
+
+
+def _sp(x: float) -> float:
+    """A Fortran literal without kind suffix: a single-precision value."""
+    return float(np.float32(x))
+
+
+def _ss_scheme(g):
+    """SS_scheme (SOLVER/time_evol_wave.F90:972-992) as Fortran evaluates it:
+    its middle drift 1 / 2 - sum(a(1:n)) has the integer quotient 1 / 2 = 0."""
+    n = len(g)
+    a = [0.0] * (2 * n + 2)
+    b = [0.0] * (2 * n + 1)
+    a[0] = g[0] / 2.0
+    for i in range(1, n):
+        a[i] = (g[i - 1] + g[i]) / 2.0
+    sa = 0.0
+    for i in range(n):
+        sa += a[i]
+    a[n] = 0 - sa
+    for i in range(n + 1, 2 * n + 2):
+        a[i] = a[2 * n + 1 - i]
+    sg = 0.0
+    for i in range(n):
+        b[i] = g[i]
+        sg += g[i]
+    b[n] = 1.0 - 2.0 * sg
+    for i in range(n + 1, 2 * n + 1):
+        b[i] = b[2 * n - i]
+    return a, b
+
+
+def symplectic_coefficients(scheme: int, deltat: float):
+    """symplectic_coefficients (SOLVER/time_evol_wave.F90:749-967): drifts
+    coefd(1:n+1), kicks coefv(1:n) times deltat and the stage times coeff."""
+    if scheme == 1:    # symplec4, PEFRL
+        zeta, iota, kappa = _sp(+0.1786178958448091), _sp(-0.2123418310626054), _sp(-0.06626458266981849)
+        cd = [zeta, kappa, 1.0 - 2.0 * (zeta + kappa), kappa, zeta]
+        cv = [0.5 - iota, iota, iota, 0.5 - iota]
+    elif scheme == 2:  # ML_SO4m5
+        rho = (14.0 - np.sqrt(19.0)) / 108.0
+        theta = (20.0 - 7.0 * np.sqrt(19.0)) / 108.0
+        nu, lam = 2.0 / 5.0, -1.0 / 10.0
+        cd = [rho, theta, 0.5 - rho - theta, 0.5 - rho - theta, theta, rho]
+        cv = [nu, lam, 1.0 - 2.0 * (nu + lam), lam, nu]
+    elif scheme == 3:  # ML_SO6m7
+        d = [_sp(x) for x in (-1.01308797891717472981, 1.18742957373254270702, -0.01833585209646059034,
+                              0.34399425728109261313)]
+        v = [_sp(x) for x in (0.00016600692650009894, -0.37962421426377360608, 0.68913741185181063674,
+                              0.38064159097092574080)]
+        cd = d + d[::-1]
+        cv = v + v[2::-1]
+    elif scheme == 4:  # KL_O8m17
+        cd, cv = _ss_scheme([_sp(x) for x in (
+            0.13020248308889008088, 0.56116298177510838456, -0.38947496264484728641, 0.15884190655515560090,
+            -0.39590389413323757734, 0.18453964097831570709, 0.25837438768632204729, 0.29501172360931029887)])
+    elif scheme == 5:  # SS_35o10
+        cd, cv = _ss_scheme([_sp(x) for x in (
+            0.078795722521686419263907679337684, 0.31309610341510852776481247192647,
+            0.027918383235078066109520273275299, -0.22959284159390709415121339679655,
+            0.13096206107716486317465685927961, -0.26973340565451071434460973222411,
+            0.074973343155891435666137105641410, 0.11199342399981020488957508073640,
+            0.36613344954622675119314812353150, -0.39910563013603589787862981058340,
+            0.10308739852747107731580277001372, 0.41143087395589023782070411897608,
+            -0.0048663605831352617621956593099771, -0.39203335370863990644808193642610,
+            0.051942502962449647037182904015976, 0.050665090759924496335874344156866,
+            0.049674370639729879054568800279461)])
+    else:
+        raise ValueError(f"unknown symplectic scheme {scheme}")
+    cd = np.array(cd, dtype=np.float64) * deltat
+    cv = np.array(cv, dtype=np.float64) * deltat
+    coeff = np.cumsum(cd[:-1])
+    return cd, cv, coeff
