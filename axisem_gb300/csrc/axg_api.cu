@@ -99,6 +99,8 @@ struct axg_handle {
   int32_t niter = 0, seis_it = 1, num_rec = 0, nseismo = 0;
   bool absorbing = false;
   double dt = 0, magnitude = 0;
+  // igloc in the plans' internal point numbering (DomainPlan::new_of_old):
+  // every per-point table and device array of the handle uses it
   std::vector<int32_t> igloc_s, igloc_f, rec_gidx;
   std::vector<uint8_t> pre_s, pre_f;
   DomainPlan ps, pf;
@@ -119,6 +121,12 @@ struct axg_handle {
   int32_t *src_gidx_d = nullptr;
   float *src_val_d = nullptr;
   int32_t n_src = 0;
+  // gvec I/O in the reference's numbering (made on first use): the solid
+  // plan's new_of_old, a 3-component staging buffer, a copy stream
+  int32_t *gvec_perm = nullptr;
+  float *gvec_stage = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_io[5] = {};
   Coupling to_fluid{}, to_solid{};
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
@@ -727,6 +735,12 @@ void release(axg_handle *h) {
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->ev_done) cudaEventDestroy(h->ev_done);
+  for (cudaEvent_t e : h->ev_io)
+    if (e) cudaEventDestroy(e);
+  if (h->copy_stream) {
+    cudaStreamSynchronize(h->copy_stream);
+    cudaStreamDestroy(h->copy_stream);
+  }
   for (void *p : h->allocs) cudaFreeAsync(p, h->stream);
   if (h->stream) cudaStreamDestroy(h->stream);
   h->allocs.clear();
@@ -847,11 +861,11 @@ int symplectic_coefficients(int scheme, std::vector<double> &cd, std::vector<dou
 
 // tuned (or requested) patch shape, then the plan
 std::string plan_domain(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
-                        const std::vector<uint8_t> &prepass, DomainPlan &plan) {
+                        const std::vector<uint8_t> &prepass, DomainPlan &plan, bool renumber = true) {
   int pe = patch_elems, gr = growth;
   std::string e = tune_plan(igloc, nel, nglob, patch_elems, growth, &pe, &gr);
   if (!e.empty()) return e;
-  return build_plan(igloc, nel, nglob, pe, gr, prepass, plan);
+  return build_plan(igloc, nel, nglob, pe, gr, prepass, plan, renumber);
 }
 
 int check_igloc(const int32_t *ig, int64_t n, int64_t nglob, const char *what) {
@@ -971,8 +985,15 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
         share->nglob_s != h->nglob_s || share->nglob_f != h->nglob_f || share->absorbing != h->absorbing ||
         share->anel != h->anel || (h->anel && share->nsls != d->n_sls))
       return fail(h, AXG_ERR_BAD_DESC, "axg_create_sharing: the descriptor is not of the handle's mesh");
-    if (std::memcmp(share->igloc_s.data(), d->igloc_solid, 25 * h->nel_s * sizeof(int32_t)) != 0 ||
-        (h->nel_f > 0 && std::memcmp(share->igloc_f.data(), d->igloc_fluid, 25 * h->nel_f * sizeof(int32_t)) != 0))
+    // (the handle holds igloc in its internal numbering)
+    auto same = [](const std::vector<int32_t> &mine, const int32_t *ig, int64_t n, int64_t nglob,
+                   const std::vector<int32_t> &nofo) {
+      for (int64_t p = 0; p < n; ++p)
+        if (ig[p] < 1 || ig[p] > nglob || mine[p] != nofo[ig[p] - 1] + 1) return false;
+      return true;
+    };
+    if (!same(share->igloc_s, d->igloc_solid, 25 * h->nel_s, h->nglob_s, share->ps.new_of_old) ||
+        (h->nel_f > 0 && !same(share->igloc_f, d->igloc_fluid, 25 * h->nel_f, h->nglob_f, share->pf.new_of_old)))
       return fail(h, AXG_ERR_BAD_DESC, "axg_create_sharing: the global numbering differs from the handle's mesh");
     h->igloc_s = share->igloc_s;
     h->igloc_f = share->igloc_f;
@@ -1028,6 +1049,13 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
     perr = validate_plan(h->igloc_s.data(), h->nel_s, h->nglob_s, h->pre_s, h->ps);
     if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "solid plan invalid: " + perr);
 #endif
+    // from here on points carry the plans' internal numbers
+    for (int32_t &g : h->igloc_s) g = h->ps.new_of_old[g - 1] + 1;
+    for (int32_t &g : h->igloc_f) g = h->pf.new_of_old[g - 1] + 1;
+    for (int32_t &g : cs.pt_gidx) g = h->ps.new_of_old[g];
+    for (int32_t &g : cs.src_gidx) g = h->pf.new_of_old[g];
+    for (int32_t &g : cf.pt_gidx) g = h->pf.new_of_old[g];
+    for (int32_t &g : cf.src_gidx) g = h->ps.new_of_old[g];
   }
 
   // receivers and the solid source table
@@ -1229,7 +1257,7 @@ extern "C" int axg_stiffness_assembled_noalloc(const axg_mesh_desc *d, const flo
   const int pole = d->src_type;
   const int64_t nel = d->nel_solid, nglob = d->nglob_solid;
   DomainPlan pl;
-  std::string perr = plan_domain(d->igloc_solid, nel, nglob, 0, -1, std::vector<uint8_t>(), pl);
+  std::string perr = plan_domain(d->igloc_solid, nel, nglob, 0, -1, std::vector<uint8_t>(), pl, false);
   if (!perr.empty()) return fail(nullptr, AXG_ERR_BAD_DESC, "solid plan: " + perr);
   const std::vector<int> slots = solid_slots(pole), aslots = axial_slots(pole);
   const int nt = (int)slots.size(), na = (int)aslots.size();
@@ -1486,6 +1514,52 @@ int check_flags(axg_handle *h) {
                 fmt("displacements blew up: |disp(1,1,:,:)| > 10 |magnitude| at time step %d", flags[0] + 1));
   return AXG_OK;
 }
+
+// The gvec I/O (axg_upload_gvec_disp / axg_download_gvec_force) is in the
+// reference's point numbering, the handle's arrays in the plan's.  The host
+// copies go through a staging buffer in chunks of points on a copy stream;
+// a permutation kernel on the handle's stream moves each chunk as soon as it
+// has landed (uploads) or before it leaves (downloads), so that copies and
+// permutations overlap.
+constexpr int kGvecChunks = 4;
+static_assert(sizeof(axg_handle::ev_io) / sizeof(cudaEvent_t) == kGvecChunks + 1, "one event per chunk + one");
+
+// u[c][new_of_old[g]] = stage[c][g], g in [a, b)
+__global__ void gvec_to_internal_kernel(const float *__restrict__ stage, const int32_t *__restrict__ new_of_old,
+                                        int64_t n, int64_t a, int64_t b, float *u0, float *u1, float *u2) {
+  for (int64_t g = a + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < b; g += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t t = new_of_old[g];
+    if (u0) u0[t] = stage[g];
+    if (u1) u1[t] = stage[n + g];
+    if (u2) u2[t] = stage[2 * n + g];
+  }
+}
+
+// stage[c][g] = f[c][new_of_old[g]], g in [a, b)
+__global__ void gvec_from_internal_kernel(const float *__restrict__ f0, const float *__restrict__ f1,
+                                          const float *__restrict__ f2, const int32_t *__restrict__ new_of_old,
+                                          int64_t n, int64_t a, int64_t b, float *stage) {
+  for (int64_t g = a + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < b; g += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t t = new_of_old[g];
+    if (f0) stage[g] = f0[t];
+    if (f1) stage[n + g] = f1[t];
+    if (f2) stage[2 * n + g] = f2[t];
+  }
+}
+
+unsigned gvec_grid(const axg_handle *h, int64_t n) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * (int64_t)h->num_sms));
+}
+
+int gvec_io_prepare(axg_handle *h) {
+  if (h->gvec_perm) return AXG_OK;
+  int rc;
+  if ((rc = upload(h, &h->gvec_perm, h->ps.new_of_old))) return rc;
+  if ((rc = dalloc(h, &h->gvec_stage, 3 * (size_t)h->nglob_s))) return rc;
+  CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  for (cudaEvent_t &e : h->ev_io) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return AXG_OK;
+}
 }  // namespace
 
 extern "C" {
@@ -1603,23 +1677,47 @@ int axg_set_state(axg_handle *h, int32_t field, const float *in) {
 
 int axg_upload_gvec_disp(axg_handle *h, const float *u) {
   if (!h || !u) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
-  for (int c = 0; c < 3; ++c)
-    if (h->su[c])
-      CK(cudaMemcpyAsync(h->su[c], u + h->nglob_s * c, h->nglob_s * sizeof(float), cudaMemcpyHostToDevice,
-                         h->stream));
+  int rc = gvec_io_prepare(h);
+  if (rc) return rc;
+  const int64_t n = h->nglob_s;
+  // the staging buffer is free once the work queued so far has run
+  CK(cudaEventRecord(h->ev_io[kGvecChunks], h->stream));
+  CK(cudaStreamWaitEvent(h->copy_stream, h->ev_io[kGvecChunks], 0));
+  for (int k = 0; k < kGvecChunks; ++k) {
+    const int64_t a = n * k / kGvecChunks, b = n * (k + 1) / kGvecChunks;
+    for (int c = 0; c < 3; ++c)
+      if (h->su[c])
+        CK(cudaMemcpyAsync(h->gvec_stage + n * c + a, u + n * c + a, (b - a) * sizeof(float),
+                           cudaMemcpyHostToDevice, h->copy_stream));
+    CK(cudaEventRecord(h->ev_io[k], h->copy_stream));
+    CK(cudaStreamWaitEvent(h->stream, h->ev_io[k], 0));
+    gvec_to_internal_kernel<<<gvec_grid(h, b - a), 256, 0, h->stream>>>(h->gvec_stage, h->gvec_perm, n, a, b,
+                                                                         h->su[0], h->su[1], h->su[2]);
+    CK(cudaGetLastError());
+  }
   return AXG_OK;
 }
 
 int axg_download_gvec_force(axg_handle *h, float *f) {
   if (!h || !f) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
-  for (int c = 0; c < 3; ++c) {
-    if (h->sf[c])
-      CK(cudaMemcpyAsync(f + h->nglob_s * c, h->sf[c], h->nglob_s * sizeof(float), cudaMemcpyDeviceToHost,
-                         h->stream));
-    else
-      std::memset(f + h->nglob_s * c, 0, h->nglob_s * sizeof(float));
+  int rc = gvec_io_prepare(h);
+  if (rc) return rc;
+  const int64_t n = h->nglob_s;
+  for (int k = 0; k < kGvecChunks; ++k) {
+    const int64_t a = n * k / kGvecChunks, b = n * (k + 1) / kGvecChunks;
+    gvec_from_internal_kernel<<<gvec_grid(h, b - a), 256, 0, h->stream>>>(h->sf[0], h->sf[1], h->sf[2],
+                                                                           h->gvec_perm, n, a, b, h->gvec_stage);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev_io[k], h->stream));
+    CK(cudaStreamWaitEvent(h->copy_stream, h->ev_io[k], 0));
+    for (int c = 0; c < 3; ++c)
+      if (h->sf[c])
+        CK(cudaMemcpyAsync(f + n * c + a, h->gvec_stage + n * c + a, (b - a) * sizeof(float),
+                           cudaMemcpyDeviceToHost, h->copy_stream));
   }
-  CK(cudaStreamSynchronize(h->stream));
+  for (int c = 0; c < 3; ++c)
+    if (!h->sf[c]) std::memset(f + n * c, 0, n * sizeof(float));
+  CK(cudaStreamSynchronize(h->copy_stream));
   return AXG_OK;
 }
 

@@ -42,7 +42,7 @@ PointElems point_elements(const int32_t *igloc, int64_t nel, int64_t nglob) {
 }  // namespace
 
 std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
-                       const std::vector<uint8_t> &prepass, DomainPlan &plan) {
+                       const std::vector<uint8_t> &prepass, DomainPlan &plan, bool renumber) {
   plan = DomainPlan();
   plan.nel = nel;
   plan.nglob = nglob;
@@ -281,6 +281,49 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
   for (int32_t p = 0; p < plan.n_patches; ++p) plan.colour_start[plan.colour_of_patch[p] + 1]++;
   for (int32_t c = 0; c < ncol; ++c) plan.colour_start[c + 1] += plan.colour_start[c];
 
+  // ---- 2b. internal point numbering --------------------------------------
+  // Points held by the same patches get consecutive numbers: grouped by the
+  // first and second patch (in launch order) that hold them, in reference
+  // order inside a group.  A patch's interior is then one run, each edge it
+  // shares with a later patch another, so that gathers and write-backs read
+  // and write whole sectors instead of rows scattered over the reference's
+  // numbering.
+  plan.new_of_old.resize(nglob);
+  plan.old_of_new.resize(nglob);
+  if (!renumber) {
+    std::iota(plan.new_of_old.begin(), plan.new_of_old.end(), 0);
+    std::iota(plan.old_of_new.begin(), plan.old_of_new.end(), 0);
+  } else {
+    std::vector<int32_t> rank(plan.n_patches);
+    for (int32_t lp = 0; lp < plan.n_patches; ++lp) rank[order[lp]] = lp;
+    const int32_t none = plan.n_patches;  // points no element holds come last
+    std::vector<int32_t> r0(nglob, none), r1(nglob, none);
+    for (int64_t e = 0; e < nel; ++e) {
+      const int32_t p = rank[plan.patch_of_elem[e]];
+      for (int k = 0; k < 25; ++k) {
+        const int64_t g = igloc[25 * e + k] - 1;
+        if (p == r0[g] || p == r1[g]) continue;
+        if (p < r0[g]) {
+          r1[g] = r0[g];
+          r0[g] = p;
+        } else if (p < r1[g]) {
+          r1[g] = p;
+        }
+      }
+    }
+    // counting sort by the first patch, then by the second inside a bucket
+    std::vector<int64_t> start(plan.n_patches + 2, 0);
+    for (int64_t g = 0; g < nglob; ++g) start[r0[g] + 1]++;
+    for (int32_t p = 0; p <= plan.n_patches; ++p) start[p + 1] += start[p];
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    for (int64_t g = 0; g < nglob; ++g) plan.old_of_new[fill[r0[g]]++] = (int32_t)g;
+    for (int32_t p = 0; p <= plan.n_patches; ++p)
+      std::stable_sort(plan.old_of_new.begin() + start[p], plan.old_of_new.begin() + start[p + 1],
+                       [&](int32_t a, int32_t b) { return r1[a] < r1[b]; });
+    for (int64_t n = 0; n < nglob; ++n) plan.new_of_old[plan.old_of_new[n]] = (int32_t)n;
+  }
+  const std::vector<int32_t> &nofo = plan.new_of_old;
+
   // ---- 3. first / last writer per point ----------------------------------
   // colour range of the patches touching each point
   std::vector<int32_t> cmin(nglob, INT32_MAX), cmax(nglob, -1);
@@ -347,18 +390,19 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
       m.round_end[r] = (uint8_t)cnt;
     }
     plan.max_rounds = std::max(plan.max_rounds, nrounds);
-    // unique points, sorted by global index
+    // unique points, sorted by internal number
     pts.clear();
     for (int a = 0; a < n; ++a)
-      for (int k = 0; k < 25; ++k) pts.push_back((uint32_t)(igloc[25 * (int64_t)mem[a] + k] - 1));
+      for (int k = 0; k < 25; ++k) pts.push_back((uint32_t)nofo[igloc[25 * (int64_t)mem[a] + k] - 1]);
     std::sort(pts.begin(), pts.end());
     pts.erase(std::unique(pts.begin(), pts.end()), pts.end());
     if (pts.size() > (size_t)kMaxPatchPoints) return "patch has too many points";
     m.n_pts = (uint16_t)pts.size();
     plan.max_pts = std::max<int32_t>(plan.max_pts, (int32_t)pts.size());
     const int32_t col = plan.colour_of_patch[p];
-    for (uint32_t g : pts) {
-      uint32_t w = g;
+    for (uint32_t gn : pts) {
+      uint32_t w = gn;
+      const int64_t g = plan.old_of_new[gn];
       const bool pre = !prepass.empty() && prepass[g];
       if (cmin[g] == col && !pre) w |= kPtFirst;
       if (cmax[g] == col) w |= kPtLast;
@@ -371,7 +415,7 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
       const int32_t e = mem[a];
       plan.elem_order[eslot] = e;
       for (int k = 0; k < 25; ++k) {
-        const uint32_t g = (uint32_t)(igloc[25 * (int64_t)e + k] - 1);
+        const uint32_t g = (uint32_t)nofo[igloc[25 * (int64_t)e + k] - 1];
         const auto it = std::lower_bound(pts.begin(), pts.end(), g);
         plan.elem_pts[25 * eslot + k] = (uint16_t)(it - pts.begin());
       }
@@ -391,6 +435,13 @@ std::string validate_plan(const int32_t *igloc, int64_t nel, int64_t nglob,
     const int32_t e = plan.elem_order[s];
     if (e < 0 || e >= nel) return "elem_order out of range";
     if (seen[e]++) return "element appears twice in launch order";
+  }
+  // the internal numbering is a permutation
+  if ((int64_t)plan.new_of_old.size() != nglob || (int64_t)plan.old_of_new.size() != nglob)
+    return "point numbering size";
+  for (int64_t g = 0; g < nglob; ++g) {
+    const int32_t n = plan.new_of_old[g];
+    if (n < 0 || n >= nglob || plan.old_of_new[n] != g) return "point numbering is not a permutation";
   }
   // same-colour patches must not share a point; same-round elements neither
   std::vector<int32_t> owner_patch(nglob, -1), owner_colour(nglob, -1);
@@ -424,7 +475,7 @@ std::string validate_plan(const int32_t *igloc, int64_t nel, int64_t nglob,
           for (int k = 0; k < 25; ++k) {
             const uint16_t li = plan.elem_pts[25 * (int64_t)(m.elem_start + s) + k];
             if (li >= m.n_pts) return "element point index outside patch";
-            if ((int64_t)(plan.pt_words[m.pt_start + li] & kPtIndexMask) != igloc[25 * (int64_t)e + k] - 1)
+            if ((int64_t)(plan.pt_words[m.pt_start + li] & kPtIndexMask) != plan.new_of_old[igloc[25 * (int64_t)e + k] - 1])
               return "element point index maps to the wrong global point";
           }
         }
@@ -436,9 +487,9 @@ std::string validate_plan(const int32_t *igloc, int64_t nel, int64_t nglob,
       if (r0 != m.n_elems) return "sub-round counts do not cover the patch";
     }
   }
-  for (int64_t g = 0; g < nglob; ++g) {
+  for (int64_t g = 0; g < nglob; ++g) {  // g: internal number
     if (ntouch[g] == 0) continue;
-    const bool pre = !prepass.empty() && prepass[g];
+    const bool pre = !prepass.empty() && prepass[plan.old_of_new[g]];
     if (nlast[g] != 1) return "point without exactly one last writer";
     if (nfirst[g] != (pre ? 0 : 1)) return "point first-writer count wrong";
   }
@@ -487,7 +538,7 @@ std::string tune_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patc
   for (int pe : sizes)
     for (int gr : growths) {
       DomainPlan pl;
-      std::string e = build_plan(ig.data(), n, (int64_t)ids.size(), pe, gr, std::vector<uint8_t>(), pl);
+      std::string e = build_plan(ig.data(), n, (int64_t)ids.size(), pe, gr, std::vector<uint8_t>(), pl, false);
       if (!e.empty()) continue;
       const double c = (double)plan_cost(pl);
       if (best < 0 || c < best) {

@@ -63,6 +63,9 @@ struct DomainPlan {
   std::vector<PatchMeta> meta;           // n_patches, launch order
   std::vector<int32_t> elem_order;       // nel: reference element (0-based) at each launch slot
   std::vector<uint32_t> pt_words;        // patch point words, each patch padded to a multiple of 4
+  // internal point numbering: the point words and every per-point device
+  // array use new_of_old[g] for the reference's (0-based) point g
+  std::vector<int32_t> new_of_old, old_of_new;
   std::vector<uint16_t> elem_pts;        // 25*nel, launch order: patch-local point index
   int64_t total_pts = 0;
 };
@@ -75,8 +78,10 @@ struct DomainPlan {
 //   prepass   : per global point, 1 if a pre-pass kernel writes it first
 //               (solid-fluid coupling), may be empty
 // Returns an empty string on success, else the reason.
+// renumber: give points an internal numbering in which the points held by
+// the same patches are contiguous (else the identity).
 std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
-                       const std::vector<uint8_t> &prepass, DomainPlan &plan);
+                       const std::vector<uint8_t> &prepass, DomainPlan &plan, bool renumber = true);
 
 // Model cost of a plan in 1/256 warp iterations of the patch kernels.
 int64_t plan_cost(const DomainPlan &plan);
