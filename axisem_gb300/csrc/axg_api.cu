@@ -1520,7 +1520,10 @@ int check_flags(axg_handle *h) {
 // copies go through a staging buffer in chunks of points on a copy stream;
 // a permutation kernel on the handle's stream moves each chunk as soon as it
 // has landed (uploads) or before it leaves (downloads), so that copies and
-// permutations overlap.
+// permutations overlap.  (Letting the permutation kernel read and write a
+// pinned host buffer directly over the CPU-GPU link was slower on GB300:
+// 3.21 against 2.95 ms for a 1024 x 1024 quadrupole step, the copy engines
+// moving ~200 GB/s each way; 8 or 16 chunks gained nothing over 4.)
 constexpr int kGvecChunks = 4;
 static_assert(sizeof(axg_handle::ev_io) / sizeof(cudaEvent_t) == kGvecChunks + 1, "one event per chunk + one");
 
@@ -1551,6 +1554,7 @@ unsigned gvec_grid(const axg_handle *h, int64_t n) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * (int64_t)h->num_sms));
 }
 
+// the permutation, staging buffer, copy stream and events, on first use
 int gvec_io_prepare(axg_handle *h) {
   if (h->gvec_perm) return AXG_OK;
   int rc;

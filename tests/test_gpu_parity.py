@@ -40,6 +40,36 @@ def test_stiffness_assembled_parity(gpu_lib, orc, pole, axial):
         assert not f[:, 1].any()
 
 
+@pytest.mark.parametrize("pole", [0, 2])
+def test_gvec_io_pinned_and_pageable(gpu_lib, orc, pole):
+    """The gvec I/O is in the reference's numbering (the device arrays are
+    in the plan's): pinned and pageable host buffers, and uploads and
+    downloads mixed with device-side stiffness calls, give one result."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    m = structured_mesh(37, 29, pole, seed=300 + pole)
+    u = random_gvec(m, seed=9)
+    ng = m.nglob_solid
+    hu = torch.empty((3, ng), dtype=torch.float32, pin_memory=True).numpy()
+    hf = torch.full((3, ng), np.nan, dtype=torch.float32, pin_memory=True).numpy()
+    hu[:] = u.T
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    with Solver(m) as s:
+        f_pageable = s.stiffness_assembled(u)
+        assert s.lib.axg_stiffness_assembled(s.h, fp(hu), fp(hf)) == 0
+        f_pinned = hf.T.copy()
+        s.upload_disp(u)                        # staged upload, pinned download
+        s.stiffness_device()
+        assert s.lib.axg_download_gvec_force(s.h, fp(hf)) == 0
+        f_mixed = hf.T.copy()
+        assert s.lib.axg_upload_gvec_disp(s.h, fp(hu)) == 0   # pinned upload, staged download
+        s.stiffness_device()
+        f_mixed2 = s.download_force()
+    assert np.array_equal(f_pinned, f_pageable)
+    assert np.array_equal(f_mixed, f_pageable) and np.array_equal(f_mixed2, f_pageable)
+    assert rel(f_pageable, orc.stiffness_assembled(m, u, np.float64)) < 1e-5
+
+
 def test_stiffness_golden_fixture(gpu_lib, orc):
     from pathlib import Path
     gold = np.load(Path(__file__).resolve().parent / "golden" / "oracle_golden.npz")
