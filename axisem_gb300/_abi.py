@@ -150,6 +150,13 @@ SIGNATURES = {
     "axg_run_async": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "axg_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "axg_wait": (C.c_int, [C.c_void_p]),
+    "axg_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
+    "axg_batch_run_async": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32]),
+    "axg_batch_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "axg_batch_wait": (C.c_int, [C.c_void_p]),
+    "axg_batch_launches_per_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "axg_batch_destroy": (None, [C.c_void_p]),
+    "axg_batch_last_error": (C.c_char_p, [C.c_void_p]),
     "axg_reset": (C.c_int, [C.c_void_p]),
     "axg_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "axg_get_receivers": (C.c_int, [C.c_void_p, _fp, C.c_int32, _ip]),

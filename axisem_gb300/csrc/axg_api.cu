@@ -511,6 +511,10 @@ StateArgs fluid_state(axg_handle *h) {
   return s;
 }
 
+RecWork rec_work(axg_handle *h, const StateArgs &ss) {
+  return RecWork{ss, h->rec_gidx_d, h->num_rec, h->seis_it, h->pole, h->nseismo, h->rec, h->iter};
+}
+
 DomainArgs domain_args(const DomainDev &dd, const DomainPlan &pl) {
   DomainArgs a{};
   a.n_patches = pl.n_patches;
@@ -536,10 +540,8 @@ constexpr int solid_smem_bytes() {
 }
 
 // sets the kernel's shared-memory attributes; *ctas = resident CTAs on the GPU
-template <int POLE, int MODE, bool ANEL, bool KAHAN>
-int prepare_solid_kernel(axg_handle *h, int *ctas) {
-  auto fn = solid_patch_kernel<POLE, MODE, ANEL, KAHAN>;
-  constexpr int bytes = solid_smem_bytes<POLE, MODE, ANEL, KAHAN>();
+template <class F>
+int prepare_kernel_fn(axg_handle *h, F fn, int bytes, int *ctas) {
   CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   CK(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   int per_sm = 0;
@@ -547,6 +549,12 @@ int prepare_solid_kernel(axg_handle *h, int *ctas) {
   if (per_sm < 1) return fail(h, AXG_ERR_CUDA, "solid kernel does not fit on an SM");
   *ctas = per_sm * h->num_sms;
   return AXG_OK;
+}
+
+template <int POLE, int MODE, bool ANEL, bool KAHAN>
+int prepare_solid_kernel(axg_handle *h, int *ctas) {
+  return prepare_kernel_fn(h, solid_patch_kernel<POLE, MODE, ANEL, KAHAN>,
+                           solid_smem_bytes<POLE, MODE, ANEL, KAHAN>(), ctas);
 }
 
 // the stiffness kernel and the Newmark kernel the handle's modes select
@@ -631,31 +639,33 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
   if (h->nel_f > 0) {
     if (h->to_fluid.n > 0) {
       const int nb = (h->to_fluid.n + 255) / 256;
-      if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(h->to_fluid, ss, h->ff);
-      else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(h->to_fluid, ss, h->ff);
+      const One<ToFluidWork> w{{h->to_fluid, ss, h->ff}, h->to_fluid.n};
+      if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(w);
+      else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(w);
     }
     DomainArgs a = domain_args(h->df, h->pf);
     for (int c = 0; c < h->pf.n_colours; ++c) {
       a.patch_begin = h->pf.colour_start[c];
       const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
+      const One<PatchWork> w{{a, fs}, n};
       if (h->pole == AXG_MONOPOLE) {
-        if (h->kahan) fluid_patch_kernel<0, true><<<n, kThreads, 0, s>>>(a, fs, h->spec);
-        else fluid_patch_kernel<0, false><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+        if (h->kahan) fluid_patch_kernel<0, true><<<n, kThreads, 0, s>>>(w, h->spec);
+        else fluid_patch_kernel<0, false><<<n, kThreads, 0, s>>>(w, h->spec);
       } else {
-        if (h->kahan) fluid_patch_kernel<1, true><<<n, kThreads, 0, s>>>(a, fs, h->spec);
-        else fluid_patch_kernel<1, false><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+        if (h->kahan) fluid_patch_kernel<1, true><<<n, kThreads, 0, s>>>(w, h->spec);
+        else fluid_patch_kernel<1, false><<<n, kThreads, 0, s>>>(w, h->spec);
       }
     }
     if (h->to_solid.n > 0) {
       const int nb = (h->to_solid.n + 255) / 256;
-      if (h->pole == AXG_MONOPOLE) couple_to_solid_kernel<POLE_MONO><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
-      else if (h->pole == AXG_DIPOLE) couple_to_solid_kernel<POLE_DI><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
-      else couple_to_solid_kernel<POLE_QUAD><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
+      const One<ToSolidWork> w{{h->to_solid, fs, ss}, h->to_solid.n};
+      if (h->pole == AXG_MONOPOLE) couple_to_solid_kernel<POLE_MONO><<<nb, 256, 0, s>>>(w);
+      else if (h->pole == AXG_DIPOLE) couple_to_solid_kernel<POLE_DI><<<nb, 256, 0, s>>>(w);
+      else couple_to_solid_kernel<POLE_QUAD><<<nb, 256, 0, s>>>(w);
     }
   }
   launch_solid<MODE_NEWMARK>(h, s);
-  receivers_kernel<<<1, 256, 0, s>>>(ss, h->rec_gidx_d, h->num_rec, h->seis_it, h->pole, h->rec, h->nseismo,
-                                     h->iter);
+  receivers_kernel<<<1, 256, 0, s>>>(One<RecWork>{rec_work(h, ss), 1});
 }
 
 // One step of symplectic_time_loop (SOLVER/time_evol_wave.F90:587-727):
@@ -684,22 +694,25 @@ void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
     if (h->nel_f > 0) {
       if (h->to_fluid.n > 0) {
         const int nb = (h->to_fluid.n + 255) / 256;
-        if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(h->to_fluid, ss, h->ff);
-        else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(h->to_fluid, ss, h->ff);
+        const One<ToFluidWork> w{{h->to_fluid, ss, h->ff}, h->to_fluid.n};
+        if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(w);
+        else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(w);
       }
       DomainArgs a = domain_args(h->df, h->pf);
       a.fsmask = nullptr;  // symplectic_time_loop applies no free-surface mask
       for (int c = 0; c < h->pf.n_colours; ++c) {
         a.patch_begin = h->pf.colour_start[c];
         const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
-        if (h->pole == AXG_MONOPOLE) fluid_patch_kernel<0, false, true><<<n, kThreads, 0, s>>>(a, fs, h->spec);
-        else fluid_patch_kernel<1, false, true><<<n, kThreads, 0, s>>>(a, fs, h->spec);
+        const One<PatchWork> w{{a, fs}, n};
+        if (h->pole == AXG_MONOPOLE) fluid_patch_kernel<0, false, true><<<n, kThreads, 0, s>>>(w, h->spec);
+        else fluid_patch_kernel<1, false, true><<<n, kThreads, 0, s>>>(w, h->spec);
       }
       if (h->to_solid.n > 0) {
         const int nb = (h->to_solid.n + 255) / 256;
-        if (h->pole == AXG_MONOPOLE) couple_to_solid_kernel<POLE_MONO><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
-        else if (h->pole == AXG_DIPOLE) couple_to_solid_kernel<POLE_DI><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
-        else couple_to_solid_kernel<POLE_QUAD><<<nb, 256, 0, s>>>(h->to_solid, fs, ss);
+        const One<ToSolidWork> w{{h->to_solid, fs, ss}, h->to_solid.n};
+        if (h->pole == AXG_MONOPOLE) couple_to_solid_kernel<POLE_MONO><<<nb, 256, 0, s>>>(w);
+        else if (h->pole == AXG_DIPOLE) couple_to_solid_kernel<POLE_DI><<<nb, 256, 0, s>>>(w);
+        else couple_to_solid_kernel<POLE_QUAD><<<nb, 256, 0, s>>>(w);
       }
     }
     if (h->pole == AXG_MONOPOLE) launch_solid_symplectic<POLE_MONO>(h, s, ss);
@@ -709,8 +722,7 @@ void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
   StateArgs ss = solid_state(h), fs = fluid_state(h);
   const int64_t n = std::max(h->nglob_s, h->nel_f > 0 ? h->nglob_f : 0);
   drift_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ss, fs, h->sym_cd[h->nstages]);
-  receivers_kernel<<<1, 256, 0, s>>>(ss, h->rec_gidx_d, h->num_rec, h->seis_it, h->pole, h->rec, h->nseismo,
-                                     h->iter);
+  receivers_kernel<<<1, 256, 0, s>>>(One<RecWork>{rec_work(h, ss), 1});
 }
 
 int build_graph(axg_handle *h, int nsteps) {
@@ -1946,3 +1958,323 @@ int axg_device_check_report(int32_t *out8) {
 const char *axg_last_error(axg_handle *h) { return h ? h->err.c_str() : g_create_error.c_str(); }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ batches
+
+struct axg_batch {
+  std::vector<axg_handle *> hs;
+  int device = 0, num_sms = 1;
+  SpecDev spec{};
+  int solid_ctas[3][2] = {};  // resident CTAs of the batched Newmark kernel per (pole, compensated)
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev_done = nullptr;
+  bool pending = false;
+  int64_t launches_per_step = 0;
+  std::string err = "no error";
+};
+
+namespace {
+
+int bfail(axg_batch *b, int code, const std::string &msg) {
+  b->err = msg;
+  return code;
+}
+
+#define BCK(call)                                                                                        \
+  do {                                                                                                   \
+    cudaError_t e_ = (call);                                                                             \
+    if (e_ != cudaSuccess)                                                                               \
+      return bfail(b, e_ == cudaErrorMemoryAllocation ? AXG_ERR_OOM : AXG_ERR_CUDA,                      \
+                   fmt("%s: %s", #call, cudaGetErrorString(e_)));                                        \
+  } while (0)
+
+// Launches over the solves that `items` gives work (> 0 items), at most
+// kMaxBatch solves per launch; returns the number of launches.
+template <class W, class ItemsFn, class WorkFn, class LaunchFn>
+int64_t for_batches(const std::vector<axg_handle *> &hs, ItemsFn items, WorkFn work, LaunchFn launch) {
+  int64_t nl = 0;
+  Many<W> m{};
+  auto flush = [&]() {
+    if (m.n > 0) {
+      launch(m);
+      ++nl;
+    }
+    m.n = 0;
+    m.start[0] = 0;
+  };
+  for (axg_handle *h : hs) {
+    const int32_t k = items(h);
+    if (k <= 0) continue;
+    m.w[m.n] = work(h);
+    m.start[m.n + 1] = m.start[m.n] + k;
+    if (++m.n == kMaxBatch) flush();
+  }
+  flush();
+  return nl;
+}
+
+template <int NONMONO, bool KAHAN>
+int64_t batch_fluid_colour(axg_batch *b, int c, cudaStream_t s) {
+  return for_batches<PatchWork>(
+      b->hs,
+      [&](axg_handle *h) {
+        const bool mine = h->nel_f > 0 && c < h->pf.n_colours && (h->pole != AXG_MONOPOLE) == (NONMONO != 0) &&
+                          h->kahan == KAHAN;
+        return mine ? h->pf.colour_start[c + 1] - h->pf.colour_start[c] : 0;
+      },
+      [&](axg_handle *h) {
+        DomainArgs a = domain_args(h->df, h->pf);
+        a.patch_begin = h->pf.colour_start[c];
+        return PatchWork{a, fluid_state(h)};
+      },
+      [&](const Many<PatchWork> &m) {
+        fluid_patch_kernel<NONMONO, KAHAN, false, Many<PatchWork>><<<m.start[m.n], kThreads, 0, s>>>(m, b->spec);
+      });
+}
+
+template <int POLE, bool KAHAN>
+int64_t batch_solid_colour(axg_batch *b, int c, cudaStream_t s) {
+  const int pole = POLE == POLE_MONO ? AXG_MONOPOLE : POLE == POLE_DI ? AXG_DIPOLE : AXG_QUADPOLE;
+  return for_batches<PatchWork>(
+      b->hs,
+      [&](axg_handle *h) {
+        const bool mine = c < h->ps.n_colours && h->pole == pole && h->kahan == KAHAN;
+        return mine ? h->ps.colour_start[c + 1] - h->ps.colour_start[c] : 0;
+      },
+      [&](axg_handle *h) {
+        DomainArgs a = domain_args(h->ds, h->ps);
+        a.patch_begin = h->ps.colour_start[c];
+        return PatchWork{a, solid_state(h)};
+      },
+      [&](const Many<PatchWork> &m) {
+        const int grid = std::min(m.start[m.n], b->solid_ctas[POLE][KAHAN]);
+        solid_batch_kernel<POLE, KAHAN>
+            <<<grid, kThreads, solid_smem_bytes<POLE, MODE_NEWMARK, false, KAHAN>(), s>>>(m, b->spec);
+      });
+}
+
+template <int POLE>
+int64_t batch_to_solid(axg_batch *b, cudaStream_t s) {
+  const int pole = POLE == POLE_MONO ? AXG_MONOPOLE : POLE == POLE_DI ? AXG_DIPOLE : AXG_QUADPOLE;
+  return for_batches<ToSolidWork>(
+      b->hs, [&](axg_handle *h) { return h->nel_f > 0 && h->pole == pole ? h->to_solid.n : 0; },
+      [&](axg_handle *h) { return ToSolidWork{h->to_solid, fluid_state(h), solid_state(h)}; },
+      [&](const Many<ToSolidWork> &m) {
+        couple_to_solid_kernel<POLE, Many<ToSolidWork>><<<(m.start[m.n] + 255) / 256, 256, 0, s>>>(m);
+      });
+}
+
+template <int DIPOLE>
+int64_t batch_to_fluid(axg_batch *b, cudaStream_t s) {
+  return for_batches<ToFluidWork>(
+      b->hs,
+      [&](axg_handle *h) { return h->nel_f > 0 && (h->pole == AXG_DIPOLE) == (DIPOLE != 0) ? h->to_fluid.n : 0; },
+      [&](axg_handle *h) { return ToFluidWork{h->to_fluid, solid_state(h), h->ff}; },
+      [&](const Many<ToFluidWork> &m) {
+        couple_to_fluid_kernel<DIPOLE, Many<ToFluidWork>><<<(m.start[m.n] + 255) / 256, 256, 0, s>>>(m);
+      });
+}
+
+// One Newmark step of every solve, in the order of enqueue_step: coupling
+// into the fluid, fluid colours, coupling into the solid, solid colours,
+// seismograms and step counters.
+int64_t enqueue_batch_step(axg_batch *b, cudaStream_t s) {
+  int64_t nl = batch_to_fluid<0>(b, s) + batch_to_fluid<1>(b, s);
+  int fc = 0, sc = 0;
+  for (axg_handle *h : b->hs) {
+    if (h->nel_f > 0) fc = std::max(fc, h->pf.n_colours);
+    sc = std::max(sc, h->ps.n_colours);
+  }
+  for (int c = 0; c < fc; ++c)
+    nl += batch_fluid_colour<0, false>(b, c, s) + batch_fluid_colour<0, true>(b, c, s) +
+          batch_fluid_colour<1, false>(b, c, s) + batch_fluid_colour<1, true>(b, c, s);
+  nl += batch_to_solid<POLE_MONO>(b, s) + batch_to_solid<POLE_DI>(b, s) + batch_to_solid<POLE_QUAD>(b, s);
+  for (int c = 0; c < sc; ++c)
+    nl += batch_solid_colour<POLE_MONO, false>(b, c, s) + batch_solid_colour<POLE_MONO, true>(b, c, s) +
+          batch_solid_colour<POLE_DI, false>(b, c, s) + batch_solid_colour<POLE_DI, true>(b, c, s) +
+          batch_solid_colour<POLE_QUAD, false>(b, c, s) + batch_solid_colour<POLE_QUAD, true>(b, c, s);
+  nl += for_batches<RecWork>(
+      b->hs, [](axg_handle *) { return 1; }, [](axg_handle *h) { return rec_work(h, solid_state(h)); },
+      [&](const Many<RecWork> &m) { receivers_kernel<Many<RecWork>><<<m.n, 256, 0, s>>>(m); });
+  return nl;
+}
+
+// kernel parameters are limited to 32764 bytes
+static_assert(sizeof(Many<PatchWork>) <= 32000 && sizeof(Many<ToSolidWork>) <= 32000 &&
+                  sizeof(Many<ToFluidWork>) <= 32000 && sizeof(Many<RecWork>) <= 32000,
+              "a batched launch's descriptors must fit the kernel parameter space");
+
+// the step counters of up to kMaxBatch solves
+struct IterSet {
+  int32_t n;
+  int32_t *ctr[kMaxBatch];
+  int32_t first[kMaxBatch];
+};
+__global__ void set_iters_kernel(const __grid_constant__ IterSet a) {
+  if ((int)threadIdx.x < a.n) *a.ctr[threadIdx.x] = a.first[threadIdx.x];
+}
+
+template <int POLE, bool KAHAN>
+int prepare_batch_kernel(axg_batch *b, axg_handle *h) {
+  int rc = prepare_kernel_fn(h, solid_batch_kernel<POLE, KAHAN>, solid_smem_bytes<POLE, MODE_NEWMARK, false, KAHAN>(),
+                             &b->solid_ctas[POLE][KAHAN]);
+  if (rc) b->err = h->err;
+  return rc;
+}
+
+int batch_create_impl(axg_batch *b, axg_handle *const *hs, int32_t n) {
+  if (!hs || n < 1) return bfail(b, AXG_ERR_BAD_ARG, "axg_batch_create: no handles");
+  for (int k = 0; k < n; ++k) {
+    axg_handle *h = hs[k];
+    if (!h) return bfail(b, AXG_ERR_BAD_ARG, fmt("axg_batch_create: handle %d is NULL", k));
+    for (int q = 0; q < k; ++q)
+      if (hs[q] == h) return bfail(b, AXG_ERR_BAD_ARG, fmt("axg_batch_create: handle %d appears twice", k));
+    if (h->scheme != AXG_SCHEME_NEWMARK2 || h->anel)
+      return bfail(b, AXG_ERR_UNSUPPORTED,
+                   fmt("axg_batch_create: solve %d is not an elastic Newmark solve (attenuation and symplectic "
+                       "schemes run alone)", k));
+    if (k > 0 && (h->device != hs[0]->device || std::memcmp(&h->spec, &hs[0]->spec, sizeof(SpecDev)) != 0))
+      return bfail(b, AXG_ERR_BAD_ARG,
+                   fmt("axg_batch_create: solve %d is on another device or has other GLL matrices", k));
+    if (h->pending) return bfail(b, AXG_ERR_BAD_ARG, fmt("axg_batch_create: solve %d has queued steps", k));
+    b->hs.push_back(h);
+  }
+  b->device = hs[0]->device;
+  b->spec = hs[0]->spec;
+  b->num_sms = hs[0]->num_sms;
+  int rc = AXG_OK;
+  for (axg_handle *h : b->hs) {
+    const bool kh = h->kahan;
+    if (h->pole == AXG_MONOPOLE) rc = kh ? prepare_batch_kernel<POLE_MONO, true>(b, h) : prepare_batch_kernel<POLE_MONO, false>(b, h);
+    else if (h->pole == AXG_DIPOLE) rc = kh ? prepare_batch_kernel<POLE_DI, true>(b, h) : prepare_batch_kernel<POLE_DI, false>(b, h);
+    else rc = kh ? prepare_batch_kernel<POLE_QUAD, true>(b, h) : prepare_batch_kernel<POLE_QUAD, false>(b, h);
+    if (rc) return rc;
+  }
+  BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  BCK(cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming));
+  // one step, captured once; every step of every run replays it
+  cudaGraph_t g;
+  BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  b->launches_per_step = enqueue_batch_step(b, b->stream);
+  const cudaError_t le = cudaGetLastError();
+  const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+  if (le != cudaSuccess) {
+    if (ce == cudaSuccess) cudaGraphDestroy(g);
+    return bfail(b, AXG_ERR_CUDA, fmt("batch step capture: %s", cudaGetErrorString(le)));
+  }
+  BCK(ce);
+  const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  BCK(ie);
+  return AXG_OK;
+}
+
+void batch_release(axg_batch *b) {
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->ev_done) cudaEventDestroy(b->ev_done);
+  if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+// the solves' flags once the batch's work completed; the first error found
+int batch_flags(axg_batch *b) {
+  for (size_t k = 0; k < b->hs.size(); ++k) {
+    const int rc = check_flags(b->hs[k]);
+    if (rc) return bfail(b, rc, fmt("solve %d: %s", (int)k, b->hs[k]->err.c_str()));
+  }
+  return AXG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int axg_batch_create(axg_handle *const *hs, int32_t n, axg_batch **out) {
+  if (!out) return fail(nullptr, AXG_ERR_BAD_ARG, "out is NULL");
+  *out = nullptr;
+  axg_batch *b = new axg_batch();
+  const int rc = batch_create_impl(b, hs, n);
+  if (rc) {
+    g_create_error = b->err;
+    batch_release(b);
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return AXG_OK;
+}
+
+int axg_batch_run_async(axg_batch *b, const int32_t *first_iters, int32_t n_iter) {
+  if (!b || !first_iters) return b ? bfail(b, AXG_ERR_BAD_ARG, "first_iters is NULL") : AXG_ERR_BAD_ARG;
+  if (b->pending) return bfail(b, AXG_ERR_BAD_ARG, "the batch has queued steps (axg_batch_poll / axg_batch_wait)");
+  if (n_iter < 0) return bfail(b, AXG_ERR_BAD_ARG, "n_iter < 0");
+  const int n = (int)b->hs.size();
+  for (int k = 0; k < n; ++k) {
+    const axg_handle *h = b->hs[k];
+    if (first_iters[k] < 1 || (int64_t)first_iters[k] + n_iter - 1 > h->niter)
+      return bfail(b, AXG_ERR_BAD_ARG, fmt("solve %d: iterations %d..%d outside 1..niter=%d", k, first_iters[k],
+                                           first_iters[k] + n_iter - 1, h->niter));
+  }
+  if (n_iter == 0) return AXG_OK;
+  // the batch follows the work already queued on each solve's stream
+  for (axg_handle *h : b->hs) {
+    BCK(cudaEventRecord(h->ev_done, h->stream));
+    BCK(cudaStreamWaitEvent(b->stream, h->ev_done, 0));
+  }
+  for (int k0 = 0; k0 < n; k0 += kMaxBatch) {
+    IterSet a{};
+    a.n = std::min(kMaxBatch, n - k0);
+    for (int q = 0; q < a.n; ++q) {
+      a.ctr[q] = b->hs[k0 + q]->iter;
+      a.first[q] = first_iters[k0 + q];
+    }
+    set_iters_kernel<<<1, kMaxBatch, 0, b->stream>>>(a);
+  }
+  BCK(cudaGetLastError());
+  for (int32_t q = 0; q < n_iter; ++q) BCK(cudaGraphLaunch(b->graph, b->stream));
+  BCK(cudaEventRecord(b->ev_done, b->stream));
+  // and each solve's later work follows the batch
+  for (axg_handle *h : b->hs) BCK(cudaStreamWaitEvent(h->stream, b->ev_done, 0));
+  b->pending = true;
+  return AXG_OK;
+}
+
+int axg_batch_poll(axg_batch *b, int32_t *done) {
+  if (!b || !done) return b ? bfail(b, AXG_ERR_BAD_ARG, "done is NULL") : AXG_ERR_BAD_ARG;
+  *done = 1;
+  if (!b->pending) return AXG_OK;
+  const cudaError_t e = cudaEventQuery(b->ev_done);
+  if (e == cudaErrorNotReady) {
+    *done = 0;
+    return AXG_OK;
+  }
+  b->pending = false;
+  BCK(e);
+  return batch_flags(b);
+}
+
+int axg_batch_wait(axg_batch *b) {
+  if (!b) return AXG_ERR_BAD_ARG;
+  const bool was = b->pending;
+  b->pending = false;
+  BCK(cudaStreamSynchronize(b->stream));
+  return was ? batch_flags(b) : AXG_OK;
+}
+
+int axg_batch_launches_per_step(axg_batch *b, int64_t *n) {
+  if (!b || !n) return b ? bfail(b, AXG_ERR_BAD_ARG, "n is NULL") : AXG_ERR_BAD_ARG;
+  *n = b->launches_per_step;
+  return AXG_OK;
+}
+
+void axg_batch_destroy(axg_batch *b) {
+  if (!b) return;
+  batch_release(b);
+  delete b;
+}
+
+const char *axg_batch_last_error(axg_batch *b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+}  // extern "C"
+

@@ -129,6 +129,73 @@ struct StateArgs {
   int32_t niter;            // extent of stf
 };
 
+// ------------------------------------------------------------ work descriptors
+
+// A launch's per-solve arguments, passed in its parameter space
+// (__grid_constant__).  One<W>: one solve owns all of the launch's work items
+// (a colour's patches, the boundary points, ...).  Many<W>: up to kMaxBatch
+// solves advanced together by one launch; solve s owns the items
+// [start[s], start[s + 1]), and a CTA or thread finds its solve from them.
+constexpr int kMaxBatch = 32;
+
+template <class W>
+struct One {
+  static constexpr bool kMany = false;
+  W w;
+  int32_t n_items;
+  __device__ __forceinline__ int32_t items() const { return n_items; }
+  __device__ __forceinline__ int locate(int32_t) const { return 0; }
+  __device__ __forceinline__ int32_t first(int) const { return 0; }
+  __device__ __forceinline__ const W &at(int) const { return w; }
+};
+
+template <class W>
+struct Many {
+  static constexpr bool kMany = true;
+  int32_t n;                       // solves, 1..kMaxBatch
+  int32_t start[kMaxBatch + 1];    // item prefix over the solves
+  W w[kMaxBatch];
+  __device__ __forceinline__ int32_t items() const { return start[n]; }
+  __device__ __forceinline__ int locate(int32_t it) const {
+    int s = 0;
+    while (s + 1 < n && start[s + 1] <= it) ++s;
+    return s;
+  }
+  __device__ __forceinline__ int32_t first(int s) const { return start[s]; }
+  __device__ __forceinline__ const W &at(int s) const { return w[s]; }
+};
+
+// patch kernels: the domain (patch_begin = the colour's first patch) and state
+struct PatchWork {
+  DomainArgs d;
+  StateArgs st;
+};
+
+// How a patch kernel's body sees its work items.  OneSolve refers to the
+// kernel's own by-value parameters, so that the body reads them exactly as a
+// kernel written for one solve does (as constant-bank operands); ManySolves
+// indexes the batch's descriptors at run time.
+struct OneSolve {
+  static constexpr bool kMany = false;
+  const DomainArgs &d;
+  const StateArgs &st;
+  int32_t n;
+  __device__ __forceinline__ int32_t items() const { return n; }
+  __device__ __forceinline__ int locate(int32_t) const { return 0; }
+  __device__ __forceinline__ int32_t first(int) const { return 0; }
+  __device__ __forceinline__ const DomainArgs &dom(int) const { return d; }
+  __device__ __forceinline__ const StateArgs &state(int) const { return st; }
+};
+struct ManySolves {
+  static constexpr bool kMany = true;
+  const Many<PatchWork> &m;
+  __device__ __forceinline__ int32_t items() const { return m.items(); }
+  __device__ __forceinline__ int locate(int32_t it) const { return m.locate(it); }
+  __device__ __forceinline__ int32_t first(int s) const { return m.first(s); }
+  __device__ __forceinline__ const DomainArgs &dom(int s) const { return m.w[s].d; }
+  __device__ __forceinline__ const StateArgs &state(int s) const { return m.w[s].st; }
+};
+
 // ------------------------------------------------------------ small helpers
 
 __device__ __forceinline__ float predict(float d, float v, float a, float dt, float hdt2) {
@@ -670,11 +737,10 @@ struct WarpIter {
 // KAHAN (time loop only): compensated summation of the predictor and the
 // velocity corrector (kahan_add); the predictor's new compensation travels
 // from the gather to the last writer in shared memory.
-template <int POLE, int MODE, bool ANEL, bool KAHAN>
-__global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
-    solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches,
-                       const __grid_constant__ AnelArgs an) {  // an.ex[] is indexed at run time
+template <int POLE, int MODE, bool ANEL, bool KAHAN, class P>
+__device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, const AnelArgs &an) {
   static_assert(!ANEL || MODE == MODE_NEWMARK, "attenuation runs in the Newmark time loop only");
+  static_assert(!P::kMany || (MODE == MODE_NEWMARK && !ANEL), "batches run the elastic Newmark step");
   static_assert(!KAHAN || MODE == MODE_NEWMARK, "the compensated mode is a Newmark time-loop mode");
   constexpr bool TL = MODE != MODE_FORCE;  // a time-loop mode
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
@@ -708,10 +774,15 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
   if (threadIdx.x < kWarps * STG) mbar_init(&bars[threadIdx.x], 1);
   if (threadIdx.x < kMaxSubrounds) mbar_init(&s_round[threadIdx.x], kThreads);
   if (threadIdx.x < 2) mbar_init(&s_wbar[threadIdx.x], 1);
-  if (threadIdx.x == 0) s_stop = TL ? *st.blowup : 0;
+  // one solve: nothing to do after a blow-up (a batch checks per solve below)
+  if (threadIdx.x == 0) s_stop = TL && !P::kMany ? *p.state(0).blowup : 0;
   fence_mbar_init();
   __syncthreads();
   if (s_stop) return;  // uniform across the CTA; no copy has been issued
+  // the step's source time function value (a batch reads it per solve below)
+  float stf_one = 0.f;
+  if (TL && !P::kMany && AXG_BOUND(*p.state(0).iter - 1, p.state(0).niter, 3))
+    stf_one = p.state(0).stf[*p.state(0).iter - 1];
 
   const bool active = lane < 25;
   const int i = lane % 5, j = active ? lane / 5 : 0;
@@ -731,8 +802,8 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
   const bool cg = active && (i == 1 || i == 3) && (j == 1 || j == 3);
   const int kcg = 2 * (i >> 1) + (j >> 1);
   const uint32_t state_bytes = ANEL ? (uint32_t)an.state_stride * 4u : 0u;
-  // one thread: start the copies of element `el` into ring slot `slot`
-  auto issue = [&](uint32_t slot, int64_t el) {
+  // one thread: start the copies of element `el` of domain d into ring slot `slot`
+  auto issue = [&](const DomainArgs &d, uint32_t slot, int64_t el) {
     if (ANEL) {
       mbar_expect_tx(&my_bars[slot], BSB + kAnelConst * 4 + state_bytes);
       bulk_g2s_tx(my_ring + slot * BS, d.metric + el * BS, BSB, &my_bars[slot], pol);
@@ -743,12 +814,9 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
       bulk_g2s(my_ring + slot * BS, d.metric + el * BS, BSB, &my_bars[slot], pol);
     }
   };
-  float stf1 = 0.f;
-  if (TL && AXG_BOUND(*st.iter - 1, st.niter, 3)) stf1 = st.stf[*st.iter - 1];
-
   // one thread: bulk copy of a patch's point words into buffer b (each
   // patch's words start 16-byte aligned, padded to a multiple of four)
-  auto issue_words = [&](int b, int32_t pt_start, int n_pts) {
+  auto issue_words = [&](const DomainArgs &d, int b, int32_t pt_start, int n_pts) {
     const uint32_t nw = ((uint32_t)n_pts + 3u) & ~3u;
     if (nw > 0 && AXG_BOUND((int64_t)pt_start + nw - 1, d.n_pts, 1)) {
       fence_proxy_async();  // earlier generic reads of the buffer precede the async-proxy write
@@ -761,7 +829,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
   // u, and of the partial sums of points an earlier writer (earlier colour,
   // coupling pre-pass) holds, straight into buffer b.  A point's accumulator
   // starts from that partial sum, so that the write-back is a plain store.
-  auto issue_gather = [&](int b, int n_pts) {
+  auto issue_gather = [&](const StateArgs &st, int b, int n_pts) {
     float(*gu)[ROW] = su_of(b);
     float(*gf)[ROW] = sf_of(b);
     const uint32_t *gw = sw_of(b);
@@ -785,14 +853,24 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
   };
   // stiffness mode: the CTA's first patch is gathered here, each later one
   // while the CTA computes the patch before it
-  if (MODE == MODE_FORCE && blockIdx.x < n_colour_patches && AXG_BOUND(d.patch_begin + blockIdx.x, d.n_patches, 1)) {
+  if (MODE == MODE_FORCE && (int32_t)blockIdx.x < p.items() &&
+      AXG_BOUND(p.dom(0).patch_begin + blockIdx.x, p.dom(0).n_patches, 1)) {
+    const DomainArgs &d = p.dom(0);
     const PatchMeta m0 = d.meta[d.patch_begin + blockIdx.x];
-    if (threadIdx.x == 0) issue_words(0, m0.pt_start, m0.n_pts);
-    mbar_wait_bounded(&s_wbar[0], 0u, st.err);
-    issue_gather(0, m0.n_pts);
+    if (threadIdx.x == 0) issue_words(d, 0, m0.pt_start, m0.n_pts);
+    mbar_wait_bounded(&s_wbar[0], 0u, p.state(0).err);
+    issue_gather(p.state(0), 0, m0.n_pts);
   }
 
-  for (int pp = blockIdx.x; pp < n_colour_patches; pp += gridDim.x) {
+  for (int32_t it = blockIdx.x; it < p.items(); it += gridDim.x) {
+    // the work item's solve and patch
+    const int sv = p.locate(it);
+    const DomainArgs &d = p.dom(sv);
+    const StateArgs &st = p.state(sv);
+    const int pp = it - p.first(sv);
+    if (P::kMany && __syncthreads_or(threadIdx.x == 0 && *st.blowup != 0)) continue;  // that solve has stopped
+    float stf1 = stf_one;
+    if (TL && P::kMany && AXG_BOUND(*st.iter - 1, st.niter, 3)) stf1 = st.stf[*st.iter - 1];
     if (!AXG_BOUND(d.patch_begin + pp, d.n_patches, 1)) break;
     const PatchMeta m = d.meta[d.patch_begin + pp];
     const PatchRounds pr(m);
@@ -803,14 +881,14 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
     // stiffness mode: the next patch's point words go to the other buffer now
     int next_npts = 0;
     if (MODE == MODE_FORCE) {
-      const int ppn = pp + gridDim.x;
-      if (ppn < n_colour_patches && AXG_BOUND(d.patch_begin + ppn, d.n_patches, 1)) {
+      const int ppn = pp + gridDim.x;  // one solve: items are patches
+      if (ppn < p.items() && AXG_BOUND(d.patch_begin + ppn, d.n_patches, 1)) {
         const PatchMeta mn = d.meta[d.patch_begin + ppn];
         next_npts = mn.n_pts;
-        if (threadIdx.x == 0) issue_words(buf ^ 1, mn.pt_start, mn.n_pts);
+        if (threadIdx.x == 0) issue_words(d, buf ^ 1, mn.pt_start, mn.n_pts);
       }
     } else if (threadIdx.x == 0) {
-      issue_words(0, m.pt_start, m.n_pts);
+      issue_words(d, 0, m.pt_start, m.n_pts);
     }
     // this warp's first STG element blocks
     WarpIter pf{0, warp};
@@ -820,7 +898,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
       for (int q = 0; q < STG && pf.valid(pr); ++q) {
         if (lane == 0) {
           const int64_t el = (int64_t)m.elem_start + pf.s;
-          if (AXG_BOUND(el, d.n_elem, 2)) issue((kcount + q) % STG, el);
+          if (AXG_BOUND(el, d.n_elem, 2)) issue(d, (kcount + q) % STG, el);
         }
         pf.s += kWarps;
         pf.norm(pr, warp);
@@ -974,7 +1052,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
           if (lane == 0) {
             const int64_t pel = (int64_t)m.elem_start + pf.s;
             fence_proxy_async();  // the warp's reads of the slot precede the async-proxy write
-            if (AXG_BOUND(pel, d.n_elem, 2)) issue(slot, pel);
+            if (AXG_BOUND(pel, d.n_elem, 2)) issue(d, slot, pel);
           }
           pf.s += kWarps;
           pf.norm(pr, warp);
@@ -986,7 +1064,7 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
       if (MODE == MODE_FORCE && r == 0 && next_npts > 0) {
         // the next patch's words have landed in the other buffer: start its gather
         mbar_wait_bounded(&s_wbar[buf ^ 1], ((pcount + 1) / NB) & 1u, st.err);
-        issue_gather(buf ^ 1, next_npts);
+        issue_gather(st, buf ^ 1, next_npts);
       }
     }
     round_par ^= (1u << pr.n) - 1u;  // each used s_round completed once in this patch
@@ -1086,15 +1164,39 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
   }
 }
 
+// One solve: the patches of one colour.  The arguments are plain by-value
+// parameters, so that the body reads them as constant-bank operands.
+template <int POLE, int MODE, bool ANEL, bool KAHAN>
+__global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
+    solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches,
+                       const __grid_constant__ AnelArgs an) {  // an.ex[] is indexed at run time
+  solid_patch_body<POLE, MODE, ANEL, KAHAN>(OneSolve{d, st, n_colour_patches}, sp, an);
+}
+
+// A batch: colour c of every solve of the launch, found by run-time index
+// into the descriptors (hence in the parameter space, __grid_constant__).
+template <int POLE, bool KAHAN>
+__global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE_NEWMARK, false, KAHAN))
+    solid_batch_kernel(const __grid_constant__ Many<PatchWork> p, SpecDev sp) {
+  solid_patch_body<POLE, MODE_NEWMARK, false, KAHAN>(ManySolves{p}, sp, AnelArgs{});
+}
+
 // ------------------------------------------------------------ fluid patch kernel
 
-// One CTA per patch.  The gather reads each point's chi, dchi, ddchi0 (and the
-// partial sum of an earlier writer) in one batch of loads per thread; each
-// warp loads the metric terms of its next element while it computes the
-// current one; the write-back loads the last writers' inverse mass, dchi and
-// ddchi0 in one batch before it stores.
-template <int NONMONO, bool KAHAN, bool SYMP = false>
-__global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp) {
+// One CTA per patch (per work item: a patch of one of the solves).  The
+// gather reads each point's chi, dchi, ddchi0 (and the partial sum of an
+// earlier writer) in one batch of loads per thread; each warp loads the metric
+// terms of its next element while it computes the current one; the
+// write-back loads the last writers' inverse mass, dchi and ddchi0 in one
+// batch before it stores.
+template <int NONMONO, bool KAHAN, bool SYMP = false, class P = One<PatchWork>>
+__global__ void __launch_bounds__(kThreads) fluid_patch_kernel(const __grid_constant__ P p, SpecDev sp) {
+  static_assert(!P::kMany || !SYMP, "batches run the Newmark step");
+  if ((int32_t)blockIdx.x >= p.items()) return;  // uniform across the CTA
+  const int sv = p.locate(blockIdx.x);
+  const DomainArgs &d = p.at(sv).d;
+  const StateArgs &st = p.at(sv).st;
+  const int pp = blockIdx.x - p.first(sv);
   __shared__ float s_u[kMaxPatchPoints];
   __shared__ float s_f[kMaxPatchPoints];
   __shared__ float s_cu[KAHAN ? kMaxPatchPoints : 1];  // compensated mode: predictor compensation
@@ -1105,8 +1207,8 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(DomainArgs d, Sta
   if (threadIdx.x == 0) s_stop = *st.blowup;
   __syncthreads();
   if (s_stop) return;  // uniform across the CTA
-  if (!AXG_BOUND(d.patch_begin + blockIdx.x, d.n_patches, 11)) return;
-  const PatchMeta m = d.meta[d.patch_begin + blockIdx.x];
+  if (!AXG_BOUND(d.patch_begin + pp, d.n_patches, 11)) return;
+  const PatchMeta m = d.meta[d.patch_begin + pp];
   {
     uint32_t w[kGB];
     float uu[kGB], ff[kGB], cc[KAHAN ? kGB : 1];
@@ -1284,10 +1386,21 @@ struct Coupling {
 
 // bdry_copy2fluid (SOLVER/time_evol_wave.F90:1532-1571): fluid force starts
 // with -(b1 * u_s [+ u_phi] + b2 * u_z) of the predicted solid displacement
-template <int DIPOLE>
-__global__ void couple_to_fluid_kernel(Coupling cp, StateArgs solid, float *ffl) {
+struct ToFluidWork {
+  Coupling cp;
+  StateArgs solid;
+  float *ffl;  // the fluid force partial sums
+};
+template <int DIPOLE, class P = One<ToFluidWork>>
+__global__ void couple_to_fluid_kernel(const __grid_constant__ P p) {
+  const int32_t it = blockIdx.x * blockDim.x + threadIdx.x;  // a receiving point of one of the solves
+  if (it >= p.items()) return;
+  const int sv = p.locate(it);
+  const Coupling &cp = p.at(sv).cp;
+  const StateArgs &solid = p.at(sv).solid;
+  float *ffl = p.at(sv).ffl;
+  const int q = it - p.first(sv);
   if (*solid.blowup) return;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= cp.n) return;
   float acc = 0.f;
   for (int k = cp.start[q]; k < cp.start[q + 1]; ++k) {
@@ -1314,10 +1427,20 @@ __global__ void couple_to_fluid_kernel(Coupling cp, StateArgs solid, float *ffl)
 // bdry_copy2solid (SOLVER/time_evol_wave.F90:1577-1611): solid force starts
 // with b1 * ddchi (s [and phi] components) and b2 * ddchi (z) of the new
 // fluid acceleration; `mask` holds per contribution the axis mask bits.
-template <int POLE>
-__global__ void couple_to_solid_kernel(Coupling cp, StateArgs fluid, StateArgs solid) {
+struct ToSolidWork {
+  Coupling cp;
+  StateArgs fluid, solid;
+};
+template <int POLE, class P = One<ToSolidWork>>
+__global__ void couple_to_solid_kernel(const __grid_constant__ P p) {
+  const int32_t it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= p.items()) return;
+  const int sv = p.locate(it);
+  const Coupling &cp = p.at(sv).cp;
+  const StateArgs &fluid = p.at(sv).fluid;
+  const StateArgs &solid = p.at(sv).solid;
+  const int q = it - p.first(sv);
   if (*solid.blowup) return;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= cp.n) return;
   float fs = 0.f, fp = 0.f, fz = 0.f;
   for (int k = cp.start[q]; k < cp.start[q + 1]; ++k) {
@@ -1345,8 +1468,23 @@ __global__ void couple_to_solid_kernel(Coupling cp, StateArgs fluid, StateArgs s
 
 // nc_compute_recfile_seis_bare (SOLVER/seismograms.f90:783-820) every seis_it
 // steps into rec(nseismo, 3, num_rec); advances the step counter afterwards.
-__global__ void receivers_kernel(StateArgs solid, const int32_t *rec_gidx, int32_t num_rec, int32_t seis_it,
-                                 int32_t pole, float *rec, int32_t nseismo, int32_t *iter_ctr) {
+// One CTA per solve.
+struct RecWork {
+  StateArgs solid;
+  const int32_t *rec_gidx;
+  int32_t num_rec, seis_it, pole, nseismo;
+  float *rec;
+  int32_t *iter_ctr;
+};
+template <class P = One<RecWork>>
+__global__ void receivers_kernel(const __grid_constant__ P p) {
+  if ((int32_t)blockIdx.x >= p.items()) return;
+  const RecWork &rw = p.at(p.locate(blockIdx.x));
+  const StateArgs &solid = rw.solid;
+  const int32_t *rec_gidx = rw.rec_gidx;
+  const int32_t num_rec = rw.num_rec, seis_it = rw.seis_it, pole = rw.pole, nseismo = rw.nseismo;
+  float *rec = rw.rec;
+  int32_t *iter_ctr = rw.iter_ctr;
   const int32_t iter = *iter_ctr;
   __syncthreads();
   if (!*solid.blowup && seis_it > 0 && iter % seis_it == 0) {

@@ -14,7 +14,15 @@ receiver count and a seismogram duration.  The server
   * advances every admitted solve in chunks of steps queued on its own
     stream (axg_run_async), so that the solves' kernels overlap on the GPU,
     and polls them (axg_poll); a finished solve returns its seismograms and
-    frees its memory, which admits the next request.
+    frees its memory, which admits the next request;
+  * or, batched, advances all admitted solves together (axg_batch_*): one
+    launch per colour and kernel class covers every solve's patches, and a
+    step is one CUDA graph replay.  Between chunks finished solves retire and
+    waiting ones join (continuous batching at chunk granularity); new solves
+    are created while the current chunk runs.
+
+Solves run in the compensated (Kahan) FP32 mode by default, the precision of
+the serving workload.
 
 The meshes are seeded synthetic coupled meshes (a solid layer over a fluid
 layer, `coupled_mesh`) whose size grows as the period shrinks; they stand in
@@ -31,7 +39,7 @@ import numpy as np
 
 from . import _abi
 from .mesh import Mesh, coupled_mesh, set_source_receivers
-from .solver import Solver
+from .solver import Batch, Solver
 
 # period (s) -> coupled mesh (ni, nj_solid, nj_fluid): ~4x the elements per halving
 MESH_OF_PERIOD = {50: (32, 24, 8), 25: (64, 48, 16), 10: (128, 96, 32)}
@@ -130,12 +138,15 @@ class Server:
     """The serving loop; `budget_bytes` bounds the HBM the solves and
     resident meshes may hold."""
 
-    def __init__(self, budget_bytes: float = 64e9, chunk: int = 0, lib=None):
+    def __init__(self, budget_bytes: float = 64e9, chunk: int = 0, lib=None, compensated: bool = True):
         """chunk: steps queued per call for a solve (0: all of them at once;
-        smaller chunks let a long solve yield the host loop between chunks)."""
+        smaller chunks let a long solve yield the host loop between chunks);
+        in the batched loop, the most steps a batch runs before solves may
+        join it (0: until its first solve finishes)."""
         self.lib = lib or _abi.load_library()
         self.budget = budget_bytes
         self.chunk = chunk
+        self.compensated = compensated
         self.meshes: dict = {}      # key -> holder Solver (keeps the mesh resident)
         self.mesh_bytes: dict = {}
         self.used = 0
@@ -144,6 +155,11 @@ class Server:
         for s in self.meshes.values():
             s.close()
         self.meshes.clear()
+
+    def _solver(self, req: Request, share: bool) -> Solver:
+        s = Solver(request_mesh(req), lib=self.lib, share_with=self._holder(req) if share else None)
+        s.set_compensated(self.compensated)
+        return s
 
     def _holder(self, req: Request) -> Solver:
         if req.key not in self.meshes:
@@ -173,11 +189,15 @@ class Server:
         job.solver.run_async(job.next_iter, n)
         job.next_iter += n
 
-    def run(self, requests: list[Request], sequential: bool = False, resident: bool = False) -> ServeStats:
+    def run(self, requests: list[Request], sequential: bool = False, resident: bool = False,
+            batched: bool = False) -> ServeStats:
         """Serves `requests` (arrival times relative to the call).  sequential:
         one solve at a time, each on its own freshly built mesh -- the plain
         path run request after request, the baseline -- or, with `resident`,
-        on the server's resident meshes (the gain of overlapping alone)."""
+        on the server's resident meshes (the gain of overlapping alone).
+        batched: the admitted solves advance together in batches."""
+        if batched:
+            return self._run_batched(requests)
         pending = collections.deque(sorted(requests, key=lambda r: r.t_arrive))
         waiting: collections.deque = collections.deque()
         active: list[Job] = []
@@ -194,10 +214,7 @@ class Server:
                     break
                 waiting.popleft()
                 fresh = sequential and not resident
-                if fresh:
-                    s = Solver(request_mesh(req), lib=self.lib)
-                else:
-                    s = Solver(request_mesh(req), lib=self.lib, share_with=self._holder(req))
+                s = self._solver(req, share=not fresh)
                 own, mesh = _solve_bytes(s)
                 nbytes = own + (mesh if fresh else 0)
                 self.used += nbytes
@@ -229,9 +246,69 @@ class Server:
         stats.wall_s = time.perf_counter() - t0
         return stats
 
+    def _run_batched(self, requests: list[Request]) -> ServeStats:
+        pending = collections.deque(sorted(requests, key=lambda r: r.t_arrive))
+        waiting: collections.deque = collections.deque()
+        active: list[Job] = []
+        stats = ServeStats(wall_s=0.0)
+        batch, members, n_steps = None, [], 0
+        t0 = time.perf_counter()
+        while pending or waiting or active:
+            now = time.perf_counter() - t0
+            while pending and pending[0].t_arrive <= now:
+                waiting.append(pending.popleft())
+            # admission, also while a batch runs: the new solves join the next one
+            while waiting:
+                req = waiting[0]
+                if active and self.used + self._estimate(req) > self.budget:
+                    break
+                waiting.popleft()
+                s = self._solver(req, share=True)
+                own, _ = _solve_bytes(s)
+                self.used += own
+                active.append(Job(req, s, own, t_admit=time.perf_counter() - t0))
+            stats.peak_bytes = max(stats.peak_bytes, self.used)
+            if batch is not None:
+                if not batch.poll():
+                    time.sleep(20e-6)
+                    continue
+                done = time.perf_counter() - t0
+                for job in members:
+                    job.next_iter += n_steps
+                finished = [j for j in members if j.next_iter > j.req.niter]
+                if finished:
+                    batch.close()
+                    batch = None
+                for job in finished:
+                    stats.results[job.req.rid] = Result(job.req.rid, done - job.req.t_arrive,
+                                                        job.solver.receivers().copy())
+                    job.solver.close()
+                    self.used -= job.bytes
+                    active.remove(job)
+            if not active:
+                if pending and not waiting:
+                    time.sleep(max(0.0, min(0.01, pending[0].t_arrive - (time.perf_counter() - t0))))
+                continue
+            # the next chunk: the same batch while no solve joined or left
+            if batch is None or [j.req.rid for j in members] != [j.req.rid for j in active]:
+                if batch is not None:
+                    batch.close()
+                members = list(active)
+                batch = Batch([j.solver for j in members])
+            stats.max_concurrent = max(stats.max_concurrent, len(members))
+            n_steps = min(j.req.niter - j.next_iter + 1 for j in members)
+            if self.chunk > 0:
+                n_steps = min(n_steps, self.chunk)
+            batch.run_async([j.next_iter for j in members], n_steps)
+        if batch is not None:
+            batch.close()
+        stats.wall_s = time.perf_counter() - t0
+        return stats
 
-def solve_alone(req: Request, lib=None) -> np.ndarray:
+
+def solve_alone(req: Request, lib=None, compensated: bool = True) -> np.ndarray:
     """The request's seismograms from a solve on its own, built from scratch."""
     with Solver(request_mesh(req), lib=lib) as s:
+        s.set_compensated(compensated)
         s.run()
         return s.receivers().copy()

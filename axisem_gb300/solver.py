@@ -193,3 +193,65 @@ class Solver:
             self.h, pe.ctypes.data_as(C.POINTER(C.c_int32)), cp.ctypes.data_as(C.POINTER(C.c_int32)),
             len(cp)))
         return pe, cp
+
+
+class Batch:
+    """Several solves advanced together (axg_batch_*): one launch per colour
+    and kernel class covers all of them, and the step is replayed from one
+    CUDA graph.  Each solve's results are bit-for-bit those it gets alone.
+    The solvers must stay open while the batch exists."""
+
+    def __init__(self, solvers: "list[Solver]"):
+        if not solvers:
+            raise ValueError("a batch needs at least one solve")
+        self.lib = solvers[0].lib
+        self.solvers = list(solvers)
+        hs = (C.c_void_p * len(solvers))(*[s.h for s in solvers])
+        b = C.c_void_p()
+        rc = self.lib.axg_batch_create(hs, len(solvers), C.byref(b))
+        if rc != _abi.AXG_OK:
+            raise AxgError(rc, self.lib.axg_batch_last_error(None).decode())
+        self.b = b
+
+    def _check(self, rc):
+        if rc != _abi.AXG_OK:
+            raise AxgError(rc, self.lib.axg_batch_last_error(self.b).decode())
+
+    def run_async(self, first_iters, n_iter: int):
+        """Queue n_iter steps; solve k starts at first_iters[k]."""
+        fi = (C.c_int32 * len(self.solvers))(*[int(x) for x in first_iters])
+        self._check(self.lib.axg_batch_run_async(self.b, fi, int(n_iter)))
+
+    def poll(self) -> bool:
+        done = C.c_int32(0)
+        self._check(self.lib.axg_batch_poll(self.b, C.byref(done)))
+        return bool(done.value)
+
+    def wait(self):
+        self._check(self.lib.axg_batch_wait(self.b))
+
+    def run(self, first_iters, n_iter: int):
+        self.run_async(first_iters, n_iter)
+        self.wait()
+
+    def launches_per_step(self) -> int:
+        n = C.c_int64()
+        self._check(self.lib.axg_batch_launches_per_step(self.b, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.axg_batch_destroy(self.b)
+            self.b = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

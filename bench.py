@@ -387,16 +387,19 @@ def run_timeloop(args, pole, ws, rank, anel=False, compensated=False):
 
 def run_serving(args):
     """Continuous-batching serving (axisem_gb300.serve; the meshes of the
-    stream resident before it starts) against the same request list run one
-    solve at a time, each on its own freshly built mesh (the plain path,
-    sequentially).  Seeded Poisson arrivals at args.serve_rate per second;
-    each request's seismograms must be identical in both runs."""
+    stream resident before it starts), with solves overlapping on their own
+    streams and with solves advanced together in batches, against the same
+    request list run one solve at a time, each on its own freshly built mesh
+    (the plain path, sequentially).  Seeded Poisson arrivals at
+    args.serve_rate per second; each request's seismograms must be identical
+    in all runs."""
     from axisem_gb300.serve import Server, request_stream
     reqs = request_stream(args.serve_requests, args.serve_rate, seed=2026)
     srv = Server(budget_bytes=64e9)
     try:
         srv.preload({r.key for r in reqs})   # the server's meshes are resident before the stream starts
         served = srv.run(reqs)
+        batched = srv.run(reqs, batched=True)
     finally:
         srv.close()
     seq_srv = Server(budget_bytes=64e9)
@@ -406,13 +409,16 @@ def run_serving(args):
         seq_res = seq_srv.run(reqs, sequential=True, resident=True)
     finally:
         seq_srv.close()
-    same = all(np.array_equal(served.results[r.rid].seismograms, seq.results[r.rid].seismograms) for r in reqs)
-    a, b = served.summary(), seq.summary()
+    same = all(np.array_equal(served.results[r.rid].seismograms, seq.results[r.rid].seismograms) and
+               np.array_equal(batched.results[r.rid].seismograms, seq.results[r.rid].seismograms) for r in reqs)
+    a, b, c = served.summary(), seq.summary(), batched.summary()
     return {"requests": len(reqs), "arrival_rate_per_s": args.serve_rate,
             "mix": "period {50,25,10} s -> 1k/4k/16k-element coupled meshes, pole {mono,di,quad}, "
-                   "depth 0-700 km, 20-500 receivers, 1800-3600 s",
-            "served": a, "sequential_plain": b, "sequential_resident_meshes": seq_res.summary(),
+                   "depth 0-700 km, 20-500 receivers, 1800-3600 s; compensated (Kahan) FP32",
+            "served": a, "served_batched": c, "sequential_plain": b,
+            "sequential_resident_meshes": seq_res.summary(),
             "solves_per_hour_ratio": a["solves_per_hour"] / b["solves_per_hour"],
+            "batched_solves_per_hour_ratio": c["solves_per_hour"] / b["solves_per_hour"],
             "results_identical_to_sequential": bool(same)}
 
 

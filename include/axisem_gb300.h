@@ -263,6 +263,30 @@ int axg_run_async(axg_handle *h, int32_t first_iter, int32_t n_iter);
 int axg_poll(axg_handle *h, int32_t *done);
 int axg_wait(axg_handle *h);
 
+/* Batches: several solves advanced together, on the same or on different
+ * meshes (uneven element counts).  A batch step makes one launch per colour
+ * and kernel class for all its solves -- the kernels take a work list of
+ * (solve, patch) items -- and is captured once in a CUDA graph that every
+ * step replays.  Solves of a batch run the elastic Newmark step (any pole,
+ * plain or compensated; not attenuation or a symplectic scheme) and share
+ * the GLL derivative matrices.  Each solve's results are bit-for-bit those
+ * it gets alone.  The handles must stay open while the batch exists and are
+ * not run by other calls meanwhile; their later calls are ordered after the
+ * batch's work.  No counterpart in the reference. */
+typedef struct axg_batch axg_batch;
+int axg_batch_create(axg_handle *const *hs, int32_t n, axg_batch **out);
+/* Queue n_iter steps of every solve, solve k from iteration first_iters[k]
+ * (each within 1..niter of its solve); returns at once. */
+int axg_batch_run_async(axg_batch *b, const int32_t *first_iters, int32_t n_iter);
+/* *done = 1 once the queued steps finished; then (and in axg_batch_wait)
+ * a blow-up or timeout of any solve is reported as axg_run reports it. */
+int axg_batch_poll(axg_batch *b, int32_t *done);
+int axg_batch_wait(axg_batch *b);
+/* kernel launches of one batch step */
+int axg_batch_launches_per_step(axg_batch *b, int64_t *n);
+void axg_batch_destroy(axg_batch *b);
+const char *axg_batch_last_error(axg_batch *b);
+
 /* Time schemes of the reference (time_scheme in inparam_advanced,
  * SOLVER/time_evol_wave.F90:231-245, 516-967). */
 enum axg_scheme {
