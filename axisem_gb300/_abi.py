@@ -62,6 +62,8 @@ AXIAL_TERMS_USED = {
  SCHEME_SS_35O10) = range(6)
 (FIELD_DISP, FIELD_VELO, FIELD_ACC0, FIELD_CHI, FIELD_DCHI, FIELD_DDCHI0, FIELD_MEMVAR, FIELD_ATT_SRC_TR,
  FIELD_ATT_SRC_DEV, FIELD_DISP_COMP, FIELD_VELO_COMP, FIELD_CHI_COMP, FIELD_DCHI_COMP) = range(13)
+# enum axg_dump_type (dump_type of the reference's inparam_advanced)
+DUMP_NONE, DUMP_DISPL_ONLY, DUMP_STRAIN_ONLY, DUMP_DISPL_VELO, DUMP_FULLFIELDS = range(5)
 
 _fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int32)
@@ -109,6 +111,20 @@ class MeshDesc(C.Structure):
     ]
 
 
+class DumpDesc(C.Structure):
+    """struct axg_dump_desc"""
+
+    _fields_ = [
+        ("dump_type", C.c_int32), ("strain_it", C.c_int32),
+        ("ibeg", C.c_int32), ("iend", C.c_int32), ("jbeg", C.c_int32), ("jend", C.c_int32),
+        ("DsDeta_over_J_sol", _fp), ("DzDeta_over_J_sol", _fp), ("DsDxi_over_J_sol", _fp),
+        ("DzDxi_over_J_sol", _fp), ("inv_s_solid", _fp),
+        ("DsDeta_over_J_flu", _fp), ("DzDeta_over_J_flu", _fp), ("DsDxi_over_J_flu", _fp),
+        ("DzDxi_over_J_flu", _fp), ("inv_s_fluid", _fp), ("inv_rho_fluid", _fp),
+        ("out", _fp), ("capacity", C.c_int64),
+    ]
+
+
 class Info(C.Structure):
     """struct axg_info"""
 
@@ -150,6 +166,9 @@ SIGNATURES = {
     "axg_run_async": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "axg_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "axg_wait": (C.c_int, [C.c_void_p]),
+    "axg_set_wavefield_dump": (C.c_int, [C.c_void_p, C.POINTER(DumpDesc)]),
+    "axg_wavefield_dump_layout": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                            C.POINTER(C.c_int64), C.c_char_p, C.c_int32]),
     "axg_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
     "axg_batch_run_async": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32]),
     "axg_batch_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),

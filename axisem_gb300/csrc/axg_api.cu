@@ -150,12 +150,31 @@ struct axg_handle {
   int nsls = 0;
   AnelArgs an{};
   std::vector<int32_t> slot_of_elem_s;  // solid element -> launch slot
+  // kernel wavefield dumps (axg_set_wavefield_dump)
+  std::vector<uint8_t> axial_s, axial_f;  // per element (reference order): on the axis
+  struct Dump {
+    int type = 0, strain_it = 1, ibeg = 0, iend = 4, jbeg = 0, jend = 4, ns = 0, nf = 0;
+    int64_t np = 25, floats = 0;  // points per element, floats per snapshot
+    float *out = nullptr;
+    int64_t capacity = 0;
+    int32_t *gidx_s = nullptr, *gidx_f = nullptr;
+    uint8_t *ax_s = nullptr, *ax_f = nullptr;
+    float *pw_s[5] = {}, *pw_f[5] = {}, *inv_rho = nullptr;
+    float *slot[2] = {};
+    int64_t slot_floats = 0;
+    cudaEvent_t ev_dump[2] = {}, ev_copy[2] = {};
+    std::vector<std::string> names;
+  } dump;
+  cudaGraphExec_t graph_dump = nullptr;  // strain_it steps, when that differs from steps_per_graph
+  int graph_dump_steps = 0;
   // mesh-level buffers, shared with the handles created from this one
   std::shared_ptr<MeshPool> mesh;
   bool in_mesh = false;  // allocations go to the mesh pool while set
 };
 
 namespace {
+
+using Dump = axg_handle::Dump;
 
 int fail(axg_handle *h, int code, const std::string &msg) {
   if (h) h->err = msg;
@@ -725,20 +744,34 @@ void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
   receivers_kernel<<<1, 256, 0, s>>>(One<RecWork>{rec_work(h, ss), 1});
 }
 
-int build_graph(axg_handle *h, int nsteps) {
-  if (h->graph) {
-    cudaGraphExecDestroy(h->graph);
-    h->graph = nullptr;
+// a CUDA graph of nsteps steps into *exec (replacing what it held)
+int build_graph_into(axg_handle *h, int nsteps, cudaGraphExec_t *exec) {
+  if (*exec) {
+    cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
   }
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < nsteps; ++k) enqueue_step(h, h->stream);
   CK(cudaStreamEndCapture(h->stream, &g));
-  cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaError_t e = cudaGraphInstantiate(exec, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
-  h->graph_steps = nsteps;
   return AXG_OK;
+}
+
+int build_graph(axg_handle *h, int nsteps) {
+  int rc = build_graph_into(h, nsteps, &h->graph);
+  if (!rc) h->graph_steps = nsteps;
+  return rc;
+}
+
+// the step graphs no longer match the handle's kernels or step count
+void drop_graphs(axg_handle *h) {
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->graph_dump) cudaGraphExecDestroy(h->graph_dump);
+  h->graph = h->graph_dump = nullptr;
+  h->graph_steps = h->graph_dump_steps = 0;
 }
 
 void release(axg_handle *h) {
@@ -749,6 +782,11 @@ void release(axg_handle *h) {
   if (h->ev_done) cudaEventDestroy(h->ev_done);
   for (cudaEvent_t e : h->ev_io)
     if (e) cudaEventDestroy(e);
+  for (int k = 0; k < 2; ++k) {
+    if (h->dump.ev_dump[k]) cudaEventDestroy(h->dump.ev_dump[k]);
+    if (h->dump.ev_copy[k]) cudaEventDestroy(h->dump.ev_copy[k]);
+  }
+  if (h->graph_dump) cudaGraphExecDestroy(h->graph_dump);
   if (h->copy_stream) {
     cudaStreamSynchronize(h->copy_stream);
     cudaStreamDestroy(h->copy_stream);
@@ -1009,6 +1047,8 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
       return fail(h, AXG_ERR_BAD_DESC, "axg_create_sharing: the global numbering differs from the handle's mesh");
     h->igloc_s = share->igloc_s;
     h->igloc_f = share->igloc_f;
+    h->axial_s = share->axial_s;
+    h->axial_f = share->axial_f;
     h->pre_s = share->pre_s;
     h->pre_f = share->pre_f;
     h->ps = share->ps;
@@ -1029,6 +1069,8 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
     std::vector<uint8_t> axs(h->nel_s, 0), axf(h->nel_f > 0 ? h->nel_f : 1, 0);
     for (int k = 0; k < d->naxel_solid; ++k) axs[d->ax_el_solid[k] - 1] = 1;
     for (int k = 0; k < d->naxel_fluid; ++k) axf[d->ax_el_fluid[k] - 1] = 1;
+    h->axial_s = axs;
+    h->axial_f = axf;
     const int nb = d->nel_bdry;
     for (int b = 0; b < nb; ++b) {
       const int64_t es = d->bdry_solid_el[b] - 1, ef = d->bdry_fluid_el[b] - 1;
@@ -1484,6 +1526,10 @@ int axg_run(axg_handle *h, int32_t first_iter, int32_t n_iter) {
     return fail(h, AXG_ERR_BAD_ARG, fmt("iterations %d..%d outside 1..niter=%d", first_iter, first_iter + n_iter - 1,
                                         h->niter));
   if (n_iter == 0) return AXG_OK;
+  if (h->dump.type) {  // runs that dump are split at the dump steps
+    int rc = axg_run_async(h, first_iter, n_iter);
+    return rc ? rc : axg_wait(h);
+  }
   CK(cudaMemcpyAsync(h->iter, &first_iter, sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
   int32_t done = 0;
   while (done < n_iter) {
@@ -1572,8 +1618,97 @@ int gvec_io_prepare(axg_handle *h) {
   int rc;
   if ((rc = upload(h, &h->gvec_perm, h->ps.new_of_old))) return rc;
   if ((rc = dalloc(h, &h->gvec_stage, 3 * (size_t)h->nglob_s))) return rc;
-  CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  if (!h->copy_stream) CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
   for (cudaEvent_t &e : h->ev_io) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return AXG_OK;
+}
+
+// ---- kernel wavefield dumps
+
+// the fields of a dump type for one domain, with the reference's names
+std::vector<std::string> dump_fields(int type, int pole, bool fluid) {
+  const bool nm = pole != AXG_MONOPOLE;
+  const std::string dom = fluid ? "_flu" : "_sol";
+  std::vector<std::string> f;
+  auto strain = [&]() {
+    for (const char *n : {"strain_dsus", "strain_dsuz", "strain_dpup", "straintrace"}) f.push_back(n + dom);
+    if (nm)
+      for (const char *n : {"strain_dsup", "strain_dzup"}) f.push_back(n + dom);
+  };
+  auto vec = [&](const std::string &v) {
+    f.push_back(v + dom + "_s");
+    if (nm) f.push_back(v + dom + "_p");
+    f.push_back(v + dom + "_z");
+  };
+  if (type == AXG_DUMP_STRAIN_ONLY || type == AXG_DUMP_FULLFIELDS) strain();
+  if (type == AXG_DUMP_DISPL_ONLY) vec("disp");
+  if (type == AXG_DUMP_DISPL_VELO) {
+    if (fluid) {
+      f.push_back("chi_flu");
+      f.push_back("dchi_flu");
+    } else {
+      vec("disp");
+      vec("velo");
+    }
+  }
+  if (type == AXG_DUMP_FULLFIELDS) vec("velo");
+  return f;
+}
+
+template <int POLE>
+void launch_dump_pole(axg_handle *h, float *slot) {
+  const Dump &dp = h->dump;
+  const unsigned ws = kThreads / 32;
+  DumpArgs a{};
+  a.type = dp.type;
+  a.ibeg = dp.ibeg;
+  a.iend = dp.iend;
+  a.jbeg = dp.jbeg;
+  a.jend = dp.jend;
+  a.gidx = dp.gidx_s;
+  a.axial = dp.ax_s;
+  for (int k = 0; k < 5; ++k) a.pw[k] = dp.pw_s[k];
+  for (int c = 0; c < 3; ++c) {
+    a.u[c] = h->su[c];
+    a.v[c] = h->sv[c];
+  }
+  a.out = slot;
+  a.nel = h->nel_s;
+  a.nglob = h->nglob_s;
+  const unsigned gs = (unsigned)std::min<int64_t>((h->nel_s + ws - 1) / ws, 16 * (int64_t)h->num_sms);
+  wavefield_dump_kernel<POLE, false><<<gs, kThreads, 0, h->stream>>>(a, h->spec);
+  if (h->nel_f > 0 && dp.nf > 0) {
+    a.gidx = dp.gidx_f;
+    a.axial = dp.ax_f;
+    for (int k = 0; k < 5; ++k) a.pw[k] = dp.pw_f[k];
+    a.inv_rho = dp.inv_rho;
+    a.u[0] = h->fu;
+    a.v[0] = h->fv;
+    a.u[1] = a.u[2] = a.v[1] = a.v[2] = nullptr;
+    a.out = slot + (int64_t)dp.ns * h->nel_s * dp.np;
+    a.nel = h->nel_f;
+    a.nglob = h->nglob_f;
+    const unsigned gf = (unsigned)std::min<int64_t>((h->nel_f + ws - 1) / ws, 16 * (int64_t)h->num_sms);
+    wavefield_dump_kernel<POLE, true><<<gf, kThreads, 0, h->stream>>>(a, h->spec);
+  }
+}
+
+// snapshot `idx` from the state at the end of the steps queued so far: the
+// kernels write one of two device slots, the copy stream moves it to the
+// host buffer while the next steps run
+int enqueue_dump(axg_handle *h, int64_t idx) {
+  Dump &dp = h->dump;
+  const int k = (int)(idx & 1);
+  CK(cudaStreamWaitEvent(h->stream, dp.ev_copy[k], 0));  // the slot's previous snapshot has left
+  if (h->pole == AXG_MONOPOLE) launch_dump_pole<POLE_MONO>(h, dp.slot[k]);
+  else if (h->pole == AXG_DIPOLE) launch_dump_pole<POLE_DI>(h, dp.slot[k]);
+  else launch_dump_pole<POLE_QUAD>(h, dp.slot[k]);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(dp.ev_dump[k], h->stream));
+  CK(cudaStreamWaitEvent(h->copy_stream, dp.ev_dump[k], 0));
+  CK(cudaMemcpyAsync(dp.out + idx * dp.floats, dp.slot[k], dp.floats * sizeof(float), cudaMemcpyDeviceToHost,
+                     h->copy_stream));
+  CK(cudaEventRecord(dp.ev_copy[k], h->copy_stream));
   return AXG_OK;
 }
 }  // namespace
@@ -1586,23 +1721,46 @@ int axg_run_async(axg_handle *h, int32_t first_iter, int32_t n_iter) {
     return fail(h, AXG_ERR_BAD_ARG, fmt("iterations %d..%d outside 1..niter=%d", first_iter, first_iter + n_iter - 1,
                                         h->niter));
   if (n_iter == 0) return AXG_OK;
+  const Dump &dp = h->dump;
+  if (dp.type) {
+    const int64_t last = ((int64_t)first_iter + n_iter - 1) / dp.strain_it - 1;  // last snapshot of the run
+    if (last >= dp.capacity)
+      return fail(h, AXG_ERR_BAD_ARG, fmt("snapshot %lld of the run is beyond the dump buffer's capacity %lld",
+                                          (long long)last, (long long)dp.capacity));
+  }
   // the kernels of a step after a blow-up return at once, so all steps can
   // be queued without a check in between
   CK(cudaMemcpyAsync(h->iter, &first_iter, sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
   for (int32_t done = 0; done < n_iter;) {
-    const int k = std::min<int32_t>(h->steps_per_graph, n_iter - done);
+    const int32_t it = first_iter + done;
+    int k = std::min<int32_t>(h->steps_per_graph, n_iter - done);
+    if (dp.type) k = std::min<int32_t>(k, dp.strain_it - (it - 1) % dp.strain_it);  // up to the next dump
     if (k == h->steps_per_graph) {
       if (!h->graph || h->graph_steps != k) {
         int rc = build_graph(h, k);
         if (rc) return rc;
       }
       CK(cudaGraphLaunch(h->graph, h->stream));
+    } else if (dp.type && k == dp.strain_it) {
+      if (!h->graph_dump || h->graph_dump_steps != k) {
+        int rc = build_graph_into(h, k, &h->graph_dump);
+        if (rc) return rc;
+        h->graph_dump_steps = k;
+      }
+      CK(cudaGraphLaunch(h->graph_dump, h->stream));
     } else {
       for (int q = 0; q < k; ++q) enqueue_step(h, h->stream);
       CK(cudaGetLastError());
     }
     done += k;
+    const int32_t last_it = first_iter + done - 1;
+    if (dp.type && last_it % dp.strain_it == 0) {
+      int rc = enqueue_dump(h, last_it / dp.strain_it - 1);
+      if (rc) return rc;
+    }
   }
+  if (dp.type)  // the run is complete once its snapshots are in the host buffer
+    for (int k = 0; k < 2; ++k) CK(cudaStreamWaitEvent(h->stream, dp.ev_copy[k], 0));
   CK(cudaEventRecord(h->ev_done, h->stream));
   h->pending = true;
   return AXG_OK;
@@ -1761,10 +1919,7 @@ int axg_set_tuning(axg_handle *h, int32_t patch_elems, int32_t steps_per_graph) 
     return fail(h, AXG_ERR_UNSUPPORTED, "the patch shape is fixed at creation (axg_create_tuned)");
   if (steps_per_graph > 0 && steps_per_graph != h->steps_per_graph) {
     h->steps_per_graph = steps_per_graph;
-    if (h->graph) {
-      cudaGraphExecDestroy(h->graph);
-      h->graph = nullptr;
-    }
+    drop_graphs(h);
   }
   return AXG_OK;
 }
@@ -1789,10 +1944,7 @@ int axg_set_compensated(axg_handle *h, int32_t on) {
     CK(cudaStreamSynchronize(h->stream));
   }
   h->kahan = on != 0;
-  if (h->graph) {
-    cudaGraphExecDestroy(h->graph);
-    h->graph = nullptr;
-  }
+  drop_graphs(h);
   return prepare_kernels(h);
 }
 
@@ -1837,10 +1989,7 @@ int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages) 
     h->scheme = scheme;
     h->nstages = n;
   }
-  if (h->graph) {
-    cudaGraphExecDestroy(h->graph);
-    h->graph = nullptr;
-  }
+  drop_graphs(h);
   int rc = prepare_kernels(h);
   if (rc) return rc;
   if (h->scheme) {
@@ -1956,6 +2105,107 @@ int axg_device_check_report(int32_t *out8) {
 }
 
 const char *axg_last_error(axg_handle *h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+}  // extern "C"
+
+extern "C" {
+
+int axg_set_wavefield_dump(axg_handle *h, const axg_dump_desc *dd) {
+  if (!h || !dd) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  if (h->pending) return fail(h, AXG_ERR_BAD_ARG, "the handle has queued steps");
+  if (dd->dump_type < AXG_DUMP_NONE || dd->dump_type > AXG_DUMP_FULLFIELDS)
+    return fail(h, AXG_ERR_BAD_ARG, "unknown dump_type");
+  Dump &dp = h->dump;
+  drop_graphs(h);
+  if (dd->dump_type == AXG_DUMP_NONE) {
+    dp.type = 0;
+    return AXG_OK;
+  }
+  if (dd->strain_it < 1) return fail(h, AXG_ERR_BAD_ARG, "strain_it must be >= 1");
+  if (dd->ibeg < 0 || dd->iend > 4 || dd->ibeg > dd->iend || dd->jbeg < 0 || dd->jend > 4 || dd->jbeg > dd->jend)
+    return fail(h, AXG_ERR_BAD_ARG, "ibeg..iend, jbeg..jend must lie in 0..4");
+  if (!dd->out || dd->capacity < 1) return fail(h, AXG_ERR_BAD_ARG, "no dump buffer");
+  const float *sol[5] = {dd->DsDeta_over_J_sol, dd->DzDeta_over_J_sol, dd->DsDxi_over_J_sol, dd->DzDxi_over_J_sol,
+                         dd->inv_s_solid};
+  const float *flu[6] = {dd->DsDeta_over_J_flu, dd->DzDeta_over_J_flu, dd->DsDxi_over_J_flu, dd->DzDxi_over_J_flu,
+                         dd->inv_s_fluid, dd->inv_rho_fluid};
+  for (const float *a : sol)
+    if (!a) return fail(h, AXG_ERR_BAD_ARG, "a solid data_pointwise array is NULL");
+  if (h->nel_f > 0)
+    for (const float *a : flu)
+      if (!a) return fail(h, AXG_ERR_BAD_ARG, "a fluid data_pointwise array is NULL");
+  int rc;
+  const size_t es = 25 * (size_t)h->nel_s, ef = 25 * (size_t)std::max<int64_t>(h->nel_f, 0);
+  if (!dp.gidx_s) {  // first use: numbering, axis flags, pointwise arrays on the device
+    std::vector<int32_t> g(h->igloc_s.size());
+    for (size_t p = 0; p < g.size(); ++p) g[p] = h->igloc_s[p] - 1;
+    if ((rc = upload(h, &dp.gidx_s, g)) || (rc = upload(h, &dp.ax_s, h->axial_s))) return rc;
+    for (int k = 0; k < 5; ++k)
+      if ((rc = dalloc(h, &dp.pw_s[k], es))) return rc;
+    if (h->nel_f > 0) {
+      std::vector<int32_t> gf(h->igloc_f.size());
+      for (size_t p = 0; p < gf.size(); ++p) gf[p] = h->igloc_f[p] - 1;
+      if ((rc = upload(h, &dp.gidx_f, gf)) || (rc = upload(h, &dp.ax_f, h->axial_f))) return rc;
+      for (int k = 0; k < 5; ++k)
+        if ((rc = dalloc(h, &dp.pw_f[k], ef))) return rc;
+      if ((rc = dalloc(h, &dp.inv_rho, ef))) return rc;
+    }
+    for (int k = 0; k < 2; ++k) {
+      CK(cudaEventCreateWithFlags(&dp.ev_dump[k], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&dp.ev_copy[k], cudaEventDisableTiming));
+    }
+    if (!h->copy_stream) CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  }
+  for (int k = 0; k < 5; ++k)
+    CK(cudaMemcpyAsync(dp.pw_s[k], sol[k], es * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  if (h->nel_f > 0) {
+    for (int k = 0; k < 5; ++k)
+      CK(cudaMemcpyAsync(dp.pw_f[k], flu[k], ef * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(dp.inv_rho, flu[5], ef * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  }
+  const std::vector<std::string> fs = dump_fields(dd->dump_type, h->pole, false);
+  const std::vector<std::string> ff = h->nel_f > 0 ? dump_fields(dd->dump_type, h->pole, true)
+                                                    : std::vector<std::string>();
+  dp.type = dd->dump_type;
+  dp.strain_it = dd->strain_it;
+  dp.ibeg = dd->ibeg;
+  dp.iend = dd->iend;
+  dp.jbeg = dd->jbeg;
+  dp.jend = dd->jend;
+  dp.ns = (int)fs.size();
+  dp.nf = (int)ff.size();
+  dp.np = (int64_t)(dd->iend - dd->ibeg + 1) * (dd->jend - dd->jbeg + 1);
+  dp.floats = dp.np * ((int64_t)dp.ns * h->nel_s + (int64_t)dp.nf * std::max<int64_t>(h->nel_f, 0));
+  dp.out = dd->out;
+  dp.capacity = dd->capacity;
+  dp.names = fs;
+  dp.names.insert(dp.names.end(), ff.begin(), ff.end());
+  if (dp.floats > dp.slot_floats) {
+    for (int k = 0; k < 2; ++k)
+      if ((rc = dalloc(h, &dp.slot[k], (size_t)dp.floats))) return rc;
+    dp.slot_floats = dp.floats;
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return AXG_OK;
+}
+
+int axg_wavefield_dump_layout(axg_handle *h, int32_t *n_solid_fields, int32_t *n_fluid_fields,
+                              int64_t *floats_per_snapshot, char *names, int32_t names_cap) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  const Dump &dp = h->dump;
+  if (n_solid_fields) *n_solid_fields = dp.type ? dp.ns : 0;
+  if (n_fluid_fields) *n_fluid_fields = dp.type ? dp.nf : 0;
+  if (floats_per_snapshot) *floats_per_snapshot = dp.type ? dp.floats : 0;
+  if (names && names_cap > 0) {
+    std::string all;
+    if (dp.type)
+      for (size_t k = 0; k < dp.names.size(); ++k) all += (k ? "," : "") + dp.names[k];
+    const size_t n = std::min(all.size(), (size_t)names_cap - 1);
+    std::memcpy(names, all.data(), n);
+    names[n] = 0;
+  }
+  return AXG_OK;
+}
 
 }  // extern "C"
 
@@ -2138,6 +2388,8 @@ int batch_create_impl(axg_batch *b, axg_handle *const *hs, int32_t n) {
       return bfail(b, AXG_ERR_BAD_ARG,
                    fmt("axg_batch_create: solve %d is on another device or has other GLL matrices", k));
     if (h->pending) return bfail(b, AXG_ERR_BAD_ARG, fmt("axg_batch_create: solve %d has queued steps", k));
+    if (h->dump.type)
+      return bfail(b, AXG_ERR_UNSUPPORTED, fmt("axg_batch_create: solve %d dumps wavefields (it runs alone)", k));
     b->hs.push_back(h);
   }
   b->device = hs[0]->device;

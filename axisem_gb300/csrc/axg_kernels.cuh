@@ -1509,4 +1509,156 @@ __global__ void receivers_kernel(const __grid_constant__ P p) {
   if (threadIdx.x == 0) *iter_ctr = iter + 1;
 }
 
+// ------------------------------------------------------------ kernel wavefield dumps
+
+// dump_stuff (SOLVER/time_evol_wave.F90:1201-1249): the fields of one
+// snapshot from the state at the end of a step.  One warp per element in the
+// reference's element order, lane = GLL point (i, j); the gradients are the
+// reference's axisym_gradient_* (SOLVER/pointwise_derivatives.f90:329-545)
+// as shuffle contractions: mxm1 = G1T f (axial element) or G2T f, mxm2 = f G2,
+// d/ds = dzdeta mxm1 + dzdxi mxm2, d/dz = dsdeta mxm1 + dsdxi mxm2.
+enum { DUMP_DISPL_ONLY = 1, DUMP_STRAIN_ONLY = 2, DUMP_DISPL_VELO = 3, DUMP_FULLFIELDS = 4 };
+
+struct DumpArgs {
+  const int32_t *gidx;     // (25, nel): the element's points (0-based, internal numbering)
+  const uint8_t *axial;    // per element: 1 on the axis
+  const float *pw[5];      // DsDeta, DzDeta, DsDxi, DzDxi over J, 1/s: (25, nel)
+  const float *inv_rho;    // fluid: 1/rho (25, nel)
+  const float *u[3];       // solid disp (u[1] null for the monopole) / fluid chi (u[0])
+  const float *v[3];       // solid velo / fluid dchi (v[0])
+  float *out;              // the domain's first field
+  int64_t nel, nglob;
+  int32_t type, ibeg, iend, jbeg, jend;
+};
+
+struct DumpLane {
+  float dsdeta, dzdeta, dsdxi, dzdxi, inv_s;
+};
+
+// (d/ds f, d/dz f) at this lane; warp-uniform `ax`
+__device__ __forceinline__ void dump_grad(const LaneCoef &c, const DumpLane &w, bool ax, int i, int j5, float f,
+                                          float &gs, float &gz) {
+  const float m1 = ax ? dxi(f, c.xi1, j5) : dxi(f, c.xi2, j5);
+  const float m2 = deta(f, c.eta, i);
+  gs = fmaf(w.dzdeta, m1, w.dzdxi * m2);
+  gz = fmaf(w.dsdeta, m1, w.dsdxi * m2);
+}
+
+// f_over_s_*: f / s, and at the axis (i = 0 of an axial element) L'Hospital's
+// df/ds (dsdf_*_allaxis, with G1T)
+__device__ __forceinline__ float dump_fos(const LaneCoef &c, const DumpLane &w, bool ax, int i, int j5, float f) {
+  float r = w.inv_s * f;
+  if (ax) {
+    const float m1 = dxi(f, c.xi1, j5), m2 = deta(f, c.eta, i);
+    if (i == 0) r = fmaf(w.dzdeta, m1, w.dzdxi * m2);
+  }
+  return r;
+}
+
+template <int POLE, bool FLUID>
+__global__ void __launch_bounds__(kThreads) wavefield_dump_kernel(DumpArgs a, SpecDev sp) {
+  const int lane = threadIdx.x & 31;
+  const bool active = lane < 25;
+  const int ml = active ? lane : 24;  // idle lanes take part in the shuffles on point 24's data
+  const int i = ml % 5, j = ml / 5, j5 = 5 * j;
+  LaneCoef coef;
+  load_coef(sp, i, j, coef);
+  const int ni = a.iend - a.ibeg + 1, nj = a.jend - a.jbeg + 1;
+  const int64_t np = (int64_t)ni * nj;
+  const bool mine = active && i >= a.ibeg && i <= a.iend && j >= a.jbeg && j <= a.jend;
+  const int64_t pidx = (i - a.ibeg) + (int64_t)ni * (j - a.jbeg);
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < a.nel; e += nwarps) {
+    const int64_t q = 25 * e + ml;
+    int32_t g = a.gidx[q];
+    if (!AXG_BOUND(g, a.nglob, 41)) g = 0;
+    const bool ax = a.axial[e] != 0;
+    const DumpLane w{a.pw[0][q], a.pw[1][q], a.pw[2][q], a.pw[3][q], a.pw[4][q]};
+    int fld = 0;
+    auto put = [&](float val) {
+      if (mine) a.out[(fld * a.nel + e) * np + pidx] = val;
+      ++fld;
+    };
+    constexpr bool nonmono = POLE != POLE_MONO;
+    if (!FLUID) {
+      const float x1 = a.u[0][g], x2 = nonmono ? a.u[1][g] : 0.f, x3 = a.u[2][g];
+      if (a.type == DUMP_STRAIN_ONLY || a.type == DUMP_FULLFIELDS) {
+        // compute_strain, SOLVER/time_evol_wave.F90:1286-1345
+        float g1, g2, h1, h2;
+        dump_grad(coef, w, ax, i, j5, POLE == POLE_DI ? x1 + x2 : x1, g1, g2);  // dsus, dzus
+        put(g1);
+        dump_grad(coef, w, ax, i, j5, x3, h1, h2);                              // dsuz, dzuz
+        const float n1 = (g2 + h1) / 2.f, n2 = g1 + h2;
+        put(n1);                                                                // E31
+        float buff;
+        if (POLE == POLE_MONO) buff = dump_fos(coef, w, ax, i, j5, x1);
+        else if (POLE == POLE_DI) buff = 2.f * dump_fos(coef, w, ax, i, j5, x2);
+        else buff = dump_fos(coef, w, ax, i, j5, x1 - 2.f * x2);
+        put(buff);                                                              // E22
+        put(buff + n2);                                                         // Ekk
+        if (POLE == POLE_DI) {
+          float p1, p2;
+          dump_grad(coef, w, ax, i, j5, x1 - x2, p1, p2);                       // dsup, dzup
+          put(-dump_fos(coef, w, ax, i, j5, x2) - p1 / 2.f);                    // E12
+          put(-(dump_fos(coef, w, ax, i, j5, x3) + p2) / 2.f);                  // E23
+        } else if (POLE == POLE_QUAD) {
+          float p1, p2;
+          dump_grad(coef, w, ax, i, j5, x2, p1, p2);
+          put(-dump_fos(coef, w, ax, i, j5, x1 + x2 / 2.f) - p1 / 2.f);
+          put(-dump_fos(coef, w, ax, i, j5, x3) - p2 / 2.f);
+        }
+      }
+      // dump_disp_global / dump_velo_global transform the dipole to (s, phi);
+      // dump_disp / dump_velo_dchi write the state as it is
+      const bool global = a.type != DUMP_DISPL_VELO;
+      auto vec = [&](float y1, float y2, float y3) {
+        put(global && POLE == POLE_DI ? y1 + y2 : y1);
+        if (nonmono) put(global && POLE == POLE_DI ? y1 - y2 : y2);
+        put(y3);
+      };
+      if (a.type == DUMP_DISPL_ONLY || a.type == DUMP_DISPL_VELO) vec(x1, x2, x3);
+      if (a.type == DUMP_DISPL_VELO || a.type == DUMP_FULLFIELDS)
+        vec(a.v[0][g], nonmono ? a.v[1][g] : 0.f, a.v[2][g]);
+    } else {
+      const float chi = a.u[0][g];
+      const float irho = a.inv_rho[q];
+      if (a.type == DUMP_DISPL_VELO) {
+        put(chi);
+        put(a.v[0][g]);
+        continue;
+      }
+      if (a.type == DUMP_STRAIN_ONLY || a.type == DUMP_FULLFIELDS) {
+        // SOLVER/time_evol_wave.F90:1347-1408: usz = grad(chi) / rho
+        float c1, c2, g1, g2, h1, h2;
+        dump_grad(coef, w, ax, i, j5, chi, c1, c2);
+        const float us = c1 * irho, uz = c2 * irho;
+        dump_grad(coef, w, ax, i, j5, us, g1, g2);
+        put(g1);
+        dump_grad(coef, w, ax, i, j5, uz, h1, h2);
+        const float n1 = (g2 + h1) / 2.f, n2 = g1 + h2;
+        put(n1);
+        const float fs = dump_fos(coef, w, ax, i, j5, us);
+        put(fs);
+        put(fs + n2);
+        if (POLE == POLE_DI) {
+          put((-fs) / 2.f);
+          put(dump_fos(coef, w, ax, i, j5, uz) / 2.f);
+        } else if (POLE == POLE_QUAD) {
+          put(-fs);
+          put(-dump_fos(coef, w, ax, i, j5, uz));
+        }
+      }
+      auto flu_vec = [&](float f) {  // inv_rho grad(f): s, phi (zero), z
+        float c1, c2;
+        dump_grad(coef, w, ax, i, j5, f, c1, c2);
+        put(irho * c1);
+        if (nonmono) put(0.f);
+        put(irho * c2);
+      };
+      if (a.type == DUMP_DISPL_ONLY) flu_vec(chi);
+      if (a.type == DUMP_FULLFIELDS) flu_vec(a.v[0][g]);
+    }
+  }
+}
+
 }  // namespace axg

@@ -84,6 +84,7 @@ class Mesh:
     recfile_el: np.ndarray | None = None           # (num_rec, 3)
     # attenuation (cg4)
     anel: dict | None = None
+    pointwise: dict = field(default_factory=dict)  # data_pointwise arrays (add_pointwise)
     # absorbing boundaries
     solid_absorbing_gamma: np.ndarray | None = None
     fluid_absorbing_gamma: np.ndarray | None = None
@@ -480,3 +481,50 @@ def add_attenuation(m: Mesh, n_sls: int = 5, seed: int = 77, do_corr_lowq: bool 
         "inv_s_solid": inv_s,
     }
     return m
+
+
+PW_SOLID = ("DsDeta_over_J_sol", "DzDeta_over_J_sol", "DsDxi_over_J_sol", "DzDxi_over_J_sol", "inv_s_solid")
+PW_FLUID = ("DsDeta_over_J_flu", "DzDeta_over_J_flu", "DsDxi_over_J_flu", "DzDxi_over_J_flu", "inv_s_fluid",
+            "inv_rho_fluid")
+
+
+def add_pointwise(m: Mesh, seed: int = 91) -> Mesh:
+    """Seeded data_pointwise arrays (SOLVER/def_precomp_terms.f90:171-230):
+    the mapping derivatives over the Jacobian with physical signs and scales,
+    1/s and the fluid's 1/rho, each (0:4,0:4,nel) per point.  The dump
+    kernels are data-oblivious, as the stiffness kernels are."""
+    rng = np.random.default_rng(seed)
+
+    def sgn(nel):
+        return _f(rng.uniform(0.5, 2.0, size=(5, 5, nel)) * rng.choice([-1.0, 1.0], size=(5, 5, nel)))
+
+    pw = {}
+    for nm in PW_SOLID[:4]:
+        pw[nm] = sgn(m.nel_solid)
+    pw["inv_s_solid"] = _f(rng.uniform(0.5, 2.0, size=(5, 5, m.nel_solid)))
+    if m.nel_fluid > 0:
+        for nm in PW_FLUID[:4]:
+            pw[nm] = sgn(m.nel_fluid)
+        pw["inv_s_fluid"] = _f(rng.uniform(0.5, 2.0, size=(5, 5, m.nel_fluid)))
+        pw["inv_rho_fluid"] = _f(rng.uniform(1.0 / 13000.0, 1.0 / 2500.0, size=(5, 5, m.nel_fluid)))
+    m.pointwise = pw
+    return m
+
+
+def dump_desc(m: Mesh, dump_type: int, strain_it: int, out: np.ndarray | None, capacity: int,
+              ibeg: int = 0, iend: int = 4, jbeg: int = 0, jend: int = 4) -> _abi.DumpDesc:
+    """An axg_dump_desc for the mesh's pointwise arrays; keeps them alive."""
+    dd = _abi.DumpDesc()
+    dd.dump_type, dd.strain_it = dump_type, strain_it
+    dd.ibeg, dd.iend, dd.jbeg, dd.jend = ibeg, iend, jbeg, jend
+    keep = []
+    for nm in PW_SOLID + PW_FLUID:
+        a = m.pointwise.get(nm)
+        if a is not None:
+            a = np.asfortranarray(a, dtype=F32)
+            keep.append(a)
+        setattr(dd, nm, _abi.ptr(a, C.c_float))
+    dd.out = _abi.ptr(out, C.c_float)
+    dd.capacity = capacity
+    dd._keep = keep  # type: ignore[attr-defined]
+    return dd

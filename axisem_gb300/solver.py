@@ -177,6 +177,38 @@ class Solver:
         """Kahan-compensated predictor / corrector (axg_set_compensated)."""
         _check(self.lib, self.h, self.lib.axg_set_compensated(self.h, int(bool(on))))
 
+    def set_wavefield_dump(self, dump_type: int, strain_it: int = 1, capacity: int = 1, ibeg: int = 0,
+                           iend: int = 4, jbeg: int = 0, jend: int = 4, out: np.ndarray | None = None):
+        """axg_set_wavefield_dump with the mesh's data_pointwise arrays
+        (mesh.add_pointwise).  Returns the snapshot buffer, (capacity,
+        floats_per_snapshot) float32 (`out` if given: page-locked memory lets
+        the copies overlap the steps)."""
+        from .mesh import dump_desc
+        probe = np.zeros(1, dtype=np.float32)
+        dd = dump_desc(self.mesh, dump_type, strain_it, probe, 1, ibeg, iend, jbeg, jend)
+        _check(self.lib, self.h, self.lib.axg_set_wavefield_dump(self.h, C.byref(dd)))
+        if dump_type == _abi.DUMP_NONE:
+            self._dump = None
+            return None
+        floats = self.dump_layout()[2]
+        if out is None:
+            out = np.zeros((capacity, floats), dtype=np.float32)
+        if out.dtype != np.float32 or not out.flags.c_contiguous or out.size < capacity * floats:
+            raise ValueError(f"out must be C-contiguous float32 with room for {capacity} x {floats}")
+        dd = dump_desc(self.mesh, dump_type, strain_it, out, capacity, ibeg, iend, jbeg, jend)
+        _check(self.lib, self.h, self.lib.axg_set_wavefield_dump(self.h, C.byref(dd)))
+        self._dump = (out, dd)
+        return out
+
+    def dump_layout(self):
+        """(solid fields, fluid fields, floats per snapshot, field names)."""
+        ns, nf, fl = C.c_int32(), C.c_int32(), C.c_int64()
+        names = C.create_string_buffer(4096)
+        _check(self.lib, self.h, self.lib.axg_wavefield_dump_layout(self.h, C.byref(ns), C.byref(nf), C.byref(fl),
+                                                                    names, len(names)))
+        nm = names.value.decode()
+        return ns.value, nf.value, fl.value, nm.split(",") if nm else []
+
     def set_tuning(self, patch_elems: int = 0, steps_per_graph: int = 0):
         _check(self.lib, self.h, self.lib.axg_set_tuning(self.h, patch_elems, steps_per_graph))
 

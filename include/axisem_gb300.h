@@ -364,6 +364,58 @@ int axg_get_solid_colouring(axg_handle *h, int32_t *patch_of_elem, int32_t *colo
  * (device_bytes = 0).  Returns AXG_ERR_BAD_DESC with the violated invariant. */
 int axg_plan_check(const axg_mesh_desc *desc, int32_t patch_elems, int32_t growth, axg_info *info);
 
+/* Kernel wavefield dumps (dump_wavefields / dump_type of inparam_advanced;
+ * dump_stuff, SOLVER/time_evol_wave.F90:1201-1249).  After every step with
+ * mod(iter, strain_it) == 0 the fields of `dump_type` are computed on the GPU
+ * from the state at the end of the step and copied into snapshot
+ * iter / strain_it - 1 of `out`, while the following steps run.  A snapshot
+ * holds the solid fields, then the fluid fields (none without a fluid); each
+ * field covers the points (ibeg:iend, jbeg:jend) of every element in the
+ * reference's element order, i.e. pack(f(ibeg:iend, jbeg:jend, :)) as
+ * nc_dump_field_solid/fluid receive it (SOLVER/wavefields_io.f90:787-836).
+ * axg_wavefield_dump_layout names the fields with the reference's variable
+ * names.  Fields per type (p components and the last two strain terms only for
+ * the dipole and quadrupole):
+ *   DISPL_ONLY   dump_disp_global:  disp_sol_s, _p, _z (dipole in s, phi);
+ *                                   disp_flu_s, _p (zero), _z = grad(chi) / rho
+ *   STRAIN_ONLY  compute_strain:    strain_dsus, strain_dsuz, strain_dpup,
+ *                                   straintrace, strain_dsup, strain_dzup (_sol, _flu)
+ *   DISPL_VELO   dump_disp + dump_velo_dchi: disp_sol_s, _p, _z and velo_sol_s,
+ *                                   _p, _z as stored; chi_flu, dchi_flu
+ *   FULLFIELDS   compute_strain + dump_velo_global: the strain terms, then
+ *                                   velo_sol_s, _p, _z; velo_flu_s, _p (zero), _z
+ * The values of compute_strain's fields are the reference's, the kernel
+ * wavefield point mapping of its NetCDF 'displ_only' / 'strain_only' output
+ * (kwf_mapping_*) is left to the caller.  `out` should be page-locked host
+ * memory (cudaHostAlloc / cudaHostRegister) for the copies to overlap the
+ * steps.  No counterpart needed for the ABI of the time loop itself. */
+enum axg_dump_type {
+  AXG_DUMP_NONE = 0,
+  AXG_DUMP_DISPL_ONLY,
+  AXG_DUMP_STRAIN_ONLY,
+  AXG_DUMP_DISPL_VELO,
+  AXG_DUMP_FULLFIELDS
+};
+
+typedef struct axg_dump_desc {
+  int32_t dump_type;                 /* AXG_DUMP_*; AXG_DUMP_NONE switches the dumps off */
+  int32_t strain_it;                 /* dump interval in steps (>= 1) */
+  int32_t ibeg, iend, jbeg, jend;    /* points of each element, 0 <= beg <= end <= 4 */
+  /* data_pointwise, (0:4,0:4,nel) column-major; the fluid ones only with a fluid */
+  const float *DsDeta_over_J_sol, *DzDeta_over_J_sol, *DsDxi_over_J_sol, *DzDxi_over_J_sol;
+  const float *inv_s_solid;
+  const float *DsDeta_over_J_flu, *DzDeta_over_J_flu, *DsDxi_over_J_flu, *DzDxi_over_J_flu;
+  const float *inv_s_fluid, *inv_rho_fluid;
+  float *out;                        /* capacity snapshots of floats_per_snapshot floats */
+  int64_t capacity;
+} axg_dump_desc;
+
+int axg_set_wavefield_dump(axg_handle *h, const axg_dump_desc *dd);
+/* Fields per snapshot and their names, comma-separated into `names` (NUL
+ * terminated, truncated to names_cap bytes; names may be NULL). */
+int axg_wavefield_dump_layout(axg_handle *h, int32_t *n_solid_fields, int32_t *n_fluid_fields,
+                              int64_t *floats_per_snapshot, char *names, int32_t names_cap);
+
 /* Event-timed repeat of axg_stiffness_assembled_device: n launches, returns the
  * average device time in ms of one stiffness+assembly (all colour launches). */
 int axg_time_stiffness(axg_handle *h, int32_t n, float *ms_avg);

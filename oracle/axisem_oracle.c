@@ -25,6 +25,11 @@
  *   nc_compute_recfile_seis_bare                            SOLVER/seismograms.f90:783-820
  *   sf_time_loop_newmark                                    SOLVER/time_evol_wave.F90:264-502
  *   symplectic_time_loop (elastic)                          SOLVER/time_evol_wave.F90:516-742
+ *   axisym_gradient_solid / _fluid, f_over_s_solid / _fluid,
+ *   dsdf_solid_allaxis / dsdf_fluid_allaxis                 SOLVER/pointwise_derivatives.f90:130-178,329-545
+ *   compute_strain                                          SOLVER/time_evol_wave.F90:1264-1410
+ *   dump_disp_global, dump_velo_global, dump_disp,
+ *   dump_velo_dchi                                          SOLVER/wavefields_io.f90:840-1115
  *
  * Compiled twice: REAL=float (the reference's realkind=sp build) and
  * REAL=double (realkind=dp, the FP64 oracle).  Mixed-precision expressions
@@ -1133,4 +1138,200 @@ void ORC(gradient_cg4_all)(const axg_mesh_desc *d, const REAL *f, REAL *out) {
     }
   }
   free(ax);
+}
+
+
+/* ------------------------------------------------- kernel wavefield dumps */
+
+/* axisym_gradient_solid / _fluid on one element
+ * (SOLVER/pointwise_derivatives.f90:329-365, 509-545):
+ *   mxm1 = G1T f (axial element) or G2T f, mxm2 = f G2,
+ *   d/ds = dzdeta * mxm1 + dzdxi * mxm2,  d/dz = dsdeta * mxm1 + dsdxi * mxm2
+ * (the reference's names of the mapping terms). */
+typedef struct pw_el {
+  const float *dsdeta, *dzdeta, *dsdxi, *dzdxi, *inv_s;
+} pw_el;
+
+static void grad_el(const spec *s, int axis, const pw_el *w, const REAL *f, REAL *gs, REAL *gz) {
+  mat5 m1, m2;
+  mxm_4(axis ? s->G1T : s->G2T, f, m1);
+  mxm_4(f, s->G2, m2);
+  for (int k = 0; k < 25; ++k) {
+    gs[k] = (REAL)w->dzdeta[k] * m1[k] + (REAL)w->dzdxi[k] * m2[k];
+    gz[k] = (REAL)w->dsdeta[k] * m1[k] + (REAL)w->dsdxi[k] * m2[k];
+  }
+}
+
+/* f_over_s_solid / _fluid on one element (SOLVER/pointwise_derivatives.f90:
+ * 130-178): inv_s * f, and at the axis (ipol = 0 of an axial element)
+ * L'Hospital's f/s = df/ds (dsdf_*_allaxis, always with G1T, :480-505). */
+static void f_over_s_el(const spec *s, int axis, const pw_el *w, const REAL *f, REAL *o) {
+  for (int k = 0; k < 25; ++k) o[k] = (REAL)w->inv_s[k] * f[k];
+  if (!axis) return;
+  mat5 m1, m2;
+  mxm_4(s->G1T, f, m1);
+  mxm_4(f, s->G2, m2);
+  for (int j = 0; j < 5; ++j) o[5 * j] = (REAL)w->dzdeta[5 * j] * m1[5 * j] + (REAL)w->dzdxi[5 * j] * m2[5 * j];
+}
+
+/* compute_strain for one element of the solid (SOLVER/time_evol_wave.F90:
+ * 1286-1345) or, from the fluid displacement (usz_s, usz_z), of the fluid
+ * (:1347-1408): dsus, dsuz, dpup, straintrace[, dsup, dzup] into o[0..5]. */
+static void strain_el(const spec *s, int axis, const pw_el *w, int pole, int fluid, const REAL *u1, const REAL *u2,
+                      const REAL *u3, REAL *o[6]) {
+  mat5 us, g1, g2, h1, h2, n1, n2, buff, t, t2, p1, p2;
+  for (int k = 0; k < 25; ++k) us[k] = (!fluid && pole == AXG_DIPOLE) ? u1[k] + u2[k] : u1[k];
+  grad_el(s, axis, w, us, g1, g2);  /* 1: dsus, 2: dzus */
+  for (int k = 0; k < 25; ++k) o[0][k] = g1[k];
+  grad_el(s, axis, w, u3, h1, h2);  /* axisym_gradient_*_add: 1: dzus + dsuz, 2: dsus + dzuz */
+  for (int k = 0; k < 25; ++k) {
+    n1[k] = g2[k] + h1[k];
+    n2[k] = g1[k] + h2[k];
+    n1[k] = n1[k] / (REAL)2;
+    o[1][k] = n1[k];
+  }
+  if (fluid) {
+    f_over_s_el(s, axis, w, u1, buff);                         /* us / s */
+    for (int k = 0; k < 25; ++k) {
+      o[2][k] = buff[k];
+      o[3][k] = buff[k] + n2[k];
+    }
+    if (pole == AXG_MONOPOLE) return;
+    f_over_s_el(s, axis, w, u3, t);                            /* uz / s */
+    for (int k = 0; k < 25; ++k) {
+      o[4][k] = pole == AXG_DIPOLE ? (-buff[k]) / (REAL)2 : -buff[k];
+      o[5][k] = pole == AXG_DIPOLE ? t[k] / (REAL)2 : -t[k];
+    }
+    return;
+  }
+  if (pole == AXG_MONOPOLE) {
+    f_over_s_el(s, axis, w, u1, buff);
+  } else if (pole == AXG_DIPOLE) {
+    f_over_s_el(s, axis, w, u2, t);
+    for (int k = 0; k < 25; ++k) buff[k] = (REAL)2 * t[k];
+  } else {
+    for (int k = 0; k < 25; ++k) t[k] = u1[k] - (REAL)2 * u2[k];
+    f_over_s_el(s, axis, w, t, buff);
+  }
+  for (int k = 0; k < 25; ++k) {
+    o[2][k] = buff[k];
+    o[3][k] = buff[k] + n2[k];
+  }
+  if (pole == AXG_DIPOLE) {
+    for (int k = 0; k < 25; ++k) t2[k] = u1[k] - u2[k];
+    grad_el(s, axis, w, t2, p1, p2);                           /* dsup, dzup */
+    f_over_s_el(s, axis, w, u2, t);
+    for (int k = 0; k < 25; ++k) o[4][k] = -t[k] - p1[k] / (REAL)2;
+    f_over_s_el(s, axis, w, u3, t);
+    for (int k = 0; k < 25; ++k) o[5][k] = -(t[k] + p2[k]) / (REAL)2;
+  } else if (pole == AXG_QUADPOLE) {
+    grad_el(s, axis, w, u2, p1, p2);
+    for (int k = 0; k < 25; ++k) t2[k] = u1[k] + u2[k] / (REAL)2;
+    f_over_s_el(s, axis, w, t2, t);
+    for (int k = 0; k < 25; ++k) o[4][k] = -t[k] - p1[k] / (REAL)2;
+    f_over_s_el(s, axis, w, u3, t);
+    for (int k = 0; k < 25; ++k) o[5][k] = -t[k] - p2[k] / (REAL)2;
+  }
+}
+
+/* pack(f(ibeg:iend, jbeg:jend, e)) of one element into field `fld` */
+static void put_el(const axg_dump_desc *dd, REAL *out, int64_t nel, int64_t e, int64_t fld, const REAL *f) {
+  const int ni = dd->iend - dd->ibeg + 1, nj = dd->jend - dd->jbeg + 1;
+  REAL *o = out + (fld * nel + e) * (int64_t)(ni * nj);
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i < ni; ++i) o[i + ni * j] = f[(dd->ibeg + i) + 5 * (dd->jbeg + j)];
+}
+
+/* One snapshot of dump_stuff's fields (the layout of axg_wavefield_dump_layout)
+ * from the element-local state; returns the number of fields written. */
+int ORC(wavefield_dump)(const axg_mesh_desc *d, const axg_dump_desc *dd, const REAL *disp, const REAL *velo,
+                        const REAL *chi, const REAL *dchi, REAL *out) {
+  spec s;
+  load_spec(d, &s);
+  const int pole = d->src_type, type = dd->dump_type;
+  const int nonmono = pole != AXG_MONOPOLE;
+  const int64_t nes = d->nel_solid, nef = d->nel_fluid;
+  const int ns = type == AXG_DUMP_STRAIN_ONLY ? (nonmono ? 6 : 4)
+                 : type == AXG_DUMP_FULLFIELDS ? (nonmono ? 6 : 4) + (nonmono ? 3 : 2)
+                 : type == AXG_DUMP_DISPL_VELO ? 2 * (nonmono ? 3 : 2)
+                                                : (nonmono ? 3 : 2);
+  const int nf = nef <= 0 ? 0
+                 : type == AXG_DUMP_STRAIN_ONLY ? (nonmono ? 6 : 4)
+                 : type == AXG_DUMP_FULLFIELDS ? (nonmono ? 6 : 4) + (nonmono ? 3 : 2)
+                 : type == AXG_DUMP_DISPL_VELO ? 2
+                                                : (nonmono ? 3 : 2);
+  const int np = (dd->iend - dd->ibeg + 1) * (dd->jend - dd->jbeg + 1);
+  REAL *fout = out + (int64_t)ns * nes * np;
+  unsigned char *axs = axis_flags((int)nes, d->naxel_solid, d->ax_el_solid);
+  mat5 buf[6], v3[3];
+  REAL *o[6] = {buf[0], buf[1], buf[2], buf[3], buf[4], buf[5]};
+  for (int64_t e = 0; e < nes; ++e) {
+    const int64_t off = 25 * e;
+    const pw_el w = {dd->DsDeta_over_J_sol + off, dd->DzDeta_over_J_sol + off, dd->DsDxi_over_J_sol + off,
+                     dd->DzDxi_over_J_sol + off, dd->inv_s_solid + off};
+    const REAL *u1 = disp + off, *u2 = disp + 25 * nes + off, *u3 = disp + 50 * nes + off;
+    const REAL *vv1 = velo + off, *vv2 = velo + 25 * nes + off, *vv3 = velo + 50 * nes + off;
+    int fld = 0;
+    /* the s, phi, z components as dump_*_global write them (dipole: s, phi from +, -) */
+    const REAL *vecs[2][3] = {{u1, u2, u3}, {vv1, vv2, vv3}};
+    if (type == AXG_DUMP_STRAIN_ONLY || type == AXG_DUMP_FULLFIELDS) {
+      strain_el(&s, axs[e], &w, pole, 0, u1, u2, u3, o);
+      for (int q = 0; q < (nonmono ? 6 : 4); ++q) put_el(dd, out, nes, e, fld++, o[q]);
+    }
+    for (int which = 0; which < 2; ++which) {
+      const int want = which == 0 ? (type == AXG_DUMP_DISPL_ONLY || type == AXG_DUMP_DISPL_VELO)
+                                  : (type == AXG_DUMP_DISPL_VELO || type == AXG_DUMP_FULLFIELDS);
+      if (!want) continue;
+      const REAL **x = vecs[which];
+      const int global = type != AXG_DUMP_DISPL_VELO;  /* dump_*_global transform the dipole */
+      for (int k = 0; k < 25; ++k) {
+        v3[0][k] = (global && pole == AXG_DIPOLE) ? x[0][k] + x[1][k] : x[0][k];
+        v3[1][k] = (global && pole == AXG_DIPOLE) ? x[0][k] - x[1][k] : x[1][k];
+        v3[2][k] = x[2][k];
+      }
+      put_el(dd, out, nes, e, fld++, v3[0]);
+      if (nonmono) put_el(dd, out, nes, e, fld++, v3[1]);
+      put_el(dd, out, nes, e, fld++, v3[2]);
+    }
+  }
+  free(axs);
+  if (nef > 0) {
+    unsigned char *axf = axis_flags((int)nef, d->naxel_fluid, d->ax_el_fluid);
+    mat5 c1, c2, zero;
+    for (int k = 0; k < 25; ++k) zero[k] = 0;
+    for (int64_t e = 0; e < nef; ++e) {
+      const int64_t off = 25 * e;
+      const pw_el w = {dd->DsDeta_over_J_flu + off, dd->DzDeta_over_J_flu + off, dd->DsDxi_over_J_flu + off,
+                       dd->DzDxi_over_J_flu + off, dd->inv_s_fluid + off};
+      const float *irho = dd->inv_rho_fluid + off;
+      int fld = 0;
+      if (type == AXG_DUMP_DISPL_VELO) {
+        put_el(dd, fout, nef, e, fld++, chi + off);
+        put_el(dd, fout, nef, e, fld++, dchi + off);
+        continue;
+      }
+      if (type == AXG_DUMP_STRAIN_ONLY || type == AXG_DUMP_FULLFIELDS) {
+        mat5 us, uz;
+        grad_el(&s, axf[e], &w, chi + off, c1, c2);            /* usz = grad(chi) / rho */
+        for (int k = 0; k < 25; ++k) {
+          us[k] = c1[k] * (REAL)irho[k];
+          uz[k] = c2[k] * (REAL)irho[k];
+        }
+        strain_el(&s, axf[e], &w, pole, 1, us, zero, uz, o);
+        for (int q = 0; q < (nonmono ? 6 : 4); ++q) put_el(dd, fout, nef, e, fld++, o[q]);
+      }
+      if (type == AXG_DUMP_DISPL_ONLY || type == AXG_DUMP_FULLFIELDS) {
+        grad_el(&s, axf[e], &w, type == AXG_DUMP_DISPL_ONLY ? chi + off : dchi + off, c1, c2);
+        for (int k = 0; k < 25; ++k) {
+          v3[0][k] = (REAL)irho[k] * c1[k];
+          v3[2][k] = (REAL)irho[k] * c2[k];
+        }
+        put_el(dd, fout, nef, e, fld++, v3[0]);
+        if (nonmono) put_el(dd, fout, nef, e, fld++, zero);
+        put_el(dd, fout, nef, e, fld++, v3[2]);
+      }
+    }
+    free(axf);
+  }
+  return ns + nf;
 }

@@ -73,6 +73,22 @@ def gradient_cg4(mesh, f_elem: np.ndarray, dtype=np.float64) -> np.ndarray:
     return out
 
 
+def wavefield_dump(mesh, dd, disp, velo, chi, dchi, dtype=np.float64) -> np.ndarray:
+    """One snapshot of dump_stuff's fields (compute_strain, dump_*_global,
+    SOLVER/time_evol_wave.F90:1201-1410, SOLVER/wavefields_io.f90:840-1115)
+    from element-local state, in the layout of axg_wavefield_dump_layout;
+    dd is the axg_dump_desc (its out and capacity are not used)."""
+    tag, ct, nt = _t(dtype)
+    d = mesh.desc()
+    np_el = (dd.iend - dd.ibeg + 1) * (dd.jend - dd.jbeg + 1)
+    out = np.zeros(12 * np_el * (mesh.nel_solid + max(mesh.nel_fluid, 0)), dtype=nt)
+    args = [np.asfortranarray(a, dtype=nt) for a in (disp, velo, chi, dchi)]
+    fn = getattr(lib(), f"orc_{tag}_wavefield_dump")
+    fn.restype = C.c_int
+    nfld = fn(C.byref(d), C.byref(dd), *[_p(a, ct) for a in args], _p(out, ct))
+    return out, nfld
+
+
 class TimeLoop:
     """sf_time_loop_newmark on element-local state, as the reference holds it."""
 
