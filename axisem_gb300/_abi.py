@@ -139,7 +139,7 @@ class Info(C.Structure):
         ("patch_elems_solid", C.c_int32), ("growth_solid", C.c_int32),
         ("patch_elems_fluid", C.c_int32), ("growth_fluid", C.c_int32),
         ("ctas_per_sm_force", C.c_int32), ("ctas_per_sm_step", C.c_int32),
-        ("mesh_bytes", C.c_int64),
+        ("mesh_bytes", C.c_int64), ("steps_per_graph", C.c_int32),
     ]
 
 
@@ -166,6 +166,7 @@ SIGNATURES = {
     "axg_run_async": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "axg_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "axg_wait": (C.c_int, [C.c_void_p]),
+    "axg_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "axg_set_wavefield_dump": (C.c_int, [C.c_void_p, C.POINTER(DumpDesc)]),
     "axg_wavefield_dump_layout": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                             C.POINTER(C.c_int64), C.c_char_p, C.c_int32]),

@@ -1583,6 +1583,10 @@ int check_flags(axg_handle *h) {
 // 3.21 against 2.95 ms for a 1024 x 1024 quadrupole step, the copy engines
 // moving ~200 GB/s each way; 8 or 16 chunks gained nothing over 4.)
 constexpr int kGvecChunks = 4;
+
+// a step counter set on the stream, without a host synchronisation
+__global__ void set_counter_kernel(int32_t *ctr, int32_t v) { *ctr = v; }
+
 static_assert(sizeof(axg_handle::ev_io) / sizeof(cudaEvent_t) == kGvecChunks + 1, "one event per chunk + one");
 
 // u[c][new_of_old[g]] = stage[c][g], g in [a, b)
@@ -1924,6 +1928,87 @@ int axg_set_tuning(axg_handle *h, int32_t patch_elems, int32_t steps_per_graph) 
   return AXG_OK;
 }
 
+int axg_autotune(axg_handle *h, int32_t *chosen) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  if (h->pending) return fail(h, AXG_ERR_BAD_ARG, "the handle has queued steps");
+  // every device array a step writes: saved, then restored
+  std::vector<std::pair<void *, size_t>> st;
+  auto add = [&](void *p, size_t bytes) {
+    if (p && bytes) st.emplace_back(p, bytes);
+  };
+  const size_t gs = h->nglob_s * sizeof(float), gf = std::max<int64_t>(h->nglob_f, 0) * sizeof(float);
+  for (int c = 0; c < 3; ++c) {
+    add(h->su[c], gs), add(h->sv[c], gs), add(h->sa[c], gs), add(h->sf[c], gs);
+    add(h->cu_s[c], gs), add(h->cv_s[c], gs);
+  }
+  add(h->fu, gf), add(h->fv, gf), add(h->fa, gf), add(h->ff, gf), add(h->cu_f, gf), add(h->cv_f, gf);
+  if (h->anel) add(h->an.state, (size_t)h->nel_s * h->an.state_stride * sizeof(float));
+  add(h->rec, (size_t)h->nseismo * 3 * std::max(h->num_rec, 1) * sizeof(float));
+  add(h->iter, 4 * sizeof(int32_t));
+  size_t total = 0;
+  for (auto &p : st) total += (p.second + 255) / 256 * 256;
+  char *save = nullptr;
+  CK(cudaMallocAsync((void **)&save, total, h->stream));
+  size_t off = 0;
+  for (auto &p : st) {
+    CK(cudaMemcpyAsync(save + off, p.first, p.second, cudaMemcpyDeviceToDevice, h->stream));
+    off += (p.second + 255) / 256 * 256;
+  }
+  int best = h->steps_per_graph, rc = AXG_OK;
+  float best_ms = 0.f;
+  for (int k = 2; k <= 64 && rc == AXG_OK; k *= 2) {
+    // one untimed launch, then `reps` launches of at least 256 steps in all;
+    // the step counter restarts at 1 whenever the next launch would pass niter
+    const int per_run = h->niter / k;  // launches from iteration 1 within niter
+    if (per_run < 1) break;
+    const int reps = std::max(1, 256 / k);
+    cudaGraphExec_t g = nullptr;
+    if ((rc = build_graph_into(h, k, &g))) break;
+    float ms = 0.f;
+    set_counter_kernel<<<1, 1, 0, h->stream>>>(h->iter, 1);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGraphLaunch(g, h->stream);
+    int in_run = 1;
+    if (e == cudaSuccess) e = cudaEventRecord(h->ev0, h->stream);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+      if (in_run == per_run) {
+        set_counter_kernel<<<1, 1, 0, h->stream>>>(h->iter, 1);
+        e = cudaGetLastError();
+        in_run = 0;
+      }
+      if (e == cudaSuccess) e = cudaGraphLaunch(g, h->stream);
+      ++in_run;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(h->ev1, h->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(h->ev1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    cudaGraphExecDestroy(g);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(h, e, "axg_autotune");
+      break;
+    }
+    const float per_step = ms / (reps * k);
+    if (best_ms == 0.f || per_step < best_ms) {
+      best_ms = per_step;
+      best = k;
+    }
+  }
+  off = 0;
+  for (auto &p : st) {  // the solve's state as it was
+    CK(cudaMemcpyAsync(p.first, save + off, p.second, cudaMemcpyDeviceToDevice, h->stream));
+    off += (p.second + 255) / 256 * 256;
+  }
+  CK(cudaFreeAsync(save, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (rc) return rc;
+  if (best != h->steps_per_graph) {
+    h->steps_per_graph = best;
+    drop_graphs(h);
+  }
+  if (chosen) *chosen = best;
+  return AXG_OK;
+}
+
 int axg_set_compensated(axg_handle *h, int32_t on) {
   if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
   if (on && !h->cu_s[0]) {
@@ -2020,6 +2105,7 @@ int axg_get_info(axg_handle *h, axg_info *info) {
   info->growth_solid = h->ps.growth;
   info->patch_elems_fluid = h->pf.patch_elems;
   info->growth_fluid = h->pf.growth;
+  info->steps_per_graph = h->steps_per_graph;
   info->mesh_bytes = h->mesh ? h->mesh->bytes : 0;
   info->ctas_per_sm_force = h->solid_ctas / std::max(h->num_sms, 1);
   info->ctas_per_sm_step = h->solid_ctas_step / std::max(h->num_sms, 1);

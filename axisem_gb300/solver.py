@@ -209,6 +209,13 @@ class Solver:
         nm = names.value.decode()
         return ns.value, nf.value, fl.value, nm.split(",") if nm else []
 
+    def autotune(self) -> int:
+        """axg_autotune: the measured steps per CUDA graph (the solve's state
+        is left as it was)."""
+        k = C.c_int32()
+        _check(self.lib, self.h, self.lib.axg_autotune(self.h, C.byref(k)))
+        return k.value
+
     def set_tuning(self, patch_elems: int = 0, steps_per_graph: int = 0):
         _check(self.lib, self.h, self.lib.axg_set_tuning(self.h, patch_elems, steps_per_graph))
 

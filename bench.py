@@ -266,12 +266,13 @@ def run_gpu(args):
     if prof.exists():
         traffic = json.loads(prof.read_text()).get("dram_bytes_per_step")
 
-    timeloop = timeloop_anel = timeloop_comp = None
+    timeloop = timeloop_anel = timeloop_comp = timeloop_dumps = None
     if args.timeloop_steps > 0:
         s.close()
         timeloop = run_timeloop(args, pole, ws, rank)
         timeloop_anel = run_timeloop(args, pole, ws, rank, anel=True)
         timeloop_comp = run_timeloop(args, pole, ws, rank, compensated=True)
+        timeloop_dumps = run_timeloop_dumps(args, pole, ws, rank)
 
     serving = run_serving(args) if args.serve_requests > 0 else None
 
@@ -302,6 +303,7 @@ def run_gpu(args):
         "timeloop": timeloop,
         "timeloop_anel": timeloop_anel,
         "timeloop_compensated": timeloop_comp,
+        "timeloop_dumps": timeloop_dumps,
         "serving": serving,
         "clocks": clocks,
         "gpu_launches": int(args.steps * info["kernels_per_force"]),
@@ -351,15 +353,15 @@ def run_timeloop(args, pole, ws, rank, anel=False, compensated=False):
     from axisem_gb300.solver import Solver
     n = args.size
     nsteps = args.timeloop_steps
-    warm = 16
-    m = coupled_mesh(n, 3 * n // 4, n // 4, pole, niter=warm + nsteps, seed=5 + rank, num_rec=200,
+    m = coupled_mesh(n, 3 * n // 4, n // 4, pole, niter=64 + nsteps, seed=5 + rank, num_rec=200,
                      seis_it=4, deltat=2e-6, terms="pole")
     if anel:
         m = add_attenuation(m, n_sls=5, seed=77 + rank)
     s = Solver(m)
-    s.set_tuning(steps_per_graph=16)
     if compensated:
         s.set_compensated(True)
+    spg = s.autotune()   # measured steps per CUDA graph
+    warm = max(16, spg)  # the warm-up instantiates the step graph
     s.run(1, warm)
     torch.cuda.synchronize()
     barrier(ws)
@@ -381,8 +383,54 @@ def run_timeloop(args, pole, ws, rank, anel=False, compensated=False):
                     + (", compensated (Kahan) time integration" if compensated else ""),
             "algorithmic_bytes_per_step": nb, "achieved_gbs": nb / dt / 1e9,
             "frac_of_hbm": nb / dt / 1e9 / peak, "kernels_per_step": info["kernels_per_step"],
-            "solid_ctas_per_sm": info["ctas_per_sm_step"],
+            "solid_ctas_per_sm": info["ctas_per_sm_step"], "steps_per_graph": spg,
             "finite": bool(np.isfinite(rec).all())}
+
+
+def run_timeloop_dumps(args, pole, ws, rank, strain_it=8):
+    """The elastic time loop of run_timeloop without and with kernel wavefield
+    dumps (axg_set_wavefield_dump: displ_only and strain_only every strain_it
+    steps into page-locked host memory): the cost of a snapshot, whose
+    device-to-host copy overlaps the following steps."""
+    import torch
+    from axisem_gb300 import _abi
+    from axisem_gb300.mesh import add_pointwise, coupled_mesh
+    from axisem_gb300.solver import Solver
+    n, nsteps, warm = args.size, args.timeloop_steps, 16
+    m = add_pointwise(coupled_mesh(n, 3 * n // 4, n // 4, pole, niter=warm + nsteps, seed=5 + rank, num_rec=200,
+                                   seis_it=4, deltat=2e-6, terms="pole"))
+    out = {"strain_it": strain_it, "steps": nsteps}
+    s = Solver(m)
+    s.set_tuning(steps_per_graph=16)
+
+    def timed():
+        s.reset()
+        s.run(1, warm)
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        s.run(warm + 1, nsteps)
+        torch.cuda.synchronize()
+        return max_over_ranks((time.perf_counter() - t0) / nsteps, ws)
+
+    base = timed()
+    out["plain_ms_per_step"] = base * 1e3
+    cap = (warm + nsteps) // strain_it
+    for name, t in (("displ_only", _abi.DUMP_DISPL_ONLY), ("strain_only", _abi.DUMP_STRAIN_ONLY)):
+        s.set_wavefield_dump(t, strain_it, capacity=1)
+        floats = s.dump_layout()[2]
+        buf = torch.empty((cap, floats), dtype=torch.float32, pin_memory=True).numpy()
+        s.set_wavefield_dump(t, strain_it, capacity=cap, out=buf)
+        dt = timed()
+        snaps = nsteps // strain_it
+        out[name] = {"ms_per_step": dt * 1e3, "snapshot_bytes": floats * 4,
+                     "ms_per_snapshot": (dt - base) * nsteps / snaps * 1e3,
+                     "snapshot_gbs": floats * 4 * snaps / (dt * nsteps) / 1e9,
+                     "finite": bool(np.isfinite(buf).all())}
+        s.set_wavefield_dump(_abi.DUMP_NONE)
+        del buf
+    s.close()
+    return out
 
 
 def run_serving(args):

@@ -244,6 +244,15 @@ int axg_download_gvec_force(axg_handle *h, float *f_gvec);
  * handle's value. */
 int axg_set_tuning(axg_handle *h, int32_t patch_elems, int32_t steps_per_graph);
 
+/* Measured choice of the steps per CUDA graph: the handle's step (its scheme
+ * and modes as set) is timed with CUDA events in graphs of 2, 4, ..., 64
+ * steps (those that fit in niter), from a saved copy of the solve's state
+ * that is restored afterwards, so the solve continues as if untouched.  The
+ * fastest becomes the handle's steps_per_graph (*chosen).  Together with the
+ * planner's tuner of the patch shape (axg_create), this is the autotuner of
+ * the launch shapes. */
+int axg_autotune(axg_handle *h, int32_t *chosen);
+
 /* A further solve on the mesh of an existing handle (serving: meshes stay
  * resident, solves come and go).  `desc` must describe the same mesh -- sizes,
  * pole type, global numbering, axial elements, attenuation layout are
@@ -347,6 +356,7 @@ typedef struct axg_info {
   int32_t patch_elems_fluid, growth_fluid;
   int32_t ctas_per_sm_force, ctas_per_sm_step;  /* resident solid-kernel CTAs per SM */
   int64_t mesh_bytes;                 /* part of device_bytes shared by the handles of one mesh */
+  int32_t steps_per_graph;            /* steps per CUDA graph (axg_set_tuning / axg_autotune) */
 } axg_info;
 int axg_get_info(axg_handle *h, axg_info *info);
 
@@ -388,7 +398,7 @@ int axg_plan_check(const axg_mesh_desc *desc, int32_t patch_elems, int32_t growt
  * wavefield point mapping of its NetCDF 'displ_only' / 'strain_only' output
  * (kwf_mapping_*) is left to the caller.  `out` should be page-locked host
  * memory (cudaHostAlloc / cudaHostRegister) for the copies to overlap the
- * steps.  No counterpart needed for the ABI of the time loop itself. */
+ * steps.  A dumping solve runs alone (not in a batch). */
 enum axg_dump_type {
   AXG_DUMP_NONE = 0,
   AXG_DUMP_DISPL_ONLY,
