@@ -1949,12 +1949,15 @@ int axg_autotune(axg_handle *h, int32_t *chosen) {
   for (auto &p : st) total += (p.second + 255) / 256 * 256;
   char *save = nullptr;
   CK(cudaMallocAsync((void **)&save, total, h->stream));
+  // from here on errors are collected, so that the state is restored and the
+  // scratch freed on every path
+  cudaError_t ce = cudaSuccess;
   size_t off = 0;
   for (auto &p : st) {
-    CK(cudaMemcpyAsync(save + off, p.first, p.second, cudaMemcpyDeviceToDevice, h->stream));
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(save + off, p.first, p.second, cudaMemcpyDeviceToDevice, h->stream);
     off += (p.second + 255) / 256 * 256;
   }
-  int best = h->steps_per_graph, rc = AXG_OK;
+  int best = h->steps_per_graph, rc = ce == cudaSuccess ? AXG_OK : cuda_fail(h, ce, "axg_autotune: saving the state");
   float best_ms = 0.f;
   for (int k = 2; k <= 64 && rc == AXG_OK; k *= 2) {
     // one untimed launch, then `reps` launches of at least 256 steps in all;
@@ -1994,13 +1997,16 @@ int axg_autotune(axg_handle *h, int32_t *chosen) {
     }
   }
   off = 0;
+  ce = cudaSuccess;
   for (auto &p : st) {  // the solve's state as it was
-    CK(cudaMemcpyAsync(p.first, save + off, p.second, cudaMemcpyDeviceToDevice, h->stream));
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(p.first, save + off, p.second, cudaMemcpyDeviceToDevice, h->stream);
     off += (p.second + 255) / 256 * 256;
   }
-  CK(cudaFreeAsync(save, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
+  const cudaError_t fe = cudaFreeAsync(save, h->stream);
+  if (ce == cudaSuccess) ce = fe;
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->stream);
   if (rc) return rc;
+  if (ce != cudaSuccess) return cuda_fail(h, ce, "axg_autotune: restoring the state");
   if (best != h->steps_per_graph) {
     h->steps_per_graph = best;
     drop_graphs(h);

@@ -29,10 +29,12 @@ def test_exports_every_declared_symbol(lib):
         assert n in _abi.SIGNATURES, f"{n} missing from the Python mirror"
 
 
-def test_header_struct_matches_mirror():
-    # every field of axg_mesh_desc appears in the ctypes mirror, in order
+@pytest.mark.parametrize("name,mirror", [("axg_mesh_desc", _abi.MeshDesc), ("axg_dump_desc", _abi.DumpDesc),
+                                         ("axg_info", _abi.Info)])
+def test_header_struct_matches_mirror(name, mirror):
+    # every field of the struct appears in the ctypes mirror, in order
     txt = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
-    body = txt[txt.index("typedef struct axg_mesh_desc {"):txt.index("} axg_mesh_desc;")]
+    body = txt[txt.index(f"typedef struct {name} {{"):txt.index(f"}} {name};")]
     fields = []
     for decl in body.split(";")[:-1]:
         decl = decl.split("{")[-1]
@@ -40,8 +42,7 @@ def test_header_struct_matches_mirror():
             nm = re.findall(r"\**\s*([A-Za-z_][A-Za-z0-9_]*)\s*(\[[^\]]*\])?\s*$", part.strip())
             if nm:
                 fields.append(nm[0][0])
-    mirror = [f for f, _ in _abi.MeshDesc._fields_]
-    assert fields == mirror
+    assert fields == [f for f, _ in mirror._fields_]
 
 
 def test_version_and_device_count(lib):
