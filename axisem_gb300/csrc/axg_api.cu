@@ -150,6 +150,8 @@ struct axg_handle {
   int nsls = 0;
   AnelArgs an{};
   std::vector<int32_t> slot_of_elem_s;  // solid element -> launch slot
+  int32_t *sym_gidx = nullptr;           // symplectic + attenuation: each launch slot's points
+  uint8_t *sym_axial = nullptr;          // and axis flag
   // kernel wavefield dumps (axg_set_wavefield_dump)
   std::vector<uint8_t> axial_s, axial_f;  // per element (reference order): on the axis
   struct Dump {
@@ -582,7 +584,9 @@ int prepare_solid_kernels(axg_handle *h) {
   int rc = prepare_solid_kernel<POLE, MODE_FORCE, false, false>(h, &h->solid_ctas);
   if (rc) return rc;
   int *c = &h->solid_ctas_step;
-  if (h->scheme != AXG_SCHEME_NEWMARK2) return prepare_solid_kernel<POLE, MODE_SYMPLECTIC, false, false>(h, c);
+  if (h->scheme != AXG_SCHEME_NEWMARK2)
+    return h->anel ? prepare_solid_kernel<POLE, MODE_SYMPLECTIC, true, false>(h, c)
+                   : prepare_solid_kernel<POLE, MODE_SYMPLECTIC, false, false>(h, c);
   if (h->anel) {
     return h->kahan ? prepare_solid_kernel<POLE, MODE_NEWMARK, true, true>(h, c)
                     : prepare_solid_kernel<POLE, MODE_NEWMARK, true, false>(h, c);
@@ -691,16 +695,22 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
 // per stage the drift (on the gathers), fluid stiffness and the coupling
 // into it, solid stiffness, the coupling into the solid, the kicks (by the
 // last writers); then the final drift and the seismograms.
-template <int POLE>
+template <int POLE, bool ANEL>
 void launch_solid_symplectic(axg_handle *h, cudaStream_t s, const StateArgs &st) {
   DomainArgs a = domain_args(h->ds, h->ps);
   for (int c = 0; c < h->ps.n_colours; ++c) {
     a.patch_begin = h->ps.colour_start[c];
     const int n = h->ps.colour_start[c + 1] - h->ps.colour_start[c];
-    solid_patch_kernel<POLE, MODE_SYMPLECTIC, false, false>
-        <<<std::min(n, h->solid_ctas_step), kThreads, solid_smem_bytes<POLE, MODE_SYMPLECTIC, false, false>(), s>>>(
+    solid_patch_kernel<POLE, MODE_SYMPLECTIC, ANEL, false>
+        <<<std::min(n, h->solid_ctas_step), kThreads, solid_smem_bytes<POLE, MODE_SYMPLECTIC, ANEL, false>(), s>>>(
             a, st, h->spec, n, h->an);
   }
+}
+
+template <int POLE>
+void launch_solid_symplectic(axg_handle *h, cudaStream_t s, const StateArgs &st) {
+  if (h->anel) launch_solid_symplectic<POLE, true>(h, s, st);
+  else launch_solid_symplectic<POLE, false>(h, s, st);
 }
 
 void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
@@ -741,6 +751,15 @@ void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
   StateArgs ss = solid_state(h), fs = fluid_state(h);
   const int64_t n = std::max(h->nglob_s, h->nel_f > 0 ? h->nglob_f : 0);
   drift_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ss, fs, h->sym_cd[h->nstages]);
+  if (h->anel) {  // the memory variables from the drifted displacement
+    const unsigned g = (unsigned)std::min<int64_t>((h->nel_s + kWarps - 1) / kWarps, 16 * (int64_t)h->num_sms);
+    if (h->pole == AXG_MONOPOLE)
+      anel_memvar_kernel<POLE_MONO><<<g, kThreads, 0, s>>>(h->an, h->sym_gidx, h->sym_axial, ss, h->nel_s, h->spec);
+    else if (h->pole == AXG_DIPOLE)
+      anel_memvar_kernel<POLE_DI><<<g, kThreads, 0, s>>>(h->an, h->sym_gidx, h->sym_axial, ss, h->nel_s, h->spec);
+    else
+      anel_memvar_kernel<POLE_QUAD><<<g, kThreads, 0, s>>>(h->an, h->sym_gidx, h->sym_axial, ss, h->nel_s, h->spec);
+  }
   receivers_kernel<<<1, 256, 0, s>>>(One<RecWork>{rec_work(h, ss), 1});
 }
 
@@ -2065,11 +2084,22 @@ int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages) 
     std::vector<double> cd, cv;
     const int n = symplectic_coefficients(scheme, cd, cv);
     if (n == 0) return fail(h, AXG_ERR_BAD_ARG, fmt("unknown time scheme %d", scheme));
-    if (h->anel || h->kahan || h->fluid_src || h->df.fsmask)
+    if (h->kahan || h->fluid_src || h->df.fsmask)
       return fail(h, AXG_ERR_UNSUPPORTED,
-                  "symplectic schemes: attenuation, the compensated mode, a fluid source and a fluid free surface "
-                  "are not supported");
+                  "symplectic schemes: the compensated mode, a fluid source and a fluid free surface are not "
+                  "supported");
     if (!stf_stages) return fail(h, AXG_ERR_BAD_ARG, "stf_stages is NULL");
+    if (h->anel && !h->sym_gidx) {  // per launch slot: the element's points and axis flag
+      std::vector<int32_t> g(25 * (size_t)h->nel_s);
+      std::vector<uint8_t> ax(h->nel_s);
+      for (int64_t e = 0; e < h->nel_s; ++e) {
+        const int64_t sl = h->slot_of_elem_s[e];
+        for (int k = 0; k < 25; ++k) g[25 * sl + k] = h->igloc_s[25 * e + k] - 1;
+        ax[sl] = h->axial_s[e];
+      }
+      int rc;
+      if ((rc = upload(h, &h->sym_gidx, g)) || (rc = upload(h, &h->sym_axial, ax))) return rc;
+    }
     h->sym_cd.resize(n + 1);
     h->sym_cv.resize(n);
     for (int i = 0; i <= n; ++i) h->sym_cd[i] = (float)(cd[i] * h->dt);
@@ -2085,7 +2115,7 @@ int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages) 
   if (rc) return rc;
   if (h->scheme) {
     h->kernels_per_step = (int64_t)h->nstages * (h->ps.n_colours + (h->nel_f > 0 ? h->pf.n_colours +
-                          (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0)) + 2;
+                          (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0)) + 2 + (h->anel ? 1 : 0);
   } else {
     h->kernels_per_step = h->ps.n_colours + 1 +
                           (h->nel_f > 0 ? h->pf.n_colours + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);

@@ -739,7 +739,7 @@ struct WarpIter {
 // from the gather to the last writer in shared memory.
 template <int POLE, int MODE, bool ANEL, bool KAHAN, class P>
 __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, const AnelArgs &an) {
-  static_assert(!ANEL || MODE == MODE_NEWMARK, "attenuation runs in the Newmark time loop only");
+  static_assert(!ANEL || MODE != MODE_FORCE, "attenuation runs in a time loop");
   static_assert(!P::kMany || (MODE == MODE_NEWMARK && !ANEL), "batches run the elastic Newmark step");
   static_assert(!KAHAN || MODE == MODE_NEWMARK, "the compensated mode is a Newmark time-loop mode");
   constexpr bool TL = MODE != MODE_FORCE;  // a time-loop mode
@@ -1036,10 +1036,12 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
             s_f[2][idx] += f2;
           }
         }
-        if (ANEL) {
+        if (ANEL && MODE == MODE_NEWMARK) {
           // memory variables of this step from the predicted, masked
           // displacement (time_step_memvars after pdistsum_solid in
-          // SOLVER/time_evol_wave.F90), then the element's state back to HBM
+          // SOLVER/time_evol_wave.F90), then the element's state back to HBM.
+          // (A symplectic stage only reads them: anel_memvar_kernel updates
+          // them once per step.)
           anel_memvar_step<POLE>(ablk, ablk + kAnelConst, scr + warp * 32, an, cg, kcg, lane, u, gx, ge);
           __syncwarp();
           const float4 *src4 = reinterpret_cast<const float4 *>(ablk + kAnelConst);
@@ -1161,6 +1163,49 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
     }
     __syncthreads();
     ++pcount;
+  }
+}
+
+// time_step_memvars (SOLVER/attenuation.f90:81-202) once per step of the
+// symplectic loop, after the final drift (SOLVER/time_evol_wave.F90:727-731):
+// one warp per element in launch order (the order of the attenuation data),
+// the masked displacement gathered from its points, the first-stage
+// derivatives as in the stiffness (G1T on axial elements), then the same
+// update as the Newmark kernel's, on the state in HBM.
+template <int POLE>
+__global__ void __launch_bounds__(kThreads) anel_memvar_kernel(const __grid_constant__ AnelArgs an,
+                                                               const int32_t *gidx, const uint8_t *axial,
+                                                               StateArgs st, int64_t nel, SpecDev sp) {
+  __shared__ float scr_all[kWarps * 32];
+  if (*st.blowup) return;  // no block-wide synchronisation below
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool active = lane < 25;
+  const int ml = active ? lane : 24;
+  const int i = ml % 5, j = ml / 5, j5 = 5 * j;
+  LaneCoef coef;
+  load_coef(sp, i, j, coef);
+  const bool cg = active && (i == 1 || i == 3) && (j == 1 || j == 3);
+  const int kcg = 2 * (i >> 1) + (j >> 1);
+  float *scr = scr_all + warp * 32;
+  for (int64_t el = (int64_t)blockIdx.x * kWarps + warp; el < nel; el += (int64_t)gridDim.x * kWarps) {
+    int32_t g = gidx[25 * el + ml];
+    if (!AXG_BOUND(g, st.nglob, 51)) g = 0;
+    const bool ax = axial[el] != 0;
+    float u[3] = {st.u[0][g], POLE == POLE_MONO ? 0.f : st.u[1][g], st.u[2][g]};
+    if (ax && i == 0) {  // apply_axis_mask_* on disp
+      if (POLE == POLE_MONO) u[0] = 0.f;
+      if (POLE == POLE_DI) { u[1] = 0.f; u[2] = 0.f; }
+      if (POLE == POLE_QUAD) { u[0] = 0.f; u[1] = 0.f; u[2] = 0.f; }
+    }
+    float gx[3], ge[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      gx[c] = ax ? dxi(u[c], coef.xi1, j5) : dxi(u[c], coef.xi2, j5);
+      ge[c] = deta(u[c], coef.eta, i);
+    }
+    anel_memvar_step<POLE>(an.consts + el * kAnelConst, an.state + el * an.state_stride, scr, an, cg, kcg, lane, u,
+                           gx, ge);
+    __syncwarp();
   }
 }
 

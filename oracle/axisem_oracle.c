@@ -24,7 +24,7 @@
  *   runtime_info blow-up check                              SOLVER/time_evol_wave.F90:1042-1054
  *   nc_compute_recfile_seis_bare                            SOLVER/seismograms.f90:783-820
  *   sf_time_loop_newmark                                    SOLVER/time_evol_wave.F90:264-502
- *   symplectic_time_loop (elastic)                          SOLVER/time_evol_wave.F90:516-742
+ *   symplectic_time_loop                                    SOLVER/time_evol_wave.F90:516-742
  *   axisym_gradient_solid / _fluid, f_over_s_solid / _fluid,
  *   dsdf_solid_allaxis / dsdf_fluid_allaxis                 SOLVER/pointwise_derivatives.f90:130-178,329-545
  *   compute_strain                                          SOLVER/time_evol_wave.F90:1264-1410
@@ -1005,14 +1005,18 @@ int ORC(time_loop)(const axg_mesh_desc *d, REAL *disp, REAL *velo, REAL *acc0, R
   return status;
 }
 
-/* symplectic_time_loop (SOLVER/time_evol_wave.F90:516-742) without
- * attenuation: iterations first_iter..first_iter+n_iter-1 of an nstages
- * scheme whose drifts coefd(1:nstages+1) and kicks coefv(1:nstages) are
- * given times deltat; stf_stages(niter, nstages) holds the source time
- * function at the stage times.  disp, velo (0:4,0:4,nel_solid,3), chi, dchi
- * (0:4,0:4,nel_fluid) carry the state; seismograms as in time_loop. */
+/* symplectic_time_loop (SOLVER/time_evol_wave.F90:516-742): iterations
+ * first_iter..first_iter+n_iter-1 of an nstages scheme whose drifts
+ * coefd(1:nstages+1) and kicks coefv(1:nstages) are given times deltat;
+ * stf_stages(niter, nstages) holds the source time function at the stage
+ * times.  disp, velo (0:4,0:4,nel_solid,3), chi, dchi (0:4,0:4,nel_fluid)
+ * carry the state; with attenuation every stage adds the anelastic stiffness
+ * of the previous step's memory variables, which time_step_memvars updates
+ * after the final drift (memvar, src_*_tm1 as in time_loop); seismograms as
+ * in time_loop. */
 int ORC(time_loop_symplectic)(const axg_mesh_desc *d, int32_t nstages, const double *coefd, const double *coefv,
                               const float *stf_stages, REAL *disp, REAL *velo, REAL *chi, REAL *dchi,
+                              REAL *memvar, REAL *src_tr_tm1, REAL *src_dev_tm1,
                               int32_t first_iter, int32_t n_iter, float *rec, int32_t nseismo_cap,
                               int32_t *iseismo, int32_t *blowup_iter) {
   const int64_t nes = d->nel_solid, cs = 25 * nes, nef = d->nel_fluid, cf = 25 * nef;
@@ -1049,6 +1053,8 @@ int ORC(time_loop_symplectic)(const axg_mesh_desc *d, int32_t nstages, const dou
       }
       mask_solid(d, disp);
       ORC(stiffness_solid)(d, disp, acc);
+      /* glob_anel_stiffness_*: the memory variables of the previous step */
+      if (d->anel_true) ORC(anel_stiffness_cg4)(d, memvar, acc);
       if (nef > 0) {
         for (int64_t p = 0; p < cf; ++p) ddchi[p] = -ddchi[p] * (REAL)d->inv_mass_fluid[p];
         if (d->have_absorbing_bc)
@@ -1094,6 +1100,8 @@ int ORC(time_loop_symplectic)(const axg_mesh_desc *d, int32_t nstages, const dou
       for (int64_t p = 0; p < cs; ++p)
         disp[p + cs * c] = (REAL)((double)disp[p + cs * c] + (double)velo[p + cs * c] * coefd[nstages]);
     }
+    /* time_step_memvars from the drifted displacement (SOLVER/time_evol_wave.F90:727-731) */
+    if (d->anel_true) ORC(time_step_memvars_cg4)(d, memvar, disp, src_tr_tm1, src_dev_tm1);
     if (d->num_rec > 0 && rec && d->seis_it > 0 && iter % d->seis_it == 0) {
       if (*iseismo < nseismo_cap) {
         const int64_t n = nseismo_cap, is = *iseismo;

@@ -124,7 +124,7 @@ class TimeLoop:
                   C.byref(self.iseismo), C.byref(self.blowup_iter))
 
     def run_symplectic(self, first_iter: int, n_iter: int, scheme: int, stf_stages: np.ndarray) -> int:
-        """symplectic_time_loop (elastic) for iterations first_iter..; the
+        """symplectic_time_loop (with attenuation if the mesh has it) for iterations first_iter..; the
         scheme's coefficients are this module's restatement
         (symplectic_coefficients), stf_stages (niter, nstages) the source time
         function at the stage times."""
@@ -135,6 +135,7 @@ class TimeLoop:
         fn.restype = C.c_int
         return fn(C.byref(self.d), C.c_int32(len(cv)), _p(cd, C.c_double), _p(cv, C.c_double),
                   _p(stf, C.c_float), _p(self.disp, ct), _p(self.velo, ct), _p(self.chi, ct), _p(self.dchi, ct),
+                  _p(self.memvar, ct), _p(self.src_tr_tm1, ct), _p(self.src_dev_tm1, ct),
                   C.c_int32(first_iter), C.c_int32(n_iter), _p(self.rec, C.c_float), C.c_int32(self.nseismo),
                   C.byref(self.iseismo), C.byref(self.blowup_iter))
 
