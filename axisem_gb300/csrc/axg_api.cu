@@ -584,9 +584,13 @@ int prepare_solid_kernels(axg_handle *h) {
   int rc = prepare_solid_kernel<POLE, MODE_FORCE, false, false>(h, &h->solid_ctas);
   if (rc) return rc;
   int *c = &h->solid_ctas_step;
-  if (h->scheme != AXG_SCHEME_NEWMARK2)
-    return h->anel ? prepare_solid_kernel<POLE, MODE_SYMPLECTIC, true, false>(h, c)
-                   : prepare_solid_kernel<POLE, MODE_SYMPLECTIC, false, false>(h, c);
+  if (h->scheme != AXG_SCHEME_NEWMARK2) {
+    if (h->anel)
+      return h->kahan ? prepare_solid_kernel<POLE, MODE_SYMPLECTIC, true, true>(h, c)
+                      : prepare_solid_kernel<POLE, MODE_SYMPLECTIC, true, false>(h, c);
+    return h->kahan ? prepare_solid_kernel<POLE, MODE_SYMPLECTIC, false, true>(h, c)
+                    : prepare_solid_kernel<POLE, MODE_SYMPLECTIC, false, false>(h, c);
+  }
   if (h->anel) {
     return h->kahan ? prepare_solid_kernel<POLE, MODE_NEWMARK, true, true>(h, c)
                     : prepare_solid_kernel<POLE, MODE_NEWMARK, true, false>(h, c);
@@ -695,22 +699,27 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
 // per stage the drift (on the gathers), fluid stiffness and the coupling
 // into it, solid stiffness, the coupling into the solid, the kicks (by the
 // last writers); then the final drift and the seismograms.
-template <int POLE, bool ANEL>
-void launch_solid_symplectic(axg_handle *h, cudaStream_t s, const StateArgs &st) {
+template <int POLE, bool ANEL, bool KAHAN>
+void launch_solid_symplectic_modes(axg_handle *h, cudaStream_t s, const StateArgs &st) {
   DomainArgs a = domain_args(h->ds, h->ps);
   for (int c = 0; c < h->ps.n_colours; ++c) {
     a.patch_begin = h->ps.colour_start[c];
     const int n = h->ps.colour_start[c + 1] - h->ps.colour_start[c];
-    solid_patch_kernel<POLE, MODE_SYMPLECTIC, ANEL, false>
-        <<<std::min(n, h->solid_ctas_step), kThreads, solid_smem_bytes<POLE, MODE_SYMPLECTIC, ANEL, false>(), s>>>(
+    solid_patch_kernel<POLE, MODE_SYMPLECTIC, ANEL, KAHAN>
+        <<<std::min(n, h->solid_ctas_step), kThreads, solid_smem_bytes<POLE, MODE_SYMPLECTIC, ANEL, KAHAN>(), s>>>(
             a, st, h->spec, n, h->an);
   }
 }
 
 template <int POLE>
 void launch_solid_symplectic(axg_handle *h, cudaStream_t s, const StateArgs &st) {
-  if (h->anel) launch_solid_symplectic<POLE, true>(h, s, st);
-  else launch_solid_symplectic<POLE, false>(h, s, st);
+  if (h->anel) {
+    if (h->kahan) launch_solid_symplectic_modes<POLE, true, true>(h, s, st);
+    else launch_solid_symplectic_modes<POLE, true, false>(h, s, st);
+  } else {
+    if (h->kahan) launch_solid_symplectic_modes<POLE, false, true>(h, s, st);
+    else launch_solid_symplectic_modes<POLE, false, false>(h, s, st);
+  }
 }
 
 void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
@@ -733,8 +742,13 @@ void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
         a.patch_begin = h->pf.colour_start[c];
         const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
         const One<PatchWork> w{{a, fs}, n};
-        if (h->pole == AXG_MONOPOLE) fluid_patch_kernel<0, false, true><<<n, kThreads, 0, s>>>(w, h->spec);
-        else fluid_patch_kernel<1, false, true><<<n, kThreads, 0, s>>>(w, h->spec);
+        if (h->pole == AXG_MONOPOLE) {
+          if (h->kahan) fluid_patch_kernel<0, true, true><<<n, kThreads, 0, s>>>(w, h->spec);
+          else fluid_patch_kernel<0, false, true><<<n, kThreads, 0, s>>>(w, h->spec);
+        } else {
+          if (h->kahan) fluid_patch_kernel<1, true, true><<<n, kThreads, 0, s>>>(w, h->spec);
+          else fluid_patch_kernel<1, false, true><<<n, kThreads, 0, s>>>(w, h->spec);
+        }
       }
       if (h->to_solid.n > 0) {
         const int nb = (h->to_solid.n + 255) / 256;
@@ -2084,10 +2098,10 @@ int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages) 
     std::vector<double> cd, cv;
     const int n = symplectic_coefficients(scheme, cd, cv);
     if (n == 0) return fail(h, AXG_ERR_BAD_ARG, fmt("unknown time scheme %d", scheme));
-    if (h->kahan || h->fluid_src || h->df.fsmask)
+    if (h->fluid_src || h->df.fsmask)
       return fail(h, AXG_ERR_UNSUPPORTED,
-                  "symplectic schemes: the compensated mode, a fluid source and a fluid free surface are not "
-                  "supported");
+                  "symplectic schemes: a fluid source and a fluid free surface are not supported (the reference's "
+                  "symplectic loop applies neither)");
     if (!stf_stages) return fail(h, AXG_ERR_BAD_ARG, "stf_stages is NULL");
     if (h->anel && !h->sym_gidx) {  // per launch slot: the element's points and axis flag
       std::vector<int32_t> g(25 * (size_t)h->nel_s);

@@ -741,7 +741,7 @@ template <int POLE, int MODE, bool ANEL, bool KAHAN, class P>
 __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, const AnelArgs &an) {
   static_assert(!ANEL || MODE != MODE_FORCE, "attenuation runs in a time loop");
   static_assert(!P::kMany || (MODE == MODE_NEWMARK && !ANEL), "batches run the elastic Newmark step");
-  static_assert(!KAHAN || MODE == MODE_NEWMARK, "the compensated mode is a Newmark time-loop mode");
+  static_assert(!KAHAN || MODE != MODE_FORCE, "the compensated mode is a time-loop mode");
   constexpr bool TL = MODE != MODE_FORCE;  // a time-loop mode
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
   constexpr int NT = n_terms(POLE), NA = n_axial(POLE);
@@ -933,7 +933,9 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
             float u = ok ? st.u[gc(c)][g] : 0.f;
             if (KAHAN) {
               float k = ok ? st.cu[gc(c)][g] : 0.f;
-              if (ok) u = predict_comp(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2, k);
+              // (a symplectic stage: hdt2 = 0, the compensated drift u + coefd(i) v)
+              if (ok) u = predict_comp(u, st.v[gc(c)][g], MODE == MODE_SYMPLECTIC ? 0.f : st.a[gc(c)][g], st.dt,
+                                       st.hdt2, k);
               cc[KAHAN ? q : 0][c] = k;
             } else if (ok && MODE == MODE_SYMPLECTIC) {
               u = fmaf(st.dt, st.v[gc(c)][g], u);  // drift: disp + velo * coefd(i)
@@ -1136,10 +1138,19 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
               // component takes twice the whole acceleration
               float a = -im[q] * v[c];
               if (st.gamma) a = a - 2.f * gam[q] * vel[q][c] - gam[q] * gam[q] * dsp;
-              st.v[cg][g] = fmaf((POLE == POLE_DI && cg == 2) ? 2.f * st.kick : st.kick, a, vel[q][c]);
+              const float kick = (POLE == POLE_DI && cg == 2) ? 2.f * st.kick : st.kick;
+              if (KAHAN) {
+                float k = kv[KAHAN ? q : 0][c];
+                st.v[cg][g] = kahan_add(vel[q][c], kick * a, k);
+                st.cv[cg][g] = k;
+                st.cu[cg][g] = s_cu[c][spos(t)];
+              } else {
+                st.v[cg][g] = fmaf(kick, a, vel[q][c]);
+              }
               st.a[cg][g] = a;
               const bool zero = (w[q] & kPtAxis) && axis_masked<POLE>(cg);
               st.u[cg][g] = zero ? 0.f : dsp;
+              if (KAHAN && zero) st.cu[cg][g] = 0.f;
               continue;
             }
             float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im[q]) * v[c] : -im[q] * v[c];
@@ -1268,7 +1279,7 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(const __grid_cons
       const bool ok = w[q] != kPtPad && AXG_BOUND(g, st.nglob, 11);
       if (KAHAN) {
         float k = ok ? st.cu[0][g] : 0.f;
-        uu[q] = ok ? predict_comp(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2, k) : 0.f;
+        uu[q] = ok ? predict_comp(st.u[0][g], st.v[0][g], SYMP ? 0.f : st.a[0][g], st.dt, st.hdt2, k) : 0.f;
         cc[KAHAN ? q : 0] = k;
       } else if (SYMP) {
         uu[q] = ok ? fmaf(st.dt, st.v[0][g], st.u[0][g]) : 0.f;  // drift: chi + dchi * coefd(i)
@@ -1385,7 +1396,12 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(const __grid_cons
       float a = -im[q] * v;
       const float chi = s_u[t];
       if (st.gamma) a = a - 2.f * gam[q] * vel[q] - gam[q] * gam[q] * chi;
-      if (SYMP) {
+      if (SYMP && KAHAN) {
+        float k = kv[KAHAN ? q : 0];
+        st.v[0][g] = kahan_add(vel[q], st.kick * a, k);  // dchi + coefv(i) * ddchi, compensated
+        st.cv[0][g] = k;
+        st.cu[0][g] = s_cu[t];
+      } else if (SYMP) {
         st.v[0][g] = fmaf(st.kick, a, vel[q]);  // dchi + coefv(i) * ddchi
       } else if (KAHAN) {
         float k = kv[KAHAN ? q : 0];
@@ -1410,10 +1426,20 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(const __grid_cons
 __global__ void drift_kernel(StateArgs solid, StateArgs fluid, float cd) {
   if (*solid.blowup) return;
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // u + coefd(nstages+1) v; compensated where the handle keeps compensation
+  auto drift = [&](float *u, const float *v, float *cu) {
+    if (cu) {
+      float k = cu[q];
+      u[q] = kahan_add(u[q], cd * v[q], k);
+      cu[q] = k;
+    } else {
+      u[q] = fmaf(cd, v[q], u[q]);
+    }
+  };
   if (q < solid.nglob)
     for (int c = 0; c < 3; ++c)
-      if (solid.u[c]) solid.u[c][q] = fmaf(cd, solid.v[c][q], solid.u[c][q]);
-  if (fluid.u[0] && q < fluid.nglob) fluid.u[0][q] = fmaf(cd, fluid.v[0][q], fluid.u[0][q]);
+      if (solid.u[c]) drift(solid.u[c], solid.v[c], solid.cu[c]);
+  if (fluid.u[0] && q < fluid.nglob) drift(fluid.u[0], fluid.v[0], fluid.cu[0]);
 }
 
 // ------------------------------------------------------------ coupling pre-passes

@@ -319,14 +319,17 @@ int axg_symplectic_coefficients(int32_t scheme, double deltat, double *coefd, do
  * scheme, stf_stages(niter, nstages) (column-major) holds the source time
  * function at the stage times of every step (compute_stf_t at
  * t - deltat + coeff(i)); the Newmark scheme ignores it.  The symplectic
- * schemes follow symplectic_time_loop; attenuation, the compensated mode, a
- * fluid source and a fluid free surface are not supported with them here
+ * schemes follow symplectic_time_loop, with attenuation (anelastic stiffness
+ * in every stage, memory variables once per step after the final drift) and
+ * the compensated mode; a fluid source and a fluid free surface, which the
+ * reference's symplectic loop does not apply, are refused
  * (AXG_ERR_UNSUPPORTED).  Resets the state. */
 int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages);
 
 /* Compensated time integration on (1) or off (0): the predictor
  * disp += dt velo + dt^2/2 acc0 and the corrector velo += dt/2 (acc0 + acc1)
- * (and chi, dchi in the fluid) use Kahan's compensated summation in FP32, with
+ * (and chi, dchi in the fluid) -- or a symplectic scheme's drifts
+ * disp += coefd velo and kicks velo += coefv acc -- use Kahan's compensated summation in FP32, with
  * a running compensation per point kept in HBM, so that rounding does not
  * accumulate over 1e4-1e5 steps.  Stiffness, coupling and attenuation are
  * unchanged.  The first call allocates the compensation (zero; axg_reset

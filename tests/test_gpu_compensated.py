@@ -18,7 +18,8 @@ import pytest
 
 from axisem_gb300 import _abi
 from axisem_gb300.mesh import add_attenuation, coupled_mesh, gvec_to_elemental
-from axisem_gb300.solver import AxgError, Solver
+from axisem_gb300.mesh import gauss_at
+from axisem_gb300.solver import AxgError, Solver, symplectic_coefficients
 
 pytestmark = pytest.mark.gpu
 
@@ -131,3 +132,74 @@ def test_compensation_fields_need_the_mode(gpu_lib):
         with pytest.raises(AxgError) as ei:
             s.get_state(_abi.FIELD_DISP_COMP)
         assert ei.value.code == _abi.AXG_ERR_BAD_ARG
+
+
+def _stf_stages(m, scheme):
+    _, _, coeff = symplectic_coefficients(scheme, m.deltat)
+    return gauss_at(np.arange(m.niter)[:, None] * m.deltat + coeff[None, :], 20 * m.deltat)
+
+
+@pytest.mark.parametrize("pole", [0, 1, 2])
+def test_compensated_symplectic_parity(gpu_lib, orc, pole):
+    """Compensated drifts and kicks of symplec4 against the FP64 oracle."""
+    m = coupled_mesh(10, 5, 4, pole, niter=40)
+    stf = _stf_stages(m, _abi.SCHEME_SYMPLEC4)
+    with Solver(m) as s:
+        s.set_compensated(True)
+        s.set_time_scheme(_abi.SCHEME_SYMPLEC4, stf)
+        s.run()
+        rec, disp, chi = s.receivers(), s.get_state(_abi.FIELD_DISP), s.get_state(_abi.FIELD_CHI)
+    t64 = orc.TimeLoop(m, np.float64)
+    assert t64.run_symplectic(1, m.niter, _abi.SCHEME_SYMPLEC4, stf) == 0
+    c = _comps(pole)
+    assert rel(rec, t64.receivers()) < 1e-4
+    assert rel(disp[..., c], t64.disp[..., c]) < 1e-4
+    assert rel(chi, t64.chi) < 1e-4
+
+
+@pytest.mark.parametrize("pole", [0, 2])
+def test_compensated_symplectic_reduces_accumulated_rounding(gpu_lib, orc, pole):
+    m, init = _drift_case(pole, niter=2000)
+    stf = _stf_stages(m, _abi.SCHEME_SYMPLEC4)
+    t64 = orc.TimeLoop(m, np.float64)
+    t64.disp[...] = init[_abi.FIELD_DISP]
+    t64.velo[...] = init[_abi.FIELD_VELO]
+    t64.chi[...] = init[_abi.FIELD_CHI]
+    t64.dchi[...] = init[_abi.FIELD_DCHI]
+    assert t64.run_symplectic(1, m.niter, _abi.SCHEME_SYMPLEC4, stf) == 0
+    err = {}
+    for comp in (False, True):
+        with Solver(m) as s:
+            s.set_compensated(comp)
+            s.set_time_scheme(_abi.SCHEME_SYMPLEC4, stf)
+            for f, a in init.items():
+                if f in (_abi.FIELD_DISP, _abi.FIELD_VELO, _abi.FIELD_CHI, _abi.FIELD_DCHI):
+                    s.set_state(f, a)
+            s.run(1, m.niter)
+            c = _comps(pole)
+            err[comp] = (rel(s.get_state(_abi.FIELD_DISP)[..., c], t64.disp[..., c]),
+                         rel(s.get_state(_abi.FIELD_CHI), t64.chi))
+    print(f"symplec4 pole {pole}: plain disp {err[False][0]:.2e} chi {err[False][1]:.2e}; "
+          f"compensated disp {err[True][0]:.2e} chi {err[True][1]:.2e}")
+    assert err[True][0] < err[False][0] / 3
+    assert err[True][1] < err[False][1] / 3
+
+
+def test_compensated_symplectic_in_pieces(gpu_lib):
+    m, init = _drift_case(1, niter=60, dt=2e-8)
+    stf = _stf_stages(m, _abi.SCHEME_ML_SO4M5)
+    with Solver(m) as s:
+        s.set_compensated(True)
+        s.set_time_scheme(_abi.SCHEME_ML_SO4M5, stf)
+        s.set_tuning(steps_per_graph=8)
+        for f, a in init.items():
+            s.set_state(f, a)
+        s.run(1, 60)
+        a = s.get_state(_abi.FIELD_DISP)
+        assert np.abs(s.get_state(_abi.FIELD_VELO_COMP)).max() > 0
+        s.reset()
+        for f, arr in init.items():
+            s.set_state(f, arr)
+        s.run(1, 17)
+        s.run(18, 43)
+        assert np.array_equal(a, s.get_state(_abi.FIELD_DISP))
