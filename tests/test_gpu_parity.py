@@ -1,6 +1,6 @@
 """GPU parity: the CUDA path through the C-ABI against the CPU oracle.
 
-Tolerances (spec: seismograms within relative L2 1e-4 of the FP32
+Tolerances (seismograms are required within relative L2 1e-4 of the FP32
 reference): the GPU sums element contributions in patch/colour order and uses
 fused multiply-adds, so it differs from the oracle at the FP32 rounding level.
   * stiffness + assembly: relative L2 <= 1e-5 against the FP64 oracle
