@@ -5,6 +5,9 @@
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <system_error>
+#include <thread>
+#include <utility>
 
 namespace axg {
 
@@ -73,8 +76,9 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
   std::vector<std::vector<int32_t>> patches;
   int64_t next_seed = 0;
   const bool layered = growth == kGrowLayered;
-  std::vector<uint32_t> ptstamp(nglob, 0), elstamp(nel, 0);
-  uint32_t stamp = 0;
+  std::vector<uint32_t> ptstamp(nglob, 0), elstamp(nel, 0), inlayer(nel, 0);
+  uint32_t stamp = 0, layer_id = 0;
+  std::vector<int32_t> dirty;
   while (layered) {
     while (next_seed < nel && plan.patch_of_elem[next_seed] >= 0) ++next_seed;
     if (next_seed >= nel) break;
@@ -109,6 +113,8 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
       std::stable_sort(next.begin(), next.end(), [&](int32_t a, int32_t b) {
         return score[a] != score[b] ? score[a] > score[b] : a < b;
       });
+      ++layer_id;
+      for (int32_t c : next) inlayer[c] = layer_id;
       layer.clear();
       for (int32_t c : next) {
         if ((int)members.size() >= patch_elems) break;
@@ -118,14 +124,23 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
         plan.patch_of_elem[c] = pid;
         members.push_back(c);
         layer.push_back(c);
-        for (int k = 0; k < 25; ++k) ptstamp[igloc[25 * (int64_t)c + k] - 1] = stamp;
-        // later candidates of this layer may now share more points
-        for (int32_t c2 : next)
-          if (plan.patch_of_elem[c2] < 0) {
-            int sc = 0;
-            for (int k = 0; k < 25; ++k) sc += ptstamp[igloc[25 * (int64_t)c2 + k] - 1] == stamp;
-            score[c2] = sc;
+        // later candidates of this layer may now share more points: those
+        // holding a point c brings into the patch are counted again
+        dirty.clear();
+        for (int k = 0; k < 25; ++k) {
+          const int64_t g = igloc[25 * (int64_t)c + k] - 1;
+          if (ptstamp[g] == stamp) continue;
+          ptstamp[g] = stamp;
+          for (int64_t q = pe.start[g]; q < pe.start[g + 1]; ++q) {
+            const int32_t e2 = pe.elems[q];
+            if (e2 >= 0 && inlayer[e2] == layer_id && plan.patch_of_elem[e2] < 0) dirty.push_back(e2);
           }
+        }
+        for (int32_t c2 : dirty) {
+          int sc = 0;
+          for (int k = 0; k < 25; ++k) sc += ptstamp[igloc[25 * (int64_t)c2 + k] - 1] == stamp;
+          score[c2] = sc;
+        }
       }
       if (layer.empty()) break;
       for (int32_t c : next) score[c] = 0;
@@ -311,15 +326,21 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
         }
       }
     }
-    // counting sort by the first patch, then by the second inside a bucket
-    std::vector<int64_t> start(plan.n_patches + 2, 0);
-    for (int64_t g = 0; g < nglob; ++g) start[r0[g] + 1]++;
-    for (int32_t p = 0; p <= plan.n_patches; ++p) start[p + 1] += start[p];
-    std::vector<int64_t> fill(start.begin(), start.end() - 1);
-    for (int64_t g = 0; g < nglob; ++g) plan.old_of_new[fill[r0[g]]++] = (int32_t)g;
-    for (int32_t p = 0; p <= plan.n_patches; ++p)
-      std::stable_sort(plan.old_of_new.begin() + start[p], plan.old_of_new.begin() + start[p + 1],
-                       [&](int32_t a, int32_t b) { return r1[a] < r1[b]; });
+    // order (first patch, second patch, reference number): two stable
+    // counting sorts, by the second patch and then by the first
+    std::vector<int64_t> fill(plan.n_patches + 2);
+    auto csort = [&](const std::vector<int32_t> &key, const int32_t *in, int32_t *out) {
+      std::fill(fill.begin(), fill.end(), 0);
+      for (int64_t g = 0; g < nglob; ++g) fill[key[g] + 1]++;
+      for (int32_t p = 0; p <= plan.n_patches; ++p) fill[p + 1] += fill[p];
+      for (int64_t q = 0; q < nglob; ++q) {
+        const int32_t g = in ? in[q] : (int32_t)q;
+        out[fill[key[g]]++] = g;
+      }
+    };
+    std::vector<int32_t> by_r1(nglob);
+    csort(r1, nullptr, by_r1.data());
+    csort(r0, by_r1.data(), plan.old_of_new.data());
     for (int64_t n = 0; n < nglob; ++n) plan.new_of_old[plan.old_of_new[n]] = (int32_t)n;
   }
   const std::vector<int32_t> &nofo = plan.new_of_old;
@@ -346,6 +367,10 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
   std::vector<int32_t> round_of(kMaxPatchElems);
   std::vector<uint32_t> pts;
   std::vector<uint32_t> ptmask(nglob, 0);
+  // per point (reference number): the last patch that listed it (+1); per
+  // point (internal number): its index in that patch
+  std::vector<int32_t> listed(nglob, 0);
+  std::vector<uint16_t> local_of(nglob, 0);
   for (int32_t lp = 0; lp < plan.n_patches; ++lp) {
     const int32_t p = order[lp];
     std::vector<int32_t> mem = patches[p];
@@ -393,10 +418,15 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
     // unique points, sorted by internal number
     pts.clear();
     for (int a = 0; a < n; ++a)
-      for (int k = 0; k < 25; ++k) pts.push_back((uint32_t)nofo[igloc[25 * (int64_t)mem[a] + k] - 1]);
+      for (int k = 0; k < 25; ++k) {
+        const int64_t g = igloc[25 * (int64_t)mem[a] + k] - 1;
+        if (listed[g] == lp + 1) continue;
+        listed[g] = lp + 1;
+        pts.push_back((uint32_t)nofo[g]);
+      }
     std::sort(pts.begin(), pts.end());
-    pts.erase(std::unique(pts.begin(), pts.end()), pts.end());
     if (pts.size() > (size_t)kMaxPatchPoints) return "patch has too many points";
+    for (size_t t = 0; t < pts.size(); ++t) local_of[pts[t]] = (uint16_t)t;
     m.n_pts = (uint16_t)pts.size();
     plan.max_pts = std::max<int32_t>(plan.max_pts, (int32_t)pts.size());
     const int32_t col = plan.colour_of_patch[p];
@@ -414,11 +444,7 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
       const int a = idx[t];
       const int32_t e = mem[a];
       plan.elem_order[eslot] = e;
-      for (int k = 0; k < 25; ++k) {
-        const uint32_t g = (uint32_t)nofo[igloc[25 * (int64_t)e + k] - 1];
-        const auto it = std::lower_bound(pts.begin(), pts.end(), g);
-        plan.elem_pts[25 * eslot + k] = (uint16_t)(it - pts.begin());
-      }
+      for (int k = 0; k < 25; ++k) plan.elem_pts[25 * eslot + k] = local_of[nofo[igloc[25 * (int64_t)e + k] - 1]];
       ++eslot;
     }
   }
@@ -534,18 +560,34 @@ std::string tune_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patc
   std::vector<int> growths;
   if (growth >= 0) growths.push_back(growth);
   else growths = {kGrowLayered, kGrowCompact};
-  double best = -1;
+  std::vector<std::pair<int, int>> cand;
   for (int pe : sizes)
-    for (int gr : growths) {
-      DomainPlan pl;
-      std::string e = build_plan(ig.data(), n, (int64_t)ids.size(), pe, gr, std::vector<uint8_t>(), pl, false);
-      if (!e.empty()) continue;
-      const double c = (double)plan_cost(pl);
-      if (best < 0 || c < best) {
-        best = c;
-        *best_pe = pe;
-        *best_growth = gr;
-      }
+    for (int gr : growths) cand.emplace_back(pe, gr);
+  // the candidates' plans are independent: built on threads, compared in order
+  std::vector<double> cost(cand.size(), -1.0);
+  auto eval = [&](size_t i) {
+    DomainPlan pl;
+    if (build_plan(ig.data(), n, (int64_t)ids.size(), cand[i].first, cand[i].second, std::vector<uint8_t>(), pl,
+                   false).empty())
+      cost[i] = (double)plan_cost(pl);
+  };
+  std::vector<std::thread> threads;
+  if (cand.size() > 1 && std::thread::hardware_concurrency() > 1) {
+    try {
+      for (size_t i = 0; i < cand.size(); ++i) threads.emplace_back(eval, i);
+    } catch (const std::system_error &) {  // no threads: the rest in this one
+      for (size_t i = threads.size(); i < cand.size(); ++i) eval(i);
+    }
+    for (std::thread &t : threads) t.join();
+  } else {
+    for (size_t i = 0; i < cand.size(); ++i) eval(i);
+  }
+  double best = -1;
+  for (size_t i = 0; i < cand.size(); ++i)
+    if (cost[i] >= 0 && (best < 0 || cost[i] < best)) {
+      best = cost[i];
+      *best_pe = cand[i].first;
+      *best_growth = cand[i].second;
     }
   if (best < 0) return "no patch size yields a valid plan";
   return "";
