@@ -1,6 +1,7 @@
 """Generates tests/golden/oracle_golden.npz: outputs of the FP64 oracle on small
-seeded meshes (stiffness + assembly for each pole type; a coupled solid-fluid
-Newmark run for each pole type).  The reference itself cannot be compiled here
+seeded meshes, for each pole type: stiffness + assembly; a coupled solid-fluid
+Newmark run; the same with cg4 attenuation; a symplec4 run with attenuation;
+the fullfields wavefield dump of the Newmark run's final state.  The reference itself cannot be compiled here
 (no Fortran compiler), so these fixtures pin the oracle restatement against
 regressions; the oracle is pinned to the reference through the known-answer
 tests in tests/test_oracle.py and tests/test_spectral.py.
@@ -15,7 +16,9 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
-from axisem_gb300.mesh import coupled_mesh, random_gvec, structured_mesh  # noqa: E402
+from axisem_gb300 import _abi  # noqa: E402
+from axisem_gb300.mesh import (add_attenuation, add_pointwise, coupled_mesh, dump_desc, gauss_at,  # noqa: E402
+                               random_gvec, structured_mesh)
 
 
 def make_cases(orc):
@@ -30,6 +33,21 @@ def make_cases(orc):
         assert t.run(1, cm.niter) == 0
         out[f"seis_p{pole}"] = t.receivers().copy()
         out[f"chi_p{pole}"] = t.chi.copy()
+        pw = add_pointwise(cm, seed=41 + pole)
+        full, _ = orc.wavefield_dump(pw, dump_desc(pw, _abi.DUMP_FULLFIELDS, 1, None, 1), t.disp, t.velo, t.chi,
+                                     t.dchi, np.float64)
+        out[f"dump_full_p{pole}"] = full
+        am = add_attenuation(coupled_mesh(6, 3, 2, pole, niter=24, seed=51 + pole), seed=61 + pole)
+        ta = orc.TimeLoop(am, np.float64)
+        assert ta.run(1, am.niter) == 0
+        out[f"anel_seis_p{pole}"] = ta.receivers().copy()
+        out[f"anel_memvar_p{pole}"] = ta.memvar.copy()
+        _, _, coeff = orc.symplectic_coefficients(_abi.SCHEME_SYMPLEC4, am.deltat)
+        stf = gauss_at(np.arange(am.niter)[:, None] * am.deltat + np.asarray(coeff)[None, :], 20 * am.deltat)
+        ts = orc.TimeLoop(am, np.float64)
+        assert ts.run_symplectic(1, am.niter, _abi.SCHEME_SYMPLEC4, stf) == 0
+        out[f"symp_anel_seis_p{pole}"] = ts.receivers().copy()
+        out[f"symp_anel_memvar_p{pole}"] = ts.memvar.copy()
     return out
 
 
