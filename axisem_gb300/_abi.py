@@ -193,6 +193,7 @@ SIGNATURES = {
     "axg_plan_check": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(Info)]),
     "axg_time_stiffness": (C.c_int, [C.c_void_p, C.c_int32, _fp]),
     "axg_device_check_report": (C.c_int, [_ip]),
+    "axg_selftest_wait_timeout": (C.c_int, [_ip, C.POINTER(C.c_double)]),
     "axg_destroy": (None, [C.c_void_p]),
     "axg_last_error": (C.c_char_p, [C.c_void_p]),
 }

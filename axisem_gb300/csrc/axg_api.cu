@@ -232,6 +232,31 @@ int upload(axg_handle *h, T **p, const std::vector<T> &v) {
 
 // ---------------------------------------------------------------- validation
 
+// The descriptor fields a stiffness + assembly reads: sizes, pole type, the
+// solid numbering, the spectral matrices, the pole's solid metric arrays and
+// the axial elements with their vectors.
+int validate_stiffness(const axg_mesh_desc *d) {
+  auto bad = [](const std::string &m) { return fail(nullptr, AXG_ERR_BAD_DESC, m); };
+  if (!d) return bad("descriptor is NULL");
+  if (d->abi_version != AXG_ABI_VERSION) return bad(fmt("abi_version %d, expected %d", d->abi_version, AXG_ABI_VERSION));
+  if (d->npol != AXG_NPOL) return bad(fmt("npol = %d; only npol = 4 is supported", d->npol));
+  if (d->src_type < 0 || d->src_type > 2) return bad("src_type must be monopole/dipole/quadpole (0..2)");
+  if (d->nel_solid <= 0 || d->nglob_solid <= 0) return bad("nel_solid and nglob_solid must be positive");
+  if (!d->igloc_solid) return bad("igloc_solid is NULL");
+  if (!d->G0 || !d->G1 || !d->G2) return bad("spectral matrices G0, G1, G2 are required");
+  for (int s : solid_slots(d->src_type))
+    if (!d->m_solid[s]) return bad(fmt("solid metric array %d required by this pole type is NULL", s));
+  if (d->naxel_solid < 0 || d->naxel_solid > d->nel_solid) return bad("naxel_solid out of range");
+  if (d->naxel_solid > 0) {
+    if (!d->ax_el_solid) return bad("ax_el_solid is NULL");
+    for (int s : axial_slots(d->src_type))
+      if (!d->m0_solid[s]) return bad(fmt("axial vector M0_w%d is NULL", s + 1));
+    for (int k = 0; k < d->naxel_solid; ++k)
+      if (d->ax_el_solid[k] < 1 || d->ax_el_solid[k] > d->nel_solid) return bad("ax_el_solid entry out of range");
+  }
+  return AXG_OK;
+}
+
 int validate(const axg_mesh_desc *d) {
   auto bad = [](const std::string &m) { return fail(nullptr, AXG_ERR_BAD_DESC, m); };
   if (!d) return bad("descriptor is NULL");
@@ -1267,6 +1292,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 struct NoAllocDevice {
   bool ready = false;
+  unsigned long long ctx_id = 0;  // the CUDA context the set-up was made in
   unsigned char *base = nullptr;  // device address of g_noalloc_scratch on this device
   int grid_cap[3] = {0, 0, 0};    // resident CTAs of the FORCE kernel per pole
 };
@@ -1287,15 +1313,38 @@ int noalloc_prepare_kernel(int nsm, int *cap) {
   return AXG_OK;
 }
 
-// once per device, with that device current: the symbol's device address and
-// the kernel attributes (call before any stream capture)
+// Id of the current CUDA context (cuCtxGetId, looked up through the runtime so
+// that the library does not link the driver library); 0 when unavailable.
+unsigned long long current_context_id() {
+  typedef int (*CtxGetId)(void *, unsigned long long *);
+  static CtxGetId fn = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetId>(p);
+    looked_up = true;
+  }
+  unsigned long long id = 0;
+  if (fn && fn(nullptr, &id) != 0) id = 0;
+  return id;
+}
+
+// Once per device (and again when the device's context was replaced, e.g.
+// after a cudaDeviceReset), with that device current: the symbol's device
+// address and the kernel attributes.  The first call on a device makes this
+// set-up; it should come before any stream capture.
 int noalloc_setup(NoAllocDevice **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDevice");
   if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(nullptr, AXG_ERR_UNSUPPORTED, "device ordinal too large");
   NoAllocDevice &nd = g_noalloc_dev[dev];
-  if (!nd.ready) {
+  const unsigned long long ctx = current_context_id();
+  if (!nd.ready || ctx == 0 || ctx != nd.ctx_id) {
+    nd.ready = false;
     void *ptr = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
@@ -1308,7 +1357,8 @@ int noalloc_setup(NoAllocDevice **out) {
         (rc = noalloc_prepare_kernel<POLE_QUAD>(nsm, &nd.grid_cap[2])))
       return rc;
     nd.base = static_cast<unsigned char *>(ptr);
-    nd.ready = true;
+    nd.ctx_id = current_context_id();  // the symbol look-up made the context current if it was not
+    nd.ready = nd.ctx_id != 0;         // without a context id the set-up is repeated on every call
   }
   *out = &nd;
   return AXG_OK;
@@ -1332,7 +1382,7 @@ size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 extern "C" int axg_stiffness_assembled_noalloc(const axg_mesh_desc *d, const float *u_gvec, float *f_gvec) {
   if (!u_gvec || !f_gvec) return fail(nullptr, AXG_ERR_BAD_ARG, "u_gvec and f_gvec must not be NULL");
-  int rc = validate(d);
+  int rc = validate_stiffness(d);
   if (rc) return rc;
   if ((rc = check_igloc(d->igloc_solid, 25 * (int64_t)d->nel_solid, d->nglob_solid, "igloc_solid"))) return rc;
   if (axg_device_count() < 1) return fail(nullptr, AXG_ERR_NO_DEVICE, "no CUDA device is visible");
@@ -1399,6 +1449,10 @@ extern "C" int axg_stiffness_assembled_noalloc(const axg_mesh_desc *d, const flo
       (rc = put(o_m0, m0.data(), m0.size() * sizeof(float))) ||
       (rc = put(o_u, u_gvec, (size_t)nglob * 3 * sizeof(float))) || (rc = put(o_ctl, zeros, sizeof zeros)))
     return rc;
+  // the array keeps the previous call's force: a global point no element
+  // refers to must read zero, not that value (cudaMemset allocates nothing)
+  cudaError_t ez = cudaMemset(base + o_f, 0, (size_t)nglob * 3 * sizeof(float));
+  if (ez != cudaSuccess) return cuda_fail(nullptr, ez, "cudaMemset of the no-allocation scratch");
 
   DomainArgs a{};
   a.meta = reinterpret_cast<const PatchMeta *>(base + o_meta);
@@ -2243,6 +2297,48 @@ int axg_device_check_report(int32_t *out8) {
 const char *axg_last_error(axg_handle *h) { return h ? h->err.c_str() : g_create_error.c_str(); }
 
 }  // extern "C"
+
+namespace {
+// One thread waits, through the kernels' own bounded wait, on an mbarrier that
+// nothing arrives at and no copy targets; the wait must give up after about
+// kWaitNs and record AXG_ERR_TIMEOUT.  No copy is in flight when it returns.
+__global__ void wait_selftest_kernel(int32_t *err, unsigned long long *elapsed_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  fence_mbar_init();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint64_t t0 = globaltimer_ns();
+    const bool done = mbar_wait_bounded(&bar, 0u, err);
+    *elapsed_ns = globaltimer_ns() - t0;
+    if (done) atomicExch(err, -1);  // the phase cannot have completed
+  }
+}
+}  // namespace
+
+extern "C" int axg_selftest_wait_timeout(int32_t *status, double *elapsed_s) {
+  if (!status || !elapsed_s) return fail(nullptr, AXG_ERR_BAD_ARG, "NULL argument");
+  if (axg_device_count() < 1) return fail(nullptr, AXG_ERR_NO_DEVICE, "no CUDA device is visible");
+  void *buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, 16);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
+  int32_t *err = static_cast<int32_t *>(buf);
+  unsigned long long *ns = reinterpret_cast<unsigned long long *>(static_cast<char *>(buf) + 8);
+  unsigned char host[16] = {};
+  e = cudaMemset(buf, 0, 16);
+  if (e == cudaSuccess) {
+    wait_selftest_kernel<<<1, 32>>>(err, ns);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(host, buf, 16, cudaMemcpyDeviceToHost);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "wait self-test");
+  std::memcpy(status, host, 4);
+  unsigned long long t = 0;
+  std::memcpy(&t, host + 8, 8);
+  *elapsed_s = 1e-9 * (double)t;
+  return AXG_OK;
+}
 
 extern "C" {
 

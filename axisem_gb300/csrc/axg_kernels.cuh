@@ -763,6 +763,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
   float *scr = reinterpret_cast<float *>(smem + L::scr_off);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::bar_off);
   __shared__ int s_stop;
+  __shared__ int s_timeout;  // a bounded wait of this CTA gave up
   // sub-round r of a patch is complete when all threads have arrived on
   // s_round[r] after their accumulations of round r
   __shared__ __align__(8) uint64_t s_round[kMaxSubrounds];
@@ -776,6 +777,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
   if (threadIdx.x < 2) mbar_init(&s_wbar[threadIdx.x], 1);
   // one solve: nothing to do after a blow-up (a batch checks per solve below)
   if (threadIdx.x == 0) s_stop = TL && !P::kMany ? *p.state(0).blowup : 0;
+  if (threadIdx.x == 0) s_timeout = 0;
   fence_mbar_init();
   __syncthreads();
   if (s_stop) return;  // uniform across the CTA; no copy has been issued
@@ -858,7 +860,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
     const DomainArgs &d = p.dom(0);
     const PatchMeta m0 = d.meta[d.patch_begin + blockIdx.x];
     if (threadIdx.x == 0) issue_words(d, 0, m0.pt_start, m0.n_pts);
-    mbar_wait_bounded(&s_wbar[0], 0u, p.state(0).err);
+    if (!mbar_wait_bounded(&s_wbar[0], 0u, p.state(0).err)) s_timeout = 1;
     issue_gather(p.state(0), 0, m0.n_pts);
   }
 
@@ -911,7 +913,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
     if (MODE == MODE_FORCE) {
       cp_async_wait_all();  // this thread's copies of the patch (issued during the previous one)
     } else {
-      mbar_wait_bounded(&s_wbar[0], pcount & 1u, st.err);
+      if (!mbar_wait_bounded(&s_wbar[0], pcount & 1u, st.err)) s_timeout = 1;
       // Newmark predictor on the fly; kGB points per thread in flight cover
       // a whole patch (kGB * kThreads >= kMaxPatchPoints): one memory latency
       constexpr int kGB = (kMaxPatchPoints + kThreads - 1) / kThreads;
@@ -971,7 +973,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
         int64_t el = (int64_t)m.elem_start + s;
         if (!AXG_BOUND(el, d.n_elem, 2)) el = 0;
         const uint32_t slot = kcount % STG;
-        mbar_wait_bounded(&my_bars[slot], (kcount / STG) & 1u, st.err);
+        if (!mbar_wait_bounded(&my_bars[slot], (kcount / STG) & 1u, st.err)) s_timeout = 1;
         const float *blk = my_ring + slot * BS;
         const int32_t info = *reinterpret_cast<const int32_t *>(blk + solid_info_off(NT));
         int axslot = (info & 0xFFFFFF) - 1;
@@ -1026,7 +1028,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
         // the previous sub-round's accumulations must be complete; the wait
         // comes after this element's stiffness, which hides it
         if (!ready) {
-          mbar_wait_bounded(&s_round[r - 1], (round_par >> (r - 1)) & 1u, st.err);
+          if (!mbar_wait_bounded(&s_round[r - 1], (round_par >> (r - 1)) & 1u, st.err)) s_timeout = 1;
           ready = true;
         }
         if (active) {
@@ -1067,7 +1069,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
       r0 = r1;
       if (MODE == MODE_FORCE && r == 0 && next_npts > 0) {
         // the next patch's words have landed in the other buffer: start its gather
-        mbar_wait_bounded(&s_wbar[buf ^ 1], ((pcount + 1) / NB) & 1u, st.err);
+        if (!mbar_wait_bounded(&s_wbar[buf ^ 1], ((pcount + 1) / NB) & 1u, st.err)) s_timeout = 1;
         issue_gather(st, buf ^ 1, next_npts);
       }
     }
@@ -1174,6 +1176,22 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
     }
     __syncthreads();
     ++pcount;
+  }
+  // After a timeout, bulk copies of this CTA may still be in flight into its
+  // shared memory: wait (bounded) for the last phase of each ring slot and of
+  // the point-word buffer before the CTA exits.
+  __syncthreads();
+  if (s_timeout) {
+    if (lane == 0)
+      for (uint32_t q = 0; q < (uint32_t)STG && q < kcount; ++q) {
+        const uint32_t k = kcount - 1 - q;  // the last element consumed from slot k % STG
+        mbar_drain(&my_bars[k % STG], (k / STG) & 1u);
+      }
+    if (threadIdx.x == 0 && pcount > 0) {
+      const uint32_t b = MODE == MODE_FORCE ? (pcount - 1) % NB : 0u;
+      const uint32_t par = MODE == MODE_FORCE ? ((pcount - 1) / NB) & 1u : (pcount - 1) & 1u;
+      mbar_drain(&s_wbar[b], par);
+    }
   }
 }
 

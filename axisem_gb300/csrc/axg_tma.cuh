@@ -2,9 +2,10 @@
 //
 // Element blocks of metric terms are contiguous, 16-byte aligned and a
 // multiple of 16 bytes long, so they are moved with the 1-D form
-// cp.async.bulk (no tensor map).  Every wait on an mbarrier is bounded: after
-// kSpinLimit polls the waiter records AXG_ERR_TIMEOUT in the kernel's error
-// word and gives up, so a lost copy cannot hang the GPU.
+// cp.async.bulk (no tensor map).  Every wait on an mbarrier is bounded in
+// time, measured on the GPU's global nanosecond timer: after kWaitNs the
+// waiter records AXG_ERR_TIMEOUT in the kernel's error word and gives up, so a
+// lost copy cannot hang the GPU.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -12,7 +13,12 @@
 
 namespace axg {
 
-constexpr uint32_t kSpinLimit = 1u << 24;   // ~seconds of polling
+constexpr uint64_t kWaitNs = 1000000000ull;  // a wait gives up after 1 s
+// a wait still pending after this long first checks whether another wait of
+// the kernel already gave up; if so it returns at once, so that a kernel whose
+// copies were lost ends within about kWaitNs instead of kWaitNs per wait
+constexpr uint64_t kWaitCheckNs = 20000ull;
+constexpr int kPollsPerTimerRead = 16;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -91,12 +97,44 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait; returns false (and records the timeout) when it gave up
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int32_t *err) {
-  for (uint32_t k = 0; k < kSpinLimit; ++k)
-    if (mbar_try_wait(bar, parity)) return true;
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait for the phase of `bar` with `parity`; returns false when it
+// gave up, after recording AXG_ERR_TIMEOUT in *err.  The first poll is the
+// fast path; the timer is read only once the wait is pending.
+__device__ __noinline__ bool mbar_wait_slow(uint64_t *bar, uint32_t parity, int32_t *err) {
+  const uint64_t t0 = globaltimer_ns();
+  bool checked = false;
+  for (;;) {
+    for (int k = 0; k < kPollsPerTimerRead; ++k)
+      if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t dt = globaltimer_ns() - t0;
+    if (!checked && dt > kWaitCheckNs) {
+      checked = true;
+      if (err && *reinterpret_cast<volatile int32_t *>(err) != 0) return false;  // a wait already gave up
+    }
+    if (dt > kWaitNs) break;
+  }
   if (err) atomicCAS(err, 0, 5 /* AXG_ERR_TIMEOUT */);
   return false;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int32_t *err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  return mbar_wait_slow(bar, parity, err);
+}
+
+// After a timeout, copies issued by this CTA may still be in flight into its
+// shared memory: wait (bounded again) for the last phase issued on `bar`
+// before the CTA exits.  A phase that never completes gives up after kWaitNs.
+__device__ __forceinline__ void mbar_drain(uint64_t *bar, uint32_t parity) {
+  const uint64_t t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (globaltimer_ns() - t0 > kWaitNs) break;
 }
 
 }  // namespace axg

@@ -11,7 +11,11 @@ The metric is GLL-point-steps/s: 25 * 2^20 element-local GLL points per step.
 
   value : device-resident inputs, CUDA events on the library's stream;
   e2e   : through the C-ABI call with host (pinned) buffers, the host->device
-          copy of u and the device->host copy of f inside every step.
+          copy of u and the device->host copy of f inside every step;
+  poles : the same for each pole type, each with its roofline.
+  cpu_baseline / --impl reference : the same stiffness + assembly of the same
+          mesh on the host cores, the oracle's FP32 timing build on all threads
+          (the reference's Fortran cannot be compiled here: no compiler).
 The inputs (2.8 GB of metric terms) are far larger than the 129 MB L2, so no
 L2 flush is needed between steps.
 
@@ -30,7 +34,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 from pathlib import Path
 
@@ -138,81 +141,90 @@ def max_over_ranks(x: float, ws: int) -> float:
     return float(t.item())
 
 
-def cpu_sample_mesh(pole: int, n: int):
+def cpu_build() -> str:
+    """The oracle timing build's flags (oracle/Makefile)."""
+    import platform
+    native = " -mcpu=native" if platform.machine() == "aarch64" else ""
+    return f"oracle FP32 restatement, gcc -O3{native} -ffp-contract=fast, OpenMP over coloured elements"
+
+
+def bench_mesh(pole: int, n: int, rank: int = 0):
+    """The micro-benchmark's mesh and displacement (seeded per replica)."""
     from axisem_gb300.mesh import random_gvec, structured_mesh
-    m = structured_mesh(n, n, pole, terms="pole")
-    return m, random_gvec(m)
+    m = structured_mesh(n, n, pole, terms="pole", seed=20261203 + rank)
+    return m, random_gvec(m, seed=20261204 + rank)
 
 
-def time_oracle(pole: int, seconds: float, threads: int, n: int = 96):
-    """Throughput of the FP32 oracle (the CPU restatement of the reference's
-    stiffness + pdistsum) on `threads` independent n x n element sub-meshes
-    run concurrently (ctypes releases the GIL), for about `seconds`."""
+def time_cpu(mesh, u, seconds: float, threads: int, min_steps: int = 1):
+    """Stiffness + assembly of the whole mesh on the host cores with the
+    oracle's timing build (the FP32 restatement at -O3 for the host CPU,
+    coloured elements on `threads` threads); steps for about `seconds`.
+    Returns (GLL-point-steps/s, steps)."""
     from oracle import oracle as orc
-    orc.build()
-    meshes = [cpu_sample_mesh(pole, n) for _ in range(threads)]
-    counts = [0] * threads
-    stop = time.perf_counter() + seconds
-
-    def work(k):
-        m, u = meshes[k]
-        while time.perf_counter() < stop or counts[k] == 0:
-            orc.stiffness_assembled(m, u, np.float32)
-            counts[k] += 1
-
-    t0 = time.perf_counter()
-    ths = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
-    for t in ths:
-        t.start()
-    for t in ths:
-        t.join()
+    cs = orc.CpuStiffness(mesh)
+    f = np.zeros_like(u, order="F")
+    cs(u, f, threads)   # warm-up
+    n, t0 = 0, time.perf_counter()
+    while n < min_steps or time.perf_counter() - t0 < seconds:
+        cs(u, f, threads)
+        n += 1
     dt = time.perf_counter() - t0
-    pts = sum(c * meshes[0][0].nel_solid * 25 for c in counts)
-    return pts / dt, f"{threads} x {n}x{n} elements, {sum(counts)} steps in {dt:.1f} s"
+    assert np.isfinite(f).all()
+    return n * mesh.nel_solid * 25 / dt, n
 
 
 def run_reference(args):
+    """The reference's algorithm on the host cores: the oracle's FP32 timing
+    build (the reference cannot be compiled here or on the GPU hosts: no
+    Fortran compiler) on the same 1024 x 1024 mesh and pole as the GPU arm,
+    all host threads, elements coloured so that threads scatter without
+    races.  One step = one stiffness + assembly of the whole mesh."""
     ws, rank, _ = dist_init()
     if rank != 0:
         return
+    from oracle import oracle as orc
+    orc.build()
     pole = POLES[args.pole]
+    n = args.size
     threads = os.cpu_count() or 1
-    # each step is a bounded sample; the whole run stays within ~2 minutes
-    per_step = max(0.2, min(args.ref_seconds, 120.0 / max(args.steps, 1)))
-    vals = []
+    mesh, u = bench_mesh(pole, n)
+    cs = orc.CpuStiffness(mesh)
+    f = np.zeros_like(u, order="F")
     for _ in range(args.warmup):
-        time_oracle(pole, 0.2, threads)
+        cs(u, f, threads)
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, sample = time_oracle(pole, per_step, threads)
-        vals.append(v)
-    value = statistics.median(vals)
+        cs(u, f, threads)
+    dt = time.perf_counter() - t0
+    assert np.isfinite(f).all()
+    pts = mesh.nel_solid * 25
+    value = args.steps * pts / dt
+    sample = (f"{args.steps} full steps of the {n}x{n} mesh ({mesh.nel_solid} elements), "
+              f"{threads} threads, {cs.ncol} element colours")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GLL-point-steps/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": f"stiffness+assembly, {args.pole}pole, structured grid (oracle sample)",
-                       "pole": args.pole},
-            "cpu_baseline": {"value": value, "unit": "GLL-point-steps/s", "cores": threads,
-                             "kind": "port", "sample": sample},
+            "config": {"workload": f"stiffness+assembly, {args.pole}pole, {n}x{n} structured quads "
+                                   f"({mesh.nel_solid} elements, {mesh.nglob_solid} global points, 1% axial)",
+                       "pole": args.pole, "elements": mesh.nel_solid, "global_points": mesh.nglob_solid},
+            "cpu_baseline": {"value": value, "unit": "GLL-point-steps/s", "cores": threads, "kind": "port",
+                             "sample": sample,
+                             "build": cpu_build()},
             "e2e": {"value": value, "unit": "GLL-point-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_gpu(args):
-    ws, rank, local = dist_init()
+def measure_stiffness(args, pole, ws, rank, local, e2e=True):
+    """Stiffness + assembly of one pole type on the benchmark mesh: device
+    timing (CUDA events on the library's stream), optionally end to end
+    through the C-ABI with pinned host buffers, and the roofline."""
     import torch
-    torch.cuda.set_device(local)
-    import axisem_gb300.build as b
-    b.build()
-    from axisem_gb300.mesh import random_gvec, structured_mesh
     from axisem_gb300.solver import Solver
-
-    pole = POLES[args.pole]
     n = args.size
     t0 = time.perf_counter()
-    mesh = structured_mesh(n, n, pole, terms="pole", seed=20261203 + rank)
-    u = random_gvec(mesh, seed=20261204 + rank)
+    mesh, u = bench_mesh(pole, n, rank)
     t_mesh = time.perf_counter() - t0
     t0 = time.perf_counter()
     s = Solver(mesh)
@@ -223,7 +235,6 @@ def run_gpu(args):
         s.stiffness_device()
     torch.cuda.synchronize()
 
-    # ---- device-resident timing (CUDA events on the library's stream)
     with ClockSampler(local) as clk:
         barrier(ws)
         torch.cuda.synchronize()
@@ -235,41 +246,79 @@ def run_gpu(args):
     clocks = clk.summary()
     ms = max_over_ranks(ms, ws)
     pts_step = mesh.nel_solid * 25
-    value = ws * pts_step / (ms * 1e-3)
-
-    # ---- end-to-end through the C-ABI with pinned host buffers
     ng = mesh.nglob_solid
-    hu = torch.empty((3, ng), dtype=torch.float32, pin_memory=True).numpy()
-    hu[:] = u.T
-    hf = torch.empty((3, ng), dtype=torch.float32, pin_memory=True).numpy()
-    ufort = hu.T  # (ng, 3) column-major view of the pinned buffer
-    import ctypes as C
-    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
-    for _ in range(2):
-        s.lib.axg_stiffness_assembled(s.h, fp(hu), fp(hf))
-    barrier(ws)
-    torch.cuda.synchronize()
-    e0 = time.perf_counter()
-    for _ in range(args.steps):
-        rc = s.lib.axg_stiffness_assembled(s.h, fp(hu), fp(hf))
-        assert rc == 0, s.lib.axg_last_error(s.h)
-    torch.cuda.synchronize()
-    e_s = max_over_ranks((time.perf_counter() - e0) / args.steps, ws)
-    e2e = ws * pts_step / e_s
-    assert np.isfinite(hf).all() and ufort.shape == (ng, 3)
-
-    # ---- roofline of the stiffness+assembly kernels (all colour launches of one step)
+    out = {"value": ws * pts_step / (ms * 1e-3), "ms_per_step": ms, "clocks": clocks, "wall_s": wall,
+           "info": info, "setup_s": {"mesh": round(t_mesh, 2), "create": round(t_create, 2)},
+           "mesh": mesh, "u": u}
+    if e2e:
+        hu = torch.empty((3, ng), dtype=torch.float32, pin_memory=True).numpy()
+        hu[:] = u.T
+        hf = torch.empty((3, ng), dtype=torch.float32, pin_memory=True).numpy()
+        import ctypes as C
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+        for _ in range(2):
+            s.lib.axg_stiffness_assembled(s.h, fp(hu), fp(hf))
+        barrier(ws)
+        torch.cuda.synchronize()
+        e0 = time.perf_counter()
+        for _ in range(args.steps):
+            rc = s.lib.axg_stiffness_assembled(s.h, fp(hu), fp(hf))
+            assert rc == 0, s.lib.axg_last_error(s.h)
+        torch.cuda.synchronize()
+        e_s = max_over_ranks((time.perf_counter() - e0) / args.steps, ws)
+        assert np.isfinite(hf).all()
+        out["e2e"] = {"value": ws * pts_step / e_s, "unit": "GLL-point-steps/s",
+                      "h2d_bytes_per_step": int(ng * 12), "d2h_bytes_per_step": int(ng * 12)}
+    s.close()
     nbytes = algorithmic_bytes(mesh.nel_solid, ng, len(mesh.ax_el_solid), pole)
     peak, peak_kind = measured_peaks()
     achieved = nbytes / (ms * 1e-3) / 1e9
-    prof = ROOT / "profiles" / f"stiffness_assembly_{args.pole}_{n}x{n}.traffic.json"
-    traffic = None
-    if prof.exists():
-        traffic = json.loads(prof.read_text()).get("dram_bytes_per_step")
+    name = {v: k for k, v in POLES.items()}[pole]
+    prof = ROOT / "profiles" / f"stiffness_assembly_{name}_{n}x{n}.traffic.json"
+    traffic = json.loads(prof.read_text()).get("dram_bytes_per_step") if prof.exists() else None
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                       "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                       "algorithmic_bytes_per_step": nbytes,
+                       "kernel": f"solid_patch_kernel<{name},force> (all colour launches of one step)"}
+    return out
+
+
+def run_gpu(args):
+    ws, rank, local = dist_init()
+    import torch
+    torch.cuda.set_device(local)
+    import axisem_gb300.build as b
+    b.build()
+
+    pole = POLES[args.pole]
+    n = args.size
+    head = measure_stiffness(args, pole, ws, rank, local)
+    mesh, u, info = head.pop("mesh"), head.pop("u"), head["info"]
+    ng = mesh.nglob_solid
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v_all, k_all = time_cpu(mesh, u, args.cpu_seconds, threads)
+        v_one, k_one = time_cpu(mesh, u, args.cpu_seconds / 2, 1)
+        cpu = {"value": v_all, "unit": "GLL-point-steps/s", "cores": threads, "kind": "port",
+               "sample": f"the benchmark's {n}x{n} mesh: {k_all} stiffness+assembly steps on {threads} threads; "
+                         f"{k_one} on one thread",
+               "single_core": v_one,
+               "build": cpu_build()}
+    del mesh, u
+
+    poles = {args.pole: {"value": head["value"], "ms_per_step": head["ms_per_step"], "roofline": head["roofline"],
+                         "e2e": head["e2e"]}}
+    if not args.no_other_poles:
+        for other in (k for k in POLES if k != args.pole):
+            r = measure_stiffness(args, POLES[other], ws, rank, local)
+            r.pop("mesh"), r.pop("u")
+            poles[other] = {"value": r["value"], "ms_per_step": r["ms_per_step"], "roofline": r["roofline"],
+                            "e2e": r["e2e"], "clocks": r["clocks"]}
 
     timeloop = timeloop_anel = timeloop_comp = timeloop_dumps = None
     if args.timeloop_steps > 0:
-        s.close()
         timeloop = run_timeloop(args, pole, ws, rank)
         timeloop_anel = run_timeloop(args, pole, ws, rank, anel=True)
         timeloop_comp = run_timeloop(args, pole, ws, rank, compensated=True)
@@ -277,44 +326,35 @@ def run_gpu(args):
 
     serving = run_serving(args) if args.serve_requests > 0 else None
 
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        v, sample = time_oracle(pole, args.cpu_seconds, 1)
-        cpu = {"value": v, "unit": "GLL-point-steps/s", "cores": 1, "kind": "port", "sample": sample}
-
-    s.close()
     if rank != 0:
         return
     line = {
-        "metric": METRIC, "value": value, "unit": "GLL-point-steps/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "metric": METRIC, "value": head["value"], "unit": "GLL-point-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"stiffness+assembly, {args.pole}pole, {n}x{n} structured quads "
-                               f"({mesh.nel_solid} elements, {ng} global points, 1% axial)",
-                   "pole": args.pole, "elements": mesh.nel_solid, "global_points": ng,
+                               f"({n * n} elements, {ng} global points, 1% axial)",
+                   "pole": args.pole, "elements": n * n, "global_points": ng,
                    "parallelism": f"replicas x{ws}",
                    "l2": "inputs (metric terms) 20x larger than L2; no flush needed"},
-        "e2e": {"value": e2e, "unit": "GLL-point-steps/s", "h2d_bytes_per_step": int(ng * 12),
-                "d2h_bytes_per_step": int(ng * 12)},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_step": nbytes,
-                     "kernel": "solid_patch_kernel<quad,force> (all colour launches of one step)"},
+        "e2e": head["e2e"],
+        "roofline": head["roofline"],
         "cpu_baseline": cpu,
+        "poles": poles,
         "timeloop": timeloop,
         "timeloop_anel": timeloop_anel,
         "timeloop_compensated": timeloop_comp,
         "timeloop_dumps": timeloop_dumps,
         "serving": serving,
-        "clocks": clocks,
+        "clocks": head["clocks"],
         "gpu_launches": int(args.steps * info["kernels_per_force"]),
         "plan": {"patches": info["n_patches_solid"], "colours": info["n_colours_solid"],
                  "patch_elems": info["patch_elems_solid"], "growth": ["compact", "layered"][info["growth_solid"]],
                  "ctas_per_sm": info["ctas_per_sm_force"],
                  "patch_points_over_global": info["patch_points_solid"] / ng,
                  "device_gb": info["device_bytes"] / 1e9},
-        "setup_s": {"mesh": round(t_mesh, 2), "create": round(t_create, 2)},
-        "wall_s": wall,
+        "setup_s": head["setup_s"],
+        "wall_s": head["wall_s"],
     }
     print(json.dumps(line), flush=True)
 
@@ -480,8 +520,8 @@ def main():
     ap.add_argument("--pole", default="quad", choices=list(POLES))
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-other-poles", action="store_true")
     ap.add_argument("--timeloop-steps", type=int, default=64)
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rate", type=float, default=1000.0)   # saturating: measures capacity

@@ -17,8 +17,10 @@
  * All entry points return an `int` status (AXG_OK == 0); none of them
  * calls exit()/abort().  A handle is single-caller: calls on one handle
  * must not overlap.  Every function is `extern "C"`, takes plain pointers
- * and sizes, and can be bound from Fortran with `bind(c)` interfaces
- * (the binding is shown in INTEGRATION.md).
+ * and sizes, and can be bound from Fortran with `bind(c)` interfaces: the
+ * descriptor is a `bind(c)` derived type holding `c_loc` of the module
+ * arrays, and the calls are `bind(c, name='axg_...')` interfaces, as the
+ * reference binds its NetCDF helpers (SOLVER/nc_routines.F90:291-300).
  */
 #ifndef AXISEM_GB300_H
 #define AXISEM_GB300_H
@@ -227,11 +229,16 @@ int axg_stiffness_assembled_device(axg_handle *h, void *stream);
  * u, f) lives in one 32 MiB static device array that every GPU loading the
  * library holds until exit, which limits the mesh to roughly 11 000
  * quadrupole elements (larger meshes return AXG_ERR_BAD_ARG naming the size
- * needed).  The first call on a device looks up the array's device address
- * and sets kernel attributes; make that first call before any stream capture.
- * All calls share the array: calls that overlap on the GPU race (host threads
- * are serialised).  Uses the legacy default stream; host memory is used for
- * planning. */
+ * needed).  Of the descriptor it reads only what a stiffness + assembly
+ * needs: abi_version, npol, src_type, nel_solid, nglob_solid, igloc_solid,
+ * G0, G1, G2, the pole's solid metric arrays, naxel_solid, ax_el_solid and
+ * the pole's axial vectors.  The first call on a device (and the first after
+ * the device's context was replaced, e.g. by cudaDeviceReset) looks up the
+ * array's device address and sets kernel attributes; make that first call
+ * before any stream capture.  All calls share the array, which keeps the
+ * last call's contents (the force region is cleared on every call): calls
+ * that overlap on the GPU race (host threads are serialised).  Uses the
+ * legacy default stream; host memory is used for planning. */
 int axg_stiffness_assembled_noalloc(const axg_mesh_desc *desc, const float *u_gvec, float *f_gvec);
 
 /* Uploads a gvec-layout displacement (nglob_solid,3) into the handle's
@@ -438,6 +445,13 @@ int axg_time_stiffness(axg_handle *h, int32_t n, float *ms_avg);
  * memory.  Fills out8 = {flag, kernel id, source line, 0, index lo, index hi,
  * bound lo, bound hi}; returns AXG_ERR_UNSUPPORTED in normal builds. */
 int axg_device_check_report(int32_t *out8);
+
+/* Self-test of the kernels' bounded device wait: one GPU thread waits on an
+ * mbarrier that nothing arrives at (no copy is involved), through the same
+ * wait the patch kernels use.  *status receives what the wait recorded
+ * (AXG_ERR_TIMEOUT when it gave up as designed) and *elapsed_s how long it
+ * waited (about one second).  No counterpart in the reference. */
+int axg_selftest_wait_timeout(int32_t *status, double *elapsed_s);
 
 void axg_destroy(axg_handle *h);
 

@@ -35,7 +35,10 @@
  * REAL=double (realkind=dp, the FP64 oracle).  Mixed-precision expressions
  * of the reference (FP64 constants deltat, half_dt, third, two; FP64 SLS
  * coefficients) are evaluated in double and rounded to REAL, as Fortran does.
- * Build with -ffp-contract=off so that no FMA changes the rounding.
+ * Build with -ffp-contract=off so that no FMA changes the rounding.  With
+ * -fopenmp the element (and point) loops run on threads; every element's
+ * arithmetic is unchanged and the assembly stays serial in the reference's
+ * order, so the results do not depend on the thread count.
  */
 #include <math.h>
 #include <stdint.h>
@@ -407,6 +410,7 @@ void ORC(stiffness_solid)(const axg_mesh_desc *d, const REAL *u, REAL *out) {
   load_spec(d, &s);
   const int64_t ne = d->nel_solid, cs = 25 * ne;
   unsigned char *ax = axis_flags(d->nel_solid, d->naxel_solid, d->ax_el_solid);
+#pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < ne; ++e) {
     const REAL *u1 = u + 25 * e, *u2 = u1 + cs, *u3 = u2 + cs;
     REAL *o1 = out + 25 * e, *o2 = o1 + cs, *o3 = o2 + cs;
@@ -427,6 +431,7 @@ void ORC(stiffness_fluid)(const axg_mesh_desc *d, const REAL *chi, REAL *out) {
   spec s;
   load_spec(d, &s);
   unsigned char *ax = axis_flags(d->nel_fluid, d->naxel_fluid, d->ax_el_fluid);
+#pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < d->nel_fluid; ++e) {
     const int64_t off = 25 * e;
     mat5 c, X1, X2, S1, S2, m1, m2, m4, loc;
@@ -474,6 +479,7 @@ void ORC(anel_stiffness_cg4)(const axg_mesh_desc *d, const REAL *R, REAL *gs) {
   const int64_t ne = d->nel_solid, cs = 25 * ne;
   const int nsls = d->n_sls;
   unsigned char *ax = axis_flags(d->nel_solid, d->naxel_solid, d->ax_el_solid);
+#pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < ne; ++e) {
     REAL yl[4], vse[4], vsx[4], vze[4], vzx[4], r[7][4];
     load4(yl, CG(d->Y_cg4, e));
@@ -678,8 +684,13 @@ void ORC(time_step_memvars_cg4)(const axg_mesh_desc *d, REAL *memvar, const REAL
   const int nsls = d->n_sls;
   const double third = 1.0 / 3.0;
   unsigned char *ax = axis_flags(d->nel_solid, d->naxel_solid, d->ax_el_solid);
+  /* elements are independent; each thread keeps its own cache of the SLS
+   * weights of the last Q value it met (a deterministic function of Q) */
+#pragma omp parallel
+  {
   double a_mu[32], a_ka[32];
   double Qmu_last = NAN, Qka_last = NAN;
+#pragma omp for schedule(static)
   for (int64_t e = 0; e < ne; ++e) {
     REAL gu[7][4];
     strain_cg4(d, &s, e, ax[e], disp + 25 * e, disp + cs + 25 * e, disp + 2 * cs + 25 * e, gu);
@@ -730,6 +741,7 @@ void ORC(time_step_memvars_cg4)(const axg_mesh_desc *d, REAL *memvar, const REAL
       trm1[k] = src_tr[k];
       for (int c = 1; c <= 6; ++c) devm1[k + 4 * (c - 1)] = src_dev[c][k];
     }
+  }
   }
   free(ax);
 }
@@ -898,10 +910,12 @@ int ORC(time_loop)(const axg_mesh_desc *d, REAL *disp, REAL *velo, REAL *acc0, R
       break;
     }
     /* predictor */
+#pragma omp parallel for schedule(static)
     for (int64_t p = 0; p < cf; ++p)
       chi[p] = (REAL)((double)chi[p] + deltat * dchi[p] + half_dt_sq * ddchi0[p]);
     for (int c = 0; c < 3; ++c) {
       if (c == 1 && mono) continue;
+#pragma omp parallel for schedule(static)
       for (int64_t p = 0; p < cs; ++p)
         disp[p + cs * c] =
             (REAL)((double)disp[p + cs * c] + deltat * velo[p + cs * c] + half_dt_sq * acc0[p + cs * c]);
@@ -959,6 +973,7 @@ int ORC(time_loop)(const axg_mesh_desc *d, REAL *disp, REAL *velo, REAL *acc0, R
     for (int oc = 0; oc < 3; ++oc) {
       const int c = order[oc];
       if (c == 1 && mono) continue;
+#pragma omp parallel for schedule(static)
       for (int64_t p = 0; p < cs; ++p) {
         const int64_t q = p + cs * c;
         const REAL im = (REAL)d->inv_mass_rho[p];

@@ -214,3 +214,44 @@ def symplectic_coefficients(scheme: int, deltat: float):
     cv = np.array(cv, dtype=np.float64) * deltat
     coeff = np.cumsum(cd[:-1])
     return cd, cv, coeff
+
+
+# ---------------------------------------------------------------- timing build
+FAST_LIB = HERE / "_build" / "liboracle_fast.so"
+_fast = None
+
+
+def fast_lib():
+    """The FP32 restatement built for speed (-O3, the host's instruction set,
+    OpenMP): the CPU baseline's timing build, not a parity reference."""
+    global _fast
+    if _fast is None:
+        if not FAST_LIB.exists():
+            build()
+        _fast = C.CDLL(str(FAST_LIB))
+        _fast.orc_fast_colour_elements.restype = C.c_int
+    return _fast
+
+
+class CpuStiffness:
+    """Threaded stiffness + assembly of one mesh on the host cores: elements
+    coloured once (no two elements of a colour share a point), then per
+    colour threads over disjoint element ranges, each element gathering,
+    masking, applying glob_stiffness_<pole>_4 and adding into the assembled
+    force."""
+
+    def __init__(self, mesh):
+        self.mesh = mesh
+        self.d = mesh.desc()
+        self.order = np.zeros(mesh.nel_solid, dtype=np.int32)
+        self.cstart = np.zeros(33, dtype=np.int32)
+        self.ncol = fast_lib().orc_fast_colour_elements(C.byref(self.d), _p(self.order, C.c_int32),
+                                                        _p(self.cstart, C.c_int32))
+        if self.ncol < 0:
+            raise RuntimeError("element colouring needs more than 32 colours")
+
+    def __call__(self, u_gvec: np.ndarray, f_gvec: np.ndarray, threads: int = 0):
+        fast_lib().orc_fast_stiffness_assembled_coloured(
+            C.byref(self.d), _p(self.order, C.c_int32), _p(self.cstart, C.c_int32), C.c_int(self.ncol),
+            _p(u_gvec, C.c_float), _p(f_gvec, C.c_float), C.c_int(threads))
+        return f_gvec

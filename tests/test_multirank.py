@@ -54,7 +54,7 @@ def test_reference_arm_under_torchrun_prints_once():
     env = dict(os.environ, AXG_BENCH_BACKEND="gloo")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_port()), str(ROOT / "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1", "--ref-seconds", "0.2"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1", "--size", "64"]
     r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=300, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
