@@ -1,0 +1,867 @@
+"""Axisymmetric whole-Earth meshes and the precomputed arrays of the time loop.
+
+The reference builds a solve's inputs in two programs: its MESHER writes the
+element skeleton (MESHER/main.f90:52-106), and its SOLVER turns the skeleton
+and the background model into the time loop's arrays in FP64
+(SOLVER/def_precomp_terms.f90).  This module does both for the PREM models of
+``axisem_gb300.earth`` and returns a ``Mesh`` whose arrays go through the
+C-ABI descriptor like the reference's module arrays.
+
+Skeleton (this module's own layout; the reference's MESHER is not restated):
+  * the meridional half-plane (s >= 0) of a sphere of radius 6371 km, north
+    hemisphere built first and mirrored (z -> -z, corner order reversed) to the
+    south, as MESHER/meshgen.f90:1575-1636 mirrors its skeleton;
+  * a central square 0 <= s, z <= a of n_c x n_c bilinear elements, a ring of
+    n_ring layers blending the square's edge into the circle r = R1 (straight
+    edges, the outermost ones arcs of r = R1), then spheroidal shells
+    (edges r = const arcs and theta = const rays) up to the surface, with a
+    radial level on every discontinuity of the model;
+  * elements per wavelength as the reference's mesher sizes them
+    (MESHER/discont_meshing.f90: el_per_lambda = 1.5 over the GLL spacing
+    ratio, the period times the slowest velocity of a domain), and the
+    number of shell elements doubled outward where the surface needs it by
+    conforming coarsening bands: per coarse element three quadrilaterals,
+    alternately mirrored so that the bands' split side edges pair up.
+Every element edge is a straight segment or an arc of constant radius, and the
+element map is the transfinite (Coons) interpolation of its four edges, with
+theta linear along arcs.  On spheroidal elements this is the reference's
+map_spheroid (SOLVER/analytic_spheroid_mapping.f90); axial elements have their
+xi = -1 edge on the axis, as the reference's do.
+
+Precomputed arrays (restated from SOLVER/def_precomp_terms.f90, in FP64,
+rounded to FP32 where the reference stores realkind):
+  * def_mass_matrix_k (:596-800): massmat_k, massmat_kwts2, the solid and
+    fluid inverse masses (assembled in FP32 in pdistsum_solid's walk order,
+    then inverted; the dipole's 1/2), inv_rho_fluid;
+  * def_solid_stiffness_terms / compute_{monopole,dipole,quadrupole}_stiff_terms
+    (:1162-2285) with the elastic tensor c_ijkl_ani (:2291-2335), including
+    the axial vectors M0_w* and the cg4 weights Y_cg4, V_*_cg4;
+  * def_fluid_stiffness_terms (:2336-2467) and def_solid_fluid_boundary_terms
+    (:2474-2799);
+  * compute_pointwisederiv_matrices (:148-290);
+  * the moment-tensor source (define_moment_tensor, SOLVER/source.f90:985-1226,
+    with dsdf/dzdf_elem_solid, SOLVER/pointwise_derivatives.f90:419-476) and
+    the Gaussian source time function (gauss, SOLVER/source.f90:587-598);
+  * the mesh's own checks: volumes, spherical surfaces and the mass of the
+    model (SOLVER/def_grid.f90:992-1332, SOLVER/def_precomp_terms.f90:998-1160).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from .earth import CMB, DISCONTINUITIES_KM, FLUID_DOMAIN, ICB, NDISC, R_EARTH, domain_of, velocity
+from .mesh import F32, I32, Mesh
+from .spectral import Spectral
+
+SP = Spectral()
+_h = np.diff(SP.eta)
+GLL_SPACING_RATIO = float(_h.max() / _h.mean())   # maxh / aveh of the GLL nodes (1.309 for npol = 4)
+EDGE_BOTTOM, EDGE_RIGHT, EDGE_TOP, EDGE_LEFT = 0, 1, 2, 3
+
+
+# ============================================================== skeleton
+@dataclass
+class Skeleton:
+    """Corner nodes (s, z) and elements of the mesh.  elems[e] = (c1, c2, c3,
+    c4) are the corners at (xi, eta) = (-1,-1), (1,-1), (1,1), (-1,1); arc[e, k]
+    marks edge k (bottom c1-c2, right c2-c3, top c4-c3, left c1-c4) as an arc
+    of constant radius; axis[e] marks the xi = -1 edge on the axis."""
+
+    nodes: np.ndarray
+    elems: np.ndarray
+    arc: np.ndarray
+    axis: np.ndarray
+    kind: np.ndarray                  # 0 square, 1 ring, 2 shell, 3 coarsening band
+    info: dict = field(default_factory=dict)
+
+
+class _Builder:
+    def __init__(self):
+        self.key = {}
+        self.nodes = []
+        self.elems = []
+        self.arcs = []
+        self.kinds = []
+
+    def node(self, s, z):
+        s = 0.0 if abs(s) < 1e-3 else float(s)
+        z = 0.0 if abs(z) < 1e-3 else float(z)
+        k = (int(round(s * 1e3)), int(round(z * 1e3)))
+        i = self.key.get(k)
+        if i is None:
+            i = len(self.nodes)
+            self.key[k] = i
+            self.nodes.append((s, z))
+        return i
+
+    def polar(self, r, th):
+        return self.node(r * np.sin(th), r * np.cos(th))
+
+    def elem(self, c, arcs, kind):
+        self.elems.append(tuple(c))
+        self.arcs.append(tuple(arcs))
+        self.kinds.append(kind)
+
+
+def _vmin(idom: int, r0: float, r1: float, model: str) -> float:
+    r = np.linspace(r0, r1, 65)
+    v = velocity(r, "v_p" if idom == FLUID_DOMAIN else "v_s", idom, model)
+    return float(v.min())
+
+
+def _layers(period: float, model: str, el_per_lambda: float, r1: float):
+    """Radial layers from R1 up to the surface: (r_bottom, r_top, domain,
+    target element size), a level on every discontinuity."""
+    d = DISCONTINUITIES_KM * 1000.0
+    out = []
+    tops = list(d) + [r1]
+    for k in range(NDISC - 1, -1, -1):      # inner core first
+        idom = k + 1
+        r_top, r_bot = tops[k], tops[k + 1]
+        h = period * _vmin(idom, r_bot, r_top, model) / (el_per_lambda * GLL_SPACING_RATIO)
+        n = max(1, int(np.ceil((r_top - r_bot) / h)))
+        lv = np.linspace(r_bot, r_top, n + 1)
+        for i in range(n):
+            out.append((lv[i], lv[i + 1], idom, h, i, n))
+    return out
+
+
+def _plan_counts(layers, n_req, n_min_r1: int, n_surf: int):
+    """Outside in from n_surf elements per quarter: a layer becomes a
+    coarsening band (count halved below it) when no neighbour is a band, it is
+    neither the first nor the last layer of its domain, the halved count is
+    even and still resolves every layer below.  Returns (counts at each
+    layer's top, band flags, count at R1)."""
+    L = len(layers)
+    need_below = np.zeros(L)
+    m = 0
+    for i in range(L):
+        need_below[i] = m          # max requirement of the layers below layer i
+        m = max(m, n_req[i])
+    top = np.zeros(L, dtype=np.int64)
+    band = np.zeros(L, dtype=bool)
+    N = n_surf
+    for i in range(L - 1, -1, -1):
+        top[i] = N
+        _, _, idom, _, k, n = layers[i]
+        inner = 0 < k < n - 1
+        if (inner and not (i + 1 < L and band[i + 1]) and N % 4 == 0 and N // 2 >= need_below[i]
+                and N // 2 >= max(n_req[i] * 0.5, 1) and N // 2 >= n_min_r1):
+            band[i] = True
+            N //= 2
+    return top, band, N
+
+
+def build_skeleton(period: float = 50.0, model: str = "prem_iso", el_per_lambda: float = 1.5,
+                   r1_frac: float = 0.5, square_frac: float = 0.55) -> Skeleton:
+    """The element skeleton of a whole-Earth mesh resolving `period` seconds."""
+    r1 = r1_frac * ICB
+    layers = _layers(period, model, el_per_lambda, r1)
+    h_ic = layers[0][3]
+    n_req = np.array([int(np.ceil(0.5 * np.pi * rt / h)) for (_, rt, _, h, _, _) in layers])
+    a = square_frac * r1
+    n_c_min = max(2, int(np.ceil(a / h_ic)))
+    best = None
+    for q in range(0, 7):
+        n_surf = int(np.ceil(n_req[-1] / 2 ** q)) * 2 ** q
+        n_surf += n_surf % 2
+        top, band, n_r1 = _plan_counts(layers, n_req, 2 * n_c_min, n_surf)
+        if n_r1 % 2 or n_r1 < 2 * n_c_min:
+            continue
+        if np.any(top < n_req):
+            continue
+        n_c = n_r1 // 2
+        n_ring = max(1, int(round((r1 - a) / (0.5 * np.pi * r1 / n_r1))))
+        bot = np.where(band, top // 2, top)
+        count = n_c * n_c + n_ring * n_r1 + int(np.sum(np.where(band, 3 * bot, top)))
+        if best is None or count < best[0]:
+            best = (count, top, band, n_c, n_ring)
+    if best is None:
+        raise RuntimeError("no element layout satisfies the resolution")
+    _, top, band, n_c, n_ring = best
+
+    b = _Builder()
+    # central square (north quarter): element (i, j), xi along s, eta along z
+    hs = a / n_c
+    for j in range(n_c):
+        for i in range(n_c):
+            c = [b.node(i * hs, j * hs), b.node((i + 1) * hs, j * hs), b.node((i + 1) * hs, (j + 1) * hs),
+                 b.node(i * hs, (j + 1) * hs)]
+            b.elem(c, (False, False, False, False), 0)
+    # ring: square edge -> circle r = R1, 2 n_c columns (xi from the axis to the equator)
+    m = 2 * n_c
+
+    def sq(k):
+        return (k * hs, a) if k <= n_c else (a, a - (k - n_c) * hs)
+
+    def circ(k):
+        th = k * 0.5 * np.pi / m
+        return (r1 * np.sin(th), r1 * np.cos(th))
+
+    def ring_pt(k, l):
+        t = l / n_ring
+        if l == n_ring:
+            return circ(k)
+        p, q = sq(k), circ(k)
+        return ((1 - t) * p[0] + t * q[0], (1 - t) * p[1] + t * q[1])
+
+    for l in range(n_ring):
+        for k in range(m):
+            c = [b.node(*ring_pt(k, l)), b.node(*ring_pt(k + 1, l)), b.node(*ring_pt(k + 1, l + 1)),
+                 b.node(*ring_pt(k, l + 1))]
+            b.elem(c, (False, False, l + 1 == n_ring, False), 1)
+    # shells and coarsening bands
+    for i, (rb, rt, idom, _, _, _) in enumerate(layers):
+        N = int(top[i])
+        if not band[i]:
+            dth = 0.5 * np.pi / N
+            for k in range(N):
+                c = [b.polar(rb, k * dth), b.polar(rb, (k + 1) * dth), b.polar(rt, (k + 1) * dth),
+                     b.polar(rt, k * dth)]
+                b.elem(c, (True, False, True, False), 2)
+            continue
+        nc_ = N // 2
+        dc = 0.5 * np.pi / nc_
+        df = 0.5 * dc
+        rm = 0.5 * (rb + rt)
+        for j in range(nc_):
+            B0, B1 = b.polar(rb, j * dc), b.polar(rb, (j + 1) * dc)
+            T0, T1, T2 = b.polar(rt, j * dc), b.polar(rt, j * dc + df), b.polar(rt, (j + 1) * dc)
+            X = b.polar(rm, j * dc + df)
+            if j % 2 == 0:   # split side on the left
+                Ls = b.polar(rm, j * dc)
+                b.elem((B0, B1, X, Ls), (True, False, True, False), 3)
+                b.elem((X, B1, T2, T1), (False, False, True, False), 3)
+                b.elem((Ls, X, T1, T0), (True, False, True, False), 3)
+            else:            # split side on the right
+                Rs = b.polar(rm, (j + 1) * dc)
+                b.elem((B0, B1, Rs, X), (True, False, True, False), 3)
+                b.elem((B0, X, T1, T0), (False, False, True, False), 3)
+                b.elem((X, Rs, T2, T1), (True, False, True, False), 3)
+    nodes_n = np.array(b.nodes, dtype=np.float64)
+    elems_n = np.array(b.elems, dtype=np.int64)
+    arcs_n = np.array(b.arcs, dtype=bool)
+    kinds_n = np.array(b.kinds, dtype=np.int8)
+    # the southern hemisphere: z -> -z, corners reversed (c4, c3, c2, c1)
+    for (s, z) in nodes_n:
+        b.node(s, -z)
+    south = np.array([[b.node(nodes_n[c, 0], -nodes_n[c, 1]) for c in el[::-1]] for el in elems_n],
+                     dtype=np.int64)
+    nodes = np.array(b.nodes, dtype=np.float64)
+    elems = np.concatenate([elems_n, south])
+    arcs = np.concatenate([arcs_n, arcs_n[:, [EDGE_TOP, EDGE_RIGHT, EDGE_BOTTOM, EDGE_LEFT]]])
+    kinds = np.concatenate([kinds_n, kinds_n])
+    axis = (nodes[elems[:, 0], 0] == 0.0) & (nodes[elems[:, 3], 0] == 0.0)
+    info = {"period": period, "model": model, "r1": r1, "square": a, "n_c": n_c, "n_ring": n_ring,
+            "n_surface_quarter": int(top[-1]), "bands": int(band.sum()),
+            "layers": [(float(rb), float(rt), int(idom)) for (rb, rt, idom, _, _, _) in layers],
+            "layer_counts": [int(t) for t in top], "band_layers": [int(i) for i in np.flatnonzero(band)],
+            "el_per_lambda": el_per_lambda}
+    return Skeleton(nodes=nodes, elems=elems, arc=arcs, axis=axis, kind=kinds, info=info)
+
+
+# ============================================================== mapping
+def _edge_map(p, q, arc, t):
+    """Points and d/dt of the edges from p (t = -1) to q (t = 1): straight,
+    or an arc of constant radius with theta linear in t.  p, q (E, 2); arc
+    (E,); t (E, n) or (n,).  Returns (E, n, 2) arrays."""
+    t = np.broadcast_to(np.asarray(t, dtype=np.float64), (p.shape[0],) + np.shape(t)[-1:])
+    w0 = 0.5 * (1.0 - t)[..., None]
+    w1 = 0.5 * (1.0 + t)[..., None]
+    pt = w0 * p[:, None, :] + w1 * q[:, None, :]
+    dt = np.broadcast_to(0.5 * (q - p)[:, None, :], pt.shape).copy()
+    if np.any(arc):
+        a = np.flatnonzero(arc)
+        rp = np.hypot(p[a, 0], p[a, 1])
+        rq = np.hypot(q[a, 0], q[a, 1])
+        R = 0.5 * (rp + rq)
+        thp = np.arctan2(np.maximum(p[a, 0], 0.0), p[a, 1])
+        thq = np.arctan2(np.maximum(q[a, 0], 0.0), q[a, 1])
+        th = 0.5 * (1.0 - t[a]) * thp[:, None] + 0.5 * (1.0 + t[a]) * thq[:, None]
+        pt[a, :, 0] = R[:, None] * np.sin(th)
+        pt[a, :, 1] = R[:, None] * np.cos(th)
+        half = 0.5 * (thq - thp) * R
+        dt[a, :, 0] = half[:, None] * np.cos(th)
+        dt[a, :, 1] = -half[:, None] * np.sin(th)
+    return pt, dt
+
+
+def element_geometry(sk: Skeleton, els: np.ndarray | None = None):
+    """s, z and the partial derivatives ds/dxi, dz/dxi, ds/deta, dz/deta at
+    the 5 x 5 points of elements `els`: GLL x GLL, or GLJ(0,1) x GLL on axial
+    elements (compute_partial_derivatives, SOLVER/analytic_mapping.f90:680-700).
+    Arrays (E, 5 [ipol], 5 [jpol])."""
+    els = np.arange(len(sk.elems)) if els is None else els
+    el = sk.elems[els]
+    c = [sk.nodes[el[:, k]] for k in range(4)]
+    arc = sk.arc[els]
+    ax = sk.axis[els]
+    xi = np.where(ax[:, None], SP.xi_k[None, :], SP.eta[None, :])   # (E, 5)
+    eta = SP.eta
+    B, dB = _edge_map(c[0], c[1], arc[:, EDGE_BOTTOM], xi)
+    T, dT = _edge_map(c[3], c[2], arc[:, EDGE_TOP], xi)
+    Lf, dLf = _edge_map(c[0], c[3], arc[:, EDGE_LEFT], eta)
+    Rt, dRt = _edge_map(c[1], c[2], arc[:, EDGE_RIGHT], eta)
+    X = xi[:, :, None, None]                      # (E, i, 1, 1)
+    Y = eta[None, None, :, None]                  # (1, 1, j, 1)
+    C = [ck[:, None, None, :] for ck in c]
+    bil = 0.25 * ((1 - X) * (1 - Y) * C[0] + (1 + X) * (1 - Y) * C[1] + (1 + X) * (1 + Y) * C[2]
+                  + (1 - X) * (1 + Y) * C[3])
+    dbx = 0.25 * (-(1 - Y) * C[0] + (1 - Y) * C[1] + (1 + Y) * C[2] - (1 + Y) * C[3])
+    dby = 0.25 * (-(1 - X) * C[0] - (1 + X) * C[1] + (1 + X) * C[2] + (1 - X) * C[3])
+    Bi, Ti = B[:, :, None, :], T[:, :, None, :]
+    dBi, dTi = dB[:, :, None, :], dT[:, :, None, :]
+    Lj, Rj = Lf[:, None, :, :], Rt[:, None, :, :]
+    dLj, dRj = dLf[:, None, :, :], dRt[:, None, :, :]
+    x = 0.5 * (1 - Y) * Bi + 0.5 * (1 + Y) * Ti + 0.5 * (1 - X) * Lj + 0.5 * (1 + X) * Rj - bil
+    dx = 0.5 * (1 - Y) * dBi + 0.5 * (1 + Y) * dTi - 0.5 * Lj + 0.5 * Rj - dbx
+    dy = -0.5 * Bi + 0.5 * Ti + 0.5 * (1 - X) * dLj + 0.5 * (1 + X) * dRj - dby
+    s = x[..., 0]
+    s = np.where(np.abs(s) < 1e-6 * R_EARTH, 0.0, s)   # on the axis (map_spheroid's min_distance_dim)
+    return {"s": s, "z": x[..., 1], "dsdxi": dx[..., 0], "dzdxi": dx[..., 1], "dsdeta": dy[..., 0],
+            "dzdeta": dy[..., 1], "axis": ax, "xi": xi}
+
+
+# ============================================================== numbering
+def global_numbering(sk: Skeleton, els: np.ndarray):
+    """igloc (1-based, walk ipol fastest per element) of the points of
+    elements `els`, numbered topologically: a corner by its node, an edge
+    point by its edge and its position from the lower node id, an interior
+    point by its element.  Returns (igloc, nglob)."""
+    el = sk.elems[els]
+    E = len(els)
+    nn = len(sk.nodes)
+    keys = np.zeros((E, 5, 5), dtype=np.int64)   # [e, i, j]
+    c1, c2, c3, c4 = (el[:, k] for k in range(4))
+    keys[:, 0, 0], keys[:, 4, 0], keys[:, 4, 4], keys[:, 0, 4] = c1, c2, c3, c4
+    base = nn
+
+    def ekey(a, b, k):
+        lo, hi = np.minimum(a, b), np.maximum(a, b)
+        kk = np.where(a < b, k, 4 - k)
+        return base + (lo * nn + hi) * 5 + kk
+
+    for k in range(1, 4):
+        keys[:, k, 0] = ekey(c1, c2, k)
+        keys[:, k, 4] = ekey(c4, c3, k)
+        keys[:, 0, k] = ekey(c1, c4, k)
+        keys[:, 4, k] = ekey(c2, c3, k)
+    ibase = base + nn * nn * 5 + 5
+    loc = np.arange(25).reshape(5, 5)
+    for i in range(1, 4):
+        for j in range(1, 4):
+            keys[:, i, j] = ibase + np.asarray(els, dtype=np.int64) * 25 + loc[i, j]
+    flat = keys.transpose(0, 2, 1).reshape(-1)    # element-major, then jpol, ipol fastest
+    uniq, inv = np.unique(flat, return_inverse=True)
+    return (inv + 1).astype(I32), len(uniq)
+
+
+# ============================================================== precomputed terms
+def _c_ijkl(lam, mu, xi_a, phi_a, eta_a, th_fa, ph_fa, i, j, k, l):
+    """c_ijkl_ani (SOLVER/def_precomp_terms.f90:2291-2335): the elastic tensor
+    of a transversely isotropic medium with fast axis (th_fa, ph_fa)
+    (Nolet 2008, eq. 16.2); indices 1..3."""
+    d = lambda a, b: 1.0 if a == b else 0.0  # noqa: E731
+    sv = [np.cos(ph_fa) * np.sin(th_fa), np.sin(ph_fa) * np.sin(th_fa), np.cos(th_fa)]
+    s = lambda a: sv[a - 1]  # noqa: E731
+    c = lam * d(i, j) * d(k, l) + mu * (d(i, k) * d(j, l) + d(i, l) * d(j, k))
+    c = c + ((eta_a - 1.0) * lam + 2.0 * eta_a * mu * (1.0 - 1.0 / xi_a)) * (d(i, j) * s(k) * s(l)
+                                                                            + d(k, l) * s(i) * s(j))
+    c = c + mu * (1.0 / xi_a - 1.0) * (d(i, k) * s(j) * s(l) + d(i, l) * s(j) * s(k) + d(j, k) * s(i) * s(l)
+                                       + d(j, l) * s(i) * s(k))
+    c = c + ((1.0 - 2.0 * eta_a + phi_a) * (lam + 2.0 * mu) + (4.0 * eta_a - 4.0) * mu / xi_a) * (
+        s(i) * s(j) * s(k) * s(l))
+    return c
+
+
+def _pdistsum_f32(vals_f: np.ndarray, igloc: np.ndarray, nglob: int) -> np.ndarray:
+    """pdistsum_solid / pdistsum_fluid (SOLVER/commun.F90:69-283) of an
+    element-local FP32 field (5, 5, E): edge points summed in FP32 in the walk
+    order (element by element, ipol fastest, interior points skipped), the sums
+    scattered back."""
+    E = vals_f.shape[2]
+    ig = igloc.reshape(E, 5, 5) - 1                # [e, j, i]
+    v = np.asarray(vals_f, dtype=F32).transpose(2, 1, 0)   # [e, j, i]
+    edge = np.zeros((5, 5), dtype=bool)
+    edge[0, :] = edge[4, :] = edge[:, 0] = edge[:, 4] = True
+    idx = ig[:, edge].reshape(-1)
+    g = np.zeros(nglob, dtype=F32)
+    np.add.at(g, idx, v[:, edge].reshape(-1))
+    out = v.copy()
+    out[:, edge] = g[ig[:, edge]]
+    return np.asfortranarray(out.transpose(2, 1, 0))
+
+
+def _to_f(a):
+    """(E, i, j) FP64 -> Fortran (i, j, E) FP32."""
+    return np.asfortranarray(np.transpose(a, (1, 2, 0)).astype(F32))
+
+
+@dataclass
+class SphereSolve:
+    """Options of one solve on a whole-Earth mesh."""
+
+    pole: int = _abi.MONOPOLE
+    source: str = ""                 # explosion / mrr / mtt_p_mpp (mono), mtr / mpr (di), mtp / mtt_m_mpp (quad)
+    depth_km: float = 100.0
+    magnitude: float = 1e20
+    seconds: float = 1800.0
+    receivers_deg: np.ndarray | None = None     # colatitudes of surface receivers
+    seis_it: int = 1
+    courant: float = 0.6
+
+
+def build_mesh(period: float = 50.0, solve: SphereSolve | None = None, model: str = "prem_iso",
+               skeleton: Skeleton | None = None, pointwise: bool = True, attenuation=None) -> Mesh:
+    """A whole-Earth solve on the PREM model at `period` seconds: the skeleton,
+    every precomputed array of the time loop, source, receivers and the source
+    time function, as a ``Mesh`` (FP32 module arrays, 1-based indices)."""
+    solve = solve or SphereSolve()
+    sk = skeleton or build_skeleton(period, model)
+    pole = solve.pole
+    geo = element_geometry(sk)
+    s, z = geo["s"], geo["z"]
+    dsdxi, dzdxi, dsdeta, dzdeta = geo["dsdxi"], geo["dzdxi"], geo["dsdeta"], geo["dzdeta"]
+    ax = geo["axis"]
+    E = len(sk.elems)
+    r = np.hypot(s, z)
+    theta = np.arctan2(s, z)
+    jac = dsdxi * dzdeta - dsdeta * dzdxi
+    if not (jac > 0).all():
+        raise RuntimeError(f"mesh has {int((jac <= 0).sum())} points with a non-positive Jacobian")
+    idom_el = domain_of(r[:, 2, 2])
+    idom = np.broadcast_to(idom_el[:, None, None], r.shape)
+    fluid_el = idom_el == FLUID_DOMAIN
+    # materials at the GLL points (read_model, SOLVER/get_model.F90:149-200)
+    rho = velocity(r, "rho", idom, model)
+    vph, vpv = velocity(r, "vph", idom, model), velocity(r, "vpv", idom, model)
+    vsh, vsv = velocity(r, "vsh", idom, model), velocity(r, "vsv", idom, model)
+    eta_a = velocity(r, "eta", idom, model)
+    lam = rho * (vph ** 2 - 2.0 * vsh ** 2)
+    mu = rho * vsh ** 2
+    xi_a = np.where(vsv > 1e-6 * vph, vsh ** 2 / np.where(vsv > 0, vsv, 1.0) ** 2, 1.0)
+    phi_a = vpv ** 2 / vph ** 2
+
+    # ---- weights and the axial s / (1 + xi) (s_over_oneplusxi_axis)
+    wti = np.where(ax[:, None], SP.wt_axial_k[None, :], SP.wt[None, :])[:, :, None]   # (E, i, 1)
+    wtj = SP.wt[None, None, :]
+    xi = geo["xi"][:, :, None]
+    onexi = 1.0 + xi
+    sox = np.where(ax[:, None, None], np.where(xi == -1.0, dsdxi, s / np.where(onexi == 0, 1.0, onexi)), s)
+    inv_j = 1.0 / jac
+    # massmat_k and massmat_kwts2 (def_mass_matrix_k)
+    massmat = jac * sox * wti * wtj
+    with np.errstate(divide="ignore", invalid="ignore"):
+        kw_non = jac / s * wti * wtj
+        kw_ax = np.where(xi == -1.0, jac / sox, jac / (s * onexi)) * wti * wtj
+    massmat_kwts2 = np.where(ax[:, None, None], kw_ax, kw_non)
+    # the alpha .. zeta and Ms_* terms times the weights (alpha, alphak, ..., analytic_mapping.f90)
+    sfac = sox * wti * wtj        # s wt wt (non-axial); s/(1+xi) wt_ax wt (axial)
+    T = {
+        "alpha": -inv_j * dsdxi * dsdeta * sfac, "beta": inv_j * dsdxi ** 2 * sfac,
+        "gamma": inv_j * dsdeta ** 2 * sfac, "delta": -inv_j * dzdxi * dzdeta * sfac,
+        "epsil": inv_j * dzdxi ** 2 * sfac, "zeta": inv_j * dzdeta ** 2 * sfac,
+        "Mzes_xi": inv_j * dsdxi * dzdeta * sfac, "Mzes_eta": -inv_j * dsdeta * dzdeta * sfac,
+        "Mzxs_eta": inv_j * dsdeta * dzdxi * sfac, "Mzxs_xi": -inv_j * dsdxi * dzdxi * sfac,
+    }
+    mfac = np.where(ax[:, None, None], np.where(xi == -1.0, 0.0, wti * wtj / np.where(onexi == 0, 1.0, onexi)),
+                    wti * wtj)
+    Msxi, Mzxi = dsdxi * mfac, -dzdxi * mfac
+    Mzeta, Mseta = dzdeta * mfac, -dsdeta * mfac
+    # non_diag_fact of axial elements: wt_ax(0) wt(j) J(xi_0, eta_j) / s_over_oneplusxi
+    ndf = SP.wt_axial_k[0] * SP.wt[None, :] * jac[:, 0, :] / np.where(ax[:, None], dsdxi[:, 0, :], 1.0)
+    ndf = np.where(ax[:, None], ndf, 0.0)
+
+    solid = np.flatnonzero(~fluid_el)
+    fluid = np.flatnonzero(fluid_el)
+    ig_s, ng_s = global_numbering(sk, solid)
+    m = Mesh(src_type=pole, nel_solid=len(solid), nglob_solid=ng_s, igloc_solid=ig_s,
+             ax_el_solid=(np.flatnonzero(ax[solid]) + 1).astype(I32), spec=SP, m_solid={}, m0_solid={},
+             inv_mass_rho=None)
+    # ---- solid stiffness terms
+    S = solid
+    th_fa = theta[S]
+    C = {}
+    args = (lam[S], mu[S], xi_a[S], phi_a[S], eta_a[S], th_fa, 0.0)
+    for nm, ijkl in (("11", (1, 1, 1, 1)), ("12", (1, 1, 2, 2)), ("13", (1, 1, 3, 3)), ("15", (1, 1, 3, 1)),
+                     ("22", (2, 2, 2, 2)), ("23", (2, 2, 3, 3)), ("25", (2, 2, 3, 1)), ("33", (3, 3, 3, 3)),
+                     ("35", (3, 3, 3, 1)), ("44", (2, 3, 2, 3)), ("46", (2, 3, 1, 2)), ("55", (3, 1, 3, 1)),
+                     ("66", (1, 2, 1, 2))):
+        C[nm] = _c_ijkl(*args, *ijkl)
+    t = {k: v[S] for k, v in T.items()}
+    kw = massmat_kwts2[S]
+    Ms, Mz, Me, Mse = Msxi[S], Mzxi[S], Mzeta[S], Mseta[S]
+    axS = ax[S]
+    M = {}
+    if pole in (_abi.MONOPOLE, _abi.QUADPOLE):
+        M["M11s"] = C["11"] * t["delta"] + C["15"] * t["Mzes_xi"] + C["15"] * t["Mzxs_eta"] + C["55"] * t["alpha"]
+        M["M21s"] = C["11"] * t["zeta"] + C["15"] * 2.0 * t["Mzes_eta"] + C["55"] * t["gamma"]
+        M["M41s"] = C["11"] * t["epsil"] + C["15"] * 2.0 * t["Mzxs_xi"] + C["55"] * t["beta"]
+        M["M12s"] = C["15"] * t["delta"] + C["13"] * t["Mzes_xi"] + C["55"] * t["Mzxs_eta"] + C["35"] * t["alpha"]
+        M["M22s"] = C["15"] * t["zeta"] + (C["13"] + C["55"]) * t["Mzes_eta"] + C["35"] * t["gamma"]
+        M["M32s"] = C["15"] * t["delta"] + C["13"] * t["Mzxs_eta"] + C["55"] * t["Mzes_xi"] + C["35"] * t["alpha"]
+        M["M42s"] = C["15"] * t["epsil"] + (C["13"] + C["55"]) * t["Mzxs_xi"] + C["35"] * t["beta"]
+        M["M_1"] = C["12"] * Me + C["25"] * Mse
+        M["M_2"] = C["12"] * Mz + C["25"] * Ms
+        M["M_3"] = C["23"] * Mse + C["25"] * Me
+        M["M_4"] = C["23"] * Ms + C["25"] * Mz
+    else:  # dipole: the + and - components
+        M["M11s"] = (C["11"] + C["66"]) * t["delta"] + (C["15"] + C["46"]) * (t["Mzes_xi"] + t["Mzxs_eta"]) \
+            + (C["55"] + C["44"]) * t["alpha"]
+        M["M21s"] = (C["11"] + C["66"]) * t["zeta"] + (C["15"] + C["46"]) * 2.0 * t["Mzes_eta"] \
+            + (C["55"] + C["44"]) * t["gamma"]
+        M["M41s"] = (C["11"] + C["66"]) * t["epsil"] + (C["15"] + C["46"]) * 2.0 * t["Mzxs_xi"] \
+            + (C["55"] + C["44"]) * t["beta"]
+        M["M12s"] = (C["11"] - C["66"]) * t["delta"] + (C["15"] - C["46"]) * (t["Mzes_xi"] + t["Mzxs_eta"]) \
+            + (C["55"] - C["44"]) * t["alpha"]
+        M["M22s"] = (C["11"] - C["66"]) * t["zeta"] + (C["15"] - C["46"]) * 2.0 * t["Mzes_eta"] \
+            + (C["55"] - C["44"]) * t["gamma"]
+        M["M42s"] = (C["11"] - C["66"]) * t["epsil"] + (C["15"] - C["46"]) * 2.0 * t["Mzxs_xi"] \
+            + (C["55"] - C["44"]) * t["beta"]
+        M["M13s"] = C["15"] * t["delta"] + C["13"] * t["Mzes_xi"] + C["55"] * t["Mzxs_eta"] + C["35"] * t["alpha"]
+        M["M32s"] = C["15"] * t["zeta"] + (C["13"] + C["55"]) * t["Mzes_eta"] + C["35"] * t["gamma"]
+        M["M33s"] = C["15"] * t["delta"] + C["13"] * t["Mzxs_eta"] + C["55"] * t["Mzes_xi"] + C["35"] * t["alpha"]
+        M["M43s"] = C["15"] * t["epsil"] + (C["13"] + C["55"]) * t["Mzxs_xi"] + C["35"] * t["beta"]
+        M["M_1"] = (C["12"] + C["66"]) * 2.0 * Me + (C["25"] + C["46"]) * 2.0 * Mse
+        M["M_2"] = (C["12"] + C["66"]) * 2.0 * Mz + (C["25"] + C["46"]) * 2.0 * Ms
+        M["M_3"] = C["46"] * Me + C["44"] * Mse
+        M["M_4"] = C["46"] * Mz + C["44"] * Ms
+        M["M_5"] = (C["12"] - C["66"]) * 2.0 * Me + (C["25"] - C["46"]) * 2.0 * Mse
+        M["M_6"] = (C["12"] - C["66"]) * 2.0 * Mz + (C["25"] - C["46"]) * 2.0 * Ms
+        M["M_7"] = C["25"] * 2.0 * Me + C["23"] * 2.0 * Mse
+        M["M_8"] = C["25"] * 2.0 * Mz + C["23"] * 2.0 * Ms
+        M["M_w1"] = 4.0 * (C["22"] + C["66"]) * kw
+        M["M_w2"] = 2.0 * C["46"] * kw
+        M["M_w3"] = C["44"] * kw
+    M["M11z"] = C["55"] * t["delta"] + C["35"] * (t["Mzes_xi"] + t["Mzxs_eta"]) + C["33"] * t["alpha"]
+    M["M21z"] = C["55"] * t["zeta"] + C["35"] * 2.0 * t["Mzes_eta"] + C["33"] * t["gamma"]
+    M["M41z"] = C["55"] * t["epsil"] + C["35"] * 2.0 * t["Mzxs_xi"] + C["33"] * t["beta"]
+    if pole == _abi.MONOPOLE:
+        M["M11z"] = C["55"] * t["delta"] + C["35"] * t["Mzes_xi"] + C["35"] * t["Mzxs_eta"] + C["33"] * t["alpha"]
+        M["M_w1"] = C["22"] * kw
+    if pole == _abi.QUADPOLE:
+        M["M1phi"] = C["66"] * t["delta"] + C["46"] * t["Mzes_xi"] + C["46"] * t["Mzxs_eta"] + C["44"] * t["alpha"]
+        M["M2phi"] = C["66"] * t["zeta"] + C["46"] * 2.0 * t["Mzes_eta"] + C["44"] * t["gamma"]
+        M["M4phi"] = C["66"] * t["epsil"] + C["46"] * 2.0 * t["Mzxs_xi"] + C["44"] * t["beta"]
+        M["M_5"] = C["66"] * Me + C["46"] * Mse
+        M["M_6"] = C["66"] * Mz + C["46"] * Ms
+        M["M_7"] = C["44"] * Mse + C["46"] * Me
+        M["M_8"] = C["44"] * Ms + C["46"] * Mz
+        M["M_w1"] = (C["22"] + 4.0 * C["66"]) * kw
+        M["M_w2"] = -2.0 * (C["22"] + C["66"]) * kw
+        M["M_w3"] = 2.0 * C["46"] * kw
+        M["M_w4"] = (4.0 * C["22"] + C["66"]) * kw
+        M["M_w5"] = 4.0 * C["44"] * kw
+    # axial masking of the ipol = 0 rows (compute_*_stiff_terms)
+    zero_rows = ["M_w1"] + ([] if pole == _abi.MONOPOLE else
+                            ["M_1", "M_2", "M_3", "M_4", "M_5", "M_6", "M_7", "M_8", "M_w1", "M_w3"]
+                            + (["M_w2", "M_w4", "M_w5"] if pole == _abi.QUADPOLE else []))
+    for nm in set(zero_rows):
+        M[nm][axS, 0, :] = 0.0
+    # axial vectors M0_w* (ipol = 0 of axial elements)
+    ndfS = ndf[S]
+    C0 = {k: v[:, 0, :] for k, v in C.items()}
+    wa0 = SP.wt_axial_k[0] * SP.wt[None, :]
+    dsx0, dzx0 = dsdxi[S][:, 0, :], dzdxi[S][:, 0, :]
+    M0 = {}
+    if pole == _abi.MONOPOLE:
+        M0["M0_w1"] = (2.0 * C0["12"] + C0["22"]) * ndfS
+        M0["M0_w2"] = C0["25"] * ndfS
+        M0["M0_w3"] = C0["23"] * dsx0 * wa0 - C0["25"] * dzx0 * wa0
+    elif pole == _abi.DIPOLE:
+        M0["M0_w1"] = (C0["12"] + C0["66"]) * 2.0 * ndfS
+        M0["M0_w2"] = -(C0["12"] + C0["66"]) * 2.0 * dzx0 * wa0
+        M0["M0_w3"] = C0["46"] * ndfS
+        M0["M0_w4"] = -C0["46"] * dzx0 * wa0
+        M0["M0_w5"] = np.zeros_like(ndfS)
+        M0["M0_w6"] = (C0["25"] + C0["46"]) * 2.0 * dsx0 * wa0
+        M0["M0_w7"] = C0["44"] * ndfS
+        M0["M0_w8"] = C0["44"] * dsx0 * wa0
+        M0["M0_w9"] = (C0["12"] + C0["22"]) * 4.0 * ndfS
+        M0["M0_w10"] = (2.0 * C0["25"] + C0["46"]) * ndfS
+    else:
+        M0["M0_w1"] = (2.0 * C0["12"] + C0["22"] + 4.0 * C0["66"]) * ndfS
+        M0["M0_w2"] = -2.0 * (C0["12"] + C0["22"]) * ndfS
+        M0["M0_w3"] = (C0["25"] + 4.0 * C0["46"]) * ndfS
+        M0["M0_w4"] = (4.0 * C0["22"] - C0["66"]) * ndfS
+        M0["M0_w5"] = -2.0 * C0["25"] * ndfS
+        M0["M0_w6"] = 4.0 * C0["44"] * ndfS
+    for k in M0:
+        M0[k] = np.where(axS[:, None], M0[k], 0.0)
+    used = set(_abi.SOLID_TERMS_USED[pole])
+    m.m_solid = {k: _to_f(M[k]) for k in used}
+    used0 = set(_abi.AXIAL_TERMS_USED[pole])
+    m.m0_solid = {k: np.asfortranarray(M0[k].T.astype(F32)) for k in used0}
+    # solid inverse mass (def_mass_matrix_k): FP32 rho * massmat_k, assembled, inverted
+    mass_s = _to_f(rho[S] * massmat[S])
+    unassem = mass_s * F32(2.0) if pole == _abi.DIPOLE else mass_s
+    m.meta["unassem_mass_rho_solid"] = np.asfortranarray(unassem)
+    mass_s = _pdistsum_f32(mass_s, ig_s, ng_s)
+    inv_s = (F32(1.0) / mass_s).astype(F32)
+    if pole == _abi.DIPOLE:
+        inv_s = (inv_s * F32(0.5)).astype(F32)
+    m.inv_mass_rho = np.asfortranarray(inv_s)
+    m.meta.update(skeleton=sk.info, kind="sphere", period=period, model=model,
+                  massmat_k=massmat, rho=rho, solid=solid, fluid=fluid, r=r, theta=theta)
+
+    # ---- fluid
+    if len(fluid):
+        ig_f, ng_f = global_numbering(sk, fluid)
+        Fl = fluid
+        m.nel_fluid, m.nglob_fluid, m.igloc_fluid = len(Fl), ng_f, ig_f
+        m.ax_el_fluid = (np.flatnonzero(ax[Fl]) + 1).astype(I32)
+        rf = rho[Fl]
+        m.m_fluid = {"M1chi_fl": _to_f((T["delta"][Fl] + T["alpha"][Fl]) / rf),
+                     "M2chi_fl": _to_f((T["zeta"][Fl] + T["gamma"][Fl]) / rf),
+                     "M4chi_fl": _to_f((T["epsil"][Fl] + T["beta"][Fl]) / rf)}
+        if pole != _abi.MONOPOLE:
+            mw = massmat_kwts2[Fl] / rf
+            mw[ax[Fl], 0, :] = 0.0
+            m0 = np.where(ax[Fl][:, None], ndf[Fl] / rf[:, 0, :], 0.0)
+            if pole == _abi.QUADPOLE:
+                mw, m0 = 4.0 * mw, 4.0 * m0
+            m.m_fluid["M_w_fl"] = _to_f(mw)
+            m.m0_w_fl = np.asfortranarray(m0.T.astype(F32))
+        lam_f = lam[Fl]
+        mass_f = _to_f(massmat[Fl] / lam_f)
+        m.meta["unassem_mass_lam_fluid"] = np.asfortranarray(mass_f)
+        mass_f = _pdistsum_f32(mass_f, ig_f, ng_f)
+        m.inv_mass_fluid = np.asfortranarray((F32(1.0) / mass_f).astype(F32))
+        _boundary(m, sk, geo, solid, fluid)
+    if pointwise:
+        _pointwise(m, geo, solid, fluid, rho)
+    _source_receivers(m, sk, geo, solve, period)
+    return m
+
+
+def _boundary(m: Mesh, sk: Skeleton, geo, solid, fluid):
+    """The solid-fluid boundary tables and bdry_matr
+    (def_solid_fluid_boundary_terms, SOLVER/def_precomp_terms.f90:2474-2799):
+    for every solid element edge on the CMB or the ICB, the fluid element
+    across it; bdry_matr(ipol, 1:2) = dtheta/2 w sin(theta) (sin, cos)(theta)
+    r^2, with the axial L'Hopital point, negative where the fluid lies above
+    the solid (the ICB)."""
+    def edge_index(els):
+        el = sk.elems[els]
+        bot = np.stack([np.minimum(el[:, 0], el[:, 1]), np.maximum(el[:, 0], el[:, 1])], 1)
+        topk = np.stack([np.minimum(el[:, 3], el[:, 2]), np.maximum(el[:, 3], el[:, 2])], 1)
+        return bot, topk
+    sb, st = edge_index(solid)
+    fb, ft = edge_index(fluid)
+    fmap = {}
+    for k in range(len(fluid)):
+        fmap[tuple(fb[k])] = (k, 0)
+        fmap[tuple(ft[k])] = (k, 4)
+    rows = []
+    for k in range(len(solid)):
+        for ed, jp in ((sb[k], 0), (st[k], 4)):
+            hit = fmap.get(tuple(ed))
+            if hit is not None:
+                rows.append((k, jp, hit[0], hit[1]))
+    rows.sort()
+    nb = len(rows)
+    bs = np.array([r[0] for r in rows], dtype=np.int64)
+    js = np.array([r[1] for r in rows], dtype=np.int64)
+    bf = np.array([r[2] for r in rows], dtype=np.int64)
+    jf = np.array([r[3] for r in rows], dtype=np.int64)
+    s, z = geo["s"][solid][bs], geo["z"][solid][bs]     # (nb, 5, 5)
+    sf, zf = geo["s"][fluid][bf], geo["z"][fluid][bf]
+    ip = np.arange(5)
+    ss, zs = s[np.arange(nb)[:, None], ip[None, :], js[:, None]], z[np.arange(nb)[:, None], ip[None, :], js[:, None]]
+    sff, zff = sf[np.arange(nb)[:, None], ip[None, :], jf[:, None]], zf[np.arange(nb)[:, None], ip[None, :], jf[:, None]]
+    if np.max(np.hypot(ss - sff, zs - zff)) > 1e-3:
+        raise RuntimeError("solid and fluid boundary points do not coincide")
+    r = np.hypot(ss, zs)
+    th = np.arctan2(ss, zs)
+    dth = 0.5 * np.abs(th[:, 4] - th[:, 0])
+    axs = geo["axis"][solid][bs]
+    w = np.where(axs[:, None], SP.wt_axial_k[None, :], SP.wt[None, :])
+    xi = np.where(axs[:, None], SP.xi_k[None, :], SP.eta[None, :])
+    fac = np.where(axs[:, None], 1.0 / np.where(xi == -1.0, 1.0, 1.0 + xi), 1.0)
+    b1 = dth[:, None] * w * np.sin(th) * fac * np.sin(th)
+    b2 = dth[:, None] * w * np.sin(th) * fac * np.cos(th)
+    if axs.any():
+        # the axis point: 0 and (1/r) dtheta/2 w_ax(0) s/(1+xi) at xi = -1 (= ds/dxi)
+        dsx = geo["dsdxi"][solid][bs][np.arange(nb), 0, js]
+        b1[axs, 0] = 0.0
+        b2[axs, 0] = (1.0 / r[axs, 0]) * dth[axs] * SP.wt_axial_k[0] * dsx[axs]
+    rad = r[:, 0]
+    sign = np.where(np.abs(rad - ICB) < 1.0, -1.0, 1.0)
+    b1 = b1 * sign[:, None] * rad[:, None] ** 2
+    b2 = b2 * sign[:, None] * rad[:, None] ** 2
+    m.bdry_solid_el = (bs + 1).astype(I32)
+    m.bdry_fluid_el = (bf + 1).astype(I32)
+    m.bdry_jpol_solid = js.astype(I32)
+    m.bdry_jpol_fluid = jf.astype(I32)
+    m.bdry_matr = np.asfortranarray(np.stack([b1.T, b2.T], axis=2).astype(F32))   # (5, nb, 2)
+    m.meta["bdry_radius"] = rad
+
+
+def _pointwise(m: Mesh, geo, solid, fluid, rho):
+    """data_pointwise (compute_pointwisederiv_matrices,
+    SOLVER/def_precomp_terms.f90:148-290): the mapping derivatives over the
+    Jacobian, 1/s (1 on the axis points of axial elements) and the fluid's
+    1/rho."""
+    jac = geo["dsdxi"] * geo["dzdeta"] - geo["dsdeta"] * geo["dzdxi"]
+    pw = {}
+
+    def put(els, suf):
+        j = jac[els]
+        pw[f"DsDeta_over_J_{suf}"] = _to_f(-geo["dsdeta"][els] / j)
+        pw[f"DzDeta_over_J_{suf}"] = _to_f(geo["dzdeta"][els] / j)
+        pw[f"DsDxi_over_J_{suf}"] = _to_f(geo["dsdxi"][els] / j)
+        pw[f"DzDxi_over_J_{suf}"] = _to_f(-geo["dzdxi"][els] / j)
+        sv = geo["s"][els]
+        with np.errstate(divide="ignore"):
+            inv = np.where(sv > 0, 1.0 / np.where(sv > 0, sv, 1.0), 1.0)
+        inv[geo["axis"][els], 0, :] = 1.0
+        return inv
+
+    inv_s = put(solid, "sol")
+    pw["inv_s_solid"] = _to_f(inv_s)
+    if len(fluid):
+        pw["inv_s_fluid"] = _to_f(put(fluid, "flu"))
+        pw["inv_rho_fluid"] = _to_f(1.0 / rho[fluid])
+    m.pointwise = pw
+
+
+def gauss_stf(niter: int, deltat: float, t0: float, magnitude: float, seis_it: int = 1) -> np.ndarray:
+    """The `gauss` source time function (SOLVER/source.f90:587-598): t rounded
+    to realkind, exp(-(decay / t0 (t - shift))^2) magnitude decay / (t0
+    sqrt(pi)), decay 3.5, shift = seis_dt ceiling(1.5 t0 / seis_dt)
+    (SOLVER/parameters.F90:1071)."""
+    decay = 3.5
+    seis_dt = deltat * seis_it
+    shift = seis_dt * np.ceil(1.5 * t0 / seis_dt)
+    t = (np.arange(1, niter + 1, dtype=np.float64) * deltat).astype(F32).astype(np.float64)
+    stf = np.exp(-((decay / t0 * (t - shift)) ** 2)).astype(F32)
+    return (stf.astype(np.float64) * magnitude * decay / t0 / np.sqrt(np.pi)).astype(F32)
+
+
+def time_step(m: Mesh, courant: float = 0.6) -> float:
+    """CFL time step of the mesh: courant times the smallest distance between
+    neighbouring GLL points over the P velocity there (the criterion of
+    MESHER/discont_meshing.f90:336-339, evaluated on the actual points)."""
+    meta = m.meta
+    geo_s, geo_z = meta["geo_s"], meta["geo_z"]
+    vp = meta["vp"]
+    ds_i = np.hypot(np.diff(geo_s, axis=1), np.diff(geo_z, axis=1))
+    ds_j = np.hypot(np.diff(geo_s, axis=2), np.diff(geo_z, axis=2))
+    vi = np.maximum(vp[:, 1:, :], vp[:, :-1, :])
+    vj = np.maximum(vp[:, :, 1:], vp[:, :, :-1])
+    return float(courant * min((ds_i / vi).min(), (ds_j / vj).min()))
+
+
+def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: float):
+    """Moment-tensor source on the northern axis at the requested depth
+    (find_srcloc / define_moment_tensor, SOLVER/source.f90:435-583, 985-1226),
+    receivers at the surface points nearest to the requested colatitudes, the
+    time step, niter and the Gaussian source time function at the mesh
+    period."""
+    solid = m.meta["solid"]
+    s, z = geo["s"][solid], geo["z"][solid]
+    r = np.hypot(s, z)
+    vp = velocity(np.hypot(geo["s"], geo["z"]), "v_p",
+                  np.broadcast_to(domain_of(np.hypot(geo["s"][:, 2, 2], geo["z"][:, 2, 2]))[:, None, None],
+                                  geo["s"].shape), m.meta["model"])
+    m.meta.update(geo_s=geo["s"], geo_z=geo["z"], vp=vp)
+    dt = time_step(m, solve.courant)
+    m.deltat = dt
+    m.seis_it = solve.seis_it
+    niter = int(np.ceil((solve.seconds + 1e-11) / dt))
+    m.magnitude = solve.magnitude
+    m.stf = gauss_stf(niter, dt, period, solve.magnitude, solve.seis_it)
+    # ---- source: the northern axis point nearest to the source depth
+    zsrc = R_EARTH - solve.depth_km * 1000.0
+    on_axis = (s == 0.0) & (z > 0.0)
+    cand = np.argwhere(on_axis)
+    dz = np.abs(z[on_axis] - zsrc)
+    best = dz.min()
+    hits = cand[np.abs(dz - best) <= 1e-6 * R_EARTH]
+    # the point's elements (at most 2 along the axis), as find_srcloc keeps them
+    pts = {}
+    for e, i, j in hits:
+        pts.setdefault(int(e), (int(i), int(j)))
+    src_els = sorted(pts)[:2]
+    pole = m.src_type
+    kind = solve.source or {0: "explosion", 1: "mtr", 2: "mtp"}[pole]
+    nsrc = len(src_els)
+    E = m.nel_solid
+    st = np.zeros((E, 5, 5, 3))          # [e, ipol, jpol, comp] FP64
+    axis_s = geo["axis"][solid]
+    pw = m.pointwise
+    for e in src_els:
+        li, lj = pts[e]
+        G = SP.G1 if axis_s[e] else SP.G2
+        jac = geo["dsdxi"][solid][e] * geo["dzdeta"][solid][e] - geo["dsdeta"][solid][e] * geo["dzdxi"][solid][e]
+        dzdeta_j = geo["dzdeta"][solid][e] / jac
+        dzdxi_j = -geo["dzdxi"][solid][e] / jac
+        dsdeta_j = -geo["dsdeta"][solid][e] / jac
+        dsdxi_j = geo["dsdxi"][solid][e] / jac
+        for ip in range(5):
+            for jp in range(5):
+                # derivatives at (li, lj) of the Lagrange basis function of (ip, jp)
+                dfdxi = G[ip, li] * (1.0 if jp == lj else 0.0)
+                dfdeta = (1.0 if ip == li else 0.0) * SP.G2[jp, lj]
+                dsdf = dzdeta_j[li, lj] * dfdxi + dzdxi_j[li, lj] * dfdeta
+                dzdf = dsdeta_j[li, lj] * dfdxi + dsdxi_j[li, lj] * dfdeta
+                if pole == _abi.MONOPOLE:
+                    if kind == "explosion":
+                        st[e, ip, jp, 0] = 2.0 * dsdf
+                        st[e, ip, jp, 2] = dzdf
+                    elif kind == "mtt_p_mpp":
+                        st[e, ip, jp, 0] = dsdf
+                    elif kind == "mrr":
+                        st[e, ip, jp, 2] = dzdf
+                    else:
+                        raise ValueError(f"monopole source {kind}")
+                elif pole == _abi.DIPOLE:
+                    if kind not in ("mtr", "mpr"):
+                        raise ValueError(f"dipole source {kind}")
+                    st[e, ip, jp, 0] = dzdf
+                    st[e, ip, jp, 2] = dsdf
+                else:
+                    if kind not in ("mtp", "mtt_m_mpp"):
+                        raise ValueError(f"quadrupole source {kind}")
+                    st[e, ip, jp, 0] = dsdf
+                    st[e, ip, jp, 1] = dsdf
+    st = st / nsrc
+    # pdistsum_solid in FP32, small values cut (smallval = 1e-6), the pole's axis mask
+    stf_ = np.zeros((5, 5, E, 3), dtype=F32, order="F")
+    for c in range(3):
+        stf_[..., c] = _pdistsum_f32(_to_f(st[..., c]), m.igloc_solid, m.nglob_solid)
+    stf_[np.abs(stf_) < 1e-6] = 0.0
+    ax_el = m.ax_el_solid - 1
+    comps = {0: [0], 1: [1, 2], 2: [0, 1, 2]}[pole]
+    for c in comps:
+        stf_[0, :, ax_el, c] = 0.0
+    stf_ = stf_ / F32(np.pi if pole == _abi.DIPOLE else 2.0 * np.pi)
+    nz = [e for e in range(E) if np.any(stf_[:, :, e, :] != 0)]
+    if len(nz) > 8:
+        raise RuntimeError(f"source term spans {len(nz)} elements (8 at most)")
+    m.ielsrc = np.zeros(8, dtype=I32)
+    m.ielsrc[:len(nz)] = np.array(nz, dtype=I32) + 1
+    m.nelsrc = len(nz)
+    ste = np.zeros((5, 5, 8, 3), dtype=F32, order="F")
+    for k, e in enumerate(nz):
+        ste[:, :, k, :] = stf_[:, :, e, :]
+    m.source_term_el = ste
+    m.fluid_src = 0
+    m.meta["source"] = {"kind": kind, "depth_km": float((R_EARTH - z[tuple(hits[0])]) / 1000.0),
+                        "elements": [int(e) + 1 for e in src_els]}
+    # ---- receivers: the surface point nearest to each colatitude
+    rec = solve.receivers_deg
+    if rec is None:
+        rec = np.linspace(0.0, 180.0, 20)
+    surf = np.argwhere(np.abs(r - R_EARTH) < 1.0)
+    th = np.degrees(np.arctan2(s[tuple(surf.T)], z[tuple(surf.T)]))
+    rows = []
+    for c in np.asarray(rec, dtype=np.float64):
+        k = int(np.argmin(np.abs(th - c)))
+        e, i, j = surf[k]
+        rows.append((e + 1, i, j))
+    m.recfile_el = np.asfortranarray(np.array(rows, dtype=I32).reshape(-1, 3))
+    m.meta["receiver_colat_deg"] = np.array([th[int(np.argmin(np.abs(th - c)))] for c in rec])

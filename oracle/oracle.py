@@ -63,6 +63,67 @@ def stiffness_solid(mesh, u_elem: np.ndarray, dtype=np.float32) -> np.ndarray:
     return f
 
 
+def stiffness_fluid(mesh, chi_elem: np.ndarray, dtype=np.float64) -> np.ndarray:
+    """glob_fluid_stiffness element-local (no masks, no assembly)."""
+    tag, ct, nt = _t(dtype)
+    d = mesh.desc()
+    c = np.asfortranarray(chi_elem, dtype=nt)
+    f = np.zeros_like(c, order="F")
+    getattr(lib(), f"orc_{tag}_stiffness_fluid")(C.byref(d), _p(c, ct), _p(f, ct))
+    return f
+
+
+def _mask_axis(mesh, a, comps, fluid=False):
+    """apply_axis_mask_* on an element-local array (a copy)."""
+    a = np.array(a, dtype=np.float64, order="F", copy=True)
+    ax = (mesh.ax_el_fluid if fluid else mesh.ax_el_solid)
+    if ax is None or len(ax) == 0:
+        return a
+    e = np.asarray(ax) - 1
+    if a.ndim == 3:
+        a[0, :, e] = 0.0
+    else:
+        for c in comps:
+            a[0, :, e, c] = 0.0
+    return a
+
+
+def energy(mesh, disp, velo, dchi=None, ddchi=None) -> dict:
+    """The total energy of `energy` (SOLVER/time_evol_wave.F90:1424-1526) in
+    FP64: elastic 2 pi sum(u K u) and kinetic 2 pi sum(v^2 m) of the solid,
+    with the unassembled mass rho J s w (the dipole's z twice), and in the
+    fluid 2 pi sum(ddchi^2 m / lambda) and 2 pi sum(dchi K_f dchi); the
+    total is half their sum.  The unassembled masses come from
+    mesh.meta['unassem_mass_rho_solid'] and ['unassem_mass_lam_fluid']."""
+    pole = mesh.src_type
+    comps = {0: [0], 1: [1, 2], 2: [0, 1, 2]}[pole]
+    u = _mask_axis(mesh, disp, comps)
+    if pole == 0:
+        u[..., 1] = 0.0
+    ku = stiffness_solid(mesh, u, np.float64)
+    ku = _mask_axis(mesh, ku, comps)
+    epot_sol = 2.0 * np.pi * float(np.sum(ku * u))
+    m = np.asarray(mesh.meta["unassem_mass_rho_solid"], dtype=np.float64)
+    v2 = np.asarray(velo, dtype=np.float64) ** 2
+    kin = v2[..., 0] * m + v2[..., 1] * m + v2[..., 2] * m * (2.0 if pole == 1 else 1.0)
+    if pole == 0:
+        kin = v2[..., 0] * m + v2[..., 2] * m
+    ekin_sol = 2.0 * np.pi * float(np.sum(kin))
+    epot_flu = ekin_flu = 0.0
+    if mesh.nel_fluid > 0 and dchi is not None:
+        mf = np.asarray(mesh.meta["unassem_mass_lam_fluid"], dtype=np.float64)
+        epot_flu = 2.0 * np.pi * float(np.sum(np.asarray(ddchi, np.float64) ** 2 * mf))
+        dc = np.array(dchi, dtype=np.float64, order="F", copy=True)
+        if pole != 0:
+            dc = _mask_axis(mesh, dc, None, fluid=True)
+        kf = stiffness_fluid(mesh, dc, np.float64)
+        if pole != 0:
+            kf = _mask_axis(mesh, kf, None, fluid=True)
+        ekin_flu = 2.0 * np.pi * float(np.sum(kf * dc))
+    return {"epot_sol": epot_sol, "ekin_sol": ekin_sol, "epot_flu": epot_flu, "ekin_flu": ekin_flu,
+            "total": 0.5 * (epot_sol + ekin_sol + epot_flu + ekin_flu)}
+
+
 def gradient_cg4(mesh, f_elem: np.ndarray, dtype=np.float64) -> np.ndarray:
     """axisym_gradient_solid_el_cg4 for every element: (4, 2, nel)."""
     tag, ct, nt = _t(dtype)
