@@ -624,7 +624,34 @@ int prepare_solid_kernels(axg_handle *h) {
                   : prepare_solid_kernel<POLE, MODE_NEWMARK, false, false>(h, c);
 }
 
+// the fluid kernels' dynamic shared memory (every variant a handle or a
+// batch may launch: Newmark or symplectic, plain or compensated)
+template <int NONMONO, bool KAHAN, bool SYMP, class P>
+int prepare_fluid_fn(axg_handle *h) {
+  auto fn = fluid_patch_kernel<NONMONO, KAHAN, SYMP, P>;
+  CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, FluidSmem<NONMONO, KAHAN>::bytes));
+  CK(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  return AXG_OK;
+}
+
+template <int NONMONO>
+int prepare_fluid_kernels(axg_handle *h) {
+  int rc;
+  if ((rc = prepare_fluid_fn<NONMONO, false, false, One<PatchWork>>(h)) ||
+      (rc = prepare_fluid_fn<NONMONO, true, false, One<PatchWork>>(h)) ||
+      (rc = prepare_fluid_fn<NONMONO, false, true, One<PatchWork>>(h)) ||
+      (rc = prepare_fluid_fn<NONMONO, true, true, One<PatchWork>>(h)) ||
+      (rc = prepare_fluid_fn<NONMONO, false, false, Many<PatchWork>>(h)) ||
+      (rc = prepare_fluid_fn<NONMONO, true, false, Many<PatchWork>>(h)))
+    return rc;
+  return AXG_OK;
+}
+
 int prepare_kernels(axg_handle *h) {
+  if (h->nel_f > 0) {
+    const int rc = h->pole == AXG_MONOPOLE ? prepare_fluid_kernels<0>(h) : prepare_fluid_kernels<1>(h);
+    if (rc) return rc;
+  }
   if (h->pole == AXG_MONOPOLE) return prepare_solid_kernels<POLE_MONO>(h);
   if (h->pole == AXG_DIPOLE) return prepare_solid_kernels<POLE_DI>(h);
   return prepare_solid_kernels<POLE_QUAD>(h);
@@ -701,11 +728,11 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
       const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
       const One<PatchWork> w{{a, fs}, n};
       if (h->pole == AXG_MONOPOLE) {
-        if (h->kahan) fluid_patch_kernel<0, true><<<n, kThreads, 0, s>>>(w, h->spec);
-        else fluid_patch_kernel<0, false><<<n, kThreads, 0, s>>>(w, h->spec);
+        if (h->kahan) fluid_patch_kernel<0, true><<<n, kThreads, FluidSmem<0, true>::bytes, s>>>(w, h->spec);
+        else fluid_patch_kernel<0, false><<<n, kThreads, FluidSmem<0, false>::bytes, s>>>(w, h->spec);
       } else {
-        if (h->kahan) fluid_patch_kernel<1, true><<<n, kThreads, 0, s>>>(w, h->spec);
-        else fluid_patch_kernel<1, false><<<n, kThreads, 0, s>>>(w, h->spec);
+        if (h->kahan) fluid_patch_kernel<1, true><<<n, kThreads, FluidSmem<1, true>::bytes, s>>>(w, h->spec);
+        else fluid_patch_kernel<1, false><<<n, kThreads, FluidSmem<1, false>::bytes, s>>>(w, h->spec);
       }
     }
     if (h->to_solid.n > 0) {
@@ -768,11 +795,11 @@ void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
         const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
         const One<PatchWork> w{{a, fs}, n};
         if (h->pole == AXG_MONOPOLE) {
-          if (h->kahan) fluid_patch_kernel<0, true, true><<<n, kThreads, 0, s>>>(w, h->spec);
-          else fluid_patch_kernel<0, false, true><<<n, kThreads, 0, s>>>(w, h->spec);
+          if (h->kahan) fluid_patch_kernel<0, true, true><<<n, kThreads, FluidSmem<0, true>::bytes, s>>>(w, h->spec);
+          else fluid_patch_kernel<0, false, true><<<n, kThreads, FluidSmem<0, false>::bytes, s>>>(w, h->spec);
         } else {
-          if (h->kahan) fluid_patch_kernel<1, true, true><<<n, kThreads, 0, s>>>(w, h->spec);
-          else fluid_patch_kernel<1, false, true><<<n, kThreads, 0, s>>>(w, h->spec);
+          if (h->kahan) fluid_patch_kernel<1, true, true><<<n, kThreads, FluidSmem<1, true>::bytes, s>>>(w, h->spec);
+          else fluid_patch_kernel<1, false, true><<<n, kThreads, FluidSmem<1, false>::bytes, s>>>(w, h->spec);
         }
       }
       if (h->to_solid.n > 0) {
@@ -2511,7 +2538,8 @@ int64_t batch_fluid_colour(axg_batch *b, int c, cudaStream_t s) {
         return PatchWork{a, fluid_state(h)};
       },
       [&](const Many<PatchWork> &m) {
-        fluid_patch_kernel<NONMONO, KAHAN, false, Many<PatchWork>><<<m.start[m.n], kThreads, 0, s>>>(m, b->spec);
+        fluid_patch_kernel<NONMONO, KAHAN, false, Many<PatchWork>>
+            <<<m.start[m.n], kThreads, FluidSmem<NONMONO, KAHAN>::bytes, s>>>(m, b->spec);
       });
 }
 

@@ -1257,32 +1257,84 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE_NEWMARK, false, 
 
 // ------------------------------------------------------------ fluid patch kernel
 
-// One CTA per patch (per work item: a patch of one of the solves).  The
-// gather reads each point's chi, dchi, ddchi0 (and the partial sum of an
-// earlier writer) in one batch of loads per thread; each warp loads the metric
-// terms of its next element while it computes the current one; the
+// Shared-memory layout of the fluid patch kernel (dynamic): the patch's
+// element blocks (metric terms, BS floats each), their patch-local point
+// indices and info words, and the patch's points (chi, force, compensation,
+// point words).  Offsets in bytes, 16-byte aligned.
+template <int NONMONO, bool KAHAN>
+struct FluidSmem {
+  static constexpr int BS = block_stride(NONMONO ? 4 : 3);
+  static constexpr int el_off = 0;
+  static constexpr int el_bytes = kMaxPatchElems * BS * 4;
+  static constexpr int idx_off = el_off + el_bytes;
+  static constexpr int idx_bytes = ((kMaxPatchElems * 25 * 2 + 15) / 16) * 16;
+  static constexpr int info_off = idx_off + idx_bytes;
+  static constexpr int info_bytes = kMaxPatchElems * 4;
+  static constexpr int u_off = info_off + info_bytes;
+  static constexpr int pt_bytes = kMaxPatchPoints * 4;
+  static constexpr int f_off = u_off + pt_bytes;
+  static constexpr int w_off = f_off + pt_bytes;
+  static constexpr int c_off = w_off + pt_bytes;
+  static constexpr int bar_off = c_off + (KAHAN ? pt_bytes : 0);
+  static constexpr int bytes = bar_off + 16;
+};
+
+// One CTA per patch (per work item: a patch of one of the solves).  Thread 0
+// starts one bulk copy of the patch's element blocks (contiguous in launch
+// order) into shared memory; meanwhile every thread loads the element
+// indices and info words, and gathers each point's chi, dchi, ddchi0 (and the
+// partial sum of an earlier writer) in one batch of loads, applying the
+// predictor.  The sub-rounds then read everything from shared memory, and the
 // write-back loads the last writers' inverse mass, dchi and ddchi0 in one
 // batch before it stores.
 template <int NONMONO, bool KAHAN, bool SYMP = false, class P = One<PatchWork>>
-__global__ void __launch_bounds__(kThreads) fluid_patch_kernel(const __grid_constant__ P p, SpecDev sp) {
+__global__ void __launch_bounds__(kThreads, 4) fluid_patch_kernel(const __grid_constant__ P p, SpecDev sp) {
   static_assert(!P::kMany || !SYMP, "batches run the Newmark step");
+  using L = FluidSmem<NONMONO, KAHAN>;
+  constexpr int BS = L::BS;
+  constexpr int NT = NONMONO ? 4 : 3;
   if ((int32_t)blockIdx.x >= p.items()) return;  // uniform across the CTA
   const int sv = p.locate(blockIdx.x);
   const DomainArgs &d = p.at(sv).d;
   const StateArgs &st = p.at(sv).st;
   const int pp = blockIdx.x - p.first(sv);
-  __shared__ float s_u[kMaxPatchPoints];
-  __shared__ float s_f[kMaxPatchPoints];
-  __shared__ float s_cu[KAHAN ? kMaxPatchPoints : 1];  // compensated mode: predictor compensation
-  __shared__ uint32_t s_w[kMaxPatchPoints];
-  constexpr int BS = block_stride(NONMONO ? 4 : 3);
+  extern __shared__ __align__(128) unsigned char smem[];
+  float *s_el = reinterpret_cast<float *>(smem + L::el_off);
+  uint16_t *s_idx = reinterpret_cast<uint16_t *>(smem + L::idx_off);
+  int32_t *s_info = reinterpret_cast<int32_t *>(smem + L::info_off);
+  float *s_u = reinterpret_cast<float *>(smem + L::u_off);
+  float *s_f = reinterpret_cast<float *>(smem + L::f_off);
+  uint32_t *s_w = reinterpret_cast<uint32_t *>(smem + L::w_off);
+  float *s_cu = reinterpret_cast<float *>(smem + L::c_off);  // compensated mode only
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::bar_off);
   constexpr int kGB = (kMaxPatchPoints + kThreads - 1) / kThreads;  // points per thread: one batch per patch
   __shared__ int s_stop;
-  if (threadIdx.x == 0) s_stop = *st.blowup;
+  __shared__ int s_timeout;
+  if (threadIdx.x == 0) {
+    s_stop = *st.blowup;
+    s_timeout = 0;
+    mbar_init(bar, 1);
+  }
+  fence_mbar_init();
   __syncthreads();
-  if (s_stop) return;  // uniform across the CTA
+  if (s_stop) return;  // uniform across the CTA; no copy has been issued
   if (!AXG_BOUND(d.patch_begin + pp, d.n_patches, 11)) return;
   const PatchMeta m = d.meta[d.patch_begin + pp];
+  const int ne = m.n_elems;
+  const bool elems_ok = ne >= 1 && ne <= kMaxPatchElems && AXG_BOUND((int64_t)m.elem_start + ne - 1, d.n_elem, 12);
+  // 1. the patch's element blocks: one bulk copy (each block is BS floats, a
+  //    multiple of 16 bytes, from a 16-byte aligned base)
+  if (threadIdx.x == 0) {
+    if (elems_ok) bulk_g2s(s_el, d.metric + (int64_t)m.elem_start * BS, (uint32_t)(ne * BS * 4), bar,
+                           policy_evict_first());
+    else mbar_arrive(bar);
+  }
+  // element point indices and info words
+  if (elems_ok) {
+    for (int t = threadIdx.x; t < ne * 25; t += kThreads) s_idx[t] = __ldcs(d.elpts + (int64_t)m.elem_start * 25 + t);
+    for (int t = threadIdx.x; t < ne; t += kThreads) s_info[t] = __ldg(d.elinfo + m.elem_start + t);
+  }
+  // 2. gather with the predictor on the fly
   {
     uint32_t w[kGB];
     float uu[kGB], ff[kGB], cc[KAHAN ? kGB : 1];
@@ -1319,72 +1371,49 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(const __grid_cons
       }
     }
   }
+  if (!mbar_wait_bounded(bar, 0u, st.err)) s_timeout = 1;
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool active = lane < 25;
   const int i = lane % 5, j = active ? lane / 5 : 0;
-  // idle lanes 25..31 take part in the shuffles; their loads of an element's
-  // data go to point 24 so that no lane reads past the element's block (the
-  // block of the last element ends where the allocation ends)
+  // idle lanes 25..31 take part in the shuffles; their reads of an element's
+  // data go to point 24
   const int ml = active ? lane : 24;
   LaneCoef coef;
   load_coef(sp, i, j, coef);
   const float stf1 = AXG_BOUND(*st.iter - 1, st.niter, 12) ? st.stf[*st.iter - 1] : 0.f;
   const PatchRounds pr(m);
-  // an element's data as this lane needs it
-  struct FluidElem {
-    float mt[4];
-    int32_t info;
-    int idx;
-  };
-  auto load_elem = [&](int s_) {
-    FluidElem e;
-    int64_t el = (int64_t)m.elem_start + s_;
-    if (!AXG_BOUND(el, d.n_elem, 12)) el = 0;
-    const float *blk = d.metric + el * BS;
-#pragma unroll
-    for (int t = 0; t < 4; ++t) e.mt[t] = (t < (NONMONO ? 4 : 3)) ? __ldcs(blk + t * 25 + ml) : 0.f;
-    e.info = __ldg(d.elinfo + el);
-    e.idx = active ? __ldcs(d.elpts + el * 25 + lane) : 0;
-    return e;
-  };
-  WarpIter it{0, warp};
-  it.norm(pr, warp);
-  FluidElem cur{};
-  if (it.valid(pr)) cur = load_elem(it.s);
+  // 3. elements, sub-round by sub-round, from shared memory
   int r0 = 0;
   for (int r = 0; r < pr.n; ++r) {
     const int r1 = pr.end(r);
-    for (int s = r0 + warp; s < r1; s += kWarps) {
-      // start the loads of this warp's next element (in this or a later round)
-      WarpIter nxt = it;
-      nxt.s += kWarps;
-      nxt.norm(pr, warp);
-      FluidElem nx{};
-      if (nxt.valid(pr)) nx = load_elem(nxt.s);
-      int64_t el = (int64_t)m.elem_start + s;
-      if (!AXG_BOUND(el, d.n_elem, 12)) el = 0;
-      int axslot = (cur.info & 0xFFFFFF) - 1;
-      if (axslot >= 0 && !AXG_BOUND((int64_t)(axslot + 1) * 5 - 1, d.n_m0, 12)) axslot = -1;
-      const int srcslot = ((cur.info >> 24) & 0xF) - 1;
-      const bool ax = axslot >= 0;
-      int idx = cur.idx;
+    for (int s = r0 + warp; s < r1 && elems_ok; s += kWarps) {
+      const float *blk = s_el + s * BS;
+      float mt[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) mt[t] = t < NT ? blk[t * 25 + ml] : 0.f;
+      const int32_t info = s_info[s];
+      int idx = active ? s_idx[s * 25 + lane] : 0;
       if (!AXG_BOUND(idx, m.n_pts, 12)) idx = 0;
+      const int64_t el = (int64_t)m.elem_start + s;
+      int axslot = (info & 0xFFFFFF) - 1;
+      if (axslot >= 0 && !AXG_BOUND((int64_t)(axslot + 1) * 5 - 1, d.n_m0, 12)) axslot = -1;
+      const int srcslot = ((info >> 24) & 0xF) - 1;
+      const bool ax = axslot >= 0;
       float chi = active ? s_u[idx] : 0.f;
       if (NONMONO && ax && i == 0) chi = 0.f;  // apply_axis_mask_scal(chi)
       const float *m0 = ax ? d.m0 + (int64_t)axslot * 5 : nullptr;
-      float f = ax ? stiff_fluid<true, NONMONO>(coef, cur.mt, m0, i, j, chi)
-                   : stiff_fluid<false, NONMONO>(coef, cur.mt, m0, i, j, chi);
+      float f = ax ? stiff_fluid<true, NONMONO>(coef, mt, m0, i, j, chi)
+                   : stiff_fluid<false, NONMONO>(coef, mt, m0, i, j, chi);
       if (srcslot >= 0 && stf1 != 0.f && active) f = f - d.srcfl[srcslot * 25 + lane] * stf1;
       if (NONMONO && ax && i == 0) f = 0.f;
       if (d.fsmask && active) f = f * d.fsmask[el * 25 + lane];
       if (active) s_f[idx] += f;
-      cur = nx;
-      it = nxt;
     }
     r0 = r1;
     __syncthreads();
   }
+  // 4. write-back
   {
     uint32_t w[kGB];
     float vel[kGB], acc[kGB], im[kGB], gam[kGB], kv[KAHAN ? kGB : 1];
@@ -1436,6 +1465,9 @@ __global__ void __launch_bounds__(kThreads) fluid_patch_kernel(const __grid_cons
       if (KAHAN && zero) st.cu[0][g] = 0.f;
     }
   }
+  // after a timeout the bulk copy may still be in flight: wait (bounded)
+  // for it before the CTA exits
+  if (s_timeout && threadIdx.x == 0) mbar_drain(bar, 0u);
 }
 
 // The final drift of a symplectic step (SOLVER/time_evol_wave.F90:722-727):

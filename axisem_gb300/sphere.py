@@ -289,7 +289,7 @@ def _edge_map(p, q, arc, t):
     return pt, dt
 
 
-def element_geometry(sk: Skeleton, els: np.ndarray | None = None):
+def element_geometry(sk: Skeleton, els: np.ndarray | None = None, gll_only: bool = False):
     """s, z and the partial derivatives ds/dxi, dz/dxi, ds/deta, dz/deta at
     the 5 x 5 points of elements `els`: GLL x GLL, or GLJ(0,1) x GLL on axial
     elements (compute_partial_derivatives, SOLVER/analytic_mapping.f90:680-700).
@@ -299,7 +299,8 @@ def element_geometry(sk: Skeleton, els: np.ndarray | None = None):
     c = [sk.nodes[el[:, k]] for k in range(4)]
     arc = sk.arc[els]
     ax = sk.axis[els]
-    xi = np.where(ax[:, None], SP.xi_k[None, :], SP.eta[None, :])   # (E, 5)
+    use_glj = ax & (not gll_only)
+    xi = np.where(use_glj[:, None], SP.xi_k[None, :], SP.eta[None, :])   # (E, 5)
     eta = SP.eta
     B, dB = _edge_map(c[0], c[1], arc[:, EDGE_BOTTOM], xi)
     T, dT = _edge_map(c[3], c[2], arc[:, EDGE_TOP], xi)
@@ -401,6 +402,76 @@ def _to_f(a):
 
 
 @dataclass
+class Attenuation:
+    """Options of the anelastic model (inparam_advanced's attenuation keys,
+    SOLVER/attenuation.f90:710-730 defaults): n_sls standard linear solids
+    over [f_min, f_max] Hz, moduli given at f_ref Hz, the low-Q correction,
+    the coarse-grained (cg4) memory variables."""
+
+    n_sls: int = 5
+    f_min: float = 0.001
+    f_max: float = 1.0
+    f_ref: float = 1.0
+    do_corr_lowq: bool = True
+    nfsamp: int = 100
+
+
+def sls_fit(att: Attenuation):
+    """Relaxation frequencies w_j (rad/s) and weights y_j of the SLS for
+    Q = 1.  The reference anneals them from random draws
+    (invert_linear_solids, SOLVER/attenuation.f90:1183-1330), which no run
+    reproduces; here the w_j stay at the annealing's start, log-spaced over
+    [f_min, f_max] (its FIX_FREQ mode), and y_j minimise the frequency-weighted
+    misfit of the linearised 1/Q(w) = sum_j y_j w w_j / (w^2 + w_j^2)
+    (Emmerich & Korn 1987, eq. 22) on the reference's nfsamp log-spaced
+    samples, by linear least squares."""
+    n = att.n_sls
+    if n > 1:
+        expo = (np.log10(att.f_max) - np.log10(att.f_min)) / (n - 1.0)
+        w_j = 2 * np.pi * 10 ** (np.log10(att.f_min) + np.arange(n) * expo)
+    else:
+        w_j = np.array([np.sqrt(att.f_max * att.f_min) * 2 * np.pi])
+    expo = (np.log10(att.f_max) - np.log10(att.f_min)) / (att.nfsamp - 1.0)
+    w = 2 * np.pi * 10 ** (np.log10(att.f_min) + np.arange(att.nfsamp) * expo)
+    weights = w / w.sum() * att.nfsamp
+    A = (w[:, None] * w_j[None, :]) / (w[:, None] ** 2 + w_j[None, :] ** 2)
+    sw = np.sqrt(weights)[:, None]
+    y_j, *_ = np.linalg.lstsq(A * sw, sw[:, 0], rcond=None)
+    return w_j, y_j
+
+
+def fast_correct(y: np.ndarray) -> np.ndarray:
+    """fast_correct (SOLVER/attenuation.f90:1139-1155): first-order
+    correction of the linearised SLS weights, yp_j = y_j dy_j."""
+    yp = np.zeros_like(y)
+    dy = 1.0 + 0.5 * y[0]
+    yp[0] = y[0] * dy
+    for k in range(1, len(y)):
+        dy = dy + (dy - 0.5) * y[k - 1] + 0.5 * y[k]
+        yp[k] = y[k] * dy
+    return yp
+
+
+CG4 = ((1, 1), (1, 3), (3, 1), (3, 3))
+
+
+def _weights_cg(g):
+    """weights_cg of prepare_attenuation (SOLVER/attenuation.f90:968-992): each
+    cg4 point stands for its quarter of the element, gamma_w_l = g (the mass
+    weights wt wt J s); returns (E, 4) in the cg4 order (1,1), (1,3), (3,1), (3,3)."""
+    out = np.zeros((g.shape[0], 4))
+    out[:, 0] = (g[:, 0, 0] + g[:, 0, 1] + g[:, 1, 0] + g[:, 1, 1]
+                 + 0.5 * (g[:, 0, 2] + g[:, 1, 2] + g[:, 2, 0] + g[:, 2, 1]) + 0.25 * g[:, 2, 2]) / g[:, 1, 1]
+    out[:, 1] = (g[:, 0, 3] + g[:, 0, 4] + g[:, 1, 3] + g[:, 1, 4]
+                 + 0.5 * (g[:, 0, 2] + g[:, 1, 2] + g[:, 2, 3] + g[:, 2, 4]) + 0.25 * g[:, 2, 2]) / g[:, 1, 3]
+    out[:, 2] = (g[:, 3, 0] + g[:, 3, 1] + g[:, 4, 0] + g[:, 4, 1]
+                 + 0.5 * (g[:, 2, 0] + g[:, 2, 1] + g[:, 3, 2] + g[:, 4, 2]) + 0.25 * g[:, 2, 2]) / g[:, 3, 1]
+    out[:, 3] = (g[:, 3, 3] + g[:, 3, 4] + g[:, 4, 3] + g[:, 4, 4]
+                 + 0.5 * (g[:, 2, 3] + g[:, 2, 4] + g[:, 3, 2] + g[:, 4, 2]) + 0.25 * g[:, 2, 2]) / g[:, 3, 3]
+    return out
+
+
+@dataclass
 class SphereSolve:
     """Options of one solve on a whole-Earth mesh."""
 
@@ -415,10 +486,13 @@ class SphereSolve:
 
 
 def build_mesh(period: float = 50.0, solve: SphereSolve | None = None, model: str = "prem_iso",
-               skeleton: Skeleton | None = None, pointwise: bool = True, attenuation=None) -> Mesh:
+               skeleton: Skeleton | None = None, pointwise: bool = True,
+               attenuation: Attenuation | None = None) -> Mesh:
     """A whole-Earth solve on the PREM model at `period` seconds: the skeleton,
     every precomputed array of the time loop, source, receivers and the source
-    time function, as a ``Mesh`` (FP32 module arrays, 1-based indices)."""
+    time function, as a ``Mesh`` (FP32 module arrays, 1-based indices).  With
+    `attenuation`, the cg4 anelastic model of prepare_attenuation: the solid's
+    moduli become the unrelaxed ones before the stiffness terms are formed."""
     solve = solve or SphereSolve()
     sk = skeleton or build_skeleton(period, model)
     pole = solve.pole
@@ -476,6 +550,12 @@ def build_mesh(period: float = 50.0, solve: SphereSolve | None = None, model: st
     ndf = np.where(ax[:, None], ndf, 0.0)
 
     solid = np.flatnonzero(~fluid_el)
+    # the CFL time step, from the elastic P velocities (the mesher's dt)
+    vp_el = velocity(r, "v_p", idom, model)
+    deltat = _cfl(s, z, vp_el, solve.courant)
+    anel = None
+    if attenuation is not None:
+        anel = _prepare_attenuation(attenuation, solid, lam, mu, massmat, r, idom, model, deltat)
     fluid = np.flatnonzero(fluid_el)
     ig_s, ng_s = global_numbering(sk, solid)
     m = Mesh(src_type=pole, nel_solid=len(solid), nglob_solid=ng_s, igloc_solid=ig_s,
@@ -631,10 +711,83 @@ def build_mesh(period: float = 50.0, solve: SphereSolve | None = None, model: st
         mass_f = _pdistsum_f32(mass_f, ig_f, ng_f)
         m.inv_mass_fluid = np.asfortranarray((F32(1.0) / mass_f).astype(F32))
         _boundary(m, sk, geo, solid, fluid)
-    if pointwise:
+    if pointwise or anel is not None:
         _pointwise(m, geo, solid, fluid, rho)
-    _source_receivers(m, sk, geo, solve, period)
+    if anel is not None:
+        # Y, V_* of def_solid_stiffness_terms (anel_true): wt wt J and s times
+        # the M_*_wt_k terms; on axial elements s is taken at the GLL node
+        # eta(ipol), as the reference's mapping(eta(ipol), eta(jpol)) call does
+        sg = element_geometry(sk, solid, gll_only=True)["s"]
+        Yf = jac[S] * mfac[S]
+        cg = lambda a: np.asfortranarray(np.stack([a[:, i, j] for (i, j) in CG4], 0).astype(F32))  # noqa: E731
+        pw = m.pointwise
+        anel.update({
+            "Y_cg4": cg(Yf), "V_s_eta_cg4": cg(sg * Mseta[S]), "V_s_xi_cg4": cg(sg * Msxi[S]),
+            "V_z_eta_cg4": cg(sg * Mzeta[S]), "V_z_xi_cg4": cg(sg * Mzxi[S]),
+            "inv_s_solid": pw["inv_s_solid"],
+        })
+        for nm in ("DsDeta_over_J_sol", "DzDeta_over_J_sol", "DsDxi_over_J_sol", "DzDxi_over_J_sol"):
+            a = np.transpose(pw[nm], (2, 0, 1))
+            anel[nm + "_cg4"] = cg(a)
+        m.anel = anel
+    _source_receivers(m, sk, geo, solve, period, deltat)
     return m
+
+
+def _cfl(s, z, vp, courant: float) -> float:
+    """CFL time step: courant times the smallest distance between
+    neighbouring GLL points over the P velocity there (the criterion of
+    MESHER/discont_meshing.f90:336-339, evaluated on the actual points)."""
+    ds_i = np.hypot(np.diff(s, axis=1), np.diff(z, axis=1))
+    ds_j = np.hypot(np.diff(s, axis=2), np.diff(z, axis=2))
+    vi = np.maximum(vp[:, 1:, :], vp[:, :-1, :])
+    vj = np.maximum(vp[:, :, 1:], vp[:, :, :-1])
+    return float(courant * min((ds_i / vi).min(), (ds_j / vj).min()))
+
+
+def _prepare_attenuation(att: Attenuation, solid, lam, mu, massmat, r, idom, model, deltat):
+    """prepare_attenuation (SOLVER/attenuation.f90:682-1137), coarse-grained:
+    per solid element Q from the model at its point (1,1), the SLS weights
+    yp_j = y_j / Q (fast_correct'ed), the moduli at the band's central
+    frequency, the delta moduli, the unrelaxed moduli (written back into
+    lam and mu, which the stiffness terms then use) and the cg4-weighted
+    delta moduli; the time-stepping factors of the exact SLS integration."""
+    w_j, y_j = sls_fit(att)
+    w_0 = att.f_ref * 2 * np.pi
+    w_1 = np.sqrt(att.f_min * att.f_max) * 2 * np.pi
+    S = solid
+    ri = r[S][:, 1, 1]
+    dom = idom[S][:, 1, 1]
+    Q_mu = velocity(ri, "Qmu", dom, model).astype(F32)
+    Q_ka = velocity(ri, "Qka", dom, model).astype(F32)
+    wcg = _weights_cg(massmat[S])                       # (E, 4)
+    wfull = np.zeros((len(S), 5, 5))
+    for k, (i, j) in enumerate(CG4):
+        wfull[:, i, j] = wcg[:, k]
+    dmu_cg4 = np.zeros((4, len(S)))
+    dka_cg4 = np.zeros((4, len(S)))
+    for e in range(len(S)):
+        qm, qk = float(Q_mu[e]), float(Q_ka[e])
+        ypm = fast_correct(y_j / qm) if att.do_corr_lowq else y_j / qm
+        ypk = fast_correct(y_j / qk) if att.do_corr_lowq else y_j / qk
+        mu_fac = float(np.sum(ypm * w_j ** 2 / (w_1 ** 2 + w_j ** 2))) / float(np.sum(ypm))
+        ka_fac = float(np.sum(ypk * w_j ** 2 / (w_1 ** 2 + w_j ** 2))) / float(np.sum(ypk))
+        ge = S[e]
+        mu_w1 = mu[ge] * (1 + 2.0 / (np.pi * qm) * np.log(w_1 / w_0))
+        ka_w1 = (lam[ge] + 2.0 / 3.0 * mu[ge]) * (1 + 2.0 / (np.pi * qk) * np.log(w_1 / w_0))
+        dmu0 = mu_w1 / (1.0 / np.sum(ypm) + 1 - mu_fac)
+        dka0 = ka_w1 / (1.0 / np.sum(ypk) + 1 - ka_fac)
+        mu[ge] = mu_w1 + wfull[e] * dmu0 * mu_fac
+        lam[ge] = ka_w1 + wfull[e] * dka0 * ka_fac - 2.0 / 3.0 * mu[ge]
+        for k, (i, j) in enumerate(CG4):
+            dmu_cg4[k, e] = wcg[e, k] * dmu0[i, j]
+            dka_cg4[k, e] = wcg[e, k] * dka0[i, j]
+    ex = np.exp(-w_j * deltat)
+    return {"y_j": y_j, "w_j": w_j, "exp_w_j_deltat": ex,
+            "ts_fac_tm1": (1 - ex) / (w_j * deltat) - ex, "ts_fac_t": (ex - 1) / (w_j * deltat) + 1,
+            "do_corr_lowq": int(att.do_corr_lowq), "Q_mu": Q_mu, "Q_kappa": Q_ka,
+            "delta_mu_cg4": np.asfortranarray(dmu_cg4.astype(F32)),
+            "delta_kappa_cg4": np.asfortranarray(dka_cg4.astype(F32))}
 
 
 def _boundary(m: Mesh, sk: Skeleton, geo, solid, fluid):
@@ -741,21 +894,7 @@ def gauss_stf(niter: int, deltat: float, t0: float, magnitude: float, seis_it: i
     return (stf.astype(np.float64) * magnitude * decay / t0 / np.sqrt(np.pi)).astype(F32)
 
 
-def time_step(m: Mesh, courant: float = 0.6) -> float:
-    """CFL time step of the mesh: courant times the smallest distance between
-    neighbouring GLL points over the P velocity there (the criterion of
-    MESHER/discont_meshing.f90:336-339, evaluated on the actual points)."""
-    meta = m.meta
-    geo_s, geo_z = meta["geo_s"], meta["geo_z"]
-    vp = meta["vp"]
-    ds_i = np.hypot(np.diff(geo_s, axis=1), np.diff(geo_z, axis=1))
-    ds_j = np.hypot(np.diff(geo_s, axis=2), np.diff(geo_z, axis=2))
-    vi = np.maximum(vp[:, 1:, :], vp[:, :-1, :])
-    vj = np.maximum(vp[:, :, 1:], vp[:, :, :-1])
-    return float(courant * min((ds_i / vi).min(), (ds_j / vj).min()))
-
-
-def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: float):
+def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: float, dt: float):
     """Moment-tensor source on the northern axis at the requested depth
     (find_srcloc / define_moment_tensor, SOLVER/source.f90:435-583, 985-1226),
     receivers at the surface points nearest to the requested colatitudes, the
@@ -764,11 +903,6 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
     solid = m.meta["solid"]
     s, z = geo["s"][solid], geo["z"][solid]
     r = np.hypot(s, z)
-    vp = velocity(np.hypot(geo["s"], geo["z"]), "v_p",
-                  np.broadcast_to(domain_of(np.hypot(geo["s"][:, 2, 2], geo["z"][:, 2, 2]))[:, None, None],
-                                  geo["s"].shape), m.meta["model"])
-    m.meta.update(geo_s=geo["s"], geo_z=geo["z"], vp=vp)
-    dt = time_step(m, solve.courant)
     m.deltat = dt
     m.seis_it = solve.seis_it
     niter = int(np.ceil((solve.seconds + 1e-11) / dt))

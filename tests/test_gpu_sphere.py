@@ -104,3 +104,20 @@ def test_energy_conserved_on_gpu(gpu_lib, orc, sk50, compensated):
             es.append(e["total"])
     es = np.array(es)
     assert (es.max() - es.min()) / es.mean() < 1e-6
+
+
+@pytest.mark.parametrize("pole", [0, 1, 2])
+def test_prem_50s_anelastic(gpu_lib, orc, sk50, pole):
+    """cg4 attenuation with 5 SLS (prepare_attenuation's PREM Q): 600 s of
+    seismograms and the memory variables against the FP64 oracle."""
+    m = sphere.build_mesh(50.0, sphere.SphereSolve(pole=pole, seconds=600.0), skeleton=sk50,
+                          attenuation=sphere.Attenuation())
+    with Solver(m) as s:
+        s.run()
+        rec = s.receivers()
+        mv = s.get_state(_abi.FIELD_MEMVAR)
+    t = orc.TimeLoop(m, np.float64)
+    assert t.run(1, m.niter) == 0
+    assert per_receiver(rec, t.receivers()) <= 1e-4
+    comps = [0, 1, 2, 4] if pole == 0 else list(range(6))
+    assert rel(mv[:, comps], t.memvar[:, comps]) <= 1e-4
