@@ -15,7 +15,7 @@ import numpy as np
 PKG_DIR = Path(__file__).resolve().parent
 LIB_PATH = PKG_DIR / "_build" / "libaxisem_gb300.so"
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 NPOL = 4
 
 # status codes (enum axg_status)
@@ -108,6 +108,7 @@ class MeshDesc(C.Structure):
         ("DsDeta_over_J_sol_cg4", _fp), ("DzDeta_over_J_sol_cg4", _fp),
         ("DsDxi_over_J_sol_cg4", _fp), ("DzDxi_over_J_sol_cg4", _fp),
         ("inv_s_solid", _fp),
+        ("inv_mass_rho_dp", _dp), ("inv_mass_fluid_dp", _dp), ("source_term_el_dp", _dp),
     ]
 
 

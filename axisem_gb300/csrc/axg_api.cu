@@ -116,6 +116,8 @@ struct axg_handle {
   float *su[3] = {}, *sv[3] = {}, *sa[3] = {}, *sf[3] = {};
   float *fu = nullptr, *fv = nullptr, *fa = nullptr, *ff = nullptr;
   float *inv_mass_s = nullptr, *inv_mass_f = nullptr, *gamma_s = nullptr, *gamma_f = nullptr;
+  // FP64 inverse masses (mesh) and source values (solve), when the descriptor had them
+  double *inv_mass_s_dp = nullptr, *inv_mass_f_dp = nullptr, *src_val_dp_d = nullptr;
   float *stf = nullptr, *rec = nullptr;
   int32_t *iter = nullptr, *blowup = nullptr, *rec_gidx_d = nullptr;
   int32_t *src_gidx_d = nullptr;
@@ -344,8 +346,9 @@ int validate(const axg_mesh_desc *d) {
 }
 
 // per global point value of an element-local array (first copy wins)
-std::vector<float> per_point(const float *elem, const std::vector<int32_t> &igloc, int64_t nglob) {
-  std::vector<float> out(nglob, 0.f);
+template <class T>
+std::vector<T> per_point(const T *elem, const std::vector<int32_t> &igloc, int64_t nglob) {
+  std::vector<T> out(nglob, T(0));
   std::vector<uint8_t> set(nglob, 0);
   for (size_t p = 0; p < igloc.size(); ++p) {
     const int64_t g = igloc[p] - 1;
@@ -524,6 +527,7 @@ StateArgs solid_state(axg_handle *h) {
     s.cv[c] = h->kahan ? h->cv_s[c] : nullptr;
   }
   s.inv_mass = h->inv_mass_s;
+  s.inv_mass_dp = h->kahan ? h->inv_mass_s_dp : nullptr;
   s.gamma = h->gamma_s;
   s.stf = h->stf;
   s.iter = h->iter;
@@ -535,6 +539,7 @@ StateArgs solid_state(axg_handle *h) {
   s.hdt2 = (float)(0.5 * h->dt * h->dt);
   s.src.gidx = h->src_gidx_d;
   s.src.val = h->src_val_d;
+  s.src.val_dp = h->kahan ? h->src_val_dp_d : nullptr;
   s.src.n = h->n_src;
   s.nglob = h->nglob_s;
   s.niter = std::max(h->niter, 1);
@@ -551,6 +556,7 @@ StateArgs fluid_state(axg_handle *h) {
   s.a[0] = h->fa;
   s.f[0] = h->ff;
   s.inv_mass = h->inv_mass_f;
+  s.inv_mass_dp = h->kahan ? h->inv_mass_f_dp : nullptr;
   s.gamma = h->gamma_f;
   s.src.n = 0;
   s.nglob = h->nglob_f;
@@ -1205,6 +1211,7 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
   }
   std::vector<int32_t> src_g;
   std::vector<float> src_v;
+  std::vector<double> src_v_dp;
   if (!d->fluid_src) {
     std::map<int32_t, int> seen;
     for (int k = 0; k < d->nelsrc; ++k) {
@@ -1221,6 +1228,8 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
         seen[g] = 1;
         src_g.push_back(g);
         src_v.insert(src_v.end(), v, v + 3);
+        if (d->source_term_el_dp)
+          for (int c = 0; c < 3; ++c) src_v_dp.push_back(d->source_term_el_dp[q + 25 * k + 200 * c]);
       }
     }
   }
@@ -1246,6 +1255,8 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
     h->df = share->df;
     h->inv_mass_s = share->inv_mass_s;
     h->inv_mass_f = share->inv_mass_f;
+    h->inv_mass_s_dp = share->inv_mass_s_dp;
+    h->inv_mass_f_dp = share->inv_mass_f_dp;
     h->gamma_s = share->gamma_s;
     h->gamma_f = share->gamma_f;
     h->to_fluid = share->to_fluid;
@@ -1258,6 +1269,10 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
     rc = upload(h, &h->inv_mass_s, per_point(d->inv_mass_rho, h->igloc_s, h->nglob_s));
     if (!rc && h->absorbing) rc = upload(h, &h->gamma_s, per_point(d->solid_absorbing_gamma, h->igloc_s, h->nglob_s));
     if (!rc && h->nel_f > 0) rc = upload(h, &h->inv_mass_f, per_point(d->inv_mass_fluid, h->igloc_f, h->nglob_f));
+    if (!rc && d->inv_mass_rho_dp)
+      rc = upload(h, &h->inv_mass_s_dp, per_point(d->inv_mass_rho_dp, h->igloc_s, h->nglob_s));
+    if (!rc && h->nel_f > 0 && d->inv_mass_fluid_dp)
+      rc = upload(h, &h->inv_mass_f_dp, per_point(d->inv_mass_fluid_dp, h->igloc_f, h->nglob_f));
     if (!rc && h->nel_f > 0 && h->absorbing)
       rc = upload(h, &h->gamma_f, per_point(d->fluid_absorbing_gamma, h->igloc_f, h->nglob_f));
     if (!rc) rc = upload_coupling(h, cf, h->to_fluid);
@@ -1290,6 +1305,7 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
   if ((rc = upload(h, &h->rec_gidx_d, h->rec_gidx))) return rc;
   if ((rc = upload(h, &h->src_gidx_d, src_g))) return rc;
   if ((rc = upload(h, &h->src_val_d, src_v))) return rc;
+  if (!src_v_dp.empty() && (rc = upload(h, &h->src_val_dp_d, src_v_dp))) return rc;
   if ((rc = dalloc(h, &h->iter, 4))) return rc;
   h->blowup = h->iter + 1;
   h->errw = h->iter + 2;

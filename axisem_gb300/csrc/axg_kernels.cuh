@@ -93,6 +93,7 @@ struct SpecDev {
 struct SrcTable {           // solid source points (<= 200)
   const int32_t *gidx;      // global point
   const float *val;         // (n, 3)
+  const double *val_dp;     // (n, 3) in FP64, applied in FP64 by the compensated mode; or null
   int32_t n;
 };
 
@@ -116,6 +117,7 @@ struct StateArgs {
   float *f[3];              // force partial sums
   float *cu[3], *cv[3];     // compensated mode: running compensation of disp / velo (chi / dchi), else null
   const float *inv_mass;    // per global point
+  const double *inv_mass_dp;  // per global point in FP64 (compensated mode) or null
   const float *gamma;       // absorbing gamma per global point or null
   const float *stf;         // (niter)
   const int32_t *iter;      // device iteration counter (1-based iter of this step)
@@ -1093,6 +1095,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
       for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += kWB * kThreads) {
         uint32_t w[kWB];
         float vel[kWB][NC], acc[kWB][NC], im[kWB], gam[kWB], kv[KAHAN ? kWB : 1][NC];
+        double imd[KAHAN ? kWB : 1];  // compensated mode: the FP64 inverse mass, when the handle has it
 #pragma unroll
         for (int q = 0; q < kWB; ++q) {
           const int t = t0 + q * kThreads;
@@ -1100,6 +1103,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
           const uint32_t g = w[q] & kPtIndexMask;
           const bool last = w[q] != kPtPad && (w[q] & kPtLast) && AXG_BOUND(g, st.nglob, 3);
           im[q] = last ? st.inv_mass[g] : 0.f;
+          if (KAHAN) imd[KAHAN ? q : 0] = last && st.inv_mass_dp ? st.inv_mass_dp[g] : 0.0;
           gam[q] = last && st.gamma ? st.gamma[g] : 0.f;
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
@@ -1126,8 +1130,14 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
           if ((w[q] & kPtSource) && stf1 != 0.f) {
             for (int k = 0; k < st.src.n; ++k)
               if ((uint32_t)st.src.gidx[k] == g) {
+                if (KAHAN && st.src.val_dp) {  // the source projection in FP64, one rounding
 #pragma unroll
-                for (int c = 0; c < NC; ++c) v[c] = v[c] - st.src.val[3 * k + gc(c)] * stf1;
+                  for (int c = 0; c < NC; ++c)
+                    v[c] = (float)((double)v[c] - st.src.val_dp[3 * k + gc(c)] * (double)stf1);
+                } else {
+#pragma unroll
+                  for (int c = 0; c < NC; ++c) v[c] = v[c] - st.src.val[3 * k + gc(c)] * stf1;
+                }
               }
           }
 #pragma unroll
@@ -1138,7 +1148,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
               // kick (SOLVER/time_evol_wave.F90:688-717): acc = -inv_mass acc
               // [- absorbing terms], velo += acc * coefv(i); the dipole's z
               // component takes twice the whole acceleration
-              float a = -im[q] * v[c];
+              float a = (KAHAN && st.inv_mass_dp) ? (float)(-imd[KAHAN ? q : 0] * (double)v[c]) : -im[q] * v[c];
               if (st.gamma) a = a - 2.f * gam[q] * vel[q][c] - gam[q] * gam[q] * dsp;
               const float kick = (POLE == POLE_DI && cg == 2) ? 2.f * st.kick : st.kick;
               if (KAHAN) {
@@ -1155,7 +1165,13 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
               if (KAHAN && zero) st.cu[cg][g] = 0.f;
               continue;
             }
-            float a = (POLE == POLE_DI && cg == 2) ? (-2.f * im[q]) * v[c] : -im[q] * v[c];
+            float a;
+            if (KAHAN && st.inv_mass_dp) {  // the inverse mass in FP64, one rounding
+              const double md = imd[KAHAN ? q : 0];
+              a = (float)((POLE == POLE_DI && cg == 2) ? (-2.0 * md) * (double)v[c] : -md * (double)v[c]);
+            } else {
+              a = (POLE == POLE_DI && cg == 2) ? (-2.f * im[q]) * v[c] : -im[q] * v[c];
+            }
             if (st.gamma) a = a - 2.f * gam[q] * vel[q][c] - gam[q] * gam[q] * dsp;
             if (KAHAN) {
               float k = kv[KAHAN ? q : 0][c];
@@ -1417,6 +1433,7 @@ __global__ void __launch_bounds__(kThreads, 4) fluid_patch_kernel(const __grid_c
   {
     uint32_t w[kGB];
     float vel[kGB], acc[kGB], im[kGB], gam[kGB], kv[KAHAN ? kGB : 1];
+    double imd[KAHAN ? kGB : 1];  // compensated mode: the FP64 inverse mass, when the handle has it
 #pragma unroll
     for (int q = 0; q < kGB; ++q) {
       const int t = threadIdx.x + q * kThreads;
@@ -1424,6 +1441,7 @@ __global__ void __launch_bounds__(kThreads, 4) fluid_patch_kernel(const __grid_c
       const uint32_t g = w[q] & kPtIndexMask;
       const bool last = w[q] != kPtPad && (w[q] & kPtLast) && AXG_BOUND(g, st.nglob, 13);
       im[q] = last ? st.inv_mass[g] : 0.f;
+      if (KAHAN) imd[KAHAN ? q : 0] = last && st.inv_mass_dp ? st.inv_mass_dp[g] : 0.0;
       gam[q] = last && st.gamma ? st.gamma[g] : 0.f;
       vel[q] = last ? st.v[0][g] : 0.f;
       acc[q] = last && !SYMP ? st.a[0][g] : 0.f;
@@ -1441,6 +1459,7 @@ __global__ void __launch_bounds__(kThreads, 4) fluid_patch_kernel(const __grid_c
         continue;
       }
       float a = -im[q] * v;
+      if (KAHAN && st.inv_mass_dp) a = (float)(-imd[KAHAN ? q : 0] * (double)v);  // FP64, one rounding
       const float chi = s_u[t];
       if (st.gamma) a = a - 2.f * gam[q] * vel[q] - gam[q] * gam[q] * chi;
       if (SYMP && KAHAN) {

@@ -88,6 +88,10 @@ class Mesh:
     # absorbing boundaries
     solid_absorbing_gamma: np.ndarray | None = None
     fluid_absorbing_gamma: np.ndarray | None = None
+    # FP64 copies the compensated mode applies in FP64 (optional)
+    inv_mass_rho_dp: np.ndarray | None = None      # (5,5,nel_solid) float64
+    inv_mass_fluid_dp: np.ndarray | None = None    # (5,5,nel_fluid) float64
+    source_term_el_dp: np.ndarray | None = None    # (5,5,8,3) float64
     # bookkeeping for tests: element grid shape, geometry
     meta: dict = field(default_factory=dict)
 
@@ -122,7 +126,7 @@ class Mesh:
         def dp(a):
             if a is None:
                 return C.cast(None, C.POINTER(C.c_double))
-            a = np.ascontiguousarray(a, dtype=np.float64)
+            a = np.asfortranarray(a, dtype=np.float64) if np.ndim(a) > 1 else np.ascontiguousarray(a, np.float64)
             keep.append(a)
             return a.ctypes.data_as(C.POINTER(C.c_double))
 
@@ -190,6 +194,9 @@ class Mesh:
                        "DsDeta_over_J_sol_cg4", "DzDeta_over_J_sol_cg4",
                        "DsDxi_over_J_sol_cg4", "DzDxi_over_J_sol_cg4", "inv_s_solid"):
                 setattr(d, nm, fp(a[nm]))
+        d.inv_mass_rho_dp = dp(self.inv_mass_rho_dp)
+        d.inv_mass_fluid_dp = dp(self.inv_mass_fluid_dp)
+        d.source_term_el_dp = dp(self.source_term_el_dp)
         d._keep = keep  # type: ignore[attr-defined]
         return d
 

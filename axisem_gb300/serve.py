@@ -24,28 +24,29 @@ receiver count and a seismogram duration.  The server
 Solves run in the compensated (Kahan) FP32 mode by default, the precision of
 the serving workload.
 
-The meshes are seeded synthetic coupled meshes (a solid layer over a fluid
-layer, `coupled_mesh`) whose size grows as the period shrinks; they stand in
-for the mesher's PREM meshes, which this build has no mesher for.
+The meshes are the whole-Earth prem_iso meshes of axisem_gb300.sphere at the
+request's period (50 s: 6.6k elements, 25 s: 22k, 10 s: 117k), each with its
+CFL time step; a request puts its own source depth, receivers and run length
+on the cached mesh (sphere.with_solve).  Seismograms are sampled every
+period / 8 seconds.  `duration_scale` shortens every run by the same factor
+(the default benchmark serves 1/10 of the requested seismogram lengths so
+that a rate sweep fits in minutes); the steps keep the physical time step.
 """
 from __future__ import annotations
 
 import collections
-import copy
 import time
 from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import _abi
-from .mesh import Mesh, coupled_mesh, set_source_receivers
+from . import _abi, sphere
+from .mesh import Mesh
 from .solver import Batch, Solver
 
-# period (s) -> coupled mesh (ni, nj_solid, nj_fluid): ~4x the elements per halving
-MESH_OF_PERIOD = {50: (32, 24, 8), 25: (64, 48, 16), 10: (128, 96, 32)}
-STEPS_PER_PERIOD = 4     # steps per period of seismogram (scaled down from the mesher's dt)
-DELTAT = 2e-8            # s; keeps the synthetic operators stable over the run lengths used
+PERIODS = (50, 25, 10)
 POLES = (_abi.MONOPOLE, _abi.DIPOLE, _abi.QUADPOLE)
+SOURCE_OF_POLE = {_abi.MONOPOLE: "explosion", _abi.DIPOLE: "mtr", _abi.QUADPOLE: "mtp"}
 
 
 @dataclass
@@ -56,46 +57,63 @@ class Request:
     pole: int            # 0 mono, 1 di, 2 quad
     depth_km: float      # source depth, 0..700 km
     n_rec: int           # receivers on the surface
-    duration_s: float    # seismogram length
+    duration_s: float    # seismogram length requested
+    duration_scale: float = 1.0
 
     @property
     def key(self):
         return (self.period, self.pole)
 
     @property
+    def seconds(self) -> float:
+        return self.duration_s * self.duration_scale
+
+    @property
     def niter(self) -> int:
-        return max(8, int(round(self.duration_s / self.period * STEPS_PER_PERIOD)))
+        return int(np.ceil((self.seconds + 1e-11) / template(self.period, self.pole).deltat))
 
 
-def request_stream(n: int, rate_per_s: float, seed: int = 2026) -> list[Request]:
+def request_stream(n: int, rate_per_s: float, seed: int = 2026, duration_scale: float = 1.0) -> list[Request]:
     """Seeded Poisson arrivals; period uniform in {50, 25, 10} s, source type
     uniform, depth uniform in [0, 700] km, receivers uniform in [20, 500],
-    duration uniform in [1800, 3600] s."""
+    duration uniform in [1800, 3600] s (times duration_scale).  A rate of
+    0 or less makes every request arrive at once (a saturating stream)."""
     rng = np.random.default_rng(seed)
-    t = np.cumsum(rng.exponential(1.0 / rate_per_s, size=n))
+    gaps = rng.exponential(1.0 / rate_per_s if rate_per_s > 0 else 1.0, size=n)
+    t = np.cumsum(gaps) if rate_per_s > 0 else np.zeros(n)
     return [Request(k, float(t[k]), int(rng.choice([50, 25, 10])), int(rng.integers(0, 3)),
-                    float(rng.uniform(0, 700)), int(rng.integers(20, 501)), float(rng.uniform(1800, 3600)))
+                    float(rng.uniform(0, 700)), int(rng.integers(20, 501)), float(rng.uniform(1800, 3600)),
+                    duration_scale)
             for k in range(n)]
 
 
-_TEMPLATES: dict = {}   # (period, pole) -> (host mesh, source moment): the mesh database a server keeps loaded
+_SKELETONS: dict = {}   # period -> skeleton
+_TEMPLATES: dict = {}   # (period, pole) -> Mesh: the mesh database a server keeps loaded
+
+
+def template(period: int, pole: int) -> Mesh:
+    """The period's prem_iso mesh for a pole type (built once per process)."""
+    if (period, pole) not in _TEMPLATES:
+        if period not in _SKELETONS:
+            _SKELETONS[period] = sphere.build_skeleton(float(period))
+        _TEMPLATES[(period, pole)] = sphere.build_mesh(
+            float(period), sphere.SphereSolve(pole=pole, source=SOURCE_OF_POLE[pole], seconds=float(period),
+                                              receivers_deg=np.array([90.0])),
+            skeleton=_SKELETONS[period], pointwise=False)
+    return _TEMPLATES[(period, pole)]
 
 
 def request_mesh(req: Request, niter: int | None = None) -> Mesh:
-    """The solve's mesh descriptor: the period's mesh (kept on the host after
-    its first use) with this request's source row (depth), receivers and run
-    length."""
-    ni, njs, njf = MESH_OF_PERIOD[req.period]
-    if req.key not in _TEMPLATES:
-        t = coupled_mesh(ni, njs, njf, req.pole, niter=1, seed=11, num_rec=1, seis_it=4, deltat=DELTAT,
-                         terms="pole")
-        _TEMPLATES[req.key] = (t, t.source_term_el[4, 4, 0, :].copy())   # the moment at the source corner
-    tmpl, val = _TEMPLATES[req.key]
-    m = copy.copy(tmpl)   # shares the mesh arrays; the solve's fields are replaced below
-    row = 1 + int(round(req.depth_km / 700.0 * (njs - 2)))
-    nrec = min(req.n_rec, ni)   # receivers on distinct surface elements
-    return set_source_receivers(m, ni, njs, njf, val, src_row=njs - 1 - row, num_rec=nrec,
-                                niter=req.niter if niter is None else niter, deltat=DELTAT, seis_it=4)
+    """The solve's mesh descriptor: the period's cached mesh with this
+    request's source depth, receivers (uniform in colatitude), run length
+    and sampling (period / 8)."""
+    t = template(req.period, req.pole)
+    seis_it = max(1, int(round(req.period / 8.0 / t.deltat)))
+    seconds = req.seconds if niter is None else niter * t.deltat
+    solve = sphere.SphereSolve(pole=req.pole, source=SOURCE_OF_POLE[req.pole], depth_km=req.depth_km,
+                               seconds=seconds, receivers_deg=np.linspace(0.0, 180.0, req.n_rec),
+                               seis_it=seis_it)
+    return sphere.with_solve(t, solve, _SKELETONS[req.period])
 
 
 @dataclass
@@ -171,8 +189,8 @@ class Server:
         return self.meshes[req.key]
 
     def _estimate(self, req: Request) -> int:
-        ni, njs, njf = MESH_OF_PERIOD[req.period]
-        nglob = (4 * ni + 1) * (4 * njs + 1) + (4 * ni + 1) * (4 * njf + 1)
+        t = template(req.period, req.pole)
+        nglob = t.nglob_solid + t.nglob_fluid
         need = nglob * 4 * 4 * 3 + 4 * req.niter * 3 * req.n_rec + (1 << 20)   # wavefields, seismograms
         if req.key not in self.meshes:
             need += 4 * need   # a mesh is a few times its wavefields

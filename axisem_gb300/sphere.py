@@ -47,6 +47,7 @@ rounded to FP32 where the reference stores realkind):
 """
 from __future__ import annotations
 
+import copy
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -76,6 +77,7 @@ class Skeleton:
     axis: np.ndarray
     kind: np.ndarray                  # 0 square, 1 ring, 2 shell, 3 coarsening band
     info: dict = field(default_factory=dict)
+    cache: dict = field(default_factory=dict, repr=False)   # geometry and numbering, shared by the pole types
 
 
 class _Builder:
@@ -361,35 +363,53 @@ def global_numbering(sk: Skeleton, els: np.ndarray):
 
 
 # ============================================================== precomputed terms
-def _c_ijkl(lam, mu, xi_a, phi_a, eta_a, th_fa, ph_fa, i, j, k, l):
-    """c_ijkl_ani (SOLVER/def_precomp_terms.f90:2291-2335): the elastic tensor
-    of a transversely isotropic medium with fast axis (th_fa, ph_fa)
-    (Nolet 2008, eq. 16.2); indices 1..3."""
+C_COMPONENTS = (("11", (1, 1, 1, 1)), ("12", (1, 1, 2, 2)), ("13", (1, 1, 3, 3)), ("15", (1, 1, 3, 1)),
+                ("22", (2, 2, 2, 2)), ("23", (2, 2, 3, 3)), ("25", (2, 2, 3, 1)), ("33", (3, 3, 3, 3)),
+                ("35", (3, 3, 3, 1)), ("44", (2, 3, 2, 3)), ("46", (2, 3, 1, 2)), ("55", (3, 1, 3, 1)),
+                ("66", (1, 2, 1, 2)))
+
+
+def elastic_tensor(lam, mu, xi_a, phi_a, eta_a, th_fa, ph_fa=0.0) -> dict:
+    """c_ijkl_ani (SOLVER/def_precomp_terms.f90:2291-2335) for the 13
+    components the stiffness terms use (C11 = c_1111, C12 = c_1122, ...,
+    C66 = c_1212): the elastic tensor of a transversely isotropic medium with
+    fast axis (th_fa, ph_fa) (Nolet 2008, eq. 16.2).  The anisotropic terms
+    are formed only where the medium is anisotropic (they vanish for
+    xi = phi = eta = 1)."""
     d = lambda a, b: 1.0 if a == b else 0.0  # noqa: E731
-    sv = [np.cos(ph_fa) * np.sin(th_fa), np.sin(ph_fa) * np.sin(th_fa), np.cos(th_fa)]
+    out = {nm: lam * d(i, j) * d(k, l) + mu * (d(i, k) * d(j, l) + d(i, l) * d(j, k))
+           for nm, (i, j, k, l) in C_COMPONENTS}
+    ani = (xi_a != 1.0) | (phi_a != 1.0) | (eta_a != 1.0)
+    if not np.any(ani):
+        return out
+    L, M, X, P, E, T = (np.broadcast_to(a, ani.shape)[ani] for a in (lam, mu, xi_a, phi_a, eta_a, th_fa))
+    a1 = (E - 1.0) * L + 2.0 * E * M * (1.0 - 1.0 / X)
+    a2 = M * (1.0 / X - 1.0)
+    a3 = (1.0 - 2.0 * E + P) * (L + 2.0 * M) + (4.0 * E - 4.0) * M / X
+    sv = [np.cos(ph_fa) * np.sin(T), np.sin(ph_fa) * np.sin(T), np.cos(T)]
     s = lambda a: sv[a - 1]  # noqa: E731
-    c = lam * d(i, j) * d(k, l) + mu * (d(i, k) * d(j, l) + d(i, l) * d(j, k))
-    c = c + ((eta_a - 1.0) * lam + 2.0 * eta_a * mu * (1.0 - 1.0 / xi_a)) * (d(i, j) * s(k) * s(l)
-                                                                            + d(k, l) * s(i) * s(j))
-    c = c + mu * (1.0 / xi_a - 1.0) * (d(i, k) * s(j) * s(l) + d(i, l) * s(j) * s(k) + d(j, k) * s(i) * s(l)
-                                       + d(j, l) * s(i) * s(k))
-    c = c + ((1.0 - 2.0 * eta_a + phi_a) * (lam + 2.0 * mu) + (4.0 * eta_a - 4.0) * mu / xi_a) * (
-        s(i) * s(j) * s(k) * s(l))
-    return c
+    for nm, (i, j, k, l) in C_COMPONENTS:
+        add = (a1 * (d(i, j) * s(k) * s(l) + d(k, l) * s(i) * s(j))
+               + a2 * (d(i, k) * s(j) * s(l) + d(i, l) * s(j) * s(k) + d(j, k) * s(i) * s(l) + d(j, l) * s(i) * s(k))
+               + a3 * (s(i) * s(j) * s(k) * s(l)))
+        c = np.array(out[nm], dtype=np.float64, copy=True)
+        c[ani] = c[ani] + add
+        out[nm] = c
+    return out
 
 
-def _pdistsum_f32(vals_f: np.ndarray, igloc: np.ndarray, nglob: int) -> np.ndarray:
+def _pdistsum_f32(vals_f: np.ndarray, igloc: np.ndarray, nglob: int, dtype=F32) -> np.ndarray:
     """pdistsum_solid / pdistsum_fluid (SOLVER/commun.F90:69-283) of an
-    element-local FP32 field (5, 5, E): edge points summed in FP32 in the walk
-    order (element by element, ipol fastest, interior points skipped), the sums
-    scattered back."""
+    element-local field (5, 5, E): edge points summed in `dtype` (FP32, as
+    the reference's realkind build) in the walk order (element by element,
+    ipol fastest, interior points skipped), the sums scattered back."""
     E = vals_f.shape[2]
     ig = igloc.reshape(E, 5, 5) - 1                # [e, j, i]
-    v = np.asarray(vals_f, dtype=F32).transpose(2, 1, 0)   # [e, j, i]
+    v = np.asarray(vals_f, dtype=dtype).transpose(2, 1, 0)   # [e, j, i]
     edge = np.zeros((5, 5), dtype=bool)
     edge[0, :] = edge[4, :] = edge[:, 0] = edge[:, 4] = True
     idx = ig[:, edge].reshape(-1)
-    g = np.zeros(nglob, dtype=F32)
+    g = np.zeros(nglob, dtype=dtype)
     np.add.at(g, idx, v[:, edge].reshape(-1))
     out = v.copy()
     out[:, edge] = g[ig[:, edge]]
@@ -496,7 +516,9 @@ def build_mesh(period: float = 50.0, solve: SphereSolve | None = None, model: st
     solve = solve or SphereSolve()
     sk = skeleton or build_skeleton(period, model)
     pole = solve.pole
-    geo = element_geometry(sk)
+    if "geo" not in sk.cache:            # the pole-independent geometry, computed once per skeleton
+        sk.cache["geo"] = element_geometry(sk)
+    geo = sk.cache["geo"]
     s, z = geo["s"], geo["z"]
     dsdxi, dzdxi, dsdeta, dzdeta = geo["dsdxi"], geo["dzdxi"], geo["dsdeta"], geo["dzdeta"]
     ax = geo["axis"]
@@ -557,20 +579,16 @@ def build_mesh(period: float = 50.0, solve: SphereSolve | None = None, model: st
     if attenuation is not None:
         anel = _prepare_attenuation(attenuation, solid, lam, mu, massmat, r, idom, model, deltat)
     fluid = np.flatnonzero(fluid_el)
-    ig_s, ng_s = global_numbering(sk, solid)
+    if "num_solid" not in sk.cache:
+        sk.cache["num_solid"] = global_numbering(sk, solid)
+    ig_s, ng_s = sk.cache["num_solid"]
     m = Mesh(src_type=pole, nel_solid=len(solid), nglob_solid=ng_s, igloc_solid=ig_s,
              ax_el_solid=(np.flatnonzero(ax[solid]) + 1).astype(I32), spec=SP, m_solid={}, m0_solid={},
              inv_mass_rho=None)
     # ---- solid stiffness terms
     S = solid
     th_fa = theta[S]
-    C = {}
-    args = (lam[S], mu[S], xi_a[S], phi_a[S], eta_a[S], th_fa, 0.0)
-    for nm, ijkl in (("11", (1, 1, 1, 1)), ("12", (1, 1, 2, 2)), ("13", (1, 1, 3, 3)), ("15", (1, 1, 3, 1)),
-                     ("22", (2, 2, 2, 2)), ("23", (2, 2, 3, 3)), ("25", (2, 2, 3, 1)), ("33", (3, 3, 3, 3)),
-                     ("35", (3, 3, 3, 1)), ("44", (2, 3, 2, 3)), ("46", (2, 3, 1, 2)), ("55", (3, 1, 3, 1)),
-                     ("66", (1, 2, 1, 2))):
-        C[nm] = _c_ijkl(*args, *ijkl)
+    C = elastic_tensor(lam[S], mu[S], xi_a[S], phi_a[S], eta_a[S], th_fa, 0.0)
     t = {k: v[S] for k, v in T.items()}
     kw = massmat_kwts2[S]
     Ms, Mz, Me, Mse = Msxi[S], Mzxi[S], Mzeta[S], Mseta[S]
@@ -684,12 +702,17 @@ def build_mesh(period: float = 50.0, solve: SphereSolve | None = None, model: st
     if pole == _abi.DIPOLE:
         inv_s = (inv_s * F32(0.5)).astype(F32)
     m.inv_mass_rho = np.asfortranarray(inv_s)
+    # the same in FP64 throughout, for the compensated mode's FP64 terms
+    mass_d = _pdistsum_f32(np.transpose(rho[S] * massmat[S], (1, 2, 0)), ig_s, ng_s, np.float64)
+    m.inv_mass_rho_dp = np.asfortranarray((0.5 if pole == _abi.DIPOLE else 1.0) / mass_d)
     m.meta.update(skeleton=sk.info, kind="sphere", period=period, model=model,
                   massmat_k=massmat, rho=rho, solid=solid, fluid=fluid, r=r, theta=theta)
 
     # ---- fluid
     if len(fluid):
-        ig_f, ng_f = global_numbering(sk, fluid)
+        if "num_fluid" not in sk.cache:
+            sk.cache["num_fluid"] = global_numbering(sk, fluid)
+        ig_f, ng_f = sk.cache["num_fluid"]
         Fl = fluid
         m.nel_fluid, m.nglob_fluid, m.igloc_fluid = len(Fl), ng_f, ig_f
         m.ax_el_fluid = (np.flatnonzero(ax[Fl]) + 1).astype(I32)
@@ -710,6 +733,8 @@ def build_mesh(period: float = 50.0, solve: SphereSolve | None = None, model: st
         m.meta["unassem_mass_lam_fluid"] = np.asfortranarray(mass_f)
         mass_f = _pdistsum_f32(mass_f, ig_f, ng_f)
         m.inv_mass_fluid = np.asfortranarray((F32(1.0) / mass_f).astype(F32))
+        mass_fd = _pdistsum_f32(np.transpose(massmat[Fl] / lam_f, (1, 2, 0)), ig_f, ng_f, np.float64)
+        m.inv_mass_fluid_dp = np.asfortranarray(1.0 / mass_fd)
         _boundary(m, sk, geo, solid, fluid)
     if pointwise or anel is not None:
         _pointwise(m, geo, solid, fluid, rho)
@@ -973,16 +998,25 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
     for c in comps:
         stf_[0, :, ax_el, c] = 0.0
     stf_ = stf_ / F32(np.pi if pole == _abi.DIPOLE else 2.0 * np.pi)
-    nz = [e for e in range(E) if np.any(stf_[:, :, e, :] != 0)]
+    # the same in FP64 (the entries the FP32 term keeps)
+    std_ = np.zeros((5, 5, E, 3), order="F")
+    for c in range(3):
+        std_[..., c] = _pdistsum_f32(np.transpose(st[..., c], (1, 2, 0)), m.igloc_solid, m.nglob_solid, np.float64)
+    std_[stf_ == 0] = 0.0
+    std_ = std_ / (np.pi if pole == _abi.DIPOLE else 2.0 * np.pi)
+    nz = np.flatnonzero(np.any(stf_ != 0, axis=(0, 1, 3))).tolist()
     if len(nz) > 8:
         raise RuntimeError(f"source term spans {len(nz)} elements (8 at most)")
     m.ielsrc = np.zeros(8, dtype=I32)
     m.ielsrc[:len(nz)] = np.array(nz, dtype=I32) + 1
     m.nelsrc = len(nz)
     ste = np.zeros((5, 5, 8, 3), dtype=F32, order="F")
+    sted = np.zeros((5, 5, 8, 3), order="F")
     for k, e in enumerate(nz):
         ste[:, :, k, :] = stf_[:, :, e, :]
+        sted[:, :, k, :] = std_[:, :, e, :]
     m.source_term_el = ste
+    m.source_term_el_dp = sted
     m.fluid_src = 0
     m.meta["source"] = {"kind": kind, "depth_km": float((R_EARTH - z[tuple(hits[0])]) / 1000.0),
                         "elements": [int(e) + 1 for e in src_els]}
@@ -999,3 +1033,16 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
         rows.append((e + 1, i, j))
     m.recfile_el = np.asfortranarray(np.array(rows, dtype=I32).reshape(-1, 3))
     m.meta["receiver_colat_deg"] = np.array([th[int(np.argmin(np.abs(th - c)))] for c in rec])
+
+
+def with_solve(m: Mesh, solve: SphereSolve, skeleton: Skeleton) -> Mesh:
+    """The mesh `m` (built by build_mesh on `skeleton` for the same pole
+    type) with another solve's source depth, receivers, run length and
+    sampling: a shallow copy sharing every mesh array, so that meshes that
+    differ only in these are the same mesh (axg_create_sharing)."""
+    if solve.pole != m.src_type:
+        raise ValueError("with_solve keeps the pole type of the mesh")
+    out = copy.copy(m)
+    out.meta = dict(m.meta)
+    _source_receivers(out, skeleton, skeleton.cache["geo"], solve, m.meta["period"], m.deltat)
+    return out

@@ -324,6 +324,7 @@ def run_gpu(args):
         timeloop_comp = run_timeloop(args, pole, ws, rank, compensated=True)
         timeloop_dumps = run_timeloop_dumps(args, pole, ws, rank)
 
+    physical = run_physical(args, ws, rank) if args.physical_steps > 0 else None
     serving = run_serving(args) if args.serve_requests > 0 else None
 
     if rank != 0:
@@ -345,6 +346,7 @@ def run_gpu(args):
         "timeloop_anel": timeloop_anel,
         "timeloop_compensated": timeloop_comp,
         "timeloop_dumps": timeloop_dumps,
+        "physical": physical,
         "serving": serving,
         "clocks": head["clocks"],
         "gpu_launches": int(args.steps * info["kernels_per_force"]),
@@ -428,6 +430,58 @@ def run_timeloop(args, pole, ws, rank, anel=False, compensated=False):
             "finite": bool(np.isfinite(rec).all())}
 
 
+def run_physical(args, ws, rank):
+    """Time loops on the whole-Earth prem_iso meshes (axisem_gb300.sphere):
+    config 1 -- 50 s, monopole explosion at 100 km, 1800 s, 20 receivers --
+    as a whole solve, and config 3 -- 10 s, 5-SLS cg4 attenuation, explosion,
+    mrt and mtp at 50 km, 200 receivers -- over `physical_steps` steps of each
+    source type, with the whole 3600 s solve's time projected from them."""
+    import torch
+    from axisem_gb300 import sphere
+    from axisem_gb300.solver import Solver
+    out = {}
+    sk50 = sphere.build_skeleton(50.0)
+    m = sphere.build_mesh(50.0, sphere.SphereSolve(pole=0, seconds=1800.0), skeleton=sk50)
+    with Solver(m) as s:
+        s.autotune()
+        s.reset()
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        s.run()
+        torch.cuda.synchronize()
+        dt = max_over_ranks(time.perf_counter() - t0, ws)
+        rec = s.receivers()
+    pts = 25 * (m.nel_solid + m.nel_fluid)
+    out["config1_prem50s_explosion_1800s"] = {
+        "elements": m.nel_solid + m.nel_fluid, "steps": m.niter, "deltat_s": m.deltat, "solve_s": dt,
+        "value": ws * pts * m.niter / dt, "unit": "GLL-point-steps/s", "ms_per_step": dt / m.niter * 1e3,
+        "finite": bool(np.isfinite(rec).all())}
+    sk10 = sphere.build_skeleton(10.0)
+    for pole, src in ((0, "explosion"), (1, "mtr"), (2, "mtp")):
+        m = sphere.build_mesh(10.0, sphere.SphereSolve(pole=pole, source=src, depth_km=50.0, seconds=3600.0,
+                                                       receivers_deg=np.linspace(0.0, 180.0, 200)),
+                              skeleton=sk10, attenuation=sphere.Attenuation(), pointwise=False)
+        n = min(args.physical_steps, m.niter)
+        with Solver(m) as s:
+            spg = s.autotune()
+            s.reset()
+            s.run(1, min(64, m.niter))
+            torch.cuda.synchronize()
+            barrier(ws)
+            t0 = time.perf_counter()
+            s.run(65, n)
+            torch.cuda.synchronize()
+            dt = max_over_ranks((time.perf_counter() - t0) / n, ws)
+            rec = s.receivers()
+        pts = 25 * (m.nel_solid + m.nel_fluid)
+        out[f"config3_prem10s_anelastic_{src}"] = {
+            "elements": m.nel_solid + m.nel_fluid, "steps_timed": n, "steps_solve": m.niter,
+            "deltat_s": m.deltat, "ms_per_step": dt * 1e3, "value": ws * pts / dt, "unit": "GLL-point-steps/s",
+            "solve_s_projected": dt * m.niter, "steps_per_graph": spg, "finite": bool(np.isfinite(rec).all())}
+    return out
+
+
 def run_timeloop_dumps(args, pole, ws, rank, strain_it=8):
     """The elastic time loop of run_timeloop without and with kernel wavefield
     dumps (axg_set_wavefield_dump: displ_only and strain_only every strain_it
@@ -475,40 +529,48 @@ def run_timeloop_dumps(args, pole, ws, rank, strain_it=8):
 
 
 def run_serving(args):
-    """Continuous-batching serving (axisem_gb300.serve; the meshes of the
-    stream resident before it starts), with solves overlapping on their own
-    streams and with solves advanced together in batches, against the same
-    request list run one solve at a time, each on its own freshly built mesh
-    (the plain path, sequentially).  Seeded Poisson arrivals at
-    args.serve_rate per second; each request's seismograms must be identical
-    in all runs."""
-    from axisem_gb300.serve import Server, request_stream
-    reqs = request_stream(args.serve_requests, args.serve_rate, seed=2026)
+    """The serving stream of the workload's config 4 (axisem_gb300.serve) on
+    the prem_iso meshes of 50, 25 and 10 s, compensated FP32, the meshes
+    resident before the streams start.  Requests draw period, pole, depth
+    (0-700 km), receivers (20-500) and duration (1800-3600 s, times
+    duration_scale; physical time steps).  Capacity: every request at once,
+    served concurrently, batched, and one at a time on the resident meshes
+    (the baseline); seismograms must be identical in all three.  Then a sweep
+    of Poisson arrival rates with p50/p99 latency per rate."""
+    from axisem_gb300.serve import PERIODS, POLES, Server, request_stream
+    scale = args.serve_duration_scale
     srv = Server(budget_bytes=64e9)
     try:
-        srv.preload({r.key for r in reqs})   # the server's meshes are resident before the stream starts
-        served = srv.run(reqs)
-        batched = srv.run(reqs, batched=True)
+        t0 = time.perf_counter()
+        srv.preload({(p, q) for p in PERIODS for q in POLES})
+        t_preload = time.perf_counter() - t0
+        sat = request_stream(args.serve_requests, 0.0, seed=2026, duration_scale=scale)
+        served = srv.run(sat)
+        batched = srv.run(sat, batched=True)
+        seq = srv.run(sat, sequential=True, resident=True)
+        same = all(np.array_equal(served.results[r.rid].seismograms, seq.results[r.rid].seismograms) and
+                   np.array_equal(batched.results[r.rid].seismograms, seq.results[r.rid].seismograms)
+                   for r in sat)
+        sweep = []
+        for lam in [float(x) for x in args.serve_rates.split(",") if x]:
+            n = int(np.clip(round(12 * lam), 6, args.serve_requests))
+            reqs = request_stream(n, lam, seed=2027, duration_scale=scale)
+            sweep.append({"rate_per_s": lam, "requests": n, "served": srv.run(reqs).summary(),
+                          "served_batched": srv.run(reqs, batched=True).summary()})
     finally:
         srv.close()
-    seq_srv = Server(budget_bytes=64e9)
-    try:
-        seq = seq_srv.run(reqs, sequential=True)
-        seq_srv.preload({r.key for r in reqs})
-        seq_res = seq_srv.run(reqs, sequential=True, resident=True)
-    finally:
-        seq_srv.close()
-    same = all(np.array_equal(served.results[r.rid].seismograms, seq.results[r.rid].seismograms) and
-               np.array_equal(batched.results[r.rid].seismograms, seq.results[r.rid].seismograms) for r in reqs)
-    a, b, c = served.summary(), seq.summary(), batched.summary()
-    return {"requests": len(reqs), "arrival_rate_per_s": args.serve_rate,
-            "mix": "period {50,25,10} s -> 1k/4k/16k-element coupled meshes, pole {mono,di,quad}, "
-                   "depth 0-700 km, 20-500 receivers, 1800-3600 s; compensated (Kahan) FP32",
-            "served": a, "served_batched": c, "sequential_plain": b,
-            "sequential_resident_meshes": seq_res.summary(),
-            "solves_per_hour_ratio": a["solves_per_hour"] / b["solves_per_hour"],
-            "batched_solves_per_hour_ratio": c["solves_per_hour"] / b["solves_per_hour"],
-            "results_identical_to_sequential": bool(same)}
+    a, b, c = served.summary(), batched.summary(), seq.summary()
+    steps = [r.niter for r in sat]
+    return {"requests": len(sat), "arrival": "all at once (capacity)",
+            "mix": "prem_iso meshes of 50/25/10 s (6.6k/22k/117k elements, CFL time steps), pole "
+                   "{mono,di,quad}, depth 0-700 km, 20-500 receivers sampled every period/8, "
+                   f"1800-3600 s of seismogram times {scale} ({min(steps)}-{max(steps)} steps); "
+                   "compensated (Kahan) FP32",
+            "duration_scale": scale, "mesh_preload_s": round(t_preload, 1),
+            "served": a, "served_batched": b, "sequential_resident_meshes": c,
+            "solves_per_hour_ratio": a["solves_per_hour"] / c["solves_per_hour"],
+            "batched_solves_per_hour_ratio": b["solves_per_hour"] / c["solves_per_hour"],
+            "results_identical_to_sequential": bool(same), "sweep": sweep}
 
 
 def main():
@@ -523,8 +585,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-other-poles", action="store_true")
     ap.add_argument("--timeloop-steps", type=int, default=64)
+    ap.add_argument("--physical-steps", type=int, default=2000)
     ap.add_argument("--serve-requests", type=int, default=24)
-    ap.add_argument("--serve-rate", type=float, default=1000.0)   # saturating: measures capacity
+    ap.add_argument("--serve-rates", default="0.5,1,2,5,10,20")
+    ap.add_argument("--serve-duration-scale", type=float, default=0.1)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

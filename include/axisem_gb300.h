@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define AXG_ABI_VERSION 1
+#define AXG_ABI_VERSION 2
 #define AXG_NPOL 4   /* only npol = 4 (5x5 GLL points) is supported, as the *_4 kernels */
 
 /* ---- status codes ---------------------------------------------------- */
@@ -149,6 +149,16 @@ typedef struct axg_mesh_desc {
   const float *DsDeta_over_J_sol_cg4, *DzDeta_over_J_sol_cg4;
   const float *DsDxi_over_J_sol_cg4, *DzDxi_over_J_sol_cg4;                  /* (1:4,nel_solid) */
   const float *inv_s_solid;                      /* (0:4,0:4,nel_solid) */
+
+  /* FP64 copies (optional; NULL: none) of the terms the compensated mode
+   * (axg_set_compensated) applies in FP64: the assembled inverse masses and
+   * the solid source term as the precompute forms them before the cast to
+   * realkind (SOLVER/def_precomp_terms.f90:735-800 without the FP32
+   * assembly, SOLVER/source.f90:985-1226).  No counterpart in the reference,
+   * which stores them in realkind. */
+  const double *inv_mass_rho_dp;                 /* (0:4,0:4,nel_solid) */
+  const double *inv_mass_fluid_dp;               /* (0:4,0:4,nel_fluid) */
+  const double *source_term_el_dp;               /* (0:4,0:4,8,3) */
 } axg_mesh_desc;
 
 typedef struct axg_handle axg_handle;
@@ -338,9 +348,12 @@ int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages);
  * (and chi, dchi in the fluid) -- or a symplectic scheme's drifts
  * disp += coefd velo and kicks velo += coefv acc -- use Kahan's compensated summation in FP32, with
  * a running compensation per point kept in HBM, so that rounding does not
- * accumulate over 1e4-1e5 steps.  Stiffness, coupling and attenuation are
- * unchanged.  The first call allocates the compensation (zero; axg_reset
- * zeroes it too).  No counterpart in the reference. */
+ * accumulate over 1e4-1e5 steps.  When the descriptor carried the FP64
+ * inverse masses and source term, the compensated mode also multiplies by
+ * the inverse mass and subtracts the source in FP64 (one rounding to FP32
+ * each).  Stiffness, coupling and attenuation are unchanged.  The first call
+ * allocates the compensation (zero; axg_reset zeroes it too).  No
+ * counterpart in the reference. */
 int axg_set_compensated(axg_handle *h, int32_t on);
 
 /* axg_create with the patch shape chosen by the caller: patch_elems 1..64

@@ -78,7 +78,7 @@ def test_async_runs_overlap_and_match(gpu_lib):
 
 @pytest.mark.parametrize("batched", [False, True])
 def test_served_results_equal_alone(gpu_lib, batched):
-    reqs = [Request(k, 0.002 * k, period, pole, depth, nrec, dur)
+    reqs = [Request(k, 0.002 * k, period, pole, depth, nrec, dur, 0.03)
             for k, (period, pole, depth, nrec, dur) in enumerate(
                 [(50, 0, 100, 20, 1800), (25, 2, 400, 60, 2400), (50, 1, 650, 30, 3600),
                  (50, 2, 10, 25, 2000), (25, 0, 300, 40, 1800), (50, 0, 500, 20, 2600)])]
@@ -95,7 +95,7 @@ def test_served_results_equal_alone(gpu_lib, batched):
 
 @pytest.mark.parametrize("batched", [False, True])
 def test_admission_keeps_to_the_budget(gpu_lib, batched):
-    reqs = [Request(k, 0.0, 50, k % 3, 200, 20, 1800) for k in range(6)]
+    reqs = [Request(k, 0.0, 50, k % 3, 200, 20, 1800, 0.03) for k in range(6)]
     srv = Server(budget_bytes=1, chunk=32)   # nothing fits: one solve at a time
     try:
         stats = srv.run(reqs, batched=batched)

@@ -1,15 +1,15 @@
 """Host-side parts of the serving loop (no GPU): the seeded request stream
-and the per-request mesh descriptors."""
+and the per-request mesh descriptors on the PREM meshes."""
 import numpy as np
 
-from axisem_gb300.serve import MESH_OF_PERIOD, request_mesh, request_stream
+from axisem_gb300.serve import PERIODS, request_mesh, request_stream
 
 
 def test_request_stream_is_seeded():
     a, b = request_stream(16, 5.0, seed=3), request_stream(16, 5.0, seed=3)
     assert [(r.period, r.pole, r.n_rec, r.depth_km) for r in a] == [(r.period, r.pole, r.n_rec, r.depth_km) for r in b]
     assert all(x.t_arrive < y.t_arrive for x, y in zip(a, a[1:]))
-    assert {r.period for r in request_stream(64, 5.0)} == set(MESH_OF_PERIOD)
+    assert {r.period for r in request_stream(64, 5.0)} == set(PERIODS)
 
 
 def test_request_meshes_of_one_key_are_one_mesh():
@@ -25,6 +25,9 @@ def test_request_meshes_of_one_key_are_one_mesh():
         assert np.array_equal(a.m_fluid[name], b.m_fluid[name])
     assert np.array_equal(a.inv_mass_rho, b.inv_mass_rho) and np.array_equal(a.bdry_matr, b.bdry_matr)
     assert a.niter == reqs[0].niter and b.niter == reqs[1].niter
+    # the request's own source depth and receivers
+    assert a.recfile_el.shape[0] == reqs[0].n_rec and b.recfile_el.shape[0] == reqs[1].n_rec
+    assert abs(a.meta["source"]["depth_km"] - reqs[0].depth_km) < 60.0
 
 
 # ---- the batched serving loop's logic, on fakes of the solve and batch objects
@@ -80,7 +83,7 @@ def _serve(monkeypatch, reqs, **kw):
 
 def test_batched_loop_steps_every_solve_once(monkeypatch):
     from axisem_gb300.serve import Request
-    reqs = [Request(k, 0.0005 * k, 50, k % 3, 100.0 * k, 20, 1800.0 + 200 * k) for k in range(7)]
+    reqs = [Request(k, 0.0005 * k, 50, k % 3, 100.0 * k, 20, 1800.0 + 200 * k, 0.05) for k in range(7)]
     srv, stats = _serve(monkeypatch, reqs, chunk=40)
     assert set(stats.results) == {r.rid for r in reqs}
     for r in reqs:  # each solve ran iterations 1..niter exactly once, in order
@@ -95,7 +98,7 @@ def test_batched_loop_steps_every_solve_once(monkeypatch):
 
 def test_batched_loop_keeps_to_the_budget(monkeypatch):
     from axisem_gb300.serve import Request
-    reqs = [Request(k, 0.0, 50, k % 3, 200.0, 20, 1800.0) for k in range(4)]
+    reqs = [Request(k, 0.0, 50, k % 3, 200.0, 20, 1800.0, 0.05) for k in range(4)]
     _, stats = _serve(monkeypatch, reqs, budget_bytes=1, chunk=32)
     assert len(stats.results) == 4 and stats.max_concurrent == 1
 
@@ -106,7 +109,7 @@ def test_served_solves_are_compensated_by_default(monkeypatch):
     made = []
     monkeypatch.setattr(serve, "Solver", lambda *a, **k: made.append(_FakeSolver(*a, **k)) or made[-1])
     monkeypatch.setattr(serve, "Batch", _FakeBatch)
-    serve.Server(lib=object()).run([Request(0, 0.0, 50, 1, 10.0, 20, 1800.0)], batched=True)
+    serve.Server(lib=object()).run([Request(0, 0.0, 50, 1, 10.0, 20, 1800.0, 0.05)], batched=True)
     assert made and all(s.comp for s in made if s.shared)
 
 
@@ -123,7 +126,7 @@ def test_concurrent_loop_steps_every_solve_once(monkeypatch):
             return True
 
     monkeypatch.setattr(serve, "Solver", S)
-    reqs = [Request(k, 0.0003 * k, 25 if k % 2 else 50, k % 3, 50.0 * k, 30, 2000.0) for k in range(6)]
+    reqs = [Request(k, 0.0003 * k, 25 if k % 2 else 50, k % 3, 50.0 * k, 30, 2000.0, 0.05) for k in range(6)]
     for seq in (False, True):
         srv = serve.Server(lib=object(), chunk=48)
         stats = srv.run(reqs, sequential=seq)
