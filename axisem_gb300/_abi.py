@@ -123,6 +123,8 @@ class DumpDesc(C.Structure):
         ("DsDeta_over_J_flu", _fp), ("DzDeta_over_J_flu", _fp), ("DsDxi_over_J_flu", _fp),
         ("DzDxi_over_J_flu", _fp), ("inv_s_fluid", _fp), ("inv_rho_fluid", _fp),
         ("out", _fp), ("capacity", C.c_int64),
+        ("kwf_mask", _ip), ("mapping_ijel_ikwf", _ip), ("npoint_solid_kwf", C.c_int32),
+        ("npoint_fluid_kwf", C.c_int32),
     ]
 
 
@@ -195,6 +197,8 @@ SIGNATURES = {
     "axg_time_stiffness": (C.c_int, [C.c_void_p, C.c_int32, _fp]),
     "axg_device_check_report": (C.c_int, [_ip]),
     "axg_selftest_wait_timeout": (C.c_int, [_ip, C.POINTER(C.c_double)]),
+    "axg_set_seismogram_checkpoint": (C.c_int, [C.c_void_p, C.c_int32, _fp, C.c_int32]),
+    "axg_seismogram_checkpoint_samples": (C.c_int, [C.c_void_p, _ip]),
     "axg_destroy": (None, [C.c_void_p]),
     "axg_last_error": (C.c_char_p, [C.c_void_p]),
 }

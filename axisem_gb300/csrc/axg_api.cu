@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -164,6 +165,9 @@ struct axg_handle {
     int32_t *gidx_s = nullptr, *gidx_f = nullptr;
     uint8_t *ax_s = nullptr, *ax_f = nullptr;
     float *pw_s[5] = {}, *pw_f[5] = {}, *inv_rho = nullptr;
+    int32_t *kwf_s = nullptr, *kwf_f = nullptr;  // kernel wavefield layout: position of each element point or -1
+    bool kwf = false;
+    int64_t npt_s = 0, npt_f = 0;                // points per field in that layout
     float *slot[2] = {};
     int64_t slot_floats = 0;
     cudaEvent_t ev_dump[2] = {}, ev_copy[2] = {};
@@ -171,6 +175,15 @@ struct axg_handle {
   } dump;
   cudaGraphExec_t graph_dump = nullptr;  // strain_it steps, when that differs from steps_per_graph
   int graph_dump_steps = 0;
+  // seismogram checkpoints: every check_it steps the final samples go to `out`
+  struct Checkpoint {
+    int32_t check_it = 0, cap = 0;
+    float *out = nullptr;
+    int32_t queued = 0;                                     // samples whose copies are queued
+    std::deque<std::pair<cudaEvent_t, int32_t>> inflight;   // copy completions, oldest first
+    int32_t done = 0;                                       // samples whose copies completed
+    std::vector<cudaEvent_t> free_events;
+  } ckpt;
   // mesh-level buffers, shared with the handles created from this one
   std::shared_ptr<MeshPool> mesh;
   bool in_mesh = false;  // allocations go to the mesh pool while set
@@ -179,6 +192,7 @@ struct axg_handle {
 namespace {
 
 using Dump = axg_handle::Dump;
+int checkpoint_progress(axg_handle *h);
 
 int fail(axg_handle *h, int code, const std::string &msg) {
   if (h) h->err = msg;
@@ -882,6 +896,10 @@ void release(axg_handle *h) {
     cudaStreamSynchronize(h->copy_stream);
     cudaStreamDestroy(h->copy_stream);
   }
+  for (auto &q : h->ckpt.inflight) cudaEventDestroy(q.first);
+  for (cudaEvent_t e : h->ckpt.free_events) cudaEventDestroy(e);
+  h->ckpt.inflight.clear();
+  h->ckpt.free_events.clear();
   for (void *p : h->allocs) cudaFreeAsync(p, h->stream);
   if (h->stream) cudaStreamDestroy(h->stream);
   h->allocs.clear();
@@ -1639,6 +1657,10 @@ int axg_reset(axg_handle *h) {
     CK(cudaMemsetAsync(h->fa, 0, h->nglob_f * sizeof(float), h->stream));
     CK(cudaMemsetAsync(h->ff, 0, h->nglob_f * sizeof(float), h->stream));
   }
+  // checkpoints restart with the run
+  if (h->copy_stream) CK(cudaStreamSynchronize(h->copy_stream));
+  if (int rc = checkpoint_progress(h)) return rc;
+  h->ckpt.queued = h->ckpt.done = 0;
   // the iter-0 seismogram sample (dump_stuff(0,...)) is the zero wavefield
   CK(cudaMemsetAsync(h->rec, 0, (size_t)h->nseismo * 3 * std::max(h->num_rec, 1) * sizeof(float), h->stream));
   CK(cudaMemsetAsync(h->iter, 0, 4 * sizeof(int32_t), h->stream));
@@ -1656,7 +1678,7 @@ int axg_run(axg_handle *h, int32_t first_iter, int32_t n_iter) {
     return fail(h, AXG_ERR_BAD_ARG, fmt("iterations %d..%d outside 1..niter=%d", first_iter, first_iter + n_iter - 1,
                                         h->niter));
   if (n_iter == 0) return AXG_OK;
-  if (h->dump.type) {  // runs that dump are split at the dump steps
+  if (h->dump.type || h->ckpt.check_it > 0) {  // runs that dump or checkpoint: the asynchronous path
     int rc = axg_run_async(h, first_iter, n_iter);
     return rc ? rc : axg_wait(h);
   }
@@ -1809,6 +1831,8 @@ void launch_dump_pole(axg_handle *h, float *slot) {
   a.out = slot;
   a.nel = h->nel_s;
   a.nglob = h->nglob_s;
+  a.kwf = dp.kwf ? dp.kwf_s : nullptr;
+  a.npt = dp.npt_s;
   const unsigned gs = (unsigned)std::min<int64_t>((h->nel_s + ws - 1) / ws, 16 * (int64_t)h->num_sms);
   wavefield_dump_kernel<POLE, false><<<gs, kThreads, 0, h->stream>>>(a, h->spec);
   if (h->nel_f > 0 && dp.nf > 0) {
@@ -1819,9 +1843,11 @@ void launch_dump_pole(axg_handle *h, float *slot) {
     a.u[0] = h->fu;
     a.v[0] = h->fv;
     a.u[1] = a.u[2] = a.v[1] = a.v[2] = nullptr;
-    a.out = slot + (int64_t)dp.ns * h->nel_s * dp.np;
+    a.out = slot + (dp.kwf ? (int64_t)dp.ns * dp.npt_s : (int64_t)dp.ns * h->nel_s * dp.np);
     a.nel = h->nel_f;
     a.nglob = h->nglob_f;
+    a.kwf = dp.kwf ? dp.kwf_f : nullptr;
+    a.npt = dp.npt_f;
     const unsigned gf = (unsigned)std::min<int64_t>((h->nel_f + ws - 1) / ws, 16 * (int64_t)h->num_sms);
     wavefield_dump_kernel<POLE, true><<<gf, kThreads, 0, h->stream>>>(a, h->spec);
   }
@@ -1843,6 +1869,54 @@ int enqueue_dump(axg_handle *h, int64_t idx) {
   CK(cudaMemcpyAsync(dp.out + idx * dp.floats, dp.slot[k], dp.floats * sizeof(float), cudaMemcpyDeviceToHost,
                      h->copy_stream));
   CK(cudaEventRecord(dp.ev_copy[k], h->copy_stream));
+  return AXG_OK;
+}
+
+// seismogram checkpoint after iteration `last_it` (queued on the handle's
+// stream): the samples the steps up to the latest multiple of check_it have
+// recorded -- sample 0 is iteration 0, then one every seis_it steps -- are
+// final; the ones not yet copied go to the caller's buffer in one strided copy
+// of every (component, receiver) column, on the copy stream
+int enqueue_checkpoint(axg_handle *h, int32_t last_it) {
+  auto &ck = h->ckpt;
+  const int32_t c = last_it / ck.check_it * ck.check_it;
+  if (c <= 0 || h->num_rec <= 0) return AXG_OK;
+  const int32_t s1 = std::min<int32_t>(c / std::max(h->seis_it, 1) + 1, std::min(ck.cap, h->nseismo));
+  if (s1 <= ck.queued) return AXG_OK;
+  if (!h->copy_stream) CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  cudaEvent_t ev;
+  if (ck.free_events.empty()) {
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  } else {
+    ev = ck.free_events.back();
+    ck.free_events.pop_back();
+  }
+  CK(cudaEventRecord(ev, h->stream));
+  CK(cudaStreamWaitEvent(h->copy_stream, ev, 0));
+  const int32_t s0 = ck.queued;
+  CK(cudaMemcpy2DAsync(ck.out + s0, (size_t)ck.cap * sizeof(float), h->rec + s0, (size_t)h->nseismo * sizeof(float),
+                       (size_t)(s1 - s0) * sizeof(float), (size_t)3 * h->num_rec, cudaMemcpyDeviceToHost,
+                       h->copy_stream));
+  CK(cudaEventRecord(ev, h->copy_stream));
+  ck.inflight.emplace_back(ev, s1);
+  ck.queued = s1;
+  return AXG_OK;
+}
+
+// completed checkpoint copies (non-blocking)
+int checkpoint_progress(axg_handle *h) {
+  auto &ck = h->ckpt;
+  while (!ck.inflight.empty()) {
+    const cudaError_t e = cudaEventQuery(ck.inflight.front().first);
+    if (e == cudaErrorNotReady) {
+      cudaGetLastError();
+      break;
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "checkpoint copy");
+    ck.done = ck.inflight.front().second;
+    ck.free_events.push_back(ck.inflight.front().first);
+    ck.inflight.pop_front();
+  }
   return AXG_OK;
 }
 }  // namespace
@@ -1892,9 +1966,15 @@ int axg_run_async(axg_handle *h, int32_t first_iter, int32_t n_iter) {
       int rc = enqueue_dump(h, last_it / dp.strain_it - 1);
       if (rc) return rc;
     }
+    if (h->ckpt.check_it > 0) {
+      int rc = enqueue_checkpoint(h, last_it);
+      if (rc) return rc;
+    }
   }
   if (dp.type)  // the run is complete once its snapshots are in the host buffer
     for (int k = 0; k < 2; ++k) CK(cudaStreamWaitEvent(h->stream, dp.ev_copy[k], 0));
+  if (!h->ckpt.inflight.empty())  // and its checkpoint copies
+    CK(cudaStreamWaitEvent(h->stream, h->ckpt.inflight.back().first, 0));
   CK(cudaEventRecord(h->ev_done, h->stream));
   h->pending = true;
   return AXG_OK;
@@ -1918,7 +1998,33 @@ int axg_wait(axg_handle *h) {
   if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
   CK(cudaStreamSynchronize(h->stream));
   h->pending = false;
-  return check_flags(h);
+  int rc = checkpoint_progress(h);
+  return rc ? rc : check_flags(h);
+}
+
+int axg_set_seismogram_checkpoint(axg_handle *h, int32_t check_it, float *out, int32_t nseismo_cap) {
+  if (!h) return fail(nullptr, AXG_ERR_BAD_ARG, "handle is NULL");
+  if (h->pending) return fail(h, AXG_ERR_BAD_ARG, "the handle has queued steps");
+  if (check_it < 0) return fail(h, AXG_ERR_BAD_ARG, "check_it must be >= 0");
+  if (check_it > 0 && (!out || nseismo_cap < 1)) return fail(h, AXG_ERR_BAD_ARG, "out and nseismo_cap are required");
+  CK(cudaStreamSynchronize(h->stream));
+  if (h->copy_stream) CK(cudaStreamSynchronize(h->copy_stream));
+  int rc = checkpoint_progress(h);
+  if (rc) return rc;
+  auto &ck = h->ckpt;
+  ck.check_it = check_it;
+  ck.out = out;
+  ck.cap = nseismo_cap;
+  ck.queued = ck.done = 0;
+  return AXG_OK;
+}
+
+int axg_seismogram_checkpoint_samples(axg_handle *h, int32_t *n_samples) {
+  if (!h || !n_samples) return fail(h, AXG_ERR_BAD_ARG, "NULL argument");
+  int rc = checkpoint_progress(h);
+  if (rc) return rc;
+  *n_samples = h->ckpt.done;
+  return AXG_OK;
 }
 
 int axg_get_receivers(axg_handle *h, float *out, int32_t cap, int32_t *nseismo_out) {
@@ -2451,6 +2557,31 @@ int axg_set_wavefield_dump(axg_handle *h, const axg_dump_desc *dd) {
   dp.nf = (int)ff.size();
   dp.np = (int64_t)(dd->iend - dd->ibeg + 1) * (dd->jend - dd->jbeg + 1);
   dp.floats = dp.np * ((int64_t)dp.ns * h->nel_s + (int64_t)dp.nf * std::max<int64_t>(h->nel_f, 0));
+  dp.kwf = dd->kwf_mask != nullptr || dd->mapping_ijel_ikwf != nullptr;
+  if (dp.kwf) {
+    // the kernel wavefield point layout: the position each writing element
+    // point has in its field, in the reference's element order
+    if (!dd->kwf_mask || !dd->mapping_ijel_ikwf || dd->npoint_solid_kwf < 0 || dd->npoint_fluid_kwf < 0)
+      return fail(h, AXG_ERR_BAD_ARG, "kwf_mask, mapping_ijel_ikwf and the kwf point counts go together");
+    std::vector<int32_t> ps(es, -1), pf(ef, -1);
+    for (size_t q = 0; q < es + ef; ++q) {
+      if (!dd->kwf_mask[q]) continue;
+      const bool fl = q >= es;
+      const int64_t pos = (int64_t)dd->mapping_ijel_ikwf[q] - 1 - (fl ? dd->npoint_solid_kwf : 0);
+      if (pos < 0 || pos >= (fl ? dd->npoint_fluid_kwf : dd->npoint_solid_kwf))
+        return fail(h, AXG_ERR_BAD_ARG, "mapping_ijel_ikwf entry outside its domain's kwf points");
+      (fl ? pf[q - es] : ps[q]) = (int32_t)pos;
+    }
+    if (!dp.kwf_s && (rc = dalloc(h, &dp.kwf_s, es))) return rc;
+    CK(cudaMemcpyAsync(dp.kwf_s, ps.data(), es * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    if (ef > 0) {
+      if (!dp.kwf_f && (rc = dalloc(h, &dp.kwf_f, ef))) return rc;
+      CK(cudaMemcpyAsync(dp.kwf_f, pf.data(), ef * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    }
+    dp.npt_s = dd->npoint_solid_kwf;
+    dp.npt_f = ef > 0 ? dd->npoint_fluid_kwf : 0;
+    dp.floats = (int64_t)dp.ns * dp.npt_s + (int64_t)dp.nf * dp.npt_f;
+  }
   dp.out = dd->out;
   dp.capacity = dd->capacity;
   dp.names = fs;

@@ -1669,6 +1669,8 @@ struct DumpArgs {
   float *out;              // the domain's first field
   int64_t nel, nglob;
   int32_t type, ibeg, iend, jbeg, jend;
+  const int32_t *kwf;      // kernel wavefield layout: position of each element point (25, nel), -1: none; or null
+  int64_t npt;             // points per field in that layout
 };
 
 struct DumpLane {
@@ -1715,8 +1717,13 @@ __global__ void __launch_bounds__(kThreads) wavefield_dump_kernel(DumpArgs a, Sp
     const bool ax = a.axial[e] != 0;
     const DumpLane w{a.pw[0][q], a.pw[1][q], a.pw[2][q], a.pw[3][q], a.pw[4][q]};
     int fld = 0;
+    const int32_t kpos = a.kwf && active ? a.kwf[q] : -1;
     auto put = [&](float val) {
-      if (mine) a.out[(fld * a.nel + e) * np + pidx] = val;
+      if (a.kwf) {
+        if (kpos >= 0 && AXG_BOUND(kpos, a.npt, 42)) a.out[fld * a.npt + kpos] = val;
+      } else if (mine) {
+        a.out[(fld * a.nel + e) * np + pidx] = val;
+      }
       ++fld;
     };
     constexpr bool nonmono = POLE != POLE_MONO;

@@ -518,9 +518,49 @@ def add_pointwise(m: Mesh, seed: int = 91) -> Mesh:
     return m
 
 
+def kwf_mapping(m: Mesh, ibeg: int = 0, iend: int = 4, jbeg: int = 0, jend: int = 4):
+    """The kernel wavefield point layout of the reference's NetCDF output
+    (SOLVER/meshes_io.F90:543-630) with every element inside the output
+    region: walking the solid elements, then the fluid ones, each over
+    jpol = jbeg..jend, ipol = ibeg..iend plus the axis point ipol = 0 of an
+    axial element, a global point not met before gets the next position and
+    marks that element point in kwf_mask.  Returns (kwf_mask,
+    mapping_ijel_ikwf, npoint_solid_kwf, npoint_fluid_kwf); the arrays are
+    int32 (5, 5, nel_solid + nel_fluid), Fortran order."""
+    nes, nef = m.nel_solid, m.nel_fluid
+    mask = np.zeros((5, 5, nes + nef), dtype=I32, order="F")
+    mapping = np.zeros((5, 5, nes + nef), dtype=I32, order="F")
+    ct = 0
+    counts = []
+    for dom in range(2 if nef > 0 else 1):
+        nel = nes if dom == 0 else nef
+        ig = (m.igloc_solid if dom == 0 else m.igloc_fluid).reshape(nel, 25) - 1
+        axial = np.zeros(nel, dtype=bool)
+        ax = m.ax_el_solid if dom == 0 else m.ax_el_fluid
+        if ax is not None and len(ax):
+            axial[np.asarray(ax) - 1] = True
+        seen = {}
+        off = 0 if dom == 0 else nes
+        for e in range(nel):
+            for j in range(jbeg, jend + 1):
+                pts = list(range(ibeg, iend + 1)) + ([0] if axial[e] and ibeg > 0 else [])
+                for i in pts:
+                    g = int(ig[e, i + 5 * j])
+                    if g not in seen:
+                        ct += 1
+                        seen[g] = ct
+                        mask[i, j, off + e] = 1
+                    mapping[i, j, off + e] = seen[g]
+        counts.append(ct)
+    n_sol = counts[0]
+    return mask, mapping, n_sol, ct - n_sol
+
+
 def dump_desc(m: Mesh, dump_type: int, strain_it: int, out: np.ndarray | None, capacity: int,
-              ibeg: int = 0, iend: int = 4, jbeg: int = 0, jend: int = 4) -> _abi.DumpDesc:
-    """An axg_dump_desc for the mesh's pointwise arrays; keeps them alive."""
+              ibeg: int = 0, iend: int = 4, jbeg: int = 0, jend: int = 4, kwf=None) -> _abi.DumpDesc:
+    """An axg_dump_desc for the mesh's pointwise arrays; keeps them alive.
+    kwf: (kwf_mask, mapping_ijel_ikwf, npoint_solid_kwf, npoint_fluid_kwf)
+    for the kernel wavefield point layout, or None."""
     dd = _abi.DumpDesc()
     dd.dump_type, dd.strain_it = dump_type, strain_it
     dd.ibeg, dd.iend, dd.jbeg, dd.jend = ibeg, iend, jbeg, jend
@@ -533,5 +573,11 @@ def dump_desc(m: Mesh, dump_type: int, strain_it: int, out: np.ndarray | None, c
         setattr(dd, nm, _abi.ptr(a, C.c_float))
     dd.out = _abi.ptr(out, C.c_float)
     dd.capacity = capacity
+    if kwf is not None:
+        kmask, kmap = np.asfortranarray(kwf[0], dtype=I32), np.asfortranarray(kwf[1], dtype=I32)
+        keep += [kmask, kmap]
+        dd.kwf_mask = _abi.ptr(kmask, C.c_int32)
+        dd.mapping_ijel_ikwf = _abi.ptr(kmap, C.c_int32)
+        dd.npoint_solid_kwf, dd.npoint_fluid_kwf = int(kwf[2]), int(kwf[3])
     dd._keep = keep  # type: ignore[attr-defined]
     return dd

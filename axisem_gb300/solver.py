@@ -31,6 +31,8 @@ def _check(lib, h, rc):
 
 
 def _fp(a):
+    if a is None:
+        return C.cast(None, C.POINTER(C.c_float))
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
@@ -178,14 +180,14 @@ class Solver:
         _check(self.lib, self.h, self.lib.axg_set_compensated(self.h, int(bool(on))))
 
     def set_wavefield_dump(self, dump_type: int, strain_it: int = 1, capacity: int = 1, ibeg: int = 0,
-                           iend: int = 4, jbeg: int = 0, jend: int = 4, out: np.ndarray | None = None):
+                           iend: int = 4, jbeg: int = 0, jend: int = 4, out: np.ndarray | None = None, kwf=None):
         """axg_set_wavefield_dump with the mesh's data_pointwise arrays
         (mesh.add_pointwise).  Returns the snapshot buffer, (capacity,
         floats_per_snapshot) float32 (`out` if given: page-locked memory lets
         the copies overlap the steps)."""
         from .mesh import dump_desc
         probe = np.zeros(1, dtype=np.float32)
-        dd = dump_desc(self.mesh, dump_type, strain_it, probe, 1, ibeg, iend, jbeg, jend)
+        dd = dump_desc(self.mesh, dump_type, strain_it, probe, 1, ibeg, iend, jbeg, jend, kwf)
         _check(self.lib, self.h, self.lib.axg_set_wavefield_dump(self.h, C.byref(dd)))
         if dump_type == _abi.DUMP_NONE:
             self._dump = None
@@ -195,7 +197,7 @@ class Solver:
             out = np.zeros((capacity, floats), dtype=np.float32)
         if out.dtype != np.float32 or not out.flags.c_contiguous or out.size < capacity * floats:
             raise ValueError(f"out must be C-contiguous float32 with room for {capacity} x {floats}")
-        dd = dump_desc(self.mesh, dump_type, strain_it, out, capacity, ibeg, iend, jbeg, jend)
+        dd = dump_desc(self.mesh, dump_type, strain_it, out, capacity, ibeg, iend, jbeg, jend, kwf)
         _check(self.lib, self.h, self.lib.axg_set_wavefield_dump(self.h, C.byref(dd)))
         self._dump = (out, dd)
         return out
@@ -208,6 +210,21 @@ class Solver:
                                                                     names, len(names)))
         nm = names.value.decode()
         return ns.value, nf.value, fl.value, nm.split(",") if nm else []
+
+    def set_seismogram_checkpoint(self, check_it: int, out: np.ndarray | None = None):
+        """Checkpoint the seismograms into `out` (nseismo_cap, 3, num_rec),
+        F-ordered float32, every check_it steps (0: off); the array must stay
+        alive while runs use it."""
+        if check_it and out is not None:
+            assert out.dtype == np.float32 and out.flags["F_CONTIGUOUS"] and out.shape[1:] == (3, self.mesh.num_rec)
+        self._ckpt = out
+        cap = 0 if out is None else out.shape[0]
+        _check(self.lib, self.h, self.lib.axg_set_seismogram_checkpoint(self.h, check_it, _fp(out), cap))
+
+    def checkpoint_samples(self) -> int:
+        n = C.c_int32(0)
+        _check(self.lib, self.h, self.lib.axg_seismogram_checkpoint_samples(self.h, C.byref(n)))
+        return n.value
 
     def autotune(self) -> int:
         """axg_autotune: the measured steps per CUDA graph (the solve's state

@@ -417,9 +417,10 @@ int axg_plan_check(const axg_mesh_desc *desc, int32_t patch_elems, int32_t growt
  *                                   _p, _z as stored; chi_flu, dchi_flu
  *   FULLFIELDS   compute_strain + dump_velo_global: the strain terms, then
  *                                   velo_sol_s, _p, _z; velo_flu_s, _p (zero), _z
- * The values of compute_strain's fields are the reference's, the kernel
- * wavefield point mapping of its NetCDF 'displ_only' / 'strain_only' output
- * (kwf_mapping_*) is left to the caller.  `out` should be page-locked host
+ * The values of compute_strain's fields are the reference's; with kwf_mask
+ * and mapping_ijel_ikwf the fields come in the kernel wavefield point layout
+ * of its NetCDF 'displ_only' / 'strain_only' output (kwf_mapping_*) instead
+ * of the packed one.  `out` should be page-locked host
  * memory (cudaHostAlloc / cudaHostRegister) for the copies to overlap the
  * steps.  A dumping solve runs alone (not in a batch). */
 enum axg_dump_type {
@@ -441,6 +442,17 @@ typedef struct axg_dump_desc {
   const float *inv_s_fluid, *inv_rho_fluid;
   float *out;                        /* capacity snapshots of floats_per_snapshot floats */
   int64_t capacity;
+  /* Optional (NULL: the packed layout above): the kernel wavefield point
+   * layout of the NetCDF 'displ_only' / 'strain_only' output
+   * (kwf_mapping_sol / kwf_mapping_flu, SOLVER/wavefields_io.f90:743-780,
+   * built in SOLVER/meshes_io.F90:543-630).  Both are (0:4,0:4,nel_solid +
+   * nel_fluid), the fluid's elements after the solid's; kwf_mask nonzero marks
+   * the one element point that writes each output point, mapping_ijel_ikwf
+   * its 1-based position (fluid positions after npoint_solid_kwf).  Each field
+   * then holds npoint_solid_kwf (solid) or npoint_fluid_kwf (fluid) values. */
+  const int32_t *kwf_mask;
+  const int32_t *mapping_ijel_ikwf;
+  int32_t npoint_solid_kwf, npoint_fluid_kwf;
 } axg_dump_desc;
 
 int axg_set_wavefield_dump(axg_handle *h, const axg_dump_desc *dd);
@@ -448,6 +460,20 @@ int axg_set_wavefield_dump(axg_handle *h, const axg_dump_desc *dd);
  * terminated, truncated to names_cap bytes; names may be NULL). */
 int axg_wavefield_dump_layout(axg_handle *h, int32_t *n_solid_fields, int32_t *n_fluid_fields,
                               int64_t *floats_per_snapshot, char *names, int32_t names_cap);
+
+/* Seismogram checkpoints (the reference's check_it = niter / 20,
+ * SOLVER/parameters.F90:932, flushing the receivers at
+ * SOLVER/time_evol_wave.F90:1142-1146 through nc_rec_checkpoint,
+ * SOLVER/nc_routines.F90:588): during every later run, after the steps up to
+ * each multiple of check_it the seismogram samples recorded so far (sample 0
+ * is iteration 0, then one every seis_it steps) are copied into `out`, in the
+ * layout of axg_get_receivers with first extent nseismo_cap, on a copy stream
+ * while the following steps run.  check_it 0 switches the checkpoints off.
+ * `out` should be page-locked host memory (cudaHostAlloc / cudaHostRegister)
+ * for the copies to overlap the steps.  axg_reset restarts them. */
+int axg_set_seismogram_checkpoint(axg_handle *h, int32_t check_it, float *out, int32_t nseismo_cap);
+/* Samples (from sample 0) whose checkpoint copies have completed. */
+int axg_seismogram_checkpoint_samples(axg_handle *h, int32_t *n_samples);
 
 /* Event-timed repeat of axg_stiffness_assembled_device: n launches, returns the
  * average device time in ms of one stiffness+assembly (all colour launches). */

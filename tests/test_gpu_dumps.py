@@ -116,3 +116,45 @@ def test_dump_errors(gpu_lib):
     with Solver(bare) as s:
         with pytest.raises(AxgError):
             s.set_wavefield_dump(_abi.DUMP_STRAIN_ONLY, 1, capacity=4)
+
+
+@pytest.mark.parametrize("pole", [0, 2])
+@pytest.mark.parametrize("dtype_", [_abi.DUMP_DISPL_ONLY, _abi.DUMP_STRAIN_ONLY])
+def test_dump_kernel_wavefield_layout(gpu_lib, pole, dtype_):
+    """With kwf_mask / mapping_ijel_ikwf the snapshots come in the point
+    layout of the reference's NetCDF kernel wavefields (kwf_mapping_sol /
+    _flu, SOLVER/wavefields_io.f90:743-780): every kwf point holds the value
+    its marking element point has in the packed dump (bit for bit: the same
+    kernel computes both), here for the inner points 1..3 plus the axis."""
+    from axisem_gb300.mesh import kwf_mapping
+    m = _mesh(pole)
+    strain_it = 4
+    cap = m.niter // strain_it
+    kmask, kmap, nps, npf = kwf = kwf_mapping(m, 1, 3, 1, 3)
+    with Solver(m) as s:
+        packed = s.set_wavefield_dump(dtype_, strain_it, capacity=cap).copy() * 0
+        packed = s.set_wavefield_dump(dtype_, strain_it, capacity=cap, out=packed)
+        s.run()
+        ns, nf, _, names = s.dump_layout()
+    with Solver(m) as s:
+        kw = s.set_wavefield_dump(dtype_, strain_it, capacity=cap, kwf=kwf)
+        assert s.dump_layout()[2] == ns * nps + nf * npf
+        s.run()
+    nes, nef = m.nel_solid, m.nel_fluid
+    for k in range(cap):
+        for q in range(ns + nf):
+            fluid = q >= ns
+            nel = nef if fluid else nes
+            off = (ns * nes + (q - ns) * nef) * 25 if fluid else q * nes * 25
+            field = packed[k, off: off + nel * 25].reshape(nel, 25)      # [e, i + 5 j]
+            koff = ns * nps + (q - ns) * npf if fluid else q * nps
+            npt = npf if fluid else nps
+            got = kw[k, koff: koff + npt]
+            want = np.zeros(npt, np.float32)
+            e0 = nes if fluid else 0
+            for e in range(nel):
+                for j in range(5):
+                    for i in range(5):
+                        if kmask[i, j, e0 + e]:
+                            want[kmap[i, j, e0 + e] - 1 - (nps if fluid else 0)] = field[e, i + 5 * j]
+            assert np.array_equal(got, want), (k, names[q])
