@@ -115,6 +115,7 @@ struct axg_handle {
   int64_t dev_bytes = 0;
   DomainDev ds, df;
   float *su[3] = {}, *sv[3] = {}, *sa[3] = {}, *sf[3] = {};
+  float *sup[3] = {};  // the plain Newmark step's predicted displacement (kept by the last writers)
   float *fu = nullptr, *fv = nullptr, *fa = nullptr, *ff = nullptr;
   float *inv_mass_s = nullptr, *inv_mass_f = nullptr, *gamma_s = nullptr, *gamma_f = nullptr;
   // FP64 inverse masses (mesh) and source values (solve), when the descriptor had them
@@ -528,6 +529,10 @@ CouplingHost make_coupling(std::vector<std::tuple<int32_t, int32_t, float, float
   return c;
 }
 
+// the plain Newmark step: its gather reads the predicted displacement the
+// previous step's last writers stored
+bool lookahead(const axg_handle *h) { return h->scheme == AXG_SCHEME_NEWMARK2 && !h->kahan; }
+
 StateArgs solid_state(axg_handle *h) {
   StateArgs s{};
   for (int c = 0; c < 3; ++c) {
@@ -539,6 +544,7 @@ StateArgs solid_state(axg_handle *h) {
   for (int c = 0; c < 3; ++c) {
     s.cu[c] = h->kahan ? h->cu_s[c] : nullptr;
     s.cv[c] = h->kahan ? h->cv_s[c] : nullptr;
+    s.up[c] = lookahead(h) ? h->sup[c] : nullptr;
   }
   s.inv_mass = h->inv_mass_s;
   s.inv_mass_dp = h->kahan ? h->inv_mass_s_dp : nullptr;
@@ -562,7 +568,7 @@ StateArgs solid_state(axg_handle *h) {
 
 StateArgs fluid_state(axg_handle *h) {
   StateArgs s = solid_state(h);
-  for (int c = 0; c < 3; ++c) s.u[c] = s.v[c] = s.a[c] = s.f[c] = s.cu[c] = s.cv[c] = nullptr;
+  for (int c = 0; c < 3; ++c) s.u[c] = s.v[c] = s.a[c] = s.f[c] = s.cu[c] = s.cv[c] = s.up[c] = nullptr;
   s.cu[0] = h->kahan ? h->cu_f : nullptr;
   s.cv[0] = h->kahan ? h->cv_f : nullptr;
   s.u[0] = h->fu;
@@ -575,6 +581,16 @@ StateArgs fluid_state(axg_handle *h) {
   s.src.n = 0;
   s.nglob = h->nglob_f;
   return s;
+}
+
+// Before a run of the plain Newmark step: the predicted displacement of the
+// current state (it may have been set, reset, restored or advanced by
+// another scheme or mode since the last run).  The last writers keep it from
+// there on; recomputing it is exact, so runs in pieces match one run.
+cudaError_t refresh_predicted(axg_handle *h, cudaStream_t s) {
+  if (!lookahead(h) || h->nglob_s <= 0) return cudaSuccess;
+  predict_kernel<<<(unsigned)((h->nglob_s + 255) / 256), 256, 0, s>>>(solid_state(h));
+  return cudaGetLastError();
 }
 
 RecWork rec_work(axg_handle *h, const StateArgs &ss) {
@@ -602,7 +618,7 @@ template <int POLE, int MODE, bool ANEL, bool KAHAN = false>
 constexpr int solid_smem_bytes() {
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;
   return SolidSmem<NC, solid_block_stride(n_terms(POLE)), solid_stages(ANEL), ANEL ? kAnelSlot : 0,
-                   solid_buffers(MODE), solid_row(MODE, ANEL, KAHAN), KAHAN>::bytes;
+                   solid_buffers(MODE, ANEL, KAHAN), solid_row(MODE, ANEL, KAHAN), KAHAN>::bytes;
 }
 
 // sets the kernel's shared-memory attributes; *ctas = resident CTAs on the GPU
@@ -662,7 +678,9 @@ int prepare_fluid_kernels(axg_handle *h) {
       (rc = prepare_fluid_fn<NONMONO, false, true, One<PatchWork>>(h)) ||
       (rc = prepare_fluid_fn<NONMONO, true, true, One<PatchWork>>(h)) ||
       (rc = prepare_fluid_fn<NONMONO, false, false, Many<PatchWork>>(h)) ||
-      (rc = prepare_fluid_fn<NONMONO, true, false, Many<PatchWork>>(h)))
+      (rc = prepare_fluid_fn<NONMONO, true, false, Many<PatchWork>>(h)) ||
+      (rc = prepare_fluid_fn<NONMONO, false, true, Many<PatchWork>>(h)) ||
+      (rc = prepare_fluid_fn<NONMONO, true, true, Many<PatchWork>>(h)))
     return rc;
   return AXG_OK;
 }
@@ -794,13 +812,41 @@ void launch_solid_symplectic(axg_handle *h, cudaStream_t s, const StateArgs &st)
   }
 }
 
+// the solid and fluid state of stage i of a symplectic step
+void symplectic_stage_states(axg_handle *h, int i, StateArgs &ss, StateArgs &fs) {
+  ss = solid_state(h);
+  fs = fluid_state(h);
+  ss.dt = fs.dt = h->sym_cd[i];
+  ss.hdt2 = fs.hdt2 = 0.f;  // the coupling's predictor is then the drift u + coefd(i) v
+  ss.kick = fs.kick = h->sym_cv[i];
+  ss.stf = h->stf_stages + (int64_t)i * std::max(h->niter, 1);
+}
+
+// the final drift of a symplectic step: one thread per point of the larger domain
+DriftWork drift_work(axg_handle *h) {
+  return DriftWork{solid_state(h), fluid_state(h), h->sym_cd[h->nstages]};
+}
+int32_t drift_points(const axg_handle *h) {
+  return (int32_t)std::max(h->nglob_s, h->nel_f > 0 ? h->nglob_f : 0);
+}
+
+template <int POLE>
+void launch_anel_memvar(axg_handle *h, cudaStream_t s) {
+  const unsigned g = (unsigned)std::min<int64_t>((h->nel_s + kWarps - 1) / kWarps, 16 * (int64_t)h->num_sms);
+  anel_memvar_kernel<POLE><<<g, kThreads, 0, s>>>(h->an, h->sym_gidx, h->sym_axial, solid_state(h), h->nel_s,
+                                                  h->spec);
+}
+// the memory variables from the drifted displacement, once per symplectic step
+void launch_anel_memvar_pole(axg_handle *h, cudaStream_t s) {
+  if (h->pole == AXG_MONOPOLE) launch_anel_memvar<POLE_MONO>(h, s);
+  else if (h->pole == AXG_DIPOLE) launch_anel_memvar<POLE_DI>(h, s);
+  else launch_anel_memvar<POLE_QUAD>(h, s);
+}
+
 void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
   for (int i = 0; i < h->nstages; ++i) {
-    StateArgs ss = solid_state(h), fs = fluid_state(h);
-    ss.dt = fs.dt = h->sym_cd[i];
-    ss.hdt2 = fs.hdt2 = 0.f;  // the coupling's predictor is then the drift u + coefd(i) v
-    ss.kick = fs.kick = h->sym_cv[i];
-    ss.stf = h->stf_stages + (int64_t)i * std::max(h->niter, 1);
+    StateArgs ss, fs;
+    symplectic_stage_states(h, i, ss, fs);
     if (h->nel_f > 0) {
       if (h->to_fluid.n > 0) {
         const int nb = (h->to_fluid.n + 255) / 256;
@@ -834,19 +880,10 @@ void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
     else if (h->pole == AXG_DIPOLE) launch_solid_symplectic<POLE_DI>(h, s, ss);
     else launch_solid_symplectic<POLE_QUAD>(h, s, ss);
   }
-  StateArgs ss = solid_state(h), fs = fluid_state(h);
-  const int64_t n = std::max(h->nglob_s, h->nel_f > 0 ? h->nglob_f : 0);
-  drift_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(ss, fs, h->sym_cd[h->nstages]);
-  if (h->anel) {  // the memory variables from the drifted displacement
-    const unsigned g = (unsigned)std::min<int64_t>((h->nel_s + kWarps - 1) / kWarps, 16 * (int64_t)h->num_sms);
-    if (h->pole == AXG_MONOPOLE)
-      anel_memvar_kernel<POLE_MONO><<<g, kThreads, 0, s>>>(h->an, h->sym_gidx, h->sym_axial, ss, h->nel_s, h->spec);
-    else if (h->pole == AXG_DIPOLE)
-      anel_memvar_kernel<POLE_DI><<<g, kThreads, 0, s>>>(h->an, h->sym_gidx, h->sym_axial, ss, h->nel_s, h->spec);
-    else
-      anel_memvar_kernel<POLE_QUAD><<<g, kThreads, 0, s>>>(h->an, h->sym_gidx, h->sym_axial, ss, h->nel_s, h->spec);
-  }
-  receivers_kernel<<<1, 256, 0, s>>>(One<RecWork>{rec_work(h, ss), 1});
+  const int32_t n = drift_points(h);
+  drift_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(One<DriftWork>{drift_work(h), n});
+  if (h->anel) launch_anel_memvar_pole(h, s);
+  receivers_kernel<<<1, 256, 0, s>>>(One<RecWork>{rec_work(h, solid_state(h)), 1});
 }
 
 // a CUDA graph of nsteps steps into *exec (replacing what it held)
@@ -1308,7 +1345,8 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
   for (int c = 0; c < 3; ++c) {
     if (mono && c == 1) continue;
     if ((rc = dalloc(h, &h->su[c], h->nglob_s)) || (rc = dalloc(h, &h->sv[c], h->nglob_s)) ||
-        (rc = dalloc(h, &h->sa[c], h->nglob_s)) || (rc = dalloc(h, &h->sf[c], h->nglob_s)))
+        (rc = dalloc(h, &h->sa[c], h->nglob_s)) || (rc = dalloc(h, &h->sf[c], h->nglob_s)) ||
+        (rc = dalloc(h, &h->sup[c], h->nglob_s)))
       return rc;
   }
   if (h->nel_f > 0) {
@@ -1683,6 +1721,7 @@ int axg_run(axg_handle *h, int32_t first_iter, int32_t n_iter) {
     return rc ? rc : axg_wait(h);
   }
   CK(cudaMemcpyAsync(h->iter, &first_iter, sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  CK(refresh_predicted(h, h->stream));
   int32_t done = 0;
   while (done < n_iter) {
     const int k = std::min<int32_t>(h->steps_per_graph, n_iter - done);
@@ -1939,6 +1978,7 @@ int axg_run_async(axg_handle *h, int32_t first_iter, int32_t n_iter) {
   // the kernels of a step after a blow-up return at once, so all steps can
   // be queued without a check in between
   CK(cudaMemcpyAsync(h->iter, &first_iter, sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+  CK(refresh_predicted(h, h->stream));
   for (int32_t done = 0; done < n_iter;) {
     const int32_t it = first_iter + done;
     int k = std::min<int32_t>(h->steps_per_graph, n_iter - done);
@@ -2193,6 +2233,7 @@ int axg_autotune(axg_handle *h, int32_t *chosen) {
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(save + off, p.first, p.second, cudaMemcpyDeviceToDevice, h->stream);
     off += (p.second + 255) / 256 * 256;
   }
+  if (ce == cudaSuccess) ce = refresh_predicted(h, h->stream);
   int best = h->steps_per_graph, rc = ce == cudaSuccess ? AXG_OK : cuda_fail(h, ce, "axg_autotune: saving the state");
   float best_ms = 0.f;
   for (int k = 2; k <= 64 && rc == AXG_OK; k *= 2) {
@@ -2621,7 +2662,8 @@ struct axg_batch {
   std::vector<axg_handle *> hs;
   int device = 0, num_sms = 1;
   SpecDev spec{};
-  int solid_ctas[3][2] = {};  // resident CTAs of the batched Newmark kernel per (pole, compensated)
+  // resident CTAs of the batched solid kernels per (symplectic, pole, compensated, attenuated)
+  int solid_ctas[2][3][2][2] = {};
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev_done = nullptr;
@@ -2670,87 +2712,178 @@ int64_t for_batches(const std::vector<axg_handle *> &hs, ItemsFn items, WorkFn w
   return nl;
 }
 
+// A batched launch covers the solves taking part in one phase: the Newmark
+// step (stage < 0) or stage `stage` of a symplectic step.
+bool in_stage(const axg_handle *h, int stage) {
+  return stage < 0 ? h->scheme == AXG_SCHEME_NEWMARK2 : h->scheme != AXG_SCHEME_NEWMARK2 && stage < h->nstages;
+}
+// the solve's solid and fluid state in that phase
+void stage_states(axg_handle *h, int stage, StateArgs &ss, StateArgs &fs) {
+  if (stage < 0) {
+    ss = solid_state(h);
+    fs = fluid_state(h);
+  } else {
+    symplectic_stage_states(h, stage, ss, fs);
+  }
+}
+
 template <int NONMONO, bool KAHAN>
-int64_t batch_fluid_colour(axg_batch *b, int c, cudaStream_t s) {
+int64_t batch_fluid_colour(axg_batch *b, int stage, int c, cudaStream_t s) {
   return for_batches<PatchWork>(
       b->hs,
       [&](axg_handle *h) {
-        const bool mine = h->nel_f > 0 && c < h->pf.n_colours && (h->pole != AXG_MONOPOLE) == (NONMONO != 0) &&
-                          h->kahan == KAHAN;
+        const bool mine = in_stage(h, stage) && h->nel_f > 0 && c < h->pf.n_colours &&
+                          (h->pole != AXG_MONOPOLE) == (NONMONO != 0) && h->kahan == KAHAN;
         return mine ? h->pf.colour_start[c + 1] - h->pf.colour_start[c] : 0;
       },
       [&](axg_handle *h) {
         DomainArgs a = domain_args(h->df, h->pf);
         a.patch_begin = h->pf.colour_start[c];
-        return PatchWork{a, fluid_state(h)};
+        if (stage >= 0) a.fsmask = nullptr;  // symplectic_time_loop applies no free-surface mask
+        StateArgs ss, fs;
+        stage_states(h, stage, ss, fs);
+        return PatchWork{a, fs};
       },
       [&](const Many<PatchWork> &m) {
-        fluid_patch_kernel<NONMONO, KAHAN, false, Many<PatchWork>>
-            <<<m.start[m.n], kThreads, FluidSmem<NONMONO, KAHAN>::bytes, s>>>(m, b->spec);
+        if (stage < 0)
+          fluid_patch_kernel<NONMONO, KAHAN, false, Many<PatchWork>>
+              <<<m.start[m.n], kThreads, FluidSmem<NONMONO, KAHAN>::bytes, s>>>(m, b->spec);
+        else
+          fluid_patch_kernel<NONMONO, KAHAN, true, Many<PatchWork>>
+              <<<m.start[m.n], kThreads, FluidSmem<NONMONO, KAHAN>::bytes, s>>>(m, b->spec);
       });
 }
 
-template <int POLE, bool KAHAN>
-int64_t batch_solid_colour(axg_batch *b, int c, cudaStream_t s) {
+// a solve's colour work with its attenuation data (attenuated batches)
+struct AnelPatchWork {
+  PatchWork pw;
+  AnelArgs an;
+};
+
+template <int POLE, int MODE, bool KAHAN, bool ANEL>
+int64_t batch_solid_colour(axg_batch *b, int stage, int c, cudaStream_t s) {
   const int pole = POLE == POLE_MONO ? AXG_MONOPOLE : POLE == POLE_DI ? AXG_DIPOLE : AXG_QUADPOLE;
-  return for_batches<PatchWork>(
+  return for_batches<AnelPatchWork>(
       b->hs,
       [&](axg_handle *h) {
-        const bool mine = c < h->ps.n_colours && h->pole == pole && h->kahan == KAHAN;
+        const bool mine = in_stage(h, stage) && c < h->ps.n_colours && h->pole == pole && h->kahan == KAHAN &&
+                          h->anel == ANEL;
         return mine ? h->ps.colour_start[c + 1] - h->ps.colour_start[c] : 0;
       },
       [&](axg_handle *h) {
         DomainArgs a = domain_args(h->ds, h->ps);
         a.patch_begin = h->ps.colour_start[c];
-        return PatchWork{a, solid_state(h)};
+        StateArgs ss, fs;
+        stage_states(h, stage, ss, fs);
+        return AnelPatchWork{PatchWork{a, ss}, h->an};
       },
-      [&](const Many<PatchWork> &m) {
-        const int grid = std::min(m.start[m.n], b->solid_ctas[POLE][KAHAN]);
-        solid_batch_kernel<POLE, KAHAN>
-            <<<grid, kThreads, solid_smem_bytes<POLE, MODE_NEWMARK, false, KAHAN>(), s>>>(m, b->spec);
+      [&](const Many<AnelPatchWork> &mw) {
+        Many<PatchWork> m{};
+        m.n = mw.n;
+        std::memcpy(m.start, mw.start, sizeof(m.start));
+        for (int q = 0; q < mw.n; ++q) m.w[q] = mw.w[q].pw;
+        const int grid = std::min(m.start[m.n], b->solid_ctas[MODE == MODE_SYMPLECTIC][POLE][KAHAN][ANEL]);
+        constexpr int smem = solid_smem_bytes<POLE, MODE, ANEL, KAHAN>();
+        if constexpr (ANEL) {
+          AnelBatch an{};
+          for (int q = 0; q < mw.n; ++q) an.a[q] = mw.w[q].an;
+          solid_anel_batch_kernel<POLE, MODE, KAHAN><<<grid, kThreads, smem, s>>>(m, b->spec, an);
+        } else {
+          solid_batch_kernel<POLE, MODE, KAHAN><<<grid, kThreads, smem, s>>>(m, b->spec);
+        }
       });
 }
 
+// colour c of the solid, every pole and precision mode, plain and attenuated
+template <int MODE>
+int64_t batch_solid_colours(axg_batch *b, int stage, int c, cudaStream_t s) {
+  return batch_solid_colour<POLE_MONO, MODE, false, false>(b, stage, c, s) +
+         batch_solid_colour<POLE_MONO, MODE, true, false>(b, stage, c, s) +
+         batch_solid_colour<POLE_DI, MODE, false, false>(b, stage, c, s) +
+         batch_solid_colour<POLE_DI, MODE, true, false>(b, stage, c, s) +
+         batch_solid_colour<POLE_QUAD, MODE, false, false>(b, stage, c, s) +
+         batch_solid_colour<POLE_QUAD, MODE, true, false>(b, stage, c, s) +
+         batch_solid_colour<POLE_MONO, MODE, false, true>(b, stage, c, s) +
+         batch_solid_colour<POLE_MONO, MODE, true, true>(b, stage, c, s) +
+         batch_solid_colour<POLE_DI, MODE, false, true>(b, stage, c, s) +
+         batch_solid_colour<POLE_DI, MODE, true, true>(b, stage, c, s) +
+         batch_solid_colour<POLE_QUAD, MODE, false, true>(b, stage, c, s) +
+         batch_solid_colour<POLE_QUAD, MODE, true, true>(b, stage, c, s);
+}
+
 template <int POLE>
-int64_t batch_to_solid(axg_batch *b, cudaStream_t s) {
+int64_t batch_to_solid(axg_batch *b, int stage, cudaStream_t s) {
   const int pole = POLE == POLE_MONO ? AXG_MONOPOLE : POLE == POLE_DI ? AXG_DIPOLE : AXG_QUADPOLE;
   return for_batches<ToSolidWork>(
-      b->hs, [&](axg_handle *h) { return h->nel_f > 0 && h->pole == pole ? h->to_solid.n : 0; },
-      [&](axg_handle *h) { return ToSolidWork{h->to_solid, fluid_state(h), solid_state(h)}; },
+      b->hs,
+      [&](axg_handle *h) { return in_stage(h, stage) && h->nel_f > 0 && h->pole == pole ? h->to_solid.n : 0; },
+      [&](axg_handle *h) {
+        StateArgs ss, fs;
+        stage_states(h, stage, ss, fs);
+        return ToSolidWork{h->to_solid, fs, ss};
+      },
       [&](const Many<ToSolidWork> &m) {
         couple_to_solid_kernel<POLE, Many<ToSolidWork>><<<(m.start[m.n] + 255) / 256, 256, 0, s>>>(m);
       });
 }
 
 template <int DIPOLE>
-int64_t batch_to_fluid(axg_batch *b, cudaStream_t s) {
+int64_t batch_to_fluid(axg_batch *b, int stage, cudaStream_t s) {
   return for_batches<ToFluidWork>(
       b->hs,
-      [&](axg_handle *h) { return h->nel_f > 0 && (h->pole == AXG_DIPOLE) == (DIPOLE != 0) ? h->to_fluid.n : 0; },
-      [&](axg_handle *h) { return ToFluidWork{h->to_fluid, solid_state(h), h->ff}; },
+      [&](axg_handle *h) {
+        return in_stage(h, stage) && h->nel_f > 0 && (h->pole == AXG_DIPOLE) == (DIPOLE != 0) ? h->to_fluid.n : 0;
+      },
+      [&](axg_handle *h) {
+        StateArgs ss, fs;
+        stage_states(h, stage, ss, fs);
+        return ToFluidWork{h->to_fluid, ss, h->ff};
+      },
       [&](const Many<ToFluidWork> &m) {
         couple_to_fluid_kernel<DIPOLE, Many<ToFluidWork>><<<(m.start[m.n] + 255) / 256, 256, 0, s>>>(m);
       });
 }
 
-// One Newmark step of every solve, in the order of enqueue_step: coupling
-// into the fluid, fluid colours, coupling into the solid, solid colours,
-// seismograms and step counters.
-int64_t enqueue_batch_step(axg_batch *b, cudaStream_t s) {
-  int64_t nl = batch_to_fluid<0>(b, s) + batch_to_fluid<1>(b, s);
+// One phase of the solves taking part in it, in the order of enqueue_step
+// (enqueue_step_symplectic for a stage): coupling into the fluid, fluid
+// colours, coupling into the solid, solid colours.
+template <int MODE>
+int64_t enqueue_batch_phase(axg_batch *b, int stage, cudaStream_t s) {
+  int64_t nl = batch_to_fluid<0>(b, stage, s) + batch_to_fluid<1>(b, stage, s);
   int fc = 0, sc = 0;
   for (axg_handle *h : b->hs) {
+    if (!in_stage(h, stage)) continue;
     if (h->nel_f > 0) fc = std::max(fc, h->pf.n_colours);
     sc = std::max(sc, h->ps.n_colours);
   }
   for (int c = 0; c < fc; ++c)
-    nl += batch_fluid_colour<0, false>(b, c, s) + batch_fluid_colour<0, true>(b, c, s) +
-          batch_fluid_colour<1, false>(b, c, s) + batch_fluid_colour<1, true>(b, c, s);
-  nl += batch_to_solid<POLE_MONO>(b, s) + batch_to_solid<POLE_DI>(b, s) + batch_to_solid<POLE_QUAD>(b, s);
-  for (int c = 0; c < sc; ++c)
-    nl += batch_solid_colour<POLE_MONO, false>(b, c, s) + batch_solid_colour<POLE_MONO, true>(b, c, s) +
-          batch_solid_colour<POLE_DI, false>(b, c, s) + batch_solid_colour<POLE_DI, true>(b, c, s) +
-          batch_solid_colour<POLE_QUAD, false>(b, c, s) + batch_solid_colour<POLE_QUAD, true>(b, c, s);
+    nl += batch_fluid_colour<0, false>(b, stage, c, s) + batch_fluid_colour<0, true>(b, stage, c, s) +
+          batch_fluid_colour<1, false>(b, stage, c, s) + batch_fluid_colour<1, true>(b, stage, c, s);
+  nl += batch_to_solid<POLE_MONO>(b, stage, s) + batch_to_solid<POLE_DI>(b, stage, s) +
+        batch_to_solid<POLE_QUAD>(b, stage, s);
+  for (int c = 0; c < sc; ++c) nl += batch_solid_colours<MODE>(b, stage, c, s);
+  return nl;
+}
+
+// One step of every solve: the Newmark solves' step, the symplectic solves'
+// stages (stage i of every solve with more than i stages in one phase), their
+// final drifts and memory variables, then the seismograms and step counters.
+int64_t enqueue_batch_step(axg_batch *b, cudaStream_t s) {
+  int64_t nl = enqueue_batch_phase<MODE_NEWMARK>(b, -1, s);
+  int ns = 0;
+  for (axg_handle *h : b->hs) ns = std::max(ns, h->scheme != AXG_SCHEME_NEWMARK2 ? h->nstages : 0);
+  for (int i = 0; i < ns; ++i) nl += enqueue_batch_phase<MODE_SYMPLECTIC>(b, i, s);
+  if (ns > 0) {
+    nl += for_batches<DriftWork>(
+        b->hs, [](axg_handle *h) { return h->scheme != AXG_SCHEME_NEWMARK2 ? drift_points(h) : 0; },
+        [](axg_handle *h) { return drift_work(h); },
+        [&](const Many<DriftWork> &m) { drift_kernel<Many<DriftWork>><<<(m.start[m.n] + 255) / 256, 256, 0, s>>>(m); });
+    for (axg_handle *h : b->hs)
+      if (h->scheme != AXG_SCHEME_NEWMARK2 && h->anel) {
+        launch_anel_memvar_pole(h, s);
+        ++nl;
+      }
+  }
   nl += for_batches<RecWork>(
       b->hs, [](axg_handle *) { return 1; }, [](axg_handle *h) { return rec_work(h, solid_state(h)); },
       [&](const Many<RecWork> &m) { receivers_kernel<Many<RecWork>><<<m.n, 256, 0, s>>>(m); });
@@ -2758,7 +2891,8 @@ int64_t enqueue_batch_step(axg_batch *b, cudaStream_t s) {
 }
 
 // kernel parameters are limited to 32764 bytes
-static_assert(sizeof(Many<PatchWork>) <= 32000 && sizeof(Many<ToSolidWork>) <= 32000 &&
+static_assert(sizeof(Many<PatchWork>) + sizeof(SpecDev) + sizeof(AnelBatch) <= 32000 &&
+                  sizeof(Many<ToSolidWork>) <= 32000 && sizeof(Many<DriftWork>) <= 32000 &&
                   sizeof(Many<ToFluidWork>) <= 32000 && sizeof(Many<RecWork>) <= 32000,
               "a batched launch's descriptors must fit the kernel parameter space");
 
@@ -2772,12 +2906,30 @@ __global__ void set_iters_kernel(const __grid_constant__ IterSet a) {
   if ((int)threadIdx.x < a.n) *a.ctr[threadIdx.x] = a.first[threadIdx.x];
 }
 
-template <int POLE, bool KAHAN>
+template <int POLE, int MODE, bool KAHAN, bool ANEL>
 int prepare_batch_kernel(axg_batch *b, axg_handle *h) {
-  int rc = prepare_kernel_fn(h, solid_batch_kernel<POLE, KAHAN>, solid_smem_bytes<POLE, MODE_NEWMARK, false, KAHAN>(),
-                             &b->solid_ctas[POLE][KAHAN]);
+  int *ctas = &b->solid_ctas[MODE == MODE_SYMPLECTIC][POLE][KAHAN][ANEL];
+  constexpr int smem = solid_smem_bytes<POLE, MODE, ANEL, KAHAN>();
+  int rc;
+  if constexpr (ANEL) rc = prepare_kernel_fn(h, solid_anel_batch_kernel<POLE, MODE, KAHAN>, smem, ctas);
+  else rc = prepare_kernel_fn(h, solid_batch_kernel<POLE, MODE, KAHAN>, smem, ctas);
   if (rc) b->err = h->err;
   return rc;
+}
+
+template <int POLE, int MODE>
+int prepare_batch_kernels(axg_batch *b, axg_handle *h) {
+  if (h->anel)
+    return h->kahan ? prepare_batch_kernel<POLE, MODE, true, true>(b, h) : prepare_batch_kernel<POLE, MODE, false, true>(b, h);
+  return h->kahan ? prepare_batch_kernel<POLE, MODE, true, false>(b, h) : prepare_batch_kernel<POLE, MODE, false, false>(b, h);
+}
+
+// the batched solid kernel a solve of the batch launches
+template <int MODE>
+int prepare_batch_mode(axg_batch *b, axg_handle *h) {
+  if (h->pole == AXG_MONOPOLE) return prepare_batch_kernels<POLE_MONO, MODE>(b, h);
+  if (h->pole == AXG_DIPOLE) return prepare_batch_kernels<POLE_DI, MODE>(b, h);
+  return prepare_batch_kernels<POLE_QUAD, MODE>(b, h);
 }
 
 int batch_create_impl(axg_batch *b, axg_handle *const *hs, int32_t n) {
@@ -2787,27 +2939,23 @@ int batch_create_impl(axg_batch *b, axg_handle *const *hs, int32_t n) {
     if (!h) return bfail(b, AXG_ERR_BAD_ARG, fmt("axg_batch_create: handle %d is NULL", k));
     for (int q = 0; q < k; ++q)
       if (hs[q] == h) return bfail(b, AXG_ERR_BAD_ARG, fmt("axg_batch_create: handle %d appears twice", k));
-    if (h->scheme != AXG_SCHEME_NEWMARK2 || h->anel)
-      return bfail(b, AXG_ERR_UNSUPPORTED,
-                   fmt("axg_batch_create: solve %d is not an elastic Newmark solve (attenuation and symplectic "
-                       "schemes run alone)", k));
     if (k > 0 && (h->device != hs[0]->device || std::memcmp(&h->spec, &hs[0]->spec, sizeof(SpecDev)) != 0))
       return bfail(b, AXG_ERR_BAD_ARG,
                    fmt("axg_batch_create: solve %d is on another device or has other GLL matrices", k));
     if (h->pending) return bfail(b, AXG_ERR_BAD_ARG, fmt("axg_batch_create: solve %d has queued steps", k));
     if (h->dump.type)
       return bfail(b, AXG_ERR_UNSUPPORTED, fmt("axg_batch_create: solve %d dumps wavefields (it runs alone)", k));
+    if (h->ckpt.check_it > 0)
+      return bfail(b, AXG_ERR_UNSUPPORTED,
+                   fmt("axg_batch_create: solve %d checkpoints its seismograms (it runs alone)", k));
     b->hs.push_back(h);
   }
   b->device = hs[0]->device;
   b->spec = hs[0]->spec;
   b->num_sms = hs[0]->num_sms;
-  int rc = AXG_OK;
   for (axg_handle *h : b->hs) {
-    const bool kh = h->kahan;
-    if (h->pole == AXG_MONOPOLE) rc = kh ? prepare_batch_kernel<POLE_MONO, true>(b, h) : prepare_batch_kernel<POLE_MONO, false>(b, h);
-    else if (h->pole == AXG_DIPOLE) rc = kh ? prepare_batch_kernel<POLE_DI, true>(b, h) : prepare_batch_kernel<POLE_DI, false>(b, h);
-    else rc = kh ? prepare_batch_kernel<POLE_QUAD, true>(b, h) : prepare_batch_kernel<POLE_QUAD, false>(b, h);
+    const int rc = h->scheme == AXG_SCHEME_NEWMARK2 ? prepare_batch_mode<MODE_NEWMARK>(b, h)
+                                                    : prepare_batch_mode<MODE_SYMPLECTIC>(b, h);
     if (rc) return rc;
   }
   BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
@@ -2880,6 +3028,7 @@ int axg_batch_run_async(axg_batch *b, const int32_t *first_iters, int32_t n_iter
   for (axg_handle *h : b->hs) {
     BCK(cudaEventRecord(h->ev_done, h->stream));
     BCK(cudaStreamWaitEvent(b->stream, h->ev_done, 0));
+    BCK(refresh_predicted(h, b->stream));
   }
   for (int k0 = 0; k0 < n; k0 += kMaxBatch) {
     IterSet a{};

@@ -116,6 +116,7 @@ struct StateArgs {
   float *a[3];              // acc0 / ddchi0
   float *f[3];              // force partial sums
   float *cu[3], *cv[3];     // compensated mode: running compensation of disp / velo (chi / dchi), else null
+  float *up[3];             // plain Newmark solid: the next step's predicted displacement, else null
   const float *inv_mass;    // per global point
   const double *inv_mass_dp;  // per global point in FP64 (compensated mode) or null
   const float *gamma;       // absorbing gamma per global point or null
@@ -167,10 +168,46 @@ struct Many {
   __device__ __forceinline__ const W &at(int s) const { return w[s]; }
 };
 
+// Attenuation data (cg4).
+//
+// Coarse-grained SLS attenuation: memory variables live at the four GLL
+// points (1,1), (1,3), (3,1), (3,3) of every solid element, the lanes 6, 16,
+// 8, 18 of the element's warp ("cg lanes", cg index k = 0..3 in that order,
+// the order of the reference's (1:4) arrays).
+//
+// Per element (launch order) the host packs two arrays:
+//   constants, kAnelConst floats: [field][k] for the fields below, then the
+//     two Q-table rows (int32 bits) of Q_mu and Q_kappa;
+//   state, anel_state_stride(n_sls) floats: memory_var_cg4(1:4,6,n_sls) in
+//     the reference's order, src_tr_tm1(1:4), src_dev_tm1(1:4,6).
+// Both travel with the element's metric block into the warp's ring; the
+// updated state is written back from shared memory.
+constexpr int kMaxSls = 8;
+enum : int {
+  A_DMU = 0, A_DKA = 4, A_Y = 8, A_VSE = 12, A_VSX = 16, A_VZE = 20, A_VZX = 24,
+  A_DSDETA = 28, A_DZDETA = 32, A_DSDXI = 36, A_DZDXI = 40, A_INVS = 44, A_QMU = 48, A_QKA = 49
+};
+constexpr int kAnelConst = 52;  // floats, a 16-byte multiple
+__host__ __device__ constexpr int anel_state_stride(int nsls) { return ((24 * nsls + 28 + 3) / 4) * 4; }
+constexpr int kAnelSlot = kAnelConst + anel_state_stride(kMaxSls);  // floats per ring slot
+
+struct AnelArgs {
+  const float *consts;      // per element kAnelConst floats (launch order)
+  float *state;             // per element state_stride floats (launch order)
+  const float *qtab;        // per distinct Q: ts_fac_t(j) a_j(Q) at [0, kMaxSls), ts_fac_tm1(j) a_j(Q) after
+  float ex[kMaxSls];        // exp_w_j_deltat
+  int32_t nsls, state_stride, n_q;
+};
+
 // patch kernels: the domain (patch_begin = the colour's first patch) and state
 struct PatchWork {
   DomainArgs d;
   StateArgs st;
+};
+// the attenuation data of the solves of an attenuated batch launch (the
+// launch's Many<PatchWork> order)
+struct AnelBatch {
+  AnelArgs a[kMaxBatch];
 };
 
 // How a patch kernel's body sees its work items.  OneSolve refers to the
@@ -182,20 +219,24 @@ struct OneSolve {
   const DomainArgs &d;
   const StateArgs &st;
   int32_t n;
+  const AnelArgs &an;
   __device__ __forceinline__ int32_t items() const { return n; }
   __device__ __forceinline__ int locate(int32_t) const { return 0; }
   __device__ __forceinline__ int32_t first(int) const { return 0; }
   __device__ __forceinline__ const DomainArgs &dom(int) const { return d; }
   __device__ __forceinline__ const StateArgs &state(int) const { return st; }
+  __device__ __forceinline__ const AnelArgs *anel(int) const { return &an; }
 };
 struct ManySolves {
   static constexpr bool kMany = true;
   const Many<PatchWork> &m;
+  const AnelArgs *an;  // per solve of the launch (attenuated batches), else null
   __device__ __forceinline__ int32_t items() const { return m.items(); }
   __device__ __forceinline__ int locate(int32_t it) const { return m.locate(it); }
   __device__ __forceinline__ int32_t first(int s) const { return m.first(s); }
   __device__ __forceinline__ const DomainArgs &dom(int s) const { return m.w[s].d; }
   __device__ __forceinline__ const StateArgs &state(int s) const { return m.w[s].st; }
+  __device__ __forceinline__ const AnelArgs *anel(int s) const { return an + s; }
 };
 
 // ------------------------------------------------------------ small helpers
@@ -477,35 +518,6 @@ __device__ __forceinline__ float stiff_fluid(const LaneCoef &c, const float (&mt
 }
 
 // ------------------------------------------------------------ attenuation (cg4)
-//
-// Coarse-grained SLS attenuation: memory variables live at the four GLL
-// points (1,1), (1,3), (3,1), (3,3) of every solid element, the lanes 6, 16,
-// 8, 18 of the element's warp ("cg lanes", cg index k = 0..3 in that order,
-// the order of the reference's (1:4) arrays).
-//
-// Per element (launch order) the host packs two arrays:
-//   constants, kAnelConst floats: [field][k] for the fields below, then the
-//     two Q-table rows (int32 bits) of Q_mu and Q_kappa;
-//   state, anel_state_stride(n_sls) floats: memory_var_cg4(1:4,6,n_sls) in
-//     the reference's order, src_tr_tm1(1:4), src_dev_tm1(1:4,6).
-// Both travel with the element's metric block into the warp's ring; the
-// updated state is written back from shared memory.
-constexpr int kMaxSls = 8;
-enum : int {
-  A_DMU = 0, A_DKA = 4, A_Y = 8, A_VSE = 12, A_VSX = 16, A_VZE = 20, A_VZX = 24,
-  A_DSDETA = 28, A_DZDETA = 32, A_DSDXI = 36, A_DZDXI = 40, A_INVS = 44, A_QMU = 48, A_QKA = 49
-};
-constexpr int kAnelConst = 52;  // floats, a 16-byte multiple
-__host__ __device__ constexpr int anel_state_stride(int nsls) { return ((24 * nsls + 28 + 3) / 4) * 4; }
-constexpr int kAnelSlot = kAnelConst + anel_state_stride(kMaxSls);  // floats per ring slot
-
-struct AnelArgs {
-  const float *consts;      // per element kAnelConst floats (launch order)
-  float *state;             // per element state_stride floats (launch order)
-  const float *qtab;        // per distinct Q: ts_fac_t(j) a_j(Q) at [0, kMaxSls), ts_fac_tm1(j) a_j(Q) after
-  float ex[kMaxSls];        // exp_w_j_deltat
-  int32_t nsls, state_stride, n_q;
-};
 
 // Anelastic stiffness (glob_anel_stiffness_{mono,di,quad}_cg4,
 // SOLVER/stiffness_mono.f90:511, SOLVER/stiffness_di.f90:727,
@@ -678,22 +690,34 @@ struct SolidSmem {
 };
 // ring depth (the same with attenuation, whose blocks ride in a second ring)
 __host__ __device__ constexpr int solid_stages(bool) { return kStages; }
-// patch-state buffers: the stiffness kernel gathers the next patch while it
-// computes the current one (two CTAs per SM fit), the Newmark kernel does not
-__host__ __device__ constexpr int solid_buffers(int mode) { return mode == MODE_FORCE ? 2 : 1; }
-// resident CTAs per SM the kernel is compiled for: the Newmark kernel keeps
-// three (its register-staged gather is latency-bound; 80 registers), the
-// others two (no spills at 128 registers)
+// The gather is asynchronous (cp.async into shared memory, the next patch's
+// during the current one's element rounds) where it only copies: the
+// stiffness mode's u, and the plain elastic Newmark step's predicted
+// displacement, which the previous step's last writers stored (up).  The
+// others compute on the way in (the compensated predictor, a symplectic
+// drift) or have no shared memory left for a second buffer (attenuation), and
+// gather through registers.
+__host__ __device__ constexpr bool solid_async(int mode, bool anel, bool kahan) {
+  return mode == MODE_FORCE || (mode == MODE_NEWMARK && !anel && !kahan);
+}
+// patch-state buffers: two for the asynchronous gather
+__host__ __device__ constexpr int solid_buffers(int mode, bool anel, bool kahan) {
+  return solid_async(mode, anel, kahan) ? 2 : 1;
+}
+// resident CTAs per SM the kernel is compiled for: the plain elastic
+// symplectic stage keeps three (its register-staged gather is latency-bound;
+// 80 registers), the others two (no spills at 128 registers; two patch
+// buffers fit)
 __host__ __device__ constexpr int solid_min_ctas(int mode, bool anel, bool kahan = false) {
-  return mode != MODE_FORCE && !anel && !kahan ? 3 : 2;
+  return mode == MODE_SYMPLECTIC && !anel && !kahan ? 3 : 2;
 }
 // Bank swizzle of the shared point arrays: patch point t lives at
 // t + pad * (t / 32).  An element's 25 points sit in five runs of five
 // consecutive patch points, one run per element row; on structured blocks
 // the runs lie a patch width (33 for 8 x 8 patches) apart, so unpadded they
 // share only 9 of the 32 banks (5-way conflicts), padded by 4 words per 32
-// they fall on 25 distinct banks.  The three-CTA elastic Newmark kernel can
-// only afford 2 words per 32 (banks i + 3j: at most 2-way conflicts).
+// they fall on 25 distinct banks.  The three-CTA elastic symplectic kernel
+// can only afford 2 words per 32 (banks i + 3j: at most 2-way conflicts).
 __host__ __device__ constexpr int solid_pad(int mode, bool anel, bool kahan = false) {
   return solid_min_ctas(mode, anel, kahan) == 2 ? 4 : 2;
 }
@@ -740,9 +764,9 @@ struct WarpIter {
 // velocity corrector (kahan_add); the predictor's new compensation travels
 // from the gather to the last writer in shared memory.
 template <int POLE, int MODE, bool ANEL, bool KAHAN, class P>
-__device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, const AnelArgs &an) {
+__device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) {
   static_assert(!ANEL || MODE != MODE_FORCE, "attenuation runs in a time loop");
-  static_assert(!P::kMany || (MODE == MODE_NEWMARK && !ANEL), "batches run the elastic Newmark step");
+  static_assert(!P::kMany || MODE != MODE_FORCE, "batches run time-loop steps");
   static_assert(!KAHAN || MODE != MODE_FORCE, "the compensated mode is a time-loop mode");
   constexpr bool TL = MODE != MODE_FORCE;  // a time-loop mode
   constexpr int NC = POLE == POLE_MONO ? 2 : 3;           // stored components
@@ -751,7 +775,11 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
   constexpr uint32_t BSB = BS * 4;
   constexpr int STG = solid_stages(ANEL);
   constexpr int AS = ANEL ? kAnelSlot : 0;
-  constexpr int NB = solid_buffers(MODE);
+  constexpr int NB = solid_buffers(MODE, ANEL, KAHAN);
+  constexpr bool ASYNC = solid_async(MODE, ANEL, KAHAN);
+  // plain Newmark: the gather reads the predicted displacement (up), and the
+  // last writers store the next step's
+  constexpr bool LOOK = MODE == MODE_NEWMARK && !KAHAN;
   constexpr int ROW = solid_row(MODE, ANEL, KAHAN), PAD = solid_pad(MODE, ANEL, KAHAN);
   using L = SolidSmem<NC, BS, STG, AS, NB, ROW, KAHAN>;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -805,14 +833,15 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
   // cg lane index k of the attenuation points (1,1), (1,3), (3,1), (3,3)
   const bool cg = active && (i == 1 || i == 3) && (j == 1 || j == 3);
   const int kcg = 2 * (i >> 1) + (j >> 1);
-  const uint32_t state_bytes = ANEL ? (uint32_t)an.state_stride * 4u : 0u;
-  // one thread: start the copies of element `el` of domain d into ring slot `slot`
-  auto issue = [&](const DomainArgs &d, uint32_t slot, int64_t el) {
+  // one thread: start the copies of element `el` of domain d (attenuation
+  // data an) into ring slot `slot`
+  auto issue = [&](const DomainArgs &d, const AnelArgs *an, uint32_t slot, int64_t el) {
     if (ANEL) {
+      const uint32_t state_bytes = (uint32_t)an->state_stride * 4u;
       mbar_expect_tx(&my_bars[slot], BSB + kAnelConst * 4 + state_bytes);
       bulk_g2s_tx(my_ring + slot * BS, d.metric + el * BS, BSB, &my_bars[slot], pol);
-      bulk_g2s_tx(my_aring + slot * AS, an.consts + el * kAnelConst, kAnelConst * 4, &my_bars[slot], pol);
-      bulk_g2s_tx(my_aring + slot * AS + kAnelConst, an.state + el * an.state_stride, state_bytes, &my_bars[slot],
+      bulk_g2s_tx(my_aring + slot * AS, an->consts + el * kAnelConst, kAnelConst * 4, &my_bars[slot], pol);
+      bulk_g2s_tx(my_aring + slot * AS + kAnelConst, an->state + el * an->state_stride, state_bytes, &my_bars[slot],
                   pol);
     } else {
       bulk_g2s(my_ring + slot * BS, d.metric + el * BS, BSB, &my_bars[slot], pol);
@@ -829,11 +858,13 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
       mbar_arrive(&s_wbar[b]);
     }
   };
-  // every thread (stiffness mode): asynchronous 4-byte copies of its points'
-  // u, and of the partial sums of points an earlier writer (earlier colour,
-  // coupling pre-pass) holds, straight into buffer b.  A point's accumulator
-  // starts from that partial sum, so that the write-back is a plain store.
+  // every thread (asynchronous gather): 4-byte copies of its points' u (the
+  // predicted displacement up in a Newmark step), and of the partial sums of
+  // points an earlier writer (earlier colour, coupling pre-pass) holds,
+  // straight into buffer b.  A point's accumulator starts from that partial
+  // sum, so that the write-back is a plain store.
   auto issue_gather = [&](const StateArgs &st, int b, int n_pts) {
+    float *const *src = MODE == MODE_NEWMARK ? st.up : st.u;
     float(*gu)[ROW] = su_of(b);
     float(*gf)[ROW] = sf_of(b);
     const uint32_t *gw = sw_of(b);
@@ -848,22 +879,25 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
       }
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        cp_async4(&gu[c][pt], st.u[gc(c)] + g);
+        cp_async4(&gu[c][pt], src[gc(c)] + g);
         if (w & kPtFirst) gf[c][pt] = 0.f;
         else cp_async4(&gf[c][pt], st.f[gc(c)] + g);
       }
     }
     cp_async_commit();
   };
-  // stiffness mode: the CTA's first patch is gathered here, each later one
-  // while the CTA computes the patch before it
-  if (MODE == MODE_FORCE && (int32_t)blockIdx.x < p.items() &&
-      AXG_BOUND(p.dom(0).patch_begin + blockIdx.x, p.dom(0).n_patches, 1)) {
-    const DomainArgs &d = p.dom(0);
-    const PatchMeta m0 = d.meta[d.patch_begin + blockIdx.x];
-    if (threadIdx.x == 0) issue_words(d, 0, m0.pt_start, m0.n_pts);
-    if (!mbar_wait_bounded(&s_wbar[0], 0u, p.state(0).err)) s_timeout = 1;
-    issue_gather(p.state(0), 0, m0.n_pts);
+  // asynchronous gather: the CTA's first work item is gathered here, each
+  // later one while the CTA computes the item before it
+  if (ASYNC && (int32_t)blockIdx.x < p.items()) {
+    const int sv0 = p.locate(blockIdx.x);
+    const DomainArgs &d = p.dom(sv0);
+    const int pp0 = blockIdx.x - p.first(sv0);
+    if (AXG_BOUND(d.patch_begin + pp0, d.n_patches, 1)) {
+      const PatchMeta m0 = d.meta[d.patch_begin + pp0];
+      if (threadIdx.x == 0) issue_words(d, 0, m0.pt_start, m0.n_pts);
+      if (!mbar_wait_bounded(&s_wbar[0], 0u, p.state(sv0).err)) s_timeout = 1;
+      issue_gather(p.state(sv0), 0, m0.n_pts);
+    }
   }
 
   for (int32_t it = blockIdx.x; it < p.items(); it += gridDim.x) {
@@ -871,8 +905,12 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
     const int sv = p.locate(it);
     const DomainArgs &d = p.dom(sv);
     const StateArgs &st = p.state(sv);
+    const AnelArgs *an = ANEL ? p.anel(sv) : nullptr;
     const int pp = it - p.first(sv);
-    if (P::kMany && __syncthreads_or(threadIdx.x == 0 && *st.blowup != 0)) continue;  // that solve has stopped
+    // that solve has stopped (with the asynchronous gather, whose next item is
+    // already in flight, a blown-up solve's items are computed on: its run
+    // has failed either way)
+    if (P::kMany && !ASYNC && __syncthreads_or(threadIdx.x == 0 && *st.blowup != 0)) continue;
     float stf1 = stf_one;
     if (TL && P::kMany && AXG_BOUND(*st.iter - 1, st.niter, 3)) stf1 = st.stf[*st.iter - 1];
     if (!AXG_BOUND(d.patch_begin + pp, d.n_patches, 1)) break;
@@ -882,14 +920,19 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
     float(*s_u)[ROW] = su_of(buf);
     float(*s_f)[ROW] = sf_of(buf);
     const uint32_t *s_w = sw_of(buf);
-    // stiffness mode: the next patch's point words go to the other buffer now
-    int next_npts = 0;
-    if (MODE == MODE_FORCE) {
-      const int ppn = pp + gridDim.x;  // one solve: items are patches
-      if (ppn < p.items() && AXG_BOUND(d.patch_begin + ppn, d.n_patches, 1)) {
-        const PatchMeta mn = d.meta[d.patch_begin + ppn];
-        next_npts = mn.n_pts;
-        if (threadIdx.x == 0) issue_words(d, buf ^ 1, mn.pt_start, mn.n_pts);
+    // asynchronous gather: the next item's point words go to the other buffer now
+    int next_npts = 0, next_sv = 0;
+    if (ASYNC) {
+      const int32_t itn = it + gridDim.x;
+      if (itn < p.items()) {
+        next_sv = p.locate(itn);
+        const DomainArgs &dn = p.dom(next_sv);
+        const int ppn = itn - p.first(next_sv);
+        if (AXG_BOUND(dn.patch_begin + ppn, dn.n_patches, 1)) {
+          const PatchMeta mn = dn.meta[dn.patch_begin + ppn];
+          next_npts = mn.n_pts;
+          if (threadIdx.x == 0) issue_words(dn, buf ^ 1, mn.pt_start, mn.n_pts);
+        }
       }
     } else if (threadIdx.x == 0) {
       issue_words(d, 0, m.pt_start, m.n_pts);
@@ -902,7 +945,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
       for (int q = 0; q < STG && pf.valid(pr); ++q) {
         if (lane == 0) {
           const int64_t el = (int64_t)m.elem_start + pf.s;
-          if (AXG_BOUND(el, d.n_elem, 2)) issue(d, (kcount + q) % STG, el);
+          if (AXG_BOUND(el, d.n_elem, 2)) issue(d, an, (kcount + q) % STG, el);
         }
         pf.s += kWarps;
         pf.norm(pr, warp);
@@ -912,12 +955,14 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
     //    colour) already holds a partial sum for starts its accumulator from
     //    that sum, so that the write-back is a plain store.
     prefetch_first();
-    if (MODE == MODE_FORCE) {
+    if (ASYNC) {
       cp_async_wait_all();  // this thread's copies of the patch (issued during the previous one)
     } else {
       if (!mbar_wait_bounded(&s_wbar[0], pcount & 1u, st.err)) s_timeout = 1;
-      // Newmark predictor on the fly; kGB points per thread in flight cover
-      // a whole patch (kGB * kThreads >= kMaxPatchPoints): one memory latency
+      // through registers: the compensated predictor or a symplectic drift on
+      // the fly, or the stored predicted displacement (plain Newmark with
+      // attenuation); kGB points per thread in flight cover a whole patch
+      // (kGB * kThreads >= kMaxPatchPoints): one memory latency
       constexpr int kGB = (kMaxPatchPoints + kThreads - 1) / kThreads;
       for (int t0 = threadIdx.x; t0 < m.n_pts; t0 += kGB * kThreads) {
         uint32_t w[kGB];
@@ -934,7 +979,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
           const bool part = ok && !(w[q] & kPtFirst);
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
-            float u = ok ? st.u[gc(c)][g] : 0.f;
+            float u = ok ? (LOOK ? st.up[gc(c)][g] : st.u[gc(c)][g]) : 0.f;
             if (KAHAN) {
               float k = ok ? st.cu[gc(c)][g] : 0.f;
               // (a symplectic stage: hdt2 = 0, the compensated drift u + coefd(i) v)
@@ -943,9 +988,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
               cc[KAHAN ? q : 0][c] = k;
             } else if (ok && MODE == MODE_SYMPLECTIC) {
               u = fmaf(st.dt, st.v[gc(c)][g], u);  // drift: disp + velo * coefd(i)
-            } else if (ok) {
-              u = predict(u, st.v[gc(c)][g], st.a[gc(c)][g], st.dt, st.hdt2);
-            }
+            }  // (plain Newmark: up is the predicted displacement)
             uu[q][c] = u;
             ff[q][c] = part ? st.f[gc(c)][g] : 0.f;
           }
@@ -1019,8 +1062,8 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
         }
         float *ablk = my_aring + slot * AS;  // attenuation constants, then state
         if (ANEL) {
-          if (ax) anel_stiffness<POLE, true>(coef, ablk, ablk + kAnelConst, an.nsls, cg, kcg, i, j, active, lane, f0, f1, f2);
-          else anel_stiffness<POLE, false>(coef, ablk, ablk + kAnelConst, an.nsls, cg, kcg, i, j, active, lane, f0, f1, f2);
+          if (ax) anel_stiffness<POLE, true>(coef, ablk, ablk + kAnelConst, an->nsls, cg, kcg, i, j, active, lane, f0, f1, f2);
+          else anel_stiffness<POLE, false>(coef, ablk, ablk + kAnelConst, an->nsls, cg, kcg, i, j, active, lane, f0, f1, f2);
         }
         if (ax && i == 0) {  // axis mask of acc1
           if (POLE == POLE_MONO) f0 = 0.f;
@@ -1048,11 +1091,11 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
           // SOLVER/time_evol_wave.F90), then the element's state back to HBM.
           // (A symplectic stage only reads them: anel_memvar_kernel updates
           // them once per step.)
-          anel_memvar_step<POLE>(ablk, ablk + kAnelConst, scr + warp * 32, an, cg, kcg, lane, u, gx, ge);
+          anel_memvar_step<POLE>(ablk, ablk + kAnelConst, scr + warp * 32, *an, cg, kcg, lane, u, gx, ge);
           __syncwarp();
           const float4 *src4 = reinterpret_cast<const float4 *>(ablk + kAnelConst);
-          float4 *dst4 = reinterpret_cast<float4 *>(an.state + el * an.state_stride);
-          for (int q = lane; q < an.state_stride / 4; q += 32) dst4[q] = src4[q];
+          float4 *dst4 = reinterpret_cast<float4 *>(an->state + el * an->state_stride);
+          for (int q = lane; q < an->state_stride / 4; q += 32) dst4[q] = src4[q];
         }
         // the slot is free again: start the copy of the element STG ahead
         __syncwarp();
@@ -1060,7 +1103,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
           if (lane == 0) {
             const int64_t pel = (int64_t)m.elem_start + pf.s;
             fence_proxy_async();  // the warp's reads of the slot precede the async-proxy write
-            if (AXG_BOUND(pel, d.n_elem, 2)) issue(d, slot, pel);
+            if (AXG_BOUND(pel, d.n_elem, 2)) issue(d, an, slot, pel);
           }
           pf.s += kWarps;
           pf.norm(pr, warp);
@@ -1069,10 +1112,10 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
       }
       mbar_arrive(&s_round[r]);  // this thread's accumulations of round r are done
       r0 = r1;
-      if (MODE == MODE_FORCE && r == 0 && next_npts > 0) {
-        // the next patch's words have landed in the other buffer: start its gather
+      if (ASYNC && r == 0 && next_npts > 0) {
+        // the next item's words have landed in the other buffer: start its gather
         if (!mbar_wait_bounded(&s_wbar[buf ^ 1], ((pcount + 1) / NB) & 1u, st.err)) s_timeout = 1;
-        issue_gather(st, buf ^ 1, next_npts);
+        issue_gather(p.state(next_sv), buf ^ 1, next_npts);
       }
     }
     round_par ^= (1u << pr.n) - 1u;  // each used s_round completed once in this patch
@@ -1173,19 +1216,25 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
               a = (POLE == POLE_DI && cg == 2) ? (-2.f * im[q]) * v[c] : -im[q] * v[c];
             }
             if (st.gamma) a = a - 2.f * gam[q] * vel[q][c] - gam[q] * gam[q] * dsp;
+            float vn;
             if (KAHAN) {
               float k = kv[KAHAN ? q : 0][c];
-              st.v[cg][g] = kahan_add(vel[q][c], st.hdt * (acc[q][c] + a), k);
+              vn = kahan_add(vel[q][c], st.hdt * (acc[q][c] + a), k);
               st.cv[cg][g] = k;
               st.cu[cg][g] = s_cu[c][spos(t)];
             } else {
-              st.v[cg][g] = fmaf(st.hdt, acc[q][c] + a, vel[q][c]);
+              vn = fmaf(st.hdt, acc[q][c] + a, vel[q][c]);
             }
+            st.v[cg][g] = vn;
             st.a[cg][g] = a;
             // the axis masks of the reference zero these components of its state
             const bool zero = (w[q] & kPtAxis) && axis_masked<POLE>(cg);
-            st.u[cg][g] = zero ? 0.f : dsp;
+            const float un = zero ? 0.f : dsp;
+            st.u[cg][g] = un;
             if (KAHAN && zero) st.cu[cg][g] = 0.f;
+            // the next step's predictor disp + deltat*velo + half_dt_sq*acc0
+            // (SOLVER/time_evol_wave.F90:357-364), from the state just stored
+            if (LOOK) st.up[cg][g] = predict(un, vn, a, st.dt, st.hdt2);
           }
         }
       }
@@ -1204,8 +1253,8 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp, 
         mbar_drain(&my_bars[k % STG], (k / STG) & 1u);
       }
     if (threadIdx.x == 0 && pcount > 0) {
-      const uint32_t b = MODE == MODE_FORCE ? (pcount - 1) % NB : 0u;
-      const uint32_t par = MODE == MODE_FORCE ? ((pcount - 1) / NB) & 1u : (pcount - 1) & 1u;
+      const uint32_t b = ASYNC ? (pcount - 1) % NB : 0u;
+      const uint32_t par = ASYNC ? ((pcount - 1) / NB) & 1u : (pcount - 1) & 1u;
       mbar_drain(&s_wbar[b], par);
     }
   }
@@ -1260,15 +1309,24 @@ template <int POLE, int MODE, bool ANEL, bool KAHAN>
 __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, ANEL, KAHAN))
     solid_patch_kernel(DomainArgs d, StateArgs st, SpecDev sp, int32_t n_colour_patches,
                        const __grid_constant__ AnelArgs an) {  // an.ex[] is indexed at run time
-  solid_patch_body<POLE, MODE, ANEL, KAHAN>(OneSolve{d, st, n_colour_patches}, sp, an);
+  solid_patch_body<POLE, MODE, ANEL, KAHAN>(OneSolve{d, st, n_colour_patches, an}, sp);
 }
 
-// A batch: colour c of every solve of the launch, found by run-time index
-// into the descriptors (hence in the parameter space, __grid_constant__).
-template <int POLE, bool KAHAN>
-__global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE_NEWMARK, false, KAHAN))
+// A batch: colour c of every solve of the launch (a Newmark step, or one
+// stage of a symplectic step), found by run-time index into the descriptors
+// (hence in the parameter space, __grid_constant__).
+template <int POLE, int MODE, bool KAHAN>
+__global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, false, KAHAN))
     solid_batch_kernel(const __grid_constant__ Many<PatchWork> p, SpecDev sp) {
-  solid_patch_body<POLE, MODE_NEWMARK, false, KAHAN>(ManySolves{p}, sp, AnelArgs{});
+  solid_patch_body<POLE, MODE, false, KAHAN>(ManySolves{p, nullptr}, sp);
+}
+// An attenuated batch: the same, with each solve's attenuation data (cg4)
+// beside its descriptors.
+template <int POLE, int MODE, bool KAHAN>
+__global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, true, KAHAN))
+    solid_anel_batch_kernel(const __grid_constant__ Many<PatchWork> p, SpecDev sp,
+                            const __grid_constant__ AnelBatch an) {
+  solid_patch_body<POLE, MODE, true, KAHAN>(ManySolves{p, an.a}, sp);
 }
 
 // ------------------------------------------------------------ fluid patch kernel
@@ -1305,7 +1363,6 @@ struct FluidSmem {
 // batch before it stores.
 template <int NONMONO, bool KAHAN, bool SYMP = false, class P = One<PatchWork>>
 __global__ void __launch_bounds__(kThreads, 4) fluid_patch_kernel(const __grid_constant__ P p, SpecDev sp) {
-  static_assert(!P::kMany || !SYMP, "batches run the Newmark step");
   using L = FluidSmem<NONMONO, KAHAN>;
   constexpr int BS = L::BS;
   constexpr int NT = NONMONO ? 4 : 3;
@@ -1492,9 +1549,20 @@ __global__ void __launch_bounds__(kThreads, 4) fluid_patch_kernel(const __grid_c
 // The final drift of a symplectic step (SOLVER/time_evol_wave.F90:722-727):
 // chi += dchi * coefd(nstages+1), disp += velo * coefd(nstages+1), on every
 // global point.
-__global__ void drift_kernel(StateArgs solid, StateArgs fluid, float cd) {
+struct DriftWork {
+  StateArgs solid, fluid;
+  float cd;  // coefd(nstages + 1) deltat
+};
+template <class P = One<DriftWork>>
+__global__ void drift_kernel(const __grid_constant__ P p) {
+  const int32_t it = blockIdx.x * blockDim.x + threadIdx.x;  // a point of one of the solves
+  if (it >= p.items()) return;
+  const int sv = p.locate(it);
+  const StateArgs &solid = p.at(sv).solid;
+  const StateArgs &fluid = p.at(sv).fluid;
+  const float cd = p.at(sv).cd;
   if (*solid.blowup) return;
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t q = it - p.first(sv);
   // u + coefd(nstages+1) v; compensated where the handle keeps compensation
   auto drift = [&](float *u, const float *v, float *cu) {
     if (cu) {
@@ -1509,6 +1577,16 @@ __global__ void drift_kernel(StateArgs solid, StateArgs fluid, float cd) {
     for (int c = 0; c < 3; ++c)
       if (solid.u[c]) drift(solid.u[c], solid.v[c], solid.cu[c]);
   if (fluid.u[0] && q < fluid.nglob) drift(fluid.u[0], fluid.v[0], fluid.cu[0]);
+}
+
+// The plain Newmark step's predicted displacement up = disp + deltat*velo +
+// half_dt_sq*acc0 (SOLVER/time_evol_wave.F90:357-364) of the current state,
+// before a run: the last writers keep it from there on.
+__global__ void predict_kernel(StateArgs solid) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= solid.nglob) return;
+  for (int c = 0; c < 3; ++c)
+    if (solid.up[c]) solid.up[c][q] = predict(solid.u[c][q], solid.v[c][q], solid.a[c][q], solid.dt, solid.hdt2);
 }
 
 // ------------------------------------------------------------ coupling pre-passes
@@ -1547,12 +1625,14 @@ __global__ void couple_to_fluid_kernel(const __grid_constant__ P p) {
     if (!AXG_BOUND(k, cp.n_contrib, 21)) break;
     const int gs = cp.src_gidx[k];
     if (!AXG_BOUND(gs, cp.nglob_send, 21)) continue;
-    // the same predicted displacement as the solid kernel's gather
+    // the same predicted displacement as the solid kernel's gather (plain
+    // Newmark: the one the previous step's last writers stored)
     auto pred = [&](int c) {
       if (solid.cu[0]) {
         float k = solid.cu[c][gs];
         return predict_comp(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid.dt, solid.hdt2, k);
       }
+      if (solid.up[0]) return solid.up[c][gs];
       return predict(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid.dt, solid.hdt2);
     };
     const float us = pred(0);

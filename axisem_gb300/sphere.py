@@ -1035,6 +1035,22 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
     m.meta["receiver_colat_deg"] = np.array([th[int(np.argmin(np.abs(th - c)))] for c in rec])
 
 
+def long_run_mesh(steps: int = 100_000, period: float = 50.0, model: str = "prem_ani",
+                  skeleton: Skeleton | None = None) -> Mesh:
+    """The long anelastic run of the precision study: `steps` time steps on
+    the `model` mesh at `period` seconds with cg4 attenuation (5 SLS, PREM
+    Q), a dipole source (Mrt = 1e20 N m) at 100 km depth and 10 surface
+    receivers from 5 to 175 degrees, sampled every 50 steps."""
+    sk = skeleton or build_skeleton(period, model)
+    solve = SphereSolve(pole=_abi.DIPOLE, source="mtr", depth_km=100.0, seconds=1.0,
+                        receivers_deg=np.linspace(5.0, 175.0, 10), seis_it=50)
+    m = build_mesh(period, solve, model=model, skeleton=sk, attenuation=Attenuation())
+    solve.seconds = (steps - 0.5) * m.deltat
+    out = with_solve(m, solve, sk)
+    assert out.niter == steps
+    return out
+
+
 def with_solve(m: Mesh, solve: SphereSolve, skeleton: Skeleton) -> Mesh:
     """The mesh `m` (built by build_mesh on `skeleton` for the same pole
     type) with another solve's source depth, receivers, run length and

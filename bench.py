@@ -325,6 +325,7 @@ def run_gpu(args):
         timeloop_dumps = run_timeloop_dumps(args, pole, ws, rank)
 
     physical = run_physical(args, ws, rank) if args.physical_steps > 0 else None
+    precision = run_precision(ws, rank) if not args.no_precision else None
     serving = run_serving(args) if args.serve_requests > 0 else None
 
     if rank != 0:
@@ -347,6 +348,7 @@ def run_gpu(args):
         "timeloop_compensated": timeloop_comp,
         "timeloop_dumps": timeloop_dumps,
         "physical": physical,
+        "precision": precision,
         "serving": serving,
         "clocks": head["clocks"],
         "gpu_launches": int(args.steps * info["kernels_per_force"]),
@@ -482,6 +484,45 @@ def run_physical(args, ws, rank):
     return out
 
 
+def run_precision(ws, rank):
+    """The precision study: 1e5 steps of the anelastic dipole run of
+    axisem_gb300.sphere.long_run_mesh (prem_ani 50 s, cg4 attenuation with 5
+    SLS, Mrt at 100 km, 10 surface receivers), plain FP32 and compensated,
+    each against the FP64 oracle's seismograms of the same mesh
+    (tests/golden/precision_long_run.npz): relative L2 per component (s, phi,
+    z), with the oracle's own FP32 run beside them."""
+    import torch
+    from axisem_gb300 import sphere
+    from axisem_gb300.solver import Solver
+    fx_path = ROOT / "tests" / "golden" / "precision_long_run.npz"
+    if not fx_path.exists():
+        return {"unavailable": "no FP64 oracle fixture (tests/golden/make_precision_reference.py makes it)"}
+    fx = np.load(fx_path)
+    ref = np.asarray(fx["rec_float64"], np.float64)
+
+    def per_component(rec):
+        rec = np.asarray(rec, np.float64)
+        return [float(np.linalg.norm(rec[:, c] - ref[:, c]) / np.linalg.norm(ref[:, c])) for c in range(3)]
+
+    m = sphere.long_run_mesh(int(fx["niter"]))
+    out = {"mesh": f"prem_ani 50 s, {m.nel_solid} solid + {m.nel_fluid} fluid elements, cg4 attenuation (5 SLS), "
+                   f"dipole Mrt at 100 km, {m.num_rec} receivers",
+           "steps": m.niter, "deltat_s": m.deltat, "components": ["s", "phi", "z"],
+           "oracle_fp32": per_component(fx["rec_float32"])}
+    for mode in ("plain", "compensated"):
+        with Solver(m) as s:
+            s.set_compensated(mode == "compensated")
+            torch.cuda.synchronize()
+            barrier(ws)
+            t0 = time.perf_counter()
+            s.run()
+            torch.cuda.synchronize()
+            dt = max_over_ranks(time.perf_counter() - t0, ws)
+            out[mode] = per_component(s.receivers())
+            out[f"{mode}_solve_s"] = dt
+    return out
+
+
 def run_timeloop_dumps(args, pole, ws, rank, strain_it=8):
     """The elastic time loop of run_timeloop without and with kernel wavefield
     dumps (axg_set_wavefield_dump: displ_only and strain_only every strain_it
@@ -586,6 +627,7 @@ def main():
     ap.add_argument("--no-other-poles", action="store_true")
     ap.add_argument("--timeloop-steps", type=int, default=64)
     ap.add_argument("--physical-steps", type=int, default=2000)
+    ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rates", default="0.5,1,2,5,10,20")
     ap.add_argument("--serve-duration-scale", type=float, default=0.1)

@@ -293,12 +293,16 @@ int axg_wait(axg_handle *h);
  * meshes (uneven element counts).  A batch step makes one launch per colour
  * and kernel class for all its solves -- the kernels take a work list of
  * (solve, patch) items -- and is captured once in a CUDA graph that every
- * step replays.  Solves of a batch run the elastic Newmark step (any pole,
- * plain or compensated; not attenuation or a symplectic scheme) and share
- * the GLL derivative matrices.  Each solve's results are bit-for-bit those
- * it gets alone.  The handles must stay open while the batch exists and are
- * not run by other calls meanwhile; their later calls are ordered after the
- * batch's work.  No counterpart in the reference. */
+ * step replays.  Solves of a batch may differ in pole, precision mode
+ * (plain or compensated), attenuation (cg4) and time scheme: a symplectic
+ * solve's stages run as phases of the batch step (stage i of every solve
+ * with more than i stages in one launch per colour and kernel class).  They
+ * share the GLL derivative matrices; solves that dump wavefields or
+ * checkpoint seismograms run alone.  Each solve's results are bit-for-bit
+ * those it gets alone.  The handles must stay open while the batch exists
+ * and are neither run nor reconfigured (time scheme, precision mode) by
+ * other calls meanwhile; their later calls are ordered after the batch's
+ * work.  No counterpart in the reference. */
 typedef struct axg_batch axg_batch;
 int axg_batch_create(axg_handle *const *hs, int32_t n, axg_batch **out);
 /* Queue n_iter steps of every solve, solve k from iteration first_iters[k]

@@ -121,3 +121,27 @@ def test_prem_50s_anelastic(gpu_lib, orc, sk50, pole):
     assert per_receiver(rec, t.receivers()) <= 1e-4
     comps = [0, 1, 2, 4] if pole == 0 else list(range(6))
     assert rel(mv[:, comps], t.memvar[:, comps]) <= 1e-4
+
+
+@pytest.mark.parametrize("pole", [0, 1])
+def test_fp64_terms_of_the_compensated_mode(gpu_lib, orc, sk50, pole):
+    """The compensated mode applies the FP64 inverse masses and source term
+    the precompute provides: a run with them differs from one given only the
+    FP32 copies (the FP64 path is taken), and both meet the 1e-4 bar against
+    the FP64 oracle over 600 s."""
+    import copy
+    m = sphere.build_mesh(50.0, sphere.SphereSolve(pole=pole, seconds=600.0), skeleton=sk50)
+    assert m.inv_mass_rho_dp is not None and m.source_term_el_dp is not None
+    m32 = copy.copy(m)
+    m32.inv_mass_rho_dp = m32.inv_mass_fluid_dp = m32.source_term_el_dp = None
+    recs = []
+    for mm in (m, m32):
+        with Solver(mm) as s:
+            s.set_compensated(True)
+            s.run()
+            recs.append(s.receivers())
+    assert not np.array_equal(recs[0], recs[1])
+    t = orc.TimeLoop(m, np.float64)
+    assert t.run(1, m.niter) == 0
+    for r in recs:
+        assert per_receiver(r, t.receivers()) <= 1e-4
