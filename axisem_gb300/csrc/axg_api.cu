@@ -66,8 +66,11 @@ struct DevBuf {
 struct DomainDev {
   PatchMeta *meta = nullptr;
   uint32_t *pts = nullptr;
-  uint16_t *elpts = nullptr;
   int32_t *elinfo = nullptr;
+  // the fluid's two passes: element points (launch order), the CSR of each
+  // point's copies (flags in start), the per-copy contributions (per solve)
+  int32_t *gidx = nullptr, *start = nullptr, *ent = nullptr;
+  float *fel = nullptr;
   float *metric = nullptr;
   float *m0 = nullptr;
   float *fsmask = nullptr;
@@ -116,6 +119,7 @@ struct axg_handle {
   DomainDev ds, df;
   float *su[3] = {}, *sv[3] = {}, *sa[3] = {}, *sf[3] = {};
   float *sup[3] = {};  // the plain Newmark step's predicted displacement (kept by the last writers)
+  float *fup = nullptr;  // ... and chi
   float *fu = nullptr, *fv = nullptr, *fa = nullptr, *ff = nullptr;
   float *inv_mass_s = nullptr, *inv_mass_f = nullptr, *gamma_s = nullptr, *gamma_f = nullptr;
   // FP64 inverse masses (mesh) and source values (solve), when the descriptor had them
@@ -375,9 +379,63 @@ std::vector<T> per_point(const T *elem, const std::vector<int32_t> &igloc, int64
   return out;
 }
 
+// The fluid's arrays for its two passes.  mesh_part (mesh pool): the metric
+// blocks, axial vectors and free-surface mask per element slot (launch
+// order), the slots' global points, and per point the CSR of its copies with
+// its flags (a coupling pre-pass partial sum; on the axis); always (this
+// solve): the element info words (source slot), the fluid source terms and
+// the per-copy contribution buffer.
+int build_fluid_passes(axg_handle *h, const axg_mesh_desc *d, const DomainPlan &pl, DomainDev &dd, bool mesh_part,
+                       const std::vector<float> &metric, const std::vector<int32_t> &elinfo,
+                       const std::vector<float> &m0, const std::vector<float> &fsmask, int nax, const int32_t *axl) {
+  const int64_t nel = pl.nel, nglob = h->nglob_f;
+  int rc;
+  if (mesh_part) {
+    std::vector<int32_t> gidx((size_t)25 * nel), start(nglob + 1, 0), ent((size_t)25 * nel);
+    for (int64_t s = 0; s < nel; ++s) {
+      const int64_t e = pl.elem_order[s];
+      for (int k = 0; k < 25; ++k) {
+        const int32_t g = h->igloc_f[25 * e + k] - 1;  // internal numbering
+        gidx[25 * s + k] = g;
+        start[g + 1]++;
+      }
+    }
+    for (int64_t g = 0; g < nglob; ++g) start[g + 1] += start[g];
+    if (start[nglob] >= (int64_t)kFlStartMask) return fail(h, AXG_ERR_BAD_DESC, "fluid mesh too large");
+    {
+      std::vector<int32_t> fill(start.begin(), start.end() - 1);
+      for (int64_t c = 0; c < 25 * nel; ++c) ent[fill[gidx[c]]++] = (int32_t)c;  // copies in slot order
+    }
+    // flags: the coupling pre-pass's receiving points, the points on the axis
+    for (size_t g = 0; g < h->pre_f.size(); ++g)
+      if (h->pre_f[g]) start[pl.new_of_old[g]] |= (int32_t)kFlPartial;
+    for (int k = 0; k < nax; ++k)
+      for (int jj = 0; jj < 5; ++jj) start[h->igloc_f[25 * (int64_t)(axl[k] - 1) + 5 * jj] - 1] |= (int32_t)kFlAxis;
+    h->in_mesh = true;
+    rc = upload(h, &dd.metric, metric);
+    if (!rc) rc = upload(h, &dd.m0, m0);
+    if (!rc && !fsmask.empty()) rc = upload(h, &dd.fsmask, fsmask);
+    if (!rc) rc = upload(h, &dd.gidx, gidx);
+    if (!rc) rc = upload(h, &dd.start, start);
+    if (!rc) rc = upload(h, &dd.ent, ent);
+    h->in_mesh = false;
+    if (rc) return rc;
+    dd.n_m0 = (int64_t)m0.size();
+  }
+  if ((rc = upload(h, &dd.elinfo, elinfo))) return rc;
+  if ((rc = dalloc(h, &dd.fel, (size_t)25 * nel))) return rc;
+  if (d->fluid_src && d->nelsrc > 0) {
+    std::vector<float> s((size_t)8 * 25, 0.f);
+    for (int k = 0; k < d->nelsrc; ++k)
+      for (int q = 0; q < 25; ++q) s[25 * k + q] = d->source_term_fl[q + 25 * k];
+    if ((rc = upload(h, &dd.srcfl, s))) return rc;
+  }
+  return AXG_OK;
+}
+
 // mesh_part: the element blocks, patch metadata and axial vectors (mesh
-// pool); always: the point words (source and axis flags), element info words
-// and fluid source terms of this solve
+// pool); always: the point words (source and axis flags) and element info
+// words of this solve.  The fluid's arrays: build_fluid_passes.
 int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid, bool mesh_part) {
   const DomainPlan &pl = fluid ? h->pf : h->ps;
   DomainDev &dd = fluid ? h->df : h->ds;
@@ -439,6 +497,7 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid, bool mesh_pa
     }
     if (use_fs) std::memcpy(fsmask.data() + 25 * s, d->fluid_free_surface_mask + 25 * e, 25 * sizeof(float));
   }
+  if (fluid) return build_fluid_passes(h, d, pl, dd, mesh_part, metric, elinfo, m0, fsmask, nax, axl);
   std::vector<uint32_t> pts = pl.pt_words;
   {
     // points on the axis: the last writer stores their masked components as
@@ -468,7 +527,7 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid, bool mesh_pa
   int rc;
   if (mesh_part) {
     h->in_mesh = true;
-    if ((rc = upload(h, &dd.meta, pl.meta)) || (rc = upload(h, &dd.elpts, pl.elem_pts)) ||
+    if ((rc = upload(h, &dd.meta, pl.meta)) ||
         (rc = upload(h, &dd.metric, metric)) || (rc = upload(h, &dd.m0, m0)) ||
         (use_fs && (rc = upload(h, &dd.fsmask, fsmask)))) {
       h->in_mesh = false;
@@ -479,12 +538,6 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid, bool mesh_pa
   }
   if ((rc = upload(h, &dd.pts, pts))) return rc;
   if ((rc = upload(h, &dd.elinfo, elinfo))) return rc;
-  if (fluid && d->fluid_src && d->nelsrc > 0) {
-    std::vector<float> s((size_t)8 * 25, 0.f);
-    for (int k = 0; k < d->nelsrc; ++k)
-      for (int q = 0; q < 25; ++q) s[25 * k + q] = d->source_term_fl[q + 25 * k];
-    if ((rc = upload(h, &dd.srcfl, s))) return rc;
-  }
   return AXG_OK;
 }
 
@@ -572,6 +625,7 @@ StateArgs fluid_state(axg_handle *h) {
   s.cu[0] = h->kahan ? h->cu_f : nullptr;
   s.cv[0] = h->kahan ? h->cv_f : nullptr;
   s.u[0] = h->fu;
+  s.up[0] = lookahead(h) ? h->fup : nullptr;
   s.v[0] = h->fv;
   s.a[0] = h->fa;
   s.f[0] = h->ff;
@@ -588,8 +642,9 @@ StateArgs fluid_state(axg_handle *h) {
 // another scheme or mode since the last run).  The last writers keep it from
 // there on; recomputing it is exact, so runs in pieces match one run.
 cudaError_t refresh_predicted(axg_handle *h, cudaStream_t s) {
-  if (!lookahead(h) || h->nglob_s <= 0) return cudaSuccess;
-  predict_kernel<<<(unsigned)((h->nglob_s + 255) / 256), 256, 0, s>>>(solid_state(h));
+  if (!lookahead(h)) return cudaSuccess;
+  if (h->nglob_s > 0) predict_kernel<<<(unsigned)((h->nglob_s + 255) / 256), 256, 0, s>>>(solid_state(h));
+  if (h->nel_f > 0) predict_kernel<<<(unsigned)((h->nglob_f + 255) / 256), 256, 0, s>>>(fluid_state(h));
   return cudaGetLastError();
 }
 
@@ -605,7 +660,6 @@ DomainArgs domain_args(const DomainDev &dd, const DomainPlan &pl) {
   a.n_m0 = dd.n_m0;
   a.meta = dd.meta;
   a.pts = dd.pts;
-  a.elpts = dd.elpts;
   a.elinfo = dd.elinfo;
   a.metric = dd.metric;
   a.m0 = dd.m0;
@@ -660,36 +714,7 @@ int prepare_solid_kernels(axg_handle *h) {
                   : prepare_solid_kernel<POLE, MODE_NEWMARK, false, false>(h, c);
 }
 
-// the fluid kernels' dynamic shared memory (every variant a handle or a
-// batch may launch: Newmark or symplectic, plain or compensated)
-template <int NONMONO, bool KAHAN, bool SYMP, class P>
-int prepare_fluid_fn(axg_handle *h) {
-  auto fn = fluid_patch_kernel<NONMONO, KAHAN, SYMP, P>;
-  CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, FluidSmem<NONMONO, KAHAN>::bytes));
-  CK(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-  return AXG_OK;
-}
-
-template <int NONMONO>
-int prepare_fluid_kernels(axg_handle *h) {
-  int rc;
-  if ((rc = prepare_fluid_fn<NONMONO, false, false, One<PatchWork>>(h)) ||
-      (rc = prepare_fluid_fn<NONMONO, true, false, One<PatchWork>>(h)) ||
-      (rc = prepare_fluid_fn<NONMONO, false, true, One<PatchWork>>(h)) ||
-      (rc = prepare_fluid_fn<NONMONO, true, true, One<PatchWork>>(h)) ||
-      (rc = prepare_fluid_fn<NONMONO, false, false, Many<PatchWork>>(h)) ||
-      (rc = prepare_fluid_fn<NONMONO, true, false, Many<PatchWork>>(h)) ||
-      (rc = prepare_fluid_fn<NONMONO, false, true, Many<PatchWork>>(h)) ||
-      (rc = prepare_fluid_fn<NONMONO, true, true, Many<PatchWork>>(h)))
-    return rc;
-  return AXG_OK;
-}
-
 int prepare_kernels(axg_handle *h) {
-  if (h->nel_f > 0) {
-    const int rc = h->pole == AXG_MONOPOLE ? prepare_fluid_kernels<0>(h) : prepare_fluid_kernels<1>(h);
-    if (rc) return rc;
-  }
   if (h->pole == AXG_MONOPOLE) return prepare_solid_kernels<POLE_MONO>(h);
   if (h->pole == AXG_DIPOLE) return prepare_solid_kernels<POLE_DI>(h);
   return prepare_solid_kernels<POLE_QUAD>(h);
@@ -738,6 +763,51 @@ __global__ void zero_points_kernel(const int32_t *gidx, int32_t n, float *f0, fl
   f2[g] = 0.f;
 }
 
+FluidArgs fluid_args(axg_handle *h) {
+  const DomainDev &dd = h->df;
+  FluidArgs a{};
+  a.gidx = dd.gidx;
+  a.metric = dd.metric;
+  a.elinfo = dd.elinfo;
+  a.m0 = dd.m0;
+  a.fsmask = dd.fsmask;
+  a.srcfl = dd.srcfl;
+  a.start = dd.start;
+  a.ent = dd.ent;
+  a.fel = dd.fel;
+  a.nel = h->nel_f;
+  a.nglob = h->nglob_f;
+  a.n_m0 = dd.n_m0;
+  return a;
+}
+
+// CTAs of the fluid's element pass: a grid-stride loop of warps over the elements
+unsigned fluid_elem_grid(const axg_handle *h, int64_t nel) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((nel + kWarps - 1) / kWarps, 8 * (int64_t)h->num_sms));
+}
+
+// The fluid of a Newmark step or a symplectic stage: the element pass, then
+// the point pass.
+template <int NONMONO, int MODE, bool KAHAN>
+void launch_fluid_t(axg_handle *h, cudaStream_t s, const StateArgs &fs) {
+  FluidArgs fa = fluid_args(h);
+  if (MODE == MODE_SYMPLECTIC) fa.fsmask = nullptr;  // symplectic_time_loop applies no free-surface mask
+  fluid_elem_kernel<NONMONO, MODE, KAHAN>
+      <<<fluid_elem_grid(h, h->nel_f), kThreads, 0, s>>>(One<FluidWork>{{fa, fs}, (int32_t)h->nel_f}, h->spec);
+  fluid_point_kernel<NONMONO, MODE, KAHAN>
+      <<<(unsigned)((h->nglob_f + 255) / 256), 256, 0, s>>>(One<FluidWork>{{fa, fs}, (int32_t)h->nglob_f});
+}
+template <int MODE>
+void launch_fluid(axg_handle *h, cudaStream_t s, const StateArgs &fs) {
+  if (h->pole == AXG_MONOPOLE) {
+    if (h->kahan) launch_fluid_t<0, MODE, true>(h, s, fs);
+    else launch_fluid_t<0, MODE, false>(h, s, fs);
+  } else {
+    if (h->kahan) launch_fluid_t<1, MODE, true>(h, s, fs);
+    else launch_fluid_t<1, MODE, false>(h, s, fs);
+  }
+}
+
 void enqueue_force(axg_handle *h, cudaStream_t s) {
   if (h->to_solid.n > 0)
     zero_points_kernel<<<(h->to_solid.n + 255) / 256, 256, 0, s>>>(h->to_solid.pt_gidx, h->to_solid.n, h->sf[0],
@@ -760,19 +830,7 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
       if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(w);
       else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(w);
     }
-    DomainArgs a = domain_args(h->df, h->pf);
-    for (int c = 0; c < h->pf.n_colours; ++c) {
-      a.patch_begin = h->pf.colour_start[c];
-      const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
-      const One<PatchWork> w{{a, fs}, n};
-      if (h->pole == AXG_MONOPOLE) {
-        if (h->kahan) fluid_patch_kernel<0, true><<<n, kThreads, FluidSmem<0, true>::bytes, s>>>(w, h->spec);
-        else fluid_patch_kernel<0, false><<<n, kThreads, FluidSmem<0, false>::bytes, s>>>(w, h->spec);
-      } else {
-        if (h->kahan) fluid_patch_kernel<1, true><<<n, kThreads, FluidSmem<1, true>::bytes, s>>>(w, h->spec);
-        else fluid_patch_kernel<1, false><<<n, kThreads, FluidSmem<1, false>::bytes, s>>>(w, h->spec);
-      }
-    }
+    launch_fluid<MODE_NEWMARK>(h, s, fs);
     if (h->to_solid.n > 0) {
       const int nb = (h->to_solid.n + 255) / 256;
       const One<ToSolidWork> w{{h->to_solid, fs, ss}, h->to_solid.n};
@@ -854,20 +912,7 @@ void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
         if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(w);
         else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(w);
       }
-      DomainArgs a = domain_args(h->df, h->pf);
-      a.fsmask = nullptr;  // symplectic_time_loop applies no free-surface mask
-      for (int c = 0; c < h->pf.n_colours; ++c) {
-        a.patch_begin = h->pf.colour_start[c];
-        const int n = h->pf.colour_start[c + 1] - h->pf.colour_start[c];
-        const One<PatchWork> w{{a, fs}, n};
-        if (h->pole == AXG_MONOPOLE) {
-          if (h->kahan) fluid_patch_kernel<0, true, true><<<n, kThreads, FluidSmem<0, true>::bytes, s>>>(w, h->spec);
-          else fluid_patch_kernel<0, false, true><<<n, kThreads, FluidSmem<0, false>::bytes, s>>>(w, h->spec);
-        } else {
-          if (h->kahan) fluid_patch_kernel<1, true, true><<<n, kThreads, FluidSmem<1, true>::bytes, s>>>(w, h->spec);
-          else fluid_patch_kernel<1, false, true><<<n, kThreads, FluidSmem<1, false>::bytes, s>>>(w, h->spec);
-        }
-      }
+      launch_fluid<MODE_SYMPLECTIC>(h, s, fs);
       if (h->to_solid.n > 0) {
         const int nb = (h->to_solid.n + 255) / 256;
         const One<ToSolidWork> w{{h->to_solid, fs, ss}, h->to_solid.n};
@@ -1350,7 +1395,8 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
       return rc;
   }
   if (h->nel_f > 0) {
-    if ((rc = dalloc(h, &h->fu, h->nglob_f)) || (rc = dalloc(h, &h->fv, h->nglob_f)) ||
+    if ((rc = dalloc(h, &h->fu, h->nglob_f)) || (rc = dalloc(h, &h->fup, h->nglob_f)) ||
+        (rc = dalloc(h, &h->fv, h->nglob_f)) ||
         (rc = dalloc(h, &h->fa, h->nglob_f)) || (rc = dalloc(h, &h->ff, h->nglob_f)))
       return rc;
   }
@@ -1369,7 +1415,7 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
   if ((rc = prepare_kernels(h))) return rc;
   h->kernels_per_force = h->ps.n_colours + (h->to_solid.n > 0 ? 1 : 0);
   h->kernels_per_step = h->ps.n_colours + 1 +
-                        (h->nel_f > 0 ? h->pf.n_colours + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);
+                        (h->nel_f > 0 ? 2 + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);
   return axg_reset(h);
 }
 }  // namespace
@@ -2372,11 +2418,11 @@ int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages) 
   int rc = prepare_kernels(h);
   if (rc) return rc;
   if (h->scheme) {
-    h->kernels_per_step = (int64_t)h->nstages * (h->ps.n_colours + (h->nel_f > 0 ? h->pf.n_colours +
+    h->kernels_per_step = (int64_t)h->nstages * (h->ps.n_colours + (h->nel_f > 0 ? 2 +
                           (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0)) + 2 + (h->anel ? 1 : 0);
   } else {
     h->kernels_per_step = h->ps.n_colours + 1 +
-                          (h->nel_f > 0 ? h->pf.n_colours + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);
+                          (h->nel_f > 0 ? 2 + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);
   }
   return axg_reset(h);
 }
@@ -2727,31 +2773,34 @@ void stage_states(axg_handle *h, int stage, StateArgs &ss, StateArgs &fs) {
   }
 }
 
+// the fluid's two passes for the solves of a phase, per class (non-monopole, compensated)
 template <int NONMONO, bool KAHAN>
-int64_t batch_fluid_colour(axg_batch *b, int stage, int c, cudaStream_t s) {
-  return for_batches<PatchWork>(
-      b->hs,
-      [&](axg_handle *h) {
-        const bool mine = in_stage(h, stage) && h->nel_f > 0 && c < h->pf.n_colours &&
-                          (h->pole != AXG_MONOPOLE) == (NONMONO != 0) && h->kahan == KAHAN;
-        return mine ? h->pf.colour_start[c + 1] - h->pf.colour_start[c] : 0;
-      },
-      [&](axg_handle *h) {
-        DomainArgs a = domain_args(h->df, h->pf);
-        a.patch_begin = h->pf.colour_start[c];
-        if (stage >= 0) a.fsmask = nullptr;  // symplectic_time_loop applies no free-surface mask
-        StateArgs ss, fs;
-        stage_states(h, stage, ss, fs);
-        return PatchWork{a, fs};
-      },
-      [&](const Many<PatchWork> &m) {
-        if (stage < 0)
-          fluid_patch_kernel<NONMONO, KAHAN, false, Many<PatchWork>>
-              <<<m.start[m.n], kThreads, FluidSmem<NONMONO, KAHAN>::bytes, s>>>(m, b->spec);
-        else
-          fluid_patch_kernel<NONMONO, KAHAN, true, Many<PatchWork>>
-              <<<m.start[m.n], kThreads, FluidSmem<NONMONO, KAHAN>::bytes, s>>>(m, b->spec);
+int64_t batch_fluid(axg_batch *b, int stage, cudaStream_t s) {
+  auto mine = [&](axg_handle *h) {
+    return in_stage(h, stage) && h->nel_f > 0 && (h->pole != AXG_MONOPOLE) == (NONMONO != 0) && h->kahan == KAHAN;
+  };
+  auto work = [&](axg_handle *h) {
+    FluidArgs fa = fluid_args(h);
+    if (stage >= 0) fa.fsmask = nullptr;  // symplectic_time_loop applies no free-surface mask
+    StateArgs ss, fs;
+    stage_states(h, stage, ss, fs);
+    return FluidWork{fa, fs};
+  };
+  const int64_t ne = for_batches<FluidWork>(
+      b->hs, [&](axg_handle *h) { return mine(h) ? (int32_t)h->nel_f : 0; }, work,
+      [&](const Many<FluidWork> &m) {
+        const unsigned g = fluid_elem_grid(b->hs[0], m.start[m.n]);
+        if (stage < 0) fluid_elem_kernel<NONMONO, MODE_NEWMARK, KAHAN, Many<FluidWork>><<<g, kThreads, 0, s>>>(m, b->spec);
+        else fluid_elem_kernel<NONMONO, MODE_SYMPLECTIC, KAHAN, Many<FluidWork>><<<g, kThreads, 0, s>>>(m, b->spec);
       });
+  const int64_t np = for_batches<FluidWork>(
+      b->hs, [&](axg_handle *h) { return mine(h) ? (int32_t)h->nglob_f : 0; }, work,
+      [&](const Many<FluidWork> &m) {
+        const unsigned g = (unsigned)((m.start[m.n] + 255) / 256);
+        if (stage < 0) fluid_point_kernel<NONMONO, MODE_NEWMARK, KAHAN, Many<FluidWork>><<<g, 256, 0, s>>>(m);
+        else fluid_point_kernel<NONMONO, MODE_SYMPLECTIC, KAHAN, Many<FluidWork>><<<g, 256, 0, s>>>(m);
+      });
+  return ne + np;
 }
 
 // a solve's colour work with its attenuation data (attenuated batches)
@@ -2850,15 +2899,11 @@ int64_t batch_to_fluid(axg_batch *b, int stage, cudaStream_t s) {
 template <int MODE>
 int64_t enqueue_batch_phase(axg_batch *b, int stage, cudaStream_t s) {
   int64_t nl = batch_to_fluid<0>(b, stage, s) + batch_to_fluid<1>(b, stage, s);
-  int fc = 0, sc = 0;
-  for (axg_handle *h : b->hs) {
-    if (!in_stage(h, stage)) continue;
-    if (h->nel_f > 0) fc = std::max(fc, h->pf.n_colours);
-    sc = std::max(sc, h->ps.n_colours);
-  }
-  for (int c = 0; c < fc; ++c)
-    nl += batch_fluid_colour<0, false>(b, stage, c, s) + batch_fluid_colour<0, true>(b, stage, c, s) +
-          batch_fluid_colour<1, false>(b, stage, c, s) + batch_fluid_colour<1, true>(b, stage, c, s);
+  int sc = 0;
+  for (axg_handle *h : b->hs)
+    if (in_stage(h, stage)) sc = std::max(sc, h->ps.n_colours);
+  nl += batch_fluid<0, false>(b, stage, s) + batch_fluid<0, true>(b, stage, s) + batch_fluid<1, false>(b, stage, s) +
+        batch_fluid<1, true>(b, stage, s);
   nl += batch_to_solid<POLE_MONO>(b, stage, s) + batch_to_solid<POLE_DI>(b, stage, s) +
         batch_to_solid<POLE_QUAD>(b, stage, s);
   for (int c = 0; c < sc; ++c) nl += batch_solid_colours<MODE>(b, stage, c, s);
@@ -2892,6 +2937,7 @@ int64_t enqueue_batch_step(axg_batch *b, cudaStream_t s) {
 
 // kernel parameters are limited to 32764 bytes
 static_assert(sizeof(Many<PatchWork>) + sizeof(SpecDev) + sizeof(AnelBatch) <= 32000 &&
+                  sizeof(Many<FluidWork>) + sizeof(SpecDev) <= 32000 &&
                   sizeof(Many<ToSolidWork>) <= 32000 && sizeof(Many<DriftWork>) <= 32000 &&
                   sizeof(Many<ToFluidWork>) <= 32000 && sizeof(Many<RecWork>) <= 32000,
               "a batched launch's descriptors must fit the kernel parameter space");

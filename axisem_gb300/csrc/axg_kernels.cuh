@@ -100,7 +100,6 @@ struct SrcTable {           // solid source points (<= 200)
 struct DomainArgs {
   const PatchMeta *meta;
   const uint32_t *pts;
-  const uint16_t *elpts;
   const int32_t *elinfo;    // bits 0..23: axial slot + 1; bits 24..27: source slot + 1
   const float *metric;      // per element block_stride(nt) floats (launch order)
   const float *m0;          // per axial slot n_axial*5 floats
@@ -1329,221 +1328,156 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, true, KAHAN))
   solid_patch_body<POLE, MODE, true, KAHAN>(ManySolves{p, an.a}, sp);
 }
 
-// ------------------------------------------------------------ fluid patch kernel
+// ------------------------------------------------------------ fluid kernels
+//
+// The fluid step runs in two fully parallel passes instead of coloured
+// patches: the element pass computes every element's stiffness contribution
+// (glob_fluid_stiffness_4 with its source and masks) into a per-element
+// buffer, the point pass sums each global point's contributions in a fixed
+// order (the CSR of its (element, GLL point) copies: pdistsum_fluid) after
+// the coupling pre-pass's partial sum, and applies the corrector.  Both are
+// plain streams over HBM with no barriers, so the fluid's small element work
+// is no longer bound by the latency of patch-sized phases.
 
-// Shared-memory layout of the fluid patch kernel (dynamic): the patch's
-// element blocks (metric terms, BS floats each), their patch-local point
-// indices and info words, and the patch's points (chi, force, compensation,
-// point words).  Offsets in bytes, 16-byte aligned.
-template <int NONMONO, bool KAHAN>
-struct FluidSmem {
-  static constexpr int BS = block_stride(NONMONO ? 4 : 3);
-  static constexpr int el_off = 0;
-  static constexpr int el_bytes = kMaxPatchElems * BS * 4;
-  static constexpr int idx_off = el_off + el_bytes;
-  static constexpr int idx_bytes = ((kMaxPatchElems * 25 * 2 + 15) / 16) * 16;
-  static constexpr int info_off = idx_off + idx_bytes;
-  static constexpr int info_bytes = kMaxPatchElems * 4;
-  static constexpr int u_off = info_off + info_bytes;
-  static constexpr int pt_bytes = kMaxPatchPoints * 4;
-  static constexpr int f_off = u_off + pt_bytes;
-  static constexpr int w_off = f_off + pt_bytes;
-  static constexpr int c_off = w_off + pt_bytes;
-  static constexpr int bar_off = c_off + (KAHAN ? pt_bytes : 0);
-  static constexpr int bytes = bar_off + 16;
+struct FluidArgs {
+  const int32_t *gidx;     // per element slot (launch order): its 25 global points
+  const float *metric;     // per element slot block_stride(nt) floats: M1chi, M2chi, M4chi [, M_w_fl]
+  const int32_t *elinfo;   // per element slot: bits 0..23 axial slot + 1, bits 24..27 source slot + 1
+  const float *m0;         // per axial slot 5 floats (M0_w_fl)
+  const float *fsmask;     // per element slot 25 floats (fluid free-surface mask) or null
+  const float *srcfl;      // fluid source terms (8, 25) or null
+  const int32_t *start;    // nglob + 1: each point's first copy in ent; bit 31 of start[g]: the point
+                           // holds a coupling pre-pass partial sum (in the force array); bit 30: on the axis
+  const int32_t *ent;      // 25 nel: element slot * 25 + GLL point of each copy, points in order
+  float *fel;              // 25 nel: the element contributions of the step
+  int64_t nel, nglob, n_m0;  // extents (checked builds)
+};
+constexpr uint32_t kFlPartial = 1u << 31, kFlAxis = 1u << 30, kFlStartMask = kFlAxis - 1u;
+
+struct FluidWork {
+  FluidArgs fa;
+  StateArgs st;
 };
 
-// One CTA per patch (per work item: a patch of one of the solves).  Thread 0
-// starts one bulk copy of the patch's element blocks (contiguous in launch
-// order) into shared memory; meanwhile every thread loads the element
-// indices and info words, and gathers each point's chi, dchi, ddchi0 (and the
-// partial sum of an earlier writer) in one batch of loads, applying the
-// predictor.  The sub-rounds then read everything from shared memory, and the
-// write-back loads the last writers' inverse mass, dchi and ddchi0 in one
-// batch before it stores.
-template <int NONMONO, bool KAHAN, bool SYMP = false, class P = One<PatchWork>>
-__global__ void __launch_bounds__(kThreads, 4) fluid_patch_kernel(const __grid_constant__ P p, SpecDev sp) {
-  using L = FluidSmem<NONMONO, KAHAN>;
-  constexpr int BS = L::BS;
+// chi at the step's gather point: the plain Newmark step's stored prediction,
+// the compensated predictor, a symplectic stage's drift (compensated or not)
+template <int MODE, bool KAHAN>
+__device__ __forceinline__ float fluid_predicted(const StateArgs &st, int64_t g, float &k) {
+  if (KAHAN) {
+    k = st.cu[0][g];
+    return predict_comp(st.u[0][g], st.v[0][g], MODE == MODE_SYMPLECTIC ? 0.f : st.a[0][g], st.dt, st.hdt2, k);
+  }
+  if (MODE == MODE_SYMPLECTIC) return fmaf(st.dt, st.v[0][g], st.u[0][g]);  // chi + dchi * coefd(i)
+  return st.up[0][g];
+}
+
+// Element pass: one warp per element (items: the elements of the solves),
+// lane = GLL point; chi gathered with the predictor, the element's
+// stiffness, source, axial mask and free-surface mask, stored per copy.
+template <int NONMONO, int MODE, bool KAHAN, class P = One<FluidWork>>
+__global__ void __launch_bounds__(kThreads) fluid_elem_kernel(const __grid_constant__ P p, SpecDev sp) {
   constexpr int NT = NONMONO ? 4 : 3;
-  if ((int32_t)blockIdx.x >= p.items()) return;  // uniform across the CTA
-  const int sv = p.locate(blockIdx.x);
-  const DomainArgs &d = p.at(sv).d;
-  const StateArgs &st = p.at(sv).st;
-  const int pp = blockIdx.x - p.first(sv);
-  extern __shared__ __align__(128) unsigned char smem[];
-  float *s_el = reinterpret_cast<float *>(smem + L::el_off);
-  uint16_t *s_idx = reinterpret_cast<uint16_t *>(smem + L::idx_off);
-  int32_t *s_info = reinterpret_cast<int32_t *>(smem + L::info_off);
-  float *s_u = reinterpret_cast<float *>(smem + L::u_off);
-  float *s_f = reinterpret_cast<float *>(smem + L::f_off);
-  uint32_t *s_w = reinterpret_cast<uint32_t *>(smem + L::w_off);
-  float *s_cu = reinterpret_cast<float *>(smem + L::c_off);  // compensated mode only
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::bar_off);
-  constexpr int kGB = (kMaxPatchPoints + kThreads - 1) / kThreads;  // points per thread: one batch per patch
-  __shared__ int s_stop;
-  __shared__ int s_timeout;
-  if (threadIdx.x == 0) {
-    s_stop = *st.blowup;
-    s_timeout = 0;
-    mbar_init(bar, 1);
-  }
-  fence_mbar_init();
-  __syncthreads();
-  if (s_stop) return;  // uniform across the CTA; no copy has been issued
-  if (!AXG_BOUND(d.patch_begin + pp, d.n_patches, 11)) return;
-  const PatchMeta m = d.meta[d.patch_begin + pp];
-  const int ne = m.n_elems;
-  const bool elems_ok = ne >= 1 && ne <= kMaxPatchElems && AXG_BOUND((int64_t)m.elem_start + ne - 1, d.n_elem, 12);
-  // 1. the patch's element blocks: one bulk copy (each block is BS floats, a
-  //    multiple of 16 bytes, from a 16-byte aligned base)
-  if (threadIdx.x == 0) {
-    if (elems_ok) bulk_g2s(s_el, d.metric + (int64_t)m.elem_start * BS, (uint32_t)(ne * BS * 4), bar,
-                           policy_evict_first());
-    else mbar_arrive(bar);
-  }
-  // element point indices and info words
-  if (elems_ok) {
-    for (int t = threadIdx.x; t < ne * 25; t += kThreads) s_idx[t] = __ldcs(d.elpts + (int64_t)m.elem_start * 25 + t);
-    for (int t = threadIdx.x; t < ne; t += kThreads) s_info[t] = __ldg(d.elinfo + m.elem_start + t);
-  }
-  // 2. gather with the predictor on the fly
-  {
-    uint32_t w[kGB];
-    float uu[kGB], ff[kGB], cc[KAHAN ? kGB : 1];
-#pragma unroll
-    for (int q = 0; q < kGB; ++q) {
-      const int t = threadIdx.x + q * kThreads;
-      w[q] = (t < m.n_pts && AXG_BOUND(m.pt_start + t, d.n_pts, 11)) ? d.pts[m.pt_start + t] : kPtPad;
-    }
-#pragma unroll
-    for (int q = 0; q < kGB; ++q) {
-      const uint32_t g = w[q] & kPtIndexMask;
-      const bool ok = w[q] != kPtPad && AXG_BOUND(g, st.nglob, 11);
-      if (KAHAN) {
-        float k = ok ? st.cu[0][g] : 0.f;
-        uu[q] = ok ? predict_comp(st.u[0][g], st.v[0][g], SYMP ? 0.f : st.a[0][g], st.dt, st.hdt2, k) : 0.f;
-        cc[KAHAN ? q : 0] = k;
-      } else if (SYMP) {
-        uu[q] = ok ? fmaf(st.dt, st.v[0][g], st.u[0][g]) : 0.f;  // drift: chi + dchi * coefd(i)
-      } else {
-        uu[q] = ok ? predict(st.u[0][g], st.v[0][g], st.a[0][g], st.dt, st.hdt2) : 0.f;
-      }
-      // a point an earlier writer (coupling pre-pass, earlier colour) holds a
-      // partial sum for starts from that sum: the write-back only stores
-      ff[q] = ok && !(w[q] & kPtFirst) ? st.f[0][g] : 0.f;
-    }
-#pragma unroll
-    for (int q = 0; q < kGB; ++q) {
-      const int t = threadIdx.x + q * kThreads;
-      if (t < m.n_pts) {
-        s_w[t] = w[q];
-        s_u[t] = uu[q];
-        s_f[t] = ff[q];
-        if (KAHAN) s_cu[t] = cc[KAHAN ? q : 0];
-      }
-    }
-  }
-  if (!mbar_wait_bounded(bar, 0u, st.err)) s_timeout = 1;
-  __syncthreads();
+  constexpr int BS = block_stride(NT);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool active = lane < 25;
-  const int i = lane % 5, j = active ? lane / 5 : 0;
-  // idle lanes 25..31 take part in the shuffles; their reads of an element's
-  // data go to point 24
+  // idle lanes 25..31 take part in the shuffles; their reads go to point 24
   const int ml = active ? lane : 24;
+  const int i = ml % 5, j = ml / 5;
   LaneCoef coef;
   load_coef(sp, i, j, coef);
-  const float stf1 = AXG_BOUND(*st.iter - 1, st.niter, 12) ? st.stf[*st.iter - 1] : 0.f;
-  const PatchRounds pr(m);
-  // 3. elements, sub-round by sub-round, from shared memory
-  int r0 = 0;
-  for (int r = 0; r < pr.n; ++r) {
-    const int r1 = pr.end(r);
-    for (int s = r0 + warp; s < r1 && elems_ok; s += kWarps) {
-      const float *blk = s_el + s * BS;
-      float mt[4];
+  if (!P::kMany && *p.at(0).st.blowup) return;  // uniform across the CTA
+  const int32_t n = p.items();
+  for (int32_t it = blockIdx.x * kWarps + warp; it < n; it += gridDim.x * kWarps) {
+    const int sv = p.locate(it);
+    const FluidArgs &f = p.at(sv).fa;
+    const StateArgs &st = p.at(sv).st;
+    if (P::kMany && *st.blowup) continue;  // uniform across the warp
+    const int64_t el = it - p.first(sv);
+    if (!AXG_BOUND(el, f.nel, 14)) continue;
+    int32_t g = f.gidx[el * 25 + ml];
+    if (!AXG_BOUND(g, st.nglob, 14)) g = 0;
+    float kc = 0.f;
+    float chi = fluid_predicted<MODE, KAHAN>(st, g, kc);
+    const int32_t info = f.elinfo[el];
+    int axslot = (info & 0xFFFFFF) - 1;
+    if (axslot >= 0 && !AXG_BOUND((int64_t)axslot * 5 + 4, f.n_m0, 14)) axslot = -1;
+    const int srcslot = ((info >> 24) & 0xF) - 1;
+    const bool ax = axslot >= 0;
+    if (NONMONO && ax && i == 0) chi = 0.f;  // apply_axis_mask_scal(chi)
+    float mt[4];
 #pragma unroll
-      for (int t = 0; t < 4; ++t) mt[t] = t < NT ? blk[t * 25 + ml] : 0.f;
-      const int32_t info = s_info[s];
-      int idx = active ? s_idx[s * 25 + lane] : 0;
-      if (!AXG_BOUND(idx, m.n_pts, 12)) idx = 0;
-      const int64_t el = (int64_t)m.elem_start + s;
-      int axslot = (info & 0xFFFFFF) - 1;
-      if (axslot >= 0 && !AXG_BOUND((int64_t)(axslot + 1) * 5 - 1, d.n_m0, 12)) axslot = -1;
-      const int srcslot = ((info >> 24) & 0xF) - 1;
-      const bool ax = axslot >= 0;
-      float chi = active ? s_u[idx] : 0.f;
-      if (NONMONO && ax && i == 0) chi = 0.f;  // apply_axis_mask_scal(chi)
-      const float *m0 = ax ? d.m0 + (int64_t)axslot * 5 : nullptr;
-      float f = ax ? stiff_fluid<true, NONMONO>(coef, mt, m0, i, j, chi)
-                   : stiff_fluid<false, NONMONO>(coef, mt, m0, i, j, chi);
-      if (srcslot >= 0 && stf1 != 0.f && active) f = f - d.srcfl[srcslot * 25 + lane] * stf1;
-      if (NONMONO && ax && i == 0) f = 0.f;
-      if (d.fsmask && active) f = f * d.fsmask[el * 25 + lane];
-      if (active) s_f[idx] += f;
+    for (int t = 0; t < 4; ++t) mt[t] = t < NT ? f.metric[el * BS + t * 25 + ml] : 0.f;
+    const float *m0 = ax ? f.m0 + (int64_t)axslot * 5 : nullptr;
+    float fv = ax ? stiff_fluid<true, NONMONO>(coef, mt, m0, i, j, chi)
+                  : stiff_fluid<false, NONMONO>(coef, mt, m0, i, j, chi);
+    if (srcslot >= 0 && f.srcfl && active) {
+      const float stf1 = AXG_BOUND(*st.iter - 1, st.niter, 14) ? st.stf[*st.iter - 1] : 0.f;
+      if (stf1 != 0.f) fv = fv - f.srcfl[srcslot * 25 + lane] * stf1;
     }
-    r0 = r1;
-    __syncthreads();
+    if (NONMONO && ax && i == 0) fv = 0.f;
+    if (f.fsmask && active) fv = fv * f.fsmask[el * 25 + lane];
+    if (active) f.fel[el * 25 + lane] = fv;
   }
-  // 4. write-back
-  {
-    uint32_t w[kGB];
-    float vel[kGB], acc[kGB], im[kGB], gam[kGB], kv[KAHAN ? kGB : 1];
-    double imd[KAHAN ? kGB : 1];  // compensated mode: the FP64 inverse mass, when the handle has it
-#pragma unroll
-    for (int q = 0; q < kGB; ++q) {
-      const int t = threadIdx.x + q * kThreads;
-      w[q] = t < m.n_pts ? s_w[t] : kPtPad;
-      const uint32_t g = w[q] & kPtIndexMask;
-      const bool last = w[q] != kPtPad && (w[q] & kPtLast) && AXG_BOUND(g, st.nglob, 13);
-      im[q] = last ? st.inv_mass[g] : 0.f;
-      if (KAHAN) imd[KAHAN ? q : 0] = last && st.inv_mass_dp ? st.inv_mass_dp[g] : 0.0;
-      gam[q] = last && st.gamma ? st.gamma[g] : 0.f;
-      vel[q] = last ? st.v[0][g] : 0.f;
-      acc[q] = last && !SYMP ? st.a[0][g] : 0.f;
-      if (KAHAN) kv[KAHAN ? q : 0] = last ? st.cv[0][g] : 0.f;
-    }
-#pragma unroll
-    for (int q = 0; q < kGB; ++q) {
-      const int t = threadIdx.x + q * kThreads;
-      if (w[q] == kPtPad) continue;
-      const uint32_t g = w[q] & kPtIndexMask;
-      if (!AXG_BOUND(g, st.nglob, 13)) continue;
-      const float v = s_f[t];
-      if (!(w[q] & kPtLast)) {
-        st.f[0][g] = v;
-        continue;
-      }
-      float a = -im[q] * v;
-      if (KAHAN && st.inv_mass_dp) a = (float)(-imd[KAHAN ? q : 0] * (double)v);  // FP64, one rounding
-      const float chi = s_u[t];
-      if (st.gamma) a = a - 2.f * gam[q] * vel[q] - gam[q] * gam[q] * chi;
-      if (SYMP && KAHAN) {
-        float k = kv[KAHAN ? q : 0];
-        st.v[0][g] = kahan_add(vel[q], st.kick * a, k);  // dchi + coefv(i) * ddchi, compensated
-        st.cv[0][g] = k;
-        st.cu[0][g] = s_cu[t];
-      } else if (SYMP) {
-        st.v[0][g] = fmaf(st.kick, a, vel[q]);  // dchi + coefv(i) * ddchi
-      } else if (KAHAN) {
-        float k = kv[KAHAN ? q : 0];
-        st.v[0][g] = kahan_add(vel[q], st.hdt * (acc[q] + a), k);
-        st.cv[0][g] = k;
-        st.cu[0][g] = s_cu[t];
-      } else {
-        st.v[0][g] = fmaf(st.hdt, acc[q] + a, vel[q]);
-      }
-      st.a[0][g] = a;
-      // apply_axis_mask_scal zeroes chi on the axis (non-monopole)
-      const bool zero = NONMONO && (w[q] & kPtAxis);
-      st.u[0][g] = zero ? 0.f : chi;
-      if (KAHAN && zero) st.cu[0][g] = 0.f;
-    }
+}
+
+// Point pass: one thread per global point (items: the points of the
+// solves).  The point's force is the coupling partial sum (if any) plus its
+// copies' contributions in CSR order; then the corrector, as the last writer
+// of the patch kernels applies it: ddchi = -inv_mass_fluid * force [-
+// absorbing terms], dchi by the Newmark corrector or a symplectic kick, chi
+// (zero on the axis for the non-monopole sources) and the next step's
+// prediction stored.
+template <int NONMONO, int MODE, bool KAHAN, class P = One<FluidWork>>
+__global__ void __launch_bounds__(256) fluid_point_kernel(const __grid_constant__ P p) {
+  const int32_t it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= p.items()) return;
+  const int sv = p.locate(it);
+  const FluidArgs &f = p.at(sv).fa;
+  const StateArgs &st = p.at(sv).st;
+  if (*st.blowup) return;
+  const int64_t g = it - p.first(sv);
+  if (!AXG_BOUND(g, f.nglob, 15)) return;
+  const uint32_t s0 = (uint32_t)f.start[g], s1 = (uint32_t)f.start[g + 1] & kFlStartMask;
+  float sum = (s0 & kFlPartial) ? st.f[0][g] : 0.f;
+  for (uint32_t k = s0 & kFlStartMask; k < s1; ++k) {
+    const int32_t e = f.ent[k];
+    if (!AXG_BOUND(e, 25 * f.nel, 15)) break;
+    sum = sum + f.fel[e];
   }
-  // after a timeout the bulk copy may still be in flight: wait (bounded)
-  // for it before the CTA exits
-  if (s_timeout && threadIdx.x == 0) mbar_drain(bar, 0u);
+  float kc = 0.f;
+  const float chi = fluid_predicted<MODE, KAHAN>(st, g, kc);
+  const float vel = st.v[0][g];
+  float a = -st.inv_mass[g] * sum;
+  if (KAHAN && st.inv_mass_dp) a = (float)(-st.inv_mass_dp[g] * (double)sum);  // FP64, one rounding
+  if (st.gamma) {
+    const float gam = st.gamma[g];
+    a = a - 2.f * gam * vel - gam * gam * chi;
+  }
+  float vn;
+  if (MODE == MODE_SYMPLECTIC) {
+    if (KAHAN) {
+      float k = st.cv[0][g];
+      vn = kahan_add(vel, st.kick * a, k);  // dchi + coefv(i) * ddchi, compensated
+      st.cv[0][g] = k;
+    } else {
+      vn = fmaf(st.kick, a, vel);  // dchi + coefv(i) * ddchi
+    }
+  } else if (KAHAN) {
+    float k = st.cv[0][g];
+    vn = kahan_add(vel, st.hdt * (st.a[0][g] + a), k);
+    st.cv[0][g] = k;
+  } else {
+    vn = fmaf(st.hdt, st.a[0][g] + a, vel);
+  }
+  st.v[0][g] = vn;
+  st.a[0][g] = a;
+  // apply_axis_mask_scal zeroes chi on the axis (non-monopole)
+  const bool zero = NONMONO && (s0 & kFlAxis);
+  const float un = zero ? 0.f : chi;
+  st.u[0][g] = un;
+  if (KAHAN) st.cu[0][g] = zero ? 0.f : kc;
+  // the next step's predictor (plain Newmark)
+  if (MODE == MODE_NEWMARK && !KAHAN) st.up[0][g] = predict(un, vn, a, st.dt, st.hdt2);
 }
 
 // The final drift of a symplectic step (SOLVER/time_evol_wave.F90:722-727):

@@ -36,7 +36,9 @@ def long_run_misfits():
     fx = np.load(FIXTURE)
     m = sphere.long_run_mesh(int(fx["niter"]))
     assert (m.nel_solid, m.nel_fluid, m.seis_it) == (int(fx["nel_solid"]), int(fx["nel_fluid"]), int(fx["seis_it"]))
-    assert m.deltat == float(fx["deltat"])
+    # the mesh is rebuilt here: its FP64 precompute may differ from the
+    # fixture's machine in the last bits of transcendental functions
+    assert abs(m.deltat - float(fx["deltat"])) <= 1e-12 * m.deltat
     ref = fx["rec_float64"]
     out, secs = {}, {}
     for mode in ("plain", "compensated"):
