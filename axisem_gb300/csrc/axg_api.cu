@@ -17,6 +17,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <utility>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -720,6 +721,26 @@ int prepare_kernels(axg_handle *h) {
   return prepare_solid_kernels<POLE_QUAD>(h);
 }
 
+// A launch with programmatic stream serialization: the kernel may start
+// while the one ahead of it in the stream finishes (it waits in pdl_wait()
+// before reading what that kernel writes).  Used for the kernels of the
+// stiffness step and of the Newmark step, which all call pdl_wait().
+template <class... KArgs, class... Args>
+void launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                Args &&...args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 template <int POLE, int MODE, bool ANEL, bool KAHAN>
 void launch_solid_colours(axg_handle *h, cudaStream_t s) {
   DomainArgs a = domain_args(h->ds, h->ps);
@@ -729,8 +750,8 @@ void launch_solid_colours(axg_handle *h, cudaStream_t s) {
     a.patch_begin = h->ps.colour_start[c];
     const int n = h->ps.colour_start[c + 1] - h->ps.colour_start[c];
     const int grid = std::min(n, ctas);
-    solid_patch_kernel<POLE, MODE, ANEL, KAHAN>
-        <<<grid, kThreads, solid_smem_bytes<POLE, MODE, ANEL, KAHAN>(), s>>>(a, st, h->spec, n, h->an);
+    launch_pdl(solid_patch_kernel<POLE, MODE, ANEL, KAHAN>, grid, kThreads, solid_smem_bytes<POLE, MODE, ANEL, KAHAN>(),
+               s, a, st, h->spec, n, h->an);
   }
 }
 
@@ -792,10 +813,10 @@ template <int NONMONO, int MODE, bool KAHAN>
 void launch_fluid_t(axg_handle *h, cudaStream_t s, const StateArgs &fs) {
   FluidArgs fa = fluid_args(h);
   if (MODE == MODE_SYMPLECTIC) fa.fsmask = nullptr;  // symplectic_time_loop applies no free-surface mask
-  fluid_elem_kernel<NONMONO, MODE, KAHAN>
-      <<<fluid_elem_grid(h, h->nel_f), kThreads, 0, s>>>(One<FluidWork>{{fa, fs}, (int32_t)h->nel_f}, h->spec);
-  fluid_point_kernel<NONMONO, MODE, KAHAN>
-      <<<(unsigned)((h->nglob_f + 255) / 256), 256, 0, s>>>(One<FluidWork>{{fa, fs}, (int32_t)h->nglob_f});
+  launch_pdl(fluid_elem_kernel<NONMONO, MODE, KAHAN, One<FluidWork>>, fluid_elem_grid(h, h->nel_f), kThreads, 0, s,
+             One<FluidWork>{{fa, fs}, (int32_t)h->nel_f}, h->spec);
+  launch_pdl(fluid_point_kernel<NONMONO, MODE, KAHAN, One<FluidWork>>, (unsigned)((h->nglob_f + 255) / 256), 256, 0,
+             s, One<FluidWork>{{fa, fs}, (int32_t)h->nglob_f});
 }
 template <int MODE>
 void launch_fluid(axg_handle *h, cudaStream_t s, const StateArgs &fs) {
@@ -825,22 +846,22 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
   StateArgs ss = solid_state(h), fs = fluid_state(h);
   if (h->nel_f > 0) {
     if (h->to_fluid.n > 0) {
-      const int nb = (h->to_fluid.n + 255) / 256;
+      const unsigned nb = (h->to_fluid.n + 255) / 256;
       const One<ToFluidWork> w{{h->to_fluid, ss, h->ff}, h->to_fluid.n};
-      if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(w);
-      else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(w);
+      if (h->pole == AXG_DIPOLE) launch_pdl(couple_to_fluid_kernel<1, One<ToFluidWork>>, nb, 256, 0, s, w);
+      else launch_pdl(couple_to_fluid_kernel<0, One<ToFluidWork>>, nb, 256, 0, s, w);
     }
     launch_fluid<MODE_NEWMARK>(h, s, fs);
     if (h->to_solid.n > 0) {
-      const int nb = (h->to_solid.n + 255) / 256;
+      const unsigned nb = (h->to_solid.n + 255) / 256;
       const One<ToSolidWork> w{{h->to_solid, fs, ss}, h->to_solid.n};
-      if (h->pole == AXG_MONOPOLE) couple_to_solid_kernel<POLE_MONO><<<nb, 256, 0, s>>>(w);
-      else if (h->pole == AXG_DIPOLE) couple_to_solid_kernel<POLE_DI><<<nb, 256, 0, s>>>(w);
-      else couple_to_solid_kernel<POLE_QUAD><<<nb, 256, 0, s>>>(w);
+      if (h->pole == AXG_MONOPOLE) launch_pdl(couple_to_solid_kernel<POLE_MONO, One<ToSolidWork>>, nb, 256, 0, s, w);
+      else if (h->pole == AXG_DIPOLE) launch_pdl(couple_to_solid_kernel<POLE_DI, One<ToSolidWork>>, nb, 256, 0, s, w);
+      else launch_pdl(couple_to_solid_kernel<POLE_QUAD, One<ToSolidWork>>, nb, 256, 0, s, w);
     }
   }
   launch_solid<MODE_NEWMARK>(h, s);
-  receivers_kernel<<<1, 256, 0, s>>>(One<RecWork>{rec_work(h, ss), 1});
+  launch_pdl(receivers_kernel<One<RecWork>>, 1, 256, 0, s, One<RecWork>{rec_work(h, ss), 1});
 }
 
 // One step of symplectic_time_loop (SOLVER/time_evol_wave.F90:587-727):

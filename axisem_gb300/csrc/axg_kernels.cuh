@@ -804,6 +804,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
   if (threadIdx.x < kWarps * STG) mbar_init(&bars[threadIdx.x], 1);
   if (threadIdx.x < kMaxSubrounds) mbar_init(&s_round[threadIdx.x], kThreads);
   if (threadIdx.x < 2) mbar_init(&s_wbar[threadIdx.x], 1);
+  pdl_wait();  // the step's earlier kernels are complete
   // one solve: nothing to do after a blow-up (a batch checks per solve below)
   if (threadIdx.x == 0) s_stop = TL && !P::kMany ? *p.state(0).blowup : 0;
   if (threadIdx.x == 0) s_timeout = 0;
@@ -900,6 +901,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
   }
 
   for (int32_t it = blockIdx.x; it < p.items(); it += gridDim.x) {
+    if (it + (int32_t)gridDim.x >= p.items()) pdl_trigger();  // this CTA's last item: the next kernel may start
     // the work item's solve and patch
     const int sv = p.locate(it);
     const DomainArgs &d = p.dom(sv);
@@ -1374,8 +1376,10 @@ __device__ __forceinline__ float fluid_predicted(const StateArgs &st, int64_t g,
 // Element pass: one warp per element (items: the elements of the solves),
 // lane = GLL point; chi gathered with the predictor, the element's
 // stiffness, source, axial mask and free-surface mask, stored per copy.
+// Each warp loads its next element's points, metric terms and info word
+// before it computes the current one.
 template <int NONMONO, int MODE, bool KAHAN, class P = One<FluidWork>>
-__global__ void __launch_bounds__(kThreads) fluid_elem_kernel(const __grid_constant__ P p, SpecDev sp) {
+__global__ void __launch_bounds__(kThreads, 3) fluid_elem_kernel(const __grid_constant__ P p, SpecDev sp) {
   constexpr int NT = NONMONO ? 4 : 3;
   constexpr int BS = block_stride(NT);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1385,28 +1389,48 @@ __global__ void __launch_bounds__(kThreads) fluid_elem_kernel(const __grid_const
   const int i = ml % 5, j = ml / 5;
   LaneCoef coef;
   load_coef(sp, i, j, coef);
+  pdl_wait();
+  pdl_trigger();
   if (!P::kMany && *p.at(0).st.blowup) return;  // uniform across the CTA
-  const int32_t n = p.items();
-  for (int32_t it = blockIdx.x * kWarps + warp; it < n; it += gridDim.x * kWarps) {
+  const int32_t n = p.items(), stride = gridDim.x * kWarps;
+  // an element's loads that do not depend on its state
+  struct Pre {
+    int32_t g, info;
+    float mt[4];
+  };
+  auto load = [&](int32_t it, Pre &q) {
+    const int sv = p.locate(it);
+    const FluidArgs &f = p.at(sv).fa;
+    int64_t el = it - p.first(sv);
+    if (!AXG_BOUND(el, f.nel, 14)) el = 0;
+    q.g = f.gidx[el * 25 + ml];
+    q.info = f.elinfo[el];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) q.mt[t] = t < NT ? f.metric[el * BS + t * 25 + ml] : 0.f;
+  };
+  Pre nx{};
+  int32_t it = blockIdx.x * kWarps + warp;
+  if (it < n) load(it, nx);
+  for (; it < n; it += stride) {
+    const Pre cur = nx;
+    if (it + stride < n) load(it + stride, nx);
     const int sv = p.locate(it);
     const FluidArgs &f = p.at(sv).fa;
     const StateArgs &st = p.at(sv).st;
     if (P::kMany && *st.blowup) continue;  // uniform across the warp
     const int64_t el = it - p.first(sv);
-    if (!AXG_BOUND(el, f.nel, 14)) continue;
-    int32_t g = f.gidx[el * 25 + ml];
+    int32_t g = cur.g;
     if (!AXG_BOUND(g, st.nglob, 14)) g = 0;
     float kc = 0.f;
     float chi = fluid_predicted<MODE, KAHAN>(st, g, kc);
-    const int32_t info = f.elinfo[el];
-    int axslot = (info & 0xFFFFFF) - 1;
+    int axslot = (cur.info & 0xFFFFFF) - 1;
     if (axslot >= 0 && !AXG_BOUND((int64_t)axslot * 5 + 4, f.n_m0, 14)) axslot = -1;
-    const int srcslot = ((info >> 24) & 0xF) - 1;
+    const int srcslot = ((cur.info >> 24) & 0xF) - 1;
     const bool ax = axslot >= 0;
     if (NONMONO && ax && i == 0) chi = 0.f;  // apply_axis_mask_scal(chi)
     float mt[4];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) mt[t] = t < NT ? f.metric[el * BS + t * 25 + ml] : 0.f;
+    for (int t = 0; t < 4; ++t) mt[t] = cur.mt[t];
     const float *m0 = ax ? f.m0 + (int64_t)axslot * 5 : nullptr;
     float fv = ax ? stiff_fluid<true, NONMONO>(coef, mt, m0, i, j, chi)
                   : stiff_fluid<false, NONMONO>(coef, mt, m0, i, j, chi);
@@ -1429,6 +1453,8 @@ __global__ void __launch_bounds__(kThreads) fluid_elem_kernel(const __grid_const
 // prediction stored.
 template <int NONMONO, int MODE, bool KAHAN, class P = One<FluidWork>>
 __global__ void __launch_bounds__(256) fluid_point_kernel(const __grid_constant__ P p) {
+  pdl_wait();
+  pdl_trigger();
   const int32_t it = blockIdx.x * blockDim.x + threadIdx.x;
   if (it >= p.items()) return;
   const int sv = p.locate(it);
@@ -1545,6 +1571,8 @@ struct ToFluidWork {
 };
 template <int DIPOLE, class P = One<ToFluidWork>>
 __global__ void couple_to_fluid_kernel(const __grid_constant__ P p) {
+  pdl_wait();
+  pdl_trigger();
   const int32_t it = blockIdx.x * blockDim.x + threadIdx.x;  // a receiving point of one of the solves
   if (it >= p.items()) return;
   const int sv = p.locate(it);
@@ -1587,6 +1615,8 @@ struct ToSolidWork {
 };
 template <int POLE, class P = One<ToSolidWork>>
 __global__ void couple_to_solid_kernel(const __grid_constant__ P p) {
+  pdl_wait();
+  pdl_trigger();
   const int32_t it = blockIdx.x * blockDim.x + threadIdx.x;
   if (it >= p.items()) return;
   const int sv = p.locate(it);
@@ -1632,6 +1662,8 @@ struct RecWork {
 };
 template <class P = One<RecWork>>
 __global__ void receivers_kernel(const __grid_constant__ P p) {
+  pdl_wait();
+  pdl_trigger();
   if ((int32_t)blockIdx.x >= p.items()) return;
   const RecWork &rw = p.at(p.locate(blockIdx.x));
   const StateArgs &solid = rw.solid;

@@ -24,6 +24,16 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization may start before the kernel ahead of it in the stream has
+// finished: pdl_wait() returns once that kernel has completed and its
+// writes are visible (a no-op for an ordinary launch), so every kernel of a
+// time step calls it before its first read of data the step writes.
+// pdl_trigger() lets the next kernel's CTAs be scheduled once every CTA of
+// this one has called it (or exited); they run up to their own pdl_wait().
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
