@@ -15,7 +15,7 @@ import numpy as np
 PKG_DIR = Path(__file__).resolve().parent
 LIB_PATH = PKG_DIR / "_build" / "libaxisem_gb300.so"
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 NPOL = 4
 
 # status codes (enum axg_status)
@@ -109,6 +109,11 @@ class MeshDesc(C.Structure):
         ("DsDxi_over_J_sol_cg4", _fp), ("DzDxi_over_J_sol_cg4", _fp),
         ("inv_s_solid", _fp),
         ("inv_mass_rho_dp", _dp), ("inv_mass_fluid_dp", _dp), ("source_term_el_dp", _dp),
+        ("delta_mu", _fp), ("delta_kappa", _fp),
+        ("Y", _fp), ("V_s_eta", _fp), ("V_s_xi", _fp), ("V_z_eta", _fp), ("V_z_xi", _fp),
+        ("Y0", _fp), ("V0_s_eta", _fp), ("V0_s_xi", _fp), ("V0_z_eta", _fp), ("V0_z_xi", _fp),
+        ("DsDeta_over_J_sol", _fp), ("DzDeta_over_J_sol", _fp),
+        ("DsDxi_over_J_sol", _fp), ("DzDxi_over_J_sol", _fp),
     ]
 
 

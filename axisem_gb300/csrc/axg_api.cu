@@ -149,13 +149,15 @@ struct axg_handle {
   int solid_ctas_step = 1;
   // time scheme: 0 Newmark (newmark2), else a symplectic scheme of nstages stages
   int scheme = 0, nstages = 0;
-  std::vector<float> sym_cd, sym_cv;   // coefd(1:nstages+1) deltat, coefv(1:nstages) deltat
+  std::vector<double> sym_cd, sym_cv;  // coefd(1:nstages+1) deltat, coefv(1:nstages) deltat
   float *stf_stages = nullptr;         // (niter, nstages): the stf at the stages' times
   // compensated (Kahan) time integration
   bool kahan = false;
   float *cu_s[3] = {}, *cv_s[3] = {}, *cu_f = nullptr, *cv_f = nullptr;
   // coarse-grained attenuation
-  bool anel = false;
+  bool anel = false;       // coarse-grained (cg4) attenuation, fused into the solid kernel
+  bool anel_full = false;  // attenuation at every GLL point (anel_full_kernel)
+  float *fx = nullptr;     // ... its per-slot force terms for the next step
   int nsls = 0;
   AnelArgs an{};
   std::vector<int32_t> slot_of_elem_s;  // solid element -> launch slot
@@ -349,15 +351,21 @@ int validate(const axg_mesh_desc *d) {
     return bad("absorbing gamma arrays are NULL");
   if (!(d->deltat > 0) && d->niter > 0) return bad("deltat must be positive");
   if (d->anel_true) {
-    if (d->att_coarse_grained != 1)
-      return fail(nullptr, AXG_ERR_UNSUPPORTED,
-                  "only the coarse-grained (cg4) attenuation is implemented: att_coarse_grained must be 1");
+    if (d->att_coarse_grained != 0 && d->att_coarse_grained != 1) return bad("att_coarse_grained must be 0 or 1");
     if (d->n_sls < 1 || d->n_sls > kMaxSls)
       return fail(nullptr, AXG_ERR_UNSUPPORTED, fmt("n_sls = %d; 1..%d are supported", d->n_sls, kMaxSls));
     if (!d->y_j_attenuation || !d->exp_w_j_deltat || !d->ts_fac_t || !d->ts_fac_tm1 || !d->Q_mu || !d->Q_kappa ||
-        !d->delta_mu_cg4 || !d->delta_kappa_cg4 || !d->Y_cg4 || !d->V_s_eta_cg4 || !d->V_s_xi_cg4 ||
-        !d->V_z_eta_cg4 || !d->V_z_xi_cg4 || !d->DsDeta_over_J_sol_cg4 || !d->DzDeta_over_J_sol_cg4 ||
-        !d->DsDxi_over_J_sol_cg4 || !d->DzDxi_over_J_sol_cg4 || !d->inv_s_solid)
+        !d->inv_s_solid)
+      return bad("attenuation arrays are NULL");
+    if (!d->att_coarse_grained &&
+        (!d->delta_mu || !d->delta_kappa || !d->Y || !d->V_s_eta || !d->V_s_xi || !d->V_z_eta || !d->V_z_xi ||
+         !d->Y0 || !d->V0_s_eta || !d->V0_s_xi || !d->V0_z_eta || !d->V0_z_xi || !d->DsDeta_over_J_sol ||
+         !d->DzDeta_over_J_sol || !d->DsDxi_over_J_sol || !d->DzDxi_over_J_sol))
+      return bad("attenuation arrays of every GLL point are NULL (att_coarse_grained = 0)");
+    if (d->att_coarse_grained &&
+        (!d->delta_mu_cg4 || !d->delta_kappa_cg4 || !d->Y_cg4 || !d->V_s_eta_cg4 || !d->V_s_xi_cg4 ||
+         !d->V_z_eta_cg4 || !d->V_z_xi_cg4 || !d->DsDeta_over_J_sol_cg4 || !d->DzDeta_over_J_sol_cg4 ||
+         !d->DsDxi_over_J_sol_cg4 || !d->DzDxi_over_J_sol_cg4))
       return bad("attenuation arrays are NULL");
     for (int64_t e = 0; e < d->nel_solid; ++e)
       if (!(d->Q_mu[e] > 0.f) || !(d->Q_kappa[e] > 0.f)) return bad("Q_mu and Q_kappa must be positive");
@@ -587,6 +595,12 @@ CouplingHost make_coupling(std::vector<std::tuple<int32_t, int32_t, float, float
 // previous step's last writers stored
 bool lookahead(const axg_handle *h) { return h->scheme == AXG_SCHEME_NEWMARK2 && !h->kahan; }
 
+// an FP64 coefficient as an FP32 pair: hi = its FP32 rounding, lo = the rest
+void split(double x, float &hi, float &lo) {
+  hi = (float)x;
+  lo = (float)(x - (double)hi);
+}
+
 StateArgs solid_state(axg_handle *h) {
   StateArgs s{};
   for (int c = 0; c < 3; ++c) {
@@ -608,9 +622,9 @@ StateArgs solid_state(axg_handle *h) {
   s.blowup = h->blowup;
   s.err = h->errw;
   s.thresh = (float)(10.0 * std::fabs(h->magnitude));
-  s.dt = (float)h->dt;
-  s.hdt = (float)(0.5 * h->dt);
-  s.hdt2 = (float)(0.5 * h->dt * h->dt);
+  split(h->dt, s.dt, s.dt_lo);
+  split(0.5 * h->dt, s.hdt, s.hdt_lo);
+  split(0.5 * h->dt * h->dt, s.hdt2, s.hdt2_lo);
   s.src.gidx = h->src_gidx_d;
   s.src.val = h->src_val_d;
   s.src.val_dp = h->kahan ? h->src_val_dp_d : nullptr;
@@ -642,8 +656,11 @@ StateArgs fluid_state(axg_handle *h) {
 // current state (it may have been set, reset, restored or advanced by
 // another scheme or mode since the last run).  The last writers keep it from
 // there on; recomputing it is exact, so runs in pieces match one run.
+void launch_anel_full(axg_handle *h, cudaStream_t s, bool update);
+
 cudaError_t refresh_predicted(axg_handle *h, cudaStream_t s) {
-  if (!lookahead(h)) return cudaSuccess;
+  if (h->anel_full && h->scheme == AXG_SCHEME_NEWMARK2) launch_anel_full(h, s, false);
+  if (!lookahead(h)) return cudaGetLastError();
   if (h->nglob_s > 0) predict_kernel<<<(unsigned)((h->nglob_s + 255) / 256), 256, 0, s>>>(solid_state(h));
   if (h->nel_f > 0) predict_kernel<<<(unsigned)((h->nglob_f + 255) / 256), 256, 0, s>>>(fluid_state(h));
   return cudaGetLastError();
@@ -750,6 +767,7 @@ void launch_solid_colours(axg_handle *h, cudaStream_t s) {
     a.patch_begin = h->ps.colour_start[c];
     const int n = h->ps.colour_start[c + 1] - h->ps.colour_start[c];
     const int grid = std::min(n, ctas);
+    a.fx = MODE == MODE_NEWMARK && h->anel_full ? h->fx : nullptr;
     launch_pdl(solid_patch_kernel<POLE, MODE, ANEL, KAHAN>, grid, kThreads, solid_smem_bytes<POLE, MODE, ANEL, KAHAN>(),
                s, a, st, h->spec, n, h->an);
   }
@@ -829,6 +847,22 @@ void launch_fluid(axg_handle *h, cudaStream_t s, const StateArgs &fs) {
   }
 }
 
+// Attenuation at every GLL point: with update, the step's memory variables
+// and the next step's force terms; without, the force terms of the current
+// memory variables (before a run)
+template <int POLE>
+void launch_anel_full_pole(axg_handle *h, cudaStream_t s, bool update) {
+  const FullAnelArgs fa{h->an, h->fx, h->sym_gidx, h->sym_axial, h->nel_s};
+  const unsigned g = (unsigned)std::min<int64_t>((h->nel_s + kWarps - 1) / kWarps, 16 * (int64_t)h->num_sms);
+  if (update) launch_pdl(anel_full_kernel<POLE, true>, g, kThreads, 0, s, fa, solid_state(h), h->spec);
+  else anel_full_kernel<POLE, false><<<g, kThreads, 0, s>>>(fa, solid_state(h), h->spec);
+}
+void launch_anel_full(axg_handle *h, cudaStream_t s, bool update) {
+  if (h->pole == AXG_MONOPOLE) launch_anel_full_pole<POLE_MONO>(h, s, update);
+  else if (h->pole == AXG_DIPOLE) launch_anel_full_pole<POLE_DI>(h, s, update);
+  else launch_anel_full_pole<POLE_QUAD>(h, s, update);
+}
+
 void enqueue_force(axg_handle *h, cudaStream_t s) {
   if (h->to_solid.n > 0)
     zero_points_kernel<<<(h->to_solid.n + 255) / 256, 256, 0, s>>>(h->to_solid.pt_gidx, h->to_solid.n, h->sf[0],
@@ -861,6 +895,7 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
     }
   }
   launch_solid<MODE_NEWMARK>(h, s);
+  if (h->anel_full) launch_anel_full(h, s, true);  // the memory variables from the stored displacement
   launch_pdl(receivers_kernel<One<RecWork>>, 1, 256, 0, s, One<RecWork>{rec_work(h, ss), 1});
 }
 
@@ -895,15 +930,22 @@ void launch_solid_symplectic(axg_handle *h, cudaStream_t s, const StateArgs &st)
 void symplectic_stage_states(axg_handle *h, int i, StateArgs &ss, StateArgs &fs) {
   ss = solid_state(h);
   fs = fluid_state(h);
-  ss.dt = fs.dt = h->sym_cd[i];
-  ss.hdt2 = fs.hdt2 = 0.f;  // the coupling's predictor is then the drift u + coefd(i) v
-  ss.kick = fs.kick = h->sym_cv[i];
+  split(h->sym_cd[i], ss.dt, ss.dt_lo);
+  split(h->sym_cv[i], ss.kick, ss.kick_lo);
+  ss.hdt2 = ss.hdt2_lo = 0.f;  // the coupling's predictor is then the drift u + coefd(i) v
+  fs.dt = ss.dt;
+  fs.dt_lo = ss.dt_lo;
+  fs.kick = ss.kick;
+  fs.kick_lo = ss.kick_lo;
+  fs.hdt2 = fs.hdt2_lo = 0.f;
   ss.stf = h->stf_stages + (int64_t)i * std::max(h->niter, 1);
 }
 
 // the final drift of a symplectic step: one thread per point of the larger domain
 DriftWork drift_work(axg_handle *h) {
-  return DriftWork{solid_state(h), fluid_state(h), h->sym_cd[h->nstages]};
+  DriftWork w{solid_state(h), fluid_state(h), 0.f, 0.f};
+  split(h->sym_cd[h->nstages], w.cd, w.cd_lo);
+  return w;
 }
 int32_t drift_points(const axg_handle *h) {
   return (int32_t)std::max(h->nglob_s, h->nel_f > 0 ? h->nglob_f : 0);
@@ -1154,6 +1196,69 @@ void sls_fast_correct(const double *y, double *yp, int n) {
 //    rounded to float once;
 //  * per element (launch order) the cg4 constants and the two row indices;
 //  * the per-element state, zeroed by axg_reset.
+// the element slots' points and axis flags (launch order), for the kernels
+// that visit elements outside the patch kernel
+int upload_slot_points(axg_handle *h) {
+  if (h->sym_gidx) return AXG_OK;
+  std::vector<int32_t> g(25 * (size_t)h->nel_s);
+  std::vector<uint8_t> ax(h->nel_s);
+  for (int64_t e = 0; e < h->nel_s; ++e) {
+    const int64_t sl = h->slot_of_elem_s[e];
+    for (int k = 0; k < 25; ++k) g[25 * sl + k] = h->igloc_s[25 * e + k] - 1;
+    ax[sl] = h->axial_s[e];
+  }
+  int rc;
+  if ((rc = upload(h, &h->sym_gidx, g)) || (rc = upload(h, &h->sym_axial, ax))) return rc;
+  return AXG_OK;
+}
+
+// Attenuation at every GLL point: the per-slot constants (kFullConst
+// floats), the state (memory variables and the previous step's sources in
+// the reference's layouts), the force terms, the slots' points.
+template <class RowFn>
+int build_anel_full(axg_handle *h, const axg_mesh_desc *d, bool mesh_part, RowFn row, std::vector<float> &qtab,
+                    const std::map<float, int32_t> &qrow) {
+  const int nsls = d->n_sls;
+  const int64_t nel = h->nel_s;
+  const DomainPlan &pl = h->ps;
+  std::vector<float> consts((size_t)nel * kFullConst, 0.f);
+  const float *pt[12] = {d->delta_mu, d->delta_kappa, d->Y, d->V_s_eta, d->V_s_xi, d->V_z_eta, d->V_z_xi,
+                         d->DsDeta_over_J_sol, d->DzDeta_over_J_sol, d->DsDxi_over_J_sol, d->DzDxi_over_J_sol,
+                         d->inv_s_solid};
+  const float *ax5[5] = {d->Y0, d->V0_s_eta, d->V0_s_xi, d->V0_z_eta, d->V0_z_xi};
+  for (int64_t s = 0; s < nel; ++s) {
+    const int64_t e = pl.elem_order[s];
+    float *c = consts.data() + (size_t)s * kFullConst;
+    for (int f = 0; f < 12; ++f) std::memcpy(c + 25 * f, pt[f] + 25 * e, 25 * sizeof(float));
+    if (h->axial_s[e])
+      for (int f = 0; f < 5; ++f) std::memcpy(c + F_Y0 + 5 * f, ax5[f] + 5 * e, 5 * sizeof(float));
+    const int32_t qm = row(d->Q_mu[e]), qk = row(d->Q_kappa[e]);
+    std::memcpy(c + F_QMU, &qm, 4);
+    std::memcpy(c + F_QKA, &qk, 4);
+  }
+  h->nsls = nsls;
+  h->an.nsls = nsls;
+  h->an.state_stride = full_state_stride(nsls);
+  h->an.n_q = (int32_t)qrow.size();
+  for (int j = 0; j < kMaxSls; ++j) h->an.ex[j] = j < nsls ? (float)d->exp_w_j_deltat[j] : 0.f;
+  h->slot_of_elem_s.assign(nel, 0);
+  for (int64_t s = 0; s < nel; ++s) h->slot_of_elem_s[pl.elem_order[s]] = (int32_t)s;
+  int rc;
+  float *cp = nullptr, *qp = nullptr;
+  if (mesh_part) {
+    h->in_mesh = true;
+    rc = upload(h, &cp, consts);
+    h->in_mesh = false;
+    if (rc) return rc;
+    h->an.consts = cp;
+  }
+  if ((rc = upload(h, &qp, qtab))) return rc;
+  h->an.qtab = qp;
+  if ((rc = dalloc(h, &h->an.state, (size_t)nel * h->an.state_stride))) return rc;
+  if ((rc = dalloc(h, &h->fx, (size_t)nel * 75))) return rc;
+  return upload_slot_points(h);
+}
+
 int build_anel(axg_handle *h, const axg_mesh_desc *d, bool mesh_part) {
   const int nsls = d->n_sls;
   const int64_t nel = h->nel_s;
@@ -1178,6 +1283,7 @@ int build_anel(axg_handle *h, const axg_mesh_desc *d, bool mesh_part) {
     qrow[Q] = r;
     return r;
   };
+  if (h->anel_full) return build_anel_full(h, d, mesh_part, row, qtab, qrow);
   std::vector<float> consts((size_t)nel * kAnelConst, 0.f);
   const float *fields[11] = {d->delta_mu_cg4, d->delta_kappa_cg4, d->Y_cg4,  d->V_s_eta_cg4,
                              d->V_s_xi_cg4,   d->V_z_eta_cg4,    d->V_z_xi_cg4, d->DsDeta_over_J_sol_cg4,
@@ -1238,14 +1344,16 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
   h->absorbing = d->have_absorbing_bc != 0;
   h->dt = d->deltat;
   h->magnitude = d->magnitude;
-  h->anel = d->anel_true != 0;
+  h->anel = d->anel_true != 0 && d->att_coarse_grained != 0;
+  h->anel_full = d->anel_true != 0 && d->att_coarse_grained == 0;
   CouplingHost cf, cs;
   if (share) {
     // the same mesh: sizes, pole, numbering, axial elements, boundary and
     // attenuation layout must match (the metric terms are taken as equal)
     if (share->pole != h->pole || share->nel_s != h->nel_s || share->nel_f != h->nel_f ||
         share->nglob_s != h->nglob_s || share->nglob_f != h->nglob_f || share->absorbing != h->absorbing ||
-        share->anel != h->anel || (h->anel && share->nsls != d->n_sls))
+        share->anel != h->anel || share->anel_full != h->anel_full ||
+        ((h->anel || h->anel_full) && share->nsls != d->n_sls))
       return fail(h, AXG_ERR_BAD_DESC, "axg_create_sharing: the descriptor is not of the handle's mesh");
     // (the handle holds igloc in its internal numbering)
     auto same = [](const std::vector<int32_t> &mine, const int32_t *ig, int64_t n, int64_t nglob,
@@ -1432,10 +1540,10 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
   if ((rc = dalloc(h, &h->iter, 4))) return rc;
   h->blowup = h->iter + 1;
   h->errw = h->iter + 2;
-  if (h->anel && (rc = build_anel(h, d, !share))) return rc;
+  if ((h->anel || h->anel_full) && (rc = build_anel(h, d, !share))) return rc;
   if ((rc = prepare_kernels(h))) return rc;
   h->kernels_per_force = h->ps.n_colours + (h->to_solid.n > 0 ? 1 : 0);
-  h->kernels_per_step = h->ps.n_colours + 1 +
+  h->kernels_per_step = h->ps.n_colours + 1 + (h->anel_full ? 1 : 0) +
                         (h->nel_f > 0 ? 2 + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);
   return axg_reset(h);
 }
@@ -1668,12 +1776,14 @@ namespace {
 int anel_state_io(axg_handle *h, int field, float *out, const float *in) {
   if (field != AXG_FIELD_MEMVAR && field != AXG_FIELD_ATT_SRC_TR && field != AXG_FIELD_ATT_SRC_DEV)
     return fail(h, AXG_ERR_BAD_ARG, fmt("field %d not available", field));
-  if (!h->anel) return fail(h, AXG_ERR_BAD_ARG, "the handle was created without attenuation (anel_true = 0)");
+  if (!h->anel && !h->anel_full)
+    return fail(h, AXG_ERR_BAD_ARG, "the handle was created without attenuation (anel_true = 0)");
   const int64_t nel = h->nel_s, stride = h->an.state_stride;
   const int nsls = h->nsls;
-  int off = 0, len = 24 * nsls;  // floats per element of this field, and where they start in the state
-  if (field == AXG_FIELD_ATT_SRC_TR) off = 24 * nsls, len = 4;
-  if (field == AXG_FIELD_ATT_SRC_DEV) off = 24 * nsls + 4, len = 24;
+  const int np = h->anel_full ? 25 : 4;  // points per element with memory variables
+  int off = 0, len = 6 * np * nsls;  // floats per element of this field, and where they start in the state
+  if (field == AXG_FIELD_ATT_SRC_TR) off = 6 * np * nsls, len = np;
+  if (field == AXG_FIELD_ATT_SRC_DEV) off = 6 * np * nsls + np, len = 6 * np;
   std::vector<float> st((size_t)nel * stride);
   CK(cudaMemcpyAsync(st.data(), h->an.state, st.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -1769,7 +1879,7 @@ int axg_reset(axg_handle *h) {
   // the iter-0 seismogram sample (dump_stuff(0,...)) is the zero wavefield
   CK(cudaMemsetAsync(h->rec, 0, (size_t)h->nseismo * 3 * std::max(h->num_rec, 1) * sizeof(float), h->stream));
   CK(cudaMemsetAsync(h->iter, 0, 4 * sizeof(int32_t), h->stream));
-  if (h->anel)
+  if (h->anel || h->anel_full)
     CK(cudaMemsetAsync(h->an.state, 0, (size_t)h->nel_s * h->an.state_stride * sizeof(float), h->stream));
   for (float *p : {h->cu_s[0], h->cu_s[1], h->cu_s[2], h->cv_s[0], h->cv_s[1], h->cv_s[2], h->cu_f, h->cv_f})
     if (p) CK(cudaMemsetAsync(p, 0, (p == h->cu_f || p == h->cv_f ? h->nglob_f : h->nglob_s) * sizeof(float), h->stream));
@@ -2285,7 +2395,7 @@ int axg_autotune(axg_handle *h, int32_t *chosen) {
     add(h->cu_s[c], gs), add(h->cv_s[c], gs);
   }
   add(h->fu, gf), add(h->fv, gf), add(h->fa, gf), add(h->ff, gf), add(h->cu_f, gf), add(h->cv_f, gf);
-  if (h->anel) add(h->an.state, (size_t)h->nel_s * h->an.state_stride * sizeof(float));
+  if (h->anel || h->anel_full) add(h->an.state, (size_t)h->nel_s * h->an.state_stride * sizeof(float));
   add(h->rec, (size_t)h->nseismo * 3 * std::max(h->num_rec, 1) * sizeof(float));
   add(h->iter, 4 * sizeof(int32_t));
   size_t total = 0;
@@ -2414,21 +2524,17 @@ int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages) 
                   "symplectic schemes: a fluid source and a fluid free surface are not supported (the reference's "
                   "symplectic loop applies neither)");
     if (!stf_stages) return fail(h, AXG_ERR_BAD_ARG, "stf_stages is NULL");
-    if (h->anel && !h->sym_gidx) {  // per launch slot: the element's points and axis flag
-      std::vector<int32_t> g(25 * (size_t)h->nel_s);
-      std::vector<uint8_t> ax(h->nel_s);
-      for (int64_t e = 0; e < h->nel_s; ++e) {
-        const int64_t sl = h->slot_of_elem_s[e];
-        for (int k = 0; k < 25; ++k) g[25 * sl + k] = h->igloc_s[25 * e + k] - 1;
-        ax[sl] = h->axial_s[e];
-      }
-      int rc;
-      if ((rc = upload(h, &h->sym_gidx, g)) || (rc = upload(h, &h->sym_axial, ax))) return rc;
+    if (h->anel_full)
+      return fail(h, AXG_ERR_UNSUPPORTED,
+                  "symplectic schemes with attenuation at every GLL point (att_coarse_grained = 0) are not supported");
+    if (h->anel) {  // per launch slot: the element's points and axis flag
+      const int rc = upload_slot_points(h);
+      if (rc) return rc;
     }
     h->sym_cd.resize(n + 1);
     h->sym_cv.resize(n);
-    for (int i = 0; i <= n; ++i) h->sym_cd[i] = (float)(cd[i] * h->dt);
-    for (int i = 0; i < n; ++i) h->sym_cv[i] = (float)(cv[i] * h->dt);
+    for (int i = 0; i <= n; ++i) h->sym_cd[i] = cd[i] * h->dt;
+    for (int i = 0; i < n; ++i) h->sym_cv[i] = cv[i] * h->dt;
     std::vector<float> stf(stf_stages, stf_stages + (size_t)std::max(h->niter, 1) * n);
     int rc;
     if ((rc = upload(h, &h->stf_stages, stf))) return rc;
@@ -2442,7 +2548,7 @@ int axg_set_time_scheme(axg_handle *h, int32_t scheme, const float *stf_stages) 
     h->kernels_per_step = (int64_t)h->nstages * (h->ps.n_colours + (h->nel_f > 0 ? 2 +
                           (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0)) + 2 + (h->anel ? 1 : 0);
   } else {
-    h->kernels_per_step = h->ps.n_colours + 1 +
+    h->kernels_per_step = h->ps.n_colours + 1 + (h->anel_full ? 1 : 0) +
                           (h->nel_f > 0 ? 2 + (h->to_fluid.n > 0) + (h->to_solid.n > 0) : 0);
   }
   return axg_reset(h);
@@ -3015,6 +3121,9 @@ int batch_create_impl(axg_batch *b, axg_handle *const *hs, int32_t n) {
     if (h->ckpt.check_it > 0)
       return bfail(b, AXG_ERR_UNSUPPORTED,
                    fmt("axg_batch_create: solve %d checkpoints its seismograms (it runs alone)", k));
+    if (h->anel_full)
+      return bfail(b, AXG_ERR_UNSUPPORTED,
+                   fmt("axg_batch_create: solve %d has attenuation at every GLL point (it runs alone)", k));
     b->hs.push_back(h);
   }
   b->device = hs[0]->device;

@@ -105,6 +105,8 @@ struct DomainArgs {
   const float *m0;          // per axial slot n_axial*5 floats
   const float *fsmask;      // fluid free-surface mask per element (launch order) or null
   const float *srcfl;       // fluid element source terms (8, 25) or null
+  const float *fx;          // solid, attenuation at every GLL point: per element (launch order) 3 x 25
+                            // floats the Newmark step adds to the stiffness, or null
   int32_t patch_begin;
   int64_t n_patches, n_pts, n_elem, n_m0;   // buffer extents (checked builds)
 };
@@ -124,8 +126,10 @@ struct StateArgs {
   int32_t *blowup;          // first iteration that blew up (0 = none)
   int32_t *err;             // device error word (AXG_ERR_TIMEOUT when a bounded wait gave up)
   float thresh;             // 10 |magnitude|
-  float dt, hdt, hdt2;      // Newmark: deltat, deltat/2, deltat^2/2; symplectic stage: dt = coefd(i) deltat
-  float kick;               // symplectic stage: coefv(i) deltat
+  // Newmark: deltat, deltat/2, deltat^2/2; symplectic stage: dt = coefd(i) deltat,
+  // kick = coefv(i) deltat; each an FP32 pair (value + _lo = the FP64 value)
+  float dt, hdt, hdt2, dt_lo, hdt_lo, hdt2_lo;
+  float kick, kick_lo;
   SrcTable src;
   int64_t nglob;            // extent of the state arrays (checked builds)
   int32_t niter;            // extent of stf
@@ -240,9 +244,23 @@ struct ManySolves {
 
 // ------------------------------------------------------------ small helpers
 
-__device__ __forceinline__ float predict(float d, float v, float a, float dt, float hdt2) {
-  // disp + deltat*velo + half_dt_sq*acc0 (SOLVER/time_evol_wave.F90:357-364)
-  return fmaf(hdt2, a, fmaf(dt, v, d));
+// Time-step coefficients as FP32 pairs.  The reference multiplies its FP32
+// fields by FP64 coefficients (deltat, half_dt, half_dt_sq, coefd(i) and
+// coefv(i) times deltat) and rounds each update once.  A coefficient rounded
+// to FP32 is off by up to 3e-8 relative, the same in every step: over 1e5
+// steps a steady drift of the solution's time scale, which the compensated
+// summation cannot remove.  With the low part the increments carry only the
+// FP32 rounding of the product.
+// c x for the coefficient c + c_lo
+__device__ __forceinline__ float mul2(float c, float c_lo, float x) { return fmaf(c, x, c_lo * x); }
+// the predictor's increment deltat*velo + half_dt_sq*acc0
+__device__ __forceinline__ float pred_inc(float v, float a, const StateArgs &st) {
+  return fmaf(st.hdt2, a, fmaf(st.dt, v, fmaf(st.hdt2_lo, a, st.dt_lo * v)));
+}
+// disp + deltat*velo + half_dt_sq*acc0 (SOLVER/time_evol_wave.F90:357-364);
+// a symplectic stage's drift disp + coefd(i) velo (hdt2 = 0)
+__device__ __forceinline__ float predict(float d, float v, float a, const StateArgs &st) {
+  return d + pred_inc(v, a, st);
 }
 
 // Compensated mode (no counterpart in the reference): x + inc by Kahan's
@@ -263,9 +281,10 @@ __device__ __forceinline__ bool axis_masked(int comp) {
   return POLE == POLE_QUAD || (POLE == POLE_MONO ? comp == 0 : comp != 0);
 }
 
-// the predictor of the compensated mode: increment dt v + dt^2/2 a
-__device__ __forceinline__ float predict_comp(float d, float v, float a, float dt, float hdt2, float &c) {
-  return kahan_add(d, fmaf(hdt2, a, dt * v), c);
+// the predictor of the compensated mode: the same increment, added by
+// compensated summation
+__device__ __forceinline__ float predict_comp(float d, float v, float a, const StateArgs &st, float &c) {
+  return kahan_add(d, pred_inc(v, a, st), c);
 }
 
 // X(i,j) = sum_k c[k] * v(k,j)   (v(k,j) held by lane k + 5 j)
@@ -984,11 +1003,10 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
             if (KAHAN) {
               float k = ok ? st.cu[gc(c)][g] : 0.f;
               // (a symplectic stage: hdt2 = 0, the compensated drift u + coefd(i) v)
-              if (ok) u = predict_comp(u, st.v[gc(c)][g], MODE == MODE_SYMPLECTIC ? 0.f : st.a[gc(c)][g], st.dt,
-                                       st.hdt2, k);
+              if (ok) u = predict_comp(u, st.v[gc(c)][g], MODE == MODE_SYMPLECTIC ? 0.f : st.a[gc(c)][g], st, k);
               cc[KAHAN ? q : 0][c] = k;
             } else if (ok && MODE == MODE_SYMPLECTIC) {
-              u = fmaf(st.dt, st.v[gc(c)][g], u);  // drift: disp + velo * coefd(i)
+              u = u + mul2(st.dt, st.dt_lo, st.v[gc(c)][g]);  // drift: disp + velo * coefd(i)
             }  // (plain Newmark: up is the predicted displacement)
             uu[q][c] = u;
             ff[q][c] = part ? st.f[gc(c)][g] : 0.f;
@@ -1065,6 +1083,14 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
         if (ANEL) {
           if (ax) anel_stiffness<POLE, true>(coef, ablk, ablk + kAnelConst, an->nsls, cg, kcg, i, j, active, lane, f0, f1, f2);
           else anel_stiffness<POLE, false>(coef, ablk, ablk + kAnelConst, an->nsls, cg, kcg, i, j, active, lane, f0, f1, f2);
+        }
+        if (MODE == MODE_NEWMARK && !ANEL && d.fx && active) {
+          // attenuation at every GLL point: minus the anelastic stiffness
+          // (glob_anel_stiffness_*_4), formed by anel_full_kernel
+          const float *x = d.fx + el * 75;
+          f0 = f0 + x[lane];
+          f1 = f1 + x[25 + lane];
+          f2 = f2 + x[50 + lane];
         }
         if (ax && i == 0) {  // axis mask of acc1
           if (POLE == POLE_MONO) f0 = 0.f;
@@ -1194,14 +1220,15 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
               // component takes twice the whole acceleration
               float a = (KAHAN && st.inv_mass_dp) ? (float)(-imd[KAHAN ? q : 0] * (double)v[c]) : -im[q] * v[c];
               if (st.gamma) a = a - 2.f * gam[q] * vel[q][c] - gam[q] * gam[q] * dsp;
-              const float kick = (POLE == POLE_DI && cg == 2) ? 2.f * st.kick : st.kick;
+              const bool two = POLE == POLE_DI && cg == 2;
+              const float dv = mul2(two ? 2.f * st.kick : st.kick, two ? 2.f * st.kick_lo : st.kick_lo, a);
               if (KAHAN) {
                 float k = kv[KAHAN ? q : 0][c];
-                st.v[cg][g] = kahan_add(vel[q][c], kick * a, k);
+                st.v[cg][g] = kahan_add(vel[q][c], dv, k);
                 st.cv[cg][g] = k;
                 st.cu[cg][g] = s_cu[c][spos(t)];
               } else {
-                st.v[cg][g] = fmaf(kick, a, vel[q][c]);
+                st.v[cg][g] = vel[q][c] + dv;
               }
               st.a[cg][g] = a;
               const bool zero = (w[q] & kPtAxis) && axis_masked<POLE>(cg);
@@ -1220,11 +1247,11 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
             float vn;
             if (KAHAN) {
               float k = kv[KAHAN ? q : 0][c];
-              vn = kahan_add(vel[q][c], st.hdt * (acc[q][c] + a), k);
+              vn = kahan_add(vel[q][c], mul2(st.hdt, st.hdt_lo, acc[q][c] + a), k);
               st.cv[cg][g] = k;
               st.cu[cg][g] = s_cu[c][spos(t)];
             } else {
-              vn = fmaf(st.hdt, acc[q][c] + a, vel[q][c]);
+              vn = vel[q][c] + mul2(st.hdt, st.hdt_lo, acc[q][c] + a);
             }
             st.v[cg][g] = vn;
             st.a[cg][g] = a;
@@ -1235,7 +1262,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
             if (KAHAN && zero) st.cu[cg][g] = 0.f;
             // the next step's predictor disp + deltat*velo + half_dt_sq*acc0
             // (SOLVER/time_evol_wave.F90:357-364), from the state just stored
-            if (LOOK) st.up[cg][g] = predict(un, vn, a, st.dt, st.hdt2);
+            if (LOOK) st.up[cg][g] = predict(un, vn, a, st);
           }
         }
       }
@@ -1258,6 +1285,218 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
       const uint32_t par = ASYNC ? ((pcount - 1) / NB) & 1u : (pcount - 1) & 1u;
       mbar_drain(&s_wbar[b], par);
     }
+  }
+}
+
+// ------------------------------------------------------------ attenuation at every GLL point
+//
+// att_coarse_grained = .false.: memory variables at all 25 GLL points of
+// every solid element.  Per launch slot the host packs kFullConst constants:
+// [field][GLL point] of delta_mu, delta_kappa, Y, V_s_eta, V_s_xi, V_z_eta,
+// V_z_xi, DsDeta_over_J_sol, DzDeta_over_J_sol, DsDxi_over_J_sol,
+// DzDxi_over_J_sol, inv_s_solid; then [field][jpol] of Y0, V0_s_eta,
+// V0_s_xi, V0_z_eta, V0_z_xi (zero off the axis); then the two Q-table rows.
+// The state of a slot is memory_var(0:4,0:4,6,n_sls), src_tr_tm1(0:4,0:4),
+// src_dev_tm1(0:4,0:4,6), the reference's layouts.
+enum : int {
+  F_DMU = 0, F_DKA = 25, F_Y = 50, F_VSE = 75, F_VSX = 100, F_VZE = 125, F_VZX = 150, F_DSDETA = 175,
+  F_DZDETA = 200, F_DSDXI = 225, F_DZDXI = 250, F_INVS = 275, F_Y0 = 300, F_V0SE = 305, F_V0SX = 310,
+  F_V0ZE = 315, F_V0ZX = 320, F_QMU = 325, F_QKA = 326
+};
+constexpr int kFullConst = 328;  // floats, a 16-byte multiple
+__host__ __device__ constexpr int full_state_stride(int nsls) { return ((150 * nsls + 175 + 3) / 4) * 4; }
+
+struct FullAnelArgs {
+  AnelArgs an;            // consts (kFullConst per slot), state, qtab, ex, nsls, state_stride, n_q
+  float *fx;              // per slot 3 x 25: minus the anelastic stiffness the next Newmark step adds
+  const int32_t *gidx;    // per slot the element's 25 global points
+  const uint8_t *axial;   // per slot 1 for an axial element
+  int64_t nel;
+};
+
+// One warp per element (launch order), lane = GLL point.  UPDATE: the memory
+// variables of the step from the displacement the step stored
+// (time_step_memvars_4 with compute_strain_att_el_4, SOLVER/attenuation.f90:
+// 210-334, 542-606: the gradients of axisym_gradient_solid_el_4, f / s of
+// f_over_s_solid_el_4 with L'Hospital's df/ds on the axis).  Then, from the
+// memory variables, the anelastic stiffness of glob_anel_stiffness_*_4
+// (SOLVER/stiffness_mono.f90:409-507, SOLVER/stiffness_di.f90:604-723,
+// SOLVER/stiffness_quad.f90:555-669), stored negated in fx for the next
+// step's patch kernel.  Without UPDATE (before a run) only the latter.
+template <int POLE, bool UPDATE>
+__global__ void __launch_bounds__(kThreads) anel_full_kernel(const __grid_constant__ FullAnelArgs fa, StateArgs st,
+                                                             SpecDev sp) {
+  pdl_wait();
+  pdl_trigger();
+  if (*st.blowup) return;
+  const AnelArgs &an = fa.an;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool active = lane < 25;
+  const int ml = active ? lane : 24;
+  const int i = ml % 5, j = ml / 5, j5 = 5 * j;
+  LaneCoef coef;
+  load_coef(sp, i, j, coef);
+  const int nsls = an.nsls;
+  for (int64_t el = (int64_t)blockIdx.x * kWarps + warp; el < fa.nel; el += (int64_t)gridDim.x * kWarps) {
+    const float *cs = an.consts + el * kFullConst;
+    float *R = an.state + el * an.state_stride;
+    float *trm1 = R + 150 * nsls, *devm1 = trm1 + 25;
+    const bool ax = fa.axial[el] != 0;
+    if (UPDATE) {
+      int32_t g = fa.gidx[25 * el + ml];
+      if (!AXG_BOUND(g, st.nglob, 52)) g = 0;
+      float u[3] = {st.u[0][g], POLE == POLE_MONO ? 0.f : st.u[1][g], st.u[2][g]};
+      if (ax && i == 0) {  // apply_axis_mask_* on disp
+        if (POLE == POLE_MONO) u[0] = 0.f;
+        if (POLE == POLE_DI) { u[1] = 0.f; u[2] = 0.f; }
+        if (POLE == POLE_QUAD) { u[0] = 0.f; u[1] = 0.f; u[2] = 0.f; }
+      }
+      const float dsdeta = cs[F_DSDETA + ml], dzdeta = cs[F_DZDETA + ml];
+      const float dsdxi = cs[F_DSDXI + ml], dzdxi = cs[F_DZDXI + ml], invs = cs[F_INVS + ml];
+      // axisym_gradient_solid_el_4 of the field f held lane-wise: (d/ds, d/dz)
+      auto grad = [&](float f, float &gs, float &gz) {
+        const float m1 = ax ? dxi(f, coef.xi1, j5) : dxi(f, coef.xi2, j5);
+        const float m2 = deta(f, coef.eta, i);
+        gs = dzdeta * m1 + dzdxi * m2;
+        gz = dsdeta * m1 + dsdxi * m2;
+      };
+      // f_over_s_solid_el_4: f / s; on the axis (ipol = 0 of an axial
+      // element) df/ds (dsdf_elem_solid, G1T); the contractions run on every
+      // lane of the warp (ax is uniform across it)
+      auto fos = [&](float f) {
+        float o = invs * f;
+        if (ax) {
+          float gs, gz;
+          grad(f, gs, gz);
+          if (i == 0) o = gs;
+        }
+        return o;
+      };
+      float gu[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // Voigt 1..6
+      float b1s, b1z, b2s, b2z;
+      grad(POLE == POLE_DI ? u[0] + u[1] : u[0], b1s, b1z);
+      grad(u[2], b2s, b2z);
+      gu[0] = b1s;
+      gu[2] = b2z;
+      gu[4] = b1z + b2s;
+      if (POLE == POLE_MONO) {
+        gu[1] = fos(u[0]);
+      } else if (POLE == POLE_DI) {
+        gu[1] = 2.f * fos(u[1]);
+        grad(u[0] - u[1], b1s, b1z);
+        const float t = fos(u[2]);
+        gu[3] = -t - b1z;
+        gu[5] = -gu[1] - b1s;
+      } else {
+        gu[1] = fos(u[0] - 2.f * u[1]);
+        grad(u[1], b1s, b1z);
+        const float t = fos(u[2]);
+        const float t2 = fos(u[1] - 2.f * u[0]);
+        gu[3] = -2.f * t - b1z;
+        gu[5] = t2 - b1s;
+      }
+      if (active) {
+        const float tr = gu[0] + gu[1] + gu[2];
+        const float dm = cs[F_DMU + lane], dk = cs[F_DKA + lane];
+        float src_dev[6];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) src_dev[v] = (dm * 2.f) * (gu[v] - tr * (1.f / 3.f));
+        src_dev[3] = POLE == POLE_MONO ? 0.f : dm * gu[3];
+        src_dev[4] = dm * gu[4];
+        src_dev[5] = POLE == POLE_MONO ? 0.f : dm * gu[5];
+        const float src_tr = dk * tr;
+        int qmu = __float_as_int(cs[F_QMU]), qka = __float_as_int(cs[F_QKA]);
+        if (!AXG_BOUND(qmu, an.n_q, 52)) qmu = 0;
+        if (!AXG_BOUND(qka, an.n_q, 52)) qka = 0;
+        const float *tmu = an.qtab + qmu * 2 * kMaxSls, *tka = an.qtab + qka * 2 * kMaxSls;
+        const float trp = trm1[lane];
+        for (int q = 0; q < nsls; ++q) {
+          const float trb = __ldg(tka + q) * src_tr + __ldg(tka + kMaxSls + q) * trp;
+#pragma unroll
+          for (int v = 0; v < 6; ++v) {
+            if (POLE == POLE_MONO && (v == 3 || v == 5)) continue;  // never written for the monopole
+            float *r = R + lane + 25 * (v + 6 * q);
+            const float db = __ldg(tmu + q) * src_dev[v] + __ldg(tmu + kMaxSls + q) * devm1[lane + 25 * v];
+            float nv = an.ex[q] * *r + db;
+            if (v < 3) nv = nv + trb;
+            *r = nv;
+          }
+        }
+        trm1[lane] = src_tr;
+#pragma unroll
+        for (int v = 0; v < 6; ++v) devm1[lane + 25 * v] = src_dev[v];
+      }
+      __syncwarp();
+    }
+    // the summed memory variables at the lane's point
+    float r[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (active)
+      for (int q = 0; q < nsls; ++q)
+#pragma unroll
+        for (int v = 0; v < 6; ++v) r[v] = r[v] + R[lane + 25 * (v + 6 * q)];
+    const float yl = cs[F_Y + ml], vse = cs[F_VSE + ml], vsx = cs[F_VSX + ml];
+    const float vze = cs[F_VZE + ml], vzx = cs[F_VZX + ml];
+    // X = mxm(G, S) (G1 on axial elements) and mxm(S, G2T)
+    auto gx = [&](float S) { return ax ? dxi(S, coef.sxi1, j5) : dxi(S, coef.sxi2, j5); };
+    auto ge = [&](float S) { return deta(S, coef.seta, i); };
+    // axial vectors at jpol = j (lanes with ipol = 0 use them)
+    const float y0 = cs[F_Y0 + j], v0se = cs[F_V0SE + j], v0sx = cs[F_V0SX + j];
+    const float v0ze = cs[F_V0ZE + j], v0zx = cs[F_V0ZX + j];
+    // outerprod(G0, V)(i, j) = G0(i) V(j), V held by lane (0, j)
+    auto outer = [&](float V) { return coef.g0i * __shfl_sync(kFull, V, j5); };
+    float l0, l1 = 0.f, l2;
+    if (POLE == POLE_MONO) {
+      const float S1s = vze * r[0] + vse * r[4], S2s = vzx * r[0] + vsx * r[4];
+      const float S1z = vze * r[4] + vse * r[2], S2z = vzx * r[4] + vsx * r[2];
+      l0 = gx(S1s) + ge(S2s) + yl * r[1];
+      l2 = gx(S1z) + ge(S2z);
+      if (ax) {
+        const float V1 = v0ze * r[0] + v0se * r[4] + y0 * r[1];
+        const float V2 = v0ze * r[4] + v0se * r[2];
+        const float V3 = v0zx * r[4] + v0sx * r[2];
+        const float V4 = deta(V3, coef.seta, 0);  // vxm(V3, G2T) on the lanes with ipol = 0
+        l0 = l0 + outer(V1);
+        l2 = l2 + outer(V2);
+        if (i == 0) l2 = l2 + V4;
+      }
+    } else if (POLE == POLE_DI) {
+      const float r16m = r[0] - r[5], r54m = r[4] - r[3], r16p = r[0] + r[5], r54p = r[4] + r[3];
+      const float S1p = vze * r16m + vse * r54m, S2p = vzx * r16m + vsx * r54m;
+      const float S1m = vze * r16p + vse * r54p, S2m = vzx * r16p + vsx * r54p;
+      const float S1z = vze * r[4] + vse * r[2], S2z = vzx * r[4] + vsx * r[2];
+      l0 = gx(S1p) + ge(S2p);
+      l1 = gx(S1m) + ge(S2m) + 2.f * yl * (r[1] - r[5]);
+      l2 = gx(S1z) + ge(S2z) - yl * r[3];
+      if (ax) {
+        const float V1 = v0ze * r16m + v0se * r54m;
+        const float V2 = v0zx * r16m + v0sx * r54m;
+        const float V3 = deta(V2, coef.seta, 0);
+        l0 = l0 + outer(V1);
+        if (i == 0) l0 = l0 + V3;
+        const float V1m = v0ze * r16p + v0se * r54p + y0 * 2.f * (r[1] - r[5]);
+        l1 = l1 + outer(V1m);
+        l2 = l2 + outer(V2);  // the reference adds V2 here, as it writes it
+      }
+    } else {
+      const float S1s = vze * r[0] + vse * r[4], S2s = vzx * r[0] + vsx * r[4];
+      const float S1p = vze * r[5] + vse * r[3], S2p = vzx * r[5] + vsx * r[3];
+      const float S1z = vze * r[4] + vse * r[2], S2z = vzx * r[4] + vsx * r[2];
+      l0 = gx(S1s) + ge(S2s) + yl * (r[1] - 2.f * r[5]);
+      l1 = -gx(S1p) - ge(S2p) + yl * (r[5] - 2.f * r[1]);
+      l2 = gx(S1z) + ge(S2z) - 2.f * yl * r[3];
+      if (ax) {
+        l0 = l0 + outer(v0ze * r[0] + y0 * (r[1] - 2.f * r[5]));
+        l1 = l1 + outer(-v0ze * r[5] + y0 * (r[5] - 2.f * r[1]));
+        l2 = l2 + outer(v0se * r[2]);
+      }
+    }
+    if (active) {
+      float *x = fa.fx + el * 75;
+      x[lane] = -l0;
+      x[25 + lane] = -l1;
+      x[50 + lane] = -l2;
+    }
+    __syncwarp();
   }
 }
 
@@ -1367,9 +1606,9 @@ template <int MODE, bool KAHAN>
 __device__ __forceinline__ float fluid_predicted(const StateArgs &st, int64_t g, float &k) {
   if (KAHAN) {
     k = st.cu[0][g];
-    return predict_comp(st.u[0][g], st.v[0][g], MODE == MODE_SYMPLECTIC ? 0.f : st.a[0][g], st.dt, st.hdt2, k);
+    return predict_comp(st.u[0][g], st.v[0][g], MODE == MODE_SYMPLECTIC ? 0.f : st.a[0][g], st, k);
   }
-  if (MODE == MODE_SYMPLECTIC) return fmaf(st.dt, st.v[0][g], st.u[0][g]);  // chi + dchi * coefd(i)
+  if (MODE == MODE_SYMPLECTIC) return st.u[0][g] + mul2(st.dt, st.dt_lo, st.v[0][g]);  // chi + dchi * coefd(i)
   return st.up[0][g];
 }
 
@@ -1393,36 +1632,69 @@ __global__ void __launch_bounds__(kThreads, 3) fluid_elem_kernel(const __grid_co
   pdl_trigger();
   if (!P::kMany && *p.at(0).st.blowup) return;  // uniform across the CTA
   const int32_t n = p.items(), stride = gridDim.x * kWarps;
-  // an element's loads that do not depend on its state
+  // Two stages ahead: an element's loads that do not depend on the state
+  // (its points, metric terms, info word) are issued two iterations before
+  // it is computed, its points' state one iteration before.
   struct Pre {
-    int32_t g, info;
+    int32_t sv, g, info;
     float mt[4];
   };
+  struct Raw {
+    float u, v, a, k;
+  };
   auto load = [&](int32_t it, Pre &q) {
-    const int sv = p.locate(it);
-    const FluidArgs &f = p.at(sv).fa;
-    int64_t el = it - p.first(sv);
+    q.sv = p.locate(it);
+    const FluidArgs &f = p.at(q.sv).fa;
+    int64_t el = it - p.first(q.sv);
     if (!AXG_BOUND(el, f.nel, 14)) el = 0;
     q.g = f.gidx[el * 25 + ml];
+    if (!AXG_BOUND(q.g, p.at(q.sv).st.nglob, 14)) q.g = 0;
     q.info = f.elinfo[el];
 #pragma unroll
     for (int t = 0; t < 4; ++t) q.mt[t] = t < NT ? f.metric[el * BS + t * 25 + ml] : 0.f;
   };
-  Pre nx{};
+  // the state fluid_predicted reads
+  auto load_raw = [&](const Pre &q, Raw &r) {
+    const StateArgs &st = p.at(q.sv).st;
+    if (KAHAN) {
+      r.u = st.u[0][q.g];
+      r.v = st.v[0][q.g];
+      r.a = MODE == MODE_SYMPLECTIC ? 0.f : st.a[0][q.g];
+      r.k = st.cu[0][q.g];
+    } else if (MODE == MODE_SYMPLECTIC) {
+      r.u = st.u[0][q.g];
+      r.v = st.v[0][q.g];
+    } else {
+      r.u = st.up[0][q.g];
+    }
+  };
+  Pre cur{}, nx{};
+  Raw raw{};
   int32_t it = blockIdx.x * kWarps + warp;
-  if (it < n) load(it, nx);
+  if (it < n) {
+    load(it, cur);
+    load_raw(cur, raw);
+  }
+  if (it + stride < n) load(it + stride, nx);
   for (; it < n; it += stride) {
-    const Pre cur = nx;
-    if (it + stride < n) load(it + stride, nx);
-    const int sv = p.locate(it);
+    Pre nx2{};
+    Raw raw_nx{};
+    if (it + stride < n) load_raw(nx, raw_nx);
+    if (it + 2 * stride < n) load(it + 2 * stride, nx2);
+    const int sv = cur.sv;
     const FluidArgs &f = p.at(sv).fa;
     const StateArgs &st = p.at(sv).st;
-    if (P::kMany && *st.blowup) continue;  // uniform across the warp
     const int64_t el = it - p.first(sv);
-    int32_t g = cur.g;
-    if (!AXG_BOUND(g, st.nglob, 14)) g = 0;
-    float kc = 0.f;
-    float chi = fluid_predicted<MODE, KAHAN>(st, g, kc);
+    // chi at the gather: as fluid_predicted computes it
+    float chi;
+    if (KAHAN) {
+      float k = raw.k;
+      chi = predict_comp(raw.u, raw.v, raw.a, st, k);
+    } else if (MODE == MODE_SYMPLECTIC) {
+      chi = raw.u + mul2(st.dt, st.dt_lo, raw.v);  // chi + dchi * coefd(i)
+    } else {
+      chi = raw.u;
+    }
     int axslot = (cur.info & 0xFFFFFF) - 1;
     if (axslot >= 0 && !AXG_BOUND((int64_t)axslot * 5 + 4, f.n_m0, 14)) axslot = -1;
     const int srcslot = ((cur.info >> 24) & 0xF) - 1;
@@ -1440,7 +1712,11 @@ __global__ void __launch_bounds__(kThreads, 3) fluid_elem_kernel(const __grid_co
     }
     if (NONMONO && ax && i == 0) fv = 0.f;
     if (f.fsmask && active) fv = fv * f.fsmask[el * 25 + lane];
-    if (active) f.fel[el * 25 + lane] = fv;
+    // (a stopped solve of a batch: its contributions are not used)
+    if (active && !(P::kMany && *st.blowup)) f.fel[el * 25 + lane] = fv;
+    cur = nx;
+    nx = nx2;
+    raw = raw_nx;
   }
 }
 
@@ -1483,17 +1759,17 @@ __global__ void __launch_bounds__(256) fluid_point_kernel(const __grid_constant_
   if (MODE == MODE_SYMPLECTIC) {
     if (KAHAN) {
       float k = st.cv[0][g];
-      vn = kahan_add(vel, st.kick * a, k);  // dchi + coefv(i) * ddchi, compensated
+      vn = kahan_add(vel, mul2(st.kick, st.kick_lo, a), k);  // dchi + coefv(i) * ddchi, compensated
       st.cv[0][g] = k;
     } else {
-      vn = fmaf(st.kick, a, vel);  // dchi + coefv(i) * ddchi
+      vn = vel + mul2(st.kick, st.kick_lo, a);  // dchi + coefv(i) * ddchi
     }
   } else if (KAHAN) {
     float k = st.cv[0][g];
-    vn = kahan_add(vel, st.hdt * (st.a[0][g] + a), k);
+    vn = kahan_add(vel, mul2(st.hdt, st.hdt_lo, st.a[0][g] + a), k);
     st.cv[0][g] = k;
   } else {
-    vn = fmaf(st.hdt, st.a[0][g] + a, vel);
+    vn = vel + mul2(st.hdt, st.hdt_lo, st.a[0][g] + a);
   }
   st.v[0][g] = vn;
   st.a[0][g] = a;
@@ -1503,7 +1779,7 @@ __global__ void __launch_bounds__(256) fluid_point_kernel(const __grid_constant_
   st.u[0][g] = un;
   if (KAHAN) st.cu[0][g] = zero ? 0.f : kc;
   // the next step's predictor (plain Newmark)
-  if (MODE == MODE_NEWMARK && !KAHAN) st.up[0][g] = predict(un, vn, a, st.dt, st.hdt2);
+  if (MODE == MODE_NEWMARK && !KAHAN) st.up[0][g] = predict(un, vn, a, st);
 }
 
 // The final drift of a symplectic step (SOLVER/time_evol_wave.F90:722-727):
@@ -1511,7 +1787,7 @@ __global__ void __launch_bounds__(256) fluid_point_kernel(const __grid_constant_
 // global point.
 struct DriftWork {
   StateArgs solid, fluid;
-  float cd;  // coefd(nstages + 1) deltat
+  float cd, cd_lo;  // coefd(nstages + 1) deltat, an FP32 pair
 };
 template <class P = One<DriftWork>>
 __global__ void drift_kernel(const __grid_constant__ P p) {
@@ -1520,17 +1796,17 @@ __global__ void drift_kernel(const __grid_constant__ P p) {
   const int sv = p.locate(it);
   const StateArgs &solid = p.at(sv).solid;
   const StateArgs &fluid = p.at(sv).fluid;
-  const float cd = p.at(sv).cd;
+  const float cd = p.at(sv).cd, cd_lo = p.at(sv).cd_lo;
   if (*solid.blowup) return;
   const int64_t q = it - p.first(sv);
   // u + coefd(nstages+1) v; compensated where the handle keeps compensation
   auto drift = [&](float *u, const float *v, float *cu) {
     if (cu) {
       float k = cu[q];
-      u[q] = kahan_add(u[q], cd * v[q], k);
+      u[q] = kahan_add(u[q], mul2(cd, cd_lo, v[q]), k);
       cu[q] = k;
     } else {
-      u[q] = fmaf(cd, v[q], u[q]);
+      u[q] = u[q] + mul2(cd, cd_lo, v[q]);
     }
   };
   if (q < solid.nglob)
@@ -1546,7 +1822,7 @@ __global__ void predict_kernel(StateArgs solid) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= solid.nglob) return;
   for (int c = 0; c < 3; ++c)
-    if (solid.up[c]) solid.up[c][q] = predict(solid.u[c][q], solid.v[c][q], solid.a[c][q], solid.dt, solid.hdt2);
+    if (solid.up[c]) solid.up[c][q] = predict(solid.u[c][q], solid.v[c][q], solid.a[c][q], solid);
 }
 
 // ------------------------------------------------------------ coupling pre-passes
@@ -1592,10 +1868,10 @@ __global__ void couple_to_fluid_kernel(const __grid_constant__ P p) {
     auto pred = [&](int c) {
       if (solid.cu[0]) {
         float k = solid.cu[c][gs];
-        return predict_comp(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid.dt, solid.hdt2, k);
+        return predict_comp(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid, k);
       }
       if (solid.up[0]) return solid.up[c][gs];
-      return predict(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid.dt, solid.hdt2);
+      return predict(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid);
     };
     const float us = pred(0);
     const float uz = pred(2);

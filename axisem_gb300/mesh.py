@@ -184,15 +184,14 @@ class Mesh:
             d.anel_true = 1
             d.n_sls = len(a["y_j"])
             d.do_corr_lowq = int(a.get("do_corr_lowq", 0))
-            d.att_coarse_grained = 1
+            full = "Y" in a  # attenuation at every GLL point (att_coarse_grained = .false.)
+            d.att_coarse_grained = 0 if full else 1
             d.y_j_attenuation = dp(a["y_j"])
             d.exp_w_j_deltat = dp(a["exp_w_j_deltat"])
             d.ts_fac_t = dp(a["ts_fac_t"])
             d.ts_fac_tm1 = dp(a["ts_fac_tm1"])
-            for nm in ("Q_mu", "Q_kappa", "delta_mu_cg4", "delta_kappa_cg4", "Y_cg4",
-                       "V_s_eta_cg4", "V_s_xi_cg4", "V_z_eta_cg4", "V_z_xi_cg4",
-                       "DsDeta_over_J_sol_cg4", "DzDeta_over_J_sol_cg4",
-                       "DsDxi_over_J_sol_cg4", "DzDxi_over_J_sol_cg4", "inv_s_solid"):
+            names = FULL_ATTENUATION if full else CG4_ATTENUATION
+            for nm in ("Q_mu", "Q_kappa", "inv_s_solid") + names:
                 setattr(d, nm, fp(a[nm]))
         d.inv_mass_rho_dp = dp(self.inv_mass_rho_dp)
         d.inv_mass_fluid_dp = dp(self.inv_mass_fluid_dp)
@@ -447,8 +446,12 @@ def coupled_mesh(ni: int, nj_solid: int, nj_fluid: int, src_type: int = _abi.MON
     return m
 
 
-def add_attenuation(m: Mesh, n_sls: int = 5, seed: int = 77, do_corr_lowq: bool = True) -> Mesh:
-    """Seeded coarse-grained (cg4) attenuation data for a mesh.
+def add_attenuation(m: Mesh, n_sls: int = 5, seed: int = 77, do_corr_lowq: bool = True,
+                    coarse_grained: bool = True) -> Mesh:
+    """Seeded coarse-grained (cg4) attenuation data for a mesh, or with
+    `coarse_grained` False the same at every GLL point (att_coarse_grained =
+    .false.: per point modulus defects and anelastic weights, the axial
+    elements' Y0 / V0_* vectors, the strain's mapping terms).
 
     SLS relaxation frequencies are log-spaced over the mesh's band and the
     coefficients y_j positive; the time-stepping factors follow the exact
@@ -487,10 +490,34 @@ def add_attenuation(m: Mesh, n_sls: int = 5, seed: int = 77, do_corr_lowq: bool 
         "DsDxi_over_J_sol_cg4": sgn(0.5, 2.0), "DzDxi_over_J_sol_cg4": sgn(0.5, 2.0),
         "inv_s_solid": inv_s,
     }
+    if not coarse_grained:
+        pt = lambda lo, hi: _f(rng.uniform(lo, hi, size=(5, 5, nel)))  # noqa: E731
+        spt = lambda lo, hi: _f(rng.uniform(lo, hi, size=(5, 5, nel)) * rng.choice([-1.0, 1.0], size=(5, 5, nel)))  # noqa: E731
+        ax = np.zeros(nel, dtype=bool)
+        ax[np.asarray(m.ax_el_solid, dtype=np.int64) - 1] = True
+        ax0 = lambda lo, hi: _f(np.where(ax[None, :], rng.uniform(lo, hi, size=(5, nel)), 0.0))  # noqa: E731
+        sax0 = lambda lo, hi: _f(np.where(ax[None, :], rng.uniform(lo, hi, size=(5, nel)) * rng.choice([-1.0, 1.0], size=(5, nel)), 0.0))  # noqa: E731
+        for nm in list(m.anel):
+            if nm.endswith("_cg4"):
+                del m.anel[nm]
+        m.anel.update({
+            "delta_mu": pt(1e9, 1e10), "delta_kappa": pt(1e9, 1e10), "Y": pt(0.5, 5.0),
+            "V_s_eta": spt(0.5, 5.0), "V_s_xi": spt(0.5, 5.0), "V_z_eta": spt(0.5, 5.0), "V_z_xi": spt(0.5, 5.0),
+            "Y0": ax0(0.5, 5.0), "V0_s_eta": sax0(0.5, 5.0), "V0_s_xi": sax0(0.5, 5.0),
+            "V0_z_eta": sax0(0.5, 5.0), "V0_z_xi": sax0(0.5, 5.0),
+            "DsDeta_over_J_sol": spt(0.5, 2.0), "DzDeta_over_J_sol": spt(0.5, 2.0),
+            "DsDxi_over_J_sol": spt(0.5, 2.0), "DzDxi_over_J_sol": spt(0.5, 2.0),
+        })
     return m
 
 
 PW_SOLID = ("DsDeta_over_J_sol", "DzDeta_over_J_sol", "DsDxi_over_J_sol", "DzDxi_over_J_sol", "inv_s_solid")
+CG4_ATTENUATION = ("delta_mu_cg4", "delta_kappa_cg4", "Y_cg4", "V_s_eta_cg4", "V_s_xi_cg4", "V_z_eta_cg4",
+                   "V_z_xi_cg4", "DsDeta_over_J_sol_cg4", "DzDeta_over_J_sol_cg4", "DsDxi_over_J_sol_cg4",
+                   "DzDxi_over_J_sol_cg4")
+FULL_ATTENUATION = ("delta_mu", "delta_kappa", "Y", "V_s_eta", "V_s_xi", "V_z_eta", "V_z_xi",
+                    "Y0", "V0_s_eta", "V0_s_xi", "V0_z_eta", "V0_z_xi",
+                    "DsDeta_over_J_sol", "DzDeta_over_J_sol", "DsDxi_over_J_sol", "DzDxi_over_J_sol")
 PW_FLUID = ("DsDeta_over_J_flu", "DzDeta_over_J_flu", "DsDxi_over_J_flu", "DzDxi_over_J_flu", "inv_s_fluid",
             "inv_rho_fluid")
 

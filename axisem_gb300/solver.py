@@ -120,15 +120,17 @@ class Solver:
     def get_state(self, field: int) -> np.ndarray:
         m = self.mesh
         nsls = max(int(m.anel.get("y_j").size), 1) if m.anel else 1
+        # memory variables at the cg4 points (1:4), or at every GLL point (0:4,0:4)
+        npt = 25 if (m.anel is not None and "Y" in m.anel) else 4
         if field in (_abi.FIELD_DISP, _abi.FIELD_VELO, _abi.FIELD_ACC0, _abi.FIELD_DISP_COMP,
                      _abi.FIELD_VELO_COMP):
             out = np.zeros((5, 5, m.nel_solid, 3), dtype=np.float32, order="F")
-        elif field == _abi.FIELD_MEMVAR:      # memory_var_cg4(1:4,6,n_sls,nel_solid)
-            out = np.zeros((4, 6, nsls, m.nel_solid), dtype=np.float32, order="F")
-        elif field == _abi.FIELD_ATT_SRC_TR:  # src_tr_tm1_glob_cg4(1:4,nel_solid)
-            out = np.zeros((4, m.nel_solid), dtype=np.float32, order="F")
-        elif field == _abi.FIELD_ATT_SRC_DEV:  # src_dev_tm1_glob_cg4(1:4,6,nel_solid)
-            out = np.zeros((4, 6, m.nel_solid), dtype=np.float32, order="F")
+        elif field == _abi.FIELD_MEMVAR:      # memory_var[_cg4](points,6,n_sls,nel_solid)
+            out = np.zeros((npt, 6, nsls, m.nel_solid), dtype=np.float32, order="F")
+        elif field == _abi.FIELD_ATT_SRC_TR:  # src_tr_tm1_glob[_cg4](points,nel_solid)
+            out = np.zeros((npt, m.nel_solid), dtype=np.float32, order="F")
+        elif field == _abi.FIELD_ATT_SRC_DEV:  # src_dev_tm1_glob[_cg4](points,6,nel_solid)
+            out = np.zeros((npt, 6, m.nel_solid), dtype=np.float32, order="F")
         else:
             out = np.zeros((5, 5, m.nel_fluid), dtype=np.float32, order="F")
         _check(self.lib, self.h, self.lib.axg_get_state(self.h, field, _fp(out)))

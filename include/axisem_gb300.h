@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define AXG_ABI_VERSION 2
+#define AXG_ABI_VERSION 3
 #define AXG_NPOL 4   /* only npol = 4 (5x5 GLL points) is supported, as the *_4 kernels */
 
 /* ---- status codes ---------------------------------------------------- */
@@ -139,7 +139,7 @@ typedef struct axg_mesh_desc {
   int32_t anel_true;
   int32_t n_sls;                                 /* n_sls_attenuation, 1..8 */
   int32_t do_corr_lowq;
-  int32_t att_coarse_grained;                    /* must be 1 when anel_true */
+  int32_t att_coarse_grained;                    /* 1: cg4 (below); 0: every GLL point (end of the struct) */
   const double *y_j_attenuation;                 /* (n_sls) */
   const double *exp_w_j_deltat;                  /* (n_sls) */
   const double *ts_fac_t, *ts_fac_tm1;           /* (n_sls) */
@@ -159,6 +159,17 @@ typedef struct axg_mesh_desc {
   const double *inv_mass_rho_dp;                 /* (0:4,0:4,nel_solid) */
   const double *inv_mass_fluid_dp;               /* (0:4,0:4,nel_fluid) */
   const double *source_term_el_dp;               /* (0:4,0:4,8,3) */
+
+  /* attenuation at every GLL point, when att_coarse_grained = 0
+   * (time_step_memvars_4, glob_anel_stiffness_{mono,di,quad}_4,
+   * SOLVER/attenuation.f90:210-334, 542-606); NULL otherwise.  Q_mu,
+   * Q_kappa and inv_s_solid are the fields above; the strain takes the
+   * data_pointwise mapping terms. */
+  const float *delta_mu, *delta_kappa;           /* (0:4,0:4,nel_solid) */
+  const float *Y, *V_s_eta, *V_s_xi, *V_z_eta, *V_z_xi;        /* (0:4,0:4,nel_solid) */
+  const float *Y0, *V0_s_eta, *V0_s_xi, *V0_z_eta, *V0_z_xi;   /* (0:4,nel_solid) */
+  const float *DsDeta_over_J_sol, *DzDeta_over_J_sol;
+  const float *DsDxi_over_J_sol, *DzDxi_over_J_sol;            /* (0:4,0:4,nel_solid) */
 } axg_mesh_desc;
 
 typedef struct axg_handle axg_handle;

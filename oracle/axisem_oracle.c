@@ -746,6 +746,340 @@ void ORC(time_step_memvars_cg4)(const axg_mesh_desc *d, REAL *memvar, const REAL
   free(ax);
 }
 
+/* axisym_gradient_solid / _fluid on one element
+ * (SOLVER/pointwise_derivatives.f90:329-365, 509-545):
+ *   mxm1 = G1T f (axial element) or G2T f, mxm2 = f G2,
+ *   d/ds = dzdeta * mxm1 + dzdxi * mxm2,  d/dz = dsdeta * mxm1 + dsdxi * mxm2
+ * (the reference's names of the mapping terms). */
+typedef struct pw_el {
+  const float *dsdeta, *dzdeta, *dsdxi, *dzdxi, *inv_s;
+} pw_el;
+
+static void grad_el(const spec *s, int axis, const pw_el *w, const REAL *f, REAL *gs, REAL *gz) {
+  mat5 m1, m2;
+  mxm_4(axis ? s->G1T : s->G2T, f, m1);
+  mxm_4(f, s->G2, m2);
+  for (int k = 0; k < 25; ++k) {
+    gs[k] = (REAL)w->dzdeta[k] * m1[k] + (REAL)w->dzdxi[k] * m2[k];
+    gz[k] = (REAL)w->dsdeta[k] * m1[k] + (REAL)w->dsdxi[k] * m2[k];
+  }
+}
+
+/* f_over_s_solid / _fluid on one element (SOLVER/pointwise_derivatives.f90:
+ * 130-178): inv_s * f, and at the axis (ipol = 0 of an axial element)
+ * L'Hospital's f/s = df/ds (dsdf_*_allaxis, always with G1T, :480-505). */
+static void f_over_s_el(const spec *s, int axis, const pw_el *w, const REAL *f, REAL *o) {
+  for (int k = 0; k < 25; ++k) o[k] = (REAL)w->inv_s[k] * f[k];
+  if (!axis) return;
+  mat5 m1, m2;
+  mxm_4(s->G1T, f, m1);
+  mxm_4(f, s->G2, m2);
+  for (int j = 0; j < 5; ++j) o[5 * j] = (REAL)w->dzdeta[5 * j] * m1[5 * j] + (REAL)w->dzdxi[5 * j] * m2[5 * j];
+}
+
+/* ------------------------------------------------ attenuation (full, npol = 4) */
+
+/* The not coarse-grained variant (att_coarse_grained = .false.): memory
+ * variables at all 25 GLL points.  Arrays per point (0:4,0:4,nel_solid):
+ * delta_mu, delta_kappa, Y, V_*; per axial element (0:4,nel_solid): Y0,
+ * V0_*; the strain uses the data_pointwise mapping terms and inv_s_solid. */
+
+/* the solid's data_pointwise terms of element e (the descriptor's copies) */
+static void pw_of(const axg_mesh_desc *d, int64_t e, pw_el *w) {
+  w->dsdeta = d->DsDeta_over_J_sol + 25 * e;
+  w->dzdeta = d->DzDeta_over_J_sol + 25 * e;
+  w->dsdxi = d->DsDxi_over_J_sol + 25 * e;
+  w->dzdxi = d->DzDxi_over_J_sol + 25 * e;
+  w->inv_s = d->inv_s_solid + 25 * e;
+}
+
+/* compute_strain_att_el_4, SOLVER/attenuation.f90:542-606: grad_u(0:4,0:4,6)
+ * in Voigt order, from axisym_gradient_solid_el_4 and f_over_s_solid_el_4
+ * (SOLVER/pointwise_derivatives.f90:104-126, 252-286). */
+static void strain_att_4(const axg_mesh_desc *d, const spec *s, int64_t e, int axis, const REAL *u1,
+                         const REAL *u2, const REAL *u3, REAL gu[7][25]) {
+  pw_el w;
+  pw_of(d, e, &w);
+  mat5 b1s, b1z, b2s, b2z, tmp, t, t2;
+  for (int c = 1; c <= 6; ++c)
+    for (int k = 0; k < 25; ++k) gu[c][k] = 0;
+  if (d->src_type == AXG_DIPOLE) {
+    for (int k = 0; k < 25; ++k) tmp[k] = u1[k] + u2[k];
+    grad_el(s, axis, &w, tmp, b1s, b1z);
+  } else {
+    grad_el(s, axis, &w, u1, b1s, b1z);
+  }
+  grad_el(s, axis, &w, u3, b2s, b2z);
+  for (int k = 0; k < 25; ++k) {
+    gu[1][k] = b1s[k];
+    gu[3][k] = b2z[k];
+    gu[5][k] = b1z[k] + b2s[k];
+  }
+  if (d->src_type == AXG_MONOPOLE) {
+    f_over_s_el(s, axis, &w, u1, t);
+    for (int k = 0; k < 25; ++k) gu[2][k] = t[k];
+  } else if (d->src_type == AXG_DIPOLE) {
+    f_over_s_el(s, axis, &w, u2, t);
+    for (int k = 0; k < 25; ++k) gu[2][k] = 2 * t[k];
+    for (int k = 0; k < 25; ++k) tmp[k] = u1[k] - u2[k];
+    grad_el(s, axis, &w, tmp, b1s, b1z);
+    f_over_s_el(s, axis, &w, u3, t);
+    for (int k = 0; k < 25; ++k) {
+      gu[4][k] = -t[k] - b1z[k];
+      gu[6][k] = -gu[2][k] - b1s[k];
+    }
+  } else {
+    for (int k = 0; k < 25; ++k) tmp[k] = u1[k] - 2 * u2[k];
+    f_over_s_el(s, axis, &w, tmp, t);
+    for (int k = 0; k < 25; ++k) gu[2][k] = t[k];
+    grad_el(s, axis, &w, u2, b1s, b1z);
+    f_over_s_el(s, axis, &w, u3, t);
+    for (int k = 0; k < 25; ++k) tmp[k] = u2[k] - 2 * u1[k];
+    f_over_s_el(s, axis, &w, tmp, t2);
+    for (int k = 0; k < 25; ++k) {
+      gu[4][k] = -2 * t[k] - b1z[k];
+      gu[6][k] = t2[k] - b1s[k];
+    }
+  }
+}
+
+/* time_step_memvars_4, SOLVER/attenuation.f90:210-334.
+ * memvar(0:4,0:4,6,n_sls,nel), src_tr_tm1(0:4,0:4,nel), src_dev_tm1(0:4,0:4,6,nel). */
+void ORC(time_step_memvars_4)(const axg_mesh_desc *d, REAL *memvar, const REAL *disp, REAL *src_tr_tm1_glob,
+                              REAL *src_dev_tm1_glob) {
+  spec s;
+  load_spec(d, &s);
+  const int64_t ne = d->nel_solid, cs = 25 * ne;
+  const int nsls = d->n_sls;
+  const double third = 1.0 / 3.0;
+  unsigned char *ax = axis_flags(d->nel_solid, d->naxel_solid, d->ax_el_solid);
+#pragma omp parallel
+  {
+  double a_mu[32], a_ka[32];
+  double Qmu_last = NAN, Qka_last = NAN;
+#pragma omp for schedule(static)
+  for (int64_t e = 0; e < ne; ++e) {
+    REAL gu[7][25];
+    strain_att_4(d, &s, e, ax[e], disp + 25 * e, disp + cs + 25 * e, disp + 2 * cs + 25 * e, gu);
+    if (!((double)d->Q_mu[e] == Qmu_last)) {
+      Qmu_last = d->Q_mu[e];
+      ORC(sls_weights)(d, Qmu_last, a_mu);
+    }
+    if (!((double)d->Q_kappa[e] == Qka_last)) {
+      Qka_last = d->Q_kappa[e];
+      ORC(sls_weights)(d, Qka_last, a_ka);
+    }
+    REAL tr[25], src_tr[25], src_dev[7][25];
+    for (int k = 0; k < 25; ++k) tr[k] = gu[1][k] + gu[2][k] + gu[3][k];
+    const float *dmu = d->delta_mu + 25 * e, *dka = d->delta_kappa + 25 * e;
+    for (int c = 1; c <= 6; ++c)
+      for (int k = 0; k < 25; ++k) src_dev[c][k] = 0;
+    for (int k = 0; k < 25; ++k) {
+      const REAL dm = (REAL)dmu[k];
+      src_tr[k] = (REAL)dka[k] * tr[k];
+      for (int c = 1; c <= 3; ++c)
+        src_dev[c][k] = (REAL)((double)(dm * 2) * ((double)gu[c][k] - (double)tr[k] * third));
+      src_dev[5][k] = dm * gu[5][k];
+      if (d->src_type != AXG_MONOPOLE) {
+        src_dev[4][k] = dm * gu[4][k];
+        src_dev[6][k] = dm * gu[6][k];
+      }
+    }
+    REAL *trm1 = src_tr_tm1_glob + 25 * e, *devm1 = src_dev_tm1_glob + 150 * e;
+    for (int j = 0; j < nsls; ++j) {
+      const double ft = d->ts_fac_t[j], ftm1 = d->ts_fac_tm1[j], ex = d->exp_w_j_deltat[j];
+      REAL *R = memvar + 25 * 6 * (j + (int64_t)nsls * e);
+      for (int k = 0; k < 25; ++k) {
+        const REAL trb = (REAL)(ft * a_ka[j] * src_tr[k] + ftm1 * a_ka[j] * trm1[k]);
+        REAL db[7];
+        for (int c = 1; c <= 6; ++c)
+          db[c] = (REAL)(ft * a_mu[j] * src_dev[c][k] + ftm1 * a_mu[j] * devm1[k + 25 * (c - 1)]);
+        R[k + 25 * 0] = (REAL)(ex * R[k + 25 * 0] + db[1] + trb);
+        R[k + 25 * 1] = (REAL)(ex * R[k + 25 * 1] + db[2] + trb);
+        R[k + 25 * 2] = (REAL)(ex * R[k + 25 * 2] + db[3] + trb);
+        R[k + 25 * 4] = (REAL)(ex * R[k + 25 * 4] + db[5]);
+        if (d->src_type != AXG_MONOPOLE) {
+          R[k + 25 * 3] = (REAL)(ex * R[k + 25 * 3] + db[4]);
+          R[k + 25 * 5] = (REAL)(ex * R[k + 25 * 5] + db[6]);
+        }
+      }
+    }
+    for (int k = 0; k < 25; ++k) {
+      trm1[k] = src_tr[k];
+      for (int c = 1; c <= 6; ++c) devm1[k + 25 * (c - 1)] = src_dev[c][k];
+    }
+  }
+  }
+  free(ax);
+}
+
+/* glob_anel_stiffness_{mono,di,quad}_4 (SOLVER/stiffness_mono.f90:409-507,
+ * SOLVER/stiffness_di.f90:604-723, SOLVER/stiffness_quad.f90:555-669):
+ * subtracts the divergence of the summed memory-variable stress.  The
+ * dipole's axial z term adds outerprod(G0, V2) as the reference writes it. */
+void ORC(anel_stiffness_4)(const axg_mesh_desc *d, const REAL *R, REAL *gs) {
+  spec s;
+  load_spec(d, &s);
+  const int64_t ne = d->nel_solid, cs = 25 * ne;
+  const int nsls = d->n_sls;
+  unsigned char *ax = axis_flags(d->nel_solid, d->naxel_solid, d->ax_el_solid);
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < ne; ++e) {
+    mat5 yl, vse, vsx, vze, vzx, r[7];
+    load_mat(yl, d->Y + 25 * e);
+    load_mat(vse, d->V_s_eta + 25 * e);
+    load_mat(vsx, d->V_s_xi + 25 * e);
+    load_mat(vze, d->V_z_eta + 25 * e);
+    load_mat(vzx, d->V_z_xi + 25 * e);
+    for (int c = 1; c <= 6; ++c)
+      for (int k = 0; k < 25; ++k) r[c][k] = 0;
+    for (int j = 0; j < nsls; ++j)
+      for (int c = 1; c <= 6; ++c)
+        for (int k = 0; k < 25; ++k) r[c][k] = r[c][k] + R[k + 25 * ((c - 1) + 6 * (j + (int64_t)nsls * e))];
+    const REAL *G = ax[e] ? s.G1 : s.G2;
+    vec5 y0l = {0}, v0se = {0}, v0sx = {0}, v0ze = {0}, v0zx = {0}, V1, V2, V3;
+    if (ax[e]) {
+      for (int k = 0; k < 5; ++k) {
+        y0l[k] = (REAL)d->Y0[5 * e + k];
+        v0se[k] = (REAL)d->V0_s_eta[5 * e + k];
+        v0sx[k] = (REAL)d->V0_s_xi[5 * e + k];
+        v0ze[k] = (REAL)d->V0_z_eta[5 * e + k];
+        v0zx[k] = (REAL)d->V0_z_xi[5 * e + k];
+      }
+    }
+    mat5 S1a, S2a, S1b, S2b, S1z, S2z, X1, X2, X3, X4, X5, X6, la, lb, lz, op;
+    REAL *g1 = gs + 25 * e, *g2 = g1 + cs, *g3 = g2 + cs;
+    if (d->src_type == AXG_MONOPOLE) {
+      for (int k = 0; k < 25; ++k) {
+        S1a[k] = vze[k] * r[1][k] + vse[k] * r[5][k];
+        S2a[k] = vzx[k] * r[1][k] + vsx[k] * r[5][k];
+        S1z[k] = vze[k] * r[5][k] + vse[k] * r[3][k];
+        S2z[k] = vzx[k] * r[5][k] + vsx[k] * r[3][k];
+      }
+      mxm_4(G, S1a, X1);
+      mxm_4(G, S1z, X3);
+      mxm_4(S2a, s.G2T, X2);
+      mxm_4(S2z, s.G2T, X4);
+      for (int k = 0; k < 25; ++k) {
+        la[k] = X1[k] + X2[k] + yl[k] * r[2][k];
+        lz[k] = X3[k] + X4[k];
+      }
+      if (ax[e]) {
+        for (int j = 0; j < 5; ++j) {
+          V1[j] = v0ze[j] * A(r[1], 0, j) + v0se[j] * A(r[5], 0, j) + y0l[j] * A(r[2], 0, j);
+          V2[j] = v0ze[j] * A(r[5], 0, j) + v0se[j] * A(r[3], 0, j);
+          V3[j] = v0zx[j] * A(r[5], 0, j) + v0sx[j] * A(r[3], 0, j);
+        }
+        outerprod_4(s.G0, V1, op);
+        for (int k = 0; k < 25; ++k) la[k] = la[k] + op[k];
+        vec5 V4;
+        vxm_4(V3, s.G2T, V4);
+        outerprod_4(s.G0, V2, op);
+        for (int k = 0; k < 25; ++k) lz[k] = lz[k] + op[k];
+        for (int j = 0; j < 5; ++j) A(lz, 0, j) = A(lz, 0, j) + V4[j];
+      }
+      for (int k = 0; k < 25; ++k) {
+        g1[k] = g1[k] - la[k];
+        g3[k] = g3[k] - lz[k];
+      }
+    } else if (d->src_type == AXG_DIPOLE) {
+      mat5 r16m, r54m, r16p, r54p;
+      for (int k = 0; k < 25; ++k) {
+        r16m[k] = r[1][k] - r[6][k];
+        r54m[k] = r[5][k] - r[4][k];
+        r16p[k] = r[1][k] + r[6][k];
+        r54p[k] = r[5][k] + r[4][k];
+        S1a[k] = vze[k] * r16m[k] + vse[k] * r54m[k];
+        S2a[k] = vzx[k] * r16m[k] + vsx[k] * r54m[k];
+        S1b[k] = vze[k] * r16p[k] + vse[k] * r54p[k];
+        S2b[k] = vzx[k] * r16p[k] + vsx[k] * r54p[k];
+        S1z[k] = vze[k] * r[5][k] + vse[k] * r[3][k];
+        S2z[k] = vzx[k] * r[5][k] + vsx[k] * r[3][k];
+      }
+      mxm_4(G, S1a, X1);
+      mxm_4(G, S1b, X3);
+      mxm_4(G, S1z, X5);
+      mxm_4(S2a, s.G2T, X2);
+      mxm_4(S2b, s.G2T, X4);
+      mxm_4(S2z, s.G2T, X6);
+      for (int k = 0; k < 25; ++k) {
+        la[k] = X1[k] + X2[k];
+        lb[k] = X3[k] + X4[k] + 2 * yl[k] * (r[2][k] - r[6][k]);
+        lz[k] = X5[k] + X6[k] - yl[k] * r[4][k];
+      }
+      if (ax[e]) {
+        for (int j = 0; j < 5; ++j) {
+          V1[j] = v0ze[j] * (A(r[1], 0, j) - A(r[6], 0, j)) + v0se[j] * (A(r[5], 0, j) - A(r[4], 0, j));
+          V2[j] = v0zx[j] * (A(r[1], 0, j) - A(r[6], 0, j)) + v0sx[j] * (A(r[5], 0, j) - A(r[4], 0, j));
+        }
+        vxm_4(V2, s.G2T, V3);
+        outerprod_4(s.G0, V1, op);
+        for (int k = 0; k < 25; ++k) la[k] = la[k] + op[k];
+        for (int j = 0; j < 5; ++j) A(la, 0, j) = A(la, 0, j) + V3[j];
+        for (int j = 0; j < 5; ++j)
+          V1[j] = v0ze[j] * (A(r[1], 0, j) + A(r[6], 0, j)) + v0se[j] * (A(r[5], 0, j) + A(r[4], 0, j)) +
+                  y0l[j] * 2 * (A(r[2], 0, j) - A(r[6], 0, j));
+        outerprod_4(s.G0, V1, op);
+        for (int k = 0; k < 25; ++k) lb[k] = lb[k] + op[k];
+        outerprod_4(s.G0, V2, op);  /* (V1 of the z component is formed but not used) */
+        for (int k = 0; k < 25; ++k) lz[k] = lz[k] + op[k];
+      }
+      for (int k = 0; k < 25; ++k) {
+        g1[k] = g1[k] - la[k];
+        g2[k] = g2[k] - lb[k];
+        g3[k] = g3[k] - lz[k];
+      }
+    } else {
+      for (int k = 0; k < 25; ++k) {
+        S1a[k] = vze[k] * r[1][k] + vse[k] * r[5][k];
+        S2a[k] = vzx[k] * r[1][k] + vsx[k] * r[5][k];
+        S1b[k] = vze[k] * r[6][k] + vse[k] * r[4][k];
+        S2b[k] = vzx[k] * r[6][k] + vsx[k] * r[4][k];
+        S1z[k] = vze[k] * r[5][k] + vse[k] * r[3][k];
+        S2z[k] = vzx[k] * r[5][k] + vsx[k] * r[3][k];
+      }
+      mxm_4(G, S1a, X1);
+      mxm_4(G, S1b, X3);
+      mxm_4(G, S1z, X5);
+      mxm_4(S2a, s.G2T, X2);
+      mxm_4(S2b, s.G2T, X4);
+      mxm_4(S2z, s.G2T, X6);
+      for (int k = 0; k < 25; ++k) {
+        la[k] = X1[k] + X2[k] + yl[k] * (r[2][k] - 2 * r[6][k]);
+        lb[k] = -X3[k] - X4[k] + yl[k] * (r[6][k] - 2 * r[2][k]);
+        lz[k] = X5[k] + X6[k] - 2 * yl[k] * r[4][k];
+      }
+      if (ax[e]) {
+        for (int j = 0; j < 5; ++j) V1[j] = v0ze[j] * A(r[1], 0, j) + y0l[j] * (A(r[2], 0, j) - 2 * A(r[6], 0, j));
+        outerprod_4(s.G0, V1, op);
+        for (int k = 0; k < 25; ++k) la[k] = la[k] + op[k];
+        for (int j = 0; j < 5; ++j) V1[j] = -v0ze[j] * A(r[6], 0, j) + y0l[j] * (A(r[6], 0, j) - 2 * A(r[2], 0, j));
+        outerprod_4(s.G0, V1, op);
+        for (int k = 0; k < 25; ++k) lb[k] = lb[k] + op[k];
+        for (int j = 0; j < 5; ++j) V1[j] = v0se[j] * A(r[3], 0, j);
+        outerprod_4(s.G0, V1, op);
+        for (int k = 0; k < 25; ++k) lz[k] = lz[k] + op[k];
+      }
+      for (int k = 0; k < 25; ++k) {
+        g1[k] = g1[k] - la[k];
+        g2[k] = g2[k] - lb[k];
+        g3[k] = g3[k] - lz[k];
+      }
+    }
+  }
+  free(ax);
+}
+
+/* the attenuation variant the descriptor selects */
+static void anel_stiffness(const axg_mesh_desc *d, const REAL *R, REAL *gs) {
+  if (d->att_coarse_grained) ORC(anel_stiffness_cg4)(d, R, gs);
+  else ORC(anel_stiffness_4)(d, R, gs);
+}
+static void time_step_memvars(const axg_mesh_desc *d, REAL *memvar, const REAL *disp, REAL *trm1, REAL *devm1) {
+  if (d->att_coarse_grained) ORC(time_step_memvars_cg4)(d, memvar, disp, trm1, devm1);
+  else ORC(time_step_memvars_4)(d, memvar, disp, trm1, devm1);
+}
+
 /* ------------------------------------------------------------ assembly */
 
 /* the edge-point walk of pdistsum_*: ipol fastest, interior points skipped */
@@ -941,7 +1275,7 @@ int ORC(time_loop)(const axg_mesh_desc *d, REAL *disp, REAL *velo, REAL *acc0, R
     /* solid */
     mask_solid(d, disp);
     ORC(stiffness_solid)(d, disp, acc1);
-    if (d->anel_true) ORC(anel_stiffness_cg4)(d, memvar, acc1);
+    if (d->anel_true) anel_stiffness(d, memvar, acc1);
     if (nef > 0) {
       for (int64_t p = 0; p < cf; ++p) ddchi1[p] = -(REAL)d->inv_mass_fluid[p] * ddchi1[p];
       if (d->have_absorbing_bc)
@@ -953,7 +1287,7 @@ int ORC(time_loop)(const axg_mesh_desc *d, REAL *disp, REAL *velo, REAL *acc0, R
     }
     mask_solid(d, acc1);
     ORC(pdistsum_solid)(d, acc1, 3);
-    if (d->anel_true) ORC(time_step_memvars_cg4)(d, memvar, disp, src_tr_tm1, src_dev_tm1);
+    if (d->anel_true) time_step_memvars(d, memvar, disp, src_tr_tm1, src_dev_tm1);
     for (int64_t p = 0; p < cf; ++p) {
       dchi[p] = (REAL)((double)dchi[p] + half_dt * (ddchi0[p] + ddchi1[p]));
       ddchi0[p] = ddchi1[p];
@@ -1069,7 +1403,7 @@ int ORC(time_loop_symplectic)(const axg_mesh_desc *d, int32_t nstages, const dou
       mask_solid(d, disp);
       ORC(stiffness_solid)(d, disp, acc);
       /* glob_anel_stiffness_*: the memory variables of the previous step */
-      if (d->anel_true) ORC(anel_stiffness_cg4)(d, memvar, acc);
+      if (d->anel_true) anel_stiffness(d, memvar, acc);
       if (nef > 0) {
         for (int64_t p = 0; p < cf; ++p) ddchi[p] = -ddchi[p] * (REAL)d->inv_mass_fluid[p];
         if (d->have_absorbing_bc)
@@ -1116,7 +1450,7 @@ int ORC(time_loop_symplectic)(const axg_mesh_desc *d, int32_t nstages, const dou
         disp[p + cs * c] = (REAL)((double)disp[p + cs * c] + (double)velo[p + cs * c] * coefd[nstages]);
     }
     /* time_step_memvars from the drifted displacement (SOLVER/time_evol_wave.F90:727-731) */
-    if (d->anel_true) ORC(time_step_memvars_cg4)(d, memvar, disp, src_tr_tm1, src_dev_tm1);
+    if (d->anel_true) time_step_memvars(d, memvar, disp, src_tr_tm1, src_dev_tm1);
     if (d->num_rec > 0 && rec && d->seis_it > 0 && iter % d->seis_it == 0) {
       if (*iseismo < nseismo_cap) {
         const int64_t n = nseismo_cap, is = *iseismo;
@@ -1165,37 +1499,6 @@ void ORC(gradient_cg4_all)(const axg_mesh_desc *d, const REAL *f, REAL *out) {
 
 
 /* ------------------------------------------------- kernel wavefield dumps */
-
-/* axisym_gradient_solid / _fluid on one element
- * (SOLVER/pointwise_derivatives.f90:329-365, 509-545):
- *   mxm1 = G1T f (axial element) or G2T f, mxm2 = f G2,
- *   d/ds = dzdeta * mxm1 + dzdxi * mxm2,  d/dz = dsdeta * mxm1 + dsdxi * mxm2
- * (the reference's names of the mapping terms). */
-typedef struct pw_el {
-  const float *dsdeta, *dzdeta, *dsdxi, *dzdxi, *inv_s;
-} pw_el;
-
-static void grad_el(const spec *s, int axis, const pw_el *w, const REAL *f, REAL *gs, REAL *gz) {
-  mat5 m1, m2;
-  mxm_4(axis ? s->G1T : s->G2T, f, m1);
-  mxm_4(f, s->G2, m2);
-  for (int k = 0; k < 25; ++k) {
-    gs[k] = (REAL)w->dzdeta[k] * m1[k] + (REAL)w->dzdxi[k] * m2[k];
-    gz[k] = (REAL)w->dsdeta[k] * m1[k] + (REAL)w->dsdxi[k] * m2[k];
-  }
-}
-
-/* f_over_s_solid / _fluid on one element (SOLVER/pointwise_derivatives.f90:
- * 130-178): inv_s * f, and at the axis (ipol = 0 of an axial element)
- * L'Hospital's f/s = df/ds (dsdf_*_allaxis, always with G1T, :480-505). */
-static void f_over_s_el(const spec *s, int axis, const pw_el *w, const REAL *f, REAL *o) {
-  for (int k = 0; k < 25; ++k) o[k] = (REAL)w->inv_s[k] * f[k];
-  if (!axis) return;
-  mat5 m1, m2;
-  mxm_4(s->G1T, f, m1);
-  mxm_4(f, s->G2, m2);
-  for (int j = 0; j < 5; ++j) o[5 * j] = (REAL)w->dzdeta[5 * j] * m1[5 * j] + (REAL)w->dzdxi[5 * j] * m2[5 * j];
-}
 
 /* compute_strain for one element of the solid (SOLVER/time_evol_wave.F90:
  * 1286-1345) or, from the fluid displacement (usz_s, usz_z), of the fluid

@@ -166,9 +166,11 @@ class TimeLoop:
         self.dchi = np.zeros_like(self.chi)
         self.ddchi0 = np.zeros_like(self.chi)
         nsls = 0 if m.anel is None else len(m.anel["y_j"])
-        self.memvar = np.zeros((4, 6, max(nsls, 1), m.nel_solid), dtype=self.nt, order="F")
-        self.src_tr_tm1 = np.zeros((4, m.nel_solid), dtype=self.nt, order="F")
-        self.src_dev_tm1 = np.zeros((4, 6, m.nel_solid), dtype=self.nt, order="F")
+        # memory variables at the cg4 points, or at every GLL point
+        npt = 25 if (m.anel is not None and "Y" in m.anel) else 4
+        self.memvar = np.zeros((npt, 6, max(nsls, 1), m.nel_solid), dtype=self.nt, order="F")
+        self.src_tr_tm1 = np.zeros((npt, m.nel_solid), dtype=self.nt, order="F")
+        self.src_dev_tm1 = np.zeros((npt, 6, m.nel_solid), dtype=self.nt, order="F")
         self.nseismo = m.niter // max(m.seis_it, 1) + 1
         self.rec = np.zeros((self.nseismo, 3, max(m.num_rec, 1)), dtype=np.float32, order="F")
         self.iseismo = C.c_int32(1)  # sample 0 is the iter-0 (zero) wavefield

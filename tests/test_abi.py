@@ -62,8 +62,10 @@ def _create(lib, desc):
     (lambda d: setattr(d, "src_type", 5), _abi.AXG_ERR_BAD_DESC, "src_type"),
     (lambda d: setattr(d, "nelsrc", 9), _abi.AXG_ERR_BAD_DESC, "nelsrc"),
     (lambda d: setattr(d, "seis_it", 0), _abi.AXG_ERR_BAD_DESC, "seis_it"),
-    (lambda d: (setattr(d, "anel_true", 1), setattr(d, "att_coarse_grained", 0)), _abi.AXG_ERR_UNSUPPORTED,
-     "coarse-grained"),
+    (lambda d: (setattr(d, "anel_true", 1), setattr(d, "att_coarse_grained", 2), setattr(d, "n_sls", 5)),
+     _abi.AXG_ERR_BAD_DESC, "att_coarse_grained"),
+    (lambda d: (setattr(d, "anel_true", 1), setattr(d, "att_coarse_grained", 0), setattr(d, "n_sls", 5)),
+     _abi.AXG_ERR_BAD_DESC, "attenuation arrays"),
     (lambda d: (setattr(d, "anel_true", 1), setattr(d, "att_coarse_grained", 1)), _abi.AXG_ERR_UNSUPPORTED,
      "n_sls"),
     (lambda d: (setattr(d, "anel_true", 1), setattr(d, "att_coarse_grained", 1), setattr(d, "n_sls", 5)),

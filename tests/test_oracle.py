@@ -124,6 +124,29 @@ def test_time_loop_float_double(orc, pole):
     assert np.abs(r64).max() > 0
 
 
+@pytest.mark.parametrize("pole", [0, 1, 2])
+def test_full_attenuation_float_double(orc, pole):
+    """time_step_memvars_4 / glob_anel_stiffness_*_4 (memory variables at
+    every GLL point) in the oracle's time loop: FP32 and FP64 agree, the
+    memory variables fill all 25 points (the monopole's components 4 and 6
+    stay zero), and the result differs from the cg4 variant's."""
+    from axisem_gb300.mesh import add_attenuation
+    m = add_attenuation(coupled_mesh(6, 4, 2, pole, niter=30, src_row=2), n_sls=3, seed=5, coarse_grained=False)
+    t32 = orc.TimeLoop(m, np.float32)
+    t64 = orc.TimeLoop(m, np.float64)
+    assert t32.run(1, m.niter) == 0 and t64.run(1, m.niter) == 0
+    r32, r64 = t32.receivers(), t64.receivers()
+    assert np.abs(r64).max() > 0
+    assert np.linalg.norm(r32 - r64) / np.linalg.norm(r64) < 1e-5
+    assert t64.memvar.shape[0] == 25 and (np.abs(t64.memvar).max(axis=(1, 2, 3)) > 0).all()
+    if pole == 0:
+        assert not t64.memvar[:, [3, 5]].any()
+    cg = add_attenuation(coupled_mesh(6, 4, 2, pole, niter=30, src_row=2), n_sls=3, seed=5)
+    tc = orc.TimeLoop(cg, np.float64)
+    assert tc.run(1, cg.niter) == 0
+    assert np.linalg.norm(tc.receivers() - r64) / np.linalg.norm(r64) > 1e-3
+
+
 def test_blowup_guard(orc):
     m = coupled_mesh(8, 4, 0, 0, niter=40)
     m.magnitude = 1e-20  # threshold 10 |magnitude| is exceeded as soon as the wave arrives
