@@ -130,6 +130,7 @@ class DumpDesc(C.Structure):
         ("out", _fp), ("capacity", C.c_int64),
         ("kwf_mask", _ip), ("mapping_ijel_ikwf", _ip), ("npoint_solid_kwf", C.c_int32),
         ("npoint_fluid_kwf", C.c_int32),
+        ("src_dump_mask", C.c_int32),
     ]
 
 

@@ -119,6 +119,7 @@ struct axg_handle {
   int64_t dev_bytes = 0;
   DomainDev ds, df;
   float *su[3] = {}, *sv[3] = {}, *sa[3] = {}, *sf[3] = {};
+  std::vector<int32_t> ielsrc;  // the source elements (0-based, solid or fluid as fluid_src says)
   float *sup[3] = {};  // the plain Newmark step's predicted displacement (kept by the last writers)
   float *fup = nullptr;  // ... and chi
   float *fu = nullptr, *fv = nullptr, *fa = nullptr, *ff = nullptr;
@@ -176,6 +177,7 @@ struct axg_handle {
     int32_t *kwf_s = nullptr, *kwf_f = nullptr;  // kernel wavefield layout: position of each element point or -1
     bool kwf = false;
     int64_t npt_s = 0, npt_f = 0;                // points per field in that layout
+    bool src_mask = false;                       // src_dump_type = 'mask'
     float *slot[2] = {};
     int64_t slot_floats = 0;
     cudaEvent_t ev_dump[2] = {}, ev_copy[2] = {};
@@ -933,6 +935,7 @@ void symplectic_stage_states(axg_handle *h, int i, StateArgs &ss, StateArgs &fs)
   split(h->sym_cd[i], ss.dt, ss.dt_lo);
   split(h->sym_cv[i], ss.kick, ss.kick_lo);
   ss.hdt2 = ss.hdt2_lo = 0.f;  // the coupling's predictor is then the drift u + coefd(i) v
+  ss.stage = fs.stage = 1;
   fs.dt = ss.dt;
   fs.dt_lo = ss.dt_lo;
   fs.kick = ss.kick;
@@ -1344,6 +1347,7 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
   h->absorbing = d->have_absorbing_bc != 0;
   h->dt = d->deltat;
   h->magnitude = d->magnitude;
+  for (int k = 0; k < d->nelsrc; ++k) h->ielsrc.push_back(d->ielsrc[k] - 1);
   h->anel = d->anel_true != 0 && d->att_coarse_grained != 0;
   h->anel_full = d->anel_true != 0 && d->att_coarse_grained == 0;
   CouplingHost cf, cs;
@@ -2049,6 +2053,9 @@ void launch_dump_pole(axg_handle *h, float *slot) {
   a.nglob = h->nglob_s;
   a.kwf = dp.kwf ? dp.kwf_s : nullptr;
   a.npt = dp.npt_s;
+  a.nsrcel = 0;
+  if (dp.src_mask)
+    for (int32_t e : h->ielsrc) a.srcel[a.nsrcel++] = e;
   const unsigned gs = (unsigned)std::min<int64_t>((h->nel_s + ws - 1) / ws, 16 * (int64_t)h->num_sms);
   wavefield_dump_kernel<POLE, false><<<gs, kThreads, 0, h->stream>>>(a, h->spec);
   if (h->nel_f > 0 && dp.nf > 0) {
@@ -2763,6 +2770,7 @@ int axg_set_wavefield_dump(axg_handle *h, const axg_dump_desc *dd) {
                                                     : std::vector<std::string>();
   dp.type = dd->dump_type;
   dp.strain_it = dd->strain_it;
+  dp.src_mask = dd->src_dump_mask != 0;
   dp.ibeg = dd->ibeg;
   dp.iend = dd->iend;
   dp.jbeg = dd->jbeg;

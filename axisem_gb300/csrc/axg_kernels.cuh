@@ -130,6 +130,7 @@ struct StateArgs {
   // kick = coefv(i) deltat; each an FP32 pair (value + _lo = the FP64 value)
   float dt, hdt, hdt2, dt_lo, hdt_lo, hdt2_lo;
   float kick, kick_lo;
+  int32_t stage;            // 1 in a symplectic stage (the gathers drift), 0 in a Newmark step
   SrcTable src;
   int64_t nglob;            // extent of the state arrays (checked builds)
   int32_t niter;            // extent of stf
@@ -281,10 +282,22 @@ __device__ __forceinline__ bool axis_masked(int comp) {
   return POLE == POLE_QUAD || (POLE == POLE_MONO ? comp == 0 : comp != 0);
 }
 
-// the predictor of the compensated mode: the same increment, added by
-// compensated summation
+// The predictor of the compensated mode: the increment's FP32 part, added by
+// compensated summation.  Its low-coefficient part was taken off the stored
+// compensation by the previous step's last writer (comp_after_step), so
+// that the gathers, which hold many points' values at once, need no more
+// registers than the increment takes.
 __device__ __forceinline__ float predict_comp(float d, float v, float a, const StateArgs &st, float &c) {
-  return kahan_add(d, pred_inc(v, a, st), c);
+  return kahan_add(d, fmaf(st.hdt2, a, st.dt * v), c);
+}
+// the compensation a last writer stores with the new state: c less the low
+// part of the next predictor's increment deltat*velo + half_dt_sq*acc0
+__device__ __forceinline__ float comp_after_step(float c, float v, float a, const StateArgs &st) {
+  return c - fmaf(st.hdt2_lo, a, st.dt_lo * v);
+}
+// a symplectic stage's compensated drift disp + coefd(i) velo
+__device__ __forceinline__ float drift_comp(float d, float v, const StateArgs &st, float &c) {
+  return kahan_add(d, mul2(st.dt, st.dt_lo, v), c);
 }
 
 // X(i,j) = sum_k c[k] * v(k,j)   (v(k,j) held by lane k + 5 j)
@@ -1003,7 +1016,8 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
             if (KAHAN) {
               float k = ok ? st.cu[gc(c)][g] : 0.f;
               // (a symplectic stage: hdt2 = 0, the compensated drift u + coefd(i) v)
-              if (ok) u = predict_comp(u, st.v[gc(c)][g], MODE == MODE_SYMPLECTIC ? 0.f : st.a[gc(c)][g], st, k);
+              if (ok && MODE == MODE_SYMPLECTIC) u = drift_comp(u, st.v[gc(c)][g], st, k);
+              else if (ok) u = predict_comp(u, st.v[gc(c)][g], st.a[gc(c)][g], st, k);
               cc[KAHAN ? q : 0][c] = k;
             } else if (ok && MODE == MODE_SYMPLECTIC) {
               u = u + mul2(st.dt, st.dt_lo, st.v[gc(c)][g]);  // drift: disp + velo * coefd(i)
@@ -1249,7 +1263,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
               float k = kv[KAHAN ? q : 0][c];
               vn = kahan_add(vel[q][c], mul2(st.hdt, st.hdt_lo, acc[q][c] + a), k);
               st.cv[cg][g] = k;
-              st.cu[cg][g] = s_cu[c][spos(t)];
+              st.cu[cg][g] = comp_after_step(s_cu[c][spos(t)], vn, a, st);
             } else {
               vn = vel[q][c] + mul2(st.hdt, st.hdt_lo, acc[q][c] + a);
             }
@@ -1606,7 +1620,8 @@ template <int MODE, bool KAHAN>
 __device__ __forceinline__ float fluid_predicted(const StateArgs &st, int64_t g, float &k) {
   if (KAHAN) {
     k = st.cu[0][g];
-    return predict_comp(st.u[0][g], st.v[0][g], MODE == MODE_SYMPLECTIC ? 0.f : st.a[0][g], st, k);
+    if (MODE == MODE_SYMPLECTIC) return drift_comp(st.u[0][g], st.v[0][g], st, k);
+    return predict_comp(st.u[0][g], st.v[0][g], st.a[0][g], st, k);
   }
   if (MODE == MODE_SYMPLECTIC) return st.u[0][g] + mul2(st.dt, st.dt_lo, st.v[0][g]);  // chi + dchi * coefd(i)
   return st.up[0][g];
@@ -1689,7 +1704,7 @@ __global__ void __launch_bounds__(kThreads, 3) fluid_elem_kernel(const __grid_co
     float chi;
     if (KAHAN) {
       float k = raw.k;
-      chi = predict_comp(raw.u, raw.v, raw.a, st, k);
+      chi = MODE == MODE_SYMPLECTIC ? drift_comp(raw.u, raw.v, st, k) : predict_comp(raw.u, raw.v, raw.a, st, k);
     } else if (MODE == MODE_SYMPLECTIC) {
       chi = raw.u + mul2(st.dt, st.dt_lo, raw.v);  // chi + dchi * coefd(i)
     } else {
@@ -1777,7 +1792,7 @@ __global__ void __launch_bounds__(256) fluid_point_kernel(const __grid_constant_
   const bool zero = NONMONO && (s0 & kFlAxis);
   const float un = zero ? 0.f : chi;
   st.u[0][g] = un;
-  if (KAHAN) st.cu[0][g] = zero ? 0.f : kc;
+  if (KAHAN) st.cu[0][g] = zero ? 0.f : (MODE == MODE_NEWMARK ? comp_after_step(kc, vn, a, st) : kc);
   // the next step's predictor (plain Newmark)
   if (MODE == MODE_NEWMARK && !KAHAN) st.up[0][g] = predict(un, vn, a, st);
 }
@@ -1868,6 +1883,7 @@ __global__ void couple_to_fluid_kernel(const __grid_constant__ P p) {
     auto pred = [&](int c) {
       if (solid.cu[0]) {
         float k = solid.cu[c][gs];
+        if (solid.stage) return drift_comp(solid.u[c][gs], solid.v[c][gs], solid, k);
         return predict_comp(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid, k);
       }
       if (solid.up[0]) return solid.up[c][gs];
@@ -1993,6 +2009,8 @@ struct DumpArgs {
   int32_t type, ibeg, iend, jbeg, jend;
   const int32_t *kwf;      // kernel wavefield layout: position of each element point (25, nel), -1: none; or null
   int64_t npt;             // points per field in that layout
+  int32_t nsrcel;          // solid: elements whose values are dumped as zero (src_dump_type = 'mask')
+  int32_t srcel[8];        // ... their 0-based indices
 };
 
 struct DumpLane {
@@ -2040,7 +2058,13 @@ __global__ void __launch_bounds__(kThreads) wavefield_dump_kernel(DumpArgs a, Sp
     const DumpLane w{a.pw[0][q], a.pw[1][q], a.pw[2][q], a.pw[3][q], a.pw[4][q]};
     int fld = 0;
     const int32_t kpos = a.kwf && active ? a.kwf[q] : -1;
+    // src_dump_type = 'mask': the source elements' solid values are zero
+    // (eradicate_src_elem_values, SOLVER/wavefields_io.f90:1123-1153)
+    bool masked = false;
+    if (!FLUID)
+      for (int k = 0; k < a.nsrcel && k < 8; ++k) masked = masked || a.srcel[k] == e;
     auto put = [&](float val) {
+      if (masked) val = 0.f;
       if (a.kwf) {
         if (kpos >= 0 && AXG_BOUND(kpos, a.npt, 42)) a.out[fld * a.npt + kpos] = val;
       } else if (mine) {

@@ -584,12 +584,16 @@ def kwf_mapping(m: Mesh, ibeg: int = 0, iend: int = 4, jbeg: int = 0, jend: int 
 
 
 def dump_desc(m: Mesh, dump_type: int, strain_it: int, out: np.ndarray | None, capacity: int,
-              ibeg: int = 0, iend: int = 4, jbeg: int = 0, jend: int = 4, kwf=None) -> _abi.DumpDesc:
+              ibeg: int = 0, iend: int = 4, jbeg: int = 0, jend: int = 4, kwf=None,
+              src_mask: bool = False) -> _abi.DumpDesc:
     """An axg_dump_desc for the mesh's pointwise arrays; keeps them alive.
     kwf: (kwf_mask, mapping_ijel_ikwf, npoint_solid_kwf, npoint_fluid_kwf)
-    for the kernel wavefield point layout, or None."""
+    for the kernel wavefield point layout, or None; src_mask: the
+    reference's src_dump_type = 'mask' (the source elements' solid values
+    zeroed)."""
     dd = _abi.DumpDesc()
     dd.dump_type, dd.strain_it = dump_type, strain_it
+    dd.src_dump_mask = int(src_mask)
     dd.ibeg, dd.iend, dd.jbeg, dd.jend = ibeg, iend, jbeg, jend
     keep = []
     for nm in PW_SOLID + PW_FLUID:

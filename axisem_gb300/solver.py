@@ -182,14 +182,15 @@ class Solver:
         _check(self.lib, self.h, self.lib.axg_set_compensated(self.h, int(bool(on))))
 
     def set_wavefield_dump(self, dump_type: int, strain_it: int = 1, capacity: int = 1, ibeg: int = 0,
-                           iend: int = 4, jbeg: int = 0, jend: int = 4, out: np.ndarray | None = None, kwf=None):
+                           iend: int = 4, jbeg: int = 0, jend: int = 4, out: np.ndarray | None = None, kwf=None,
+                           src_mask: bool = False):
         """axg_set_wavefield_dump with the mesh's data_pointwise arrays
         (mesh.add_pointwise).  Returns the snapshot buffer, (capacity,
         floats_per_snapshot) float32 (`out` if given: page-locked memory lets
-        the copies overlap the steps)."""
+        the copies overlap the steps).  src_mask: src_dump_type = 'mask'."""
         from .mesh import dump_desc
         probe = np.zeros(1, dtype=np.float32)
-        dd = dump_desc(self.mesh, dump_type, strain_it, probe, 1, ibeg, iend, jbeg, jend, kwf)
+        dd = dump_desc(self.mesh, dump_type, strain_it, probe, 1, ibeg, iend, jbeg, jend, kwf, src_mask)
         _check(self.lib, self.h, self.lib.axg_set_wavefield_dump(self.h, C.byref(dd)))
         if dump_type == _abi.DUMP_NONE:
             self._dump = None
@@ -199,7 +200,7 @@ class Solver:
             out = np.zeros((capacity, floats), dtype=np.float32)
         if out.dtype != np.float32 or not out.flags.c_contiguous or out.size < capacity * floats:
             raise ValueError(f"out must be C-contiguous float32 with room for {capacity} x {floats}")
-        dd = dump_desc(self.mesh, dump_type, strain_it, out, capacity, ibeg, iend, jbeg, jend, kwf)
+        dd = dump_desc(self.mesh, dump_type, strain_it, out, capacity, ibeg, iend, jbeg, jend, kwf, src_mask)
         _check(self.lib, self.h, self.lib.axg_set_wavefield_dump(self.h, C.byref(dd)))
         self._dump = (out, dd)
         return out

@@ -468,6 +468,11 @@ typedef struct axg_dump_desc {
   const int32_t *kwf_mask;
   const int32_t *mapping_ijel_ikwf;
   int32_t npoint_solid_kwf, npoint_fluid_kwf;
+  /* src_dump_type = 'mask' (the reference's default, SOLVER/parameters.F90:
+   * 399): 1 zeroes every solid field on the points of the source elements
+   * ielsrc (eradicate_src_elem_values / _vec_values,
+   * SOLVER/wavefields_io.f90:1123-1153); 0 dumps them as computed. */
+  int32_t src_dump_mask;
 } axg_dump_desc;
 
 int axg_set_wavefield_dump(axg_handle *h, const axg_dump_desc *dd);

@@ -1568,6 +1568,17 @@ static void put_el(const axg_dump_desc *dd, REAL *out, int64_t nel, int64_t e, i
     for (int i = 0; i < ni; ++i) o[i + ni * j] = f[(dd->ibeg + i) + 5 * (dd->jbeg + j)];
 }
 
+/* a solid field of element e, zero where the source mask applies */
+static void put_sol(const axg_dump_desc *dd, REAL *out, int64_t nel, int64_t e, int64_t fld, int masked,
+                    const REAL *f) {
+  mat5 z;
+  if (masked) {
+    for (int k = 0; k < 25; ++k) z[k] = 0;
+    f = z;
+  }
+  put_el(dd, out, nel, e, fld, f);
+}
+
 /* One snapshot of dump_stuff's fields (the layout of axg_wavefield_dump_layout)
  * from the element-local state; returns the number of fields written. */
 int ORC(wavefield_dump)(const axg_mesh_desc *d, const axg_dump_desc *dd, const REAL *disp, const REAL *velo,
@@ -1595,6 +1606,12 @@ int ORC(wavefield_dump)(const axg_mesh_desc *d, const axg_dump_desc *dd, const R
     const int64_t off = 25 * e;
     const pw_el w = {dd->DsDeta_over_J_sol + off, dd->DzDeta_over_J_sol + off, dd->DsDxi_over_J_sol + off,
                      dd->DzDxi_over_J_sol + off, dd->inv_s_solid + off};
+    /* src_dump_type = 'mask': eradicate_src_elem_values / _vec_values
+     * (SOLVER/wavefields_io.f90:1123-1153) zero the solid fields of the
+     * elements ielsrc (taken as solid elements, as the reference does) */
+    int masked = 0;
+    if (dd->src_dump_mask)
+      for (int k = 0; k < d->nelsrc; ++k) masked |= d->ielsrc[k] - 1 == e;
     const REAL *u1 = disp + off, *u2 = disp + 25 * nes + off, *u3 = disp + 50 * nes + off;
     const REAL *vv1 = velo + off, *vv2 = velo + 25 * nes + off, *vv3 = velo + 50 * nes + off;
     int fld = 0;
@@ -1602,7 +1619,7 @@ int ORC(wavefield_dump)(const axg_mesh_desc *d, const axg_dump_desc *dd, const R
     const REAL *vecs[2][3] = {{u1, u2, u3}, {vv1, vv2, vv3}};
     if (type == AXG_DUMP_STRAIN_ONLY || type == AXG_DUMP_FULLFIELDS) {
       strain_el(&s, axs[e], &w, pole, 0, u1, u2, u3, o);
-      for (int q = 0; q < (nonmono ? 6 : 4); ++q) put_el(dd, out, nes, e, fld++, o[q]);
+      for (int q = 0; q < (nonmono ? 6 : 4); ++q) put_sol(dd, out, nes, e, fld++, masked, o[q]);
     }
     for (int which = 0; which < 2; ++which) {
       const int want = which == 0 ? (type == AXG_DUMP_DISPL_ONLY || type == AXG_DUMP_DISPL_VELO)
@@ -1615,9 +1632,9 @@ int ORC(wavefield_dump)(const axg_mesh_desc *d, const axg_dump_desc *dd, const R
         v3[1][k] = (global && pole == AXG_DIPOLE) ? x[0][k] - x[1][k] : x[1][k];
         v3[2][k] = x[2][k];
       }
-      put_el(dd, out, nes, e, fld++, v3[0]);
-      if (nonmono) put_el(dd, out, nes, e, fld++, v3[1]);
-      put_el(dd, out, nes, e, fld++, v3[2]);
+      put_sol(dd, out, nes, e, fld++, masked, v3[0]);
+      if (nonmono) put_sol(dd, out, nes, e, fld++, masked, v3[1]);
+      put_sol(dd, out, nes, e, fld++, masked, v3[2]);
     }
   }
   free(axs);

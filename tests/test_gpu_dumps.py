@@ -25,10 +25,11 @@ def _mesh(pole, niter=24, **kw):
     return add_pointwise(coupled_mesh(10, 5, 4, pole, niter=niter, **kw))
 
 
-def _check_snapshots(m, dump_type, snaps, ns, nf, names, strain_it, rng_ij=(0, 4, 0, 4), comp=False):
+def _check_snapshots(m, dump_type, snaps, ns, nf, names, strain_it, rng_ij=(0, 4, 0, 4), comp=False,
+                     src_mask=False):
     np_el = (rng_ij[1] - rng_ij[0] + 1) * (rng_ij[3] - rng_ij[2] + 1)
     nes, nef = m.nel_solid, m.nel_fluid
-    dd = dump_desc(m, dump_type, strain_it, None, 1, *rng_ij)
+    dd = dump_desc(m, dump_type, strain_it, None, 1, *rng_ij, src_mask=src_mask)
     with Solver(m) as s:
         s.set_compensated(comp)
         for k in range(snaps.shape[0]):
@@ -96,6 +97,32 @@ def test_dump_compensated_and_names(gpu_lib):
                          "strain_dsup_sol", "strain_dzup_sol"]
     assert names[6:] == [n.replace("_sol", "_flu") for n in names[:6]]
     _check_snapshots(m, _abi.DUMP_STRAIN_ONLY, snaps, ns, nf, names, 8, comp=True)
+
+
+@pytest.mark.parametrize("dtype_", [_abi.DUMP_DISPL_ONLY, _abi.DUMP_FULLFIELDS])
+def test_dump_source_mask(gpu_lib, dtype_):
+    """src_dump_type = 'mask' (the reference's default): the solid fields
+    are zero on the source elements and as without the mask elsewhere; the
+    whole snapshot against the oracle's masked dump."""
+    m = _mesh(1, niter=16)
+    with Solver(m) as s:
+        snaps = s.set_wavefield_dump(dtype_, 8, capacity=2, src_mask=True)
+        ns, nf, _, names = s.dump_layout()
+        s.run()
+    with Solver(m) as s:
+        plain = s.set_wavefield_dump(dtype_, 8, capacity=2)
+        s.run()
+    nes = m.nel_solid
+    src = np.asarray(m.ielsrc[:m.nelsrc], dtype=np.int64) - 1
+    for q in range(ns):
+        a = snaps[:, q * nes * 25:(q + 1) * nes * 25].reshape(2, nes, 25)
+        b = plain[:, q * nes * 25:(q + 1) * nes * 25].reshape(2, nes, 25)
+        assert not a[:, src].any()
+        keep = np.setdiff1d(np.arange(nes), src)
+        assert np.array_equal(a[:, keep], b[:, keep])
+        assert np.abs(b[:, src]).max() > 0 or q == 1
+    assert np.array_equal(snaps[:, ns * nes * 25:], plain[:, ns * nes * 25:])   # the fluid is not masked
+    _check_snapshots(m, dtype_, snaps, ns, nf, names, 8, src_mask=True)
 
 
 def test_dump_errors(gpu_lib):
