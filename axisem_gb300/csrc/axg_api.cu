@@ -396,30 +396,37 @@ std::vector<T> per_point(const T *elem, const std::vector<int32_t> &igloc, int64
 // its flags (a coupling pre-pass partial sum; on the axis); always (this
 // solve): the element info words (source slot), the fluid source terms and
 // the per-copy contribution buffer.
-int build_fluid_passes(axg_handle *h, const axg_mesh_desc *d, const DomainPlan &pl, DomainDev &dd, bool mesh_part,
-                       const std::vector<float> &metric, const std::vector<int32_t> &elinfo,
+int build_fluid_passes(axg_handle *h, const axg_mesh_desc *d, const std::vector<int32_t> &order, DomainDev &dd,
+                       bool mesh_part, const std::vector<float> &metric, const std::vector<int32_t> &elinfo,
                        const std::vector<float> &m0, const std::vector<float> &fsmask, int nax, const int32_t *axl) {
-  const int64_t nel = pl.nel, nglob = h->nglob_f;
+  const int64_t nel = (int64_t)order.size(), nglob = h->nglob_f, nch = fl_chunks(nel);
   int rc;
   if (mesh_part) {
-    std::vector<int32_t> gidx((size_t)25 * nel), start(nglob + 1, 0), ent((size_t)25 * nel);
+    if (nch * 25 * kFlChunk >= (int64_t)INT32_MAX) return fail(h, AXG_ERR_BAD_DESC, "fluid mesh too large");
+    std::vector<int32_t> gidx((size_t)nch * 25 * kFlChunk, 0), start(nglob + 1, 0), ent((size_t)25 * nel);
     for (int64_t s = 0; s < nel; ++s) {
-      const int64_t e = pl.elem_order[s];
+      const int64_t e = order[s];
       for (int k = 0; k < 25; ++k) {
         const int32_t g = h->igloc_f[25 * e + k] - 1;  // internal numbering
-        gidx[25 * s + k] = g;
+        gidx[fl_at(s, k, 25)] = g;
         start[g + 1]++;
       }
     }
     for (int64_t g = 0; g < nglob; ++g) start[g + 1] += start[g];
     if (start[nglob] >= (int64_t)kFlStartMask) return fail(h, AXG_ERR_BAD_DESC, "fluid mesh too large");
     {
+      // copies in slot order: each point's contributions are summed in the
+      // order of its elements' slots
       std::vector<int32_t> fill(start.begin(), start.end() - 1);
-      for (int64_t c = 0; c < 25 * nel; ++c) ent[fill[gidx[c]]++] = (int32_t)c;  // copies in slot order
+      for (int64_t s = 0; s < nel; ++s)
+        for (int k = 0; k < 25; ++k) {
+          const int64_t c = fl_at(s, k, 25);
+          ent[fill[gidx[c]]++] = (int32_t)c;
+        }
     }
     // flags: the coupling pre-pass's receiving points, the points on the axis
     for (size_t g = 0; g < h->pre_f.size(); ++g)
-      if (h->pre_f[g]) start[pl.new_of_old[g]] |= (int32_t)kFlPartial;
+      if (h->pre_f[g]) start[h->pf.new_of_old[g]] |= (int32_t)kFlPartial;
     for (int k = 0; k < nax; ++k)
       for (int jj = 0; jj < 5; ++jj) start[h->igloc_f[25 * (int64_t)(axl[k] - 1) + 5 * jj] - 1] |= (int32_t)kFlAxis;
     h->in_mesh = true;
@@ -434,7 +441,7 @@ int build_fluid_passes(axg_handle *h, const axg_mesh_desc *d, const DomainPlan &
     dd.n_m0 = (int64_t)m0.size();
   }
   if ((rc = upload(h, &dd.elinfo, elinfo))) return rc;
-  if ((rc = dalloc(h, &dd.fel, (size_t)25 * nel))) return rc;
+  if ((rc = dalloc(h, &dd.fel, (size_t)nch * 25 * kFlChunk))) return rc;
   if (d->fluid_src && d->nelsrc > 0) {
     std::vector<float> s((size_t)8 * 25, 0.f);
     for (int k = 0; k < d->nelsrc; ++k)
@@ -467,23 +474,29 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid, bool mesh_pa
     slots = solid_slots(pole);
     nt = (int)slots.size();
   }
-  // solid blocks carry the element's point indices and info word inline
-  const int bs = fluid ? block_stride(nt) : solid_block_stride(nt);
-  std::vector<float> metric(mesh_part ? (size_t)nel * bs : 0, 0.f);
+  // solid blocks carry the element's point indices and info word inline; the
+  // fluid's element arrays are chunked (fl_at), its slots the plan's launch
+  // order with the axial elements moved to the end, so that the element
+  // pass's warps of 32 slots seldom mix axial and other elements
+  const int bs = fluid ? 25 * nt : solid_block_stride(nt);
+  const int64_t nslots = fluid ? fl_chunks(nel) * kFlChunk : nel;
+  std::vector<float> metric(mesh_part ? (size_t)nslots * bs : 0, 0.f);
   std::vector<int32_t> elinfo(nel, 0);
   const std::vector<int> aslots = fluid ? std::vector<int>{0} : axial_slots(pole);
   const int na = (int)aslots.size();
   std::vector<float> m0;
   std::vector<float> fsmask;
   const bool use_fs = fluid && d->fluid_free_surface_mask != nullptr;
-  if (use_fs && mesh_part) fsmask.resize((size_t)nel * 25);
+  if (use_fs && mesh_part) fsmask.resize((size_t)nslots * 25);
   // source slot of each element
   std::vector<int8_t> srcslot(nel, -1);
   if (d->nelsrc > 0 && (bool)d->fluid_src == fluid)
     for (int k = 0; k < d->nelsrc; ++k) srcslot[d->ielsrc[k] - 1] = (int8_t)k;
+  std::vector<int32_t> order = pl.elem_order;
+  if (fluid) std::stable_partition(order.begin(), order.end(), [&](int32_t e) { return !axial[e]; });
   int32_t axcount = 0;
   for (int64_t s = 0; s < nel; ++s) {
-    const int64_t e = pl.elem_order[s];
+    const int64_t e = order[s];
     int32_t info = 0;
     if (axial[e]) {
       info = axcount + 1;
@@ -496,19 +509,22 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid, bool mesh_pa
     if (srcslot[e] >= 0) info |= (srcslot[e] + 1) << 24;
     elinfo[s] = info;
     if (!mesh_part) continue;
-    float *blk = metric.data() + (size_t)s * bs;
-    for (int t = 0; t < nt; ++t) {
-      const float *src = fluid ? d->m_fluid[t] : d->m_solid[slots[t]];
-      std::memcpy(blk + 25 * t, src + 25 * e, 25 * sizeof(float));
+    if (fluid) {
+      for (int t = 0; t < nt; ++t)
+        for (int q = 0; q < 25; ++q) metric[fl_at(s, 25 * t + q, bs)] = d->m_fluid[t][25 * e + q];
+      if (use_fs)
+        for (int q = 0; q < 25; ++q) fsmask[fl_at(s, q, 25)] = d->fluid_free_surface_mask[25 * e + q];
+      continue;
     }
-    if (!fluid) {
+    float *blk = metric.data() + (size_t)s * bs;
+    for (int t = 0; t < nt; ++t) std::memcpy(blk + 25 * t, d->m_solid[slots[t]] + 25 * e, 25 * sizeof(float));
+    {
       // the solid kernel reads only the axial slot of this info word
       std::memcpy(blk + solid_idx_off(nt), &pl.elem_pts[25 * s], 25 * sizeof(uint16_t));
       std::memcpy(blk + solid_info_off(nt), &info, sizeof(int32_t));
     }
-    if (use_fs) std::memcpy(fsmask.data() + 25 * s, d->fluid_free_surface_mask + 25 * e, 25 * sizeof(float));
   }
-  if (fluid) return build_fluid_passes(h, d, pl, dd, mesh_part, metric, elinfo, m0, fsmask, nax, axl);
+  if (fluid) return build_fluid_passes(h, d, order, dd, mesh_part, metric, elinfo, m0, fsmask, nax, axl);
   std::vector<uint32_t> pts = pl.pt_words;
   {
     // points on the axis: the last writer stores their masked components as
@@ -822,10 +838,8 @@ FluidArgs fluid_args(axg_handle *h) {
   return a;
 }
 
-// CTAs of the fluid's element pass: a grid-stride loop of warps over the elements
-unsigned fluid_elem_grid(const axg_handle *h, int64_t nel) {
-  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((nel + kWarps - 1) / kWarps, 8 * (int64_t)h->num_sms));
-}
+// CTAs of the fluid's element pass: one thread per element
+unsigned fluid_elem_grid(int64_t nel) { return (unsigned)std::max<int64_t>(1, (nel + kThreads - 1) / kThreads); }
 
 // The fluid of a Newmark step or a symplectic stage: the element pass, then
 // the point pass.
@@ -833,7 +847,7 @@ template <int NONMONO, int MODE, bool KAHAN>
 void launch_fluid_t(axg_handle *h, cudaStream_t s, const StateArgs &fs) {
   FluidArgs fa = fluid_args(h);
   if (MODE == MODE_SYMPLECTIC) fa.fsmask = nullptr;  // symplectic_time_loop applies no free-surface mask
-  launch_pdl(fluid_elem_kernel<NONMONO, MODE, KAHAN, One<FluidWork>>, fluid_elem_grid(h, h->nel_f), kThreads, 0, s,
+  launch_pdl(fluid_elem_kernel<NONMONO, MODE, KAHAN, One<FluidWork>>, fluid_elem_grid(h->nel_f), kThreads, 0, s,
              One<FluidWork>{{fa, fs}, (int32_t)h->nel_f}, h->spec);
   launch_pdl(fluid_point_kernel<NONMONO, MODE, KAHAN, One<FluidWork>>, (unsigned)((h->nglob_f + 255) / 256), 256, 0,
              s, One<FluidWork>{{fa, fs}, (int32_t)h->nglob_f});
@@ -2924,7 +2938,7 @@ int64_t batch_fluid(axg_batch *b, int stage, cudaStream_t s) {
   const int64_t ne = for_batches<FluidWork>(
       b->hs, [&](axg_handle *h) { return mine(h) ? (int32_t)h->nel_f : 0; }, work,
       [&](const Many<FluidWork> &m) {
-        const unsigned g = fluid_elem_grid(b->hs[0], m.start[m.n]);
+        const unsigned g = fluid_elem_grid(m.start[m.n]);
         if (stage < 0) fluid_elem_kernel<NONMONO, MODE_NEWMARK, KAHAN, Many<FluidWork>><<<g, kThreads, 0, s>>>(m, b->spec);
         else fluid_elem_kernel<NONMONO, MODE_SYMPLECTIC, KAHAN, Many<FluidWork>><<<g, kThreads, 0, s>>>(m, b->spec);
       });

@@ -1594,17 +1594,28 @@ __global__ void __launch_bounds__(kThreads, solid_min_ctas(MODE, true, KAHAN))
 // plain streams over HBM with no barriers, so the fluid's small element work
 // is no longer bound by the latency of patch-sized phases.
 
+// The element arrays of the fluid (points, metric terms, free-surface mask,
+// contributions) are stored in chunks of kFlChunk element slots: value v of
+// slot e at fl_at(e, v, nv) for nv values per element, the chunk's 32
+// elements side by side, so that a warp of 32 consecutive elements loads or
+// stores one value as one 128-byte line.
+constexpr int kFlChunk = 32;
+__host__ __device__ constexpr int64_t fl_chunks(int64_t nel) { return (nel + kFlChunk - 1) / kFlChunk; }
+__host__ __device__ constexpr int64_t fl_at(int64_t e, int v, int nv) {
+  return (e / kFlChunk) * ((int64_t)nv * kFlChunk) + (int64_t)v * kFlChunk + (e % kFlChunk);
+}
+
 struct FluidArgs {
-  const int32_t *gidx;     // per element slot (launch order): its 25 global points
-  const float *metric;     // per element slot block_stride(nt) floats: M1chi, M2chi, M4chi [, M_w_fl]
+  const int32_t *gidx;     // chunked, 25 values per element slot (launch order): its global points
+  const float *metric;     // chunked, 25 nt values per slot: M1chi, M2chi, M4chi [, M_w_fl] at 25 t + p
   const int32_t *elinfo;   // per element slot: bits 0..23 axial slot + 1, bits 24..27 source slot + 1
   const float *m0;         // per axial slot 5 floats (M0_w_fl)
-  const float *fsmask;     // per element slot 25 floats (fluid free-surface mask) or null
+  const float *fsmask;     // chunked, 25 values per slot (fluid free-surface mask) or null
   const float *srcfl;      // fluid source terms (8, 25) or null
   const int32_t *start;    // nglob + 1: each point's first copy in ent; bit 31 of start[g]: the point
                            // holds a coupling pre-pass partial sum (in the force array); bit 30: on the axis
-  const int32_t *ent;      // 25 nel: element slot * 25 + GLL point of each copy, points in order
-  float *fel;              // 25 nel: the element contributions of the step
+  const int32_t *ent;      // 25 nel: the fel index of each copy, points in order
+  float *fel;              // chunked, 25 values per slot: the element contributions of the step
   int64_t nel, nglob, n_m0;  // extents (checked builds)
 };
 constexpr uint32_t kFlPartial = 1u << 31, kFlAxis = 1u << 30, kFlStartMask = kFlAxis - 1u;
@@ -1627,112 +1638,118 @@ __device__ __forceinline__ float fluid_predicted(const StateArgs &st, int64_t g,
   return st.up[0][g];
 }
 
-// Element pass: one warp per element (items: the elements of the solves),
-// lane = GLL point; chi gathered with the predictor, the element's
-// stiffness, source, axial mask and free-surface mask, stored per copy.
-// Each warp loads its next element's points, metric terms and info word
-// before it computes the current one.
+// glob_fluid_stiffness_4 (SOLVER/stiffness_fluid.f90:139-216) of one element
+// held by one thread: chi(i, j) at chi[i + 5 j] in, the element's
+// contributions out.  met points at the element's first metric value (value
+// v at met[v * kFlChunk]).  The same products and summation order as the
+// warp-per-element form (dxi / deta above): first stage X1 = mxm_4(G2T or
+// G1T, chi), X2 = mxm_4(chi, G2); second stage mxm_4(G2 or G1, S1) +
+// mxm_4(S2, G2T).
+template <bool AX, bool NONMONO>
+__device__ __forceinline__ void fluid_elem_stiffness(const SpecDev &sp, const float *met, const float *m0,
+                                                     const float (&chi)[25], float (&loc)[25]) {
+  // G(a, b) of the xi direction: G1 on axial elements
+  auto gx = [&](int a, int b) { return AX ? sp.g1[a + 5 * b] : sp.g2[a + 5 * b]; };
+  float S1[25], S2[25];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const int q = i + 5 * j;
+      float x1 = gx(0, i) * chi[5 * j];
+#pragma unroll
+      for (int k = 1; k < 5; ++k) x1 = fmaf(gx(k, i), chi[k + 5 * j], x1);
+      float x2 = chi[i] * sp.g2[5 * j];
+#pragma unroll
+      for (int k = 1; k < 5; ++k) x2 = fmaf(chi[i + 5 * k], sp.g2[k + 5 * j], x2);
+      const float m1 = __ldg(met + q * kFlChunk), m2 = __ldg(met + (25 + q) * kFlChunk),
+                  m4 = __ldg(met + (50 + q) * kFlChunk);
+      S1[q] = m1 * x2 + m2 * x1;
+      S2[q] = m1 * x1 + m4 * x2;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const int q = i + 5 * j;
+      float y1 = gx(i, 0) * S1[5 * j];
+#pragma unroll
+      for (int k = 1; k < 5; ++k) y1 = fmaf(gx(i, k), S1[k + 5 * j], y1);
+      float y2 = S2[i] * sp.g2[j];
+#pragma unroll
+      for (int k = 1; k < 5; ++k) y2 = fmaf(S2[i + 5 * k], sp.g2[j + 5 * k], y2);
+      float l = y1 + y2;
+      if (NONMONO) {
+        l = l + __ldg(met + (75 + q) * kFlChunk) * chi[q];
+        if (AX) {
+          float v1 = sp.g0[0] * chi[5 * j];
+#pragma unroll
+          for (int k = 1; k < 5; ++k) v1 = fmaf(sp.g0[k], chi[k + 5 * j], v1);
+          l = l + sp.g0[i] * (m0[j] * v1);
+        }
+      }
+      loc[q] = l;
+    }
+  }
+}
+
+// Element pass: one thread per element (items: the elements of the solves).
+// The thread gathers its 25 points' chi with the predictor, computes the
+// element's stiffness with its source, axial mask and free-surface mask in
+// registers, and stores its 25 contributions.  The element's 25 gathers and
+// its metric loads are independent of one another, so each thread has tens
+// of loads in flight, and there are no shuffles.
 template <int NONMONO, int MODE, bool KAHAN, class P = One<FluidWork>>
-__global__ void __launch_bounds__(kThreads, 3) fluid_elem_kernel(const __grid_constant__ P p, SpecDev sp) {
-  constexpr int NT = NONMONO ? 4 : 3;
-  constexpr int BS = block_stride(NT);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const bool active = lane < 25;
-  // idle lanes 25..31 take part in the shuffles; their reads go to point 24
-  const int ml = active ? lane : 24;
-  const int i = ml % 5, j = ml / 5;
-  LaneCoef coef;
-  load_coef(sp, i, j, coef);
+__global__ void __launch_bounds__(kThreads, 2) fluid_elem_kernel(const __grid_constant__ P p, SpecDev sp) {
   pdl_wait();
   pdl_trigger();
-  if (!P::kMany && *p.at(0).st.blowup) return;  // uniform across the CTA
-  const int32_t n = p.items(), stride = gridDim.x * kWarps;
-  // Two stages ahead: an element's loads that do not depend on the state
-  // (its points, metric terms, info word) are issued two iterations before
-  // it is computed, its points' state one iteration before.
-  struct Pre {
-    int32_t sv, g, info;
-    float mt[4];
-  };
-  struct Raw {
-    float u, v, a, k;
-  };
-  auto load = [&](int32_t it, Pre &q) {
-    q.sv = p.locate(it);
-    const FluidArgs &f = p.at(q.sv).fa;
-    int64_t el = it - p.first(q.sv);
-    if (!AXG_BOUND(el, f.nel, 14)) el = 0;
-    q.g = f.gidx[el * 25 + ml];
-    if (!AXG_BOUND(q.g, p.at(q.sv).st.nglob, 14)) q.g = 0;
-    q.info = f.elinfo[el];
+  const int32_t it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= p.items()) return;
+  const int sv = p.locate(it);
+  const FluidArgs &f = p.at(sv).fa;
+  const StateArgs &st = p.at(sv).st;
+  if (*st.blowup) return;  // (a stopped solve of a batch: its contributions are not used)
+  const int64_t el = it - p.first(sv);
+  if (!AXG_BOUND(el, f.nel, 14)) return;
+  const int64_t e0 = fl_at(el, 0, 25);  // the element's value 0 of a 25-value array
+  float chi[25];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) q.mt[t] = t < NT ? f.metric[el * BS + t * 25 + ml] : 0.f;
-  };
-  // the state fluid_predicted reads
-  auto load_raw = [&](const Pre &q, Raw &r) {
-    const StateArgs &st = p.at(q.sv).st;
-    if (KAHAN) {
-      r.u = st.u[0][q.g];
-      r.v = st.v[0][q.g];
-      r.a = MODE == MODE_SYMPLECTIC ? 0.f : st.a[0][q.g];
-      r.k = st.cu[0][q.g];
-    } else if (MODE == MODE_SYMPLECTIC) {
-      r.u = st.u[0][q.g];
-      r.v = st.v[0][q.g];
-    } else {
-      r.u = st.up[0][q.g];
-    }
-  };
-  Pre cur{}, nx{};
-  Raw raw{};
-  int32_t it = blockIdx.x * kWarps + warp;
-  if (it < n) {
-    load(it, cur);
-    load_raw(cur, raw);
+  for (int q = 0; q < 25; ++q) {
+    int64_t g = __ldg(f.gidx + e0 + q * kFlChunk);
+    if (!AXG_BOUND(g, st.nglob, 14)) g = 0;
+    float k = 0.f;
+    chi[q] = fluid_predicted<MODE, KAHAN>(st, g, k);
   }
-  if (it + stride < n) load(it + stride, nx);
-  for (; it < n; it += stride) {
-    Pre nx2{};
-    Raw raw_nx{};
-    if (it + stride < n) load_raw(nx, raw_nx);
-    if (it + 2 * stride < n) load(it + 2 * stride, nx2);
-    const int sv = cur.sv;
-    const FluidArgs &f = p.at(sv).fa;
-    const StateArgs &st = p.at(sv).st;
-    const int64_t el = it - p.first(sv);
-    // chi at the gather: as fluid_predicted computes it
-    float chi;
-    if (KAHAN) {
-      float k = raw.k;
-      chi = MODE == MODE_SYMPLECTIC ? drift_comp(raw.u, raw.v, st, k) : predict_comp(raw.u, raw.v, raw.a, st, k);
-    } else if (MODE == MODE_SYMPLECTIC) {
-      chi = raw.u + mul2(st.dt, st.dt_lo, raw.v);  // chi + dchi * coefd(i)
-    } else {
-      chi = raw.u;
-    }
-    int axslot = (cur.info & 0xFFFFFF) - 1;
-    if (axslot >= 0 && !AXG_BOUND((int64_t)axslot * 5 + 4, f.n_m0, 14)) axslot = -1;
-    const int srcslot = ((cur.info >> 24) & 0xF) - 1;
-    const bool ax = axslot >= 0;
-    if (NONMONO && ax && i == 0) chi = 0.f;  // apply_axis_mask_scal(chi)
-    float mt[4];
+  const int32_t info = __ldg(f.elinfo + el);
+  int axslot = (info & 0xFFFFFF) - 1;
+  if (axslot >= 0 && !AXG_BOUND((int64_t)axslot * 5 + 4, f.n_m0, 14)) axslot = -1;
+  const int srcslot = ((info >> 24) & 0xF) - 1;
+  const bool ax = axslot >= 0;
+  const float *met = f.metric + fl_at(el, 0, (NONMONO ? 4 : 3) * 25);
+  float loc[25];
+  if (ax) {
+    if (NONMONO)
 #pragma unroll
-    for (int t = 0; t < 4; ++t) mt[t] = cur.mt[t];
-    const float *m0 = ax ? f.m0 + (int64_t)axslot * 5 : nullptr;
-    float fv = ax ? stiff_fluid<true, NONMONO>(coef, mt, m0, i, j, chi)
-                  : stiff_fluid<false, NONMONO>(coef, mt, m0, i, j, chi);
-    if (srcslot >= 0 && f.srcfl && active) {
-      const float stf1 = AXG_BOUND(*st.iter - 1, st.niter, 14) ? st.stf[*st.iter - 1] : 0.f;
-      if (stf1 != 0.f) fv = fv - f.srcfl[srcslot * 25 + lane] * stf1;
-    }
-    if (NONMONO && ax && i == 0) fv = 0.f;
-    if (f.fsmask && active) fv = fv * f.fsmask[el * 25 + lane];
-    // (a stopped solve of a batch: its contributions are not used)
-    if (active && !(P::kMany && *st.blowup)) f.fel[el * 25 + lane] = fv;
-    cur = nx;
-    nx = nx2;
-    raw = raw_nx;
+      for (int j = 0; j < 5; ++j) chi[5 * j] = 0.f;  // apply_axis_mask_scal(chi)
+    fluid_elem_stiffness<true, NONMONO != 0>(sp, met, f.m0 + (int64_t)axslot * 5, chi, loc);
+  } else {
+    fluid_elem_stiffness<false, NONMONO != 0>(sp, met, nullptr, chi, loc);
   }
+  if (srcslot >= 0 && f.srcfl) {
+    const float stf1 = AXG_BOUND(*st.iter - 1, st.niter, 14) ? st.stf[*st.iter - 1] : 0.f;
+    if (stf1 != 0.f)
+#pragma unroll
+      for (int q = 0; q < 25; ++q) loc[q] = loc[q] - f.srcfl[srcslot * 25 + q] * stf1;
+  }
+  if (NONMONO && ax)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) loc[5 * j] = 0.f;
+  if (f.fsmask)
+#pragma unroll
+    for (int q = 0; q < 25; ++q) loc[q] = loc[q] * __ldg(f.fsmask + e0 + q * kFlChunk);
+#pragma unroll
+  for (int q = 0; q < 25; ++q) f.fel[e0 + q * kFlChunk] = loc[q];
 }
 
 // Point pass: one thread per global point (items: the points of the
@@ -1756,9 +1773,28 @@ __global__ void __launch_bounds__(256) fluid_point_kernel(const __grid_constant_
   if (!AXG_BOUND(g, f.nglob, 15)) return;
   const uint32_t s0 = (uint32_t)f.start[g], s1 = (uint32_t)f.start[g + 1] & kFlStartMask;
   float sum = (s0 & kFlPartial) ? st.f[0][g] : 0.f;
-  for (uint32_t k = s0 & kFlStartMask; k < s1; ++k) {
-    const int32_t e = f.ent[k];
-    if (!AXG_BOUND(e, 25 * f.nel, 15)) break;
+  // the first four copies' indices, then their contributions, are loaded
+  // together (an interior point has 1, 2 or 4 copies), then summed in order
+  const int64_t nfel = fl_chunks(f.nel) * 25 * kFlChunk;
+  uint32_t k = s0 & kFlStartMask;
+  {
+    int32_t e[4];
+    float x[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      e[q] = k + q < s1 ? __ldg(f.ent + k + q) : -1;
+      if (e[q] >= 0 && !AXG_BOUND(e[q], nfel, 15)) e[q] = -1;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) x[q] = e[q] >= 0 ? f.fel[e[q]] : 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (e[q] >= 0) sum = sum + x[q];
+    k += 4;
+  }
+  for (; k < s1; ++k) {
+    const int32_t e = __ldg(f.ent + k);
+    if (!AXG_BOUND(e, nfel, 15)) break;
     sum = sum + f.fel[e];
   }
   float kc = 0.f;

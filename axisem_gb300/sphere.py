@@ -926,8 +926,17 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
     time step, niter and the Gaussian source time function at the mesh
     period."""
     solid = m.meta["solid"]
-    s, z = geo["s"][solid], geo["z"][solid]
-    r = np.hypot(s, z)
+    # the solid points' geometry that every solve on this skeleton searches
+    # (axis points, surface points), kept with the skeleton
+    key = ("solid_points", id(solid))
+    if key not in sk.cache:
+        s_, z_ = geo["s"][solid], geo["z"][solid]
+        r_ = np.hypot(s_, z_)
+        on_axis = (s_ == 0.0) & (z_ > 0.0)
+        surf_ = np.argwhere(np.abs(r_ - R_EARTH) < 1.0)
+        sk.cache[key] = {"axis_pts": np.argwhere(on_axis), "axis_z": z_[on_axis], "z": z_,
+                         "surf": surf_, "surf_th": np.degrees(np.arctan2(s_[tuple(surf_.T)], z_[tuple(surf_.T)]))}
+    pc = sk.cache[key]
     m.deltat = dt
     m.seis_it = solve.seis_it
     niter = int(np.ceil((solve.seconds + 1e-11) / dt))
@@ -935,9 +944,8 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
     m.stf = gauss_stf(niter, dt, period, solve.magnitude, solve.seis_it)
     # ---- source: the northern axis point nearest to the source depth
     zsrc = R_EARTH - solve.depth_km * 1000.0
-    on_axis = (s == 0.0) & (z > 0.0)
-    cand = np.argwhere(on_axis)
-    dz = np.abs(z[on_axis] - zsrc)
+    cand = pc["axis_pts"]
+    dz = np.abs(pc["axis_z"] - zsrc)
     best = dz.min()
     hits = cand[np.abs(dz - best) <= 1e-6 * R_EARTH]
     # the point's elements (at most 2 along the axis), as find_srcloc keeps them
@@ -949,7 +957,19 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
     kind = solve.source or {0: "explosion", 1: "mtr", 2: "mtp"}[pole]
     nsrc = len(src_els)
     E = m.nel_solid
-    st = np.zeros((E, 5, 5, 3))          # [e, ipol, jpol, comp] FP64
+    # The source term is nonzero only on the source elements' points, so its
+    # assembly (pdistsum_solid) involves only the elements that hold one of
+    # them: it runs on those, in element order, with the same sums in the
+    # same order as over the whole mesh.
+    ig_all = np.asarray(m.igloc_solid).reshape(E, 25) - 1
+    mark = np.zeros(m.nglob_solid, dtype=bool)
+    mark[ig_all[src_els].reshape(-1)] = True
+    near = np.flatnonzero(mark[ig_all].any(axis=1))
+    slot = {int(e): k for k, e in enumerate(near)}
+    uniq, inv = np.unique(ig_all[near], return_inverse=True)
+    ig_near = inv.reshape(-1).astype(I32) + 1
+    N = len(near)
+    st = np.zeros((N, 5, 5, 3))          # [near element, ipol, jpol, comp] FP64
     axis_s = geo["axis"][solid]
     pw = m.pointwise
     for e in src_els:
@@ -960,6 +980,7 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
         dzdxi_j = -geo["dzdxi"][solid][e] / jac
         dsdeta_j = -geo["dsdeta"][solid][e] / jac
         dsdxi_j = geo["dsdxi"][solid][e] / jac
+        k = slot[e]
         for ip in range(5):
             for jp in range(5):
                 # derivatives at (li, lj) of the Lagrange basis function of (ip, jp)
@@ -969,63 +990,62 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
                 dzdf = dsdeta_j[li, lj] * dfdxi + dsdxi_j[li, lj] * dfdeta
                 if pole == _abi.MONOPOLE:
                     if kind == "explosion":
-                        st[e, ip, jp, 0] = 2.0 * dsdf
-                        st[e, ip, jp, 2] = dzdf
+                        st[k, ip, jp, 0] = 2.0 * dsdf
+                        st[k, ip, jp, 2] = dzdf
                     elif kind == "mtt_p_mpp":
-                        st[e, ip, jp, 0] = dsdf
+                        st[k, ip, jp, 0] = dsdf
                     elif kind == "mrr":
-                        st[e, ip, jp, 2] = dzdf
+                        st[k, ip, jp, 2] = dzdf
                     else:
                         raise ValueError(f"monopole source {kind}")
                 elif pole == _abi.DIPOLE:
                     if kind not in ("mtr", "mpr"):
                         raise ValueError(f"dipole source {kind}")
-                    st[e, ip, jp, 0] = dzdf
-                    st[e, ip, jp, 2] = dsdf
+                    st[k, ip, jp, 0] = dzdf
+                    st[k, ip, jp, 2] = dsdf
                 else:
                     if kind not in ("mtp", "mtt_m_mpp"):
                         raise ValueError(f"quadrupole source {kind}")
-                    st[e, ip, jp, 0] = dsdf
-                    st[e, ip, jp, 1] = dsdf
+                    st[k, ip, jp, 0] = dsdf
+                    st[k, ip, jp, 1] = dsdf
     st = st / nsrc
     # pdistsum_solid in FP32, small values cut (smallval = 1e-6), the pole's axis mask
-    stf_ = np.zeros((5, 5, E, 3), dtype=F32, order="F")
+    stf_ = np.zeros((5, 5, N, 3), dtype=F32, order="F")
     for c in range(3):
-        stf_[..., c] = _pdistsum_f32(_to_f(st[..., c]), m.igloc_solid, m.nglob_solid)
+        stf_[..., c] = _pdistsum_f32(_to_f(st[..., c]), ig_near, len(uniq))
     stf_[np.abs(stf_) < 1e-6] = 0.0
-    ax_el = m.ax_el_solid - 1
+    ax_near = np.array([slot[int(e)] for e in m.ax_el_solid - 1 if int(e) in slot], dtype=np.int64)
     comps = {0: [0], 1: [1, 2], 2: [0, 1, 2]}[pole]
     for c in comps:
-        stf_[0, :, ax_el, c] = 0.0
+        stf_[0, :, ax_near, c] = 0.0
     stf_ = stf_ / F32(np.pi if pole == _abi.DIPOLE else 2.0 * np.pi)
     # the same in FP64 (the entries the FP32 term keeps)
-    std_ = np.zeros((5, 5, E, 3), order="F")
+    std_ = np.zeros((5, 5, N, 3), order="F")
     for c in range(3):
-        std_[..., c] = _pdistsum_f32(np.transpose(st[..., c], (1, 2, 0)), m.igloc_solid, m.nglob_solid, np.float64)
+        std_[..., c] = _pdistsum_f32(np.transpose(st[..., c], (1, 2, 0)), ig_near, len(uniq), np.float64)
     std_[stf_ == 0] = 0.0
     std_ = std_ / (np.pi if pole == _abi.DIPOLE else 2.0 * np.pi)
-    nz = np.flatnonzero(np.any(stf_ != 0, axis=(0, 1, 3))).tolist()
-    if len(nz) > 8:
-        raise RuntimeError(f"source term spans {len(nz)} elements (8 at most)")
+    nzk = np.flatnonzero(np.any(stf_ != 0, axis=(0, 1, 3))).tolist()
+    if len(nzk) > 8:
+        raise RuntimeError(f"source term spans {len(nzk)} elements (8 at most)")
     m.ielsrc = np.zeros(8, dtype=I32)
-    m.ielsrc[:len(nz)] = np.array(nz, dtype=I32) + 1
-    m.nelsrc = len(nz)
+    m.ielsrc[:len(nzk)] = near[nzk].astype(I32) + 1
+    m.nelsrc = len(nzk)
     ste = np.zeros((5, 5, 8, 3), dtype=F32, order="F")
     sted = np.zeros((5, 5, 8, 3), order="F")
-    for k, e in enumerate(nz):
+    for k, e in enumerate(nzk):
         ste[:, :, k, :] = stf_[:, :, e, :]
         sted[:, :, k, :] = std_[:, :, e, :]
     m.source_term_el = ste
     m.source_term_el_dp = sted
     m.fluid_src = 0
-    m.meta["source"] = {"kind": kind, "depth_km": float((R_EARTH - z[tuple(hits[0])]) / 1000.0),
+    m.meta["source"] = {"kind": kind, "depth_km": float((R_EARTH - pc["z"][tuple(hits[0])]) / 1000.0),
                         "elements": [int(e) + 1 for e in src_els]}
     # ---- receivers: the surface point nearest to each colatitude
     rec = solve.receivers_deg
     if rec is None:
         rec = np.linspace(0.0, 180.0, 20)
-    surf = np.argwhere(np.abs(r - R_EARTH) < 1.0)
-    th = np.degrees(np.arctan2(s[tuple(surf.T)], z[tuple(surf.T)]))
+    surf, th = pc["surf"], pc["surf_th"]
     rows = []
     for c in np.asarray(rec, dtype=np.float64):
         k = int(np.argmin(np.abs(th - c)))
