@@ -76,6 +76,9 @@ struct DomainDev {
   float *m0 = nullptr;
   float *fsmask = nullptr;
   float *srcfl = nullptr;
+  // per global point: bit c set where the pole's axis mask zeroes component
+  // c (points on the axis), or null
+  uint8_t *axmask = nullptr;
   int64_t n_m0 = 0;
 };
 
@@ -120,8 +123,14 @@ struct axg_handle {
   DomainDev ds, df;
   float *su[3] = {}, *sv[3] = {}, *sa[3] = {}, *sf[3] = {};
   std::vector<int32_t> ielsrc;  // the source elements (0-based, solid or fluid as fluid_src says)
-  float *sup[3] = {};  // the plain Newmark step's predicted displacement (kept by the last writers)
-  float *fup = nullptr;  // ... and chi
+  // The plain Newmark step's predicted displacement (and chi): the last
+  // writers store it into the buffer of the old displacement, and the step's
+  // prediction becomes the new displacement, so the two buffers trade roles
+  // (su <-> sup, fu <-> fup) after every such step; `parity` counts the
+  // trades modulo 2 (step graphs are captured per parity).
+  float *sup[3] = {};
+  float *fup = nullptr;
+  int parity = 0;
   float *fu = nullptr, *fv = nullptr, *fa = nullptr, *ff = nullptr;
   float *inv_mass_s = nullptr, *inv_mass_f = nullptr, *gamma_s = nullptr, *gamma_f = nullptr;
   // FP64 inverse masses (mesh) and source values (solve), when the descriptor had them
@@ -138,8 +147,8 @@ struct axg_handle {
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_io[5] = {};
   Coupling to_fluid{}, to_solid{};
-  cudaGraphExec_t graph = nullptr;
-  int graph_steps = 0;
+  cudaGraphExec_t graph[2] = {};  // steps_per_graph steps, per parity
+  int graph_steps[2] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ev_done = nullptr;  // end of the work axg_run_async queued
   bool pending = false;
@@ -183,8 +192,8 @@ struct axg_handle {
     cudaEvent_t ev_dump[2] = {}, ev_copy[2] = {};
     std::vector<std::string> names;
   } dump;
-  cudaGraphExec_t graph_dump = nullptr;  // strain_it steps, when that differs from steps_per_graph
-  int graph_dump_steps = 0;
+  cudaGraphExec_t graph_dump[2] = {};  // strain_it steps, when that differs from steps_per_graph
+  int graph_dump_steps[2] = {};
   // seismogram checkpoints: every check_it steps the final samples go to `out`
   struct Checkpoint {
     int32_t check_it = 0, cap = 0;
@@ -429,8 +438,15 @@ int build_fluid_passes(axg_handle *h, const axg_mesh_desc *d, const std::vector<
       if (h->pre_f[g]) start[h->pf.new_of_old[g]] |= (int32_t)kFlPartial;
     for (int k = 0; k < nax; ++k)
       for (int jj = 0; jj < 5; ++jj) start[h->igloc_f[25 * (int64_t)(axl[k] - 1) + 5 * jj] - 1] |= (int32_t)kFlAxis;
+    // apply_axis_mask_scal (non-monopole sources) zeroes chi on the axis
+    std::vector<uint8_t> axmask;
+    if (d->src_type != AXG_MONOPOLE && nax > 0) {
+      axmask.assign(nglob, 0);
+      for (int64_t g = 0; g < nglob; ++g) axmask[g] = (start[g] & (int32_t)kFlAxis) ? 1 : 0;
+    }
     h->in_mesh = true;
     rc = upload(h, &dd.metric, metric);
+    if (!rc && !axmask.empty()) rc = upload(h, &dd.axmask, axmask);
     if (!rc) rc = upload(h, &dd.m0, m0);
     if (!rc && !fsmask.empty()) rc = upload(h, &dd.fsmask, fsmask);
     if (!rc) rc = upload(h, &dd.gidx, gidx);
@@ -535,6 +551,15 @@ int build_domain(axg_handle *h, const axg_mesh_desc *d, bool fluid, bool mesh_pa
       for (int jj = 0; jj < 5; ++jj) onaxis[ig[25 * (int64_t)(axl[k] - 1) + 5 * jj] - 1] = 1;
     for (auto &w : pts)
       if (w != kPtPad && onaxis[w & kPtIndexMask]) w |= kPtAxis;
+    if (mesh_part && nax > 0) {
+      // the components the pole's axis mask zeroes (axis_masked)
+      const uint8_t bits = pole == AXG_MONOPOLE ? 1 : pole == AXG_DIPOLE ? 6 : 7;
+      for (auto &x : onaxis) x = x ? bits : 0;
+      h->in_mesh = true;
+      const int rc = upload(h, &dd.axmask, onaxis);
+      h->in_mesh = false;
+      if (rc) return rc;
+    }
   }
   if (!fluid && h->n_src > 0) {
     // mark the points that carry a solid source term
@@ -613,6 +638,35 @@ CouplingHost make_coupling(std::vector<std::tuple<int32_t, int32_t, float, float
 // previous step's last writers stored
 bool lookahead(const axg_handle *h) { return h->scheme == AXG_SCHEME_NEWMARK2 && !h->kahan; }
 
+// after a plain Newmark step is queued: its prediction buffers hold the new
+// displacement and chi, the old displacement buffers the next prediction
+void trade_buffers(axg_handle *h) {
+  if (!lookahead(h)) return;
+  for (int c = 0; c < 3; ++c) std::swap(h->su[c], h->sup[c]);
+  std::swap(h->fu, h->fup);
+  h->parity ^= 1;
+}
+
+// Back to parity 0 (the allocation's roles): the state is copied into the
+// first buffer (queued on s); the prediction is recomputed before a run.
+cudaError_t normalize_buffers(axg_handle *h, cudaStream_t s) {
+  if (!h->parity) return cudaSuccess;
+  for (int c = 0; c < 3; ++c)
+    if (h->su[c] && h->nglob_s > 0) {
+      const cudaError_t e =
+          cudaMemcpyAsync(h->sup[c], h->su[c], h->nglob_s * sizeof(float), cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return e;
+      std::swap(h->su[c], h->sup[c]);
+    }
+  if (h->fu && h->nglob_f > 0) {
+    const cudaError_t e = cudaMemcpyAsync(h->fup, h->fu, h->nglob_f * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    std::swap(h->fu, h->fup);
+  }
+  h->parity = 0;
+  return cudaSuccess;
+}
+
 // an FP64 coefficient as an FP32 pair: hi = its FP32 rounding, lo = the rest
 void split(double x, float &hi, float &lo) {
   hi = (float)x;
@@ -679,8 +733,10 @@ void launch_anel_full(axg_handle *h, cudaStream_t s, bool update);
 cudaError_t refresh_predicted(axg_handle *h, cudaStream_t s) {
   if (h->anel_full && h->scheme == AXG_SCHEME_NEWMARK2) launch_anel_full(h, s, false);
   if (!lookahead(h)) return cudaGetLastError();
-  if (h->nglob_s > 0) predict_kernel<<<(unsigned)((h->nglob_s + 255) / 256), 256, 0, s>>>(solid_state(h));
-  if (h->nel_f > 0) predict_kernel<<<(unsigned)((h->nglob_f + 255) / 256), 256, 0, s>>>(fluid_state(h));
+  if (h->nglob_s > 0)
+    predict_kernel<<<(unsigned)((h->nglob_s + 255) / 256), 256, 0, s>>>(solid_state(h), h->ds.axmask);
+  if (h->nel_f > 0)
+    predict_kernel<<<(unsigned)((h->nglob_f + 255) / 256), 256, 0, s>>>(fluid_state(h), h->df.axmask);
   return cudaGetLastError();
 }
 
@@ -897,7 +953,7 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
   if (h->nel_f > 0) {
     if (h->to_fluid.n > 0) {
       const unsigned nb = (h->to_fluid.n + 255) / 256;
-      const One<ToFluidWork> w{{h->to_fluid, ss, h->ff}, h->to_fluid.n};
+      const One<ToFluidWork> w{{h->to_fluid, ss, h->ff, h->ds.axmask}, h->to_fluid.n};
       if (h->pole == AXG_DIPOLE) launch_pdl(couple_to_fluid_kernel<1, One<ToFluidWork>>, nb, 256, 0, s, w);
       else launch_pdl(couple_to_fluid_kernel<0, One<ToFluidWork>>, nb, 256, 0, s, w);
     }
@@ -911,8 +967,9 @@ void enqueue_step(axg_handle *h, cudaStream_t s) {
     }
   }
   launch_solid<MODE_NEWMARK>(h, s);
+  trade_buffers(h);  // the state after the step
   if (h->anel_full) launch_anel_full(h, s, true);  // the memory variables from the stored displacement
-  launch_pdl(receivers_kernel<One<RecWork>>, 1, 256, 0, s, One<RecWork>{rec_work(h, ss), 1});
+  launch_pdl(receivers_kernel<One<RecWork>>, 1, 256, 0, s, One<RecWork>{rec_work(h, solid_state(h)), 1});
 }
 
 // One step of symplectic_time_loop (SOLVER/time_evol_wave.F90:587-727):
@@ -988,7 +1045,7 @@ void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
     if (h->nel_f > 0) {
       if (h->to_fluid.n > 0) {
         const int nb = (h->to_fluid.n + 255) / 256;
-        const One<ToFluidWork> w{{h->to_fluid, ss, h->ff}, h->to_fluid.n};
+        const One<ToFluidWork> w{{h->to_fluid, ss, h->ff, h->ds.axmask}, h->to_fluid.n};
         if (h->pole == AXG_DIPOLE) couple_to_fluid_kernel<1><<<nb, 256, 0, s>>>(w);
         else couple_to_fluid_kernel<0><<<nb, 256, 0, s>>>(w);
       }
@@ -1011,39 +1068,64 @@ void enqueue_step_symplectic(axg_handle *h, cudaStream_t s) {
   receivers_kernel<<<1, 256, 0, s>>>(One<RecWork>{rec_work(h, solid_state(h)), 1});
 }
 
-// a CUDA graph of nsteps steps into *exec (replacing what it held)
+// a CUDA graph of nsteps steps into *exec (replacing what it held).  The
+// capture trades the buffers of each plain Newmark step as queueing does; a
+// failed capture leaves the handle's buffer roles as they were.
 int build_graph_into(axg_handle *h, int nsteps, cudaGraphExec_t *exec) {
   if (*exec) {
     cudaGraphExecDestroy(*exec);
     *exec = nullptr;
   }
+  const int parity0 = h->parity;
+  auto undo = [&]() {
+    if (h->parity != parity0) trade_buffers(h);
+  };
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < nsteps; ++k) enqueue_step(h, h->stream);
-  CK(cudaStreamEndCapture(h->stream, &g));
-  cudaError_t e = cudaGraphInstantiate(exec, g, 0);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (e != cudaSuccess) {
+    undo();
+    return cuda_fail(h, e, "cudaStreamEndCapture");
+  }
+  e = cudaGraphInstantiate(exec, g, 0);
   cudaGraphDestroy(g);
-  if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+  if (e != cudaSuccess) {
+    undo();
+    return cuda_fail(h, e, "cudaGraphInstantiate");
+  }
   return AXG_OK;
 }
 
-int build_graph(axg_handle *h, int nsteps) {
-  int rc = build_graph_into(h, nsteps, &h->graph);
-  if (!rc) h->graph_steps = nsteps;
-  return rc;
+// Queues k steps as one graph of slots[parity] (captured on first use, which
+// trades the buffers as it goes; a replay trades them here).
+int launch_graph(axg_handle *h, int k, cudaGraphExec_t *slots, int *slot_steps) {
+  const int p = h->parity;
+  if (!slots[p] || slot_steps[p] != k) {
+    slot_steps[p] = 0;
+    const int rc = build_graph_into(h, k, &slots[p]);
+    if (rc) return rc;
+    slot_steps[p] = k;
+  } else {
+    for (int q = 0; q < (k & 1); ++q) trade_buffers(h);
+  }
+  CK(cudaGraphLaunch(slots[p], h->stream));
+  return AXG_OK;
 }
 
 // the step graphs no longer match the handle's kernels or step count
 void drop_graphs(axg_handle *h) {
-  if (h->graph) cudaGraphExecDestroy(h->graph);
-  if (h->graph_dump) cudaGraphExecDestroy(h->graph_dump);
-  h->graph = h->graph_dump = nullptr;
-  h->graph_steps = h->graph_dump_steps = 0;
+  for (int p = 0; p < 2; ++p) {
+    if (h->graph[p]) cudaGraphExecDestroy(h->graph[p]);
+    if (h->graph_dump[p]) cudaGraphExecDestroy(h->graph_dump[p]);
+    h->graph[p] = h->graph_dump[p] = nullptr;
+    h->graph_steps[p] = h->graph_dump_steps[p] = 0;
+  }
 }
 
 void release(axg_handle *h) {
   if (!h) return;
-  if (h->graph) cudaGraphExecDestroy(h->graph);
+  drop_graphs(h);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->ev_done) cudaEventDestroy(h->ev_done);
@@ -1053,7 +1135,6 @@ void release(axg_handle *h) {
     if (h->dump.ev_dump[k]) cudaEventDestroy(h->dump.ev_dump[k]);
     if (h->dump.ev_copy[k]) cudaEventDestroy(h->dump.ev_copy[k]);
   }
-  if (h->graph_dump) cudaGraphExecDestroy(h->graph_dump);
   if (h->copy_stream) {
     cudaStreamSynchronize(h->copy_stream);
     cudaStreamDestroy(h->copy_stream);
@@ -1921,11 +2002,8 @@ int axg_run(axg_handle *h, int32_t first_iter, int32_t n_iter) {
   while (done < n_iter) {
     const int k = std::min<int32_t>(h->steps_per_graph, n_iter - done);
     if (k == h->steps_per_graph) {
-      if (!h->graph || h->graph_steps != k) {
-        int rc = build_graph(h, k);
-        if (rc) return rc;
-      }
-      CK(cudaGraphLaunch(h->graph, h->stream));
+      const int rc = launch_graph(h, k, h->graph, h->graph_steps);
+      if (rc) return rc;
     } else {
       for (int s = 0; s < k; ++s) enqueue_step(h, h->stream);
       CK(cudaGetLastError());
@@ -2182,18 +2260,11 @@ int axg_run_async(axg_handle *h, int32_t first_iter, int32_t n_iter) {
     int k = std::min<int32_t>(h->steps_per_graph, n_iter - done);
     if (dp.type) k = std::min<int32_t>(k, dp.strain_it - (it - 1) % dp.strain_it);  // up to the next dump
     if (k == h->steps_per_graph) {
-      if (!h->graph || h->graph_steps != k) {
-        int rc = build_graph(h, k);
-        if (rc) return rc;
-      }
-      CK(cudaGraphLaunch(h->graph, h->stream));
+      const int rc = launch_graph(h, k, h->graph, h->graph_steps);
+      if (rc) return rc;
     } else if (dp.type && k == dp.strain_it) {
-      if (!h->graph_dump || h->graph_dump_steps != k) {
-        int rc = build_graph_into(h, k, &h->graph_dump);
-        if (rc) return rc;
-        h->graph_dump_steps = k;
-      }
-      CK(cudaGraphLaunch(h->graph_dump, h->stream));
+      const int rc = launch_graph(h, k, h->graph_dump, h->graph_dump_steps);
+      if (rc) return rc;
     } else {
       for (int q = 0; q < k; ++q) enqueue_step(h, h->stream);
       CK(cudaGetLastError());
@@ -2860,7 +2931,9 @@ struct axg_batch {
   // resident CTAs of the batched solid kernels per (symplectic, pole, compensated, attenuated)
   int solid_ctas[2][3][2][2] = {};
   cudaStream_t stream = nullptr;
-  cudaGraphExec_t graph = nullptr;
+  // one step of every solve, captured with the plain Newmark solves' buffer
+  // roles at parity 0 and at parity 1 (trade_buffers); steps alternate them
+  cudaGraphExec_t graph[2] = {};
   cudaEvent_t ev_done = nullptr;
   bool pending = false;
   int64_t launches_per_step = 0;
@@ -3035,7 +3108,7 @@ int64_t batch_to_fluid(axg_batch *b, int stage, cudaStream_t s) {
       [&](axg_handle *h) {
         StateArgs ss, fs;
         stage_states(h, stage, ss, fs);
-        return ToFluidWork{h->to_fluid, ss, h->ff};
+        return ToFluidWork{h->to_fluid, ss, h->ff, h->ds.axmask};
       },
       [&](const Many<ToFluidWork> &m) {
         couple_to_fluid_kernel<DIPOLE, Many<ToFluidWork>><<<(m.start[m.n] + 255) / 256, 256, 0, s>>>(m);
@@ -3064,6 +3137,7 @@ int64_t enqueue_batch_phase(axg_batch *b, int stage, cudaStream_t s) {
 // final drifts and memory variables, then the seismograms and step counters.
 int64_t enqueue_batch_step(axg_batch *b, cudaStream_t s) {
   int64_t nl = enqueue_batch_phase<MODE_NEWMARK>(b, -1, s);
+  for (axg_handle *h : b->hs) trade_buffers(h);  // the plain Newmark solves' state after the step
   int ns = 0;
   for (axg_handle *h : b->hs) ns = std::max(ns, h->scheme != AXG_SCHEME_NEWMARK2 ? h->nstages : 0);
   for (int i = 0; i < ns; ++i) nl += enqueue_batch_phase<MODE_SYMPLECTIC>(b, i, s);
@@ -3158,26 +3232,37 @@ int batch_create_impl(axg_batch *b, axg_handle *const *hs, int32_t n) {
   }
   BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   BCK(cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming));
-  // one step, captured once; every step of every run replays it
-  cudaGraph_t g;
-  BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  b->launches_per_step = enqueue_batch_step(b, b->stream);
-  const cudaError_t le = cudaGetLastError();
-  const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
-  if (le != cudaSuccess) {
-    if (ce == cudaSuccess) cudaGraphDestroy(g);
-    return bfail(b, AXG_ERR_CUDA, fmt("batch step capture: %s", cudaGetErrorString(le)));
+  // the solves' buffers in their parity-0 roles (each solve's stream is idle)
+  for (axg_handle *h : b->hs) {
+    BCK(normalize_buffers(h, h->stream));
+    BCK(cudaStreamSynchronize(h->stream));
   }
-  BCK(ce);
-  const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
-  cudaGraphDestroy(g);
-  BCK(ie);
+  // one step, captured once per parity; every step of every run replays one
+  for (int p = 0; p < 2; ++p) {
+    cudaGraph_t g;
+    BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    b->launches_per_step = enqueue_batch_step(b, b->stream);  // (trades the buffers: parity p + 1)
+    const cudaError_t le = cudaGetLastError();
+    const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+      if (ce == cudaSuccess) cudaGraphDestroy(g);
+      if (p == 0)
+        for (axg_handle *h : b->hs) trade_buffers(h);  // back to parity 0
+      return bfail(b, AXG_ERR_CUDA, fmt("batch step capture: %s", cudaGetErrorString(le != cudaSuccess ? le : ce)));
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&b->graph[p], g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess && p == 0)
+      for (axg_handle *h : b->hs) trade_buffers(h);
+    BCK(ie);
+  }
   return AXG_OK;
 }
 
 void batch_release(axg_batch *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
-  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (cudaGraphExec_t g : b->graph)
+    if (g) cudaGraphExecDestroy(g);
   if (b->ev_done) cudaEventDestroy(b->ev_done);
   if (b->stream) cudaStreamDestroy(b->stream);
 }
@@ -3226,6 +3311,7 @@ int axg_batch_run_async(axg_batch *b, const int32_t *first_iters, int32_t n_iter
   for (axg_handle *h : b->hs) {
     BCK(cudaEventRecord(h->ev_done, h->stream));
     BCK(cudaStreamWaitEvent(b->stream, h->ev_done, 0));
+    BCK(normalize_buffers(h, b->stream));  // the graphs' parity 0
     BCK(refresh_predicted(h, b->stream));
   }
   for (int k0 = 0; k0 < n; k0 += kMaxBatch) {
@@ -3238,7 +3324,10 @@ int axg_batch_run_async(axg_batch *b, const int32_t *first_iters, int32_t n_iter
     set_iters_kernel<<<1, kMaxBatch, 0, b->stream>>>(a);
   }
   BCK(cudaGetLastError());
-  for (int32_t q = 0; q < n_iter; ++q) BCK(cudaGraphLaunch(b->graph, b->stream));
+  for (int32_t q = 0; q < n_iter; ++q) {
+    BCK(cudaGraphLaunch(b->graph[q & 1], b->stream));
+    for (axg_handle *h : b->hs) trade_buffers(h);
+  }
   BCK(cudaEventRecord(b->ev_done, b->stream));
   // and each solve's later work follows the batch
   for (axg_handle *h : b->hs) BCK(cudaStreamWaitEvent(h->stream, b->ev_done, 0));

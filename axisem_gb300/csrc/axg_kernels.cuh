@@ -112,12 +112,14 @@ struct DomainArgs {
 };
 
 struct StateArgs {
-  float *u[3];              // disp (solid, gvec layout) / chi (fluid: u[0])
+  float *u[3];              // disp (solid, gvec layout) / chi (fluid: u[0]); plain Newmark: the
+                            // buffer the step stores the next step's prediction into
   float *v[3];              // velo / dchi
   float *a[3];              // acc0 / ddchi0
   float *f[3];              // force partial sums
   float *cu[3], *cv[3];     // compensated mode: running compensation of disp / velo (chi / dchi), else null
-  float *up[3];             // plain Newmark solid: the next step's predicted displacement, else null
+  float *up[3];             // plain Newmark: the step's predicted displacement (chi), which becomes its
+                            // new displacement (the two buffers trade roles every step); else null
   const float *inv_mass;    // per global point
   const double *inv_mass_dp;  // per global point in FP64 (compensated mode) or null
   const float *gamma;       // absorbing gamma per global point or null
@@ -1272,11 +1274,17 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
             // the axis masks of the reference zero these components of its state
             const bool zero = (w[q] & kPtAxis) && axis_masked<POLE>(cg);
             const float un = zero ? 0.f : dsp;
-            st.u[cg][g] = un;
+            if (LOOK) {
+              // The new displacement is the gathered prediction, which stays
+              // in the buffer it came from (up, with the masked components of
+              // axis points stored as zero): st.u is the other buffer, and
+              // receives the next step's predictor disp + deltat*velo +
+              // half_dt_sq*acc0 (SOLVER/time_evol_wave.F90:357-364).
+              st.u[cg][g] = zero ? 0.f : predict(un, vn, a, st);
+            } else {
+              st.u[cg][g] = un;
+            }
             if (KAHAN && zero) st.cu[cg][g] = 0.f;
-            // the next step's predictor disp + deltat*velo + half_dt_sq*acc0
-            // (SOLVER/time_evol_wave.F90:357-364), from the state just stored
-            if (LOOK) st.up[cg][g] = predict(un, vn, a, st);
           }
         }
       }
@@ -1827,10 +1835,12 @@ __global__ void __launch_bounds__(256) fluid_point_kernel(const __grid_constant_
   // apply_axis_mask_scal zeroes chi on the axis (non-monopole)
   const bool zero = NONMONO && (s0 & kFlAxis);
   const float un = zero ? 0.f : chi;
-  st.u[0][g] = un;
+  // plain Newmark: the new chi is the prediction read from up (axis points
+  // stored as zero), which keeps it; st.u is the other buffer and receives
+  // the next step's predictor
+  if (MODE == MODE_NEWMARK && !KAHAN) st.u[0][g] = zero ? 0.f : predict(un, vn, a, st);
+  else st.u[0][g] = un;
   if (KAHAN) st.cu[0][g] = zero ? 0.f : (MODE == MODE_NEWMARK ? comp_after_step(kc, vn, a, st) : kc);
-  // the next step's predictor (plain Newmark)
-  if (MODE == MODE_NEWMARK && !KAHAN) st.up[0][g] = predict(un, vn, a, st);
 }
 
 // The final drift of a symplectic step (SOLVER/time_evol_wave.F90:722-727):
@@ -1868,12 +1878,16 @@ __global__ void drift_kernel(const __grid_constant__ P p) {
 
 // The plain Newmark step's predicted displacement up = disp + deltat*velo +
 // half_dt_sq*acc0 (SOLVER/time_evol_wave.F90:357-364) of the current state,
-// before a run: the last writers keep it from there on.
-__global__ void predict_kernel(StateArgs solid) {
+// before a run: the last writers keep it from there on.  axmask (or null):
+// per point, bit c set where the axis mask zeroes component c; those are
+// stored as zero, as the step leaves them in its state.
+__global__ void predict_kernel(StateArgs solid, const uint8_t *axmask) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= solid.nglob) return;
+  const uint32_t m = axmask ? axmask[q] : 0u;
   for (int c = 0; c < 3; ++c)
-    if (solid.up[c]) solid.up[c][q] = predict(solid.u[c][q], solid.v[c][q], solid.a[c][q], solid);
+    if (solid.up[c])
+      solid.up[c][q] = ((m >> c) & 1u) ? 0.f : predict(solid.u[c][q], solid.v[c][q], solid.a[c][q], solid);
 }
 
 // ------------------------------------------------------------ coupling pre-passes
@@ -1894,7 +1908,8 @@ struct Coupling {
 struct ToFluidWork {
   Coupling cp;
   StateArgs solid;
-  float *ffl;  // the fluid force partial sums
+  float *ffl;              // the fluid force partial sums
+  const uint8_t *axmask;   // the solid's per-point axis mask bits (predict_kernel) or null
 };
 template <int DIPOLE, class P = One<ToFluidWork>>
 __global__ void couple_to_fluid_kernel(const __grid_constant__ P p) {
@@ -1906,6 +1921,7 @@ __global__ void couple_to_fluid_kernel(const __grid_constant__ P p) {
   const Coupling &cp = p.at(sv).cp;
   const StateArgs &solid = p.at(sv).solid;
   float *ffl = p.at(sv).ffl;
+  const uint8_t *axmask = p.at(sv).axmask;
   const int q = it - p.first(sv);
   if (*solid.blowup) return;
   if (q >= cp.n) return;
@@ -1922,7 +1938,13 @@ __global__ void couple_to_fluid_kernel(const __grid_constant__ P p) {
         if (solid.stage) return drift_comp(solid.u[c][gs], solid.v[c][gs], solid, k);
         return predict_comp(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid, k);
       }
-      if (solid.up[0]) return solid.up[c][gs];
+      if (solid.up[0]) {
+        // the stored prediction has the axis-masked components zeroed; the
+        // reference couples before its axis mask, with the prediction of the
+        // masked (zero) displacement
+        if (axmask && ((axmask[gs] >> c) & 1u)) return predict(0.f, solid.v[c][gs], solid.a[c][gs], solid);
+        return solid.up[c][gs];
+      }
       return predict(solid.u[c][gs], solid.v[c][gs], solid.a[c][gs], solid);
     };
     const float us = pred(0);
