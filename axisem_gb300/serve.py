@@ -156,9 +156,12 @@ class Server:
     """The serving loop; `budget_bytes` bounds the HBM the solves and
     resident meshes may hold."""
 
-    def __init__(self, budget_bytes: float = 64e9, chunk: int = 0, lib=None, compensated: bool = True):
-        """chunk: steps queued per call for a solve (0: all of them at once;
-        smaller chunks let a long solve yield the host loop between chunks);
+    def __init__(self, budget_bytes: float = 64e9, chunk: int = 1024, lib=None, compensated: bool = True):
+        """chunk: steps queued per call for a solve (0: all of them at once).
+        A whole long solve is tens of thousands of kernel launches: queueing
+        it fills the launch queue, and the call blocks the host loop until
+        most of it has run, so the solves behind it start late.  In chunks
+        every admitted solve is queued at once and refilled as it drains;
         in the batched loop, the most steps a batch runs before solves may
         join it (0: until its first solve finishes)."""
         self.lib = lib or _abi.load_library()

@@ -41,6 +41,10 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+# The serving stream keeps tens of solves' streams busy at once: let the
+# CUDA runtime map them onto 32 hardware work queues instead of its default
+# 8 (read once, when CUDA initialises).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 POLES = {"mono": 0, "di": 1, "quad": 2}
 N_TERMS = {0: 15, 1: 24, 2: 26}
@@ -599,7 +603,7 @@ def run_serving(args):
     of Poisson arrival rates with p50/p99 latency per rate."""
     from axisem_gb300.serve import PERIODS, POLES, Server, request_stream, template
     scale = args.serve_duration_scale
-    srv = Server(budget_bytes=64e9)
+    srv = Server(budget_bytes=64e9, chunk=1024)
     try:
         t0 = time.perf_counter()
         srv.preload({(p, q) for p in PERIODS for q in POLES})
@@ -632,6 +636,7 @@ def run_serving(args):
                    f"1800-3600 s of seismogram times {scale} ({min(steps)}-{max(steps)} steps); "
                    "compensated (Kahan) FP32",
             "duration_scale": scale, "mesh_preload_s": round(t_preload, 1), "gll_point_steps": work,
+            "chunk_steps": srv.chunk,
             "served": a, "served_batched": b, "sequential_resident_meshes": c,
             "solves_per_hour_ratio": a["solves_per_hour"] / c["solves_per_hour"],
             "batched_solves_per_hour_ratio": b["solves_per_hour"] / c["solves_per_hour"],
