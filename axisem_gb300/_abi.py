@@ -200,6 +200,7 @@ SIGNATURES = {
     "axg_get_info": (C.c_int, [C.c_void_p, C.POINTER(Info)]),
     "axg_get_solid_colouring": (C.c_int, [C.c_void_p, _ip, _ip, C.c_int64]),
     "axg_plan_check": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.POINTER(Info)]),
+    "axg_plan_check_ctas": (C.c_int, [C.POINTER(MeshDesc), C.c_int32, C.c_int32, C.c_int32, C.POINTER(Info)]),
     "axg_time_stiffness": (C.c_int, [C.c_void_p, C.c_int32, _fp]),
     "axg_device_check_report": (C.c_int, [_ip]),
     "axg_selftest_wait_timeout": (C.c_int, [_ip, C.POINTER(C.c_double)]),

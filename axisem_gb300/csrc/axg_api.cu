@@ -1261,11 +1261,27 @@ int symplectic_coefficients(int scheme, std::vector<double> &cd, std::vector<dou
   return (int)cv.size();
 }
 
-// tuned (or requested) patch shape, then the plan
+// resident CTAs of the solid patch kernels on the current device (two per
+// SM), which the patch tuner spreads a colour's patches over; 0 without a
+// device
+int solid_plan_ctas() {
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();  // (no device: the error is not the caller's)
+    return 0;
+  }
+  return 2 * nsm;
+}
+
+// tuned (or requested) patch shape, then the plan; ctas: as solid_plan_ctas
+// (0: the tuner assumes full launches); anel: the attenuated solid kernel
 std::string plan_domain(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
-                        const std::vector<uint8_t> &prepass, DomainPlan &plan, bool renumber = true) {
+                        const std::vector<uint8_t> &prepass, DomainPlan &plan, bool renumber = true,
+                        int ctas = 0, bool anel = false) {
   int pe = patch_elems, gr = growth;
-  std::string e = tune_plan(igloc, nel, nglob, patch_elems, growth, &pe, &gr);
+  std::string e = tune_plan(igloc, nel, nglob, patch_elems, growth, &pe, &gr, ctas,
+                            anel ? kPatchOverheadAnelastic : kPatchOverheadElastic);
   if (!e.empty()) return e;
   return build_plan(igloc, nel, nglob, pe, gr, prepass, plan, renumber);
 }
@@ -1512,7 +1528,8 @@ int create_impl(axg_handle *h, const axg_mesh_desc *d, const axg_handle *share =
       h->pre_f.assign(h->nglob_f, 0);
       for (int32_t g : cf.pt_gidx) h->pre_f[g] = 1;
     }
-    std::string perr = plan_domain(h->igloc_s.data(), h->nel_s, h->nglob_s, h->patch_elems, h->growth, h->pre_s, h->ps);
+    std::string perr = plan_domain(h->igloc_s.data(), h->nel_s, h->nglob_s, h->patch_elems, h->growth, h->pre_s, h->ps,
+                                   true, solid_plan_ctas(), h->anel);
     if (!perr.empty()) return fail(h, AXG_ERR_BAD_DESC, "solid plan: " + perr);
     if (h->nel_f > 0) {
       perr = plan_domain(h->igloc_f.data(), h->nel_f, h->nglob_f, h->patch_elems, h->growth, h->pre_f, h->pf);
@@ -1767,7 +1784,7 @@ extern "C" int axg_stiffness_assembled_noalloc(const axg_mesh_desc *d, const flo
   const int pole = d->src_type;
   const int64_t nel = d->nel_solid, nglob = d->nglob_solid;
   DomainPlan pl;
-  std::string perr = plan_domain(d->igloc_solid, nel, nglob, 0, -1, std::vector<uint8_t>(), pl, false);
+  std::string perr = plan_domain(d->igloc_solid, nel, nglob, 0, -1, std::vector<uint8_t>(), pl, false, solid_plan_ctas());
   if (!perr.empty()) return fail(nullptr, AXG_ERR_BAD_DESC, "solid plan: " + perr);
   const std::vector<int> slots = solid_slots(pole), aslots = axial_slots(pole);
   const int nt = (int)slots.size(), na = (int)aslots.size();
@@ -2680,7 +2697,12 @@ int axg_get_solid_colouring(axg_handle *h, int32_t *patch_of_elem, int32_t *colo
 }
 
 int axg_plan_check(const axg_mesh_desc *d, int32_t patch_elems, int32_t growth, axg_info *info) {
+  return axg_plan_check_ctas(d, patch_elems, growth, 0, info);
+}
+
+int axg_plan_check_ctas(const axg_mesh_desc *d, int32_t patch_elems, int32_t growth, int32_t ctas, axg_info *info) {
   if (!info) return fail(nullptr, AXG_ERR_BAD_ARG, "info is NULL");
+  if (ctas < 0) return fail(nullptr, AXG_ERR_BAD_ARG, "ctas < 0");
   int rc = validate(d);
   if (rc) return rc;
   if ((rc = check_igloc(d->igloc_solid, 25 * (int64_t)d->nel_solid, d->nglob_solid, "igloc_solid"))) return rc;
@@ -2693,7 +2715,8 @@ int axg_plan_check(const axg_mesh_desc *d, int32_t patch_elems, int32_t growth, 
   DomainPlan ps, pf;
   if (patch_elems < 0 || patch_elems > kMaxPatchElems) return fail(nullptr, AXG_ERR_BAD_ARG, "patch_elems out of range");
   if (growth < -1 || growth > kGrowLayered) return fail(nullptr, AXG_ERR_BAD_ARG, "growth must be -1, 0 or 1");
-  std::string e = plan_domain(d->igloc_solid, d->nel_solid, d->nglob_solid, patch_elems, growth, pre_s, ps);
+  std::string e = plan_domain(d->igloc_solid, d->nel_solid, d->nglob_solid, patch_elems, growth, pre_s, ps, true, ctas,
+                              d->anel_true != 0 && d->att_coarse_grained != 0);
   if (e.empty()) e = validate_plan(d->igloc_solid, d->nel_solid, d->nglob_solid, pre_s, ps);
   if (!e.empty()) return fail(nullptr, AXG_ERR_BAD_DESC, "solid plan: " + e);
   if (d->nel_fluid > 0) {

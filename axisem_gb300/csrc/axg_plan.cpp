@@ -539,14 +539,32 @@ int64_t plan_cost(const DomainPlan &plan) {
   return c;
 }
 
+int64_t plan_latency(const DomainPlan &plan, int ctas, int overhead) {
+  int64_t t = 0;
+  for (int c = 0; c < plan.n_colours; ++c) {
+    const int32_t b = plan.colour_start[c], n = plan.colour_start[c + 1] - b;
+    int64_t worst = 0;
+    for (int32_t k = 0; k < ctas && k < n; ++k) {
+      int64_t s = 0;
+      for (int32_t q = k; q < n; q += ctas) s += plan.meta[b + q].n_elems + overhead;
+      worst = std::max(worst, s);
+    }
+    t += worst;
+  }
+  return t;
+}
+
 std::string tune_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
-                      int *best_pe, int *best_growth) {
+                      int *best_pe, int *best_growth, int ctas, int overhead) {
   *best_pe = patch_elems > 0 ? patch_elems : kMaxPatchElems;
   *best_growth = growth >= 0 ? growth : kGrowLayered;
   if (patch_elems > 0 && growth >= 0) return "";
-  // candidates are compared on a prefix of the mesh (element order), its
-  // points renumbered compactly
-  const int64_t n = std::min<int64_t>(nel, kTunePrefix);
+  // a mesh of few rounds per colour: the latency model on the whole mesh
+  const bool few_rounds =
+      ctas > 0 && nel < (int64_t)kTuneFullRounds * kMaxPatchElems * 4 * (int64_t)ctas;
+  // candidates are compared on the mesh, or a prefix of it (element order),
+  // its points renumbered compactly
+  const int64_t n = few_rounds ? nel : std::min<int64_t>(nel, kTunePrefix);
   if (n == 0) return "";
   std::vector<int32_t> ig(igloc, igloc + 25 * n);
   std::vector<int32_t> ids(ig);
@@ -556,6 +574,7 @@ std::string tune_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patc
   (void)nglob;
   std::vector<int> sizes;
   if (patch_elems > 0) sizes.push_back(patch_elems);
+  else if (few_rounds) sizes = {8, 16, 24, 32, 40, 48, 56, 64};
   else sizes = {32, 40, 48, 56, 64};
   std::vector<int> growths;
   if (growth >= 0) growths.push_back(growth);
@@ -569,7 +588,7 @@ std::string tune_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patc
     DomainPlan pl;
     if (build_plan(ig.data(), n, (int64_t)ids.size(), cand[i].first, cand[i].second, std::vector<uint8_t>(), pl,
                    false).empty())
-      cost[i] = (double)plan_cost(pl);
+      cost[i] = few_rounds ? (double)plan_latency(pl, ctas, overhead) : (double)plan_cost(pl);
   };
   std::vector<std::thread> threads;
   if (cand.size() > 1 && std::thread::hardware_concurrency() > 1) {

@@ -86,10 +86,26 @@ std::string build_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int pat
 // Model cost of a plan in 1/256 warp iterations of the patch kernels.
 int64_t plan_cost(const DomainPlan &plan);
 
-// Patch-size tuner: picks (patch_elems, growth) of least plan_cost on the
-// first kTunePrefix elements.  patch_elems > 0 or growth >= 0 fix that choice.
+// Model time of a plan's colour launches when they do not fill the GPU:
+// per colour, the largest sum over one CTA's patches (patch i of a colour
+// goes to CTA i mod ctas) of (elements + overhead), summed over the colours,
+// in element iterations.  overhead: a patch's fixed cost (gather, write-back,
+// barriers) in element iterations, about 40 for the elastic kernels and 20
+// for the attenuated one, whose elements cost twice as much (fitted to step
+// times of the PREM meshes at 50, 25 and 10 s over patch sizes 8 to 64).
+constexpr int kPatchOverheadElastic = 40, kPatchOverheadAnelastic = 20;
+int64_t plan_latency(const DomainPlan &plan, int ctas, int overhead);
+
+// Patch-size tuner: picks (patch_elems, growth).  With ctas = 0, or a mesh
+// of at least kTuneFullRounds rounds of 64-element patches per colour over
+// `ctas` resident CTAs, by least plan_cost on the first kTunePrefix
+// elements: the launches are full and bandwidth-bound.  Below that, by least
+// plan_latency of the whole mesh over sizes down to 8 elements: a colour is
+// about one round of patches, and smaller patches spread it over more CTAs.
+// patch_elems > 0 or growth >= 0 fix that choice.
+constexpr int kTuneFullRounds = 2;
 std::string tune_plan(const int32_t *igloc, int64_t nel, int64_t nglob, int patch_elems, int growth,
-                      int *best_pe, int *best_growth);
+                      int *best_pe, int *best_growth, int ctas = 0, int overhead = kPatchOverheadElastic);
 
 // Checks the invariants the kernels rely on (used by the tests and by
 // axg_create in debug builds): every element in exactly one patch, no two

@@ -42,7 +42,7 @@ import numpy as np
 
 from . import _abi, sphere
 from .mesh import Mesh
-from .solver import Batch, Solver
+from .solver import Batch, Solver, plan_shape
 
 PERIODS = (50, 25, 10)
 POLES = (_abi.MONOPOLE, _abi.DIPOLE, _abi.QUADPOLE)
@@ -156,14 +156,22 @@ class Server:
     """The serving loop; `budget_bytes` bounds the HBM the solves and
     resident meshes may hold."""
 
-    def __init__(self, budget_bytes: float = 64e9, chunk: int = 1024, lib=None, compensated: bool = True):
+    def __init__(self, budget_bytes: float = 64e9, chunk: int = 1024, lib=None, compensated: bool = True,
+                 tuning: str = "shared"):
         """chunk: steps queued per call for a solve (0: all of them at once).
         A whole long solve is tens of thousands of kernel launches: queueing
         it fills the launch queue, and the call blocks the host loop until
         most of it has run, so the solves behind it start late.  In chunks
         every admitted solve is queued at once and refilled as it drains;
         in the batched loop, the most steps a batch runs before solves may
-        join it (0: until its first solve finishes)."""
+        join it (0: until its first solve finishes).  tuning: the patch
+        shape of the resident meshes, "shared" (planned for launches the mesh
+        fills, as concurrent solves fill the GPU together) or "alone" (as
+        axg_create tunes for one solve on the device: smaller patches on the
+        small meshes, faster alone, slower shared)."""
+        if tuning not in ("shared", "alone"):
+            raise ValueError("tuning is 'shared' or 'alone'")
+        self.tuning = tuning
         self.lib = lib or _abi.load_library()
         self.budget = budget_bytes
         self.chunk = chunk
@@ -184,7 +192,9 @@ class Server:
 
     def _holder(self, req: Request) -> Solver:
         if req.key not in self.meshes:
-            s = Solver(request_mesh(req, niter=1), lib=self.lib)
+            m = request_mesh(req, niter=1)
+            pe, gr = plan_shape(m, 0, self.lib) if self.tuning == "shared" else (0, -1)
+            s = Solver(m, lib=self.lib, patch_elems=pe, growth=gr)
             own, mesh = _solve_bytes(s)
             self.meshes[req.key] = s
             self.mesh_bytes[req.key] = own + mesh

@@ -47,6 +47,18 @@ def symplectic_coefficients(scheme: int, deltat: float, lib=None):
     return np.array(a[: n + 1]), np.array(b[:n]), np.array(c[:n])
 
 
+def plan_shape(mesh: Mesh, ctas: int = 0, lib=None) -> tuple[int, int]:
+    """The patch shape (patch_elems, growth) the planner picks for `mesh` on
+    a device with `ctas` resident CTAs of the solid kernel
+    (axg_plan_check_ctas, host only).  ctas = 0: the choice for launches the
+    mesh fills, as when concurrent solves share the GPU; axg_create tunes for
+    the device's own CTAs, which favours smaller patches on small meshes."""
+    lib = lib or _abi.load_library()
+    inf = _abi.Info()
+    _check(lib, None, lib.axg_plan_check_ctas(C.byref(mesh.desc()), 0, -1, ctas, C.byref(inf)))
+    return inf.patch_elems_solid, inf.growth_solid
+
+
 class Solver:
     """One solve on one GPU (one axg_handle)."""
 

@@ -411,6 +411,13 @@ int axg_get_solid_colouring(axg_handle *h, int32_t *patch_of_elem, int32_t *colo
  * and one last writer per point.  `info` receives the plan sizes
  * (device_bytes = 0).  Returns AXG_ERR_BAD_DESC with the violated invariant. */
 int axg_plan_check(const axg_mesh_desc *desc, int32_t patch_elems, int32_t growth, axg_info *info);
+/* The same, tuned as axg_create tunes on a device with `ctas` resident CTAs
+ * of the solid kernel (two per SM): a mesh of fewer than two rounds of
+ * 64-element patches per colour gets the patch size (8 to 64 elements) of
+ * least modelled colour latency.  ctas = 0 (axg_plan_check) assumes launches
+ * the mesh fills. */
+int axg_plan_check_ctas(const axg_mesh_desc *desc, int32_t patch_elems, int32_t growth, int32_t ctas,
+                        axg_info *info);
 
 /* Kernel wavefield dumps (dump_wavefields / dump_type of inparam_advanced;
  * dump_stuff, SOLVER/time_evol_wave.F90:1201-1249).  After every step with

@@ -169,3 +169,25 @@ def test_plan_coupled(lib):
     rc = lib.axg_plan_check(C.byref(m.desc()), 64, -1, C.byref(inf))
     assert rc == 0, lib.axg_last_error(None)
     assert inf.n_patches_fluid > 0
+
+
+def test_tuner_spreads_small_meshes_over_the_gpu(lib):
+    """A mesh of less than two rounds of 64-element patches per colour over
+    the device's resident CTAs gets smaller patches (the colour latency
+    model); a larger one keeps the full-launch choice.  The PREM 50 s mesh has
+    5664 solid elements: about 20 patches of 64 per colour for 304 CTAs."""
+    from axisem_gb300 import sphere
+    m = sphere.build_mesh(50.0, sphere.SphereSolve(pole=0, seconds=100.0), skeleton=sphere.build_skeleton(50.0))
+    inf = _abi.Info()
+    assert lib.axg_plan_check_ctas(C.byref(m.desc()), 0, -1, 0, C.byref(inf)) == 0
+    assert inf.patch_elems_solid == 64
+    assert lib.axg_plan_check_ctas(C.byref(m.desc()), 0, -1, 304, C.byref(inf)) == 0
+    assert inf.patch_elems_solid <= 16
+    assert inf.n_patches_solid >= 4 * 94
+    # an explicit shape is kept
+    assert lib.axg_plan_check_ctas(C.byref(m.desc()), 64, 1, 304, C.byref(inf)) == 0
+    assert inf.patch_elems_solid == 64
+    big = structured_mesh(400, 400, 2, axial="none")
+    assert lib.axg_plan_check_ctas(C.byref(big.desc()), 0, -1, 304, C.byref(inf)) == 0
+    assert (inf.patch_elems_solid, inf.growth_solid) == (64, 1)
+    assert lib.axg_plan_check_ctas(C.byref(m.desc()), 0, -1, -1, C.byref(inf)) == _abi.AXG_ERR_BAD_ARG

@@ -75,6 +75,7 @@ def _serve(monkeypatch, reqs, **kw):
     from axisem_gb300 import serve
     monkeypatch.setattr(serve, "Solver", _FakeSolver)
     monkeypatch.setattr(serve, "Batch", _FakeBatch)
+    monkeypatch.setattr(serve, "plan_shape", lambda mesh, ctas, lib: (64, 1))
     _FakeBatch.log = []
     srv = serve.Server(lib=object(), **kw)
     stats = srv.run(reqs, batched=True)
@@ -109,6 +110,7 @@ def test_served_solves_are_compensated_by_default(monkeypatch):
     made = []
     monkeypatch.setattr(serve, "Solver", lambda *a, **k: made.append(_FakeSolver(*a, **k)) or made[-1])
     monkeypatch.setattr(serve, "Batch", _FakeBatch)
+    monkeypatch.setattr(serve, "plan_shape", lambda mesh, ctas, lib: (64, 1))
     serve.Server(lib=object()).run([Request(0, 0.0, 50, 1, 10.0, 20, 1800.0, 0.05)], batched=True)
     assert made and all(s.comp for s in made if s.shared)
 
@@ -126,6 +128,7 @@ def test_concurrent_loop_steps_every_solve_once(monkeypatch):
             return True
 
     monkeypatch.setattr(serve, "Solver", S)
+    monkeypatch.setattr(serve, "plan_shape", lambda mesh, ctas, lib: (64, 1))
     reqs = [Request(k, 0.0003 * k, 25 if k % 2 else 50, k % 3, 50.0 * k, 30, 2000.0, 0.05) for k in range(6)]
     for seq in (False, True):
         srv = serve.Server(lib=object(), chunk=48)
@@ -133,3 +136,21 @@ def test_concurrent_loop_steps_every_solve_once(monkeypatch):
         for r in reqs:
             assert np.array_equal(stats.results[r.rid].seismograms, np.arange(1, r.niter + 1, dtype=np.float32))
         assert (stats.max_concurrent == 1) == seq
+
+
+def test_resident_meshes_take_the_shared_patch_shape(monkeypatch):
+    """The server plans its resident meshes for launches the mesh fills
+    (concurrent solves fill the GPU together); with tuning="alone" they take
+    axg_create's own tuning."""
+    from axisem_gb300 import serve
+    from axisem_gb300.serve import Request
+    made, asked = [], []
+    monkeypatch.setattr(serve, "Solver", lambda *a, **k: made.append((k.get("patch_elems"), k.get("growth"))) or
+                        _FakeSolver(*a, **k))
+    monkeypatch.setattr(serve, "plan_shape", lambda mesh, ctas, lib: asked.append(ctas) or (56, 0))
+    req = Request(0, 0.0, 50, 1, 10.0, 20, 1800.0, 0.05)
+    serve.Server(lib=object())._holder(req)
+    assert made == [(56, 0)] and asked == [0]
+    made.clear()
+    serve.Server(lib=object(), tuning="alone")._holder(req)
+    assert made == [(0, -1)] and asked == [0]
