@@ -337,9 +337,13 @@ class Server:
         return stats
 
 
-def solve_alone(req: Request, lib=None, compensated: bool = True) -> np.ndarray:
-    """The request's seismograms from a solve on its own, built from scratch."""
-    with Solver(request_mesh(req), lib=lib) as s:
+def solve_alone(req: Request, lib=None, compensated: bool = True, tuning: str = "shared") -> np.ndarray:
+    """The request's seismograms from a solve on its own, built from scratch
+    with the patch shape a Server of that `tuning` gives its mesh (the same
+    shape sums every point's contributions in the same order)."""
+    m = request_mesh(req)
+    pe, gr = plan_shape(m, 0, lib) if tuning == "shared" else (0, -1)
+    with Solver(m, lib=lib, patch_elems=pe, growth=gr) as s:
         s.set_compensated(compensated)
         s.run()
         return s.receivers().copy()

@@ -76,13 +76,14 @@ def test_async_runs_overlap_and_match(gpu_lib):
             s.close()
 
 
+@pytest.mark.parametrize("tuning", ["shared", "alone"])
 @pytest.mark.parametrize("batched", [False, True])
-def test_served_results_equal_alone(gpu_lib, batched):
+def test_served_results_equal_alone(gpu_lib, batched, tuning):
     reqs = [Request(k, 0.002 * k, period, pole, depth, nrec, dur, 0.03)
             for k, (period, pole, depth, nrec, dur) in enumerate(
                 [(50, 0, 100, 20, 1800), (25, 2, 400, 60, 2400), (50, 1, 650, 30, 3600),
                  (50, 2, 10, 25, 2000), (25, 0, 300, 40, 1800), (50, 0, 500, 20, 2600)])]
-    srv = Server(budget_bytes=8e9, chunk=32)
+    srv = Server(budget_bytes=8e9, chunk=32, tuning=tuning)
     try:
         stats = srv.run(reqs, batched=batched)
     finally:
@@ -90,7 +91,7 @@ def test_served_results_equal_alone(gpu_lib, batched):
     assert len(stats.results) == len(reqs)
     assert stats.max_concurrent > 1
     for r in reqs:
-        assert np.array_equal(stats.results[r.rid].seismograms, solve_alone(r)), r
+        assert np.array_equal(stats.results[r.rid].seismograms, solve_alone(r, tuning=tuning)), r
 
 
 @pytest.mark.parametrize("batched", [False, True])
