@@ -552,6 +552,16 @@ __device__ __forceinline__ float stiff_fluid(const LaneCoef &c, const float (&mt
 
 // ------------------------------------------------------------ attenuation (cg4)
 
+// Lanes 0..23: memory-variable entry (component lane / 4, cg point lane % 4)
+// of the state R summed over the n_sls solids (the sum the anelastic
+// stiffness takes); other lanes 0.
+__device__ __forceinline__ float memvar_sum(const float *R, int nsls, int lane) {
+  float rs = 0.f;
+  if (lane < 24)
+    for (int q = 0; q < nsls; ++q) rs = rs + R[q * 24 + lane];
+  return rs;
+}
+
 // Anelastic stiffness (glob_anel_stiffness_{mono,di,quad}_cg4,
 // SOLVER/stiffness_mono.f90:511, SOLVER/stiffness_di.f90:727,
 // SOLVER/stiffness_quad.f90:672) for lane (i, j): subtracts the divergence of
@@ -560,16 +570,12 @@ __device__ __forceinline__ float stiff_fluid(const LaneCoef &c, const float (&mt
 // SOLVER/unrolled_loops.f90 become two shuffles each: X1(i,j) for j in {1,3}
 // takes S1 at (1,j), (3,j); X2(i,j) for i in {1,3} takes S2 at (i,1), (i,3).
 template <int POLE, bool AX>
-__device__ __forceinline__ void anel_stiffness(const LaneCoef &c, const float *cs, const float *R, int nsls,
-                                               bool cg, int k, int i, int j, bool active, int lane, float &f0,
-                                               float &f1, float &f2) {
+__device__ __forceinline__ void anel_stiffness(const LaneCoef &c, const float *cs, float rs, bool cg, int k, int i,
+                                               int j, bool active, int lane, float &f0, float &f1, float &f2) {
   float S1a = 0.f, S2a = 0.f, S1b = 0.f, S2b = 0.f, S1z = 0.f, S2z = 0.f;
   float ya = 0.f, yb = 0.f, yz = 0.f;
-  // lanes 0..23 sum entry (component lane / 4, cg point lane % 4) over the
-  // SLS; cg lane k then collects its six components
-  float rs = 0.f;
-  if (lane < 24)
-    for (int q = 0; q < nsls; ++q) rs = rs + R[q * 24 + lane];
+  // rs: lanes 0..23 hold entry (component lane / 4, cg point lane % 4)
+  // summed over the SLS (memvar_sum); cg lane k collects its six components
   float r[6];
 #pragma unroll
   for (int v = 0; v < 6; ++v) r[v] = __shfl_sync(kFull, rs, (v * 4 + k) & 31);
@@ -639,9 +645,9 @@ __device__ __forceinline__ void anel_stiffness(const LaneCoef &c, const float *c
 // every lane of the warp updates memory variables R(k,v,j) (entry
 // 24j + 4v + k) in place, and the sources become the previous step's.
 template <int POLE>
-__device__ __forceinline__ void anel_memvar_step(const float *cs, float *R, float *scr, const AnelArgs &an, bool cg,
-                                                 int k, int lane, const float (&u)[3], const float (&gx)[3],
-                                                 const float (&ge)[3]) {
+__device__ __forceinline__ float anel_memvar_step(const float *cs, float *R, float *scr, const AnelArgs &an, bool cg,
+                                                  int k, int lane, const float (&u)[3], const float (&gx)[3],
+                                                  const float (&ge)[3]) {
   const int nsls = an.nsls;
   float *trm1 = R + 24 * nsls, *dm1 = trm1 + 4;
   if (cg) {
@@ -688,17 +694,29 @@ __device__ __forceinline__ void anel_memvar_step(const float *cs, float *R, floa
   if (!AXG_BOUND(qmu, an.n_q, 4)) qmu = 0;
   if (!AXG_BOUND(qka, an.n_q, 4)) qka = 0;
   const float *tmu = an.qtab + qmu * 2 * kMaxSls, *tka = an.qtab + qka * 2 * kMaxSls;
-  for (int e = lane; e < 24 * nsls; e += 32) {
-    const int q = e / 24, vk = e - 24 * q, v = vk >> 2, kk = vk & 3;
-    if (POLE == POLE_MONO && (v == 3 || v == 5)) continue;  // never written for the monopole
-    const float db = __ldg(tmu + q) * scr[vk] + __ldg(tmu + kMaxSls + q) * dm1[vk];
-    float nv = an.ex[q] * R[e] + db;
-    if (v < 3) nv = nv + (__ldg(tka + q) * scr[24 + kk] + __ldg(tka + kMaxSls + q) * trm1[kk]);
-    R[e] = nv;
+  // lane = entry (component v, cg point kk) of every solid q; the sum of
+  // the entries before the update is returned for the anelastic stiffness
+  float rs = 0.f;
+  if (lane < 24) {
+    const int vk = lane, v = vk >> 2, kk = vk & 3;
+    const bool upd = !(POLE == POLE_MONO && (v == 3 || v == 5));  // never written for the monopole
+    const float sv = scr[vk], dv = dm1[vk], sk = scr[24 + kk], tk = trm1[kk];
+    for (int q = 0; q < nsls; ++q) {
+      const int e = q * 24 + vk;
+      const float old = R[e];
+      rs = rs + old;
+      if (upd) {
+        const float db = __ldg(tmu + q) * sv + __ldg(tmu + kMaxSls + q) * dv;
+        float nv = an.ex[q] * old + db;
+        if (v < 3) nv = nv + (__ldg(tka + q) * sk + __ldg(tka + kMaxSls + q) * tk);
+        R[e] = nv;
+      }
+    }
   }
   __syncwarp();
   if (lane < 4) trm1[lane] = scr[24 + lane];
   else if (lane < 28) dm1[lane - 4] = scr[lane - 4];
+  return rs;
 }
 
 // ------------------------------------------------------------ solid patch kernel
@@ -1097,8 +1115,18 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
         }
         float *ablk = my_aring + slot * AS;  // attenuation constants, then state
         if (ANEL) {
-          if (ax) anel_stiffness<POLE, true>(coef, ablk, ablk + kAnelConst, an->nsls, cg, kcg, i, j, active, lane, f0, f1, f2);
-          else anel_stiffness<POLE, false>(coef, ablk, ablk + kAnelConst, an->nsls, cg, kcg, i, j, active, lane, f0, f1, f2);
+          // A Newmark step updates the memory variables here, from the
+          // predicted, masked displacement (time_step_memvars after
+          // pdistsum_solid in SOLVER/time_evol_wave.F90), and the anelastic
+          // stiffness takes their sum from before the update, as the
+          // reference's acc1 does.  (A symplectic stage only reads them:
+          // anel_memvar_kernel updates them once per step.)
+          const float rs =
+              MODE == MODE_NEWMARK
+                  ? anel_memvar_step<POLE>(ablk, ablk + kAnelConst, scr + warp * 32, *an, cg, kcg, lane, u, gx, ge)
+                  : memvar_sum(ablk + kAnelConst, an->nsls, lane);
+          if (ax) anel_stiffness<POLE, true>(coef, ablk, rs, cg, kcg, i, j, active, lane, f0, f1, f2);
+          else anel_stiffness<POLE, false>(coef, ablk, rs, cg, kcg, i, j, active, lane, f0, f1, f2);
         }
         if (MODE == MODE_NEWMARK && !ANEL && d.fx && active) {
           // attenuation at every GLL point: minus the anelastic stiffness
@@ -1129,12 +1157,7 @@ __device__ __forceinline__ void solid_patch_body(const P &p, const SpecDev &sp) 
           }
         }
         if (ANEL && MODE == MODE_NEWMARK) {
-          // memory variables of this step from the predicted, masked
-          // displacement (time_step_memvars after pdistsum_solid in
-          // SOLVER/time_evol_wave.F90), then the element's state back to HBM.
-          // (A symplectic stage only reads them: anel_memvar_kernel updates
-          // them once per step.)
-          anel_memvar_step<POLE>(ablk, ablk + kAnelConst, scr + warp * 32, *an, cg, kcg, lane, u, gx, ge);
+          // the element's updated state back to HBM
           __syncwarp();
           const float4 *src4 = reinterpret_cast<const float4 *>(ablk + kAnelConst);
           float4 *dst4 = reinterpret_cast<float4 *>(an->state + el * an->state_stride);
