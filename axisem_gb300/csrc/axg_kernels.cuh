@@ -526,30 +526,6 @@ __device__ __forceinline__ void stiff_quad(const LaneCoef &c, const float *blk, 
   f3 = lz;
 }
 
-// glob_fluid_stiffness_4 (SOLVER/stiffness_fluid.f90:139-216)
-// mt: the lane's M1chi, M2chi, M4chi (and M_w_fl) values
-template <bool AX, bool NONMONO>
-__device__ __forceinline__ float stiff_fluid(const LaneCoef &c, const float (&mt)[4], const float *m0, int i,
-                                             int j, float chi) {
-  const int j5 = 5 * j;
-  float X1 = dxi(chi, cxi<AX>(c), j5);
-  float X2 = deta(chi, c.eta, i);
-  const float m1 = mt[0], m2 = mt[1], m4 = mt[2];
-  const float S1 = m1 * X2 + m2 * X1;
-  const float S2 = m1 * X1 + m4 * X2;
-  X1 = dxi(S1, csxi<AX>(c), j5);
-  X2 = deta(S2, c.seta, i);
-  float loc = X1 + X2;
-  if (NONMONO) {
-    loc = loc + mt[3] * chi;
-    if (AX) {
-      const float V1 = dxi(chi, c.g0, j5);
-      loc = loc + c.g0i * (m0[j] * V1);
-    }
-  }
-  return loc;
-}
-
 // ------------------------------------------------------------ attenuation (cg4)
 
 // Lanes 0..23: memory-variable entry (component lane / 4, cg point lane % 4)
@@ -1672,10 +1648,11 @@ __device__ __forceinline__ float fluid_predicted(const StateArgs &st, int64_t g,
 // glob_fluid_stiffness_4 (SOLVER/stiffness_fluid.f90:139-216) of one element
 // held by one thread: chi(i, j) at chi[i + 5 j] in, the element's
 // contributions out.  met points at the element's first metric value (value
-// v at met[v * kFlChunk]).  The same products and summation order as the
-// warp-per-element form (dxi / deta above): first stage X1 = mxm_4(G2T or
-// G1T, chi), X2 = mxm_4(chi, G2); second stage mxm_4(G2 or G1, S1) +
-// mxm_4(S2, G2T).
+// v at met[v * kFlChunk]).  The products and summation order of the shuffle
+// contractions dxi / deta: first stage X1 = mxm_4(G2T or G1T, chi),
+// X2 = mxm_4(chi, G2); S1 = M1chi X2 + M2chi X1, S2 = M1chi X1 + M4chi X2;
+// second stage mxm_4(G2 or G1, S1) + mxm_4(S2, G2T); for the non-monopole
+// sources + M_w_fl chi and, on the axis, G0(i) M0_w_fl(j) mxm_4(G0, chi).
 template <bool AX, bool NONMONO>
 __device__ __forceinline__ void fluid_elem_stiffness(const SpecDev &sp, const float *met, const float *m0,
                                                      const float (&chi)[25], float (&loc)[25]) {
