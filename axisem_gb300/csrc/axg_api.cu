@@ -895,7 +895,9 @@ FluidArgs fluid_args(axg_handle *h) {
 }
 
 // CTAs of the fluid's element pass: one thread per element
-unsigned fluid_elem_grid(int64_t nel) { return (unsigned)std::max<int64_t>(1, (nel + kThreads - 1) / kThreads); }
+unsigned fluid_elem_grid(int64_t nel) {
+  return (unsigned)std::max<int64_t>(1, (nel + kFlElemThreads - 1) / kFlElemThreads);
+}
 
 // The fluid of a Newmark step or a symplectic stage: the element pass, then
 // the point pass.
@@ -903,7 +905,7 @@ template <int NONMONO, int MODE, bool KAHAN>
 void launch_fluid_t(axg_handle *h, cudaStream_t s, const StateArgs &fs) {
   FluidArgs fa = fluid_args(h);
   if (MODE == MODE_SYMPLECTIC) fa.fsmask = nullptr;  // symplectic_time_loop applies no free-surface mask
-  launch_pdl(fluid_elem_kernel<NONMONO, MODE, KAHAN, One<FluidWork>>, fluid_elem_grid(h->nel_f), kThreads, 0, s,
+  launch_pdl(fluid_elem_kernel<NONMONO, MODE, KAHAN, One<FluidWork>>, fluid_elem_grid(h->nel_f), kFlElemThreads, 0, s,
              One<FluidWork>{{fa, fs}, (int32_t)h->nel_f}, h->spec);
   launch_pdl(fluid_point_kernel<NONMONO, MODE, KAHAN, One<FluidWork>>, (unsigned)((h->nglob_f + 255) / 256), 256, 0,
              s, One<FluidWork>{{fa, fs}, (int32_t)h->nglob_f});
@@ -3035,8 +3037,10 @@ int64_t batch_fluid(axg_batch *b, int stage, cudaStream_t s) {
       b->hs, [&](axg_handle *h) { return mine(h) ? (int32_t)h->nel_f : 0; }, work,
       [&](const Many<FluidWork> &m) {
         const unsigned g = fluid_elem_grid(m.start[m.n]);
-        if (stage < 0) fluid_elem_kernel<NONMONO, MODE_NEWMARK, KAHAN, Many<FluidWork>><<<g, kThreads, 0, s>>>(m, b->spec);
-        else fluid_elem_kernel<NONMONO, MODE_SYMPLECTIC, KAHAN, Many<FluidWork>><<<g, kThreads, 0, s>>>(m, b->spec);
+        if (stage < 0)
+          fluid_elem_kernel<NONMONO, MODE_NEWMARK, KAHAN, Many<FluidWork>><<<g, kFlElemThreads, 0, s>>>(m, b->spec);
+        else
+          fluid_elem_kernel<NONMONO, MODE_SYMPLECTIC, KAHAN, Many<FluidWork>><<<g, kFlElemThreads, 0, s>>>(m, b->spec);
       });
   const int64_t np = for_batches<FluidWork>(
       b->hs, [&](axg_handle *h) { return mine(h) ? (int32_t)h->nglob_f : 0; }, work,

@@ -1708,8 +1708,11 @@ __device__ __forceinline__ void fluid_elem_stiffness(const SpecDev &sp, const fl
 // registers, and stores its 25 contributions.  The element's 25 gathers and
 // its metric loads are independent of one another, so each thread has tens
 // of loads in flight, and there are no shuffles.
+// CTAs of 128 threads, five per SM at 96 registers (20 warps; 256-thread
+// CTAs at 128 registers held 16)
+constexpr int kFlElemThreads = 128;
 template <int NONMONO, int MODE, bool KAHAN, class P = One<FluidWork>>
-__global__ void __launch_bounds__(kThreads, 2) fluid_elem_kernel(const __grid_constant__ P p, SpecDev sp) {
+__global__ void __launch_bounds__(kFlElemThreads, 5) fluid_elem_kernel(const __grid_constant__ P p, SpecDev sp) {
   pdl_wait();
   pdl_trigger();
   const int32_t it = blockIdx.x * blockDim.x + threadIdx.x;
