@@ -416,6 +416,19 @@ def _pdistsum_f32(vals_f: np.ndarray, igloc: np.ndarray, nglob: int, dtype=F32) 
     return np.asfortranarray(out.transpose(2, 1, 0))
 
 
+def _neighbourhood(igloc: np.ndarray, nel: int, elems) -> tuple[np.ndarray, np.ndarray, int]:
+    """The elements that share a point with `elems` (sorted, so in the walk
+    order of pdistsum), and their igloc renumbered compactly (1-based) with
+    the number of points: a field nonzero only on `elems` assembles on them
+    with the same sums, in the same order, as over the whole mesh."""
+    ig_all = np.asarray(igloc).reshape(nel, 25) - 1
+    mark = np.zeros(int(ig_all.max()) + 1, dtype=bool)
+    mark[ig_all[list(elems)].reshape(-1)] = True
+    near = np.flatnonzero(mark[ig_all].any(axis=1))
+    uniq, inv = np.unique(ig_all[near], return_inverse=True)
+    return near, inv.reshape(-1).astype(I32) + 1, len(uniq)
+
+
 def _to_f(a):
     """(E, i, j) FP64 -> Fortran (i, j, E) FP32."""
     return np.asfortranarray(np.transpose(a, (1, 2, 0)).astype(F32))
@@ -961,13 +974,8 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
     # assembly (pdistsum_solid) involves only the elements that hold one of
     # them: it runs on those, in element order, with the same sums in the
     # same order as over the whole mesh.
-    ig_all = np.asarray(m.igloc_solid).reshape(E, 25) - 1
-    mark = np.zeros(m.nglob_solid, dtype=bool)
-    mark[ig_all[src_els].reshape(-1)] = True
-    near = np.flatnonzero(mark[ig_all].any(axis=1))
+    near, ig_near, n_near_pts = _neighbourhood(m.igloc_solid, E, src_els)
     slot = {int(e): k for k, e in enumerate(near)}
-    uniq, inv = np.unique(ig_all[near], return_inverse=True)
-    ig_near = inv.reshape(-1).astype(I32) + 1
     N = len(near)
     st = np.zeros((N, 5, 5, 3))          # [near element, ipol, jpol, comp] FP64
     axis_s = geo["axis"][solid]
@@ -1012,7 +1020,7 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
     # pdistsum_solid in FP32, small values cut (smallval = 1e-6), the pole's axis mask
     stf_ = np.zeros((5, 5, N, 3), dtype=F32, order="F")
     for c in range(3):
-        stf_[..., c] = _pdistsum_f32(_to_f(st[..., c]), ig_near, len(uniq))
+        stf_[..., c] = _pdistsum_f32(_to_f(st[..., c]), ig_near, n_near_pts)
     stf_[np.abs(stf_) < 1e-6] = 0.0
     ax_near = np.array([slot[int(e)] for e in m.ax_el_solid - 1 if int(e) in slot], dtype=np.int64)
     comps = {0: [0], 1: [1, 2], 2: [0, 1, 2]}[pole]
@@ -1022,7 +1030,7 @@ def _source_receivers(m: Mesh, sk: Skeleton, geo, solve: SphereSolve, period: fl
     # the same in FP64 (the entries the FP32 term keeps)
     std_ = np.zeros((5, 5, N, 3), order="F")
     for c in range(3):
-        std_[..., c] = _pdistsum_f32(np.transpose(st[..., c], (1, 2, 0)), ig_near, len(uniq), np.float64)
+        std_[..., c] = _pdistsum_f32(np.transpose(st[..., c], (1, 2, 0)), ig_near, n_near_pts, np.float64)
     std_[stf_ == 0] = 0.0
     std_ = std_ / (np.pi if pole == _abi.DIPOLE else 2.0 * np.pi)
     nzk = np.flatnonzero(np.any(stf_ != 0, axis=(0, 1, 3))).tolist()

@@ -231,6 +231,29 @@ def test_source_and_receivers(mesh50):
     assert m.stf.dtype == np.float32 and np.abs(m.stf).max() > 1e17
 
 
+def test_source_assembly_on_the_neighbourhood_equals_the_whole_mesh(mesh50):
+    """with_solve assembles the source term (pdistsum_solid of a field that
+    is nonzero on the source elements only) over the elements sharing a point
+    with them: bit-identical to the assembly over the whole mesh, in FP32 and
+    FP64, and zero everywhere else."""
+    m = mesh50[2]
+    E = m.nel_solid
+    rng = np.random.default_rng(3)
+    axial = np.asarray(m.ax_el_solid) - 1
+    for src in ([int(axial[5])], [int(axial[5]), int(axial[6])], [E // 2]):
+        near, ig_near, n_pts = sphere._neighbourhood(m.igloc_solid, E, src)
+        assert set(src) <= set(near.tolist()) and len(near) < 40
+        field = np.zeros((E, 5, 5))
+        field[src] = rng.standard_normal((len(src), 5, 5))
+        for dtype in (np.float32, np.float64):
+            full = sphere._pdistsum_f32(np.transpose(field, (1, 2, 0)), m.igloc_solid, m.nglob_solid, dtype)
+            part = sphere._pdistsum_f32(np.transpose(field[near], (1, 2, 0)), ig_near, n_pts, dtype)
+            assert np.array_equal(full[:, :, near], part)
+            rest = np.ones(E, dtype=bool)
+            rest[near] = False
+            assert not full[:, :, rest].any()
+
+
 def test_attenuation_model(sk50, orc):
     """prepare_attenuation on the PREM mesh: the SLS fit reproduces a flat
     Q over the band, the cg4 weights partition each element's mass
