@@ -22,7 +22,10 @@ receiver count and a seismogram duration.  The server
     are created while the current chunk runs.
 
 Solves run in the compensated (Kahan) FP32 mode by default, the precision of
-the serving workload.
+the serving workload.  With tens of solves' streams in flight, a process that
+serves should let the CUDA runtime use more hardware work queues than its
+default 8 (CUDA_DEVICE_MAX_CONNECTIONS=32 in the environment before CUDA
+initialises; the benchmark does so).
 
 The meshes are the whole-Earth prem_iso meshes of axisem_gb300.sphere at the
 request's period (50 s: 6.6k elements, 25 s: 22k, 10 s: 117k), each with its
