@@ -439,7 +439,8 @@ class Attenuation:
     """Options of the anelastic model (inparam_advanced's attenuation keys,
     SOLVER/attenuation.f90:710-730 defaults): n_sls standard linear solids
     over [f_min, f_max] Hz, moduli given at f_ref Hz, the low-Q correction,
-    the coarse-grained (cg4) memory variables."""
+    the coarse-grained (cg4) memory variables or, with coarse_grained False
+    (att_coarse_grained = .false.), memory variables at every GLL point."""
 
     n_sls: int = 5
     f_min: float = 0.001
@@ -447,6 +448,7 @@ class Attenuation:
     f_ref: float = 1.0
     do_corr_lowq: bool = True
     nfsamp: int = 100
+    coarse_grained: bool = True
 
 
 def sls_fit(att: Attenuation):
@@ -757,16 +759,33 @@ def build_mesh(period: float = 50.0, solve: SphereSolve | None = None, model: st
         # eta(ipol), as the reference's mapping(eta(ipol), eta(jpol)) call does
         sg = element_geometry(sk, solid, gll_only=True)["s"]
         Yf = jac[S] * mfac[S]
-        cg = lambda a: np.asfortranarray(np.stack([a[:, i, j] for (i, j) in CG4], 0).astype(F32))  # noqa: E731
         pw = m.pointwise
-        anel.update({
-            "Y_cg4": cg(Yf), "V_s_eta_cg4": cg(sg * Mseta[S]), "V_s_xi_cg4": cg(sg * Msxi[S]),
-            "V_z_eta_cg4": cg(sg * Mzeta[S]), "V_z_xi_cg4": cg(sg * Mzxi[S]),
-            "inv_s_solid": pw["inv_s_solid"],
-        })
-        for nm in ("DsDeta_over_J_sol", "DzDeta_over_J_sol", "DsDxi_over_J_sol", "DzDxi_over_J_sol"):
-            a = np.transpose(pw[nm], (2, 0, 1))
-            anel[nm + "_cg4"] = cg(a)
+        anel["inv_s_solid"] = pw["inv_s_solid"]
+        V = {"V_s_eta": sg * Mseta[S], "V_s_xi": sg * Msxi[S], "V_z_eta": sg * Mzeta[S], "V_z_xi": sg * Mzxi[S]}
+        if attenuation.coarse_grained:
+            cg = lambda a: np.asfortranarray(np.stack([a[:, i, j] for (i, j) in CG4], 0).astype(F32))  # noqa: E731
+            anel["Y_cg4"] = cg(Yf)
+            for nm, a in V.items():
+                anel[nm + "_cg4"] = cg(a)
+            for nm in ("DsDeta_over_J_sol", "DzDeta_over_J_sol", "DsDxi_over_J_sol", "DzDxi_over_J_sol"):
+                anel[nm + "_cg4"] = cg(np.transpose(pw[nm], (2, 0, 1)))
+        else:
+            # at every GLL point (mfac is zero at ipol = 0 of axial elements,
+            # so Y and V_* are, as the reference sets them); the axial
+            # elements' ipol = 0 terms Y0, V0_* (def_solid_stiffness_terms,
+            # SOLVER/def_precomp_terms.f90:1504-1526), (0:4, nel_solid)
+            axs = ax[S]
+            wa0 = SP.wt_axial_k[0] * SP.wt[None, :]
+            dsx0 = dsdxi[S][:, 0, :]
+            a0 = lambda a: np.asfortranarray(np.where(axs[:, None], a, 0.0).T.astype(F32))  # noqa: E731
+            anel["Y"] = _to_f(Yf)
+            for nm, a in V.items():
+                anel[nm] = _to_f(a)
+            anel.update({"Y0": a0(wa0 * jac[S][:, 0, :]), "V0_s_eta": a0(np.zeros_like(dsx0)),
+                         "V0_s_xi": a0(wa0 * dsx0 * dsx0), "V0_z_eta": a0(wa0 * dsx0 * dzdeta[S][:, 0, :]),
+                         "V0_z_xi": a0(wa0 * dsx0 * (-dzdxi[S][:, 0, :]))})
+            for nm in ("DsDeta_over_J_sol", "DzDeta_over_J_sol", "DsDxi_over_J_sol", "DzDxi_over_J_sol"):
+                anel[nm] = pw[nm]
         m.anel = anel
     _source_receivers(m, sk, geo, solve, period, deltat)
     return m
@@ -784,12 +803,14 @@ def _cfl(s, z, vp, courant: float) -> float:
 
 
 def _prepare_attenuation(att: Attenuation, solid, lam, mu, massmat, r, idom, model, deltat):
-    """prepare_attenuation (SOLVER/attenuation.f90:682-1137), coarse-grained:
-    per solid element Q from the model at its point (1,1), the SLS weights
+    """prepare_attenuation (SOLVER/attenuation.f90:682-1137): per solid
+    element Q from the model at its point (1,1), the SLS weights
     yp_j = y_j / Q (fast_correct'ed), the moduli at the band's central
     frequency, the delta moduli, the unrelaxed moduli (written back into
     lam and mu, which the stiffness terms then use) and the cg4-weighted
-    delta moduli; the time-stepping factors of the exact SLS integration."""
+    delta moduli (coarse-grained; :1035-1052) or the delta moduli at every
+    GLL point (:1053-1063); the time-stepping factors of the exact SLS
+    integration."""
     w_j, y_j = sls_fit(att)
     w_0 = att.f_ref * 2 * np.pi
     w_1 = np.sqrt(att.f_min * att.f_max) * 2 * np.pi
@@ -798,12 +819,18 @@ def _prepare_attenuation(att: Attenuation, solid, lam, mu, massmat, r, idom, mod
     dom = idom[S][:, 1, 1]
     Q_mu = velocity(ri, "Qmu", dom, model).astype(F32)
     Q_ka = velocity(ri, "Qka", dom, model).astype(F32)
-    wcg = _weights_cg(massmat[S])                       # (E, 4)
-    wfull = np.zeros((len(S), 5, 5))
-    for k, (i, j) in enumerate(CG4):
-        wfull[:, i, j] = wcg[:, k]
+    cgr = att.coarse_grained
+    if cgr:
+        wcg = _weights_cg(massmat[S])                   # (E, 4)
+        wfull = np.zeros((len(S), 5, 5))
+        for k, (i, j) in enumerate(CG4):
+            wfull[:, i, j] = wcg[:, k]
+    else:
+        wfull = np.ones((len(S), 5, 5))
     dmu_cg4 = np.zeros((4, len(S)))
     dka_cg4 = np.zeros((4, len(S)))
+    dmu_all = np.zeros((len(S), 5, 5))
+    dka_all = np.zeros((len(S), 5, 5))
     for e in range(len(S)):
         qm, qk = float(Q_mu[e]), float(Q_ka[e])
         ypm = fast_correct(y_j / qm) if att.do_corr_lowq else y_j / qm
@@ -817,15 +844,24 @@ def _prepare_attenuation(att: Attenuation, solid, lam, mu, massmat, r, idom, mod
         dka0 = ka_w1 / (1.0 / np.sum(ypk) + 1 - ka_fac)
         mu[ge] = mu_w1 + wfull[e] * dmu0 * mu_fac
         lam[ge] = ka_w1 + wfull[e] * dka0 * ka_fac - 2.0 / 3.0 * mu[ge]
-        for k, (i, j) in enumerate(CG4):
-            dmu_cg4[k, e] = wcg[e, k] * dmu0[i, j]
-            dka_cg4[k, e] = wcg[e, k] * dka0[i, j]
+        if cgr:
+            for k, (i, j) in enumerate(CG4):
+                dmu_cg4[k, e] = wcg[e, k] * dmu0[i, j]
+                dka_cg4[k, e] = wcg[e, k] * dka0[i, j]
+        else:
+            dmu_all[e] = dmu0
+            dka_all[e] = dka0
     ex = np.exp(-w_j * deltat)
-    return {"y_j": y_j, "w_j": w_j, "exp_w_j_deltat": ex,
-            "ts_fac_tm1": (1 - ex) / (w_j * deltat) - ex, "ts_fac_t": (ex - 1) / (w_j * deltat) + 1,
-            "do_corr_lowq": int(att.do_corr_lowq), "Q_mu": Q_mu, "Q_kappa": Q_ka,
-            "delta_mu_cg4": np.asfortranarray(dmu_cg4.astype(F32)),
-            "delta_kappa_cg4": np.asfortranarray(dka_cg4.astype(F32))}
+    out = {"y_j": y_j, "w_j": w_j, "exp_w_j_deltat": ex,
+           "ts_fac_tm1": (1 - ex) / (w_j * deltat) - ex, "ts_fac_t": (ex - 1) / (w_j * deltat) + 1,
+           "do_corr_lowq": int(att.do_corr_lowq), "Q_mu": Q_mu, "Q_kappa": Q_ka}
+    if cgr:
+        out["delta_mu_cg4"] = np.asfortranarray(dmu_cg4.astype(F32))
+        out["delta_kappa_cg4"] = np.asfortranarray(dka_cg4.astype(F32))
+    else:
+        out["delta_mu"] = _to_f(dmu_all)
+        out["delta_kappa"] = _to_f(dka_all)
+    return out
 
 
 def _boundary(m: Mesh, sk: Skeleton, geo, solid, fluid):

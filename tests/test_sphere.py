@@ -254,6 +254,31 @@ def test_source_assembly_on_the_neighbourhood_equals_the_whole_mesh(mesh50):
             assert not full[:, :, rest].any()
 
 
+def test_attenuation_at_every_point_arrays(sk50):
+    """att_coarse_grained = .false. on the PREM mesh: Y and V_* at every GLL
+    point, equal to the coarse-grained arrays at the four cg points and zero
+    at ipol = 0 of axial elements, whose terms are Y0 / V0_* (zero on the
+    other elements); per-point modulus defects."""
+    solve = sphere.SphereSolve(pole=1, source="mtr", seconds=100.0)
+    a_cg = sphere.build_mesh(50.0, solve, skeleton=sk50, attenuation=sphere.Attenuation(), pointwise=False).anel
+    m = sphere.build_mesh(50.0, solve, skeleton=sk50, attenuation=sphere.Attenuation(coarse_grained=False),
+                          pointwise=False)
+    a = m.anel
+    E = m.nel_solid
+    ax = np.asarray(m.ax_el_solid) - 1
+    other = np.setdiff1d(np.arange(E), ax)
+    for nm in ("Y", "V_s_eta", "V_s_xi", "V_z_eta", "V_z_xi", "delta_mu", "delta_kappa", "DsDeta_over_J_sol"):
+        assert a[nm].shape == (5, 5, E) and a[nm].dtype == np.float32, nm
+    for nm in ("Y", "V_s_eta", "V_s_xi", "V_z_eta", "V_z_xi"):
+        for k, (i, j) in enumerate(sphere.CG4):
+            assert np.array_equal(a[nm][i, j], a_cg[nm + "_cg4"][k]), nm
+        assert not a[nm][0, :, ax].any()
+    for nm in ("Y0", "V0_s_eta", "V0_s_xi", "V0_z_eta", "V0_z_xi"):
+        assert a[nm].shape == (5, E) and not a[nm][:, other].any()
+    assert (a["Y0"][:, ax] > 0).all() and (a["V0_s_xi"][:, ax] > 0).all() and not a["V0_s_eta"].any()
+    assert (a["delta_mu"] > 0).all() and (a["delta_kappa"] > 0).all()
+
+
 def test_attenuation_model(sk50, orc):
     """prepare_attenuation on the PREM mesh: the SLS fit reproduces a flat
     Q over the band, the cg4 weights partition each element's mass
